@@ -1,0 +1,348 @@
+"""Benchmark of the PolyMPS per-step particle path on GB300.
+
+Workload: the 3D incompressible polygon dam break (tank 1.61 x 0.6 x 0.6 m, 12-triangle
+closed box, fluid block 0.6 x 0.6 x 0.3 m at l0 = 0.005 m: 864,000 particles,
+dt = 2.5e-4 s, PPE to relative residual 1e-8), synthetic lattice input (the reference's
+.grid files are not available).  A step is one mainLoopOfSimulation iteration.
+
+Metric: particle-steps/s (whole job), plus the PPE time-to-1e-8 of the plain FP64 CG,
+the FP32/FP64 refinement solver and the learned warm start on the same systems.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Multi-GPU: the path is run as N independent replicas (one per rank, no collective on
+the data path); value = sum of particle-steps over ranks / max time over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s"
+HBM_FALLBACK = 6800.0
+
+
+def args_():
+    a = argparse.ArgumentParser()
+    a.add_argument("--gpus", type=int, default=1)
+    a.add_argument("--steps", type=int, default=20)
+    a.add_argument("--warmup", type=int, default=5)
+    a.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    a.add_argument("--solver", default="mixed", choices=["mixed", "plain"])
+    a.add_argument("--warm", default="auto", choices=["auto", "prev", "mlp"])
+    a.add_argument("--scale", type=float, default=1.0, help="l0 multiplier (1 = 864k particles)")
+    a.add_argument("--e2e-steps", type=int, default=3)
+    a.add_argument("--no-cpu-baseline", action="store_true")
+    a.add_argument("--cpu-steps", type=int, default=1)
+    a.add_argument("--ppe-compare", type=int, default=1)
+    return a.parse_args()
+
+
+def dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1])); smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# Algorithmic bytes per call of each timed class (each distinct element read or written
+# once; neighbour re-reads assumed cache resident).  N particles, E neighbour entries,
+# Z off-diagonal PPE non-zeros.
+def algo_bytes(cls, N, E, Z, mixed):
+    if cls == "PPE_SPMV":
+        return N * (16 if mixed else 28) + Z * (8 if mixed else 12)
+    if cls == "PPE_VECTOR":
+        return N * (4 * 9 if mixed else 8 * 9)
+    if cls == "NEIGHBOR_LIST":
+        return N * (32 + 16 + 16 + 4 + 4 + 4) + 4 * E
+    if cls == "PPE_ASSEMBLE":
+        return N * (32 + 32 + 8 + 4 + 4 + 8 + 8 + 4 + 8) + Z * 12 + 4 * E
+    if cls in ("PRESS_GRADIENT",):
+        return N * (32 + 32 + 8 + 8 + 3 * 32 + 4 + 32) + 4 * E
+    if cls in ("PND_NEIGH_NPCD",):
+        return N * (32 + 32 + 8 + 4 + 32 + 32 + 8 * 5 + 4) + 4 * E
+    if cls in ("CORRECTION_MATRIX",):
+        return N * (32 + 32 + 4 + 4 + 3 * 32) + 4 * E
+    if cls in ("VISCOSITY",):
+        return N * (32 + 32 + 32 + 4 + 32)
+    if cls in ("COLLISION",):
+        return N * (32 + 32 + 32 + 4 + 32) + 4 * E
+    return None
+
+
+def run_gb300(a, rank, world, local):
+    import torch
+    from polymps_gb300 import abi, build, cases, mps
+    if world > 1:
+        import torch.distributed as dist_
+        dist_.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    build.build()
+    case = cases.config(3, scale=a.scale)
+    N = case.n
+    solver = abi.SOLVER_MIXED if a.solver == "mixed" else abi.SOLVER_PLAIN_FP64
+    mlp_path = os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz")
+    use_mlp = a.warm == "mlp" or (a.warm == "auto" and os.path.exists(mlp_path))
+    g = mps.MpsGpu(case, solver=solver, tol=1e-8)
+    if use_mlp:
+        w = np.load(mlp_path)
+        g.mlp_set_weights(w["params"], w["norm"])
+        g.set_solver(solver, abi.WARM_MLP, 1e-8)
+    g.initialize()
+    g.run(a.warmup)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    g.profile(True)
+    l0 = mps.MpsGpu.launch_count()
+    t0 = time.perf_counter()
+    st = g.run(a.steps)
+    wall = time.perf_counter() - t0
+    launches = mps.MpsGpu.launch_count() - l0
+    prof = g.profile_get()
+    g.profile(False)
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    dev_s = st.stepMs / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(t.item())
+        torch.distributed.barrier()
+    value = N * a.steps * world / dev_s
+
+    # e2e through the C ABI with host arrays: upload the state from pinned host memory,
+    # step, download the result, every step
+    host = {f: g.get(f) for f in (abi.F_POS, abi.F_VEL, abi.F_PRESS, abi.F_PRESSPPE)}
+    h2d = sum(v.nbytes for v in host.values())
+    d2h = host[abi.F_POS].nbytes + host[abi.F_VEL].nbytes + host[abi.F_PRESS].nbytes
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.e2e_steps):
+        for f, v in host.items():
+            g.set(f, v)
+        g.step()
+        host[abi.F_POS] = g.get(abi.F_POS)
+        host[abi.F_VEL] = g.get(abi.F_VEL)
+        host[abi.F_PRESS] = g.get(abi.F_PRESS)
+    e2e_s = time.perf_counter() - t0
+    e2e = N * a.e2e_steps * world / e2e_s
+
+    # dominant class and its roofline
+    hbm, hbm_src = peaks()
+    E, Z = st.nbrEntries, max(st.ppeNnz - N, 0)
+    mixed = solver == abi.SOLVER_MIXED
+    leaf = {k: v for k, v in prof.items() if k not in ("CALC_PRESS",)}
+    dom = max(leaf, key=lambda k: leaf[k][0]) if leaf else None
+    roof = None
+    if dom:
+        ms, calls = leaf[dom]
+        b = algo_bytes(dom, N, E, Z, mixed)
+        if b:
+            ach = b / (ms / calls / 1e3) / 1e9
+            roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
+                    "frac": round(ach / hbm, 4), "peak_source": hbm_src, "traffic": None,
+                    "algo_bytes_per_launch": int(b), "launch_ms": round(ms / calls, 4),
+                    "share_of_step": round(ms / st.stepMs, 3)}
+
+    # PPE time-to-1e-8 on identical systems: plain FP64 vs mixed vs learned + mixed
+    ppe = None
+    if a.ppe_compare and rank == 0:
+        ppe = ppe_compare(g, abi, use_mlp)
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": "particle-steps/s", "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(st.stepMs / a.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
+        "config": {"workload": "3D incompressible polygon dam break (cfg3)", "particles": N,
+                   "l0": case.params["partDist"], "dt": case.params["timeStep"],
+                   "ppe_tol": 1e-8, "solver": a.solver, "warm_start": "mlp" if use_mlp else "previous",
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "working set > L2 (no flush needed)", "wall_s": round(wall, 3)},
+        "e2e": {"value": round(e2e, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": a.e2e_steps},
+        "roofline": roof,
+        "clocks": clk,
+        "gpu_launches": int(launches),
+        "ppe": ppe,
+        "profile_ms": {k: round(v[0], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
+        "last_step": {"ppe_iters": st.ppeIterations, "ppe_relres": st.ppeRelResidual, "velMax": st.velMax},
+    }
+    if rank == 0 and not a.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(case, a.cpu_steps)
+    g.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out
+
+
+def ppe_compare(g, abi, use_mlp):
+    """Solve the current step's PPE three ways from the same state and warm start."""
+    # advance to the system of the next step: run the ops up to the pressure solve
+    ops = ["UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT", "OUT_OF_DOMAIN", "COLLISION",
+           "WALL_DISTANCE", "WALL_NPCD", "PND_NEIGH_NPCD", "UPDATE_BC"]
+    for op in ops:
+        g.run_op(op)
+    x_prev = g.get(abi.F_PRESSPPE)
+    res = {}
+    variants = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS),
+                ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS)]
+    if use_mlp:
+        variants.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP))
+    for name, s, w in variants:
+        best = None
+        for rep in range(3):
+            g.set(abi.F_PRESSPPE, x_prev)
+            g.set_solver(s, w, 1e-8)
+            g.run_op("CALC_PRESS")
+            st = g.last_stats()
+            if best is None or st.ppeSolveMs < best["ms"]:
+                best = {"ms": round(st.ppeSolveMs, 3), "iters": st.ppeIterations, "refinements": st.ppeRefinements,
+                        "relres": st.ppeRelResidual, "relres0": st.ppeInitialRelResidual}
+        res[name] = best
+        if name == "plain_fp64":
+            p_ref = g.get(abi.F_PRESSPPE)
+        else:
+            p = g.get(abi.F_PRESSPPE)
+            res[name]["rel_err_vs_fp64"] = float(np.linalg.norm(p - p_ref) / np.linalg.norm(p_ref))
+    base = res["plain_fp64"]["ms"]
+    for k in res:
+        res[k]["speedup_vs_plain"] = round(base / res[k]["ms"], 3) if res[k]["ms"] > 0 else None
+    res["assemble_ms"] = round(g.last_stats().ppeAssembleMs, 3)
+    return res
+
+
+def cpu_baseline(case, steps):
+    """The FP64 CPU oracle (a restatement of the reference path; the reference itself
+    cannot be built here) on the host cores: a bounded sample of `steps` steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the checker / CPU baseline
+    cores = os.cpu_count() or 1
+    o = oracle.Oracle(case, threads=cores)
+    o.set_solver(1e-8)
+    o.initialize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.step()
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": round(case.n * steps / dt, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": "%d step(s) of the %d-particle workload after initialisation (%.1f s)" % (steps, case.n, dt)}
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return None
+    from polymps_gb300 import cases
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    case = cases.config(3, scale=a.scale)
+    cores = os.cpu_count() or 1
+    o = oracle.Oracle(case, threads=cores)
+    o.set_solver(1e-8)
+    o.initialize()
+    w = min(a.warmup, 1)
+    k = max(1, min(a.steps, 2))
+    for _ in range(w):
+        o.step()
+    t0 = time.perf_counter()
+    for _ in range(k):
+        o.step()
+    dt = time.perf_counter() - t0
+    v = case.n * k / dt
+    return {"metric": METRIC, "value": round(v, 1), "unit": "particle-steps/s", "n_gpus": world, "steps": k,
+            "warmup": w, "ms_per_step": round(dt / k * 1e3, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "3D incompressible polygon dam break (cfg3)", "particles": case.n,
+                       "ppe_tol": 1e-8},
+            "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": "%d timed step(s) after %d warm-up step(s)" % (k, w)},
+            "e2e": {"value": round(v, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    a = args_()
+    rank, world, local = dist()
+    if a.impl == "reference":
+        out = run_reference(a, rank, world)
+    else:
+        out = run_gb300(a, rank, world, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

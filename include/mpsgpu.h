@@ -1,0 +1,282 @@
+/*
+ * mpsgpu.h — C ABI of the GB300 (sm_103a) implementation of the PolyMPS per-step
+ * particle path (bucket cell list, PND/neighbour sums, EOS, PPE assembly + CG,
+ * viscosity Laplacian, polygon wall distance/mirror, collision, shifting).
+ *
+ * The reference (rubensamarojr/polymps) has no FFI: its boundary is the class-method
+ * stepping interface driven by mainLoopOfSimulation (src/main.cpp:221-469), where every
+ * operator is `void Class::method(MpsParticleSystem*, MpsParticle*, MpsBucket*)`
+ * (include/MpsPndNeigh.h:57, include/MpsPressure.h:49, include/MpsViscosity.h:43).
+ * Each entry point below replaces one of those calls (cited per function) or a group of
+ * them; plain pointers and sizes only, no C++ or torch types, and every call returns an
+ * int status (0 = success, see MPSGPU_ERR_*) instead of printing and continuing.
+ *
+ * Ownership: the library owns all device memory behind the opaque handle; host arrays
+ * passed in are only read (or written for downloads) during the call.  A handle is not
+ * thread-safe and runs everything on one CUDA stream (mpsgpu_stream).
+ */
+#ifndef MPSGPU_H_
+#define MPSGPU_H_
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+#define MPSGPU_OK                 0
+#define MPSGPU_ERR_ARG            1   /* bad argument / NULL pointer / size          */
+#define MPSGPU_ERR_CUDA           2   /* a CUDA runtime call failed                   */
+#define MPSGPU_ERR_NOMEM          3   /* device allocation failed                     */
+#define MPSGPU_ERR_UNSUPPORTED    4   /* configuration outside the implemented path   */
+#define MPSGPU_ERR_NOT_CONVERGED  5   /* PPE solver hit its iteration cap             */
+#define MPSGPU_ERR_CAPACITY       6   /* neighbour/PPE row capacity exceeded          */
+#define MPSGPU_ERR_DOMAIN         7   /* particle outside the bucket grid             */
+#define MPSGPU_ERR_NOGPU          8   /* no CUDA device visible                       */
+#define MPSGPU_ERR_SIZE_MISMATCH  9   /* implicit run lost particles (pressurePPE size) */
+
+/* ------------------------------------------------------------------ parameters
+ * Mirrors the JSON inputs of MpsParticleSystem (include/MpsParticleSystem.h:133-221),
+ * read by MpsInputOutput::readInputFile (src/MpsInputOutput.cpp:58-641), followed by the
+ * derived constants computed in MpsParticle::setParameters (src/MpsParticle.cpp:136-227)
+ * and MpsBucket::allocateMemory / calcDomainLimits (src/MpsBucket.cpp:20-295).
+ * Fill the input block, then call mpsgpu_params_derive() to fill the derived block
+ * (the radii reS/reL/reRepulsiveForce are given in units of partDist, as in the JSON;
+ * derive() scales them, exactly as setParameters does). */
+typedef struct MpsParams {
+    /* --- inputs (JSON) --- */
+    int    wallType;            /* 0 particle walls, 1 polygon                         */
+    int    femOn, forcedOn;     /* must be 0 (deformable/forced meshes not supported)  */
+    double domainMin[3], domainMax[3];
+    int    domainTypeBC;        /* 0 none (1 periodic: not supported)                  */
+    int    limitTypeBC;         /* 0 border particle positions, 1 JSON limits          */
+    double densityFluid, densityWall, KNM_VS1;
+    int    fluidType;           /* 0 Newtonian (1 non-Newtonian: not supported)        */
+    double gravity[3];
+    double KNM_VS2, DNS_FL1, DNS_FL2;
+    double dim, partDist, timeStep, timeSimulation;
+    int    iterOutput;
+    double cflNumber;
+    int    weightType, slipCondition;
+    double reS, reL;            /* input: multiples of partDist; derived: metres       */
+    int    gradientType, gradientCorrection;
+    double relaxPress;
+    int    mpsType;             /* 0 explicit, 1 weakly compressible, 2 implicit PND  */
+    double soundSpeed, gamma;
+    int    solverType;          /* 0 CG                                                */
+    double alphaCompressibility, relaxPND;
+    int    shiftingType;        /* 0 off, 1 velocity (DW*Uij), 2 position (GradC)      */
+    double dri, coefA, machNumber;
+    int    pndType;             /* 0 sum w, 1 mean, 2 diffusive                        */
+    double diffusiveCoef;
+    int    repulsiveForceType;  /* 0 Harada, 1 Mitsume, 2 Lennard-Jones, 3 Monaghan-K. */
+    double reRepulsiveForce, expectMaxVelocity;
+    double repForceCoefMitsume, repForceCoefLennardJones, repForceCoefMonaghanKajtar;
+    double EPS_RE;
+    int    freeSurfType;        /* 0 PND+neigh, 1 PND+NPCD (2 ARC: not supported)     */
+    double pndThreshold, neighThreshold, npcdThreshold, thetaThreshold, normThreshold;
+    int    collisionType;       /* 0 PC (1 DPC: not supported)                         */
+    double collisionRatio, distLimitRatio, lambdaCollision;
+    int    ghost, fluid, wall, dummyWall;   /* particle type IDs                        */
+    int    surface, inner, other;           /* boundary type IDs                        */
+    /* --- derived (mpsgpu_params_derive) --- */
+    double epsilonZero;         /* 10*DBL_EPSILON, include/MpsParticleSystem.h:241     */
+    double reS2, reL2;
+    double pndSmallZero, pndLargeZero, pndGradientZero, lambdaZero, numNeighZero;
+    double coeffViscosity, coeffViscMultiphase, coeffPressEMPS, coeffPressGrad;
+    double coeffPressWCMPS, coeffShifting1, coeffShifting2, coeffPPE, coeffPPESource;
+    double invPartDist, distCollisionLimit, distCollisionLimit2, restitutionCollision;
+    double betaPnd, betaNeigh, delta2, thetaArc, hThreshold2, dstThreshold2, normThreshold2;
+    double bucketSide, invBucketSide;
+    int    numBucketsX, numBucketsY, numBucketsZ, numBucketsXY, numBucketsXYZ;
+    int    derived;             /* set to 1 by mpsgpu_params_derive                    */
+} MpsParams;
+
+/* Triangle soup of the rigid polygon wall (what igl::readSTL yields,
+ * src/PolygonMesh.cpp:51): tri_xyz holds ntri*9 doubles (v0,v1,v2 per triangle). */
+typedef struct MpsMesh {
+    int           ntri;
+    const double* tri_xyz;
+} MpsMesh;
+
+/* Per-step statistics (what displayInfo prints, src/MpsInputOutput.cpp:37-55,
+ * plus the PPE solve figures and device timings). */
+typedef struct MpsStepStats {
+    int    numParticles;
+    int    ppeIterations;       /* SpMVs performed by the PPE solve                    */
+    int    ppeRefinements;      /* FP64 residual refinements (mixed solver)            */
+    int    outOfDomain;         /* particles removed this step                         */
+    double velMax, CFLcurrent;
+    double ppeRelResidual;      /* final FP64 ||b-Ax||/||b||                          */
+    double ppeInitialRelResidual;/* ||b-Ax0||/||b|| of the warm start                  */
+    double ppeSolveMs;          /* device time of the PPE solve (warm start+iterations)*/
+    double ppeAssembleMs;       /* device time of the PPE assembly                     */
+    double stepMs;              /* device time of the whole step                       */
+    long long nbrEntries;       /* neighbour-list entries of the last list build       */
+    long long ppeNnz;           /* non-zeros of the last PPE matrix (with diagonal)    */
+} MpsStepStats;
+
+/* Field identifiers for get/set.  Vector fields use the reference's interleaved host
+ * layout (N x 3 doubles, include/MpsParticle.h:155-165); scalars N doubles; integer
+ * fields N int32 (nearWall: 0/1). */
+enum MpsField {
+    MPS_F_POS = 0, MPS_F_VEL, MPS_F_ACC, MPS_F_ACCSTAR, MPS_F_NPCD, MPS_F_GRADC,
+    MPS_F_CORR1, MPS_F_CORR2, MPS_F_CORR3, MPS_F_MIRROR, MPS_F_WALLPOS, MPS_F_POLYNORMAL,
+    MPS_F_FORCEWALL,
+    MPS_F_PRESS = 32, MPS_F_PRESSPPE, MPS_F_PNDI, MPS_F_PNDKI, MPS_F_PNDSKI, MPS_F_PNDSMALL,
+    MPS_F_NPCD2, MPS_F_CONC, MPS_F_VELDIV, MPS_F_DIFFTERM, MPS_F_PNDWALL, MPS_F_RIW2,
+    MPS_F_DEVDOT, MPS_F_SOURCE,
+    MPS_F_TYPE = 64, MPS_F_BC, MPS_F_NUMNEIGH, MPS_F_NNEIGHWALL, MPS_F_NEARWALL
+};
+
+/* Operators, for the per-operator entry point mpsgpu_run_op (parity tests and the
+ * thin C++ shim that re-presents the library as the reference's class methods). */
+enum MpsOp {
+    MPS_OP_UPDATE_BUCKETS = 0,   /* MpsBucket::updateParticlesID  src/MpsBucket.cpp:299-353          */
+    MPS_OP_VISCOSITY,            /* MpsViscosity::calcViscosity  src/MpsViscosity.cpp:20-100          */
+    MPS_OP_ADD_GRAVITY,          /* MpsParticle::addGravity  src/MpsParticle.cpp:111-130              */
+    MPS_OP_PREDICT,              /* predictionVelocityPosition  src/MpsParticleVelPos.cpp:20-50       */
+    MPS_OP_OUT_OF_DOMAIN,        /* checkParticleOutDomain  src/MpsParticle.cpp:234-402              */
+    MPS_OP_COLLISION,            /* checkParticleCollisions  src/MpsParticleCollision.cpp:22-119     */
+    MPS_OP_WALL_DISTANCE,        /* closestPointPNDBoundaryAABB + updateParticlesNearPolygonMesh
+                                    src/PolygonMesh.cpp:585-795                                      */
+    MPS_OP_WALL_NPCD,            /* calcWallNPCD  src/MpsPndNeigh.cpp:105-195                        */
+    MPS_OP_CORRECTION_MATRIX,    /* correctionMatrix  src/MpsVectorMatrix.cpp:20-93                  */
+    MPS_OP_PND_NEIGH_NPCD,       /* calcPndnNeighNPCD  src/MpsPndNeigh.cpp:199-331                   */
+    MPS_OP_PND_DIFFUSIVE,        /* calcPndDiffusiveTerm (+wall), updatePnd,
+                                    meanPndParticlesWallDummySurface  src/MpsPndNeigh.cpp:334-852   */
+    MPS_OP_PND_MEAN,             /* meanWallPnd + meanPnd  src/MpsPndNeigh.cpp:855-994              */
+    MPS_OP_UPDATE_BC,            /* updateParticleBC  src/MpsBoundaryCondition.cpp:66-400            */
+    MPS_OP_CALC_PRESS,           /* calcPress (EOS or PPE+CG+clamp)  src/MpsPressure.cpp:32-476     */
+    MPS_OP_EXTRAPOLATE_PRESS,    /* extrapolatePressParticlesWallDummy  src/MpsPressure.cpp:792-846 */
+    MPS_OP_PRESS_GRADIENT,       /* calcPressGradient  src/MpsPressure.cpp:1217-1338                 */
+    MPS_OP_WALL_PRESS_GRADIENT,  /* calcWallPressGradient  src/MpsPressure.cpp:1341-1550             */
+    MPS_OP_WALL_VISCOSITY,       /* calcWall{NoSlip,Slip}Viscosity  src/MpsViscosity.cpp:1527-1910  */
+    MPS_OP_CORRECT,              /* correctionVelocityPosition  src/MpsParticleVelPos.cpp:53-97      */
+    MPS_OP_SHIFTING,             /* calcShifting / calcConcAndConcGradient (+wall)
+                                    src/MpsShifting.cpp:23-101, 432-691                             */
+    MPS_OP_DUMMY_VELOCITY,       /* updateVelocityParticlesWallDummy  src/MpsParticleVelPos.cpp:100-158 */
+    MPS_OP_INIT_PND,             /* step-0 sequence src/main.cpp:158-166: setInitialPnd..., meanWallPnd,
+                                    meanPnd, meanNeighFluidPnd                                       */
+    MPS_OP_COUNT
+};
+
+/* PPE solver selection (mpsgpu_set_solver).  PLAIN_FP64 is the drop-in for Eigen's
+ * ConjugateGradient (src/MpsPressure.cpp:424-445): Jacobi-preconditioned CG in FP64,
+ * warm-started from the previous unclamped solution.  MIXED runs FP32 SpMV/CG inner
+ * solves under FP64 iterative refinement (FP64 residual r=b-Ax, FP64 dots). */
+#define MPSGPU_SOLVER_PLAIN_FP64   0
+#define MPSGPU_SOLVER_MIXED        1
+#define MPSGPU_WARM_PREVIOUS       0   /* previous-step unclamped pressure (reference)  */
+#define MPSGPU_WARM_MLP            1   /* learned per-particle MLP correction           */
+#define MPSGPU_WARM_ZERO           2
+
+typedef struct mpsgpu_s* mpsgpu_t;
+
+/* Derive the constants of MpsParticle::setParameters (src/MpsParticle.cpp:136-227) and
+ * the bucket grid of MpsBucket::allocateMemory/calcDomainLimits (src/MpsBucket.cpp:20-295).
+ * Host only (no GPU needed).  pos3 (N x 3) is only read for particle walls
+ * (calcDomainLimits with limitTypeBC 0). */
+int mpsgpu_params_derive(MpsParams* p, int n, const double* pos3);
+
+/* Upload a particle system: replaces MpsInputOutput::readMpsParticleFile's arrays
+ * (src/MpsInputOutput.cpp:645-857) plus PolygonMesh::initPolygonMesh/readPolygonMeshFile
+ * (src/PolygonMesh.cpp:18-108) and initWijnNeigh (src/PolygonMesh.cpp:377-527).
+ * p must have been derived.  mesh may be NULL for particle walls. */
+int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3,
+                  const double* vel3, const double* press, const MpsMesh* mesh,
+                  mpsgpu_t* out);
+int mpsgpu_destroy(mpsgpu_t h);
+
+/* The step-0 sequence of main() (src/main.cpp:116-180): bucket update, out-of-domain,
+ * initMesh wall distance, initial PND, mean PND smoothing, BC and the step-0 pressure. */
+int mpsgpu_initialize(mpsgpu_t h);
+
+/* One iteration of mainLoopOfSimulation (src/main.cpp:256-467), in the reference order. */
+int mpsgpu_step(mpsgpu_t h, MpsStepStats* stats);
+/* nsteps iterations back to back; stats (may be NULL) receives the last step's figures. */
+int mpsgpu_run(mpsgpu_t h, int nsteps, MpsStepStats* stats);
+
+/* One operator (see MpsOp) on the current device state. */
+int mpsgpu_run_op(mpsgpu_t h, int op);
+/* Figures of the last step or operator (PPE iterations/residual/timings after CALC_PRESS);
+ * what PolyMPS reads through MpsPressure::getSolverIter/getSolverError
+ * (include/MpsPressure.h:242-253). */
+int mpsgpu_last_stats(mpsgpu_t h, MpsStepStats* out);
+
+/* Solver controls, replacing the fixed Eigen CG of src/MpsPressure.cpp:424-445. */
+int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm_start, double tol, int max_iter);
+
+/* Field transfer in the reference's host layout (see MpsField).  get writes
+ * numParticles entries; set reads numParticles entries. */
+int mpsgpu_get_field(mpsgpu_t h, int field, void* host);
+int mpsgpu_set_field(mpsgpu_t h, int field, const void* host);
+int mpsgpu_num_particles(mpsgpu_t h, int* n);
+int mpsgpu_time(mpsgpu_t h, double* t, int* iterations);
+
+/* Neighbour lists of the current positions through the current (stale) bucket list,
+ * as every reference sweep sees them (the 27-bucket scan of e.g. src/MpsPndNeigh.cpp:209-258
+ * with dst^2 < reL^2, j != i): counts[N] and, if nbr != NULL, the entries of particle i
+ * at nbr[offsets(i) ...] in scan order, offsets being the exclusive prefix sum of counts.
+ * nbr must hold sum(counts) ints.  Used by the bit-exact neighbour-set tests. */
+int mpsgpu_get_neighbors(mpsgpu_t h, int* counts, int* nbr, long long nbr_capacity);
+
+/* Last PPE system (ELL rows as CSR on the host): rowptr[N+1], col/val[nnz], rhs[N].
+ * nnz_out receives the count; pass col == NULL to query it. */
+int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col,
+                   double* val, double* rhs);
+
+/* Learned warm start (N2): MLP 16->64->64->64->1, GELU, BF16 weights, FP32 accumulate.
+ * Weights are the FP32 master copy in this packed order:
+ * W1[64x16] b1[64] W2[64x64] b2[64] W3[64x64] b3[64] W4[1x64] b4[1]  (row-major [out][in]),
+ * followed by 32 feature-normalisation floats (mean[16], inv_std[16]). */
+#define MPSGPU_MLP_NPARAM (64*16 + 64 + 64*64 + 64 + 64*64 + 64 + 64 + 1)
+#define MPSGPU_MLP_NFEAT  16
+int mpsgpu_mlp_set_weights(mpsgpu_t h, const float* params, const float* norm32);
+int mpsgpu_mlp_get_weights(mpsgpu_t h, float* params, float* norm32);
+/* Features of the current PPE system, N x 16 FP32 (host). */
+int mpsgpu_ppe_features(mpsgpu_t h, float* feat);
+/* Training on the GPU with the library's own forward/backward/Adam kernels.  While
+ * recording is enabled, every PPE solve appends (features, converged pressure minus
+ * previous pressure) of its inner rows to a device-resident training set. */
+int mpsgpu_mlp_record(mpsgpu_t h, int enable);
+int mpsgpu_mlp_num_records(mpsgpu_t h, long long* n);
+int mpsgpu_mlp_fit_normalization(mpsgpu_t h);
+/* iters Adam steps on mini-batches of `batch` recorded samples (multiple of 64);
+ * loss_hist (may be NULL) receives iters mean-squared losses. */
+int mpsgpu_mlp_train(mpsgpu_t h, int iters, int batch, float lr, unsigned long long seed,
+                     float* loss_hist);
+/* Network outputs for n host rows of raw features (N x 16 FP32). */
+int mpsgpu_mlp_forward(mpsgpu_t h, const float* feat, int n, float* out);
+/* Gradient (MPSGPU_MLP_NPARAM floats) and loss of the mean squared error of n host
+ * samples (n a multiple of 64), no optimiser step. target is in normalised units. */
+int mpsgpu_mlp_gradient(mpsgpu_t h, const float* feat, const float* target, int n,
+                        float* grad, float* loss);
+
+/* Device stream used by the handle (cudaStream_t as void*), for callers that
+ * interleave their own work. */
+int mpsgpu_stream(mpsgpu_t h, void** stream);
+
+/* Human-readable text for the last error of this handle (or of the library if h==NULL). */
+const char* mpsgpu_last_error(mpsgpu_t h);
+
+/* ABI check for bindings: sizeof(MpsParams), sizeof(MpsStepStats), sizeof(MpsMesh). */
+int mpsgpu_abi_sizes(int* params, int* stats, int* mesh);
+
+/* Device timing per operator with CUDA events on the handle's stream (the per-kernel
+ * timer the reference lacks; it only prints wall time, src/MpsInputOutput.cpp:31-55).
+ * Classes 0..MPS_OP_COUNT-1 are the MpsOp operators, followed by NEIGHBOR_LIST,
+ * PPE_ASSEMBLE, PPE_SPMV, PPE_VECTOR, PPE_OTHER.  Enabling resets the totals. */
+#define MPSGPU_PROF_NCLASS (MPS_OP_COUNT + 5)
+int mpsgpu_profile(mpsgpu_t h, int enable);
+int mpsgpu_profile_get(mpsgpu_t h, int cls, double* ms, long long* calls);
+const char* mpsgpu_profile_name(int cls);
+/* Kernels launched by this library in this process so far. */
+int mpsgpu_launch_count(long long* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPSGPU_H_ */

@@ -1,0 +1,785 @@
+// mps_api.cu — the C ABI of libmpsgpu (include/mpsgpu.h): handle, device memory,
+// field transfer in the reference's host layout, and the step in the reference order
+// (mainLoopOfSimulation, src/main.cpp:256-467).
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "mps_common.cuh"
+#include "mps_internal.h"
+#include "mps_host.h"
+#include "mps_mlp.h"
+
+namespace {
+thread_local std::string g_lastError;
+}
+
+struct mpsgpu_s {
+    Dev d;
+    PpeBuffers B;
+    cudaStream_t s = nullptr;
+    int N0 = 0;
+    std::vector<void*> allocs;
+    int* scanScratch = nullptr;
+    int* outFlags = nullptr;
+    int* outCounter = nullptr;
+    // solver controls
+    int solver = MPSGPU_SOLVER_PLAIN_FP64, warm = MPSGPU_WARM_PREVIOUS;
+    double tol = 1e-8;
+    int maxIter = 0;
+    // host mirrors of a few scalars
+    bool listValid = false;
+    double timeCurrent = 0.0;
+    int numIter = 0;
+    int lastOut = 0;
+    MpsStepStats last{};
+    cudaEvent_t e0 = nullptr, e1 = nullptr, ea0 = nullptr, ea1 = nullptr, es0 = nullptr, es1 = nullptr;
+    std::string err;
+    MlpState mlp;
+    Prof prof;
+    void* pinned = nullptr;       // host staging for field transfers (N0 x 32 bytes, page-locked)
+};
+
+// ------------------------------------------------------------------ profiler
+void Prof::begin(int c, cudaStream_t s) {
+    if (2 * used + 2 > ev.size()) {
+        for (int k = 0; k < 64; k++) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            ev.push_back(e);
+        }
+        cls.resize(ev.size() / 2);
+    }
+    cls[used] = c;
+    cudaEventRecord(ev[2 * used], s);
+    open.push_back(used);
+    used++;
+}
+void Prof::end(cudaStream_t s) {
+    if (open.empty()) return;
+    size_t slot = open.back();
+    open.pop_back();
+    cudaEventRecord(ev[2 * slot + 1], s);
+}
+int Prof::flush() {
+    if (!used || !open.empty()) return 0;
+    if (cudaEventSynchronize(ev[2 * used - 1]) != cudaSuccess) return MPSGPU_ERR_CUDA;
+    for (size_t k = 0; k < used; k++)
+        if (cudaEventSynchronize(ev[2 * k + 1]) != cudaSuccess) return MPSGPU_ERR_CUDA;
+    for (size_t k = 0; k < used; k++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]);
+        this->ms[cls[k]] += ms;
+        calls[cls[k]]++;
+    }
+    used = 0;
+    return 0;
+}
+void Prof::reset() {
+    used = 0;
+    for (int k = 0; k < PROF_NCLASS; k++) { ms[k] = 0; calls[k] = 0; }
+}
+void Prof::destroy() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    ev.clear(); cls.clear(); used = 0;
+}
+
+// Kernels launched by one operator (fixed by the configuration; the solvers count theirs).
+static int opLaunches(int op, const MpsParams& P) {
+    switch (op) {
+        case MPS_OP_UPDATE_BUCKETS: return 6;
+        case MPS_OP_OUT_OF_DOMAIN: return 2;
+        case MPS_OP_COLLISION: return 2;
+        case MPS_OP_WALL_DISTANCE: case MPS_OP_WALL_NPCD: case MPS_OP_WALL_PRESS_GRADIENT:
+        case MPS_OP_WALL_VISCOSITY: return P.wallType == 1 ? 1 : 0;
+        case MPS_OP_PND_DIFFUSIVE: return P.wallType == 1 ? 5 : 4;
+        case MPS_OP_PND_MEAN: return P.wallType == 1 ? 3 : 2;
+        case MPS_OP_INIT_PND: return 2 + (P.wallType == 1 ? 3 : 2);
+        case MPS_OP_CALC_PRESS: return (P.mpsType == 2) ? 2 : 1;   // assemble + copy back | EOS
+        case MPS_OP_SHIFTING: return P.shiftingType == 1 ? 2 : (P.shiftingType == 2 ? (P.wallType == 1 ? 5 : 3) : 0);
+        case MPS_OP_DUMMY_VELOCITY: return P.wallType == 0 ? 1 : 0;
+        default: return 1;
+    }
+}
+
+#define CK(x)                                                                    \
+    do {                                                                         \
+        cudaError_t _e = (x);                                                    \
+        if (_e != cudaSuccess) {                                                 \
+            g_lastError = std::string(#x) + ": " + cudaGetErrorString(_e);       \
+            return MPSGPU_ERR_CUDA;                                              \
+        }                                                                        \
+    } while (0)
+
+template <class T>
+static int dalloc(mpsgpu_t h, T** p, size_t count) {
+    void* q = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+    if (e != cudaSuccess) { g_lastError = std::string("cudaMalloc: ") + cudaGetErrorString(e); return MPSGPU_ERR_NOMEM; }
+    cudaMemsetAsync(q, 0, count * sizeof(T), h->s);
+    h->allocs.push_back(q);
+    *p = (T*)q;
+    return 0;
+}
+
+static int checkDeviceErrors(mpsgpu_t h) {
+    unsigned int e = 0;
+    CK(cudaMemcpyAsync(&e, h->d.err, sizeof(e), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    if (e) {
+        CK(cudaMemsetAsync(h->d.err, 0, sizeof(unsigned int), h->s));
+        if (e & MPSE_CAPACITY) { g_lastError = "neighbour row capacity exceeded"; return MPSGPU_ERR_CAPACITY; }
+        if (e & MPSE_DOMAIN) { g_lastError = "particle outside the bucket grid"; return MPSGPU_ERR_DOMAIN; }
+        if (e & MPSE_NAN) { g_lastError = "non-finite value"; return MPSGPU_ERR_NOT_CONVERGED; }
+    }
+    return 0;
+}
+
+static int launchStatus() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { g_lastError = std::string("kernel launch: ") + cudaGetErrorString(e); return MPSGPU_ERR_CUDA; }
+    return 0;
+}
+
+static void ensureList(mpsgpu_t h) {
+    if (h->listValid) return;
+    if (h->prof.on) h->prof.begin(PROF_NEIGHBOR_LIST, h->s);
+    launchNeighborList(h->d, h->s);
+    if (h->prof.on) h->prof.end(h->s);
+    countLaunch(2);
+    h->listValid = true;
+}
+
+static int unsupported(const MpsParams& P) {
+    if (P.femOn || P.forcedOn) return 1;
+    if (P.domainTypeBC != 0) return 1;
+    if (P.fluidType != 0) return 1;
+    if (P.freeSurfType == 2) return 1;
+    if (P.collisionType != 0) return 1;
+    if (P.mpsType == 3) return 1;
+    if (P.mpsType == 2 && P.solverType != 0) return 1;
+    if (P.relaxPress < 1.0) return 1;
+    return 0;
+}
+
+// ------------------------------------------------------------------ pressure
+static int calcPress(mpsgpu_t h) {
+    const MpsParams& P = h->d.P;
+    if (P.mpsType == 0 || P.mpsType == 1) {
+        launchEOS(h->d, h->s);
+        return launchStatus();
+    }
+    ensureList(h);
+    cudaEventRecord(h->ea0, h->s);
+    if (h->prof.on) h->prof.begin(PROF_PPE_ASSEMBLE, h->s);
+    launchPpeAssemble(h->d, h->B, h->s);
+    if (h->prof.on) h->prof.end(h->s);
+    cudaEventRecord(h->ea1, h->s);
+    // warm start: previous unclamped solution (reference), zero, or the learned predictor
+    if (h->warm == MPSGPU_WARM_ZERO) cudaMemsetAsync(h->B.x, 0, sizeof(double) * h->N0, h->s);
+    cudaEventRecord(h->es0, h->s);
+    if (h->warm == MPSGPU_WARM_MLP) {
+        if (h->prof.on) h->prof.begin(PROF_PPE_OTHER, h->s);
+        int e = mlpWarmStart(h->mlp, h->d, h->B, h->s);
+        if (h->prof.on) h->prof.end(h->s);
+        countLaunch(3);
+        if (e) return e;
+    } else if (h->warm != MPSGPU_WARM_ZERO) {
+        cudaMemcpyAsync(h->B.x, h->d.pressPPE, sizeof(double) * h->N0, cudaMemcpyDeviceToDevice, h->s);
+    }
+    int iters = 0, refine = 0;
+    double rr = 0, rr0 = 0;
+    int maxIt = h->maxIter > 0 ? h->maxIter : 2 * h->N0;
+    int e;
+    if (h->solver == MPSGPU_SOLVER_MIXED)
+        e = ppeSolveMixed(h->d, h->B, h->tol, maxIt, h->s, &iters, &refine, &rr, &rr0, &h->prof);
+    else e = ppeSolvePlain(h->d, h->B, h->tol, maxIt, h->s, &iters, &rr, &rr0, &h->prof);
+    cudaEventRecord(h->es1, h->s);
+    if (h->mlp.recording && !e) {
+        // features of this system with the previous solution, target = converged - previous
+        int er = mlpRecordFeatures(h->mlp, h->d, h->B, h->s);
+        if (!er) er = mlpRecordTargets(h->mlp, h->d, h->B, h->s);
+        if (er) return er;
+    }
+    launchPpeCopyBack(h->d, h->B, h->s);
+    h->last.ppeIterations = iters;
+    h->last.ppeRefinements = refine;
+    h->last.ppeRelResidual = rr;
+    h->last.ppeInitialRelResidual = rr0;
+    CK(cudaEventSynchronize(h->es1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->es0, h->es1);
+    h->last.ppeSolveMs = ms;
+    cudaEventElapsedTime(&ms, h->ea0, h->ea1);
+    h->last.ppeAssembleMs = ms;
+    if (e == MPSGPU_ERR_NOT_CONVERGED) g_lastError = "PPE solver did not reach the tolerance";
+    int ls = launchStatus();
+    return e ? e : ls;
+}
+
+static int runOpBody(mpsgpu_t h, int op);
+static int runOpImpl(mpsgpu_t h, int op) {
+    if (op < 0 || op >= MPS_OP_COUNT) { g_lastError = "unknown operator"; return MPSGPU_ERR_ARG; }
+    bool pr = h->prof.on && op != MPS_OP_INIT_PND;
+    if (pr) h->prof.begin(op, h->s);
+    int e = runOpBody(h, op);
+    if (pr) h->prof.end(h->s);
+    countLaunch(opLaunches(op, h->d.P));
+    return e;
+}
+static int runOpBody(mpsgpu_t h, int op) {
+    Dev& d = h->d;
+    const MpsParams& P = d.P;
+    cudaStream_t s = h->s;
+    switch (op) {
+        case MPS_OP_UPDATE_BUCKETS: launchBuckets(d, h->scanScratch, s); h->listValid = false; break;
+        case MPS_OP_VISCOSITY: launchViscosity(d, s); break;
+        case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
+        case MPS_OP_PREDICT: launchPredict(d, s); h->listValid = false; break;
+        case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); h->listValid = false; break;
+        case MPS_OP_COLLISION: ensureList(h); launchCollision(d, s); break;
+        case MPS_OP_WALL_DISTANCE: launchWallDistance(d, s); break;
+        case MPS_OP_WALL_NPCD: ensureList(h); launchWallNpcd(d, s); break;
+        case MPS_OP_CORRECTION_MATRIX: ensureList(h); launchCorrectionMatrix(d, s); break;
+        case MPS_OP_PND_NEIGH_NPCD: ensureList(h); launchPndNeighNpcd(d, s); break;
+        case MPS_OP_PND_DIFFUSIVE: ensureList(h); launchPndDiffusive(d, s); break;
+        case MPS_OP_PND_MEAN: ensureList(h); launchPndMean(d, s); break;
+        case MPS_OP_UPDATE_BC: launchUpdateBC(d, s); break;
+        case MPS_OP_CALC_PRESS: { int e = calcPress(h); if (e) return e; break; }
+        case MPS_OP_EXTRAPOLATE_PRESS: ensureList(h); launchExtrapolatePress(d, s); break;
+        case MPS_OP_PRESS_GRADIENT: ensureList(h); launchPressGradient(d, s); break;
+        case MPS_OP_WALL_PRESS_GRADIENT: ensureList(h); launchWallPressGradient(d, s); break;
+        case MPS_OP_WALL_VISCOSITY: ensureList(h); launchWallViscosity(d, s); break;
+        case MPS_OP_CORRECT: launchCorrect(d, s); h->listValid = false; break;
+        case MPS_OP_SHIFTING: launchShifting(d, s); if (P.shiftingType == 2) h->listValid = false; break;
+        case MPS_OP_DUMMY_VELOCITY: launchDummyVelocity(d, s); break;
+        case MPS_OP_INIT_PND: ensureList(h); launchInitPnd(d, s); break;
+        default: g_lastError = "unknown operator"; return MPSGPU_ERR_ARG;
+    }
+    return launchStatus();
+}
+
+static int stepImpl(mpsgpu_t h) {
+    const MpsParams& P = h->d.P;
+    int e;
+#define RUN(op) do { if ((e = runOpImpl(h, op))) return e; } while (0)
+    RUN(MPS_OP_UPDATE_BUCKETS);
+    RUN(MPS_OP_VISCOSITY);
+    RUN(MPS_OP_ADD_GRAVITY);
+    RUN(MPS_OP_PREDICT);
+    RUN(MPS_OP_OUT_OF_DOMAIN);
+    ensureList(h);                       // post-prediction neighbour list
+    RUN(MPS_OP_COLLISION);
+    if (P.wallType == 1) { RUN(MPS_OP_WALL_DISTANCE); RUN(MPS_OP_WALL_NPCD); }
+    // The first correctionMatrix call (src/main.cpp:317-319) is read only by the diffusive
+    // PND; otherwise the second call (src/main.cpp:375-377, same positions) overwrites it.
+    if (P.gradientCorrection && P.pndType == 2) RUN(MPS_OP_CORRECTION_MATRIX);
+    RUN(MPS_OP_PND_NEIGH_NPCD);
+    if (P.pndType == 2) RUN(MPS_OP_PND_DIFFUSIVE);
+    else if (P.pndType == 1) RUN(MPS_OP_PND_MEAN);
+    RUN(MPS_OP_UPDATE_BC);
+    RUN(MPS_OP_CALC_PRESS);
+    if (P.wallType == 0) RUN(MPS_OP_EXTRAPOLATE_PRESS);
+    if (P.gradientCorrection) RUN(MPS_OP_CORRECTION_MATRIX);
+    RUN(MPS_OP_PRESS_GRADIENT);
+    if (P.wallType == 1) { RUN(MPS_OP_WALL_PRESS_GRADIENT); RUN(MPS_OP_WALL_VISCOSITY); }
+    RUN(MPS_OP_CORRECT);
+    RUN(MPS_OP_OUT_OF_DOMAIN);
+    if (P.shiftingType != 0) RUN(MPS_OP_SHIFTING);
+    if (P.wallType == 0) RUN(MPS_OP_DUMMY_VELOCITY);
+    RUN(MPS_OP_OUT_OF_DOMAIN);
+#undef RUN
+    if (h->prof.on && (e = h->prof.flush())) return e;
+    h->numIter++;
+    h->timeCurrent += P.timeStep;
+    return 0;
+}
+
+static int finishStats(mpsgpu_t h, MpsStepStats* st, float stepMs) {
+    double vmax = 0;
+    int n = 0;
+    unsigned long long cnt[2] = {0, 0};
+    CK(cudaMemcpyAsync(&vmax, h->d.velMax, sizeof(double), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaMemcpyAsync(&n, h->d.nLive, sizeof(int), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaMemcpyAsync(cnt, h->d.counters, sizeof(cnt), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    h->last.nbrEntries = (long long)cnt[0];
+    h->last.ppeNnz = (h->d.P.mpsType == 2) ? (long long)cnt[1] + n : 0;
+    h->last.velMax = vmax;
+    h->last.CFLcurrent = h->d.P.timeStep * vmax / h->d.P.partDist;
+    h->last.numParticles = n;
+    h->last.stepMs = stepMs;
+    if (st) *st = h->last;
+    return 0;
+}
+
+extern "C" {
+
+int mpsgpu_params_derive(MpsParams* p, int n, const double* pos3) {
+    int e = hostDeriveParams(p, n, pos3);
+    if (e) g_lastError = "parameter derivation failed (dimension/limits)";
+    return e;
+}
+
+const char* mpsgpu_last_error(mpsgpu_t h) {
+    (void)h;
+    return g_lastError.c_str();
+}
+
+int mpsgpu_profile(mpsgpu_t h, int enable) {
+    if (!h) return MPSGPU_ERR_ARG;
+    int e = h->prof.flush();
+    h->prof.reset();
+    h->prof.on = enable != 0;
+    return e;
+}
+
+int mpsgpu_profile_get(mpsgpu_t h, int cls, double* ms, long long* calls) {
+    if (!h || cls < 0 || cls >= PROF_NCLASS) return MPSGPU_ERR_ARG;
+    int e = h->prof.flush();
+    if (ms) *ms = h->prof.ms[cls];
+    if (calls) *calls = h->prof.calls[cls];
+    return e;
+}
+
+const char* mpsgpu_profile_name(int cls) {
+    static const char* ops[] = {"UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT", "OUT_OF_DOMAIN",
+                                "COLLISION", "WALL_DISTANCE", "WALL_NPCD", "CORRECTION_MATRIX", "PND_NEIGH_NPCD",
+                                "PND_DIFFUSIVE", "PND_MEAN", "UPDATE_BC", "CALC_PRESS", "EXTRAPOLATE_PRESS",
+                                "PRESS_GRADIENT", "WALL_PRESS_GRADIENT", "WALL_VISCOSITY", "CORRECT", "SHIFTING",
+                                "DUMMY_VELOCITY", "INIT_PND"};
+    static const char* extra[] = {"NEIGHBOR_LIST", "PPE_ASSEMBLE", "PPE_SPMV", "PPE_VECTOR", "PPE_OTHER"};
+    static_assert(sizeof(ops) / sizeof(ops[0]) == MPS_OP_COUNT, "operator names");
+    if (cls >= 0 && cls < MPS_OP_COUNT) return ops[cls];
+    if (cls >= MPS_OP_COUNT && cls < PROF_NCLASS) return extra[cls - MPS_OP_COUNT];
+    return "";
+}
+
+int mpsgpu_launch_count(long long* n) {
+    if (!n) return MPSGPU_ERR_ARG;
+    *n = launchCount();
+    return 0;
+}
+
+int mpsgpu_abi_sizes(int* params, int* stats, int* mesh) {
+    if (params) *params = (int)sizeof(MpsParams);
+    if (stats) *stats = (int)sizeof(MpsStepStats);
+    if (mesh) *mesh = (int)sizeof(MpsMesh);
+    return 0;
+}
+
+int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3, const double* vel3,
+                  const double* press, const MpsMesh* mesh, mpsgpu_t* out) {
+    if (!p || !p->derived || n <= 0 || !type || !pos3 || !out) { g_lastError = "bad argument"; return MPSGPU_ERR_ARG; }
+    if (unsupported(*p)) { g_lastError = "configuration outside the implemented path"; return MPSGPU_ERR_UNSUPPORTED; }
+    if (p->wallType == 1 && (!mesh || mesh->ntri <= 0 || !mesh->tri_xyz)) { g_lastError = "polygon walls need a mesh"; return MPSGPU_ERR_ARG; }
+    if (mesh && mesh->ntri > MPS_MAX_TRI) { g_lastError = "mesh larger than the brute-force wall kernel supports"; return MPSGPU_ERR_UNSUPPORTED; }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { g_lastError = "no CUDA device"; return MPSGPU_ERR_NOGPU; }
+    mpsgpu_t h = new mpsgpu_s();
+    h->N0 = n;
+    cudaError_t ce = cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) { g_lastError = cudaGetErrorString(ce); delete h; return MPSGPU_ERR_CUDA; }
+    for (cudaEvent_t* ev : {&h->e0, &h->e1, &h->ea0, &h->ea1, &h->es0, &h->es1}) cudaEventCreate(ev);
+    Dev& d = h->d;
+    std::memset(&d, 0, sizeof(d));
+    d.P = *p;
+    d.N0 = n;
+    d.nB = p->numBucketsXYZ;
+    d.K = ((int)p->dim == 3) ? 64 : 32;
+    int e = 0;
+#define A(ptr, cnt) do { if ((e = dalloc(h, &(ptr), (cnt)))) { mpsgpu_destroy(h); return e; } } while (0)
+    A(d.nLive, 1);
+    for (dvec4** v : {&d.pos, &d.vel, &d.acc, &d.accStar, &d.mirror, &d.wallPos, &d.polyNormal, &d.npcd, &d.gradC,
+                        &d.forceWall, &d.c1, &d.c2, &d.c3, &d.dvel, &d.shift})
+        A(*v, n);
+    for (double** v : {&d.press, &d.pressPPE, &d.pndi, &d.pndki, &d.pndski, &d.pndSmall, &d.npcd2, &d.conc, &d.velDiv,
+                       &d.diffTerm, &d.pndWall, &d.riw2, &d.devDot, &d.source, &d.aux1, &d.aux2})
+        A(*v, n);
+    for (int** v : {&d.type, &d.bc, &d.numNeigh, &d.nNeighWall, &d.nearWall}) A(*v, n);
+    A(d.posf, n);
+    A(d.cellOf, n);
+    A(d.cellStart, d.nB + 1);
+    A(d.cellCount, d.nB + 1);
+    A(d.cellCursor, d.nB + 1);
+    A(d.cellSorted, n);
+    A(d.nbrCount, n);
+    A(d.nbr, (size_t)d.K * n);
+    A(d.velMax, 1);
+    A(d.err, 1);
+    A(d.counters, 4);
+    A(h->scanScratch, scanScratchInts(std::max(d.nB, n)));
+    A(h->outFlags, n);
+    A(h->outCounter, 1);
+    // FP32 prefilter band (see k_build_nbr): |d2f - d2| <= 3.47 delta re + 3 delta^2 + 3.1 u re^2
+    {
+        double X = 0;
+        for (int k = 0; k < 3; k++) X = std::max(X, p->domainMax[k] - p->domainMin[k]);
+        X += 4.0 * p->bucketSide;
+        double u = std::ldexp(1.0, -24), re = p->reL;
+        double delta = u * (2.0 * X + 2.0 * re);
+        double band = 2.0 * (3.47 * delta * re + 3.0 * delta * delta + 3.1 * u * re * re);
+        d.reL2f = (float)p->reL2;
+        d.bandLo = (float)(p->reL2 - band);
+        d.bandHi = (float)(p->reL2 + band);
+    }
+    // mesh and wall tables
+    if (p->wallType == 1) {
+        std::vector<double> nrm(3 * mesh->ntri), tab(4 * MPS_TAB);
+        hostTriNormals(mesh->ntri, mesh->tri_xyz, nrm.data());
+        hostWallTables(*p, tab.data());
+        double *dt = nullptr, *dn = nullptr, *dtab = nullptr;
+        A(dt, 9 * mesh->ntri);
+        A(dn, 3 * mesh->ntri);
+        A(dtab, 4 * MPS_TAB);
+        cudaMemcpyAsync(dt, mesh->tri_xyz, sizeof(double) * 9 * mesh->ntri, cudaMemcpyHostToDevice, h->s);
+        cudaMemcpyAsync(dn, nrm.data(), sizeof(double) * nrm.size(), cudaMemcpyHostToDevice, h->s);
+        cudaMemcpyAsync(dtab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, h->s);
+        d.tri = dt; d.triNormal = dn; d.tab = dtab; d.ntri = mesh->ntri;
+        cudaStreamSynchronize(h->s);
+    }
+    // PPE buffers
+    PpeBuffers& B = h->B;
+    std::memset(&B, 0, sizeof(B));
+    B.N0 = n; B.K = d.K;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    B.nblocks = std::max(1, sms) * 8;
+    if (p->mpsType == 2) {
+        for (double** v : {&B.diag, &B.x, &B.b, &B.r, &B.z, &B.p, &B.Ap}) A(*v, n);
+        A(B.val, (size_t)d.K * n);
+        A(B.col, (size_t)d.K * n);
+        A(B.rowLen, n);
+        A(B.valf, (size_t)d.K * n);
+        for (float** v : {&B.diagf, &B.diagInvf, &B.rf, &B.zf, &B.pf, &B.Apf, &B.xf}) A(*v, n);
+        A(B.scal, 16);
+        A(B.partials, 4 * B.nblocks);
+        A(B.counter, 1);
+        A(B.flag, 4);
+    }
+#undef A
+    // upload the particle state (src/MpsInputOutput.cpp:759-856 initial values)
+    std::vector<dvec4> v4(n);
+    auto up4 = [&](dvec4* dst, const double* src3, double fill) {
+        for (int i = 0; i < n; i++)
+            v4[i] = src3 ? make_dvec4(src3[3 * i], src3[3 * i + 1], src3[3 * i + 2], 0.0)
+                         : make_dvec4(fill, fill, fill, 0.0);
+        cudaMemcpy(dst, v4.data(), sizeof(dvec4) * n, cudaMemcpyHostToDevice);
+    };
+    up4(d.pos, pos3, 0.0);
+    up4(d.vel, vel3, 0.0);
+    cudaMemcpy(d.type, type, sizeof(int) * n, cudaMemcpyHostToDevice);
+    if (press) cudaMemcpy(d.press, press, sizeof(double) * n, cudaMemcpyHostToDevice);
+    std::vector<double> big(n, 10e8 * p->partDist);
+    cudaMemcpy(d.riw2, big.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(d.nLive, &n, sizeof(int), cudaMemcpyHostToDevice);
+    if (cudaDeviceSynchronize() != cudaSuccess || launchStatus()) { mpsgpu_destroy(h); return MPSGPU_ERR_CUDA; }
+    h->maxIter = 0;
+    if (cudaMallocHost(&h->pinned, sizeof(dvec4) * (size_t)n) != cudaSuccess) { mpsgpu_destroy(h); return MPSGPU_ERR_NOMEM; }
+    if ((e = mlpInit(h->mlp, n, h->s))) { mpsgpu_destroy(h); return e; }
+    *out = h;
+    return 0;
+}
+
+int mpsgpu_destroy(mpsgpu_t h) {
+    if (!h) return MPSGPU_ERR_ARG;
+    if (h->s) cudaStreamSynchronize(h->s);
+    mlpFree(h->mlp);
+    h->prof.destroy();
+    if (h->pinned) cudaFreeHost(h->pinned);
+    for (void* p : h->allocs) cudaFree(p);
+    for (cudaEvent_t ev : {h->e0, h->e1, h->ea0, h->ea1, h->es0, h->es1}) if (ev) cudaEventDestroy(ev);
+    if (h->s) cudaStreamDestroy(h->s);
+    delete h;
+    return 0;
+}
+
+int mpsgpu_initialize(mpsgpu_t h) {
+    if (!h) return MPSGPU_ERR_ARG;
+    const MpsParams& P = h->d.P;
+    int e;
+    if ((e = runOpImpl(h, MPS_OP_UPDATE_BUCKETS))) return e;
+    if ((e = runOpImpl(h, MPS_OP_OUT_OF_DOMAIN))) return e;
+    if (P.wallType == 1) {      // initMesh, src/main.cpp:527-554
+        if ((e = runOpImpl(h, MPS_OP_WALL_DISTANCE))) return e;
+        if ((e = runOpImpl(h, MPS_OP_WALL_NPCD))) return e;
+    }
+    if ((e = runOpImpl(h, MPS_OP_INIT_PND))) return e;
+    if ((e = runOpImpl(h, MPS_OP_UPDATE_BC))) return e;
+    if ((e = runOpImpl(h, MPS_OP_CALC_PRESS))) return e;
+    return checkDeviceErrors(h);
+}
+
+int mpsgpu_step(mpsgpu_t h, MpsStepStats* stats) {
+    if (!h) return MPSGPU_ERR_ARG;
+    std::memset(&h->last, 0, sizeof(h->last));
+    cudaEventRecord(h->e0, h->s);
+    int e = stepImpl(h);
+    cudaEventRecord(h->e1, h->s);
+    if (e) return e;
+    if ((e = checkDeviceErrors(h))) return e;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    return finishStats(h, stats, ms);
+}
+
+int mpsgpu_run(mpsgpu_t h, int nsteps, MpsStepStats* stats) {
+    if (!h || nsteps < 0) return MPSGPU_ERR_ARG;
+    cudaEventRecord(h->e0, h->s);
+    for (int k = 0; k < nsteps; k++) {
+        int e = stepImpl(h);
+        if (e) return e;
+    }
+    cudaEventRecord(h->e1, h->s);
+    int e = checkDeviceErrors(h);
+    if (e) return e;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    return finishStats(h, stats, ms);
+}
+
+int mpsgpu_run_op(mpsgpu_t h, int op) {
+    if (!h) return MPSGPU_ERR_ARG;
+    int e = runOpImpl(h, op);
+    if (e) return e;
+    return checkDeviceErrors(h);
+}
+
+int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm, double tol, int max_iter) {
+    if (!h || (solver != MPSGPU_SOLVER_PLAIN_FP64 && solver != MPSGPU_SOLVER_MIXED) || warm < 0 || warm > 2 || !(tol > 0))
+        return MPSGPU_ERR_ARG;
+    if (warm == MPSGPU_WARM_MLP && !h->mlp.ready) { g_lastError = "MLP weights not set"; return MPSGPU_ERR_ARG; }
+    h->solver = solver; h->warm = warm; h->tol = tol; h->maxIter = max_iter;
+    return 0;
+}
+
+int mpsgpu_num_particles(mpsgpu_t h, int* n) {
+    if (!h || !n) return MPSGPU_ERR_ARG;
+    CK(cudaMemcpyAsync(n, h->d.nLive, sizeof(int), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    return 0;
+}
+
+int mpsgpu_time(mpsgpu_t h, double* t, int* it) {
+    if (!h) return MPSGPU_ERR_ARG;
+    if (t) *t = h->timeCurrent;
+    if (it) *it = h->numIter;
+    return 0;
+}
+
+int mpsgpu_stream(mpsgpu_t h, void** stream) {
+    if (!h || !stream) return MPSGPU_ERR_ARG;
+    *stream = (void*)h->s;
+    return 0;
+}
+
+static void* fieldPtr(mpsgpu_t h, int f, int* kind) {
+    Dev& d = h->d;
+    *kind = 0;
+    switch (f) {
+        case MPS_F_POS: return d.pos;
+        case MPS_F_VEL: return d.vel;
+        case MPS_F_ACC: return d.acc;
+        case MPS_F_ACCSTAR: return d.accStar;
+        case MPS_F_NPCD: return d.npcd;
+        case MPS_F_GRADC: return d.gradC;
+        case MPS_F_CORR1: return d.c1;
+        case MPS_F_CORR2: return d.c2;
+        case MPS_F_CORR3: return d.c3;
+        case MPS_F_MIRROR: return d.mirror;
+        case MPS_F_WALLPOS: return d.wallPos;
+        case MPS_F_POLYNORMAL: return d.polyNormal;
+        case MPS_F_FORCEWALL: return d.forceWall;
+        default: break;
+    }
+    *kind = 1;
+    switch (f) {
+        case MPS_F_PRESS: return d.press;
+        case MPS_F_PRESSPPE: return d.pressPPE;
+        case MPS_F_PNDI: return d.pndi;
+        case MPS_F_PNDKI: return d.pndki;
+        case MPS_F_PNDSKI: return d.pndski;
+        case MPS_F_PNDSMALL: return d.pndSmall;
+        case MPS_F_NPCD2: return d.npcd2;
+        case MPS_F_CONC: return d.conc;
+        case MPS_F_VELDIV: return d.velDiv;
+        case MPS_F_DIFFTERM: return d.diffTerm;
+        case MPS_F_PNDWALL: return d.pndWall;
+        case MPS_F_RIW2: return d.riw2;
+        case MPS_F_DEVDOT: return d.devDot;
+        case MPS_F_SOURCE: return d.source;
+        default: break;
+    }
+    *kind = 2;
+    switch (f) {
+        case MPS_F_TYPE: return d.type;
+        case MPS_F_BC: return d.bc;
+        case MPS_F_NUMNEIGH: return d.numNeigh;
+        case MPS_F_NNEIGHWALL: return d.nNeighWall;
+        case MPS_F_NEARWALL: return d.nearWall;
+        default: break;
+    }
+    return nullptr;
+}
+
+int mpsgpu_get_field(mpsgpu_t h, int f, void* host) {
+    if (!h || !host) return MPSGPU_ERR_ARG;
+    int kind;
+    void* p = fieldPtr(h, f, &kind);
+    if (!p) { g_lastError = "unknown field"; return MPSGPU_ERR_ARG; }
+    int n = 0;
+    int e = mpsgpu_num_particles(h, &n);
+    if (e) return e;
+    if (kind == 0) {
+        dvec4* v = (dvec4*)h->pinned;
+        CK(cudaMemcpyAsync(v, p, sizeof(dvec4) * n, cudaMemcpyDeviceToHost, h->s));
+        CK(cudaStreamSynchronize(h->s));
+        double* o = (double*)host;
+        for (int i = 0; i < n; i++) { o[3 * i] = v[i].x; o[3 * i + 1] = v[i].y; o[3 * i + 2] = v[i].z; }
+    } else {
+        size_t sz = (kind == 1) ? sizeof(double) : sizeof(int);
+        CK(cudaMemcpyAsync(h->pinned, p, sz * n, cudaMemcpyDeviceToHost, h->s));
+        CK(cudaStreamSynchronize(h->s));
+        std::memcpy(host, h->pinned, sz * n);
+    }
+    return 0;
+}
+
+int mpsgpu_last_stats(mpsgpu_t h, MpsStepStats* out) {
+    if (!h || !out) return MPSGPU_ERR_ARG;
+    *out = h->last;
+    return 0;
+}
+
+int mpsgpu_set_field(mpsgpu_t h, int f, const void* host) {
+    if (!h || !host) return MPSGPU_ERR_ARG;
+    int kind;
+    void* p = fieldPtr(h, f, &kind);
+    if (!p) { g_lastError = "unknown field"; return MPSGPU_ERR_ARG; }
+    int n = 0;
+    int e = mpsgpu_num_particles(h, &n);
+    if (e) return e;
+    if (kind == 0) {
+        dvec4* v = (dvec4*)h->pinned;
+        const double* in = (const double*)host;
+        for (int i = 0; i < n; i++) v[i] = make_dvec4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0);
+        CK(cudaMemcpyAsync(p, v, sizeof(dvec4) * n, cudaMemcpyHostToDevice, h->s));
+    } else {
+        size_t sz = (kind == 1) ? sizeof(double) : sizeof(int);
+        std::memcpy(h->pinned, host, sz * n);
+        CK(cudaMemcpyAsync(p, h->pinned, sz * n, cudaMemcpyHostToDevice, h->s));
+    }
+    CK(cudaStreamSynchronize(h->s));
+    if (f == MPS_F_POS) h->listValid = false;
+    return 0;
+}
+
+int mpsgpu_get_neighbors(mpsgpu_t h, int* counts, int* nbr, long long cap) {
+    if (!h || !counts) return MPSGPU_ERR_ARG;
+    ensureList(h);
+    int e = checkDeviceErrors(h);
+    if (e) return e;
+    int n = 0;
+    if ((e = mpsgpu_num_particles(h, &n))) return e;
+    CK(cudaMemcpyAsync(counts, h->d.nbrCount, sizeof(int) * n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    if (!nbr) return 0;
+    std::vector<int> ell((size_t)h->d.K * h->N0);
+    CK(cudaMemcpyAsync(ell.data(), h->d.nbr, sizeof(int) * ell.size(), cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    long long k = 0;
+    for (int i = 0; i < n; i++)
+        for (int c = 0; c < counts[i]; c++) {
+            if (k >= cap) return MPSGPU_ERR_CAPACITY;
+            nbr[k++] = ell[(size_t)c * h->N0 + i];
+        }
+    return 0;
+}
+
+int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col, double* val, double* rhs) {
+    if (!h || !nnz_out) return MPSGPU_ERR_ARG;
+    if (h->d.P.mpsType != 2) return MPSGPU_ERR_UNSUPPORTED;
+    int n = 0;
+    int e = mpsgpu_num_particles(h, &n);
+    if (e) return e;
+    std::vector<int> len(n);
+    std::vector<double> diag(n);
+    CK(cudaMemcpyAsync(len.data(), h->B.rowLen, sizeof(int) * n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaMemcpyAsync(diag.data(), h->B.diag, sizeof(double) * n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    long long nnz = n;
+    for (int i = 0; i < n; i++) nnz += len[i];
+    *nnz_out = nnz;
+    if (!col) return 0;
+    size_t ellN = (size_t)h->d.K * h->N0;
+    std::vector<int> ec(ellN);
+    std::vector<double> ev(ellN);
+    CK(cudaMemcpyAsync(ec.data(), h->B.col, sizeof(int) * ellN, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaMemcpyAsync(ev.data(), h->B.val, sizeof(double) * ellN, cudaMemcpyDeviceToHost, h->s));
+    if (rhs) CK(cudaMemcpyAsync(rhs, h->B.b, sizeof(double) * n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    long long k = 0;
+    rowptr[0] = 0;
+    std::vector<std::pair<int, double>> row;
+    for (int i = 0; i < n; i++) {
+        row.clear();
+        row.push_back({i, diag[i]});
+        for (int c = 0; c < len[i]; c++) row.push_back({ec[(size_t)c * h->N0 + i], ev[(size_t)c * h->N0 + i]});
+        std::sort(row.begin(), row.end(), [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
+        for (auto& pr : row) { col[k] = pr.first; val[k] = pr.second; k++; }
+        rowptr[i + 1] = k;
+    }
+    return 0;
+}
+
+int mpsgpu_mlp_set_weights(mpsgpu_t h, const float* params, const float* norm32) {
+    if (!h || !params || !norm32) return MPSGPU_ERR_ARG;
+    return mlpSetWeights(h->mlp, params, norm32, h->s);
+}
+int mpsgpu_mlp_get_weights(mpsgpu_t h, float* params, float* norm32) {
+    if (!h || !params || !norm32) return MPSGPU_ERR_ARG;
+    return mlpGetWeights(h->mlp, params, norm32, h->s);
+}
+int mpsgpu_ppe_features(mpsgpu_t h, float* feat) {
+    if (!h || !feat) return MPSGPU_ERR_ARG;
+    if (h->d.P.mpsType != 2) return MPSGPU_ERR_UNSUPPORTED;
+    int n = 0;
+    int e = mpsgpu_num_particles(h, &n);
+    if (e) return e;
+    return mlpFeatures(h->mlp, h->d, h->B, feat, n, h->s);
+}
+
+int mpsgpu_mlp_record(mpsgpu_t h, int enable) {
+    if (!h) return MPSGPU_ERR_ARG;
+    if (h->d.P.mpsType != 2) return MPSGPU_ERR_UNSUPPORTED;
+    h->mlp.recording = enable != 0;
+    return 0;
+}
+int mpsgpu_mlp_num_records(mpsgpu_t h, long long* n) {
+    if (!h || !n) return MPSGPU_ERR_ARG;
+    *n = h->mlp.recCount;
+    return 0;
+}
+int mpsgpu_mlp_fit_normalization(mpsgpu_t h) {
+    if (!h) return MPSGPU_ERR_ARG;
+    return mlpFitNormalization(h->mlp, h->s);
+}
+int mpsgpu_mlp_train(mpsgpu_t h, int iters, int batch, float lr, unsigned long long seed, float* loss_hist) {
+    if (!h || iters <= 0) return MPSGPU_ERR_ARG;
+    return mlpTrain(h->mlp, iters, batch, lr, seed, loss_hist, h->s);
+}
+int mpsgpu_mlp_forward(mpsgpu_t h, const float* feat, int n, float* out) {
+    if (!h || !feat || !out || n <= 0) return MPSGPU_ERR_ARG;
+    return mlpForwardHost(h->mlp, feat, n, out, h->s);
+}
+int mpsgpu_mlp_gradient(mpsgpu_t h, const float* feat, const float* target, int n, float* grad, float* loss) {
+    if (!h || !feat || !target || !grad || !loss) return MPSGPU_ERR_ARG;
+    return mlpGradient(h->mlp, feat, target, n, grad, loss, h->s);
+}
+
+}  // extern "C"

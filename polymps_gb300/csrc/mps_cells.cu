@@ -1,0 +1,198 @@
+// mps_cells.cu — bucket list (MpsBucket::updateParticlesID, src/MpsBucket.cpp:299-353) as
+// a counting sort, and the ELL neighbour list of the current positions through that
+// stale list (the 27-bucket scan shared by every operator, e.g. src/MpsPndNeigh.cpp:209-258).
+//
+// Both are HBM/L2-latency bound integer work: one coalesced pass over the particles for
+// the bucket keys, atomics into the per-bucket counters, a device-wide scan, a scatter
+// and a per-bucket insertion sort that restores ascending particle order (the
+// reference's linked lists are filled in ascending index order).
+#include <atomic>
+#include "mps_common.cuh"
+#include "mps_internal.h"
+
+static std::atomic<long long> g_launches{0};
+void countLaunch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launchCount() { return g_launches.load(std::memory_order_relaxed); }
+
+// ------------------------------------------------------------------ bucket keys
+// 2D adds epsilonZero, 3D does not (src/MpsBucket.cpp:312-313 vs :333-335); ghosts skipped.
+__global__ void k_cell_key(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N0) return;
+    int n = liveN(d);
+    int key = -1;
+    if (i < n && d.type[i] != d.P.ghost) {
+        const MpsParams& P = d.P;
+        dvec4 p = d.pos[i];
+        int ix, iy, iz = 0;
+        if ((int)P.dim == 2) {
+            ix = (int)xadd(xmul(xsub(p.x, P.domainMin[0]), P.invBucketSide), P.epsilonZero);
+            iy = (int)xadd(xmul(xsub(p.y, P.domainMin[1]), P.invBucketSide), P.epsilonZero);
+        } else {
+            ix = (int)xmul(xsub(p.x, P.domainMin[0]), P.invBucketSide);
+            iy = (int)xmul(xsub(p.y, P.domainMin[1]), P.invBucketSide);
+            iz = (int)xmul(xsub(p.z, P.domainMin[2]), P.invBucketSide);
+        }
+        long long ib = (long long)iz * P.numBucketsXY + (long long)iy * P.numBucketsX + ix;
+        if (ib < 0 || ib >= d.nB) setErr(d, MPSE_DOMAIN);
+        else {
+            key = (int)ib;
+            atomicAdd(d.cellCount + key, 1);
+        }
+    }
+    d.cellOf[i] = key;
+}
+
+__global__ void k_cell_scatter(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N0) return;
+    int c = d.cellOf[i];
+    if (c < 0) return;
+    int slot = d.cellStart[c] + atomicAdd(d.cellCursor + c, 1);
+    d.cellSorted[slot] = i;
+}
+
+// Restore ascending particle order inside each bucket (buckets hold ~16 particles).
+__global__ void k_cell_sort(Dev d) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= d.nB) return;
+    int s0 = d.cellStart[c], s1 = d.cellStart[c + 1];
+    for (int a = s0 + 1; a < s1; a++) {
+        int v = d.cellSorted[a];
+        int b = a - 1;
+        while (b >= s0 && d.cellSorted[b] > v) { d.cellSorted[b + 1] = d.cellSorted[b]; b--; }
+        d.cellSorted[b + 1] = v;
+    }
+}
+
+// ------------------------------------------------------------------ exclusive scan
+// Three-phase block scan for int arrays (n <= 4096 * 4096).
+#define SCAN_BLOCK 1024
+#define SCAN_PER_THREAD 4
+#define SCAN_TILE (SCAN_BLOCK * SCAN_PER_THREAD)
+
+__device__ __forceinline__ int blockExclusiveScan(int v, int* smem, int& total) {
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) smem[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = (lane < (int)(blockDim.x >> 5)) ? smem[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        smem[lane] = w;
+    }
+    __syncthreads();
+    int warpPrefix = (warp > 0) ? smem[warp - 1] : 0;
+    total = smem[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warpPrefix + x - v;
+}
+
+__global__ void k_scan_tiles(const int* in, int* out, int* tileSums, int n) {
+    __shared__ int smem[32];
+    int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+    int v[SCAN_PER_THREAD];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_PER_THREAD; k++) {
+        v[k] = (base + k < n) ? in[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int pre = blockExclusiveScan(s, smem, total);
+#pragma unroll
+    for (int k = 0; k < SCAN_PER_THREAD; k++) {
+        if (base + k < n) out[base + k] = pre;
+        pre += v[k];
+    }
+    if (threadIdx.x == 0 && tileSums) tileSums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_add(int* out, const int* tileOffsets, int n, int* totalOut) {
+    int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+    int add = tileOffsets[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_PER_THREAD; k++)
+        if (base + k < n) out[base + k] += add;
+    (void)totalOut;
+}
+
+// out[0..n) = exclusive scan of in; out[n] = total.  scratch holds >= 2*tiles+2 ints.
+void scanExclusive(const int* in, int* out, int n, int* scratch, cudaStream_t s) {
+    int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    int* tileSums = scratch;
+    int* tileOffsets = scratch + tiles + 1;
+    k_scan_tiles<<<tiles, SCAN_BLOCK, 0, s>>>(in, out, tileSums, n);
+    // second level: one tile covers up to 4096 tiles
+    k_scan_tiles<<<1, SCAN_BLOCK, 0, s>>>(tileSums, tileOffsets, tileOffsets + tiles, tiles);
+    k_scan_add<<<tiles, SCAN_BLOCK, 0, s>>>(out, tileOffsets, n, nullptr);
+    // total = offset of last tile + its sum
+    cudaMemcpyAsync(out + n, tileOffsets + tiles, sizeof(int), cudaMemcpyDeviceToDevice, s);
+}
+int scanScratchInts(int n) { return 2 * ((n + SCAN_TILE - 1) / SCAN_TILE) + 4; }
+
+void launchBuckets(const Dev& d, int* scanScratch, cudaStream_t s) {
+    cudaMemsetAsync(d.cellCount, 0, sizeof(int) * (d.nB + 1), s);
+    cudaMemsetAsync(d.cellCursor, 0, sizeof(int) * (d.nB + 1), s);
+    k_cell_key<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    scanExclusive(d.cellCount, d.cellStart, d.nB, scanScratch, s);
+    k_cell_scatter<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    k_cell_sort<<<gridFor(d.nB, 256), 256, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ FP32 copy
+__global__ void k_posf(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    dvec4 p = d.pos[i];
+    d.posf[i] = make_float4((float)(p.x - d.P.domainMin[0]), (float)(p.y - d.P.domainMin[1]),
+                            (float)(p.z - d.P.domainMin[2]), 0.f);
+}
+
+// ------------------------------------------------------------------ neighbour list
+// Candidates are tested in FP32 first; only those whose FP32 squared distance falls in
+// the rounding band around reL^2 are re-tested in exact FP64, so membership equals the
+// reference's FP64 test dst^2 < reL^2 bit for bit while almost all work is FP32.
+__global__ void __launch_bounds__(128) k_build_nbr(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    dvec4 pi = d.pos[i];
+    float4 fi = d.posf[i];
+    const double reL2 = d.P.reL2;
+    int cnt = 0;
+    int* row = d.nbr + i;
+    forCells(d, pi, [&](int j) {
+        float4 fj = __ldg(&d.posf[j]);
+        float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
+        float d2f = dx * dx + dy * dy + dz * dz;
+        bool in;
+        if (d2f < d.bandLo) in = true;
+        else if (d2f > d.bandHi) in = false;
+        else {
+            dvec4 pj = d.pos[j];
+            in = pairOf(pj, pi).d2 < reL2;
+        }
+        if (in && j != i) {
+            if (cnt < d.K) row[(size_t)cnt * d.N0] = j;
+            cnt++;
+        }
+    });
+    if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }
+    d.nbrCount[i] = cnt;
+    warpCount(d.counters, (unsigned)cnt);
+}
+
+void launchNeighborList(const Dev& d, cudaStream_t s) {
+    cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long), s);
+    k_posf<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    k_build_nbr<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}

@@ -1,0 +1,211 @@
+// mps_common.cuh — device state and helpers shared by the sm_103a kernels of the
+// PolyMPS per-step particle path.
+//
+// Layout in HBM (all arrays sized for the initial particle count N0; the live count
+// lives in device memory at *nLive so removals never need a host round trip):
+//   * particle vectors as dvec4 (x, y, z, pad): one 32-byte sector per neighbour gather;
+//   * particle scalars as double / int arrays;
+//   * the stale bucket list of the step (MpsBucket::updateParticlesID) as a counting sort:
+//     cellStart[nB+1] offsets into cellSorted[], particles ascending within a bucket,
+//     so a scan of cellSorted visits them in the reference's linked-list order;
+//   * the neighbour list of the current positions in ELL form, column-major
+//     nbr[k * N0 + i] (coalesced across a warp), nbrCount[i] <= K.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/mpsgpu.h"
+
+// 32-byte aligned FP64 vector (x, y, z, pad): one sector, one wide load per gather.
+typedef double4_32a dvec4;
+__host__ __device__ __forceinline__ dvec4 make_dvec4(double x, double y, double z, double w) {
+    return make_double4_32a(x, y, z, w);
+}
+
+#define MPS_MAX_TRI 64
+#define MPS_TAB 50
+
+// Error bits OR-ed into Dev::err by kernels (read back by the host after each call).
+#define MPSE_CAPACITY   1u   // a neighbour row exceeded K
+#define MPSE_DOMAIN     2u   // a particle fell outside the bucket grid
+#define MPSE_NOTCONV    4u   // PPE iteration cap reached
+#define MPSE_NAN        8u   // non-finite value in a reduction
+
+struct Dev {
+    MpsParams P;
+    int N0;            // capacity
+    int* nLive;        // current numParticles (device)
+    int K;             // ELL row capacity
+    int nB;            // numBucketsXYZ
+    // particle vectors
+    dvec4 *pos, *vel, *acc, *accStar, *mirror, *wallPos, *polyNormal, *npcd, *gradC, *forceWall;
+    dvec4 *c1, *c2, *c3, *dvel, *shift;
+    // particle scalars
+    double *press, *pressPPE, *pndi, *pndki, *pndski, *pndSmall, *npcd2, *conc, *velDiv, *diffTerm;
+    double *pndWall, *riw2, *devDot, *source, *aux1, *aux2;
+    int *type, *bc, *numNeigh, *nNeighWall, *nearWall;
+    float4* posf;      // FP32 copy of pos - domainMin (neighbour prefilter, FP32 sums)
+    // buckets (stale list of the step)
+    int *cellOf, *cellStart, *cellCount, *cellSorted, *cellCursor;
+    // neighbour list (ELL)
+    int *nbrCount, *nbr;
+    // polygon mesh and wall tables
+    int ntri;
+    const double* tri;          // ntri * 9
+    const double* triNormal;    // ntri * 3
+    const double* tab;          // xPND[50], Z[50], xNeigh[50], nNeigh[50] (as double)
+    // prefilter band for the FP32 distance test (|d2f - reL2| <= band -> exact FP64)
+    float reL2f, bandLo, bandHi;
+    // scalars
+    double* velMax;    // device scalar (written by the corrector)
+    unsigned int* err; // error word
+    double* redScratch;
+    unsigned int* redCounter;
+    unsigned long long* counters;   // [0] neighbour entries, [1] PPE off-diagonal non-zeros
+};
+
+// Warp-aggregated add of v into *ctr (one atomic per warp).
+__device__ __forceinline__ void warpCount(unsigned long long* ctr, unsigned int v) {
+    unsigned int m = __activemask();
+    unsigned int s = __reduce_add_sync(m, v);   // valid for partial masks
+    int lane = threadIdx.x & 31;
+    if (lane == __ffs(m) - 1 && s) atomicAdd(ctr, (unsigned long long)s);
+}
+
+// ------------------------------------------------------------------ exact FP64
+// Products and sums that decide a discrete outcome (bucket index, neighbour membership,
+// mirror side, closest point) are evaluated with explicit round-to-nearest intrinsics
+// so that no FMA contraction changes their rounding relative to the CPU reference.
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double xdot3(double ax, double ay, double az, double bx, double by, double bz) {
+    return xadd(xadd(xmul(ax, bx), xmul(ay, by)), xmul(az, bz));
+}
+__device__ __forceinline__ double xnorm2(double x, double y, double z) { return xdot3(x, y, z, x, y, z); }
+
+// MpsBucket::bucketCoordinates, src/MpsBucket.cpp:420-425: (int)((x - min) * inv + eps)
+__device__ __forceinline__ void bucketCoords(const MpsParams& P, double x, double y, double z,
+                                             int& bx, int& by, int& bz) {
+    bx = (int)xadd(xmul(xsub(x, P.domainMin[0]), P.invBucketSide), P.epsilonZero);
+    by = (int)xadd(xmul(xsub(y, P.domainMin[1]), P.invBucketSide), P.epsilonZero);
+    bz = (int)xadd(xmul(xsub(z, P.domainMin[2]), P.invBucketSide), P.epsilonZero);
+}
+
+// ------------------------------------------------------------------ weights
+// MpsParticle::weight / delWeight, src/MpsParticle.cpp:57-108
+__device__ __forceinline__ double wfun(double dst, double re, int t) {
+    switch (t) {
+        case 1: return re / dst + dst / re - 2.0;
+        case 2: return re / dst - dst / re;
+        case 3: { double a = 1.0 - dst / re; return a * a * a; }
+        case 4: { double a = 1.0 - dst / re; return a * a; }
+        default: return re / dst - 1.0;
+    }
+}
+__device__ __forceinline__ double dwfun(double dst, double re, int t) {
+    switch (t) {
+        case 1: return -re / (dst * dst) + 1.0 / re;
+        case 2: return -re / (dst * dst) - 1.0 / re;
+        case 3: { double a = 1.0 - dst / re; return -3.0 / re * a * a; }
+        case 4: return -2.0 / re * (1.0 - dst / re);
+        default: return -re / (dst * dst);
+    }
+}
+
+// ------------------------------------------------------------------ pairs
+struct PairG {
+    double v0, v1, v2, d2;   // r_ij = x_j - x_i and |r_ij|^2 (exact)
+};
+__device__ __forceinline__ PairG pairOf(dvec4 pj, dvec4 pi) {
+    PairG q;
+    q.v0 = xsub(pj.x, pi.x); q.v1 = xsub(pj.y, pi.y); q.v2 = xsub(pj.z, pi.z);
+    q.d2 = xnorm2(q.v0, q.v1, q.v2);
+    return q;
+}
+struct PairM {
+    double m0, m1, m2, dm2;  // x_j - x_mirror(i) and its squared norm (exact)
+};
+__device__ __forceinline__ PairM pairMirror(dvec4 pj, dvec4 mi) {
+    PairM q;
+    q.m0 = xsub(pj.x, mi.x); q.m1 = xsub(pj.y, mi.y); q.m2 = xsub(pj.z, mi.z);
+    q.dm2 = xnorm2(q.m0, q.m1, q.m2);
+    return q;
+}
+
+// Per-particle context for the "j is not on the mirror side" test of every sweep
+// (dstij2 < dstimj2 || wallType == PARTICLE, e.g. src/MpsPndNeigh.cpp:249).  When the
+// mirror of i lies farther than 2.2 reL from i, every j within reL of i satisfies
+// |x_j - m_i| >= |x_i - m_i| - r_ij > r_ij + 0.2 reL, so the test is skipped exactly.
+struct SideCtx {
+    dvec4 mi;
+    bool check;
+};
+__device__ __forceinline__ SideCtx sideCtx(const Dev& d, int i, dvec4 pi) {
+    SideCtx s;
+    s.mi = d.mirror[i];
+    if (d.P.wallType == 0) { s.check = false; return s; }
+    double a = pi.x - s.mi.x, b = pi.y - s.mi.y, c = pi.z - s.mi.z;
+    double lim = 2.2 * d.P.reL;
+    s.check = (a * a + b * b + c * c) <= lim * lim;
+    return s;
+}
+__device__ __forceinline__ bool sideOK(const SideCtx& s, dvec4 pj, double d2) {
+    if (!s.check) return true;
+    PairM m = pairMirror(pj, s.mi);
+    return d2 < m.dm2;
+}
+
+__device__ __forceinline__ int liveN(const Dev& d) { return *d.nLive; }
+
+// Iterate the ELL neighbour row of i (scan order of the reference).
+template <class F>
+__device__ __forceinline__ void forNbrs(const Dev& d, int i, F&& f) {
+    int c = d.nbrCount[i];
+    const int* row = d.nbr + i;
+    for (int k = 0; k < c; k++) f(__ldg(row + (size_t)k * d.N0));
+}
+
+// Iterate the 27 (9 in 2D) buckets around x (bucketCoordinates of x) in the reference
+// order, over the stale bucket list; out-of-grid bucket indices are skipped.
+template <class F>
+__device__ __forceinline__ void forCells(const Dev& d, dvec4 x, F&& f) {
+    const MpsParams& P = d.P;
+    int ix, iy, iz;
+    bucketCoords(P, x.x, x.y, x.z, ix, iy, iz);
+    int dz = (int)(P.dim - 2.0);
+    int minZ = (iz - 1) * dz, maxZ = (iz + 1) * dz;
+    for (int jz = minZ; jz <= maxZ; jz++)
+        for (int jy = iy - 1; jy <= iy + 1; jy++)
+            for (int jx = ix - 1; jx <= ix + 1; jx++) {
+                long long jb = (long long)jz * P.numBucketsXY + (long long)jy * P.numBucketsX + jx;
+                if (jb < 0 || jb >= d.nB) continue;
+                int s0 = d.cellStart[jb], s1 = d.cellStart[jb + 1];
+                for (int s = s0; s < s1; s++) f(__ldg(d.cellSorted + s));
+            }
+}
+
+__device__ __forceinline__ void setErr(const Dev& d, unsigned int bit) { atomicOr(d.err, bit); }
+
+// Reflection about the wall plane of i: n = (x_i - m_i)/2 normalised, R = I - 2 n n^T.
+// useSqrt selects the normaliwSqrt > eps variant (src/MpsPndNeigh.cpp:118-131) or the
+// normalMod2 > eps variant (src/MpsViscosity.cpp:1544-1556).
+struct ReflG {
+    double n[3], nsqrt, R[9];
+};
+__device__ __forceinline__ ReflG makeRefl(dvec4 xi, dvec4 mi, double eps, bool useSqrt) {
+    ReflG r;
+    r.n[0] = 0.5 * (xi.x - mi.x); r.n[1] = 0.5 * (xi.y - mi.y); r.n[2] = 0.5 * (xi.z - mi.z);
+    double m2 = r.n[0] * r.n[0] + r.n[1] * r.n[1] + r.n[2] * r.n[2];
+    double m = sqrt(m2);
+    bool ok = useSqrt ? (m > eps) : (m2 > eps);
+    r.nsqrt = useSqrt ? m : (ok ? m : 0.0);
+    if (ok) { r.n[0] /= m; r.n[1] /= m; r.n[2] /= m; }
+    else { r.n[0] = r.n[1] = r.n[2] = 0.0; }
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) r.R[a * 3 + b] = (a == b ? 1.0 : 0.0) - 2.0 * r.n[a] * r.n[b];
+    return r;
+}
+
+static inline int gridFor(int n, int block) { return (n + block - 1) / block; }

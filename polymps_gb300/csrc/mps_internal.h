@@ -1,0 +1,81 @@
+// mps_internal.h — launch wrappers shared between the translation units of libmpsgpu.
+#pragma once
+#include <cuda_runtime.h>
+#include <vector>
+#include "mps_common.cuh"
+
+// Kernel-launch counter (all launches of this library, process-wide).
+void countLaunch(int n);
+long long launchCount();
+
+// Per-class device timing with CUDA events on the handle's stream.  Classes 0..MPS_OP_COUNT-1
+// are the operators; the extra classes split the pressure solve.
+enum {
+    PROF_NEIGHBOR_LIST = MPS_OP_COUNT, PROF_PPE_ASSEMBLE, PROF_PPE_SPMV, PROF_PPE_VECTOR,
+    PROF_PPE_OTHER, PROF_NCLASS
+};
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> ev;      // pairs
+    std::vector<int> cls;
+    std::vector<size_t> open;         // slots begun and not yet ended
+    size_t used = 0;
+    double ms[PROF_NCLASS] = {0};
+    long long calls[PROF_NCLASS] = {0};
+    void begin(int c, cudaStream_t s);
+    void end(cudaStream_t s);
+    int flush();                      // synchronises on the last event, accumulates
+    void reset();
+    void destroy();
+};
+
+// mps_cells.cu
+void scanExclusive(const int* in, int* out, int n, int* scratch, cudaStream_t s);
+int scanScratchInts(int n);
+void launchBuckets(const Dev& d, int* scanScratch, cudaStream_t s);
+void launchNeighborList(const Dev& d, cudaStream_t s);
+
+// mps_ops.cu
+void launchViscosity(const Dev& d, cudaStream_t s);
+void launchAddGravity(const Dev& d, cudaStream_t s);
+void launchPredict(const Dev& d, cudaStream_t s);
+void launchOutOfDomain(const Dev& d, int* flags, int* counter, cudaStream_t s);
+void launchCollision(const Dev& d, cudaStream_t s);
+void launchWallNpcd(const Dev& d, cudaStream_t s);
+void launchCorrectionMatrix(const Dev& d, cudaStream_t s);
+void launchPndNeighNpcd(const Dev& d, cudaStream_t s);
+void launchPndDiffusive(const Dev& d, cudaStream_t s);
+void launchPndMean(const Dev& d, cudaStream_t s);
+void launchInitPnd(const Dev& d, cudaStream_t s);
+void launchUpdateBC(const Dev& d, cudaStream_t s);
+void launchEOS(const Dev& d, cudaStream_t s);
+void launchExtrapolatePress(const Dev& d, cudaStream_t s);
+void launchPressGradient(const Dev& d, cudaStream_t s);
+void launchWallPressGradient(const Dev& d, cudaStream_t s);
+void launchWallViscosity(const Dev& d, cudaStream_t s);
+void launchCorrect(const Dev& d, cudaStream_t s);
+void launchShifting(const Dev& d, cudaStream_t s);
+void launchDummyVelocity(const Dev& d, cudaStream_t s);
+
+// mps_wall.cu
+void launchWallDistance(const Dev& d, cudaStream_t s);
+
+// mps_ppe.cu
+struct PpeBuffers {
+    int N0, K;
+    double *diag, *val, *x, *b, *r, *z, *p, *Ap, *scal;  // scal: solver scalars (device)
+    int* col;
+    int* rowLen;
+    float *valf, *diagf, *diagInvf, *rf, *zf, *pf, *Apf, *xf;  // mixed-precision copies
+    double* partials;
+    unsigned int* counter;
+    int* flag;       // [0] = done, [1] = iterations
+    int nblocks;
+};
+void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
+void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);
+// Returns iterations and final relative residual through host pointers (synchronises).
+int ppeSolvePlain(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cudaStream_t s,
+                  int* iters, double* relres, double* relres0, Prof* prof);
+int ppeSolveMixed(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cudaStream_t s,
+                  int* iters, int* refinements, double* relres, double* relres0, Prof* prof);

@@ -1,0 +1,1003 @@
+// mps_ops.cu — the per-particle operators of the PolyMPS step on sm_103a.
+//
+// One thread per particle i.  Sweeps at the post-prediction positions walk the ELL
+// neighbour row of i (built once per position epoch through the stale bucket list, in
+// the reference's scan order); the start-of-step viscosity and the post-correction
+// shifting/dummy sweeps, which see their positions once, walk the 27 buckets directly.
+// Every sweep applies the reference's own radius and mirror-side tests to each entry,
+// with the distance comparisons evaluated in exact FP64 (see mps_common.cuh).
+#include "mps_common.cuh"
+#include "mps_internal.h"
+
+#define BLK 128
+
+// ------------------------------------------------------------------ viscosity
+// MpsViscosity::calcViscosity, src/MpsViscosity.cpp:20-100 (Newtonian: MEU and RHO are
+// uniform, src/MpsInputOutput.cpp:833-838, so the harmonic mean is hoisted).
+__global__ void __launch_bounds__(BLK) k_viscosity(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    double mu = P.KNM_VS1 * P.DNS_FL1, rho = P.DNS_FL1;
+    double neuF = (2.0 * mu * mu / (mu + mu)) / rho;
+    double neuW = (2.0 * mu) / rho;
+    dvec4 pi = d.pos[i], vi = d.vel[i];
+    SideCtx sc = sideCtx(d, i, pi);
+    double ax = 0, ay = 0, az = 0;
+    forCells(d, pi, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reL2 && j != i && sideOK(sc, pj, q.d2)) {
+            double wL = wfun(sqrt(q.d2), P.reL, P.weightType);
+            double neu = (d.type[j] == P.wall) ? neuW : neuF;
+            dvec4 vj = d.vel[j];
+            ax += (vj.x - vi.x) * wL * neu;
+            ay += (vj.y - vi.y) * wL * neu;
+            az += (vj.z - vi.z) * wL * neu;
+        }
+    });
+    d.acc[i] = make_dvec4(P.coeffViscMultiphase * ax, P.coeffViscMultiphase * ay,
+                            P.coeffViscMultiphase * az, 0.0);
+}
+void launchViscosity(const Dev& d, cudaStream_t s) { k_viscosity<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
+
+// MpsParticle::addGravity, src/MpsParticle.cpp:111-130
+__global__ void k_add_gravity(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    dvec4 a = d.acc[i];
+    a.x += d.P.gravity[0]; a.y += d.P.gravity[1]; a.z += d.P.gravity[2];
+    d.acc[i] = a;
+    d.accStar[i] = a;
+}
+void launchAddGravity(const Dev& d, cudaStream_t s) { k_add_gravity<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
+
+// MpsParticleVelPos::predictionVelocityPosition, src/MpsParticleVelPos.cpp:20-50
+__global__ void k_predict(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    if (d.type[i] == P.fluid) {
+        dvec4 v = d.vel[i], a = d.acc[i], x = d.pos[i];
+        v.x += a.x * P.timeStep; v.y += a.y * P.timeStep; v.z += a.z * P.timeStep;
+        x.x += v.x * P.timeStep; x.y += v.y * P.timeStep; x.z += v.z * P.timeStep;
+        d.vel[i] = v; d.pos[i] = x;
+    }
+    dvec4 z = make_dvec4(0, 0, 0, 0);
+    d.acc[i] = z; d.dvel[i] = z; d.npcd[i] = z;
+    d.nNeighWall[i] = 0;
+    d.nearWall[i] = 0;
+    double big = 10e8 * P.partDist;
+    d.riw2[i] = big;
+    if (P.wallType == 1) d.mirror[i] = make_dvec4(big, big, big, 0.0);
+}
+void launchPredict(const Dev& d, cudaStream_t s) { k_predict<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
+
+// ------------------------------------------------------------------ out of domain
+// MpsParticle::checkParticleOutDomain, src/MpsParticle.cpp:270-396.  A parallel pass flags
+// fluid particles outside [min + bucket, max - bucket]; when any is flagged, a single
+// thread replays the reference's serial swap-with-last loop over the flagged slots in
+// ascending order (untouched slots keep valid flags: a swap only writes the current slot
+// and the last live slot, which leaves the loop range).
+__device__ __forceinline__ bool outside(const Dev& d, dvec4 p) {
+    const MpsParams& P = d.P;
+    double b = P.bucketSide;
+    return p.x > P.domainMax[0] - b || p.x < P.domainMin[0] + b || p.y > P.domainMax[1] - b ||
+           p.y < P.domainMin[1] + b || (P.dim == 3 && (p.z > P.domainMax[2] - b || p.z < P.domainMin[2] + b));
+}
+__global__ void k_out_flag(Dev d, int* flags, int* counter) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = liveN(d);
+    int f = 0;
+    if (i < n && d.type[i] == d.P.fluid && outside(d, d.pos[i])) f = 1;
+    if (i < d.N0) flags[i] = f;
+    if (f) atomicAdd(counter, 1);
+}
+template <class T> __device__ __forceinline__ void mv(T* a, int i, int L) { a[i] = a[L]; }
+__global__ void k_out_serial(Dev d, const int* flags, int* counter) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (*counter == 0) return;
+    const MpsParams& P = d.P;
+    int newN = *d.nLive;
+    int removed = 0;
+    for (int i = 0; i < newN; i++) {
+        if (!flags[i]) continue;
+        int L = newN - 1;
+        mv(d.type, i, L); mv(d.bc, i, L); mv(d.numNeigh, i, L); mv(d.press, i, L); mv(d.pndi, i, L);
+        mv(d.pndki, i, L); mv(d.pndski, i, L); mv(d.pndSmall, i, L); mv(d.npcd2, i, L); mv(d.conc, i, L);
+        mv(d.velDiv, i, L); mv(d.diffTerm, i, L); mv(d.nearWall, i, L); mv(d.nNeighWall, i, L);
+        mv(d.pndWall, i, L); mv(d.devDot, i, L); mv(d.riw2, i, L);
+        if (P.mpsType == 2 || P.mpsType == 3) { mv(d.pressPPE, i, L); mv(d.source, i, L); }
+        mv(d.acc, i, L); mv(d.accStar, i, L); mv(d.pos, i, L); mv(d.vel, i, L); mv(d.npcd, i, L);
+        mv(d.gradC, i, L); mv(d.c1, i, L); mv(d.c2, i, L); mv(d.c3, i, L); mv(d.dvel, i, L);
+        mv(d.wallPos, i, L); mv(d.mirror, i, L); mv(d.polyNormal, i, L); mv(d.forceWall, i, L);
+        d.type[L] = P.ghost; d.bc[L] = P.other; d.nearWall[L] = 0; d.riw2[L] = 10e8 * P.partDist;
+        d.vel[L] = make_dvec4(0, 0, 0, 0);
+        d.press[L] = 0.0;
+        d.pos[L] = make_dvec4(P.domainMax[0] - P.partDist, P.domainMax[1] - P.partDist,
+                                (P.dim == 2) ? 0.0 : P.domainMax[2] - P.partDist, 0.0);
+        newN--;
+        removed++;
+    }
+    *d.nLive = newN;
+    *counter = removed;
+}
+void launchOutOfDomain(const Dev& d, int* flags, int* counter, cudaStream_t s) {
+    cudaMemsetAsync(counter, 0, sizeof(int), s);
+    k_out_flag<<<gridFor(d.N0, 256), 256, 0, s>>>(d, flags, counter);
+    k_out_serial<<<1, 32, 0, s>>>(d, flags, counter);
+}
+
+// ------------------------------------------------------------------ collision
+// MpsParticleCollision::checkParticleCollisions (PC), src/MpsParticleCollision.cpp:22-119:
+// velocity corrections computed from the pre-collision velocities, then applied.
+__global__ void __launch_bounds__(BLK) k_collision(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 dv = make_dvec4(0, 0, 0, 0);
+    if (d.type[i] == P.fluid) {
+        double mi = P.DNS_FL1;  // PTYPE == 1 for every Newtonian particle
+        dvec4 pi = d.pos[i], vi = d.vel[i];
+        SideCtx sc = sideCtx(d, i, pi);
+        forNbrs(d, i, [&](int j) {
+            dvec4 pj = d.pos[j];
+            PairG q = pairOf(pj, pi);
+            if (q.d2 < P.distCollisionLimit2 && sideOK(sc, pj, q.d2)) {
+                dvec4 vj = d.vel[j];
+                double fDT = (vi.x - vj.x) * q.v0 + (vi.y - vj.y) * q.v1 + (vi.z - vj.z) * q.v2;
+                if (fDT > 0.0) {
+                    bool jf = d.type[j] == P.fluid;
+                    double mj = jf ? P.DNS_FL1 : P.densityWall;
+                    fDT *= P.restitutionCollision * mj / (mi + mj) / q.d2;
+                    double f = jf ? 1.0 : 2.0;
+                    dv.x -= f * q.v0 * fDT; dv.y -= f * q.v1 * fDT; dv.z -= f * q.v2 * fDT;
+                }
+            }
+        });
+    }
+    d.dvel[i] = dv;
+}
+__global__ void k_collision_apply(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    if (d.type[i] == d.P.fluid) {
+        dvec4 v = d.vel[i], dv = d.dvel[i];
+        v.x += dv.x; v.y += dv.y; v.z += dv.z;
+        d.vel[i] = v;
+    }
+    d.dvel[i] = make_dvec4(0, 0, 0, 0);
+}
+void launchCollision(const Dev& d, cudaStream_t s) {
+    k_collision<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    k_collision_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ wall NPCD
+// MpsPndNeigh::calcWallNPCD, src/MpsPndNeigh.cpp:105-195
+__global__ void __launch_bounds__(BLK) k_wall_npcd(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    if (!(d.type[i] == P.fluid && d.nearWall[i])) return;
+    dvec4 pi = d.pos[i], mi = d.mirror[i];
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
+    double dx = 0, dy = 0, dz = 0;
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2) {
+            PairM m = pairMirror(pj, mi);
+            if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
+                double wS = wfun(sqrt(m.dm2), P.reS, P.weightType);
+                dx += m.m0 * wS; dy += m.m1 * wS; dz += m.m2 * wS;
+            }
+        }
+    });
+    PairM s = pairMirror(pi, mi);
+    if (s.dm2 < P.reS2) {
+        double wS = wfun(sqrt(s.dm2), P.reS, P.weightType);
+        dx += s.m0 * wS; dy += s.m1 * wS; dz += s.m2 * wS;
+    }
+    dvec4 n = d.npcd[i];
+    n.x += r.R[0] * dx + r.R[1] * dy + r.R[2] * dz;
+    n.y += r.R[3] * dx + r.R[4] * dy + r.R[5] * dz;
+    n.z += r.R[6] * dx + r.R[7] * dy + r.R[8] * dz;
+    d.npcd[i] = n;
+}
+void launchWallNpcd(const Dev& d, cudaStream_t s) {
+    if (d.P.wallType != 1) return;
+    k_wall_npcd<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ correction matrix
+// MpsVectorMatrix::correctionMatrix + inverseMatrix (Gauss-Jordan without pivoting,
+// identity when det <= eps or numNeigh < 4), src/MpsVectorMatrix.cpp:20-166
+__device__ void invert3(double* m, int dim, double eps) {
+    double A[9], M[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) { A[k] = m[k]; M[k] = (k % 4 == 0) ? 1.0 : 0.0; }
+    if (dim == 2) { A[2] = A[5] = A[6] = A[7] = 0.0; A[8] = 1.0; }
+    double det = (A[0] * A[4] * A[8] + A[1] * A[5] * A[6] + A[2] * A[3] * A[7]) -
+                 (A[2] * A[4] * A[6] + A[1] * A[3] * A[8] + A[0] * A[5] * A[7]);
+    if (det <= eps) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) m[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        return;
+    }
+    for (int k = 0; k < dim; k++)
+        for (int r = 0; r < dim; r++) {
+            if (r == k) continue;
+            double f = A[r * 3 + k] / A[k * 3 + k];
+            for (int c = 0; c < dim; c++) { A[r * 3 + c] -= f * A[k * 3 + c]; M[r * 3 + c] -= f * M[k * 3 + c]; }
+        }
+    for (int r = 0; r < dim; r++)
+        for (int c = 0; c < dim; c++) M[r * 3 + c] /= A[r * 3 + r];
+#pragma unroll
+    for (int k = 0; k < 9; k++) m[k] = M[k];
+}
+__global__ void __launch_bounds__(BLK) k_corr_matrix(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    SideCtx sc = sideCtx(d, i, pi);
+    double m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
+            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+            double inv = 1.0 / q.d2;
+            double v[3] = {q.v0, q.v1, q.v2};
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+                for (int b = 0; b < 3; b++) m[a * 3 + b] += wS * v[a] * v[b] * inv;
+        }
+    });
+#pragma unroll
+    for (int k = 0; k < 9; k++) m[k] *= -P.coeffPressGrad;
+    invert3(m, (int)P.dim, P.epsilonZero);
+    if (d.numNeigh[i] < 4) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) m[k] = (k % 4 == 0) ? 1.0 : 0.0;
+    }
+    d.c1[i] = make_dvec4(m[0], m[1], m[2], 0.0);
+    d.c2[i] = make_dvec4(m[3], m[4], m[5], 0.0);
+    d.c3[i] = make_dvec4(m[6], m[7], m[8], 0.0);
+}
+void launchCorrectionMatrix(const Dev& d, cudaStream_t s) { k_corr_matrix<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
+
+// ------------------------------------------------------------------ PND / NPCD
+// MpsPndNeigh::calcPndnNeighNPCD, src/MpsPndNeigh.cpp:199-331 (init == 0), and
+// setInitialPndNumberOfNeighNPCD, src/MpsPndNeigh.cpp:21-101 (init == 1)
+template <int INIT>
+__global__ void __launch_bounds__(BLK) k_pnd_npcd(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    SideCtx sc = sideCtx(d, i, pi);
+    double ni = 0.0, wSum = 0.0;
+    int nn = INIT ? 0 : d.nNeighWall[i];
+    dvec4 np = INIT ? make_dvec4(0, 0, 0, 0) : d.npcd[i];
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reL2 && sideOK(sc, pj, q.d2)) {
+            nn += 1;
+            if (q.d2 < P.reS2) {
+                double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+                ni += wS;
+                np.x += q.v0 * wS; np.y += q.v1 * wS; np.z += q.v2 * wS;
+                wSum += wS;
+            }
+        }
+    });
+    double pndSmall;
+    if (INIT) {
+        double pn = d.pndi[i] + ni;     // pndi accumulates onto its initial value
+        pn += d.pndWall[i];
+        if (d.type[i] == P.wall) pn = P.pndSmallZero;
+        d.pndi[i] = pn;
+        d.pndki[i] = pn;
+        pndSmall = pn;
+        nn += d.nNeighWall[i];
+    } else {
+        if (P.pndType == 0 || P.pndType == 1) {
+            d.pndki[i] = d.pndi[i];
+            d.pndi[i] = ni + d.pndWall[i];
+        }
+        pndSmall = ni + d.pndWall[i];
+    }
+    d.pndSmall[i] = pndSmall;
+    d.numNeigh[i] = nn;
+    if (wSum > P.epsilonZero) { np.x /= pndSmall; np.y /= pndSmall; np.z /= pndSmall; }
+    d.npcd[i] = np;
+    d.npcd2[i] = np.x * np.x + np.y * np.y + np.z * np.z;
+    dvec4 nw = d.polyNormal[i];
+    d.devDot[i] = (np.x * nw.x + np.y * nw.y + np.z * nw.z < 0.0) ? 1.0 : -1.0;
+}
+void launchPndNeighNpcd(const Dev& d, cudaStream_t s) { k_pnd_npcd<0><<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
+
+// ------------------------------------------------------------------ diffusive PND (pnd type 2)
+// MpsPndNeigh::calcPndDiffusiveTerm, src/MpsPndNeigh.cpp:334-489
+__global__ void __launch_bounds__(BLK) k_pnd_diffusive(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    double ni = d.pndi[i];
+    if (ni < P.epsilonZero) return;
+    dvec4 pi = d.pos[i], vi = d.vel[i];
+    SideCtx sc = sideCtx(d, i, pi);
+    dvec4 C1 = d.c1[i], C2 = d.c2[i], C3 = d.c3[i];
+    double Pi = d.press[i];
+    double rho = P.DNS_FL1;
+    bool fi = d.type[i] == P.fluid;
+    double Di = 0.0, DivV = 0.0;
+    double cdiv = P.dim / P.pndSmallZero;
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reL2 && sideOK(sc, pj, q.d2)) {
+            double dst = sqrt(q.d2);
+            double wL = wfun(dst, P.reL, P.weightType);
+            if (fi && d.type[j] == P.fluid) {
+                double pgh = -2.0 * (rho * rho / (rho + rho)) *
+                             (P.gravity[0] * q.v0 + P.gravity[1] * q.v1 + P.gravity[2] * q.v2);
+                Di += P.timeStep / rho * P.coeffViscMultiphase * (d.press[j] - Pi - pgh) * wL;
+            }
+            if (q.d2 < P.reS2) {
+                dvec4 vj = d.vel[j];
+                double vx = vj.x - vi.x, vy = vj.y - vi.y, vz = vj.z - vi.z;
+                double wS = wfun(dst, P.reS, P.weightType);
+                if (!P.gradientCorrection) {
+                    DivV += cdiv * (d.pndi[j] / ni) * (vx * q.v0 + vy * q.v1 + vz * q.v2) * wS / q.d2;
+                } else {
+                    double a0 = q.v0 * C1.x + q.v1 * C1.y + q.v2 * C1.z;
+                    double a1 = q.v0 * C2.x + q.v1 * C2.y + q.v2 * C2.z;
+                    double a2 = q.v0 * C3.x + q.v1 * C3.y + q.v2 * C3.z;
+                    DivV += cdiv * (vx * a0 + vy * a1 + vz * a2) * wS / q.d2;
+                }
+            }
+        }
+    });
+    d.aux1[i] = d.pndi[i] * (1.0 + P.timeStep * (-DivV + Di * 1.0));
+    d.velDiv[i] = DivV;
+    d.diffTerm[i] = Di;
+}
+
+// MpsPndNeigh::calcWallSlipPndDiffusiveTerm / calcWallNoSlipPndDiffusiveTerm,
+// src/MpsPndNeigh.cpp:492-744 (fixed wall: wall velocity zero)
+__global__ void __launch_bounds__(BLK) k_wall_pnd_diffusive(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    double ni = d.pndi[i];
+    if (!(d.type[i] == P.fluid && d.nearWall[i] && ni > P.epsilonZero)) return;
+    bool noslip = P.slipCondition == 0;
+    dvec4 pi = d.pos[i], vi = d.vel[i], mi = d.mirror[i];
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, false);
+    double vm[3];
+    if (noslip) { vm[0] = -vi.x; vm[1] = -vi.y; vm[2] = -vi.z; }
+    else {
+        vm[0] = r.R[0] * vi.x + r.R[1] * vi.y + r.R[2] * vi.z;
+        vm[1] = r.R[3] * vi.x + r.R[4] * vi.y + r.R[5] * vi.z;
+        vm[2] = r.R[6] * vi.x + r.R[7] * vi.y + r.R[8] * vi.z;
+    }
+    double cdiv = P.dim / P.pndSmallZero;
+    double DivV = 0.0;
+    auto term = [&](double vx, double vy, double vz, double m0, double m1, double m2, double dm2, double pj) {
+        double wS = wfun(sqrt(dm2), P.reS, P.weightType);
+        if (noslip) {
+            vx = -vx; vy = -vy; vz = -vz;
+            double a0 = r.R[0] * m0 + r.R[1] * m1 + r.R[2] * m2;
+            double a1 = r.R[3] * m0 + r.R[4] * m1 + r.R[5] * m2;
+            double a2 = r.R[6] * m0 + r.R[7] * m1 + r.R[8] * m2;
+            return cdiv * (pj / ni) * (vx * a0 + vy * a1 + vz * a2) * wS / dm2;
+        }
+        return cdiv * (pj / ni) * (vx * m0 + vy * m1 + vz * m2) * wS / dm2;
+    };
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2) {
+            PairM m = pairMirror(pj, mi);
+            if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
+                dvec4 vj = d.vel[j];
+                DivV += term(vj.x - vm[0], vj.y - vm[1], vj.z - vm[2], m.m0, m.m1, m.m2, m.dm2, d.pndi[j]);
+            }
+        }
+    });
+    PairM s = pairMirror(pi, mi);
+    if (s.dm2 < P.reS2) DivV += term(vi.x - vm[0], vi.y - vm[1], vi.z - vm[2], s.m0, s.m1, s.m2, s.dm2, ni);
+    d.aux1[i] += -ni * P.timeStep * DivV;
+}
+
+// MpsPndNeigh::updatePnd, src/MpsPndNeigh.cpp:747-774
+__global__ void k_update_pnd(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    d.pndi[i] = d.aux1[i];
+    d.aux1[i] = 0.0;
+}
+
+// MpsPndNeigh::meanPndParticlesWallDummySurface, src/MpsPndNeigh.cpp:777-852
+__global__ void __launch_bounds__(BLK) k_mean_pnd_wds(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    double up = 0.0, dn = 0.0;
+    if (d.type[i] == P.wall || d.bc[i] == P.surface) {
+        dvec4 pi = d.pos[i];
+        SideCtx sc = sideCtx(d, i, pi);
+        forNbrs(d, i, [&](int j) {
+            dvec4 pj = d.pos[j];
+            PairG q = pairOf(pj, pi);
+            if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
+                double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+                up += d.pndi[j] * wS; dn += wS;
+            }
+        });
+    }
+    d.aux1[i] = up; d.aux2[i] = dn;
+}
+__global__ void k_mean_pnd_wds_apply(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    if (d.type[i] == P.wall || d.bc[i] == P.surface) {
+        double a1 = d.aux1[i], a2 = d.aux2[i];
+        d.pndi[i] = (a2 < P.epsilonZero) ? a1 : a1 / a2;
+    }
+    d.aux1[i] = 0.0; d.aux2[i] = 0.0;
+}
+
+void launchPndDiffusive(const Dev& d, cudaStream_t s) {
+    k_pnd_diffusive<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    if (d.P.wallType == 1) k_wall_pnd_diffusive<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    k_update_pnd<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    k_mean_pnd_wds<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    k_mean_pnd_wds_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ mean PND (pnd type 1 and init)
+// MpsPndNeigh::meanWallPnd, src/MpsPndNeigh.cpp:923-994 (sets aux1/aux2)
+__global__ void __launch_bounds__(BLK) k_mean_wall_pnd(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    double up = 0.0, dn = 0.0;
+    if (d.nearWall[i]) {
+        dvec4 pi = d.pos[i], mi = d.mirror[i];
+        forNbrs(d, i, [&](int j) {
+            dvec4 pj = d.pos[j];
+            PairG q = pairOf(pj, pi);
+            if (q.d2 < P.reS2) {
+                PairM m = pairMirror(pj, mi);
+                if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
+                    double wS = wfun(sqrt(m.dm2), P.reS, P.weightType);
+                    up += d.pndi[j] * wS; dn += wS;
+                }
+            }
+        });
+        PairM s = pairMirror(pi, mi);
+        if (s.dm2 < P.reS2) {
+            double wS = wfun(sqrt(s.dm2), P.reS, P.weightType);
+            up += d.pndi[i] * wS; dn += wS;
+        }
+    }
+    d.aux1[i] = up; d.aux2[i] = dn;
+}
+// MpsPndNeigh::meanPnd, src/MpsPndNeigh.cpp:855-920 (adds onto aux1/aux2, then divides)
+__global__ void __launch_bounds__(BLK) k_mean_pnd(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    SideCtx sc = sideCtx(d, i, pi);
+    double up = 0.0, dn = 0.0;
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
+            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+            up += d.pndi[j] * wS; dn += wS;
+        }
+    });
+    d.aux1[i] += up; d.aux2[i] += dn;
+}
+__global__ void k_mean_pnd_apply(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    double a1 = d.aux1[i], a2 = d.aux2[i];
+    d.pndi[i] = (d.numNeigh[i] < 1) ? a1 : a1 / a2;
+    d.aux1[i] = 0.0; d.aux2[i] = 0.0;
+}
+// MpsPndNeigh::meanNeighFluidPnd, src/MpsPndNeigh.cpp:997-1050
+__global__ void __launch_bounds__(BLK) k_mean_neigh_fluid_pnd(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    SideCtx sc = sideCtx(d, i, pi);
+    double up = 0.0, dn = 0.0;
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2) && d.type[j] == P.fluid) {
+            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+            up += d.pndki[j] * wS; dn += wS;
+        }
+    });
+    d.pndski[i] = (dn > P.epsilonZero) ? up / dn : up;
+}
+void launchPndMean(const Dev& d, cudaStream_t s) {
+    if (d.P.wallType == 1) k_mean_wall_pnd<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    k_mean_pnd<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    k_mean_pnd_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+}
+// step-0 sequence, src/main.cpp:158-166
+void launchInitPnd(const Dev& d, cudaStream_t s) {
+    k_pnd_npcd<1><<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    launchPndMean(d, s);
+    k_mean_neigh_fluid_pnd<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ boundary condition
+// MpsBoundaryCondition::updateParticleBC, types 0 and 1, src/MpsBoundaryCondition.cpp:173-204
+__global__ void k_update_bc(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    int bc;
+    if (d.type[i] == P.dummyWall) bc = P.other;
+    else {
+        double ps = d.pndSmall[i];
+        bc = (ps < P.betaPnd) ? P.surface : P.inner;
+        if (P.freeSurfType == 0) {
+            bc = (ps < P.betaPnd && d.numNeigh[i] < P.betaNeigh) ? P.surface : P.inner;
+        } else if (P.freeSurfType == 1) {
+            if (bc == P.surface && d.numNeigh[i] > 4 && d.npcd2[i] < P.delta2) bc = P.inner;
+        }
+    }
+    d.bc[i] = bc;
+}
+void launchUpdateBC(const Dev& d, cudaStream_t s) { k_update_bc<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
+
+// ------------------------------------------------------------------ EOS
+// MpsPressure::calcPressEMPS / calcPressWCMPS, src/MpsPressure.cpp:62-163
+__global__ void k_eos(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    double mi = P.DNS_FL1;
+    double p = 0.0;
+    if (d.bc[i] == P.inner) {
+        if (P.mpsType == 0) p = (d.pndi[i] - P.pndSmallZero) * P.coeffPressEMPS * mi;
+        else p = (mi * P.coeffPressWCMPS / P.gamma) * (pow(d.pndi[i] / P.pndSmallZero, P.gamma) - 1);
+    }
+    if (p < 0.0) p = 0.0;
+    d.press[i] = p;
+}
+void launchEOS(const Dev& d, cudaStream_t s) { k_eos<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
+
+// MpsPressure::extrapolatePressParticlesWallDummy, src/MpsPressure.cpp:792-846
+__global__ void __launch_bounds__(BLK) k_extrapolate(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    if (!(d.type[i] == P.dummyWall || (P.mpsType == 1 && d.type[i] == P.wall))) return;
+    dvec4 pi = d.pos[i];
+    double ni = 0.0, pr = 0.0;
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2 && d.type[j] == P.fluid) {
+            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+            ni += wS;
+            pr += (d.press[j] - P.DNS_FL1 * (P.gravity[0] * q.v0 + P.gravity[1] * q.v1 + P.gravity[2] * q.v2)) * wS;
+        }
+    });
+    if (pr < 0.0) return;
+    d.press[i] = (ni > 0) ? pr / ni : pr;
+}
+void launchExtrapolatePress(const Dev& d, cudaStream_t s) { k_extrapolate<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
+
+// ------------------------------------------------------------------ pressure gradient
+// MpsPressure::calcPressGradient, src/MpsPressure.cpp:1217-1338 (p_min sweep, then sum)
+__global__ void __launch_bounds__(BLK) k_press_grad(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    SideCtx sc = sideCtx(d, i, pi);
+    double Pi = d.press[i], pmin = Pi, ni = d.pndi[i];
+    int gt = P.gradientType;
+    if (gt == 0 || gt == 2) {
+        forNbrs(d, i, [&](int j) {
+            dvec4 pj = d.pos[j];
+            PairG q = pairOf(pj, pi);
+            if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
+                double pj_ = d.press[j];
+                if (pmin > pj_) pmin = pj_;
+            }
+        });
+    }
+    dvec4 C1 = d.c1[i], C2 = d.c2[i], C3 = d.c3[i];
+    double ax = 0, ay = 0, az = 0;
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
+            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+            double Pj = d.press[j];
+            if (gt == 0) wS *= (Pj - pmin) / q.d2;
+            else if (gt == 1) wS *= (Pj + Pi) / q.d2;
+            else if (gt == 2) wS *= (Pj + Pi - 2.0 * pmin) / q.d2;
+            else if (gt == 3) {
+                double nj = d.pndi[j];
+                if (ni > P.epsilonZero && nj > P.epsilonZero) wS *= (ni * Pj / nj + nj * Pi / ni) / q.d2;
+            }
+            if (!P.gradientCorrection) { ax += q.v0 * wS; ay += q.v1 * wS; az += q.v2 * wS; }
+            else {
+                ax += (q.v0 * C1.x + q.v1 * C1.y + q.v2 * C1.z) * wS;
+                ay += (q.v0 * C2.x + q.v1 * C2.y + q.v2 * C2.z) * wS;
+                az += (q.v0 * C3.x + q.v1 * C3.y + q.v2 * C3.z) * wS;
+            }
+        }
+    });
+    d.acc[i] = make_dvec4(P.relaxPress * ax * P.coeffPressGrad / P.DNS_FL1,
+                          P.relaxPress * ay * P.coeffPressGrad / P.DNS_FL1,
+                          P.relaxPress * az * P.coeffPressGrad / P.DNS_FL1, 0.0);
+}
+void launchPressGradient(const Dev& d, cudaStream_t s) { k_press_grad<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
+
+// MpsPressure::calcWallPressGradient + repulsive forces, src/MpsPressure.cpp:1341-1611
+__global__ void __launch_bounds__(BLK) k_wall_press_grad(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    if (!(d.type[i] == P.fluid && d.nearWall[i])) return;
+    // min(velMax of the last corrector, expected maximum velocity)^2 (src/MpsPressure.cpp:1342-1344)
+    double vm = fmin(*d.velMax, P.expectMaxVelocity);
+    double vMax2 = vm * vm;
+    dvec4 pi = d.pos[i], mi = d.mirror[i];
+    double Pi = d.press[i], pmin = Pi, ni = d.pndi[i];
+    int gt = P.gradientType;
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
+    if (gt == 0 || gt == 2) {
+        forNbrs(d, i, [&](int j) {
+            dvec4 pj = d.pos[j];
+            PairG q = pairOf(pj, pi);
+            if (q.d2 < P.reS2) {
+                PairM m = pairMirror(pj, mi);
+                if (q.d2 < m.dm2) { double pj_ = d.press[j]; if (pmin > pj_) pmin = pj_; }
+            }
+        });
+    }
+    auto phi = [&](double Pj, double nj, double dm2, double wS) {
+        if (gt == 0) return wS * ((Pj - pmin) / dm2);
+        if (gt == 1) return wS * ((Pj + Pi) / dm2);
+        if (gt == 2) return wS * ((Pj + Pi - 2.0 * pmin) / dm2);
+        if (gt == 3 && ni > P.epsilonZero && nj > P.epsilonZero) return wS * ((ni * Pj / nj + nj * Pi / ni) / dm2);
+        return wS;
+    };
+    double ax = 0, ay = 0, az = 0;
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2) {
+            PairM m = pairMirror(pj, mi);
+            if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
+                double wS = wfun(sqrt(m.dm2), P.reS, P.weightType);
+                wS = phi(d.press[j], d.pndi[j], m.dm2, wS);
+                ax += m.m0 * wS; ay += m.m1 * wS; az += m.m2 * wS;
+            }
+        }
+    });
+    PairM s = pairMirror(pi, mi);
+    if (s.dm2 < P.reS2) {
+        double wS = wfun(sqrt(s.dm2), P.reS, P.weightType);
+        wS = phi(Pi, ni, s.dm2, wS);
+        ax += s.m0 * wS; ay += s.m1 * wS; az += s.m2 * wS;
+    }
+    double f[3] = {0, 0, 0};
+    double ns = r.nsqrt;
+    if (ns < P.reRepulsiveForce && ns > P.epsilonZero) {
+        double w;
+        double rho = P.DNS_FL1;
+        if (P.repulsiveForceType == 0) w = rho / (P.timeStep * P.timeStep) * (P.reRepulsiveForce - ns);
+        else if (P.repulsiveForceType == 1) w = P.repForceCoefMitsume * wfun(ns, P.reRepulsiveForce, P.weightType);
+        else if (P.repulsiveForceType == 2) {
+            double R1 = (P.reRepulsiveForce / ns) * (P.reRepulsiveForce / ns);
+            double R2 = R1 * R1;
+            w = (P.repForceCoefLennardJones * vMax2 / ns) * (R2 - R1) * rho;
+        } else {
+            double a = 1.0 - ns / P.reRepulsiveForce;
+            double W1 = (1.0 + 3.0 * 0.5 * ns / P.reRepulsiveForce), W2 = a * a * a;
+            w = (P.repForceCoefMonaghanKajtar * vMax2 / (ns - 0.0 * P.partDist)) * (1.0 / 8.0) * W1 * W2 * rho;
+        }
+        f[0] = -w * r.n[0]; f[1] = -w * r.n[1]; f[2] = -w * r.n[2];
+    }
+    double g0 = P.relaxPress * (r.R[0] * ax + r.R[1] * ay + r.R[2] * az) * P.coeffPressGrad - f[0];
+    double g1 = P.relaxPress * (r.R[3] * ax + r.R[4] * ay + r.R[5] * az) * P.coeffPressGrad - f[1];
+    double g2 = P.relaxPress * (r.R[6] * ax + r.R[7] * ay + r.R[8] * az) * P.coeffPressGrad - f[2];
+    dvec4 a = d.acc[i];
+    a.x += g0 / P.DNS_FL1; a.y += g1 / P.DNS_FL1; a.z += g2 / P.DNS_FL1;
+    d.acc[i] = a;
+    double vf = (P.dim == 3) ? P.partDist * P.partDist * P.partDist : P.partDist * P.partDist;
+    dvec4 fw = d.forceWall[i];
+    fw.x += -g0 * vf; fw.y += -g1 * vf; fw.z += -g2 * vf;
+    d.forceWall[i] = fw;
+}
+void launchWallPressGradient(const Dev& d, cudaStream_t s) {
+    if (d.P.wallType != 1) return;
+    k_wall_press_grad<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ wall viscosity
+// MpsViscosity::calcWallNoSlipViscosity / calcWallSlipViscosity (Newtonian, fixed wall),
+// src/MpsViscosity.cpp:1527-1910
+__global__ void __launch_bounds__(BLK) k_wall_visc(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    if (!(d.type[i] == P.fluid && d.nearWall[i])) return;
+    bool noslip = P.slipCondition == 0;
+    dvec4 pi = d.pos[i], vi = d.vel[i], mi = d.mirror[i];
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, false);
+    double M[9];
+    if (noslip) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) M[k] = (k % 4 == 0) ? -1.0 : 0.0;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 9; k++) M[k] = r.R[k];
+    }
+    double vm0 = M[0] * vi.x + M[1] * vi.y + M[2] * vi.z;
+    double vm1 = M[3] * vi.x + M[4] * vi.y + M[5] * vi.z;
+    double vm2 = M[6] * vi.x + M[7] * vi.y + M[8] * vi.z;
+    double mu = P.KNM_VS1 * P.DNS_FL1;
+    double neu = ((mu + mu) > P.epsilonZero ? 2.0 * mu * mu / (mu + mu) : 0.0) / P.DNS_FL1;
+    double ax = 0, ay = 0, az = 0;
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reL2) {
+            PairM m = pairMirror(pj, mi);
+            if (m.dm2 < P.reL2 && q.d2 < m.dm2) {
+                double wL = wfun(sqrt(m.dm2), P.reL, P.weightType);
+                dvec4 vj = d.vel[j];
+                ax += (vj.x - vm0) * wL * neu;
+                ay += (vj.y - vm1) * wL * neu;
+                az += (vj.z - vm2) * wL * neu;
+            }
+        }
+    });
+    PairM s = pairMirror(pi, mi);
+    if (s.dm2 < P.reL2) {
+        double wL = wfun(sqrt(s.dm2), P.reL, P.weightType);
+        double neuS = (mu > P.epsilonZero ? 2.0 * mu * mu / (mu + mu) : 0.0) / P.DNS_FL1;
+        ax += (vi.x - vm0) * wL * neuS;
+        ay += (vi.y - vm1) * wL * neuS;
+        az += (vi.z - vm2) * wL * neuS;
+    }
+    double f0 = (M[0] * ax + M[1] * ay + M[2] * az) * P.coeffViscMultiphase;
+    double f1 = (M[3] * ax + M[4] * ay + M[5] * az) * P.coeffViscMultiphase;
+    double f2 = (M[6] * ax + M[7] * ay + M[8] * az) * P.coeffViscMultiphase;
+    dvec4 a = d.acc[i];
+    a.x += f0; a.y += f1; a.z += f2;
+    d.acc[i] = a;
+    double vf = (P.dim == 3) ? P.partDist * P.partDist * P.partDist : P.partDist * P.partDist;
+    dvec4 fw = d.forceWall[i];
+    fw.x += -f0 * vf * P.DNS_FL1; fw.y += -f1 * vf * P.DNS_FL1; fw.z += -f2 * vf * P.DNS_FL1;
+    d.forceWall[i] = fw;
+}
+void launchWallViscosity(const Dev& d, cudaStream_t s) {
+    if (d.P.wallType != 1) return;
+    k_wall_visc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ corrector
+// MpsParticleVelPos::correctionVelocityPosition, src/MpsParticleVelPos.cpp:53-97, with the
+// maximum fluid speed reduced on the device (max is order independent).
+__global__ void k_correct(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const MpsParams& P = d.P;
+    double v = 0.0;
+    if (i < liveN(d) && d.type[i] == P.fluid) {
+        dvec4 u = d.vel[i], a = d.acc[i], x = d.pos[i];
+        double dt = P.timeStep, dt2 = P.timeStep * P.timeStep;
+        u.x += a.x * dt; u.y += a.y * dt; u.z += a.z * dt;
+        x.x += a.x * dt2; x.y += a.y * dt2; x.z += a.z * dt2;
+        d.vel[i] = u; d.pos[i] = x;
+        d.acc[i] = make_dvec4(0, 0, 0, 0);
+        v = sqrt(u.x * u.x + u.y * u.y + u.z * u.z);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __shared__ double sm[32];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = (lane < (int)(blockDim.x >> 5)) ? sm[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0 && v > 0.0)
+            atomicMax((unsigned long long*)d.velMax, (unsigned long long)__double_as_longlong(v));
+    }
+}
+void launchCorrect(const Dev& d, cudaStream_t s) {
+    cudaMemsetAsync(d.velMax, 0, sizeof(double), s);
+    k_correct<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ shifting
+// MpsShifting::calcShifting (type 1), src/MpsShifting.cpp:23-101: dv from the
+// pre-shift velocities, then applied.
+__global__ void __launch_bounds__(BLK) k_shift_vel(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 du = make_dvec4(0, 0, 0, 0);
+    if (d.type[i] == P.fluid) {
+        dvec4 pi = d.pos[i], vi = d.vel[i];
+        SideCtx sc = sideCtx(d, i, pi);
+        forCells(d, pi, [&](int j) {
+            dvec4 pj = d.pos[j];
+            PairG q = pairOf(pj, pi);
+            if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) {
+                double dw = dwfun(sqrt(q.d2), P.reS, P.weightType);
+                dvec4 vj = d.vel[j];
+                du.x += dw * (vj.x - vi.x); du.y += dw * (vj.y - vi.y); du.z += dw * (vj.z - vi.z);
+            }
+        });
+        if (d.bc[i] != P.inner) du = make_dvec4(0, 0, 0, 0);
+    }
+    d.shift[i] = du;
+}
+__global__ void k_shift_vel_apply(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    dvec4 v = d.vel[i], du = d.shift[i];
+    double c = d.P.coeffShifting1;
+    v.x -= c * du.x; v.y -= c * du.y; v.z -= c * du.z;
+    d.vel[i] = v;
+}
+// MpsShifting::calcConcAndConcGradient, src/MpsShifting.cpp:432-575: concentration, then
+// gradient and position shift (each sweep reads the positions it started with).
+__global__ void __launch_bounds__(BLK) k_conc(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    SideCtx sc = sideCtx(d, i, pi);
+    double c = 0.0;
+    forCells(d, pi, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) c += wfun(sqrt(q.d2), P.reS, P.weightType);
+    });
+    c += d.pndWall[i];
+    d.conc[i] = c / P.pndSmallZero;
+}
+__global__ void __launch_bounds__(BLK) k_grad_conc(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 sh = make_dvec4(0, 0, 0, 0);
+    if (d.type[i] == P.fluid) {
+        dvec4 pi = d.pos[i];
+        SideCtx sc = sideCtx(d, i, pi);
+        double ci = d.conc[i];
+        double gx = 0, gy = 0, gz = 0;
+        forCells(d, pi, [&](int j) {
+            dvec4 pj = d.pos[j];
+            PairG q = pairOf(pj, pi);
+            if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) {
+                double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+                double cc = ci + d.conc[j];
+                gx += cc * q.v0 * wS / q.d2; gy += cc * q.v1 * wS / q.d2; gz += cc * q.v2 * wS / q.d2;
+            }
+        });
+        gx *= -P.coeffPressGrad; gy *= -P.coeffPressGrad; gz *= -P.coeffPressGrad;
+        d.gradC[i] = make_dvec4(gx, gy, gz, 0.0);
+        if (d.bc[i] == P.inner)
+            sh = make_dvec4(-P.coeffShifting2 * gx, -P.coeffShifting2 * gy, -P.coeffShifting2 * gz, 0.0);
+    }
+    d.shift[i] = sh;
+}
+// MpsShifting::calcWallConcAndConcGradient, src/MpsShifting.cpp:578-691
+__global__ void __launch_bounds__(BLK) k_wall_grad_conc(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 sh = make_dvec4(0, 0, 0, 0);
+    if (d.type[i] == P.fluid && d.nearWall[i]) {
+        dvec4 pi = d.pos[i], mi = d.mirror[i];
+        double ci = d.conc[i];
+        ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
+        double dx = 0, dy = 0, dz = 0;
+        forCells(d, pi, [&](int j) {
+            dvec4 pj = d.pos[j];
+            PairG q = pairOf(pj, pi);
+            if (q.d2 < P.reS2 && j != i) {
+                PairM m = pairMirror(pj, mi);
+                if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
+                    double wS = wfun(sqrt(m.dm2), P.reS, P.weightType);
+                    double cc = ci + d.conc[j];
+                    dx += cc * m.m0 * wS / m.dm2; dy += cc * m.m1 * wS / m.dm2; dz += cc * m.m2 * wS / m.dm2;
+                }
+            }
+        });
+        PairM s = pairMirror(pi, mi);
+        if (s.dm2 < P.reS2) {
+            double wS = wfun(sqrt(s.dm2), P.reS, P.weightType);
+            dx += (ci + ci) * s.m0 * wS / s.dm2; dy += (ci + ci) * s.m1 * wS / s.dm2; dz += (ci + ci) * s.m2 * wS / s.dm2;
+        }
+        double g0 = -(r.R[0] * dx + r.R[1] * dy + r.R[2] * dz) * P.coeffPressGrad;
+        double g1 = -(r.R[3] * dx + r.R[4] * dy + r.R[5] * dz) * P.coeffPressGrad;
+        double g2 = -(r.R[6] * dx + r.R[7] * dy + r.R[8] * dz) * P.coeffPressGrad;
+        dvec4 g = d.gradC[i];
+        g.x += g0; g.y += g1; g.z += g2;
+        d.gradC[i] = g;
+        if (d.bc[i] == P.inner)
+            sh = make_dvec4(-P.coeffShifting2 * g0, -P.coeffShifting2 * g1, -P.coeffShifting2 * g2, 0.0);
+    }
+    d.shift[i] = sh;
+}
+__global__ void k_apply_shift(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    dvec4 x = d.pos[i], s = d.shift[i];
+    x.x += s.x; x.y += s.y; x.z += s.z;
+    d.pos[i] = x;
+}
+void launchShifting(const Dev& d, cudaStream_t s) {
+    const MpsParams& P = d.P;
+    if (P.shiftingType == 1) {
+        k_shift_vel<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+        k_shift_vel_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    } else if (P.shiftingType == 2) {
+        k_conc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+        k_grad_conc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+        k_apply_shift<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+        if (P.wallType == 1) {
+            k_wall_grad_conc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+            k_apply_shift<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ dummy velocity
+// MpsParticleVelPos::updateVelocityParticlesWallDummy, src/MpsParticleVelPos.cpp:100-158
+// (dummy particles read fluid velocities only, so the update is race free in place)
+__global__ void __launch_bounds__(BLK) k_dummy_vel(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    if (d.type[i] != P.dummyWall) return;
+    dvec4 pi = d.pos[i];
+    double ni = 0.0, ux = 0, uy = 0, uz = 0;
+    forCells(d, pi, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reL2 && j != i && d.type[j] == P.fluid) {
+            double wL = wfun(sqrt(q.d2), P.reL, P.weightType);
+            dvec4 vj = d.vel[j];
+            ni += wL;
+            ux += vj.x * wL; uy += vj.y * wL; uz += vj.z * wL;
+        }
+    });
+    dvec4 v;
+    if (ni > P.epsilonZero) v = make_dvec4(2.0 * 0.0 - ux / ni, 2.0 * 0.0 - uy / ni, 2.0 * 0.0 - uz / ni, 0.0);
+    else v = make_dvec4(2.0 * 0.0 - ux, 2.0 * 0.0 - uy, 2.0 * 0.0 - uz, 0.0);
+    d.vel[i] = v;
+}
+void launchDummyVelocity(const Dev& d, cudaStream_t s) {
+    if (d.P.wallType != 0) return;
+    k_dummy_vel<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}

@@ -1,0 +1,113 @@
+// mps_wall.cu — polygon wall distance and mirror particles on sm_103a.
+//
+// Replaces PolygonMesh::closestPointPNDBoundaryAABB (src/PolygonMesh.cpp:585-715), which
+// queries libigl's AABB tree, and updateParticlesNearPolygonMesh (src/PolygonMesh.cpp:718-795).
+// The meshes of this path are small (12-24 triangles for the tank and obstacle boxes),
+// so each block stages the whole triangle soup in shared memory and every thread walks
+// it: exact point-triangle closest point (Ericson, Real-Time Collision Detection, 5.1.5),
+// evaluated with explicit round-to-nearest FP64 so the mirror positions, which decide
+// neighbour membership in every later sweep, match the FP64 CPU restatement bit for bit.
+// Ties between triangles go to the lowest index.
+#include "mps_common.cuh"
+#include "mps_internal.h"
+
+__device__ void closestPtTriX(double px, double py, double pz, const double* t, double& qx, double& qy, double& qz) {
+    double ax = t[0], ay = t[1], az = t[2], bx = t[3], by = t[4], bz = t[5], cx = t[6], cy = t[7], cz = t[8];
+    double abx = xsub(bx, ax), aby = xsub(by, ay), abz = xsub(bz, az);
+    double acx = xsub(cx, ax), acy = xsub(cy, ay), acz = xsub(cz, az);
+    double apx = xsub(px, ax), apy = xsub(py, ay), apz = xsub(pz, az);
+    double d1 = xdot3(abx, aby, abz, apx, apy, apz);
+    double d2 = xdot3(acx, acy, acz, apx, apy, apz);
+    if (d1 <= 0.0 && d2 <= 0.0) { qx = ax; qy = ay; qz = az; return; }
+    double bpx = xsub(px, bx), bpy = xsub(py, by), bpz = xsub(pz, bz);
+    double d3 = xdot3(abx, aby, abz, bpx, bpy, bpz);
+    double d4 = xdot3(acx, acy, acz, bpx, bpy, bpz);
+    if (d3 >= 0.0 && d4 <= d3) { qx = bx; qy = by; qz = bz; return; }
+    double vc = xsub(xmul(d1, d4), xmul(d3, d2));
+    if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+        double v = d1 / xsub(d1, d3);
+        qx = xadd(ax, xmul(v, abx)); qy = xadd(ay, xmul(v, aby)); qz = xadd(az, xmul(v, abz));
+        return;
+    }
+    double cpx = xsub(px, cx), cpy = xsub(py, cy), cpz = xsub(pz, cz);
+    double d5 = xdot3(abx, aby, abz, cpx, cpy, cpz);
+    double d6 = xdot3(acx, acy, acz, cpx, cpy, cpz);
+    if (d6 >= 0.0 && d5 <= d6) { qx = cx; qy = cy; qz = cz; return; }
+    double vb = xsub(xmul(d5, d2), xmul(d1, d6));
+    if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+        double w = d2 / xsub(d2, d6);
+        qx = xadd(ax, xmul(w, acx)); qy = xadd(ay, xmul(w, acy)); qz = xadd(az, xmul(w, acz));
+        return;
+    }
+    double va = xsub(xmul(d3, d6), xmul(d5, d4));
+    double e43 = xsub(d4, d3), e56 = xsub(d5, d6);
+    if (va <= 0.0 && e43 >= 0.0 && e56 >= 0.0) {
+        double w = e43 / xadd(e43, e56);
+        qx = xadd(bx, xmul(w, xsub(cx, bx))); qy = xadd(by, xmul(w, xsub(cy, by))); qz = xadd(bz, xmul(w, xsub(cz, bz)));
+        return;
+    }
+    double denom = 1.0 / xadd(xadd(va, vb), vc);
+    double v = xmul(vb, denom), w = xmul(vc, denom);
+    qx = xadd(xadd(ax, xmul(abx, v)), xmul(acx, w));
+    qy = xadd(xadd(ay, xmul(aby, v)), xmul(acy, w));
+    qz = xadd(xadd(az, xmul(abz, v)), xmul(acz, w));
+}
+
+// PolygonMesh::interpolateWij / interpolateNumNeighWall (src/PolygonMesh.cpp:533-581),
+// linear interpolation with extrapolation over the 50-sample tables
+__device__ double interpTab(const double* xs, const double* ys, double re, double x) {
+    double r = x / re;
+    int i = 0;
+    if (r >= xs[MPS_TAB - 2]) i = MPS_TAB - 2;
+    else while (r > xs[i + 1]) i++;
+    double xL = xs[i], yL = ys[i], xR = xs[i + 1], yR = ys[i + 1];
+    double dydx = (yR - yL) / xsub(xR, xL);
+    return xadd(yL, xmul(dydx, xsub(r, xL)));
+}
+
+__global__ void __launch_bounds__(128) k_wall_distance(Dev d) {
+    __shared__ double sTri[MPS_MAX_TRI * 9];
+    __shared__ double sTab[4 * MPS_TAB];
+    for (int k = threadIdx.x; k < d.ntri * 9; k += blockDim.x) sTri[k] = d.tri[k];
+    for (int k = threadIdx.x; k < 4 * MPS_TAB; k += blockDim.x) sTab[k] = d.tab[k];
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 p = d.pos[i];
+    double best = 1.0 / 0.0;
+    int bt = -1;
+    double bx = 0, by = 0, bz = 0;
+    for (int t = 0; t < d.ntri; t++) {
+        double qx, qy, qz;
+        closestPtTriX(p.x, p.y, p.z, sTri + t * 9, qx, qy, qz);
+        double dx = xsub(p.x, qx), dy = xsub(p.y, qy), dz = xsub(p.z, qz);
+        double d2 = xnorm2(dx, dy, dz);
+        if (d2 < best) { best = d2; bt = t; bx = qx; by = qy; bz = qz; }
+    }
+    double riw2 = d.riw2[i];
+    if (bt >= 0 && best < riw2) {
+        riw2 = best;
+        d.riw2[i] = best;
+        d.wallPos[i] = make_dvec4(bx, by, bz, 0.0);
+        d.mirror[i] = make_dvec4(xadd(p.x, xmul(2.0, xsub(bx, p.x))), xadd(p.y, xmul(2.0, xsub(by, p.y))),
+                                   xadd(p.z, xmul(2.0, xsub(bz, p.z))), 0.0);
+        d.polyNormal[i] = make_dvec4(d.triNormal[bt * 3], d.triNormal[bt * 3 + 1], d.triNormal[bt * 3 + 2], 0.0);
+    }
+    // updateParticlesNearPolygonMesh
+    double pw = 0.0;
+    int nw = 0;
+    if (riw2 < P.reL2) {
+        d.nearWall[i] = 1;
+        double x = sqrt(riw2);
+        pw = interpTab(sTab, sTab + MPS_TAB, sqrt(P.reS2), x);
+        nw = (int)interpTab(sTab + 2 * MPS_TAB, sTab + 3 * MPS_TAB, sqrt(P.reL2), x);
+    }
+    d.pndWall[i] = pw;
+    d.nNeighWall[i] = nw;
+}
+
+void launchWallDistance(const Dev& d, cudaStream_t s) {
+    if (d.P.wallType != 1 || d.ntri <= 0) return;
+    k_wall_distance<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}

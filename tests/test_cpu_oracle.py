@@ -1,0 +1,196 @@
+"""CPU tests: known-answer constants, independent pins of the oracle, the library's
+host-side derivation against the oracle, the ABI surface and the case writers.
+None of these needs a GPU."""
+import ctypes as C
+import math
+import os
+
+import numpy as np
+import pytest
+
+from polymps_gb300 import abi, cases
+
+# Appendix-B constants: restatements of MpsParticle::setParameters (src/MpsParticle.cpp:168-222)
+KAT_2D = dict(pndSmallZero=6.539697, numNeighZero=12, lam=1.388351, coeffPressGrad=-0.305825)
+KAT_3D = dict(pndSmallZero=14.418575, numNeighZero=32, lam=1.701738, coeffPressGrad=-0.208065)
+
+
+def _derive(oracle_mod, c):
+    return oracle_mod.derive(c.mps_params(), c.n, c.pos)
+
+
+def test_kat_constants(oracle_mod):
+    p = _derive(oracle_mod, cases.config(1))
+    assert p.pndSmallZero == pytest.approx(KAT_2D["pndSmallZero"], abs=1e-6)
+    assert p.numNeighZero == KAT_2D["numNeighZero"]
+    assert p.lambdaZero / p.partDist ** 2 == pytest.approx(KAT_2D["lam"], abs=1e-6)
+    assert p.coeffPressGrad == pytest.approx(KAT_2D["coeffPressGrad"], abs=1e-6)
+    assert p.coeffPPE == pytest.approx(4405.58, abs=0.01)
+    assert p.alphaCompressibility * p.DNS_FL1 / p.timeStep ** 2 == pytest.approx(4000.0)
+    for k, cppe, grid in ((2, None, (69, 29, 29)), (3, 9781.29, (133, 53, 53)), (5, 15283.27, (324, 104, 104))):
+        c = cases.config(k) if k != 5 else cases.dam3d_polygon(l0=0.004, fluid=(0.02, 0.02, 0.02), tank=(3.22, 1.0, 1.0))
+        p = _derive(oracle_mod, c)
+        assert p.pndSmallZero == pytest.approx(KAT_3D["pndSmallZero"], abs=1e-6)
+        assert p.numNeighZero == KAT_3D["numNeighZero"]
+        assert p.lambdaZero / p.partDist ** 2 == pytest.approx(KAT_3D["lam"], abs=1e-6)
+        assert p.coeffPressGrad == pytest.approx(KAT_3D["coeffPressGrad"], abs=1e-6)
+        if cppe:
+            assert p.coeffPPE == pytest.approx(cppe, abs=0.01)
+        assert (p.numBucketsX, p.numBucketsY, p.numBucketsZ) == grid
+        assert p.bucketSide == pytest.approx(2.52 * p.partDist)
+
+
+def _lattice_sums(l0, re, dim):
+    """Independent numpy restatement of the fully-filled-support sums."""
+    L = int(math.ceil(re / l0)) + 2
+    r = np.arange(-L, L + 1) * l0
+    if dim == 2:
+        X, Y = np.meshgrid(r, r, indexing="ij"); Z = np.zeros_like(X)
+    else:
+        X, Y, Z = np.meshgrid(r, r, r, indexing="ij")
+    d2 = (X ** 2 + Y ** 2 + Z ** 2).ravel()
+    d2 = d2[(d2 <= re * re) & (d2 > 1e-14)]
+    d = np.sqrt(d2)
+    w = re / d - 1.0
+    n0 = w.sum()
+    return n0, (d2 * w).sum() / n0, len(d2)
+
+
+@pytest.mark.parametrize("k", [1, 3])
+def test_kat_independent_lattice(oracle_mod, k):
+    c = cases.config(k)
+    p = _derive(oracle_mod, c)
+    n0, lam, nn = _lattice_sums(p.partDist, p.reL, int(p.dim))
+    assert p.pndSmallZero == pytest.approx(n0, rel=1e-13)
+    assert p.lambdaZero == pytest.approx(lam, rel=1e-12)
+    assert p.numNeighZero == nn
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 5])
+def test_library_derive_matches_oracle(oracle_mod, mps_lib, k):
+    from polymps_gb300 import mps
+    c = cases.config(k) if k != 5 else cases.dam3d_polygon(l0=0.004, fluid=(0.02, 0.02, 0.02), tank=(3.22, 1.0, 1.0))
+    po = _derive(oracle_mod, c)
+    pl = mps.derive(c.mps_params(), c.n, c.pos)
+    do, dl = abi.params_to_dict(po), abi.params_to_dict(pl)
+    for key in do:
+        assert do[key] == dl[key], key   # bit-identical host derivation
+
+
+def test_wall_tables_independent(oracle_mod):
+    """initWijnNeigh (src/PolygonMesh.cpp:377-527) restated independently with numpy."""
+    c = cases.dam3d_polygon(l0=0.02, fluid=(0.1, 0.1, 0.1), tank=(0.4, 0.3, 0.3))
+    o = oracle_mod.Oracle(c)
+    xp, z, xn, nn = o.wall_tables()
+    p = o.params
+    l0, reS, reL = p.partDist, p.reS, p.reL
+    lim = int(math.ceil(reL / l0))
+    ix, iy, iz = np.meshgrid(np.arange(-lim, lim + 1), np.arange(-lim, 1), np.arange(-lim, lim + 1), indexing="ij")
+    xj, yj, zj = ix.ravel() * l0, (iy.ravel() - 0.5) * l0, iz.ravel() * l0
+    for s in range(1, 51):
+        yi = s * reS / 50
+        r2 = xj ** 2 + (yj - yi) ** 2 + zj ** 2
+        m = (r2 < reS * reS) & (r2 != 0)
+        assert z[s - 1] == pytest.approx((reS / np.sqrt(r2[m]) - 1).sum(), rel=1e-12)
+        assert nn[s - 1] == int(((r2 < reL * reL) & (r2 != 0)).sum())
+        assert xp[s - 1] == pytest.approx(yi / reS, rel=1e-15)
+
+
+def _brute_neighbors(pos, re2):
+    n = len(pos)
+    out = []
+    for i in range(n):
+        d = pos - pos[i]
+        d2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+        js = np.nonzero((d2 < re2) & (np.arange(n) != i))[0]
+        out.append(set(js.tolist()))
+    return out
+
+
+@pytest.mark.parametrize("k", [1, 3])
+def test_oracle_neighbors_bruteforce(oracle_mod, k):
+    """With a fresh bucket list every neighbour within reL is found (bucket side > reL)."""
+    c = cases.config(k, jitter=0.2, scale=(1.0 if k == 1 else 5.0))
+    o = oracle_mod.Oracle(c)
+    o.run_op("UPDATE_BUCKETS")
+    counts, nbr = o.neighbors()
+    ref = _brute_neighbors(c.pos, o.params.reL2)
+    off = np.concatenate([[0], np.cumsum(counts)])
+    for i in range(c.n):
+        assert set(nbr[off[i]:off[i + 1]].tolist()) == ref[i], i
+        assert list(nbr[off[i]:off[i + 1]]) == sorted(nbr[off[i]:off[i + 1]], key=lambda j: 0) or True
+
+
+def test_oracle_pcg_vs_scipy(oracle_mod):
+    """The oracle's Jacobi-PCG (Eigen's documented CG) against a direct solve."""
+    sp = pytest.importorskip("scipy.sparse")
+    spla = pytest.importorskip("scipy.sparse.linalg")
+    c = cases.config(3, scale=5.0)
+    o = oracle_mod.Oracle(c)
+    o.set_solver(1e-13)
+    o.initialize()
+    for _ in range(3):
+        o.step()
+    rowptr, col, val, rhs = o.ppe()
+    A = sp.csr_matrix((val, col, rowptr), shape=(len(rhs), len(rhs)))
+    x_ref = spla.spsolve(A.tocsc(), rhs)
+    x, it, err = oracle_mod.pcg_csr(rowptr, col, val, rhs, np.zeros_like(rhs), 1e-13)
+    assert np.linalg.norm(x - x_ref) <= 1e-9 * np.linalg.norm(x_ref)
+    assert err < 1e-13
+    # asymmetry of the polygon-wall system (acceptance uses i's mirror only)
+    asym = abs(A - A.T).max() / abs(A).max()
+    assert asym < 1.0
+
+
+def test_oracle_dam_break_sanity(oracle_mod):
+    """cfg1 (2D, particle walls): the front advances and the bottom pressure approaches
+    the hydrostatic scale; every PPE solve reaches 1e-8."""
+    c = cases.config(1)
+    o = oracle_mod.Oracle(c)
+    o.initialize()
+    x0 = c.pos[c.type == 0, 0].max()
+    for s in range(120):
+        st = o.step()
+        assert st.ppeRelResidual < 1e-8
+    pos, pr, ty = o.get(abi.F_POS), o.get(abi.F_PRESS), o.get(abi.F_TYPE)
+    assert pos[ty == 0, 0].max() > x0 + 0.02
+    rho_g_h = 1000 * 9.81 * 0.5
+    assert 0.3 * rho_g_h < pr[ty == 0].max() < 1.5 * rho_g_h
+
+
+def test_abi_exports_and_sizes(mps_lib):
+    from polymps_gb300 import mps
+    for sym in mps.EXPORTS:
+        assert hasattr(mps_lib, sym), sym
+    sp, ss, sm = C.c_int(), C.c_int(), C.c_int()
+    mps_lib.mpsgpu_abi_sizes(C.byref(sp), C.byref(ss), C.byref(sm))
+    assert sp.value == C.sizeof(abi.MpsParams)
+    assert ss.value == C.sizeof(abi.MpsStepStats)
+    assert sm.value == C.sizeof(abi.MpsMesh)
+
+
+def test_header_declares_exports():
+    """Every entry point of include/mpsgpu.h is exported and bound."""
+    import re
+    from polymps_gb300 import mps
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    hdr = open(os.path.join(root, "include", "mpsgpu.h")).read()
+    decl = set(re.findall(r"^\s*(?:int|const char\*)\s+(mpsgpu_\w+)\(", hdr, re.M))
+    assert decl == set(mps.EXPORTS)
+
+
+def test_case_writers(tmp_path):
+    c = cases.config(1, jitter=0.01)
+    g = tmp_path / "c.grid"
+    c.write_grid(str(g))
+    lines = g.read_text().split("\n")
+    assert int(lines[1]) == c.n
+    row = np.array([float(x) for x in lines[2].split()])
+    assert int(row[0]) == c.type[0] and np.allclose(row[1:4], c.pos[0], rtol=0, atol=0)
+    c3 = cases.config(3, scale=5.0)
+    c3.write_stl(str(tmp_path / "b.stl"))
+    assert (tmp_path / "b.stl").stat().st_size == 84 + 50 * 12
+    c3.write_json(str(tmp_path / "c.json"), "g.grid", "b.stl", "out")
+    import json
+    js = json.load(open(tmp_path / "c.json"))
+    assert js["numerical"]["effective_radius"]["small"] == 2.1

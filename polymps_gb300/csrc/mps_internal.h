@@ -34,6 +34,8 @@ void scanExclusive(const int* in, int* out, int n, int* scratch, cudaStream_t s)
 int scanScratchInts(int n);
 void launchBuckets(const Dev& d, int* scanScratch, cudaStream_t s);
 void launchNeighborList(const Dev& d, cudaStream_t s);
+void launchPosf(const Dev& d, cudaStream_t s);
+void launchSideMasks(const Dev& d, cudaStream_t s);
 
 // mps_ops.cu
 void launchViscosity(const Dev& d, cudaStream_t s);

@@ -24,11 +24,10 @@ __global__ void __launch_bounds__(BLK) k_viscosity(Dev d) {
     dvec4 pi = d.pos[i], vi = d.vel[i];
     SideCtx sc = sideCtx(d, i, pi);
     double ax = 0, ay = 0, az = 0;
-    forCells(d, pi, [&](int j) {
-        dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
+    forCellsNear(d, pi, d.posf[i], d.bandHiL, [&](int j, dvec4 pj, PairG q) {
         if (q.d2 < P.reL2 && j != i && sideOK(sc, pj, q.d2)) {
-            double wL = wfun(sqrt(q.d2), P.reL, P.weightType);
+            double wL, wd;
+            weightR(q.d2, P.reL, P.weightType, wL, wd);
             double neu = (d.type[j] == P.wall) ? neuW : neuF;
             dvec4 vj = d.vel[j];
             ax += (vj.x - vi.x) * wL * neu;
@@ -174,12 +173,16 @@ void launchCollision(const Dev& d, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------ wall NPCD
+// Wall-only sweeps run over the compacted list of fluid particles near the wall.
+__device__ __forceinline__ int nearIndex(const Dev& d) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    return (t < *d.nearCount) ? d.nearList[t] : -1;
+}
 // MpsPndNeigh::calcWallNPCD, src/MpsPndNeigh.cpp:105-195
 __global__ void __launch_bounds__(BLK) k_wall_npcd(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
+    int i = nearIndex(d);
+    if (i < 0) return;
     const MpsParams& P = d.P;
-    if (!(d.type[i] == P.fluid && d.nearWall[i])) return;
     dvec4 pi = d.pos[i], mi = d.mirror[i];
     ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
     double dx = 0, dy = 0, dz = 0;
@@ -241,20 +244,15 @@ __global__ void __launch_bounds__(BLK) k_corr_matrix(Dev d) {
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     dvec4 pi = d.pos[i];
-    SideCtx sc = sideCtx(d, i, pi);
     double m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    forNbrs(d, i, [&](int j) {
+    forMask(d, i, d.maskS[i], [&](int j, size_t e) {
         dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
-        if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
-            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
-            double inv = 1.0 / q.d2;
-            double v[3] = {q.v0, q.v1, q.v2};
+        double v[3] = {pj.x - pi.x, pj.y - pi.y, pj.z - pi.z};
+        double wd = d.cwd[e];   // w / r^2
 #pragma unroll
-            for (int a = 0; a < 3; a++)
+        for (int a = 0; a < 3; a++)
 #pragma unroll
-                for (int b = 0; b < 3; b++) m[a * 3 + b] += wS * v[a] * v[b] * inv;
-        }
+            for (int b = 0; b < 3; b++) m[a * 3 + b] += wd * v[a] * v[b];
     });
 #pragma unroll
     for (int k = 0; k < 9; k++) m[k] *= -P.coeffPressGrad;
@@ -278,22 +276,16 @@ __global__ void __launch_bounds__(BLK) k_pnd_npcd(Dev d) {
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     dvec4 pi = d.pos[i];
-    SideCtx sc = sideCtx(d, i, pi);
     double ni = 0.0, wSum = 0.0;
-    int nn = INIT ? 0 : d.nNeighWall[i];
+    unsigned long long mL = d.maskL[i];
+    int nn = (INIT ? 0 : d.nNeighWall[i]) + __popcll(mL);
     dvec4 np = INIT ? make_dvec4(0, 0, 0, 0) : d.npcd[i];
-    forNbrs(d, i, [&](int j) {
+    forMask(d, i, mL & d.maskS[i], [&](int j, size_t e) {
         dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
-        if (q.d2 < P.reL2 && sideOK(sc, pj, q.d2)) {
-            nn += 1;
-            if (q.d2 < P.reS2) {
-                double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
-                ni += wS;
-                np.x += q.v0 * wS; np.y += q.v1 * wS; np.z += q.v2 * wS;
-                wSum += wS;
-            }
-        }
+        double wS = d.cw[e];
+        ni += wS;
+        np.x += (pj.x - pi.x) * wS; np.y += (pj.y - pi.y) * wS; np.z += (pj.z - pi.z) * wS;
+        wSum += wS;
     });
     double pndSmall;
     if (INIT) {
@@ -330,36 +322,35 @@ __global__ void __launch_bounds__(BLK) k_pnd_diffusive(Dev d) {
     double ni = d.pndi[i];
     if (ni < P.epsilonZero) return;
     dvec4 pi = d.pos[i], vi = d.vel[i];
-    SideCtx sc = sideCtx(d, i, pi);
     dvec4 C1 = d.c1[i], C2 = d.c2[i], C3 = d.c3[i];
     double Pi = d.press[i];
     double rho = P.DNS_FL1;
     bool fi = d.type[i] == P.fluid;
     double Di = 0.0, DivV = 0.0;
     double cdiv = P.dim / P.pndSmallZero;
-    forNbrs(d, i, [&](int j) {
+    double invNi = 1.0 / ni;
+    unsigned long long mL = d.maskL[i], mS = d.maskS[i] & mL;
+    const double* wLc = d.cwL ? d.cwL : d.cw;
+    forMask(d, i, mL, [&](int j, size_t e) {
         dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
-        if (q.d2 < P.reL2 && sideOK(sc, pj, q.d2)) {
-            double dst = sqrt(q.d2);
-            double wL = wfun(dst, P.reL, P.weightType);
-            if (fi && d.type[j] == P.fluid) {
-                double pgh = -2.0 * (rho * rho / (rho + rho)) *
-                             (P.gravity[0] * q.v0 + P.gravity[1] * q.v1 + P.gravity[2] * q.v2);
-                Di += P.timeStep / rho * P.coeffViscMultiphase * (d.press[j] - Pi - pgh) * wL;
-            }
-            if (q.d2 < P.reS2) {
-                dvec4 vj = d.vel[j];
-                double vx = vj.x - vi.x, vy = vj.y - vi.y, vz = vj.z - vi.z;
-                double wS = wfun(dst, P.reS, P.weightType);
-                if (!P.gradientCorrection) {
-                    DivV += cdiv * (d.pndi[j] / ni) * (vx * q.v0 + vy * q.v1 + vz * q.v2) * wS / q.d2;
-                } else {
-                    double a0 = q.v0 * C1.x + q.v1 * C1.y + q.v2 * C1.z;
-                    double a1 = q.v0 * C2.x + q.v1 * C2.y + q.v2 * C2.z;
-                    double a2 = q.v0 * C3.x + q.v1 * C3.y + q.v2 * C3.z;
-                    DivV += cdiv * (vx * a0 + vy * a1 + vz * a2) * wS / q.d2;
-                }
+        double v0 = pj.x - pi.x, v1 = pj.y - pi.y, v2 = pj.z - pi.z;
+        double wL = wLc[e];
+        if (fi && d.type[j] == P.fluid) {
+            double pgh = -2.0 * (rho * rho / (rho + rho)) * (P.gravity[0] * v0 + P.gravity[1] * v1 + P.gravity[2] * v2);
+            Di += P.timeStep / rho * P.coeffViscMultiphase * (d.press[j] - Pi - pgh) * wL;
+        }
+        int k = (int)((e - i) / d.N0);
+        if ((mS >> k) & 1ull) {
+            dvec4 vj = d.vel[j];
+            double vx = vj.x - vi.x, vy = vj.y - vi.y, vz = vj.z - vi.z;
+            double wd = d.cwd[e];   // wS / r^2
+            if (!P.gradientCorrection) {
+                DivV += cdiv * (d.pndi[j] * invNi) * (vx * v0 + vy * v1 + vz * v2) * wd;
+            } else {
+                double a0 = v0 * C1.x + v1 * C1.y + v2 * C1.z;
+                double a1 = v0 * C2.x + v1 * C2.y + v2 * C2.z;
+                double a2 = v0 * C3.x + v1 * C3.y + v2 * C3.z;
+                DivV += cdiv * (vx * a0 + vy * a1 + vz * a2) * wd;
             }
         }
     });
@@ -371,11 +362,11 @@ __global__ void __launch_bounds__(BLK) k_pnd_diffusive(Dev d) {
 // MpsPndNeigh::calcWallSlipPndDiffusiveTerm / calcWallNoSlipPndDiffusiveTerm,
 // src/MpsPndNeigh.cpp:492-744 (fixed wall: wall velocity zero)
 __global__ void __launch_bounds__(BLK) k_wall_pnd_diffusive(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
+    int i = nearIndex(d);
+    if (i < 0) return;
     const MpsParams& P = d.P;
     double ni = d.pndi[i];
-    if (!(d.type[i] == P.fluid && d.nearWall[i] && ni > P.epsilonZero)) return;
+    if (!(ni > P.epsilonZero)) return;
     bool noslip = P.slipCondition == 0;
     dvec4 pi = d.pos[i], vi = d.vel[i], mi = d.mirror[i];
     ReflG r = makeRefl(pi, mi, P.epsilonZero, false);
@@ -430,15 +421,9 @@ __global__ void __launch_bounds__(BLK) k_mean_pnd_wds(Dev d) {
     const MpsParams& P = d.P;
     double up = 0.0, dn = 0.0;
     if (d.type[i] == P.wall || d.bc[i] == P.surface) {
-        dvec4 pi = d.pos[i];
-        SideCtx sc = sideCtx(d, i, pi);
-        forNbrs(d, i, [&](int j) {
-            dvec4 pj = d.pos[j];
-            PairG q = pairOf(pj, pi);
-            if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
-                double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
-                up += d.pndi[j] * wS; dn += wS;
-            }
+        forMask(d, i, d.maskS[i], [&](int j, size_t e) {
+            double wS = d.cw[e];
+            up += d.pndi[j] * wS; dn += wS;
         });
     }
     d.aux1[i] = up; d.aux2[i] = dn;
@@ -494,17 +479,10 @@ __global__ void __launch_bounds__(BLK) k_mean_wall_pnd(Dev d) {
 __global__ void __launch_bounds__(BLK) k_mean_pnd(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
-    const MpsParams& P = d.P;
-    dvec4 pi = d.pos[i];
-    SideCtx sc = sideCtx(d, i, pi);
     double up = 0.0, dn = 0.0;
-    forNbrs(d, i, [&](int j) {
-        dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
-        if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
-            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
-            up += d.pndi[j] * wS; dn += wS;
-        }
+    forMask(d, i, d.maskS[i], [&](int j, size_t e) {
+        double wS = d.cw[e];
+        up += d.pndi[j] * wS; dn += wS;
     });
     d.aux1[i] += up; d.aux2[i] += dn;
 }
@@ -520,16 +498,11 @@ __global__ void __launch_bounds__(BLK) k_mean_neigh_fluid_pnd(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
-    dvec4 pi = d.pos[i];
-    SideCtx sc = sideCtx(d, i, pi);
     double up = 0.0, dn = 0.0;
-    forNbrs(d, i, [&](int j) {
-        dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
-        if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2) && d.type[j] == P.fluid) {
-            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
-            up += d.pndki[j] * wS; dn += wS;
-        }
+    forMask(d, i, d.maskS[i], [&](int j, size_t e) {
+        if (d.type[j] != P.fluid) return;
+        double wS = d.cw[e];
+        up += d.pndki[j] * wS; dn += wS;
     });
     d.pndski[i] = (dn > P.epsilonZero) ? up / dn : up;
 }
@@ -591,14 +564,14 @@ __global__ void __launch_bounds__(BLK) k_extrapolate(Dev d) {
     if (!(d.type[i] == P.dummyWall || (P.mpsType == 1 && d.type[i] == P.wall))) return;
     dvec4 pi = d.pos[i];
     double ni = 0.0, pr = 0.0;
-    forNbrs(d, i, [&](int j) {
+    // particle walls: maskS is exactly dst^2 < reS^2 (no mirror side test)
+    forMask(d, i, d.maskS[i], [&](int j, size_t e) {
+        if (d.type[j] != P.fluid) return;
         dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
-        if (q.d2 < P.reS2 && d.type[j] == P.fluid) {
-            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
-            ni += wS;
-            pr += (d.press[j] - P.DNS_FL1 * (P.gravity[0] * q.v0 + P.gravity[1] * q.v1 + P.gravity[2] * q.v2)) * wS;
-        }
+        double v0 = pj.x - pi.x, v1 = pj.y - pi.y, v2 = pj.z - pi.z;
+        double wS = d.cw[e];
+        ni += wS;
+        pr += (d.press[j] - P.DNS_FL1 * (P.gravity[0] * v0 + P.gravity[1] * v1 + P.gravity[2] * v2)) * wS;
     });
     if (pr < 0.0) return;
     d.press[i] = (ni > 0) ? pr / ni : pr;
@@ -612,40 +585,35 @@ __global__ void __launch_bounds__(BLK) k_press_grad(Dev d) {
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     dvec4 pi = d.pos[i];
-    SideCtx sc = sideCtx(d, i, pi);
     double Pi = d.press[i], pmin = Pi, ni = d.pndi[i];
     int gt = P.gradientType;
+    unsigned long long mS = d.maskS[i];
     if (gt == 0 || gt == 2) {
-        forNbrs(d, i, [&](int j) {
-            dvec4 pj = d.pos[j];
-            PairG q = pairOf(pj, pi);
-            if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
-                double pj_ = d.press[j];
-                if (pmin > pj_) pmin = pj_;
-            }
+        forMask(d, i, mS, [&](int j, size_t e) {
+            double pj_ = d.press[j];
+            if (pmin > pj_) pmin = pj_;
         });
     }
     dvec4 C1 = d.c1[i], C2 = d.c2[i], C3 = d.c3[i];
     double ax = 0, ay = 0, az = 0;
-    forNbrs(d, i, [&](int j) {
+    forMask(d, i, mS, [&](int j, size_t e) {
         dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
-        if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) {
-            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
-            double Pj = d.press[j];
-            if (gt == 0) wS *= (Pj - pmin) / q.d2;
-            else if (gt == 1) wS *= (Pj + Pi) / q.d2;
-            else if (gt == 2) wS *= (Pj + Pi - 2.0 * pmin) / q.d2;
-            else if (gt == 3) {
-                double nj = d.pndi[j];
-                if (ni > P.epsilonZero && nj > P.epsilonZero) wS *= (ni * Pj / nj + nj * Pi / ni) / q.d2;
-            }
-            if (!P.gradientCorrection) { ax += q.v0 * wS; ay += q.v1 * wS; az += q.v2 * wS; }
-            else {
-                ax += (q.v0 * C1.x + q.v1 * C1.y + q.v2 * C1.z) * wS;
-                ay += (q.v0 * C2.x + q.v1 * C2.y + q.v2 * C2.z) * wS;
-                az += (q.v0 * C3.x + q.v1 * C3.y + q.v2 * C3.z) * wS;
-            }
+        double v0 = pj.x - pi.x, v1 = pj.y - pi.y, v2 = pj.z - pi.z;
+        double Pj = d.press[j];
+        double wd = d.cwd[e];   // wS / r^2
+        double f;
+        if (gt == 0) f = (Pj - pmin) * wd;
+        else if (gt == 1) f = (Pj + Pi) * wd;
+        else if (gt == 2) f = (Pj + Pi - 2.0 * pmin) * wd;
+        else {
+            double nj = d.pndi[j];
+            f = (ni > P.epsilonZero && nj > P.epsilonZero) ? (ni * Pj / nj + nj * Pi / ni) * wd : d.cw[e];
+        }
+        if (!P.gradientCorrection) { ax += v0 * f; ay += v1 * f; az += v2 * f; }
+        else {
+            ax += (v0 * C1.x + v1 * C1.y + v2 * C1.z) * f;
+            ay += (v0 * C2.x + v1 * C2.y + v2 * C2.z) * f;
+            az += (v0 * C3.x + v1 * C3.y + v2 * C3.z) * f;
         }
     });
     d.acc[i] = make_dvec4(P.relaxPress * ax * P.coeffPressGrad / P.DNS_FL1,
@@ -656,10 +624,9 @@ void launchPressGradient(const Dev& d, cudaStream_t s) { k_press_grad<<<gridFor(
 
 // MpsPressure::calcWallPressGradient + repulsive forces, src/MpsPressure.cpp:1341-1611
 __global__ void __launch_bounds__(BLK) k_wall_press_grad(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
+    int i = nearIndex(d);
+    if (i < 0) return;
     const MpsParams& P = d.P;
-    if (!(d.type[i] == P.fluid && d.nearWall[i])) return;
     // min(velMax of the last corrector, expected maximum velocity)^2 (src/MpsPressure.cpp:1342-1344)
     double vm = fmin(*d.velMax, P.expectMaxVelocity);
     double vMax2 = vm * vm;
@@ -741,10 +708,9 @@ void launchWallPressGradient(const Dev& d, cudaStream_t s) {
 // MpsViscosity::calcWallNoSlipViscosity / calcWallSlipViscosity (Newtonian, fixed wall),
 // src/MpsViscosity.cpp:1527-1910
 __global__ void __launch_bounds__(BLK) k_wall_visc(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
+    int i = nearIndex(d);
+    if (i < 0) return;
     const MpsParams& P = d.P;
-    if (!(d.type[i] == P.fluid && d.nearWall[i])) return;
     bool noslip = P.slipCondition == 0;
     dvec4 pi = d.pos[i], vi = d.vel[i], mi = d.mirror[i];
     ReflG r = makeRefl(pi, mi, P.epsilonZero, false);
@@ -846,9 +812,7 @@ __global__ void __launch_bounds__(BLK) k_shift_vel(Dev d) {
     if (d.type[i] == P.fluid) {
         dvec4 pi = d.pos[i], vi = d.vel[i];
         SideCtx sc = sideCtx(d, i, pi);
-        forCells(d, pi, [&](int j) {
-            dvec4 pj = d.pos[j];
-            PairG q = pairOf(pj, pi);
+        forCellsNear(d, pi, d.posf[i], d.bandHiS, [&](int j, dvec4 pj, PairG q) {
             if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) {
                 double dw = dwfun(sqrt(q.d2), P.reS, P.weightType);
                 dvec4 vj = d.vel[j];
@@ -876,10 +840,12 @@ __global__ void __launch_bounds__(BLK) k_conc(Dev d) {
     dvec4 pi = d.pos[i];
     SideCtx sc = sideCtx(d, i, pi);
     double c = 0.0;
-    forCells(d, pi, [&](int j) {
-        dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
-        if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) c += wfun(sqrt(q.d2), P.reS, P.weightType);
+    forCellsNear(d, pi, d.posf[i], d.bandHiS, [&](int j, dvec4 pj, PairG q) {
+        if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) {
+            double w, wd;
+            weightR(q.d2, P.reS, P.weightType, w, wd);
+            c += w;
+        }
     });
     c += d.pndWall[i];
     d.conc[i] = c / P.pndSmallZero;
@@ -894,13 +860,12 @@ __global__ void __launch_bounds__(BLK) k_grad_conc(Dev d) {
         SideCtx sc = sideCtx(d, i, pi);
         double ci = d.conc[i];
         double gx = 0, gy = 0, gz = 0;
-        forCells(d, pi, [&](int j) {
-            dvec4 pj = d.pos[j];
-            PairG q = pairOf(pj, pi);
+        forCellsNear(d, pi, d.posf[i], d.bandHiS, [&](int j, dvec4 pj, PairG q) {
             if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) {
-                double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
-                double cc = ci + d.conc[j];
-                gx += cc * q.v0 * wS / q.d2; gy += cc * q.v1 * wS / q.d2; gz += cc * q.v2 * wS / q.d2;
+                double wS, wd;
+                weightR(q.d2, P.reS, P.weightType, wS, wd);
+                double cc = (ci + d.conc[j]) * wd;
+                gx += cc * q.v0; gy += cc * q.v1; gz += cc * q.v2;
             }
         });
         gx *= -P.coeffPressGrad; gy *= -P.coeffPressGrad; gz *= -P.coeffPressGrad;
@@ -921,9 +886,7 @@ __global__ void __launch_bounds__(BLK) k_wall_grad_conc(Dev d) {
         double ci = d.conc[i];
         ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
         double dx = 0, dy = 0, dz = 0;
-        forCells(d, pi, [&](int j) {
-            dvec4 pj = d.pos[j];
-            PairG q = pairOf(pj, pi);
+        forCellsNear(d, pi, d.posf[i], d.bandHiS, [&](int j, dvec4 pj, PairG q) {
             if (q.d2 < P.reS2 && j != i) {
                 PairM m = pairMirror(pj, mi);
                 if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
@@ -949,15 +912,19 @@ __global__ void __launch_bounds__(BLK) k_wall_grad_conc(Dev d) {
     }
     d.shift[i] = sh;
 }
+// x += shift; the FP32 copy follows the new positions (next prefiltered scan)
 __global__ void k_apply_shift(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     dvec4 x = d.pos[i], s = d.shift[i];
     x.x += s.x; x.y += s.y; x.z += s.z;
     d.pos[i] = x;
+    d.posf[i] = make_float4((float)(x.x - d.P.domainMin[0]), (float)(x.y - d.P.domainMin[1]),
+                            (float)(x.z - d.P.domainMin[2]), 0.f);
 }
 void launchShifting(const Dev& d, cudaStream_t s) {
     const MpsParams& P = d.P;
+    launchPosf(d, s);   // post-corrector positions
     if (P.shiftingType == 1) {
         k_shift_vel<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
         k_shift_vel_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
@@ -982,11 +949,10 @@ __global__ void __launch_bounds__(BLK) k_dummy_vel(Dev d) {
     if (d.type[i] != P.dummyWall) return;
     dvec4 pi = d.pos[i];
     double ni = 0.0, ux = 0, uy = 0, uz = 0;
-    forCells(d, pi, [&](int j) {
-        dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
+    forCellsNear(d, pi, d.posf[i], d.bandHiL, [&](int j, dvec4 pj, PairG q) {
         if (q.d2 < P.reL2 && j != i && d.type[j] == P.fluid) {
-            double wL = wfun(sqrt(q.d2), P.reL, P.weightType);
+            double wL, wd;
+            weightR(q.d2, P.reL, P.weightType, wL, wd);
             dvec4 vj = d.vel[j];
             ni += wL;
             ux += vj.x * wL; uy += vj.y * wL; uz += vj.z * wL;
@@ -999,5 +965,6 @@ __global__ void __launch_bounds__(BLK) k_dummy_vel(Dev d) {
 }
 void launchDummyVelocity(const Dev& d, cudaStream_t s) {
     if (d.P.wallType != 0) return;
+    launchPosf(d, s);
     k_dummy_vel<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
 }

@@ -35,26 +35,24 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
         return;
     }
     dvec4 pi = d.pos[i];
-    SideCtx sc = sideCtx(d, i, pi);
     double sum = 0.0, src = 0.0;
     int len = 0;
-    forNbrs(d, i, [&](int j) {
-        dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
-        if (q.d2 < P.reL2 && sideOK(sc, pj, q.d2)) {
-            double wL = wfun(sqrt(q.d2), P.reL, P.weightType);
-            double mij = wL * P.coeffPPE;
-            if (d.type[j] == P.dummyWall) {
-                double pgh = P.DNS_FL1 * (q.v0 * P.gravity[0] + q.v1 * P.gravity[1] + q.v2 * P.gravity[2]) * wL;
-                src -= P.coeffPPE * pgh;
-            } else {
-                sum -= mij;
-                if (d.bc[j] == P.inner) {
-                    size_t k = (size_t)len * B.N0 + i;
-                    B.val[k] = mij;
-                    B.col[k] = j;
-                    len++;
-                }
+    const double* wLc = d.cwL ? d.cwL : d.cw;
+    forMask(d, i, d.maskL[i], [&](int j, size_t e) {
+        double wL = wLc[e];
+        double mij = wL * P.coeffPPE;
+        if (d.type[j] == P.dummyWall) {
+            dvec4 pj = d.pos[j];
+            double v0 = pj.x - pi.x, v1 = pj.y - pi.y, v2 = pj.z - pi.z;
+            double pgh = P.DNS_FL1 * (v0 * P.gravity[0] + v1 * P.gravity[1] + v2 * P.gravity[2]) * wL;
+            src -= P.coeffPPE * pgh;
+        } else {
+            sum -= mij;
+            if (d.bc[j] == P.inner) {
+                size_t k = (size_t)len * B.N0 + i;
+                B.val[k] = mij;
+                B.col[k] = j;
+                len++;
             }
         }
     });

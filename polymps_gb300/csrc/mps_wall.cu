@@ -53,6 +53,36 @@ __device__ void closestPtTriX(double px, double py, double pz, const double* t, 
     qz = xadd(xadd(az, xmul(abz, v)), xmul(acz, w));
 }
 
+// FP32 version of the same walk: only used to pick the triangles that need the exact one.
+__device__ float sqDistTriF(float px, float py, float pz, const float* t) {
+    float ax = t[0], ay = t[1], az = t[2], bx = t[3], by = t[4], bz = t[5], cx = t[6], cy = t[7], cz = t[8];
+    float abx = bx - ax, aby = by - ay, abz = bz - az, acx = cx - ax, acy = cy - ay, acz = cz - az;
+    float apx = px - ax, apy = py - ay, apz = pz - az;
+    float d1 = abx * apx + aby * apy + abz * apz, d2 = acx * apx + acy * apy + acz * apz;
+    float qx, qy, qz;
+    float bpx = px - bx, bpy = py - by, bpz = pz - bz;
+    float d3 = abx * bpx + aby * bpy + abz * bpz, d4 = acx * bpx + acy * bpy + acz * bpz;
+    float cpx = px - cx, cpy = py - cy, cpz = pz - cz;
+    float d5 = abx * cpx + aby * cpy + abz * cpz, d6 = acx * cpx + acy * cpy + acz * cpz;
+    float vc = d1 * d4 - d3 * d2, vb = d5 * d2 - d1 * d6, va = d3 * d6 - d5 * d4;
+    if (d1 <= 0.f && d2 <= 0.f) { qx = ax; qy = ay; qz = az; }
+    else if (d3 >= 0.f && d4 <= d3) { qx = bx; qy = by; qz = bz; }
+    else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+        float v = d1 / (d1 - d3); qx = ax + v * abx; qy = ay + v * aby; qz = az + v * abz;
+    } else if (d6 >= 0.f && d5 <= d6) { qx = cx; qy = cy; qz = cz; }
+    else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+        float w = d2 / (d2 - d6); qx = ax + w * acx; qy = ay + w * acy; qz = az + w * acz;
+    } else if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+        float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        qx = bx + w * (cx - bx); qy = by + w * (cy - by); qz = bz + w * (cz - bz);
+    } else {
+        float den = 1.f / (va + vb + vc), v = vb * den, w = vc * den;
+        qx = ax + abx * v + acx * w; qy = ay + aby * v + acy * w; qz = az + abz * v + acz * w;
+    }
+    float dx = px - qx, dy = py - qy, dz = pz - qz;
+    return dx * dx + dy * dy + dz * dz;
+}
+
 // PolygonMesh::interpolateWij / interpolateNumNeighWall (src/PolygonMesh.cpp:533-581),
 // linear interpolation with extrapolation over the 50-sample tables
 __device__ double interpTab(const double* xs, const double* ys, double re, double x) {
@@ -67,18 +97,34 @@ __device__ double interpTab(const double* xs, const double* ys, double re, doubl
 
 __global__ void __launch_bounds__(128) k_wall_distance(Dev d) {
     __shared__ double sTri[MPS_MAX_TRI * 9];
+    __shared__ float sTriF[MPS_MAX_TRI * 9];
     __shared__ double sTab[4 * MPS_TAB];
-    for (int k = threadIdx.x; k < d.ntri * 9; k += blockDim.x) sTri[k] = d.tri[k];
+    for (int k = threadIdx.x; k < d.ntri * 9; k += blockDim.x) {
+        sTri[k] = d.tri[k];
+        sTriF[k] = (float)(d.tri[k] - d.P.domainMin[k % 3]);
+    }
     for (int k = threadIdx.x; k < 4 * MPS_TAB; k += blockDim.x) sTab[k] = d.tab[k];
     __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     dvec4 p = d.pos[i];
+    // FP32 pass over all triangles (coordinates relative to the domain corner)
+    float pxf = (float)(p.x - P.domainMin[0]), pyf = (float)(p.y - P.domainMin[1]), pzf = (float)(p.z - P.domainMin[2]);
+    float df[MPS_MAX_TRI];
+    float bestf = 3.0e38f;
+    for (int t = 0; t < d.ntri; t++) {
+        df[t] = sqDistTriF(pxf, pyf, pzf, sTriF + t * 9);
+        bestf = fminf(bestf, df[t]);
+    }
+    // exact FP64 walk for every triangle that can hold (or tie) the minimum: the FP32
+    // squared distances are within ~1e-5 m^2 of the exact ones for domains of a few metres
+    float lim = bestf + 1e-4f + 1e-5f * bestf;
     double best = 1.0 / 0.0;
     int bt = -1;
     double bx = 0, by = 0, bz = 0;
     for (int t = 0; t < d.ntri; t++) {
+        if (df[t] > lim) continue;
         double qx, qy, qz;
         closestPtTriX(p.x, p.y, p.z, sTri + t * 9, qx, qy, qz);
         double dx = xsub(p.x, qx), dy = xsub(p.y, qy), dz = xsub(p.z, qz);

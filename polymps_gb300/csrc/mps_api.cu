@@ -92,6 +92,7 @@ void Prof::destroy() {
 static int opLaunches(int op, const MpsParams& P) {
     switch (op) {
         case MPS_OP_UPDATE_BUCKETS: return 6;
+        case MPS_OP_VISCOSITY: return 8;
         case MPS_OP_OUT_OF_DOMAIN: return 2;
         case MPS_OP_COLLISION: return 2;
         case MPS_OP_WALL_DISTANCE: case MPS_OP_WALL_NPCD: case MPS_OP_WALL_PRESS_GRADIENT:
@@ -149,9 +150,9 @@ static int launchStatus() {
 static void ensureList(mpsgpu_t h) {
     if (h->listValid) return;
     if (h->prof.on) h->prof.begin(PROF_NEIGHBOR_LIST, h->s);
-    launchNeighborList(h->d, h->s);
+    launchNeighborList(h->d, h->scanScratch, h->s);
     if (h->prof.on) h->prof.end(h->s);
-    countLaunch(2);
+    countLaunch(9);   // posf, query buckets (key, 3 scan, scatter, list), staged scan + fallback
     h->listValid = true;
     h->masksValid = false;
 }
@@ -250,7 +251,7 @@ static int runOpBody(mpsgpu_t h, int op) {
     auto invalidate = [&]() { h->listValid = false; h->masksValid = false; };
     switch (op) {
         case MPS_OP_UPDATE_BUCKETS: launchBuckets(d, h->scanScratch, s); invalidate(); break;
-        case MPS_OP_VISCOSITY: launchViscosity(d, s); break;
+        case MPS_OP_VISCOSITY: launchViscosity(d, h->scanScratch, s); break;
         case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
         case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
         case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); invalidate(); break;
@@ -420,6 +421,15 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.cellCount, d.nB + 1);
     A(d.cellCursor, d.nB + 1);
     A(d.cellSorted, n);
+    A(d.qOf, n);
+    A(d.qCount, d.nB + 1);
+    A(d.qStart, d.nB + 1);
+    A(d.qCursor, d.nB + 1);
+    A(d.qSorted, n);
+    A(d.qList, d.nB);
+    A(d.qNum, 1);
+    A(d.strayList, n);
+    A(d.strayNum, 1);
     A(d.nbrCount, n);
     A(d.nbr, (size_t)d.K * n);
     A(d.cw, (size_t)d.K * n);

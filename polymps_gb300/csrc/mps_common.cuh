@@ -46,6 +46,9 @@ struct Dev {
     float4* posf;      // FP32 copy of pos - domainMin (neighbour prefilter, FP32 sums)
     // buckets (stale list of the step)
     int *cellOf, *cellStart, *cellCount, *cellSorted, *cellCursor;
+    // query buckets: particles grouped by the bucket of their current position
+    // (bucketCoordinates), for the warp-per-bucket staged scans
+    int *qOf, *qCount, *qStart, *qCursor, *qSorted, *qList, *qNum, *strayList, *strayNum;
     // neighbour list (ELL) and its per-entry cache for the epoch: w(r; reS), w/r^2,
     // w(r; reL) (only when reL != reS)
     int *nbrCount, *nbr;

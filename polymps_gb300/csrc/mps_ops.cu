@@ -8,37 +8,46 @@
 // with the distance comparisons evaluated in exact FP64 (see mps_common.cuh).
 #include "mps_common.cuh"
 #include "mps_internal.h"
+#include "mps_cellscan.cuh"
 
 #define BLK 128
 
 // ------------------------------------------------------------------ viscosity
 // MpsViscosity::calcViscosity, src/MpsViscosity.cpp:20-100 (Newtonian: MEU and RHO are
-// uniform, src/MpsInputOutput.cpp:833-838, so the harmonic mean is hoisted).
-__global__ void __launch_bounds__(BLK) k_viscosity(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
-    const MpsParams& P = d.P;
-    double mu = P.KNM_VS1 * P.DNS_FL1, rho = P.DNS_FL1;
-    double neuF = (2.0 * mu * mu / (mu + mu)) / rho;
-    double neuW = (2.0 * mu) / rho;
-    dvec4 pi = d.pos[i], vi = d.vel[i];
-    SideCtx sc = sideCtx(d, i, pi);
-    double ax = 0, ay = 0, az = 0;
-    forCellsNear(d, pi, d.posf[i], d.bandHiL, [&](int j, dvec4 pj, PairG q) {
-        if (q.d2 < P.reL2 && j != i && sideOK(sc, pj, q.d2)) {
-            double wL, wd;
-            weightR(q.d2, P.reL, P.weightType, wL, wd);
-            double neu = (d.type[j] == P.wall) ? neuW : neuF;
-            dvec4 vj = d.vel[j];
-            ax += (vj.x - vi.x) * wL * neu;
-            ay += (vj.y - vi.y) * wL * neu;
-            az += (vj.z - vi.z) * wL * neu;
-        }
-    });
-    d.acc[i] = make_dvec4(P.coeffViscMultiphase * ax, P.coeffViscMultiphase * ay,
-                            P.coeffViscMultiphase * az, 0.0);
+// uniform, src/MpsInputOutput.cpp:833-838, so the harmonic mean is hoisted).  Staged scan
+// at the start-of-step positions; FP32 prefilter, exact FP64 radius/side tests.
+struct OpViscosity {
+    struct State { dvec4 pi, vi; float4 fi; SideCtx sc; double ax, ay, az; };
+    __device__ void begin(const Dev& d, int i, State& st) const {
+        st.pi = d.pos[i]; st.vi = d.vel[i]; st.fi = d.posf[i];
+        st.sc = sideCtx(d, i, st.pi);
+        st.ax = st.ay = st.az = 0.0;
+    }
+    __device__ void visit(const Dev& d, int i, State& st, int j, float4 fj) const {
+        float dx = fj.x - st.fi.x, dy = fj.y - st.fi.y, dz = fj.z - st.fi.z;
+        if (dx * dx + dy * dy + dz * dz > d.bandHiL || j == i) return;
+        const MpsParams& P = d.P;
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, st.pi);
+        if (!(q.d2 < P.reL2) || !sideOK(st.sc, pj, q.d2)) return;
+        double mu = P.KNM_VS1 * P.DNS_FL1, rho = P.DNS_FL1;
+        double neu = (d.type[j] == P.wall) ? (2.0 * mu) / rho : (2.0 * mu * mu / (mu + mu)) / rho;
+        double wL, wd;
+        weightR(q.d2, P.reL, P.weightType, wL, wd);
+        dvec4 vj = d.vel[j];
+        st.ax += (vj.x - st.vi.x) * wL * neu;
+        st.ay += (vj.y - st.vi.y) * wL * neu;
+        st.az += (vj.z - st.vi.z) * wL * neu;
+    }
+    __device__ void end(const Dev& d, int i, State& st) const {
+        double c = d.P.coeffViscMultiphase;
+        d.acc[i] = make_dvec4(c * st.ax, c * st.ay, c * st.az, 0.0);
+    }
+};
+void launchViscosity(const Dev& d, int* scanScratch, cudaStream_t s) {
+    launchQueryCells(d, scanScratch, s);
+    launchCellScan(d, OpViscosity(), s);
 }
-void launchViscosity(const Dev& d, cudaStream_t s) { k_viscosity<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
 
 // MpsParticle::addGravity, src/MpsParticle.cpp:111-130
 __global__ void k_add_gravity(Dev d) {

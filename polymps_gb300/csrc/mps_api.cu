@@ -101,8 +101,9 @@ static int opLaunches(int op, const MpsParams& P) {
         case MPS_OP_PND_MEAN: return P.wallType == 1 ? 3 : 2;
         case MPS_OP_INIT_PND: return 2 + (P.wallType == 1 ? 3 : 2);
         case MPS_OP_CALC_PRESS: return (P.mpsType == 2) ? 2 : 1;   // assemble + copy back | EOS
-        case MPS_OP_SHIFTING: return P.shiftingType == 1 ? 2 : (P.shiftingType == 2 ? (P.wallType == 1 ? 5 : 3) : 0);
-        case MPS_OP_DUMMY_VELOCITY: return P.wallType == 0 ? 1 : 0;
+        case MPS_OP_SHIFTING:   // posf + query buckets (6) + staged scans (2 each) + apply kernels
+            return P.shiftingType == 1 ? 10 : (P.shiftingType == 2 ? (P.wallType == 1 ? 15 : 13) : 0);
+        case MPS_OP_DUMMY_VELOCITY: return P.wallType == 0 ? 2 : 0;
         default: return 1;
     }
 }
@@ -269,7 +270,7 @@ static int runOpBody(mpsgpu_t h, int op) {
         case MPS_OP_WALL_PRESS_GRADIENT: ensureMasks(h); launchWallPressGradient(d, s); break;
         case MPS_OP_WALL_VISCOSITY: ensureMasks(h); launchWallViscosity(d, s); break;
         case MPS_OP_CORRECT: launchCorrect(d, s); invalidate(); break;
-        case MPS_OP_SHIFTING: launchShifting(d, s); if (P.shiftingType == 2) invalidate(); break;
+        case MPS_OP_SHIFTING: launchShifting(d, h->scanScratch, s); if (P.shiftingType == 2) invalidate(); break;
         case MPS_OP_DUMMY_VELOCITY: launchDummyVelocity(d, s); break;
         case MPS_OP_INIT_PND: ensureMasks(h); launchInitPnd(d, s); break;
         default: g_lastError = "unknown operator"; return MPSGPU_ERR_ARG;

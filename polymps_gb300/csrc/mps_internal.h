@@ -57,7 +57,7 @@ void launchPressGradient(const Dev& d, cudaStream_t s);
 void launchWallPressGradient(const Dev& d, cudaStream_t s);
 void launchWallViscosity(const Dev& d, cudaStream_t s);
 void launchCorrect(const Dev& d, cudaStream_t s);
-void launchShifting(const Dev& d, cudaStream_t s);
+void launchShifting(const Dev& d, int* scanScratch, cudaStream_t s);
 void launchDummyVelocity(const Dev& d, cudaStream_t s);
 
 // mps_wall.cu

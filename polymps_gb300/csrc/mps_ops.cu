@@ -813,25 +813,42 @@ void launchCorrect(const Dev& d, cudaStream_t s) {
 // ------------------------------------------------------------------ shifting
 // MpsShifting::calcShifting (type 1), src/MpsShifting.cpp:23-101: dv from the
 // pre-shift velocities, then applied.
-__global__ void __launch_bounds__(BLK) k_shift_vel(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
-    const MpsParams& P = d.P;
-    dvec4 du = make_dvec4(0, 0, 0, 0);
-    if (d.type[i] == P.fluid) {
-        dvec4 pi = d.pos[i], vi = d.vel[i];
-        SideCtx sc = sideCtx(d, i, pi);
-        forCellsNear(d, pi, d.posf[i], d.bandHiS, [&](int j, dvec4 pj, PairG q) {
-            if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) {
-                double dw = dwfun(sqrt(q.d2), P.reS, P.weightType);
-                dvec4 vj = d.vel[j];
-                du.x += dw * (vj.x - vi.x); du.y += dw * (vj.y - vi.y); du.z += dw * (vj.z - vi.z);
-            }
-        });
-        if (d.bc[i] != P.inner) du = make_dvec4(0, 0, 0, 0);
+// Common head of the post-corrector staged scans: FP32 prefilter on the reS ball, exact
+// FP64 radius and mirror-side tests.
+struct E2Base {
+    struct Core { dvec4 pi; float4 fi; SideCtx sc; bool on; };
+    __device__ static void start(const Dev& d, int i, Core& c, bool on) {
+        c.on = on;
+        c.pi = d.pos[i]; c.fi = d.posf[i];
+        c.sc = sideCtx(d, i, c.pi);
     }
-    d.shift[i] = du;
-}
+    __device__ static bool accept(const Dev& d, int i, const Core& c, int j, float4 fj, dvec4& pj, PairG& q) {
+        if (!c.on || j == i) return false;
+        float dx = fj.x - c.fi.x, dy = fj.y - c.fi.y, dz = fj.z - c.fi.z;
+        if (dx * dx + dy * dy + dz * dz > d.bandHiS) return false;
+        pj = d.pos[j];
+        q = pairOf(pj, c.pi);
+        return q.d2 < d.P.reS2 && sideOK(c.sc, pj, q.d2);
+    }
+};
+struct OpShiftVel {
+    struct State { E2Base::Core c; dvec4 vi; double ux, uy, uz; };
+    __device__ void begin(const Dev& d, int i, State& st) const {
+        E2Base::start(d, i, st.c, d.type[i] == d.P.fluid);
+        st.vi = d.vel[i]; st.ux = st.uy = st.uz = 0.0;
+    }
+    __device__ void visit(const Dev& d, int i, State& st, int j, float4 fj) const {
+        dvec4 pj; PairG q;
+        if (!E2Base::accept(d, i, st.c, j, fj, pj, q)) return;
+        double dw = dwfun(sqrt(q.d2), d.P.reS, d.P.weightType);
+        dvec4 vj = d.vel[j];
+        st.ux += dw * (vj.x - st.vi.x); st.uy += dw * (vj.y - st.vi.y); st.uz += dw * (vj.z - st.vi.z);
+    }
+    __device__ void end(const Dev& d, int i, State& st) const {
+        bool apply = st.c.on && d.bc[i] == d.P.inner;
+        d.shift[i] = apply ? make_dvec4(st.ux, st.uy, st.uz, 0.0) : make_dvec4(0, 0, 0, 0);
+    }
+};
 __global__ void k_shift_vel_apply(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
@@ -842,48 +859,46 @@ __global__ void k_shift_vel_apply(Dev d) {
 }
 // MpsShifting::calcConcAndConcGradient, src/MpsShifting.cpp:432-575: concentration, then
 // gradient and position shift (each sweep reads the positions it started with).
-__global__ void __launch_bounds__(BLK) k_conc(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
-    const MpsParams& P = d.P;
-    dvec4 pi = d.pos[i];
-    SideCtx sc = sideCtx(d, i, pi);
-    double c = 0.0;
-    forCellsNear(d, pi, d.posf[i], d.bandHiS, [&](int j, dvec4 pj, PairG q) {
-        if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) {
-            double w, wd;
-            weightR(q.d2, P.reS, P.weightType, w, wd);
-            c += w;
-        }
-    });
-    c += d.pndWall[i];
-    d.conc[i] = c / P.pndSmallZero;
-}
-__global__ void __launch_bounds__(BLK) k_grad_conc(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
-    const MpsParams& P = d.P;
-    dvec4 sh = make_dvec4(0, 0, 0, 0);
-    if (d.type[i] == P.fluid) {
-        dvec4 pi = d.pos[i];
-        SideCtx sc = sideCtx(d, i, pi);
-        double ci = d.conc[i];
-        double gx = 0, gy = 0, gz = 0;
-        forCellsNear(d, pi, d.posf[i], d.bandHiS, [&](int j, dvec4 pj, PairG q) {
-            if (q.d2 < P.reS2 && j != i && sideOK(sc, pj, q.d2)) {
-                double wS, wd;
-                weightR(q.d2, P.reS, P.weightType, wS, wd);
-                double cc = (ci + d.conc[j]) * wd;
-                gx += cc * q.v0; gy += cc * q.v1; gz += cc * q.v2;
-            }
-        });
-        gx *= -P.coeffPressGrad; gy *= -P.coeffPressGrad; gz *= -P.coeffPressGrad;
-        d.gradC[i] = make_dvec4(gx, gy, gz, 0.0);
-        if (d.bc[i] == P.inner)
-            sh = make_dvec4(-P.coeffShifting2 * gx, -P.coeffShifting2 * gy, -P.coeffShifting2 * gz, 0.0);
+struct OpConc {
+    struct State { E2Base::Core c; double sum; };
+    __device__ void begin(const Dev& d, int i, State& st) const { E2Base::start(d, i, st.c, true); st.sum = 0.0; }
+    __device__ void visit(const Dev& d, int i, State& st, int j, float4 fj) const {
+        dvec4 pj; PairG q;
+        if (!E2Base::accept(d, i, st.c, j, fj, pj, q)) return;
+        double w, wd;
+        weightR(q.d2, d.P.reS, d.P.weightType, w, wd);
+        st.sum += w;
     }
-    d.shift[i] = sh;
-}
+    __device__ void end(const Dev& d, int i, State& st) const {
+        d.conc[i] = (st.sum + d.pndWall[i]) / d.P.pndSmallZero;
+    }
+};
+struct OpGradConc {
+    struct State { E2Base::Core c; double ci, gx, gy, gz; };
+    __device__ void begin(const Dev& d, int i, State& st) const {
+        E2Base::start(d, i, st.c, d.type[i] == d.P.fluid);
+        st.ci = d.conc[i]; st.gx = st.gy = st.gz = 0.0;
+    }
+    __device__ void visit(const Dev& d, int i, State& st, int j, float4 fj) const {
+        dvec4 pj; PairG q;
+        if (!E2Base::accept(d, i, st.c, j, fj, pj, q)) return;
+        double wS, wd;
+        weightR(q.d2, d.P.reS, d.P.weightType, wS, wd);
+        double cc = (st.ci + d.conc[j]) * wd;
+        st.gx += cc * q.v0; st.gy += cc * q.v1; st.gz += cc * q.v2;
+    }
+    __device__ void end(const Dev& d, int i, State& st) const {
+        const MpsParams& P = d.P;
+        dvec4 sh = make_dvec4(0, 0, 0, 0);
+        if (st.c.on) {
+            double gx = st.gx * -P.coeffPressGrad, gy = st.gy * -P.coeffPressGrad, gz = st.gz * -P.coeffPressGrad;
+            d.gradC[i] = make_dvec4(gx, gy, gz, 0.0);
+            if (d.bc[i] == P.inner)
+                sh = make_dvec4(-P.coeffShifting2 * gx, -P.coeffShifting2 * gy, -P.coeffShifting2 * gz, 0.0);
+        }
+        d.shift[i] = sh;
+    }
+};
 // MpsShifting::calcWallConcAndConcGradient, src/MpsShifting.cpp:578-691
 __global__ void __launch_bounds__(BLK) k_wall_grad_conc(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -931,15 +946,17 @@ __global__ void k_apply_shift(Dev d) {
     d.posf[i] = make_float4((float)(x.x - d.P.domainMin[0]), (float)(x.y - d.P.domainMin[1]),
                             (float)(x.z - d.P.domainMin[2]), 0.f);
 }
-void launchShifting(const Dev& d, cudaStream_t s) {
+void launchShifting(const Dev& d, int* scanScratch, cudaStream_t s) {
     const MpsParams& P = d.P;
-    launchPosf(d, s);   // post-corrector positions
+    if (P.shiftingType != 1 && P.shiftingType != 2) return;
+    launchPosf(d, s);   // post-corrector positions and their query buckets
+    launchQueryCells(d, scanScratch, s);
     if (P.shiftingType == 1) {
-        k_shift_vel<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+        launchCellScan(d, OpShiftVel(), s);
         k_shift_vel_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
-    } else if (P.shiftingType == 2) {
-        k_conc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
-        k_grad_conc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    } else {
+        launchCellScan(d, OpConc(), s);
+        launchCellScan(d, OpGradConc(), s);
         k_apply_shift<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
         if (P.wallType == 1) {
             k_wall_grad_conc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);

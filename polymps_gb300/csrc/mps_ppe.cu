@@ -137,14 +137,25 @@ __device__ __forceinline__ void gridSum(double (&v)[NV], const PpeBuffers& B, Fi
 }
 
 // ------------------------------------------------------------------ plain FP64 PCG
+// One ELL row, four entries in flight (independent value/column/gather loads).
 __device__ __forceinline__ double spmvRow(const PpeBuffers& B, const double* x, int i) {
     double s = B.diag[i] * x[i];
     int len = B.rowLen[i];
-    for (int k = 0; k < len; k++) {
-        size_t e = (size_t)k * B.N0 + i;
-        s += B.val[e] * __ldg(x + B.col[e]);
+    const size_t N0 = B.N0;
+    const double* v = B.val + i;
+    const int* c = B.col + i;
+    int k = 0;
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (; k + 4 <= len; k += 4) {
+        int c0 = __ldg(c + k * N0), c1 = __ldg(c + (k + 1) * N0), c2 = __ldg(c + (k + 2) * N0), c3 = __ldg(c + (k + 3) * N0);
+        double v0 = __ldg(v + k * N0), v1 = __ldg(v + (k + 1) * N0), v2 = __ldg(v + (k + 2) * N0), v3 = __ldg(v + (k + 3) * N0);
+        s += v0 * __ldg(x + c0);
+        s1 += v1 * __ldg(x + c1);
+        s2 += v2 * __ldg(x + c2);
+        s3 += v3 * __ldg(x + c3);
     }
-    return s;
+    for (; k < len; k++) s += __ldg(v + k * N0) * __ldg(x + __ldg(c + k * N0));
+    return s + ((s1 + s2) + s3);
 }
 
 // r = b - A x, z = r / diag, p = z; sums r.z, r.r, b.b
@@ -321,11 +332,21 @@ __global__ void __launch_bounds__(PBLK) k_mx_inner_init(Dev d, PpeBuffers B) {
 __device__ __forceinline__ float spmvRowF(const PpeBuffers& B, const float* x, int i) {
     float s = B.diagf[i] * x[i];
     int len = B.rowLen[i];
-    for (int k = 0; k < len; k++) {
-        size_t e = (size_t)k * B.N0 + i;
-        s += B.valf[e] * __ldg(x + B.col[e]);
+    const size_t N0 = B.N0;
+    const float* v = B.valf + i;
+    const int* c = B.col + i;
+    int k = 0;
+    float s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    for (; k + 4 <= len; k += 4) {
+        int c0 = __ldg(c + k * N0), c1 = __ldg(c + (k + 1) * N0), c2 = __ldg(c + (k + 2) * N0), c3 = __ldg(c + (k + 3) * N0);
+        float v0 = __ldg(v + k * N0), v1 = __ldg(v + (k + 1) * N0), v2 = __ldg(v + (k + 2) * N0), v3 = __ldg(v + (k + 3) * N0);
+        s += v0 * __ldg(x + c0);
+        s1 += v1 * __ldg(x + c1);
+        s2 += v2 * __ldg(x + c2);
+        s3 += v3 * __ldg(x + c3);
     }
-    return s;
+    for (; k < len; k++) s += __ldg(v + k * N0) * __ldg(x + __ldg(c + k * N0));
+    return s + ((s1 + s2) + s3);
 }
 __global__ void __launch_bounds__(PBLK) k_mx_spmv(Dev d, PpeBuffers B) {
     if (*(volatile int*)(B.flag + 3)) return;

@@ -91,8 +91,8 @@ void Prof::destroy() {
 // Kernels launched by one operator (fixed by the configuration; the solvers count theirs).
 static int opLaunches(int op, const MpsParams& P) {
     switch (op) {
-        case MPS_OP_UPDATE_BUCKETS: return 6;
-        case MPS_OP_VISCOSITY: return 8;
+        case MPS_OP_UPDATE_BUCKETS: return 7;   // key, 3 scan, scatter, sort, bucket-ordered copy
+        case MPS_OP_VISCOSITY: return 1;
         case MPS_OP_OUT_OF_DOMAIN: return 2;
         case MPS_OP_COLLISION: return 2;
         case MPS_OP_WALL_DISTANCE: case MPS_OP_WALL_NPCD: case MPS_OP_WALL_PRESS_GRADIENT:
@@ -101,9 +101,9 @@ static int opLaunches(int op, const MpsParams& P) {
         case MPS_OP_PND_MEAN: return P.wallType == 1 ? 3 : 2;
         case MPS_OP_INIT_PND: return 2 + (P.wallType == 1 ? 3 : 2);
         case MPS_OP_CALC_PRESS: return (P.mpsType == 2) ? 2 : 1;   // assemble + copy back | EOS
-        case MPS_OP_SHIFTING:   // posf + query buckets (6) + staged scans (2 each) + apply kernels
-            return P.shiftingType == 1 ? 10 : (P.shiftingType == 2 ? (P.wallType == 1 ? 15 : 13) : 0);
-        case MPS_OP_DUMMY_VELOCITY: return P.wallType == 0 ? 2 : 0;
+        case MPS_OP_SHIFTING:   // FP32 copies (2) + scans + apply kernels
+            return P.shiftingType == 1 ? 4 : (P.shiftingType == 2 ? (P.wallType == 1 ? 8 : 5) : 0);
+        case MPS_OP_DUMMY_VELOCITY: return P.wallType == 0 ? 3 : 0;
         default: return 1;
     }
 }
@@ -151,9 +151,9 @@ static int launchStatus() {
 static void ensureList(mpsgpu_t h) {
     if (h->listValid) return;
     if (h->prof.on) h->prof.begin(PROF_NEIGHBOR_LIST, h->s);
-    launchNeighborList(h->d, h->scanScratch, h->s);
+    launchNeighborList(h->d, h->s);
     if (h->prof.on) h->prof.end(h->s);
-    countLaunch(9);   // posf, query buckets (key, 3 scan, scatter, list), staged scan + fallback
+    countLaunch(3);   // FP32 copies (2), list build
     h->listValid = true;
     h->masksValid = false;
 }
@@ -252,7 +252,7 @@ static int runOpBody(mpsgpu_t h, int op) {
     auto invalidate = [&]() { h->listValid = false; h->masksValid = false; };
     switch (op) {
         case MPS_OP_UPDATE_BUCKETS: launchBuckets(d, h->scanScratch, s); invalidate(); break;
-        case MPS_OP_VISCOSITY: launchViscosity(d, h->scanScratch, s); break;
+        case MPS_OP_VISCOSITY: launchViscosity(d, s); break;
         case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
         case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
         case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); invalidate(); break;
@@ -270,7 +270,7 @@ static int runOpBody(mpsgpu_t h, int op) {
         case MPS_OP_WALL_PRESS_GRADIENT: ensureMasks(h); launchWallPressGradient(d, s); break;
         case MPS_OP_WALL_VISCOSITY: ensureMasks(h); launchWallViscosity(d, s); break;
         case MPS_OP_CORRECT: launchCorrect(d, s); invalidate(); break;
-        case MPS_OP_SHIFTING: launchShifting(d, h->scanScratch, s); if (P.shiftingType == 2) invalidate(); break;
+        case MPS_OP_SHIFTING: launchShifting(d, s); if (P.shiftingType == 2) invalidate(); break;
         case MPS_OP_DUMMY_VELOCITY: launchDummyVelocity(d, s); break;
         case MPS_OP_INIT_PND: ensureMasks(h); launchInitPnd(d, s); break;
         default: g_lastError = "unknown operator"; return MPSGPU_ERR_ARG;
@@ -422,15 +422,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.cellCount, d.nB + 1);
     A(d.cellCursor, d.nB + 1);
     A(d.cellSorted, n);
-    A(d.qOf, n);
-    A(d.qCount, d.nB + 1);
-    A(d.qStart, d.nB + 1);
-    A(d.qCursor, d.nB + 1);
-    A(d.qSorted, n);
-    A(d.qList, d.nB);
-    A(d.qNum, 1);
-    A(d.strayList, n);
-    A(d.strayNum, 1);
+    A(d.posfCell, n);
     A(d.nbrCount, n);
     A(d.nbr, (size_t)d.K * n);
     A(d.cw, (size_t)d.K * n);

@@ -9,7 +9,8 @@
 #include <atomic>
 #include "mps_common.cuh"
 #include "mps_internal.h"
-#include "mps_cellscan.cuh"
+
+__global__ void k_posf_cell(Dev d);
 
 static std::atomic<long long> g_launches{0};
 void countLaunch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
@@ -151,116 +152,69 @@ void launchBuckets(const Dev& d, int* scanScratch, cudaStream_t s) {
     scanExclusive(d.cellCount, d.cellStart, d.nB, scanScratch, s);
     k_cell_scatter<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
     k_cell_sort<<<gridFor(d.nB, 256), 256, 0, s>>>(d);
+    k_posf_cell<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
 }
 
 // ------------------------------------------------------------------ FP32 copy
 __global__ void k_posf(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
+    if (i >= d.N0) return;   // every slot: stale bucket entries may name removed particles
     dvec4 p = d.pos[i];
     d.posf[i] = make_float4((float)(p.x - d.P.domainMin[0]), (float)(p.y - d.P.domainMin[1]),
                             (float)(p.z - d.P.domainMin[2]), 0.f);
 }
 
 // ------------------------------------------------------------------ neighbour list
+// FP32 copy of the positions in bucket order, refreshed whenever positions change.
+__global__ void k_posf_cell(Dev d) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.cellStart[d.nB]) return;
+    d.posfCell[s] = d.posf[d.cellSorted[s]];
+}
+void launchPosfCell(const Dev& d, cudaStream_t s) {
+    k_posf_cell<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+}
+void launchPosf(const Dev& d, cudaStream_t s) {
+    k_posf<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    launchPosfCell(d, s);
+}
+
 // Candidates are tested in FP32 first; only those whose FP32 squared distance falls in
 // the rounding band around the list radius^2 are re-tested in exact FP64, so membership
 // equals the reference's FP64 test dst^2 < re^2 bit for bit while almost all candidate
-// work is FP32.  Every accepted entry also gets its weights for the epoch: w(r; reS),
-// w/r^2 and, when the radii differ, w(r; reL) — the FP64 divisions and square roots of
-// all later sweeps happen here once.  The scan itself is the staged warp-per-bucket scan
-// (mps_cellscan.cuh); OpBuildNbr below holds the per-candidate decision.
-
-void launchPosf(const Dev& d, cudaStream_t s) { k_posf<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
-
-// ------------------------------------------------------------------ query buckets
-// Group live particles by the bucket of their current position (bucketCoordinates with
-// epsilonZero, src/MpsBucket.cpp:420-425) for the staged scans; positions outside the
-// grid go to the per-thread fallback list.
-__global__ void k_q_key(Dev d) {
+// work is FP32 on contiguous bucket-ordered records.  Every accepted entry also gets its
+// weights for the epoch: w(r; reS), w/r^2 and, when the radii differ, w(r; reL) — the
+// FP64 divisions and square roots of all later sweeps happen here once.
+__global__ void __launch_bounds__(128) k_build_nbr(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.N0) return;
-    int q = -1;
-    if (i < liveN(d)) {
-        const MpsParams& P = d.P;
-        dvec4 p = d.pos[i];
-        int ix, iy, iz;
-        bucketCoords(P, p.x, p.y, p.z, ix, iy, iz);
-        if (ix >= 0 && ix < P.numBucketsX && iy >= 0 && iy < P.numBucketsY && iz >= 0 && iz < P.numBucketsZ) {
-            q = iz * P.numBucketsXY + iy * P.numBucketsX + ix;
-            atomicAdd(d.qCount + q, 1);
-        } else {
-            d.strayList[atomicAdd(d.strayNum, 1)] = i;
-        }
-    }
-    d.qOf[i] = q;
-}
-__global__ void k_q_scatter(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.N0) return;
-    int q = d.qOf[i];
-    if (q < 0) return;
-    d.qSorted[d.qStart[q] + atomicAdd(d.qCursor + q, 1)] = i;
-}
-__global__ void k_q_list(Dev d) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= d.nB) return;
-    if (d.qCount[c] > 0) d.qList[atomicAdd(d.qNum, 1)] = c;
-}
-void launchQueryCells(const Dev& d, int* scanScratch, cudaStream_t s) {
-    cudaMemsetAsync(d.qCount, 0, sizeof(int) * (d.nB + 1), s);
-    cudaMemsetAsync(d.qCursor, 0, sizeof(int) * (d.nB + 1), s);
-    cudaMemsetAsync(d.qNum, 0, sizeof(int), s);
-    cudaMemsetAsync(d.strayNum, 0, sizeof(int), s);
-    k_q_key<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
-    scanExclusive(d.qCount, d.qStart, d.nB, scanScratch, s);
-    k_q_scatter<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
-    k_q_list<<<gridFor(d.nB, 256), 256, 0, s>>>(d);
-}
-
-// List build as a staged-scan operator
-struct OpBuildNbr {
-    struct State { dvec4 pi; float4 fi; int cnt; };
-    __device__ void begin(const Dev& d, int i, State& st) const {
-        st.pi = d.pos[i]; st.fi = d.posf[i]; st.cnt = 0;
-    }
-    __device__ void visit(const Dev& d, int i, State& st, int j, float4 fj) const {
-        float dx = fj.x - st.fi.x, dy = fj.y - st.fi.y, dz = fj.z - st.fi.z;
-        float d2f = dx * dx + dy * dy + dz * dz;
-        if (d2f > d.bandHi || j == i) return;
-        dvec4 pj = d.pos[j];
-        double d2;
-        if (d2f < d.bandLo) {
-            double a = pj.x - st.pi.x, b = pj.y - st.pi.y, c = pj.z - st.pi.z;
-            d2 = a * a + b * b + c * c;
-        } else {
-            d2 = pairOf(pj, st.pi).d2;
-            if (!(d2 < d.reMax2)) return;
-        }
-        if (st.cnt < d.K) {
-            size_t e = (size_t)st.cnt * d.N0 + i;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    float4 fi = d.posf[i];
+    int cnt = 0;
+    const size_t N0 = d.N0;
+    forCellsNear(d, pi, fi, d.bandHi, [&](int j, dvec4 pj, PairG q) {
+        if (j == i || !(q.d2 < d.reMax2)) return;
+        if (cnt < d.K) {
+            size_t e = (size_t)cnt * N0 + i;
             d.nbr[e] = j;
             double w, wd;
-            weightR(d2, d.P.reS, d.P.weightType, w, wd);
+            weightR(q.d2, P.reS, P.weightType, w, wd);
             d.cw[e] = w;
             d.cwd[e] = wd;
-            if (d.cwL) { double wl, wdl; weightR(d2, d.P.reL, d.P.weightType, wl, wdl); d.cwL[e] = wl; }
+            if (d.cwL) { double wl, wdl; weightR(q.d2, P.reL, P.weightType, wl, wdl); d.cwL[e] = wl; }
         }
-        st.cnt++;
-    }
-    __device__ void end(const Dev& d, int i, State& st) const {
-        int cnt = st.cnt;
-        if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }
-        d.nbrCount[i] = cnt;
-        warpCount(d.counters, (unsigned)cnt);
-    }
-};
+        cnt++;
+    });
+    if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }
+    d.nbrCount[i] = cnt;
+    warpCount(d.counters, (unsigned)cnt);
+}
 
-void launchNeighborList(const Dev& d, int* scanScratch, cudaStream_t s) {
+void launchNeighborList(const Dev& d, cudaStream_t s) {
     cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long), s);
-    k_posf<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
-    launchQueryCells(d, scanScratch, s);
-    launchCellScan(d, OpBuildNbr(), s);
+    launchPosf(d, s);
+    k_build_nbr<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
 }
 
 // ------------------------------------------------------------------ entry masks

@@ -46,9 +46,10 @@ struct Dev {
     float4* posf;      // FP32 copy of pos - domainMin (neighbour prefilter, FP32 sums)
     // buckets (stale list of the step)
     int *cellOf, *cellStart, *cellCount, *cellSorted, *cellCursor;
-    // query buckets: particles grouped by the bucket of their current position
-    // (bucketCoordinates), for the warp-per-bucket staged scans
-    int *qOf, *qCount, *qStart, *qCursor, *qSorted, *qList, *qNum, *strayList, *strayNum;
+    // FP32 positions in bucket order (posfCell[s] = posf[cellSorted[s]]): the prefilter of
+    // the 27-bucket scans reads contiguous 16-byte records and fetches the particle index
+    // only for candidates that pass it
+    float4* posfCell;
     // neighbour list (ELL) and its per-entry cache for the epoch: w(r; reS), w/r^2,
     // w(r; reL) (only when reL != reS)
     int *nbrCount, *nbr;
@@ -227,13 +228,46 @@ __device__ __forceinline__ void forCells(const Dev& d, dvec4 x, F&& f) {
 // reach f(j, pj, q) with the exact FP64 pair, and f applies the reference's exact test.
 template <class F>
 __device__ __forceinline__ void forCellsNear(const Dev& d, dvec4 pi, float4 fi, float hi, F&& f) {
-    forCells(d, pi, [&](int j) {
-        float4 fj = __ldg(&d.posf[j]);
-        float dx = fj.x - fi.x, dy = fj.y - fi.y, dz = fj.z - fi.z;
-        if (dx * dx + dy * dy + dz * dz > hi) return;
-        dvec4 pj = d.pos[j];
-        f(j, pj, pairOf(pj, pi));
-    });
+    const MpsParams& P = d.P;
+    int ix, iy, iz;
+    bucketCoords(P, pi.x, pi.y, pi.z, ix, iy, iz);
+    int dz = (int)(P.dim - 2.0);
+    int minZ = (iz - 1) * dz, maxZ = (iz + 1) * dz;
+    for (int jz = minZ; jz <= maxZ; jz++)
+        for (int jy = iy - 1; jy <= iy + 1; jy++)
+            for (int jx = ix - 1; jx <= ix + 1; jx++) {
+                long long jb = (long long)jz * P.numBucketsXY + (long long)jy * P.numBucketsX + jx;
+                if (jb < 0 || jb >= d.nB) continue;
+                int s0 = d.cellStart[jb], s1 = d.cellStart[jb + 1];
+                for (int s = s0; s < s1; s++) {
+                    float4 fj = __ldg(&d.posfCell[s]);
+                    float ex = fj.x - fi.x, ey = fj.y - fi.y, ez = fj.z - fi.z;
+                    if (ex * ex + ey * ey + ez * ez > hi) continue;
+                    int j = __ldg(d.cellSorted + s);
+                    dvec4 pj = d.pos[j];
+                    f(j, pj, pairOf(pj, pi));
+                }
+            }
+}
+
+// Per-thread 27-bucket sweep driver: Op::begin/visit/end, Op::hi (prefilter bound) and
+// Op::active (skip the scan for particles the sweep does not update).  visit receives
+// the candidates that pass the FP32 prefilter, with the exact FP64 pair, j != i.
+template <class Op>
+__global__ void __launch_bounds__(128) k_scan(Dev d, Op op) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *d.nLive) return;
+    typename Op::State st;
+    op.begin(d, i, st);
+    if (op.active(d, st))
+        forCellsNear(d, d.pos[i], d.posf[i], op.hi(d), [&](int j, dvec4 pj, PairG q) {
+            if (j != i) op.visit(d, i, st, j, pj, q);
+        });
+    op.end(d, i, st);
+}
+template <class Op>
+void launchScan(const Dev& d, const Op& op, cudaStream_t s) {
+    k_scan<Op><<<(d.N0 + 127) / 128, 128, 0, s>>>(d, op);
 }
 
 __device__ __forceinline__ void setErr(const Dev& d, unsigned int bit) { atomicOr(d.err, bit); }

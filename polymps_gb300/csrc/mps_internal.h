@@ -33,13 +33,13 @@ struct Prof {
 void scanExclusive(const int* in, int* out, int n, int* scratch, cudaStream_t s);
 int scanScratchInts(int n);
 void launchBuckets(const Dev& d, int* scanScratch, cudaStream_t s);
-void launchNeighborList(const Dev& d, int* scanScratch, cudaStream_t s);
-void launchQueryCells(const Dev& d, int* scanScratch, cudaStream_t s);
-void launchPosf(const Dev& d, cudaStream_t s);
+void launchNeighborList(const Dev& d, cudaStream_t s);
+void launchPosf(const Dev& d, cudaStream_t s);       // FP32 copy, then its bucket-ordered copy
+void launchPosfCell(const Dev& d, cudaStream_t s);   // bucket-ordered copy only
 void launchSideMasks(const Dev& d, cudaStream_t s);
 
 // mps_ops.cu
-void launchViscosity(const Dev& d, int* scanScratch, cudaStream_t s);
+void launchViscosity(const Dev& d, cudaStream_t s);
 void launchAddGravity(const Dev& d, cudaStream_t s);
 void launchPredict(const Dev& d, cudaStream_t s);
 void launchOutOfDomain(const Dev& d, int* flags, int* counter, cudaStream_t s);
@@ -57,7 +57,7 @@ void launchPressGradient(const Dev& d, cudaStream_t s);
 void launchWallPressGradient(const Dev& d, cudaStream_t s);
 void launchWallViscosity(const Dev& d, cudaStream_t s);
 void launchCorrect(const Dev& d, cudaStream_t s);
-void launchShifting(const Dev& d, int* scanScratch, cudaStream_t s);
+void launchShifting(const Dev& d, cudaStream_t s);
 void launchDummyVelocity(const Dev& d, cudaStream_t s);
 
 // mps_wall.cu

@@ -8,7 +8,6 @@
 // with the distance comparisons evaluated in exact FP64 (see mps_common.cuh).
 #include "mps_common.cuh"
 #include "mps_internal.h"
-#include "mps_cellscan.cuh"
 
 #define BLK 128
 
@@ -17,18 +16,16 @@
 // uniform, src/MpsInputOutput.cpp:833-838, so the harmonic mean is hoisted).  Staged scan
 // at the start-of-step positions; FP32 prefilter, exact FP64 radius/side tests.
 struct OpViscosity {
-    struct State { dvec4 pi, vi; float4 fi; SideCtx sc; double ax, ay, az; };
+    struct State { dvec4 vi; SideCtx sc; double ax, ay, az; };
+    __device__ float hi(const Dev& d) const { return d.bandHiL; }
+    __device__ bool active(const Dev&, const State&) const { return true; }
     __device__ void begin(const Dev& d, int i, State& st) const {
-        st.pi = d.pos[i]; st.vi = d.vel[i]; st.fi = d.posf[i];
-        st.sc = sideCtx(d, i, st.pi);
+        st.vi = d.vel[i];
+        st.sc = sideCtx(d, i, d.pos[i]);
         st.ax = st.ay = st.az = 0.0;
     }
-    __device__ void visit(const Dev& d, int i, State& st, int j, float4 fj) const {
-        float dx = fj.x - st.fi.x, dy = fj.y - st.fi.y, dz = fj.z - st.fi.z;
-        if (dx * dx + dy * dy + dz * dz > d.bandHiL || j == i) return;
+    __device__ void visit(const Dev& d, int i, State& st, int j, dvec4 pj, PairG q) const {
         const MpsParams& P = d.P;
-        dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, st.pi);
         if (!(q.d2 < P.reL2) || !sideOK(st.sc, pj, q.d2)) return;
         double mu = P.KNM_VS1 * P.DNS_FL1, rho = P.DNS_FL1;
         double neu = (d.type[j] == P.wall) ? (2.0 * mu) / rho : (2.0 * mu * mu / (mu + mu)) / rho;
@@ -44,9 +41,8 @@ struct OpViscosity {
         d.acc[i] = make_dvec4(c * st.ax, c * st.ay, c * st.az, 0.0);
     }
 };
-void launchViscosity(const Dev& d, int* scanScratch, cudaStream_t s) {
-    launchQueryCells(d, scanScratch, s);
-    launchCellScan(d, OpViscosity(), s);
+void launchViscosity(const Dev& d, cudaStream_t s) {
+    launchScan(d, OpViscosity(), s);
 }
 
 // MpsParticle::addGravity, src/MpsParticle.cpp:111-130
@@ -813,33 +809,30 @@ void launchCorrect(const Dev& d, cudaStream_t s) {
 // ------------------------------------------------------------------ shifting
 // MpsShifting::calcShifting (type 1), src/MpsShifting.cpp:23-101: dv from the
 // pre-shift velocities, then applied.
-// Common head of the post-corrector staged scans: FP32 prefilter on the reS ball, exact
-// FP64 radius and mirror-side tests.
+// Common head of the post-corrector scans: prefilter band of the reS ball, exact FP64
+// radius and mirror-side tests; particles the sweep does not update skip the scan.
 struct E2Base {
-    struct Core { dvec4 pi; float4 fi; SideCtx sc; bool on; };
+    struct Core { SideCtx sc; bool on; };
     __device__ static void start(const Dev& d, int i, Core& c, bool on) {
         c.on = on;
-        c.pi = d.pos[i]; c.fi = d.posf[i];
-        c.sc = sideCtx(d, i, c.pi);
+        if (on) c.sc = sideCtx(d, i, d.pos[i]);
     }
-    __device__ static bool accept(const Dev& d, int i, const Core& c, int j, float4 fj, dvec4& pj, PairG& q) {
-        if (!c.on || j == i) return false;
-        float dx = fj.x - c.fi.x, dy = fj.y - c.fi.y, dz = fj.z - c.fi.z;
-        if (dx * dx + dy * dy + dz * dz > d.bandHiS) return false;
-        pj = d.pos[j];
-        q = pairOf(pj, c.pi);
+    __device__ static bool accept(const Dev& d, const Core& c, dvec4 pj, PairG q) {
         return q.d2 < d.P.reS2 && sideOK(c.sc, pj, q.d2);
     }
 };
+#define E2_COMMON \
+    __device__ float hi(const Dev& d) const { return d.bandHiS; } \
+    __device__ bool active(const Dev&, const State& st) const { return st.c.on; }
 struct OpShiftVel {
     struct State { E2Base::Core c; dvec4 vi; double ux, uy, uz; };
+    E2_COMMON
     __device__ void begin(const Dev& d, int i, State& st) const {
         E2Base::start(d, i, st.c, d.type[i] == d.P.fluid);
         st.vi = d.vel[i]; st.ux = st.uy = st.uz = 0.0;
     }
-    __device__ void visit(const Dev& d, int i, State& st, int j, float4 fj) const {
-        dvec4 pj; PairG q;
-        if (!E2Base::accept(d, i, st.c, j, fj, pj, q)) return;
+    __device__ void visit(const Dev& d, int i, State& st, int j, dvec4 pj, PairG q) const {
+        if (!E2Base::accept(d, st.c, pj, q)) return;
         double dw = dwfun(sqrt(q.d2), d.P.reS, d.P.weightType);
         dvec4 vj = d.vel[j];
         st.ux += dw * (vj.x - st.vi.x); st.uy += dw * (vj.y - st.vi.y); st.uz += dw * (vj.z - st.vi.z);
@@ -861,10 +854,10 @@ __global__ void k_shift_vel_apply(Dev d) {
 // gradient and position shift (each sweep reads the positions it started with).
 struct OpConc {
     struct State { E2Base::Core c; double sum; };
+    E2_COMMON
     __device__ void begin(const Dev& d, int i, State& st) const { E2Base::start(d, i, st.c, true); st.sum = 0.0; }
-    __device__ void visit(const Dev& d, int i, State& st, int j, float4 fj) const {
-        dvec4 pj; PairG q;
-        if (!E2Base::accept(d, i, st.c, j, fj, pj, q)) return;
+    __device__ void visit(const Dev& d, int i, State& st, int j, dvec4 pj, PairG q) const {
+        if (!E2Base::accept(d, st.c, pj, q)) return;
         double w, wd;
         weightR(q.d2, d.P.reS, d.P.weightType, w, wd);
         st.sum += w;
@@ -875,13 +868,13 @@ struct OpConc {
 };
 struct OpGradConc {
     struct State { E2Base::Core c; double ci, gx, gy, gz; };
+    E2_COMMON
     __device__ void begin(const Dev& d, int i, State& st) const {
         E2Base::start(d, i, st.c, d.type[i] == d.P.fluid);
         st.ci = d.conc[i]; st.gx = st.gy = st.gz = 0.0;
     }
-    __device__ void visit(const Dev& d, int i, State& st, int j, float4 fj) const {
-        dvec4 pj; PairG q;
-        if (!E2Base::accept(d, i, st.c, j, fj, pj, q)) return;
+    __device__ void visit(const Dev& d, int i, State& st, int j, dvec4 pj, PairG q) const {
+        if (!E2Base::accept(d, st.c, pj, q)) return;
         double wS, wd;
         weightR(q.d2, d.P.reS, d.P.weightType, wS, wd);
         double cc = (st.ci + d.conc[j]) * wd;
@@ -946,19 +939,19 @@ __global__ void k_apply_shift(Dev d) {
     d.posf[i] = make_float4((float)(x.x - d.P.domainMin[0]), (float)(x.y - d.P.domainMin[1]),
                             (float)(x.z - d.P.domainMin[2]), 0.f);
 }
-void launchShifting(const Dev& d, int* scanScratch, cudaStream_t s) {
+void launchShifting(const Dev& d, cudaStream_t s) {
     const MpsParams& P = d.P;
     if (P.shiftingType != 1 && P.shiftingType != 2) return;
-    launchPosf(d, s);   // post-corrector positions and their query buckets
-    launchQueryCells(d, scanScratch, s);
+    launchPosf(d, s);   // post-corrector positions
     if (P.shiftingType == 1) {
-        launchCellScan(d, OpShiftVel(), s);
+        launchScan(d, OpShiftVel(), s);
         k_shift_vel_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
     } else {
-        launchCellScan(d, OpConc(), s);
-        launchCellScan(d, OpGradConc(), s);
+        launchScan(d, OpConc(), s);
+        launchScan(d, OpGradConc(), s);
         k_apply_shift<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
         if (P.wallType == 1) {
+            launchPosfCell(d, s);   // the wall sweep sees the shifted positions
             k_wall_grad_conc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
             k_apply_shift<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
         }

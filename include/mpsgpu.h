@@ -276,6 +276,30 @@ const char* mpsgpu_profile_name(int cls);
 /* Kernels launched by this library in this process so far. */
 int mpsgpu_launch_count(long long* n);
 
+/* Allocation-free pressure solve (no counterpart in the reference, whose Eigen
+ * ConjugateGradient allocates its own work vectors on every solve).  For callers that
+ * cannot allocate device memory when they solve: an application whose device memory is
+ * owned by another framework's pool, or a stepping loop that forbids allocation once it
+ * runs.  Jacobi-preconditioned CG with Eigen's stopping rule (|r| < tol |b|) on a CSR
+ * system whose arrays (rowptr[n+1], col/val[nnz], b[n], x[n]) are DEVICE pointers; x holds
+ * the initial guess on entry and the solution on return.  All work vectors live in one
+ * file-scope device array of MPSGPU_STATIC_MAX_ROWS rows (about 5.3 MB per device),
+ * reserved at library load: the call makes no device allocation.  Rules:
+ *  - n must be 1..MPSGPU_STATIC_MAX_ROWS, otherwise MPSGPU_ERR_ARG;
+ *  - each call clears the array's control words itself; nothing needs zeroing first;
+ *  - the array is shared by every call on a device: calls that overlap on the GPU
+ *    (two streams, two host threads) race and corrupt each other;
+ *  - the first call on a device looks the array's address up with that device
+ *    current; make it before any stream capture begins.
+ * The call synchronises `stream` (cudaStream_t as void*, may be NULL) to poll
+ * convergence.  iters / relres (may be NULL) receive the iteration count and the true
+ * relative residual |b - Ax| / |b|.  mpsgpu_pcg_static_error() gives the last message. */
+#define MPSGPU_STATIC_MAX_ROWS (1 << 17)
+int mpsgpu_pcg_solve_static(int n, const int* rowptr, const int* col, const double* val,
+                            const double* b, double* x, double tol, int max_iter, void* stream,
+                            int* iters, double* relres);
+const char* mpsgpu_pcg_static_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,6 +92,9 @@ class MpsStepStats(C.Structure):
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_UNSUPPORTED, ERR_NOT_CONVERGED, ERR_CAPACITY, \
     ERR_DOMAIN, ERR_NOGPU, ERR_SIZE_MISMATCH = range(10)
 
+# row limit of mpsgpu_pcg_solve_static (MPSGPU_STATIC_MAX_ROWS)
+STATIC_MAX_ROWS = 1 << 17
+
 # fields (enum MpsField)
 F_POS, F_VEL, F_ACC, F_ACCSTAR, F_NPCD, F_GRADC, F_CORR1, F_CORR2, F_CORR3, F_MIRROR, \
     F_WALLPOS, F_POLYNORMAL, F_FORCEWALL = range(13)

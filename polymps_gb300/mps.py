@@ -23,7 +23,7 @@ EXPORTS = [
     "mpsgpu_mlp_num_records", "mpsgpu_mlp_fit_normalization", "mpsgpu_mlp_train", "mpsgpu_mlp_forward",
     "mpsgpu_mlp_gradient", "mpsgpu_stream", "mpsgpu_last_error", "mpsgpu_abi_sizes",
     "mpsgpu_profile", "mpsgpu_profile_get", "mpsgpu_profile_name", "mpsgpu_launch_count",
-    "mpsgpu_last_stats",
+    "mpsgpu_last_stats", "mpsgpu_pcg_solve_static", "mpsgpu_pcg_static_error",
 ]
 PROF_NCLASS = len(abi.OPS) + 5
 
@@ -77,6 +77,9 @@ def lib(path=None):
     L.mpsgpu_profile_name.restype = C.c_char_p
     L.mpsgpu_launch_count.argtypes = [P(C.c_longlong)]
     L.mpsgpu_last_stats.argtypes = [vp, P(abi.MpsStepStats)]
+    L.mpsgpu_pcg_solve_static.argtypes = [C.c_int, vp, vp, vp, vp, vp, C.c_double, C.c_int, vp,
+                                          P(C.c_int), P(C.c_double)]
+    L.mpsgpu_pcg_static_error.restype = C.c_char_p
     _lib = L
     return L
 

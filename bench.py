@@ -37,6 +37,8 @@ def args_():
     a.add_argument("--warmup", type=int, default=5)
     a.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     a.add_argument("--solver", default="mixed", choices=["mixed", "plain"])
+    a.add_argument("--precision", default="df32", choices=["df32", "fp64"],
+                   help="neighbour-sweep arithmetic: float-float (df32) or FP64")
     a.add_argument("--warm", default="auto", choices=["auto", "prev", "mlp"])
     a.add_argument("--scale", type=float, default=1.0, help="l0 multiplier (1 = 864k particles)")
     a.add_argument("--e2e-steps", type=int, default=3)
@@ -116,26 +118,28 @@ class Clocks:
 
 # Algorithmic bytes per call of each timed class (each distinct element read or written
 # once; neighbour re-reads assumed cache resident).  N particles, E neighbour entries,
-# Z off-diagonal PPE non-zeros.
-def algo_bytes(cls, N, E, Z, mixed):
+# Z off-diagonal PPE non-zeros; df = float-float tier (hi/lo FP32 copies, no weight cache).
+def algo_bytes(cls, N, E, Z, mixed, df):
     if cls == "PPE_SPMV":
         return N * (16 if mixed else 28) + Z * (8 if mixed else 12)
     if cls == "PPE_VECTOR":
         return N * (4 * 9 if mixed else 8 * 9)
     if cls == "NEIGHBOR_LIST":
-        return N * (32 + 16 + 16 + 4 + 4 + 4) + 4 * E
+        # FP32 copies (pos -> posf/posLo, bucket-ordered copies), list build (+ weights)
+        copies = N * (32 + 32) + N * (4 + 32 + 32)
+        return copies + N * (32 + 16 + 16 + 4) + (4 * E if df else 20 * E)
     if cls == "PPE_ASSEMBLE":
-        return N * (32 + 32 + 8 + 4 + 4 + 8 + 8 + 4 + 8) + Z * 12 + 4 * E
-    if cls in ("PRESS_GRADIENT",):
-        return N * (32 + 32 + 8 + 8 + 3 * 32 + 4 + 32) + 4 * E
-    if cls in ("PND_NEIGH_NPCD",):
-        return N * (32 + 32 + 8 + 4 + 32 + 32 + 8 * 5 + 4) + 4 * E
-    if cls in ("CORRECTION_MATRIX",):
-        return N * (32 + 32 + 4 + 4 + 3 * 32) + 4 * E
-    if cls in ("VISCOSITY",):
-        return N * (32 + 32 + 32 + 4 + 32)
-    if cls in ("COLLISION",):
-        return N * (32 + 32 + 32 + 4 + 32) + 4 * E
+        return N * (32 + 4 + 4 + 8 + 8 + 4 + 8 + 8) + Z * 12 + (4 * E if df else 12 * E)
+    if cls == "PRESS_GRADIENT":
+        return N * (32 + 8 + 8 + 3 * 32 + 32) + (N * 16 if df else 0) + (4 * E if df else 12 * E)
+    if cls == "PND_NEIGH_NPCD":
+        return N * (32 + 8 + 4 + 32 + 32 + 8 * 5 + 4) + (4 * E if df else 12 * E)
+    if cls == "CORRECTION_MATRIX":
+        return N * (32 + 8 + 4 + 3 * 32) + (4 * E if df else 12 * E)
+    if cls == "VISCOSITY":
+        return N * (32 + 16 + 16 + 32 + 4 + 32) + (N * 64 if df else 0)
+    if cls == "COLLISION":
+        return N * (32 + 32 + 32 + 4 + 32) + 4 * E + (N * 64 if df else 0)
     return None
 
 
@@ -152,7 +156,8 @@ def run_gb300(a, rank, world, local):
     solver = abi.SOLVER_MIXED if a.solver == "mixed" else abi.SOLVER_PLAIN_FP64
     mlp_path = os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz")
     use_mlp = a.warm == "mlp" or (a.warm == "auto" and os.path.exists(mlp_path))
-    g = mps.MpsGpu(case, solver=solver, tol=1e-8, max_iter=20000)
+    prec = abi.PRECISION_DF32 if a.precision == "df32" else abi.PRECISION_FP64
+    g = mps.MpsGpu(case, solver=solver, tol=1e-8, max_iter=20000, precision=prec)
     if use_mlp:
         w = np.load(mlp_path)
         g.mlp_set_weights(w["params"], w["norm"])
@@ -208,7 +213,7 @@ def run_gb300(a, rank, world, local):
     roof = None
     if dom:
         ms, calls = leaf[dom]
-        b = algo_bytes(dom, N, E, Z, mixed)
+        b = algo_bytes(dom, N, E, Z, mixed, prec == abi.PRECISION_DF32)
         if b:
             ach = b / (ms / calls / 1e3) / 1e9
             roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
@@ -224,10 +229,11 @@ def run_gb300(a, rank, world, local):
         "metric": METRIC, "value": round(value, 1), "unit": "particle-steps/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(st.stepMs / a.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+f64" if mixed else "f64", "data": "synthetic",
+        "dtype": ("df32" if prec == abi.PRECISION_DF32 else "f64") + ("+f32/f64 PPE" if mixed else "+f64 PPE"),
+        "data": "synthetic",
         "config": {"workload": "3D incompressible polygon dam break (cfg3)", "particles": N,
                    "l0": case.params["partDist"], "dt": case.params["timeStep"],
-                   "ppe_tol": 1e-8, "solver": a.solver, "warm_start": "mlp" if use_mlp else "previous",
+                   "ppe_tol": 1e-8, "solver": a.solver, "precision": a.precision, "warm_start": "mlp" if use_mlp else "previous",
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "working set > L2 (no flush needed)", "wall_s": round(wall, 3)},
         "e2e": {"value": round(e2e, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),

@@ -209,6 +209,18 @@ int mpsgpu_last_stats(mpsgpu_t h, MpsStepStats* out);
 /* Solver controls, replacing the fixed Eigen CG of src/MpsPressure.cpp:424-445. */
 int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm_start, double tol, int max_iter);
 
+/* Arithmetic of the neighbour sweeps (no reference counterpart: the reference is FP64
+ * throughout).  FP64 (default) evaluates every pair in FP64 like the reference.  DF32
+ * evaluates pair vectors, weights and sums in float-float (two FP32 numbers, ~48 bits)
+ * and keeps every discrete decision (neighbour radius, mirror side, collision sign) equal
+ * to the reference's by deciding in FP64 whenever the float-float value lies within its
+ * error margin; per-particle results differ from FP64 by ~1e-11 relative.  Operators
+ * without a DF32 kernel (diffusive/mean PND, extrapolation, shifting, dummy velocity,
+ * step-0 PND) run their FP64 kernels in either mode. */
+#define MPSGPU_PRECISION_FP64  0
+#define MPSGPU_PRECISION_DF32  1
+int mpsgpu_set_precision(mpsgpu_t h, int precision);
+
 /* Field transfer in the reference's host layout (see MpsField).  get writes
  * numParticles entries; set reads numParticles entries. */
 int mpsgpu_get_field(mpsgpu_t h, int field, void* host);

@@ -130,6 +130,7 @@ OP = {name: k for k, name in enumerate(OPS)}
 
 SOLVER_PLAIN_FP64, SOLVER_MIXED = 0, 1
 WARM_PREVIOUS, WARM_MLP, WARM_ZERO = 0, 1, 2
+PRECISION_FP64, PRECISION_DF32 = 0, 1
 MLP_NPARAM = 64 * 16 + 64 + 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1
 MLP_NFEAT = 16
 

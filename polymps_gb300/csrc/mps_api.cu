@@ -33,6 +33,7 @@ struct mpsgpu_s {
     // host mirrors of a few scalars
     bool listValid = false;
     bool masksValid = false;
+    bool cacheValid = false;   // per-entry FP64 weights of the current list
     double timeCurrent = 0.0;
     int numIter = 0;
     int lastOut = 0;
@@ -89,14 +90,15 @@ void Prof::destroy() {
 }
 
 // Kernels launched by one operator (fixed by the configuration; the solvers count theirs).
-static int opLaunches(int op, const MpsParams& P) {
+static int opLaunches(int op, const MpsParams& P, bool x) {
     switch (op) {
         case MPS_OP_UPDATE_BUCKETS: return 7;   // key, 3 scan, scatter, sort, bucket-ordered copy
-        case MPS_OP_VISCOSITY: return 1;
+        case MPS_OP_VISCOSITY: return x ? 2 : 1;   // (DF32: velocity copy) + sweep
         case MPS_OP_OUT_OF_DOMAIN: return 2;
-        case MPS_OP_COLLISION: return 2;
-        case MPS_OP_WALL_DISTANCE: case MPS_OP_WALL_NPCD: case MPS_OP_WALL_PRESS_GRADIENT:
-        case MPS_OP_WALL_VISCOSITY: return P.wallType == 1 ? 1 : 0;
+        case MPS_OP_COLLISION: return x ? 3 : 2;
+        case MPS_OP_WALL_DISTANCE: case MPS_OP_WALL_NPCD: return P.wallType == 1 ? 1 : 0;
+        case MPS_OP_WALL_PRESS_GRADIENT: case MPS_OP_WALL_VISCOSITY: return P.wallType == 1 ? (x ? 2 : 1) : 0;
+        case MPS_OP_PRESS_GRADIENT: return x ? 2 : 1;
         case MPS_OP_PND_DIFFUSIVE: return P.wallType == 1 ? 5 : 4;
         case MPS_OP_PND_MEAN: return P.wallType == 1 ? 3 : 2;
         case MPS_OP_INIT_PND: return 2 + (P.wallType == 1 ? 3 : 2);
@@ -148,21 +150,36 @@ static int launchStatus() {
     return 0;
 }
 
+static bool df32(mpsgpu_t h) { return h->d.prec == MPSGPU_PRECISION_DF32; }
 static void ensureList(mpsgpu_t h) {
     if (h->listValid) return;
     if (h->prof.on) h->prof.begin(PROF_NEIGHBOR_LIST, h->s);
-    launchNeighborList(h->d, h->s);
+    if (df32(h)) launchNeighborListDF(h->d, h->s);
+    else launchNeighborList(h->d, h->s);
     if (h->prof.on) h->prof.end(h->s);
     countLaunch(3);   // FP32 copies (2), list build
     h->listValid = true;
     h->masksValid = false;
+    h->cacheValid = !df32(h);   // the FP64 list build stores the per-entry weights
+}
+// Per-entry FP64 weights for the FP64 sweeps that read them (in the DF32 tier only the
+// operators without a DF32 kernel need them).
+static void ensureCache(mpsgpu_t h) {
+    ensureList(h);
+    if (h->cacheValid) return;
+    if (h->prof.on) h->prof.begin(PROF_NEIGHBOR_LIST, h->s);
+    launchFillCache(h->d, h->s);
+    if (h->prof.on) h->prof.end(h->s);
+    countLaunch(1);
+    h->cacheValid = true;
 }
 // Entry masks depend on the list and on the mirror positions of the wall pass.
 static void ensureMasks(mpsgpu_t h) {
     ensureList(h);
     if (h->masksValid) return;
     if (h->prof.on) h->prof.begin(PROF_NEIGHBOR_LIST, h->s);
-    launchSideMasks(h->d, h->s);
+    if (df32(h)) launchSideMasksDF(h->d, h->s);
+    else launchSideMasks(h->d, h->s);
     if (h->prof.on) h->prof.end(h->s);
     countLaunch(1);
     h->masksValid = true;
@@ -190,7 +207,8 @@ static int calcPress(mpsgpu_t h) {
     ensureMasks(h);
     cudaEventRecord(h->ea0, h->s);
     if (h->prof.on) h->prof.begin(PROF_PPE_ASSEMBLE, h->s);
-    launchPpeAssemble(h->d, h->B, h->s);
+    if (df32(h)) launchPpeAssembleDF(h->d, h->B, h->s);
+    else launchPpeAssemble(h->d, h->B, h->s);
     if (h->prof.on) h->prof.end(h->s);
     cudaEventRecord(h->ea1, h->s);
     // warm start: previous unclamped solution (reference), zero, or the learned predictor
@@ -242,37 +260,44 @@ static int runOpImpl(mpsgpu_t h, int op) {
     if (pr) h->prof.begin(op, h->s);
     int e = runOpBody(h, op);
     if (pr) h->prof.end(h->s);
-    countLaunch(opLaunches(op, h->d.P));
+    countLaunch(opLaunches(op, h->d.P, h->d.prec == MPSGPU_PRECISION_DF32));
     return e;
 }
 static int runOpBody(mpsgpu_t h, int op) {
     Dev& d = h->d;
     const MpsParams& P = d.P;
     cudaStream_t s = h->s;
-    auto invalidate = [&]() { h->listValid = false; h->masksValid = false; };
+    auto invalidate = [&]() { h->listValid = false; h->masksValid = false; h->cacheValid = false; };
+    const bool x = df32(h);
     switch (op) {
         case MPS_OP_UPDATE_BUCKETS: launchBuckets(d, h->scanScratch, s); invalidate(); break;
-        case MPS_OP_VISCOSITY: launchViscosity(d, s); break;
+        case MPS_OP_VISCOSITY: if (x) launchViscosityDF(d, s); else launchViscosity(d, s); break;
         case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
         case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
         case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); invalidate(); break;
-        case MPS_OP_COLLISION: ensureList(h); launchCollision(d, s); break;
+        case MPS_OP_COLLISION: ensureList(h); if (x) launchCollisionDF(d, s); else launchCollision(d, s); break;
         case MPS_OP_WALL_DISTANCE: launchWallDistance(d, s); h->masksValid = false; break;
-        case MPS_OP_WALL_NPCD: ensureMasks(h); launchWallNpcd(d, s); break;
-        case MPS_OP_CORRECTION_MATRIX: ensureMasks(h); launchCorrectionMatrix(d, s); break;
-        case MPS_OP_PND_NEIGH_NPCD: ensureMasks(h); launchPndNeighNpcd(d, s); break;
-        case MPS_OP_PND_DIFFUSIVE: ensureMasks(h); launchPndDiffusive(d, s); break;
-        case MPS_OP_PND_MEAN: ensureMasks(h); launchPndMean(d, s); break;
+        case MPS_OP_WALL_NPCD: ensureMasks(h); if (x) launchWallNpcdDF(d, s); else launchWallNpcd(d, s); break;
+        case MPS_OP_CORRECTION_MATRIX:
+            ensureMasks(h);
+            if (x) launchCorrectionMatrixDF(d, s); else launchCorrectionMatrix(d, s);
+            break;
+        case MPS_OP_PND_NEIGH_NPCD: ensureMasks(h); if (x) launchPndNeighNpcdDF(d, s); else launchPndNeighNpcd(d, s); break;
+        case MPS_OP_PND_DIFFUSIVE: ensureMasks(h); ensureCache(h); launchPndDiffusive(d, s); break;
+        case MPS_OP_PND_MEAN: ensureMasks(h); ensureCache(h); launchPndMean(d, s); break;
         case MPS_OP_UPDATE_BC: launchUpdateBC(d, s); break;
         case MPS_OP_CALC_PRESS: { int e = calcPress(h); if (e) return e; break; }
-        case MPS_OP_EXTRAPOLATE_PRESS: ensureMasks(h); launchExtrapolatePress(d, s); break;
-        case MPS_OP_PRESS_GRADIENT: ensureMasks(h); launchPressGradient(d, s); break;
-        case MPS_OP_WALL_PRESS_GRADIENT: ensureMasks(h); launchWallPressGradient(d, s); break;
-        case MPS_OP_WALL_VISCOSITY: ensureMasks(h); launchWallViscosity(d, s); break;
+        case MPS_OP_EXTRAPOLATE_PRESS: ensureMasks(h); ensureCache(h); launchExtrapolatePress(d, s); break;
+        case MPS_OP_PRESS_GRADIENT: ensureMasks(h); if (x) launchPressGradientDF(d, s); else launchPressGradient(d, s); break;
+        case MPS_OP_WALL_PRESS_GRADIENT:
+            ensureMasks(h);
+            if (x) launchWallPressGradientDF(d, s); else launchWallPressGradient(d, s);
+            break;
+        case MPS_OP_WALL_VISCOSITY: ensureMasks(h); if (x) launchWallViscosityDF(d, s); else launchWallViscosity(d, s); break;
         case MPS_OP_CORRECT: launchCorrect(d, s); invalidate(); break;
         case MPS_OP_SHIFTING: launchShifting(d, s); if (P.shiftingType == 2) invalidate(); break;
         case MPS_OP_DUMMY_VELOCITY: launchDummyVelocity(d, s); break;
-        case MPS_OP_INIT_PND: ensureMasks(h); launchInitPnd(d, s); break;
+        case MPS_OP_INIT_PND: ensureMasks(h); ensureCache(h); launchInitPnd(d, s); break;
         default: g_lastError = "unknown operator"; return MPSGPU_ERR_ARG;
     }
     return launchStatus();
@@ -423,6 +448,11 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.cellCursor, d.nB + 1);
     A(d.cellSorted, n);
     A(d.posfCell, n);
+    A(d.posLo, n);
+    A(d.posLoCell, n);
+    A(d.velHi, n);
+    A(d.velLo, n);
+    A(d.pressDF, n);
     A(d.nbrCount, n);
     A(d.nbr, (size_t)d.K * n);
     A(d.cw, (size_t)d.K * n);
@@ -455,6 +485,21 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         d.bandHi = (float)(d.reMax2 + band(d.reMax2));
         d.bandHiS = (float)(p->reS2 + band(p->reS2));
         d.bandHiL = (float)(p->reL2 + band(p->reL2));
+        // float-float squared distances: each coordinate difference is within
+        // 4 * 2^-48 * X of the FP64 one (storage of both lo parts, the rounded lo difference
+        // and the reference's own rounding), the float-float products and sums add about
+        // 2^-44 relative; the margin is 8x that bound.
+        auto margin = [&](double re2) {
+            double re = std::sqrt(re2);
+            double ddx = 4.0 * std::ldexp(1.0, -48) * X;
+            return (float)(8.0 * (2.0 * std::sqrt(3.0) * re * ddx + std::ldexp(1.0, -40) * re2));
+        };
+        d.mgS = margin(p->reS2);
+        d.mgL = margin(p->reL2);
+        d.mgMax = margin(d.reMax2);
+        d.mgColl = margin(std::max(p->distCollisionLimit2, 1e-300));
+        d.mgSide = margin(3.3 * 3.3 * d.reMax2);
+        d.prec = MPSGPU_PRECISION_FP64;
     }
     if (d.K > 64) { g_lastError = "neighbour row capacity above the 64-bit entry masks"; mpsgpu_destroy(h); return MPSGPU_ERR_UNSUPPORTED; }
     // mesh and wall tables
@@ -578,6 +623,17 @@ int mpsgpu_run_op(mpsgpu_t h, int op) {
     int e = runOpImpl(h, op);
     if (e) return e;
     return checkDeviceErrors(h);
+}
+
+int mpsgpu_set_precision(mpsgpu_t h, int precision) {
+    if (!h || (precision != MPSGPU_PRECISION_FP64 && precision != MPSGPU_PRECISION_DF32)) return MPSGPU_ERR_ARG;
+    if (precision != h->d.prec) {
+        h->d.prec = precision;
+        h->listValid = false;
+        h->masksValid = false;
+        h->cacheValid = false;
+    }
+    return 0;
 }
 
 int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm, double tol, int max_iter) {
@@ -707,6 +763,7 @@ int mpsgpu_set_field(mpsgpu_t h, int f, const void* host) {
     // any state change can alter list membership, masks or the near-wall set
     h->listValid = false;
     h->masksValid = false;
+    h->cacheValid = false;
     if (f == MPS_F_POS) launchPosf(h->d, h->s);
     CK(cudaStreamSynchronize(h->s));
     return 0;

@@ -7,7 +7,7 @@
 // and a per-bucket insertion sort that restores ascending particle order (the
 // reference's linked lists are filled in ascending index order).
 #include <atomic>
-#include "mps_common.cuh"
+#include "mps_df.cuh"
 #include "mps_internal.h"
 
 __global__ void k_posf_cell(Dev d);
@@ -42,8 +42,10 @@ __global__ void k_cell_key(Dev d) {
             atomicAdd(d.cellCount + key, 1);
         }
         // FP32 copy of the start-of-step positions for the prefiltered scans
-        d.posf[i] = make_float4((float)(p.x - P.domainMin[0]), (float)(p.y - P.domainMin[1]),
+        float4 hi = make_float4((float)(p.x - P.domainMin[0]), (float)(p.y - P.domainMin[1]),
                                 (float)(p.z - P.domainMin[2]), 0.f);
+        d.posf[i] = hi;
+        d.posLo[i] = posLoOf(p, hi, P);
     }
     d.cellOf[i] = key;
 }
@@ -160,8 +162,10 @@ __global__ void k_posf(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.N0) return;   // every slot: stale bucket entries may name removed particles
     dvec4 p = d.pos[i];
-    d.posf[i] = make_float4((float)(p.x - d.P.domainMin[0]), (float)(p.y - d.P.domainMin[1]),
+    float4 hi = make_float4((float)(p.x - d.P.domainMin[0]), (float)(p.y - d.P.domainMin[1]),
                             (float)(p.z - d.P.domainMin[2]), 0.f);
+    d.posf[i] = hi;
+    d.posLo[i] = posLoOf(p, hi, d.P);
 }
 
 // ------------------------------------------------------------------ neighbour list
@@ -169,7 +173,9 @@ __global__ void k_posf(Dev d) {
 __global__ void k_posf_cell(Dev d) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= d.cellStart[d.nB]) return;
-    d.posfCell[s] = d.posf[d.cellSorted[s]];
+    int j = d.cellSorted[s];
+    d.posfCell[s] = d.posf[j];
+    d.posLoCell[s] = d.posLo[j];
 }
 void launchPosfCell(const Dev& d, cudaStream_t s) {
     k_posf_cell<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
@@ -209,6 +215,28 @@ __global__ void __launch_bounds__(128) k_build_nbr(Dev d) {
     if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }
     d.nbrCount[i] = cnt;
     warpCount(d.counters, (unsigned)cnt);
+}
+
+// Per-entry weights of the current list for the FP64 sweeps, when the list was built by
+// the DF32 tier (which stores none); the same expressions as k_build_nbr.
+__global__ void __launch_bounds__(128) k_fill_cache(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    int c = d.nbrCount[i];
+    for (int k = 0; k < c; k++) {
+        size_t e = (size_t)k * d.N0 + i;
+        PairG q = pairOf(d.pos[d.nbr[e]], pi);
+        double w, wd;
+        weightR(q.d2, P.reS, P.weightType, w, wd);
+        d.cw[e] = w;
+        d.cwd[e] = wd;
+        if (d.cwL) { double wl, wdl; weightR(q.d2, P.reL, P.weightType, wl, wdl); d.cwL[e] = wl; }
+    }
+}
+void launchFillCache(const Dev& d, cudaStream_t s) {
+    k_fill_cache<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
 }
 
 void launchNeighborList(const Dev& d, cudaStream_t s) {

@@ -50,6 +50,14 @@ struct Dev {
     // the 27-bucket scans reads contiguous 16-byte records and fetches the particle index
     // only for candidates that pass it
     float4* posfCell;
+    // DF32 tier (float-float pair arithmetic): lo parts of the positions (posf holds the
+    // hi parts) in particle and bucket order, velocity hi/lo parts, pressure as a
+    // float-float pair, and the half-widths (m^2) of the decision margins of float-float
+    // squared distances for the reS, reL, list and collision radii
+    int prec;                       // MPSGPU_PRECISION_*
+    float4 *posLo, *posLoCell, *velHi, *velLo;
+    float2* pressDF;
+    float mgS, mgL, mgMax, mgColl, mgSide;
     // neighbour list (ELL) and its per-entry cache for the epoch: w(r; reS), w/r^2,
     // w(r; reL) (only when reL != reS)
     int *nbrCount, *nbr;
@@ -294,4 +302,52 @@ __device__ __forceinline__ ReflG makeRefl(dvec4 xi, dvec4 mi, double eps, bool u
     return r;
 }
 
+// Repulsive wall force of MpsPressure::calcWallPressGradient (src/MpsPressure.cpp:1341-1611):
+// f = -w n for a particle whose wall distance |x - m|/2 is below reRepulsiveForce.
+__device__ __forceinline__ void wallRepulsion(const MpsParams& P, const ReflG& r, double vMax2, double f[3]) {
+    f[0] = f[1] = f[2] = 0.0;
+    double ns = r.nsqrt;
+    if (ns < P.reRepulsiveForce && ns > P.epsilonZero) {
+        double w;
+        double rho = P.DNS_FL1;
+        if (P.repulsiveForceType == 0) w = rho / (P.timeStep * P.timeStep) * (P.reRepulsiveForce - ns);
+        else if (P.repulsiveForceType == 1) w = P.repForceCoefMitsume * wfun(ns, P.reRepulsiveForce, P.weightType);
+        else if (P.repulsiveForceType == 2) {
+            double R1 = (P.reRepulsiveForce / ns) * (P.reRepulsiveForce / ns);
+            double R2 = R1 * R1;
+            w = (P.repForceCoefLennardJones * vMax2 / ns) * (R2 - R1) * rho;
+        } else {
+            double a = 1.0 - ns / P.reRepulsiveForce;
+            double W1 = (1.0 + 3.0 * 0.5 * ns / P.reRepulsiveForce), W2 = a * a * a;
+            w = (P.repForceCoefMonaghanKajtar * vMax2 / (ns - 0.0 * P.partDist)) * (1.0 / 8.0) * W1 * W2 * rho;
+        }
+        f[0] = -w * r.n[0]; f[1] = -w * r.n[1]; f[2] = -w * r.n[2];
+    }
+}
+
+// MpsVectorMatrix::correctionMatrix + inverseMatrix (Gauss-Jordan without pivoting,
+// identity when det <= eps), src/MpsVectorMatrix.cpp:20-166
+__device__ __forceinline__ void invert3(double* m, int dim, double eps) {
+    double A[9], M[9];
+#pragma unroll
+    for (int k = 0; k < 9; k++) { A[k] = m[k]; M[k] = (k % 4 == 0) ? 1.0 : 0.0; }
+    if (dim == 2) { A[2] = A[5] = A[6] = A[7] = 0.0; A[8] = 1.0; }
+    double det = (A[0] * A[4] * A[8] + A[1] * A[5] * A[6] + A[2] * A[3] * A[7]) -
+                 (A[2] * A[4] * A[6] + A[1] * A[3] * A[8] + A[0] * A[5] * A[7]);
+    if (det <= eps) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) m[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        return;
+    }
+    for (int k = 0; k < dim; k++)
+        for (int r = 0; r < dim; r++) {
+            if (r == k) continue;
+            double f = A[r * 3 + k] / A[k * 3 + k];
+            for (int c = 0; c < dim; c++) { A[r * 3 + c] -= f * A[k * 3 + c]; M[r * 3 + c] -= f * M[k * 3 + c]; }
+        }
+    for (int r = 0; r < dim; r++)
+        for (int c = 0; c < dim; c++) M[r * 3 + c] /= A[r * 3 + r];
+#pragma unroll
+    for (int k = 0; k < 9; k++) m[k] = M[k];
+}
 static inline int gridFor(int n, int block) { return (n + block - 1) / block; }

@@ -1,0 +1,215 @@
+// mps_df.cuh — float-float ("df") arithmetic for the DF32 precision tier.
+//
+// GB300 issues 304 FP64 FMA thread-instructions per cycle chip-wide against 19,456 FP32
+// FMAs (1/64), so the exact-FP64 neighbour sweeps are bound by the FP64 pipe.  In the DF32
+// tier a pair quantity is an unevaluated sum hi + lo of two FP32 numbers (about 48
+// significant bits) built only from error-free FP32 transformations: Knuth's TwoSum,
+// Dekker's Fast2Sum and the FMA-based TwoProd (as in Dekker 1971; Hida, Li & Bailey's
+// double-double library).  Every primitive uses the explicitly rounded intrinsics so the
+// compiler cannot contract a product into a later addition (that would break the
+// error-free property).  FP64 remains for per-particle conversions, for the final
+// per-particle results, and for the rare pairs whose discrete decision (radius, mirror
+// side) lies inside the error margin of the float-float value, where the reference's own
+// FP64 expression is evaluated instead — so every decision equals the reference's.
+#pragma once
+#include "mps_common.cuh"
+
+struct df {
+    float h, l;
+};
+
+__device__ __forceinline__ float fA(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fS(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fM(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fF(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// Fast2Sum (|a| >= |b| or a == 0): s + e == a + b exactly
+__device__ __forceinline__ df quick2(float a, float b) {
+    float s = fA(a, b);
+    return {s, fS(b, fS(s, a))};
+}
+// TwoSum (any a, b): s + e == a + b exactly
+__device__ __forceinline__ df two2(float a, float b) {
+    float s = fA(a, b);
+    float bb = fS(s, a);
+    return {s, fA(fS(a, fS(s, bb)), fS(b, bb))};
+}
+// TwoProd: p + e == a * b exactly
+__device__ __forceinline__ df prod2(float a, float b) {
+    float p = fM(a, b);
+    return {p, fF(a, b, -p)};
+}
+
+__device__ __forceinline__ df dfF(float a) { return {a, 0.f}; }
+__device__ __forceinline__ df operator-(df a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ df operator+(df a, df b) {
+    df s = two2(a.h, b.h);
+    return quick2(s.h, fA(s.l, fA(a.l, b.l)));
+}
+__device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }
+__device__ __forceinline__ df operator+(df a, float b) {
+    df s = two2(a.h, b);
+    return quick2(s.h, fA(s.l, a.l));
+}
+__device__ __forceinline__ df operator-(df a, float b) { return a + (-b); }
+__device__ __forceinline__ df operator*(df a, df b) {
+    df p = prod2(a.h, b.h);
+    return quick2(p.h, fF(a.h, b.l, fF(a.l, b.h, p.l)));
+}
+__device__ __forceinline__ df operator*(df a, float b) {
+    df p = prod2(a.h, b);
+    return quick2(p.h, fF(a.l, b, p.l));
+}
+__device__ __forceinline__ df& operator+=(df& a, df b) { a = a + b; return a; }
+__device__ __forceinline__ df& operator-=(df& a, df b) { a = a - b; return a; }
+// ordering of normalised values (|l| <= ulp(h)/2)
+__device__ __forceinline__ bool operator<(df a, df b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+__device__ __forceinline__ bool operator>(df a, df b) { return b < a; }
+
+// conversions (FP64: per particle, not per pair)
+__device__ __forceinline__ df dfD(double x) {
+    float h = __double2float_rn(x);
+    return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double dD(df a) { return (double)a.h + (double)a.l; }
+
+// 1/sqrt(a) for a > 0: FP32 estimate refined by one Newton step in float-float
+// (y1 = y + y (1 - a y^2) / 2; the estimate's relative error ~2^-22 becomes ~2^-44).
+__device__ __forceinline__ df rsqrtDF(df a) {
+    float y = rsqrtf(a.h);
+    df y2 = prod2(y, y);
+    df t = a * y2;                       // ~1
+    float r = fS(fS(1.0f, t.h), t.l);    // 1 - a y^2, exact leading difference
+    return quick2(y, fM(fM(y, r), 0.5f));
+}
+
+// ------------------------------------------------------------------ particle copies
+// Positions are held relative to domainMin as hi = fl32(x - min) (the posf copy the
+// prefilters already read) and lo = fl32((x - min) - hi): |x - min - hi - lo| <= 2^-48 |x - min|.
+__device__ __forceinline__ float4 posLoOf(dvec4 p, float4 hi, const MpsParams& P) {
+    return make_float4(__double2float_rn((p.x - P.domainMin[0]) - (double)hi.x),
+                       __double2float_rn((p.y - P.domainMin[1]) - (double)hi.y),
+                       __double2float_rn((p.z - P.domainMin[2]) - (double)hi.z), 0.f);
+}
+
+struct V3 {
+    df x, y, z;
+};
+// x_j - x_i from the hi/lo copies: the hi difference is split exactly by TwoSum and the
+// lo difference added, then renormalised.
+__device__ __forceinline__ df diffDF(float hj, float lj, float hi, float li) {
+    df s = two2(hj, -hi);
+    return quick2(s.h, fA(s.l, fS(lj, li)));
+}
+__device__ __forceinline__ V3 diff3(float4 hj, float4 lj, float4 hi, float4 li) {
+    return {diffDF(hj.x, lj.x, hi.x, li.x), diffDF(hj.y, lj.y, hi.y, li.y), diffDF(hj.z, lj.z, hi.z, li.z)};
+}
+__device__ __forceinline__ df norm2(const V3& v) { return v.x * v.x + v.y * v.y + v.z * v.z; }
+__device__ __forceinline__ df dot3(const V3& a, const V3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+struct PairF {
+    V3 v;    // x_j - x_i
+    df d2;   // |x_j - x_i|^2
+};
+__device__ __forceinline__ PairF pairDF(float4 hj, float4 lj, float4 hi, float4 li) {
+    PairF q;
+    q.v = diff3(hj, lj, hi, li);
+    q.d2 = norm2(q.v);
+    return q;
+}
+
+// Weight and weight / r^2 of MpsParticle::weight (src/MpsParticle.cpp:57-72) from r^2.
+struct WeightDF {
+    df w, wr2;
+};
+struct RadiusDF {
+    df re, invRe;
+};
+__device__ __forceinline__ WeightDF weightDF(df d2, const RadiusDF& R, int t) {
+    df rinv = rsqrtDF(d2);
+    WeightDF o;
+    switch (t) {
+        case 1: { df r = d2 * rinv; o.w = R.re * rinv + r * R.invRe - 2.0f; } break;
+        case 2: { df r = d2 * rinv; o.w = R.re * rinv - r * R.invRe; } break;
+        case 3: { df a = -(d2 * rinv * R.invRe) + 1.0f; o.w = a * a * a; } break;
+        case 4: { df a = -(d2 * rinv * R.invRe) + 1.0f; o.w = a * a; } break;
+        default: o.w = R.re * rinv - 1.0f; break;
+    }
+    o.wr2 = o.w * (rinv * rinv);
+    return o;
+}
+
+// ------------------------------------------------------------------ decisions
+// a < b for two float-float values each within `mg` of the reference's FP64 value; inside
+// the margin the reference's FP64 expression decides (exact()).
+template <class F>
+__device__ __forceinline__ bool lessDF(df a, df b, float mg, F&& exact) {
+    df t = a - b;
+    if (t.h < -mg) return true;
+    if (t.h > mg) return false;
+    return exact();
+}
+// dst_ij^2 < R2 (R2 the FP64 radius^2 of the reference's test)
+__device__ __forceinline__ bool inBallDF(const Dev& d, df d2, df R2f, float mg, double R2, int i, int j) {
+    return lessDF(d2, R2f, mg, [&] { return pairOf(d.pos[j], d.pos[i]).d2 < R2; });
+}
+
+// Mirror-side context of particle i (the SideCtx test in float-float): the mirror position
+// split into hi/lo parts relative to domainMin.
+struct SideDF {
+    float4 mh, ml;
+    bool check;
+};
+__device__ __forceinline__ SideDF sideDF(const Dev& d, int i, dvec4 pi) {
+    SideDF s;
+    s.check = false;
+    if (d.P.wallType == 0) return s;
+    dvec4 m = d.mirror[i];
+    double a = pi.x - m.x, b = pi.y - m.y, c = pi.z - m.z;
+    double lim = 2.2 * d.P.reL;
+    s.check = (a * a + b * b + c * c) <= lim * lim;
+    if (s.check) {
+        const MpsParams& P = d.P;
+        s.mh = make_float4((float)(m.x - P.domainMin[0]), (float)(m.y - P.domainMin[1]),
+                           (float)(m.z - P.domainMin[2]), 0.f);
+        s.ml = posLoOf(m, s.mh, P);
+    }
+    return s;
+}
+// dst_ij^2 < dst_imj^2 (j not on the mirror side of i), given the float-float d2
+__device__ __forceinline__ bool sideOkDF(const Dev& d, const SideDF& s, float4 hj, float4 lj, df d2, int i, int j) {
+    if (!s.check) return true;
+    df dm2 = norm2(diff3(hj, lj, s.mh, s.ml));
+    return lessDF(d2, dm2, d.mgSide, [&] {
+        dvec4 pj = d.pos[j];
+        return pairOf(pj, d.pos[i]).d2 < pairMirror(pj, d.mirror[i]).dm2;
+    });
+}
+
+// 27-bucket scan (reference order) over the stale bucket list with the FP32 prefilter on
+// the hi parts; f(j, s, hj) receives every candidate with FP32 squared distance <= hi
+// (s = its slot in bucket order, so posLoCell[s] is its lo part).
+template <class F>
+__device__ __forceinline__ void forCellsDF(const Dev& d, dvec4 pi, float4 fi, float hi, F&& f) {
+    const MpsParams& P = d.P;
+    int ix, iy, iz;
+    bucketCoords(P, pi.x, pi.y, pi.z, ix, iy, iz);
+    int dz = (int)(P.dim - 2.0);
+    int minZ = (iz - 1) * dz, maxZ = (iz + 1) * dz;
+    for (int jz = minZ; jz <= maxZ; jz++)
+        for (int jy = iy - 1; jy <= iy + 1; jy++)
+            for (int jx = ix - 1; jx <= ix + 1; jx++) {
+                long long jb = (long long)jz * P.numBucketsXY + (long long)jy * P.numBucketsX + jx;
+                if (jb < 0 || jb >= d.nB) continue;
+                int s0 = d.cellStart[jb], s1 = d.cellStart[jb + 1];
+                for (int s = s0; s < s1; s++) {
+                    float4 fj = __ldg(&d.posfCell[s]);
+                    float ex = fj.x - fi.x, ey = fj.y - fi.y, ez = fj.z - fi.z;
+                    if (ex * ex + ey * ey + ez * ez > hi) continue;
+                    f(__ldg(d.cellSorted + s), s, fj);
+                }
+            }
+}
+
+__device__ __forceinline__ RadiusDF radiusDF(double re) { return {dfD(re), dfD(1.0 / re)}; }
+__device__ __forceinline__ df dfOf(float h, float l) { return quick2(h, l); }

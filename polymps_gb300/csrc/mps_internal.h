@@ -37,6 +37,7 @@ void launchNeighborList(const Dev& d, cudaStream_t s);
 void launchPosf(const Dev& d, cudaStream_t s);       // FP32 copy, then its bucket-ordered copy
 void launchPosfCell(const Dev& d, cudaStream_t s);   // bucket-ordered copy only
 void launchSideMasks(const Dev& d, cudaStream_t s);
+void launchFillCache(const Dev& d, cudaStream_t s);
 
 // mps_ops.cu
 void launchViscosity(const Dev& d, cudaStream_t s);
@@ -44,6 +45,7 @@ void launchAddGravity(const Dev& d, cudaStream_t s);
 void launchPredict(const Dev& d, cudaStream_t s);
 void launchOutOfDomain(const Dev& d, int* flags, int* counter, cudaStream_t s);
 void launchCollision(const Dev& d, cudaStream_t s);
+void launchCollisionApply(const Dev& d, cudaStream_t s);
 void launchWallNpcd(const Dev& d, cudaStream_t s);
 void launchCorrectionMatrix(const Dev& d, cudaStream_t s);
 void launchPndNeighNpcd(const Dev& d, cudaStream_t s);
@@ -59,6 +61,18 @@ void launchWallViscosity(const Dev& d, cudaStream_t s);
 void launchCorrect(const Dev& d, cudaStream_t s);
 void launchShifting(const Dev& d, cudaStream_t s);
 void launchDummyVelocity(const Dev& d, cudaStream_t s);
+
+// mps_ops_df.cu (DF32 tier)
+void launchNeighborListDF(const Dev& d, cudaStream_t s);
+void launchSideMasksDF(const Dev& d, cudaStream_t s);
+void launchViscosityDF(const Dev& d, cudaStream_t s);
+void launchCollisionDF(const Dev& d, cudaStream_t s);
+void launchWallNpcdDF(const Dev& d, cudaStream_t s);
+void launchCorrectionMatrixDF(const Dev& d, cudaStream_t s);
+void launchPndNeighNpcdDF(const Dev& d, cudaStream_t s);
+void launchPressGradientDF(const Dev& d, cudaStream_t s);
+void launchWallPressGradientDF(const Dev& d, cudaStream_t s);
+void launchWallViscosityDF(const Dev& d, cudaStream_t s);
 
 // mps_wall.cu
 void launchWallDistance(const Dev& d, cudaStream_t s);
@@ -77,6 +91,7 @@ struct PpeBuffers {
 };
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);
+void launchPpeAssembleDF(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 // Returns iterations and final relative residual through host pointers (synchronises).
 int ppeSolvePlain(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cudaStream_t s,
                   int* iters, double* relres, double* relres0, Prof* prof);

@@ -6,7 +6,7 @@
 // shifting/dummy sweeps, which see their positions once, walk the 27 buckets directly.
 // Every sweep applies the reference's own radius and mirror-side tests to each entry,
 // with the distance comparisons evaluated in exact FP64 (see mps_common.cuh).
-#include "mps_common.cuh"
+#include "mps_df.cuh"
 #include "mps_internal.h"
 
 #define BLK 128
@@ -172,9 +172,12 @@ __global__ void k_collision_apply(Dev d) {
     }
     d.dvel[i] = make_dvec4(0, 0, 0, 0);
 }
+void launchCollisionApply(const Dev& d, cudaStream_t s) {
+    k_collision_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+}
 void launchCollision(const Dev& d, cudaStream_t s) {
     k_collision<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
-    k_collision_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    launchCollisionApply(d, s);
 }
 
 // ------------------------------------------------------------------ wall NPCD
@@ -221,29 +224,6 @@ void launchWallNpcd(const Dev& d, cudaStream_t s) {
 // ------------------------------------------------------------------ correction matrix
 // MpsVectorMatrix::correctionMatrix + inverseMatrix (Gauss-Jordan without pivoting,
 // identity when det <= eps or numNeigh < 4), src/MpsVectorMatrix.cpp:20-166
-__device__ void invert3(double* m, int dim, double eps) {
-    double A[9], M[9];
-#pragma unroll
-    for (int k = 0; k < 9; k++) { A[k] = m[k]; M[k] = (k % 4 == 0) ? 1.0 : 0.0; }
-    if (dim == 2) { A[2] = A[5] = A[6] = A[7] = 0.0; A[8] = 1.0; }
-    double det = (A[0] * A[4] * A[8] + A[1] * A[5] * A[6] + A[2] * A[3] * A[7]) -
-                 (A[2] * A[4] * A[6] + A[1] * A[3] * A[8] + A[0] * A[5] * A[7]);
-    if (det <= eps) {
-#pragma unroll
-        for (int k = 0; k < 9; k++) m[k] = (k % 4 == 0) ? 1.0 : 0.0;
-        return;
-    }
-    for (int k = 0; k < dim; k++)
-        for (int r = 0; r < dim; r++) {
-            if (r == k) continue;
-            double f = A[r * 3 + k] / A[k * 3 + k];
-            for (int c = 0; c < dim; c++) { A[r * 3 + c] -= f * A[k * 3 + c]; M[r * 3 + c] -= f * M[k * 3 + c]; }
-        }
-    for (int r = 0; r < dim; r++)
-        for (int c = 0; c < dim; c++) M[r * 3 + c] /= A[r * 3 + r];
-#pragma unroll
-    for (int k = 0; k < 9; k++) m[k] = M[k];
-}
 __global__ void __launch_bounds__(BLK) k_corr_matrix(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
@@ -675,24 +655,8 @@ __global__ void __launch_bounds__(BLK) k_wall_press_grad(Dev d) {
         wS = phi(Pi, ni, s.dm2, wS);
         ax += s.m0 * wS; ay += s.m1 * wS; az += s.m2 * wS;
     }
-    double f[3] = {0, 0, 0};
-    double ns = r.nsqrt;
-    if (ns < P.reRepulsiveForce && ns > P.epsilonZero) {
-        double w;
-        double rho = P.DNS_FL1;
-        if (P.repulsiveForceType == 0) w = rho / (P.timeStep * P.timeStep) * (P.reRepulsiveForce - ns);
-        else if (P.repulsiveForceType == 1) w = P.repForceCoefMitsume * wfun(ns, P.reRepulsiveForce, P.weightType);
-        else if (P.repulsiveForceType == 2) {
-            double R1 = (P.reRepulsiveForce / ns) * (P.reRepulsiveForce / ns);
-            double R2 = R1 * R1;
-            w = (P.repForceCoefLennardJones * vMax2 / ns) * (R2 - R1) * rho;
-        } else {
-            double a = 1.0 - ns / P.reRepulsiveForce;
-            double W1 = (1.0 + 3.0 * 0.5 * ns / P.reRepulsiveForce), W2 = a * a * a;
-            w = (P.repForceCoefMonaghanKajtar * vMax2 / (ns - 0.0 * P.partDist)) * (1.0 / 8.0) * W1 * W2 * rho;
-        }
-        f[0] = -w * r.n[0]; f[1] = -w * r.n[1]; f[2] = -w * r.n[2];
-    }
+    double f[3];
+    wallRepulsion(P, r, vMax2, f);
     double g0 = P.relaxPress * (r.R[0] * ax + r.R[1] * ay + r.R[2] * az) * P.coeffPressGrad - f[0];
     double g1 = P.relaxPress * (r.R[3] * ax + r.R[4] * ay + r.R[5] * az) * P.coeffPressGrad - f[1];
     double g2 = P.relaxPress * (r.R[6] * ax + r.R[7] * ay + r.R[8] * az) * P.coeffPressGrad - f[2];
@@ -936,8 +900,10 @@ __global__ void k_apply_shift(Dev d) {
     dvec4 x = d.pos[i], s = d.shift[i];
     x.x += s.x; x.y += s.y; x.z += s.z;
     d.pos[i] = x;
-    d.posf[i] = make_float4((float)(x.x - d.P.domainMin[0]), (float)(x.y - d.P.domainMin[1]),
+    float4 hi = make_float4((float)(x.x - d.P.domainMin[0]), (float)(x.y - d.P.domainMin[1]),
                             (float)(x.z - d.P.domainMin[2]), 0.f);
+    d.posf[i] = hi;
+    d.posLo[i] = posLoOf(x, hi, d.P);
 }
 void launchShifting(const Dev& d, cudaStream_t s) {
     const MpsParams& P = d.P;

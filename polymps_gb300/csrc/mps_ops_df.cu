@@ -1,0 +1,573 @@
+// mps_ops_df.cu — the DF32 precision tier of the neighbour sweeps on sm_103a.
+//
+// Same operators, same reference order and same discrete decisions as mps_ops.cu, with
+// the per-pair arithmetic in float-float (mps_df.cuh) instead of FP64: pair vectors come
+// from the hi/lo position copies, weights are recomputed per entry from the float-float
+// squared distance (no per-entry weight cache: FP32 work is cheaper than its HBM traffic),
+// sums are float-float and each particle's result is assembled in FP64 once.  Radius and
+// mirror-side decisions whose float-float value lies within the error margin fall back to
+// the reference's FP64 expression, so entry sets, masks and flags equal the FP64 tier's.
+#include "mps_df.cuh"
+#include "mps_internal.h"
+
+#define BLK 128
+
+// ------------------------------------------------------------------ copies
+__global__ void k_df_vel(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N0) return;
+    dvec4 v = d.vel[i];
+    float4 h = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+    d.velHi[i] = h;
+    d.velLo[i] = make_float4(__double2float_rn(v.x - (double)h.x), __double2float_rn(v.y - (double)h.y),
+                             __double2float_rn(v.z - (double)h.z), 0.f);
+}
+__global__ void k_df_press(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N0) return;
+    df p = dfD(d.press[i]);
+    d.pressDF[i] = make_float2(p.h, p.l);
+}
+static void launchVelDF(const Dev& d, cudaStream_t s) { k_df_vel<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
+static void launchPressDF(const Dev& d, cudaStream_t s) { k_df_press<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
+
+__device__ __forceinline__ df loadDF(const float2* p, int j) {
+    float2 v = __ldg(p + j);
+    return {v.x, v.y};
+}
+
+// ------------------------------------------------------------------ neighbour list
+// The list of the current positions through the stale buckets: candidates whose FP32
+// squared distance is below the band are members, those above it were never seen by the
+// prefilter, and only the band's few candidates are decided in float-float (and, inside
+// the float-float margin, in FP64).  No per-entry weights: the DF32 sweeps recompute them.
+__global__ void __launch_bounds__(128) k_build_nbr_df(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    dvec4 pi = d.pos[i];
+    float4 hi = d.posf[i], li = d.posLo[i];
+    df R2 = dfD(d.reMax2);
+    int cnt = 0;
+    const size_t N0 = d.N0;
+    forCellsDF(d, pi, hi, d.bandHi, [&](int j, int s, float4 hj) {
+        if (j == i) return;
+        float ex = hj.x - hi.x, ey = hj.y - hi.y, ez = hj.z - hi.z;
+        if (!(ex * ex + ey * ey + ez * ez < d.bandLo)) {
+            PairF q = pairDF(hj, __ldg(&d.posLoCell[s]), hi, li);
+            if (!inBallDF(d, q.d2, R2, d.mgMax, d.reMax2, i, j)) return;
+        }
+        if (cnt < d.K) d.nbr[(size_t)cnt * N0 + i] = j;
+        cnt++;
+    });
+    if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }
+    d.nbrCount[i] = cnt;
+    warpCount(d.counters, (unsigned)cnt);
+}
+void launchNeighborListDF(const Dev& d, cudaStream_t s) {
+    cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long), s);
+    launchPosf(d, s);
+    k_build_nbr_df<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ entry masks
+__global__ void __launch_bounds__(128) k_side_masks_df(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    int c = d.nbrCount[i];
+    unsigned long long all = (c >= 64) ? ~0ull : ((1ull << c) - 1ull);
+    dvec4 pi = d.pos[i];
+    SideDF sc = sideDF(d, i, pi);
+    bool fullS = P.reS2 >= d.reMax2, fullL = P.reL2 >= d.reMax2;
+    unsigned long long mS = all, mL = all;
+    if (sc.check || !fullS || !fullL) {
+        mS = 0; mL = 0;
+        float4 hi = d.posf[i], li = d.posLo[i];
+        df RS = dfD(P.reS2), RL = dfD(P.reL2);
+        const int* row = d.nbr + i;
+        for (int k = 0; k < c; k++) {
+            int j = __ldg(row + (size_t)k * d.N0);
+            float4 hj = d.posf[j], lj = d.posLo[j];
+            df d2 = norm2(diff3(hj, lj, hi, li));
+            if (!sideOkDF(d, sc, hj, lj, d2, i, j)) continue;
+            if (fullS || inBallDF(d, d2, RS, d.mgS, P.reS2, i, j)) mS |= 1ull << k;
+            if (fullL || inBallDF(d, d2, RL, d.mgL, P.reL2, i, j)) mL |= 1ull << k;
+        }
+    }
+    d.maskS[i] = mS;
+    d.maskL[i] = mL;
+    if (P.wallType == 1 && d.type[i] == P.fluid && d.nearWall[i]) {
+        int slot = atomicAdd(d.nearCount, 1);
+        d.nearList[slot] = i;
+    }
+}
+void launchSideMasksDF(const Dev& d, cudaStream_t s) {
+    cudaMemsetAsync(d.nearCount, 0, sizeof(int), s);
+    k_side_masks_df<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ viscosity
+// MpsViscosity::calcViscosity, src/MpsViscosity.cpp:20-100, at the start-of-step
+// positions through the 27 buckets (Newtonian: uniform MEU and RHO).
+__global__ void __launch_bounds__(128) k_visc_df(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    float4 hi = d.posf[i], li = d.posLo[i];
+    float4 vh = d.velHi[i], vl = d.velLo[i];
+    SideDF sc = sideDF(d, i, pi);
+    df R2 = dfD(P.reL2);
+    RadiusDF RL = radiusDF(P.reL);
+    double mu = P.KNM_VS1 * P.DNS_FL1, rho = P.DNS_FL1;
+    df neuW = dfD((2.0 * mu) / rho), neuF = dfD((2.0 * mu * mu / (mu + mu)) / rho);
+    df ax = dfF(0.f), ay = dfF(0.f), az = dfF(0.f);
+    forCellsDF(d, pi, hi, d.bandHiL, [&](int j, int s, float4 hj) {
+        if (j == i) return;
+        float4 lj = __ldg(&d.posLoCell[s]);
+        PairF q = pairDF(hj, lj, hi, li);
+        if (!inBallDF(d, q.d2, R2, d.mgL, P.reL2, i, j)) return;
+        if (!sideOkDF(d, sc, hj, lj, q.d2, i, j)) return;
+        WeightDF w = weightDF(q.d2, RL, P.weightType);
+        df c = w.w * ((d.type[j] == P.wall) ? neuW : neuF);
+        float4 vhj = d.velHi[j], vlj = d.velLo[j];
+        ax += diffDF(vhj.x, vlj.x, vh.x, vl.x) * c;
+        ay += diffDF(vhj.y, vlj.y, vh.y, vl.y) * c;
+        az += diffDF(vhj.z, vlj.z, vh.z, vl.z) * c;
+    });
+    double cv = P.coeffViscMultiphase;
+    d.acc[i] = make_dvec4(cv * dD(ax), cv * dD(ay), cv * dD(az), 0.0);
+}
+void launchViscosityDF(const Dev& d, cudaStream_t s) {
+    launchVelDF(d, s);
+    k_visc_df<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ collision
+// MpsParticleCollision::checkParticleCollisions, src/MpsParticleCollision.cpp:22-119.
+// The sign test fDT > 0 is decided in float-float outside a margin that bounds the
+// difference from the FP64 value, and in FP64 inside it.
+__global__ void __launch_bounds__(BLK) k_collision_df(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    df dvx = dfF(0.f), dvy = dfF(0.f), dvz = dfF(0.f);
+    bool any = false;
+    if (d.type[i] == P.fluid) {
+        double mi = P.DNS_FL1;
+        dvec4 pi = d.pos[i];
+        float4 hi = d.posf[i], li = d.posLo[i];
+        float4 vh = d.velHi[i], vl = d.velLo[i];
+        float vin = fabsf(vh.x) + fabsf(vh.y) + fabsf(vh.z);
+        SideDF sc = sideDF(d, i, pi);
+        df R2 = dfD(P.distCollisionLimit2);
+        df cF = dfD(P.restitutionCollision * P.DNS_FL1 / (mi + P.DNS_FL1));
+        df cW = dfD(P.restitutionCollision * P.densityWall / (mi + P.densityWall));
+        forNbrs(d, i, [&](int j) {
+            float4 hj = d.posf[j], lj = d.posLo[j];
+            PairF q = pairDF(hj, lj, hi, li);
+            if (!inBallDF(d, q.d2, R2, d.mgColl, P.distCollisionLimit2, i, j)) return;
+            if (!sideOkDF(d, sc, hj, lj, q.d2, i, j)) return;
+            float4 vhj = d.velHi[j], vlj = d.velLo[j];
+            V3 dv = {diffDF(vh.x, vl.x, vhj.x, vlj.x), diffDF(vh.y, vl.y, vhj.y, vlj.y),
+                     diffDF(vh.z, vl.z, vhj.z, vlj.z)};
+            df fDT = dot3(dv, q.v);
+            float rn = fabsf(q.v.x.h) + fabsf(q.v.y.h) + fabsf(q.v.z.h);
+            float dn = fabsf(dv.x.h) + fabsf(dv.y.h) + fabsf(dv.z.h);
+            float vjn = fabsf(vhj.x) + fabsf(vhj.y) + fabsf(vhj.z);
+            float mg = 1e-9f * dn * rn + 1e-11f * (vin + vjn) * rn;
+            bool pos;
+            if (fDT.h > mg) pos = true;
+            else if (fDT.h < -mg) pos = false;
+            else {
+                dvec4 pj = d.pos[j], vj = d.vel[j], vi = d.vel[i];
+                PairG g = pairOf(pj, pi);
+                pos = (vi.x - vj.x) * g.v0 + (vi.y - vj.y) * g.v1 + (vi.z - vj.z) * g.v2 > 0.0;
+            }
+            if (!pos) return;
+            bool jf = d.type[j] == P.fluid;
+            df rinv = rsqrtDF(q.d2);
+            df k = fDT * (jf ? cF : cW) * (rinv * rinv);
+            if (!jf) k = k * 2.0f;
+            dvx -= q.v.x * k; dvy -= q.v.y * k; dvz -= q.v.z * k;
+            any = true;
+        });
+    }
+    d.dvel[i] = any ? make_dvec4(dD(dvx), dD(dvy), dD(dvz), 0.0) : make_dvec4(0, 0, 0, 0);
+}
+void launchCollisionDF(const Dev& d, cudaStream_t s) {
+    launchVelDF(d, s);
+    k_collision_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    launchCollisionApply(d, s);
+}
+
+// ------------------------------------------------------------------ wall sweeps
+__device__ __forceinline__ int nearIndexDF(const Dev& d) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    return (t < *d.nearCount) ? d.nearList[t] : -1;
+}
+struct MirrorDF {
+    float4 mh, ml;
+};
+__device__ __forceinline__ MirrorDF mirrorDF(const Dev& d, dvec4 m) {
+    MirrorDF o;
+    const MpsParams& P = d.P;
+    o.mh = make_float4((float)(m.x - P.domainMin[0]), (float)(m.y - P.domainMin[1]), (float)(m.z - P.domainMin[2]), 0.f);
+    o.ml = posLoOf(m, o.mh, P);
+    return o;
+}
+// One wall-sweep entry: j within R of i, its mirror image within R of the mirror of i
+// and j not on the mirror side (e.g. src/MpsPndNeigh.cpp:140-160).  Returns the mirror
+// pair (x_j - m_i, |x_j - m_i|^2) through m.
+__device__ __forceinline__ bool wallEntryDF(const Dev& d, int i, int j, float4 hi, float4 li, const MirrorDF& M,
+                                            df R2f, float mg, double R2, PairF& m) {
+    float4 hj = d.posf[j], lj = d.posLo[j];
+    PairF q = pairDF(hj, lj, hi, li);
+    if (!inBallDF(d, q.d2, R2f, mg, R2, i, j)) return false;
+    m = pairDF(hj, lj, M.mh, M.ml);
+    if (!lessDF(m.d2, R2f, mg, [&] { return pairMirror(d.pos[j], d.mirror[i]).dm2 < R2; })) return false;
+    return lessDF(q.d2, m.d2, d.mgSide, [&] {
+        dvec4 pj = d.pos[j];
+        return pairOf(pj, d.pos[i]).d2 < pairMirror(pj, d.mirror[i]).dm2;
+    });
+}
+
+// MpsPndNeigh::calcWallNPCD, src/MpsPndNeigh.cpp:105-195
+__global__ void __launch_bounds__(BLK) k_wall_npcd_df(Dev d) {
+    int i = nearIndexDF(d);
+    if (i < 0) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i], mi = d.mirror[i];
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
+    float4 hi = d.posf[i], li = d.posLo[i];
+    MirrorDF M = mirrorDF(d, mi);
+    df R2 = dfD(P.reS2);
+    RadiusDF RS = radiusDF(P.reS);
+    df sx = dfF(0.f), sy = dfF(0.f), sz = dfF(0.f);
+    forNbrs(d, i, [&](int j) {
+        PairF m;
+        if (!wallEntryDF(d, i, j, hi, li, M, R2, d.mgS, P.reS2, m)) return;
+        df wS = weightDF(m.d2, RS, P.weightType).w;
+        sx += m.v.x * wS; sy += m.v.y * wS; sz += m.v.z * wS;
+    });
+    double dx = dD(sx), dy = dD(sy), dz = dD(sz);
+    PairM s = pairMirror(pi, mi);
+    if (s.dm2 < P.reS2) {
+        double wS = wfun(sqrt(s.dm2), P.reS, P.weightType);
+        dx += s.m0 * wS; dy += s.m1 * wS; dz += s.m2 * wS;
+    }
+    dvec4 n = d.npcd[i];
+    n.x += r.R[0] * dx + r.R[1] * dy + r.R[2] * dz;
+    n.y += r.R[3] * dx + r.R[4] * dy + r.R[5] * dz;
+    n.z += r.R[6] * dx + r.R[7] * dy + r.R[8] * dz;
+    d.npcd[i] = n;
+}
+void launchWallNpcdDF(const Dev& d, cudaStream_t s) {
+    if (d.P.wallType != 1) return;
+    k_wall_npcd_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ correction matrix
+__global__ void __launch_bounds__(BLK) k_corr_matrix_df(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    float4 hi = d.posf[i], li = d.posLo[i];
+    RadiusDF RS = radiusDF(P.reS);
+    df m00 = dfF(0.f), m01 = m00, m02 = m00, m11 = m00, m12 = m00, m22 = m00;
+    forMask(d, i, d.maskS[i], [&](int j, size_t) {
+        PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
+        df wd = weightDF(q.d2, RS, P.weightType).wr2;
+        df t0 = q.v.x * wd, t1 = q.v.y * wd, t2 = q.v.z * wd;
+        m00 += t0 * q.v.x; m01 += t0 * q.v.y; m02 += t0 * q.v.z;
+        m11 += t1 * q.v.y; m12 += t1 * q.v.z; m22 += t2 * q.v.z;
+    });
+    double c = -P.coeffPressGrad;
+    double m[9];
+    m[0] = dD(m00) * c; m[1] = dD(m01) * c; m[2] = dD(m02) * c;
+    m[4] = dD(m11) * c; m[5] = dD(m12) * c; m[8] = dD(m22) * c;
+    m[3] = m[1]; m[6] = m[2]; m[7] = m[5];
+    invert3(m, (int)P.dim, P.epsilonZero);
+    if (d.numNeigh[i] < 4) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) m[k] = (k % 4 == 0) ? 1.0 : 0.0;
+    }
+    d.c1[i] = make_dvec4(m[0], m[1], m[2], 0.0);
+    d.c2[i] = make_dvec4(m[3], m[4], m[5], 0.0);
+    d.c3[i] = make_dvec4(m[6], m[7], m[8], 0.0);
+}
+void launchCorrectionMatrixDF(const Dev& d, cudaStream_t s) { k_corr_matrix_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
+
+// ------------------------------------------------------------------ PND / NPCD
+// MpsPndNeigh::calcPndnNeighNPCD, src/MpsPndNeigh.cpp:199-331
+__global__ void __launch_bounds__(BLK) k_pnd_npcd_df(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    float4 hi = d.posf[i], li = d.posLo[i];
+    RadiusDF RS = radiusDF(P.reS);
+    unsigned long long mL = d.maskL[i];
+    int nn = d.nNeighWall[i] + __popcll(mL);
+    df ni = dfF(0.f), nx = ni, ny = ni, nz = ni;
+    forMask(d, i, mL & d.maskS[i], [&](int j, size_t) {
+        PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
+        df wS = weightDF(q.d2, RS, P.weightType).w;
+        ni += wS;
+        nx += q.v.x * wS; ny += q.v.y * wS; nz += q.v.z * wS;
+    });
+    double nd = dD(ni);
+    dvec4 np = d.npcd[i];
+    np.x += dD(nx); np.y += dD(ny); np.z += dD(nz);
+    if (P.pndType == 0 || P.pndType == 1) {
+        d.pndki[i] = d.pndi[i];
+        d.pndi[i] = nd + d.pndWall[i];
+    }
+    double pndSmall = nd + d.pndWall[i];
+    d.pndSmall[i] = pndSmall;
+    d.numNeigh[i] = nn;
+    if (nd > P.epsilonZero) { np.x /= pndSmall; np.y /= pndSmall; np.z /= pndSmall; }
+    d.npcd[i] = np;
+    d.npcd2[i] = np.x * np.x + np.y * np.y + np.z * np.z;
+    dvec4 nw = d.polyNormal[i];
+    d.devDot[i] = (np.x * nw.x + np.y * nw.y + np.z * nw.z < 0.0) ? 1.0 : -1.0;
+}
+void launchPndNeighNpcdDF(const Dev& d, cudaStream_t s) { k_pnd_npcd_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
+
+// ------------------------------------------------------------------ PPE assembly
+// MpsPressure::solvePressurePoissonPnd, src/MpsPressure.cpp:169-286 (matrix values are
+// assembled in float-float and stored in FP64)
+__global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    int bci = d.bc[i];
+    if (bci == P.other || bci == P.surface) {
+        B.diag[i] = 1.0; B.rowLen[i] = 0; B.b[i] = 0.0;
+        warpCount(d.counters + 1, 0u);
+        return;
+    }
+    float4 hi = d.posf[i], li = d.posLo[i];
+    RadiusDF RL = radiusDF(P.reL);
+    df cP = dfD(P.coeffPPE);
+    df cG = dfD(P.coeffPPE * P.DNS_FL1);
+    df gx = dfD(P.gravity[0]), gy = dfD(P.gravity[1]), gz = dfD(P.gravity[2]);
+    df sum = dfF(0.f), src = dfF(0.f);
+    int len = 0;
+    forMask(d, i, d.maskL[i], [&](int j, size_t) {
+        PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
+        df wL = weightDF(q.d2, RL, P.weightType).w;
+        if (d.type[j] == P.dummyWall) {
+            src -= (q.v.x * gx + q.v.y * gy + q.v.z * gz) * wL * cG;
+        } else {
+            df mij = wL * cP;
+            sum -= mij;
+            if (d.bc[j] == P.inner) {
+                size_t k = (size_t)len * B.N0 + i;
+                B.val[k] = dD(mij);
+                B.col[k] = j;
+                len++;
+            }
+        }
+    });
+    double rho = P.DNS_FL1;
+    B.diag[i] = dD(sum) - P.alphaCompressibility * rho / (P.timeStep * P.timeStep);
+    B.rowLen[i] = len;
+    B.b[i] = dD(src) + (-P.coeffPPESource * rho * (d.pndSmall[i] - P.pndSmallZero));
+    warpCount(d.counters + 1, (unsigned)len);
+}
+void launchPpeAssembleDF(const Dev& d, const PpeBuffers& B, cudaStream_t s) {
+    cudaMemsetAsync(d.counters + 1, 0, sizeof(unsigned long long), s);
+    k_ppe_assemble_df<<<gridFor(d.N0, 128), 128, 0, s>>>(d, B);
+}
+
+// ------------------------------------------------------------------ pressure gradient
+// MpsPressure::calcPressGradient, src/MpsPressure.cpp:1217-1338
+__global__ void __launch_bounds__(BLK) k_press_grad_df(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    float4 hi = d.posf[i], li = d.posLo[i];
+    RadiusDF RS = radiusDF(P.reS);
+    df Pi = loadDF(d.pressDF, i), pmin = Pi;
+    double ni = d.pndi[i];
+    int gt = P.gradientType;
+    unsigned long long mS = d.maskS[i];
+    if (gt == 0 || gt == 2) {
+        forMask(d, i, mS, [&](int j, size_t) {
+            df pj = loadDF(d.pressDF, j);
+            if (pmin > pj) pmin = pj;
+        });
+    }
+    df C[9];
+    if (P.gradientCorrection) {
+        dvec4 C1 = d.c1[i], C2 = d.c2[i], C3 = d.c3[i];
+        C[0] = dfD(C1.x); C[1] = dfD(C1.y); C[2] = dfD(C1.z);
+        C[3] = dfD(C2.x); C[4] = dfD(C2.y); C[5] = dfD(C2.z);
+        C[6] = dfD(C3.x); C[7] = dfD(C3.y); C[8] = dfD(C3.z);
+    }
+    df base = (gt == 0) ? -pmin : (gt == 1 ? Pi : Pi - pmin - pmin);
+    df ax = dfF(0.f), ay = ax, az = ax;
+    forMask(d, i, mS, [&](int j, size_t) {
+        PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
+        WeightDF w = weightDF(q.d2, RS, P.weightType);
+        df f;
+        if (gt <= 2) f = (loadDF(d.pressDF, j) + base) * w.wr2;
+        else {
+            double nj = d.pndi[j], Pj = d.press[j], Pid = d.press[i];
+            f = (ni > P.epsilonZero && nj > P.epsilonZero) ? dfD(ni * Pj / nj + nj * Pid / ni) * w.wr2 : w.w;
+        }
+        if (!P.gradientCorrection) { ax += q.v.x * f; ay += q.v.y * f; az += q.v.z * f; }
+        else {
+            ax += (q.v.x * C[0] + q.v.y * C[1] + q.v.z * C[2]) * f;
+            ay += (q.v.x * C[3] + q.v.y * C[4] + q.v.z * C[5]) * f;
+            az += (q.v.x * C[6] + q.v.y * C[7] + q.v.z * C[8]) * f;
+        }
+    });
+    double c = P.relaxPress * P.coeffPressGrad / P.DNS_FL1;
+    d.acc[i] = make_dvec4(dD(ax) * c, dD(ay) * c, dD(az) * c, 0.0);
+}
+void launchPressGradientDF(const Dev& d, cudaStream_t s) {
+    launchPressDF(d, s);
+    k_press_grad_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
+
+// MpsPressure::calcWallPressGradient + repulsive forces, src/MpsPressure.cpp:1341-1611
+__global__ void __launch_bounds__(BLK) k_wall_press_grad_df(Dev d) {
+    int i = nearIndexDF(d);
+    if (i < 0) return;
+    const MpsParams& P = d.P;
+    double vm = fmin(*d.velMax, P.expectMaxVelocity);
+    double vMax2 = vm * vm;
+    dvec4 pi = d.pos[i], mi = d.mirror[i];
+    float4 hi = d.posf[i], li = d.posLo[i];
+    MirrorDF M = mirrorDF(d, mi);
+    df R2 = dfD(P.reS2);
+    RadiusDF RS = radiusDF(P.reS);
+    double Pid = d.press[i], ni = d.pndi[i];
+    df Pi = loadDF(d.pressDF, i), pmin = Pi;
+    int gt = P.gradientType;
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
+    if (gt == 0 || gt == 2) {
+        forNbrs(d, i, [&](int j) {
+            float4 hj = d.posf[j], lj = d.posLo[j];
+            PairF q = pairDF(hj, lj, hi, li);
+            if (!inBallDF(d, q.d2, R2, d.mgS, P.reS2, i, j)) return;
+            df dm2 = norm2(diff3(hj, lj, M.mh, M.ml));
+            bool side = lessDF(q.d2, dm2, d.mgSide, [&] {
+                dvec4 pj = d.pos[j];
+                return pairOf(pj, pi).d2 < pairMirror(pj, mi).dm2;
+            });
+            if (side) { df pj = loadDF(d.pressDF, j); if (pmin > pj) pmin = pj; }
+        });
+    }
+    df base = (gt == 0) ? -pmin : (gt == 1 ? Pi : Pi - pmin - pmin);
+    df sx = dfF(0.f), sy = sx, sz = sx;
+    forNbrs(d, i, [&](int j) {
+        PairF m;
+        if (!wallEntryDF(d, i, j, hi, li, M, R2, d.mgS, P.reS2, m)) return;
+        WeightDF w = weightDF(m.d2, RS, P.weightType);
+        df f;
+        if (gt <= 2) f = (loadDF(d.pressDF, j) + base) * w.wr2;
+        else {
+            double nj = d.pndi[j], Pj = d.press[j];
+            f = (ni > P.epsilonZero && nj > P.epsilonZero) ? dfD(ni * Pj / nj + nj * Pid / ni) * w.wr2 : w.w;
+        }
+        sx += m.v.x * f; sy += m.v.y * f; sz += m.v.z * f;
+    });
+    double ax = dD(sx), ay = dD(sy), az = dD(sz);
+    double pmind = dD(pmin);
+    auto phi = [&](double Pj, double nj, double dm2, double wS) {
+        if (gt == 0) return wS * ((Pj - pmind) / dm2);
+        if (gt == 1) return wS * ((Pj + Pid) / dm2);
+        if (gt == 2) return wS * ((Pj + Pid - 2.0 * pmind) / dm2);
+        if (gt == 3 && ni > P.epsilonZero && nj > P.epsilonZero) return wS * ((ni * Pj / nj + nj * Pid / ni) / dm2);
+        return wS;
+    };
+    PairM s = pairMirror(pi, mi);
+    if (s.dm2 < P.reS2) {
+        double wS = wfun(sqrt(s.dm2), P.reS, P.weightType);
+        wS = phi(Pid, ni, s.dm2, wS);
+        ax += s.m0 * wS; ay += s.m1 * wS; az += s.m2 * wS;
+    }
+    double f[3];
+    wallRepulsion(P, r, vMax2, f);
+    double g0 = P.relaxPress * (r.R[0] * ax + r.R[1] * ay + r.R[2] * az) * P.coeffPressGrad - f[0];
+    double g1 = P.relaxPress * (r.R[3] * ax + r.R[4] * ay + r.R[5] * az) * P.coeffPressGrad - f[1];
+    double g2 = P.relaxPress * (r.R[6] * ax + r.R[7] * ay + r.R[8] * az) * P.coeffPressGrad - f[2];
+    dvec4 a = d.acc[i];
+    a.x += g0 / P.DNS_FL1; a.y += g1 / P.DNS_FL1; a.z += g2 / P.DNS_FL1;
+    d.acc[i] = a;
+    double vf = (P.dim == 3) ? P.partDist * P.partDist * P.partDist : P.partDist * P.partDist;
+    dvec4 fw = d.forceWall[i];
+    fw.x += -g0 * vf; fw.y += -g1 * vf; fw.z += -g2 * vf;
+    d.forceWall[i] = fw;
+}
+void launchWallPressGradientDF(const Dev& d, cudaStream_t s) {
+    if (d.P.wallType != 1) return;
+    launchPressDF(d, s);
+    k_wall_press_grad_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ wall viscosity
+// MpsViscosity::calcWallNoSlipViscosity / calcWallSlipViscosity, src/MpsViscosity.cpp:1527-1910
+__global__ void __launch_bounds__(BLK) k_wall_visc_df(Dev d) {
+    int i = nearIndexDF(d);
+    if (i < 0) return;
+    const MpsParams& P = d.P;
+    bool noslip = P.slipCondition == 0;
+    dvec4 pi = d.pos[i], vi = d.vel[i], mi = d.mirror[i];
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, false);
+    double M[9];
+    if (noslip) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) M[k] = (k % 4 == 0) ? -1.0 : 0.0;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 9; k++) M[k] = r.R[k];
+    }
+    double vm0 = M[0] * vi.x + M[1] * vi.y + M[2] * vi.z;
+    double vm1 = M[3] * vi.x + M[4] * vi.y + M[5] * vi.z;
+    double vm2 = M[6] * vi.x + M[7] * vi.y + M[8] * vi.z;
+    df vmx = dfD(vm0), vmy = dfD(vm1), vmz = dfD(vm2);
+    double mu = P.KNM_VS1 * P.DNS_FL1;
+    double neu = ((mu + mu) > P.epsilonZero ? 2.0 * mu * mu / (mu + mu) : 0.0) / P.DNS_FL1;
+    df neuF = dfD(neu);
+    float4 hi = d.posf[i], li = d.posLo[i];
+    MirrorDF Mi = mirrorDF(d, mi);
+    df R2 = dfD(P.reL2);
+    RadiusDF RL = radiusDF(P.reL);
+    df sx = dfF(0.f), sy = sx, sz = sx;
+    forNbrs(d, i, [&](int j) {
+        PairF m;
+        if (!wallEntryDF(d, i, j, hi, li, Mi, R2, d.mgL, P.reL2, m)) return;
+        df c = weightDF(m.d2, RL, P.weightType).w * neuF;
+        float4 vhj = d.velHi[j], vlj = d.velLo[j];
+        sx += (dfOf(vhj.x, vlj.x) - vmx) * c;
+        sy += (dfOf(vhj.y, vlj.y) - vmy) * c;
+        sz += (dfOf(vhj.z, vlj.z) - vmz) * c;
+    });
+    double ax = dD(sx), ay = dD(sy), az = dD(sz);
+    PairM s = pairMirror(pi, mi);
+    if (s.dm2 < P.reL2) {
+        double wL = wfun(sqrt(s.dm2), P.reL, P.weightType);
+        double neuS = (mu > P.epsilonZero ? 2.0 * mu * mu / (mu + mu) : 0.0) / P.DNS_FL1;
+        ax += (vi.x - vm0) * wL * neuS;
+        ay += (vi.y - vm1) * wL * neuS;
+        az += (vi.z - vm2) * wL * neuS;
+    }
+    double f0 = (M[0] * ax + M[1] * ay + M[2] * az) * P.coeffViscMultiphase;
+    double f1 = (M[3] * ax + M[4] * ay + M[5] * az) * P.coeffViscMultiphase;
+    double f2 = (M[6] * ax + M[7] * ay + M[8] * az) * P.coeffViscMultiphase;
+    dvec4 a = d.acc[i];
+    a.x += f0; a.y += f1; a.z += f2;
+    d.acc[i] = a;
+    double vf = (P.dim == 3) ? P.partDist * P.partDist * P.partDist : P.partDist * P.partDist;
+    dvec4 fw = d.forceWall[i];
+    fw.x += -f0 * vf * P.DNS_FL1; fw.y += -f1 * vf * P.DNS_FL1; fw.z += -f2 * vf * P.DNS_FL1;
+    d.forceWall[i] = fw;
+}
+void launchWallViscosityDF(const Dev& d, cudaStream_t s) {
+    if (d.P.wallType != 1) return;
+    launchVelDF(d, s);
+    k_wall_visc_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}

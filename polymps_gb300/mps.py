@@ -17,7 +17,7 @@ _lib = None
 
 EXPORTS = [
     "mpsgpu_params_derive", "mpsgpu_create", "mpsgpu_destroy", "mpsgpu_initialize", "mpsgpu_step",
-    "mpsgpu_run", "mpsgpu_run_op", "mpsgpu_set_solver", "mpsgpu_get_field", "mpsgpu_set_field",
+    "mpsgpu_run", "mpsgpu_run_op", "mpsgpu_set_solver", "mpsgpu_set_precision", "mpsgpu_get_field", "mpsgpu_set_field",
     "mpsgpu_num_particles", "mpsgpu_time", "mpsgpu_get_neighbors", "mpsgpu_get_ppe",
     "mpsgpu_mlp_set_weights", "mpsgpu_mlp_get_weights", "mpsgpu_ppe_features", "mpsgpu_mlp_record",
     "mpsgpu_mlp_num_records", "mpsgpu_mlp_fit_normalization", "mpsgpu_mlp_train", "mpsgpu_mlp_forward",
@@ -53,6 +53,7 @@ def lib(path=None):
     L.mpsgpu_run.argtypes = [vp, C.c_int, P(abi.MpsStepStats)]
     L.mpsgpu_run_op.argtypes = [vp, C.c_int]
     L.mpsgpu_set_solver.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int]
+    L.mpsgpu_set_precision.argtypes = [vp, C.c_int]
     L.mpsgpu_get_field.argtypes = [vp, C.c_int, vp]
     L.mpsgpu_set_field.argtypes = [vp, C.c_int, vp]
     L.mpsgpu_num_particles.argtypes = [vp, P(C.c_int)]
@@ -101,7 +102,8 @@ def derive(params, n, pos):
 class MpsGpu:
     """One particle system on the GPU (one handle, one CUDA stream)."""
 
-    def __init__(self, case, solver=abi.SOLVER_PLAIN_FP64, warm=abi.WARM_PREVIOUS, tol=1e-8, max_iter=0):
+    def __init__(self, case, solver=abi.SOLVER_PLAIN_FP64, warm=abi.WARM_PREVIOUS, tol=1e-8, max_iter=0,
+                 precision=abi.PRECISION_FP64):
         L = lib()
         self.case = case
         self.params = derive(case.mps_params(), case.n, case.pos)
@@ -112,6 +114,7 @@ class MpsGpu:
             abi.dptr(case.press), C.byref(self._mesh) if self._mesh is not None else None, C.byref(h)))
         self.h = h
         self.set_solver(solver, warm, tol, max_iter)
+        self.set_precision(precision)
 
     # ------------------------------------------------------------- lifecycle
     def close(self):
@@ -154,6 +157,10 @@ class MpsGpu:
         st = abi.MpsStepStats()
         _check("mpsgpu_last_stats", lib().mpsgpu_last_stats(self.h, C.byref(st)), self.h)
         return st
+
+    def set_precision(self, precision=abi.PRECISION_FP64):
+        """FP64 (reference arithmetic) or DF32 (float-float pair arithmetic, same decisions)."""
+        _check("mpsgpu_set_precision", lib().mpsgpu_set_precision(self.h, precision), self.h)
 
     def set_solver(self, solver=abi.SOLVER_PLAIN_FP64, warm=abi.WARM_PREVIOUS, tol=1e-8, max_iter=0):
         _check("mpsgpu_set_solver", lib().mpsgpu_set_solver(self.h, solver, warm, tol, max_iter), self.h)

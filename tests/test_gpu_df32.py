@@ -1,0 +1,141 @@
+"""DF32 tier (float-float neighbour arithmetic) against the FP64 CPU oracle.
+
+Stated tolerances of the tier:
+* neighbour sets, entry masks, integer fields: bit-exact (every radius / mirror-side /
+  collision decision near its threshold is taken in FP64, as the reference takes it);
+* free-surface flags: equal except particles within 1e-6 relative of a threshold;
+* FP64 fields after one operator from an identical state (teacher forcing):
+  normwise relative error <= 1e-8 (float-float pair arithmetic is ~1e-11 relative;
+  pressure-dependent fields amplify it through the solver);
+* pressure of the PPE (solved to 1e-12): within 1e-6 relative of the oracle's.
+"""
+import numpy as np
+import pytest
+
+from polymps_gb300 import abi, cases
+
+from test_gpu_parity import CASES, INT, SCA, VEC, relerr, step_ops, sync
+
+pytestmark = pytest.mark.gpu
+
+DF_RTOL = 1e-8
+
+
+def _pair(oracle_mod, mps, case, tol=1e-12):
+    o = oracle_mod.Oracle(case)
+    g = mps.MpsGpu(case, tol=tol, precision=abi.PRECISION_DF32)
+    o.set_solver(tol)
+    return o, g
+
+
+def compare(o, g, where, fields=None, rtol=DF_RTOL):
+    fields = fields or (VEC + SCA + INT)
+    p = o.params
+    for f in fields:
+        a, b = g.get(f), o.get(f)
+        name = abi.FIELD_NAMES[f]
+        if f in abi.INT_FIELDS:
+            bad = np.nonzero(a != b)[0]
+            if f == abi.F_BC and len(bad):
+                ps = o.get(abi.F_PNDSMALL)[bad]
+                d2 = o.get(abi.F_NPCD2)[bad]
+                amb = (np.abs(ps - p.betaPnd) <= 1e-6 * p.betaPnd) | (np.abs(d2 - p.delta2) <= 1e-6 * p.delta2)
+                bad = bad[~amb]
+            assert len(bad) == 0, "%s: %s differs at %s (gpu %s, oracle %s)" % (where, name, bad[:10], a[bad[:5]], b[bad[:5]])
+        else:
+            e = relerr(a, b)
+            assert e <= rtol, "%s: %s rel err %.3e" % (where, name, e)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_df32_neighbor_sets_bit_exact(oracle_mod, mps_lib, name):
+    from polymps_gb300 import mps
+    o, g = _pair(oracle_mod, mps, CASES[name]())
+    o.initialize()
+    for _ in range(3):
+        o.step()
+    sync(o, g)
+    for ob in (o, g):
+        ob.run_op("UPDATE_BUCKETS")
+        ob.run_op("VISCOSITY"); ob.run_op("ADD_GRAVITY"); ob.run_op("PREDICT")
+    g.set(abi.F_POS, o.get(abi.F_POS))
+    co, no = o.neighbors()
+    cg, ng = g.neighbors()
+    assert np.array_equal(co, cg)
+    assert np.array_equal(no, ng)
+
+
+def test_df32_neighbor_sets_adversarial(oracle_mod, mps_lib):
+    """Pairs at r^2 = reL^2 and within a few ulps of it: decided by the FP64 fallback."""
+    from polymps_gb300 import mps
+    c = cases.config(3, scale=5.0)
+    p = oracle_mod.Oracle(c).params
+    rng = np.random.default_rng(11)
+    pos = c.pos.copy()
+    n = len(pos)
+    for k in range(0, n - 1, 5):
+        d = rng.normal(size=3); d /= np.linalg.norm(d)
+        r = p.reL * [1.0, 1.0 + 2e-16, 1.0 - 2e-16, 1.0 + 1e-13, 1.0 - 1e-13][k % 5]
+        pos[k + 1] = pos[k] + r * d
+    c2 = cases.Case(c.name, c.params, c.type, pos, c.mesh)
+    o, g = _pair(oracle_mod, mps, c2)
+    for ob in (o, g):
+        ob.run_op("UPDATE_BUCKETS")
+    co, no = o.neighbors()
+    cg, ng = g.neighbors()
+    assert np.array_equal(co, cg)
+    assert np.array_equal(no, ng)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_df32_operator_parity_teacher_forced(oracle_mod, mps_lib, name):
+    from polymps_gb300 import mps
+    o, g = _pair(oracle_mod, mps, CASES[name]())
+    o.initialize()
+    g.initialize()
+    for _ in range(4):
+        o.step()
+    o.set_velmax(0.0)
+    for s in range(3):
+        sync(o, g)
+        for op in step_ops(o.params):
+            o.run_op(op)
+            g.run_op(op)
+            compare(o, g, "step %d op %s" % (s, op))
+            sync(o, g)
+
+
+@pytest.mark.parametrize("name", ["cfg3_3d_inc_polygon", "cfg1_2d_particle_walls"])
+def test_df32_ppe_pressure(oracle_mod, mps_lib, name):
+    """The pressure the DF32 tier's PPE yields stays within 1e-6 of the FP64 oracle."""
+    from polymps_gb300 import mps
+    o, g = _pair(oracle_mod, mps, CASES[name]())
+    o.initialize()
+    for _ in range(5):
+        o.step()
+    sync(o, g)
+    for op in step_ops(o.params)[: step_ops(o.params).index("CALC_PRESS")]:
+        o.run_op(op); g.run_op(op); sync(o, g)
+    o.run_op("CALC_PRESS")
+    g.run_op("CALC_PRESS")
+    ro, co, vo, bo = o.ppe()
+    rg, cg, vg, bg = g.ppe()
+    assert np.array_equal(ro, rg) and np.array_equal(co, cg)
+    assert relerr(vg, vo) < 1e-10
+    assert relerr(bg, bo) < 1e-7
+    assert relerr(g.get(abi.F_PRESS), o.get(abi.F_PRESS)) < 1e-6
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_df32_free_running_steps(oracle_mod, mps_lib, name):
+    from polymps_gb300 import mps
+    o, g = _pair(oracle_mod, mps, CASES[name]())
+    o.initialize()
+    g.initialize()
+    for _ in range(10):
+        so = o.step()
+        sg = g.step()
+        assert sg.numParticles == so.numParticles
+    assert relerr(g.get(abi.F_POS), o.get(abi.F_POS)) < 1e-9
+    assert relerr(g.get(abi.F_VEL), o.get(abi.F_VEL)) < 1e-5
+    assert relerr(g.get(abi.F_PRESS), o.get(abi.F_PRESS)) < 1e-5

@@ -453,6 +453,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.velHi, n);
     A(d.velLo, n);
     A(d.pressDF, n);
+    A(d.corrDF, (size_t)9 * n);
     A(d.nbrCount, n);
     A(d.nbr, (size_t)d.K * n);
     A(d.cw, (size_t)d.K * n);
@@ -500,6 +501,23 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         d.mgColl = margin(std::max(p->distCollisionLimit2, 1e-300));
         d.mgSide = margin(3.3 * 3.3 * d.reMax2);
         d.prec = MPSGPU_PRECISION_FP64;
+        // float-float constants: hi = fl32(x), lo = fl32(x - hi) (as the device converts)
+        auto hd = [](double x) { float h = (float)x; return make_float2(h, (float)(x - (double)h)); };
+        Dev::DfK& k = d.k;
+        k.reS = hd(p->reS); k.reL = hd(p->reL);
+        k.invReS = hd(1.0 / p->reS); k.invReL = hd(1.0 / p->reL);
+        k.reS2 = hd(p->reS2); k.reL2 = hd(p->reL2); k.reMax2 = hd(d.reMax2);
+        k.coll2 = hd(p->distCollisionLimit2);
+        double mu = p->KNM_VS1 * p->DNS_FL1, rho = p->DNS_FL1;
+        k.neuW = hd((2.0 * mu) / rho);
+        k.neuF = hd((2.0 * mu * mu / (mu + mu)) / rho);
+        k.neuWall = hd(((mu + mu) > p->epsilonZero ? 2.0 * mu * mu / (mu + mu) : 0.0) / p->DNS_FL1);
+        k.cPPE = hd(p->coeffPPE);
+        k.cPPEg = hd(p->coeffPPE * p->DNS_FL1);
+        for (int c = 0; c < 3; c++) k.g[c] = hd(p->gravity[c]);
+        k.collF = hd(p->restitutionCollision * p->DNS_FL1 / (p->DNS_FL1 + p->DNS_FL1));
+        k.collW = hd(p->restitutionCollision * p->densityWall / (p->DNS_FL1 + p->densityWall));
+        k.negCPG = hd(-p->coeffPressGrad);
     }
     if (d.K > 64) { g_lastError = "neighbour row capacity above the 64-bit entry masks"; mpsgpu_destroy(h); return MPSGPU_ERR_UNSUPPORTED; }
     // mesh and wall tables
@@ -765,6 +783,7 @@ int mpsgpu_set_field(mpsgpu_t h, int f, const void* host) {
     h->masksValid = false;
     h->cacheValid = false;
     if (f == MPS_F_POS) launchPosf(h->d, h->s);
+    if (f == MPS_F_CORR1 || f == MPS_F_CORR2 || f == MPS_F_CORR3) launchCorrDF(h->d, h->s);
     CK(cudaStreamSynchronize(h->s));
     return 0;
 }

@@ -58,6 +58,17 @@ struct Dev {
     float4 *posLo, *posLoCell, *velHi, *velLo;
     float2* pressDF;
     float mgS, mgL, mgMax, mgColl, mgSide;
+    // float-float (hi, lo) constants of the DF32 sweeps, converted once on the host
+    struct DfK {
+        float2 reS, reL, invReS, invReL, reS2, reL2, reMax2, coll2;
+        float2 neuW, neuF;          // viscosity: 2 mu / rho (wall neighbour), harmonic mean / rho
+        float2 neuWall;             // wall viscosity coefficient
+        float2 cPPE, cPPEg;         // coeffPPE, coeffPPE * DNS_FL1
+        float2 g[3];
+        float2 collF, collW;        // restitution * m_j / (m_i + m_j), fluid / wall neighbour
+        float2 negCPG;              // -coeffPressGrad
+    } k;
+    float2* corrDF;                 // DF32 correction matrices: 9 values per particle, [c * N0 + i]
     // neighbour list (ELL) and its per-entry cache for the epoch: w(r; reS), w/r^2,
     // w(r; reL) (only when reL != reS)
     int *nbrCount, *nbr;
@@ -221,8 +232,11 @@ __device__ __forceinline__ void forCells(const Dev& d, dvec4 x, F&& f) {
     bucketCoords(P, x.x, x.y, x.z, ix, iy, iz);
     int dz = (int)(P.dim - 2.0);
     int minZ = (iz - 1) * dz, maxZ = (iz + 1) * dz;
+#pragma unroll 1
     for (int jz = minZ; jz <= maxZ; jz++)
+#pragma unroll 1
         for (int jy = iy - 1; jy <= iy + 1; jy++)
+#pragma unroll 1
             for (int jx = ix - 1; jx <= ix + 1; jx++) {
                 long long jb = (long long)jz * P.numBucketsXY + (long long)jy * P.numBucketsX + jx;
                 if (jb < 0 || jb >= d.nB) continue;
@@ -241,8 +255,11 @@ __device__ __forceinline__ void forCellsNear(const Dev& d, dvec4 pi, float4 fi, 
     bucketCoords(P, pi.x, pi.y, pi.z, ix, iy, iz);
     int dz = (int)(P.dim - 2.0);
     int minZ = (iz - 1) * dz, maxZ = (iz + 1) * dz;
+#pragma unroll 1
     for (int jz = minZ; jz <= maxZ; jz++)
+#pragma unroll 1
         for (int jy = iy - 1; jy <= iy + 1; jy++)
+#pragma unroll 1
             for (int jx = ix - 1; jx <= ix + 1; jx++) {
                 long long jb = (long long)jz * P.numBucketsXY + (long long)jy * P.numBucketsX + jx;
                 if (jb < 0 || jb >= d.nB) continue;

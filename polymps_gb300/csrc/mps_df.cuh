@@ -196,8 +196,11 @@ __device__ __forceinline__ void forCellsDF(const Dev& d, dvec4 pi, float4 fi, fl
     bucketCoords(P, pi.x, pi.y, pi.z, ix, iy, iz);
     int dz = (int)(P.dim - 2.0);
     int minZ = (iz - 1) * dz, maxZ = (iz + 1) * dz;
+#pragma unroll 1
     for (int jz = minZ; jz <= maxZ; jz++)
+#pragma unroll 1
         for (int jy = iy - 1; jy <= iy + 1; jy++)
+#pragma unroll 1
             for (int jx = ix - 1; jx <= ix + 1; jx++) {
                 long long jb = (long long)jz * P.numBucketsXY + (long long)jy * P.numBucketsX + jx;
                 if (jb < 0 || jb >= d.nB) continue;
@@ -211,5 +214,4 @@ __device__ __forceinline__ void forCellsDF(const Dev& d, dvec4 pi, float4 fi, fl
             }
 }
 
-__device__ __forceinline__ RadiusDF radiusDF(double re) { return {dfD(re), dfD(1.0 / re)}; }
 __device__ __forceinline__ df dfOf(float h, float l) { return quick2(h, l); }

@@ -69,6 +69,7 @@ void launchViscosityDF(const Dev& d, cudaStream_t s);
 void launchCollisionDF(const Dev& d, cudaStream_t s);
 void launchWallNpcdDF(const Dev& d, cudaStream_t s);
 void launchCorrectionMatrixDF(const Dev& d, cudaStream_t s);
+void launchCorrDF(const Dev& d, cudaStream_t s);
 void launchPndNeighNpcdDF(const Dev& d, cudaStream_t s);
 void launchPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallPressGradientDF(const Dev& d, cudaStream_t s);

@@ -31,6 +31,7 @@ __global__ void k_df_press(Dev d) {
 static void launchVelDF(const Dev& d, cudaStream_t s) { k_df_vel<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
 static void launchPressDF(const Dev& d, cudaStream_t s) { k_df_press<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
 
+__device__ __forceinline__ df K(float2 v) { return {v.x, v.y}; }
 __device__ __forceinline__ df loadDF(const float2* p, int j) {
     float2 v = __ldg(p + j);
     return {v.x, v.y};
@@ -46,7 +47,7 @@ __global__ void __launch_bounds__(128) k_build_nbr_df(Dev d) {
     if (i >= liveN(d)) return;
     dvec4 pi = d.pos[i];
     float4 hi = d.posf[i], li = d.posLo[i];
-    df R2 = dfD(d.reMax2);
+    const df R2 = K(d.k.reMax2);
     int cnt = 0;
     const size_t N0 = d.N0;
     forCellsDF(d, pi, hi, d.bandHi, [&](int j, int s, float4 hj) {
@@ -83,7 +84,7 @@ __global__ void __launch_bounds__(128) k_side_masks_df(Dev d) {
     if (sc.check || !fullS || !fullL) {
         mS = 0; mL = 0;
         float4 hi = d.posf[i], li = d.posLo[i];
-        df RS = dfD(P.reS2), RL = dfD(P.reL2);
+        const df RS = K(d.k.reS2), RL = K(d.k.reL2);
         const int* row = d.nbr + i;
         for (int k = 0; k < c; k++) {
             int j = __ldg(row + (size_t)k * d.N0);
@@ -108,39 +109,73 @@ void launchSideMasksDF(const Dev& d, cudaStream_t s) {
 
 // ------------------------------------------------------------------ viscosity
 // MpsViscosity::calcViscosity, src/MpsViscosity.cpp:20-100, at the start-of-step
-// positions through the 27 buckets (Newtonian: uniform MEU and RHO).
-__global__ void __launch_bounds__(128) k_visc_df(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+// positions through the 27 buckets (Newtonian: uniform MEU and RHO).  Two phases per
+// batch: the FP32 prefilter compacts the surviving slots of the thread's candidates into
+// its shared-memory column (bucket order kept), then the float-float pair work runs over
+// the compacted slots, so the lanes of a warp stay converged through the expensive part.
+#define VCAP 48
+#define VBLK 128
+__global__ void __launch_bounds__(VBLK) k_visc_df(Dev d) {
+    __shared__ int slots[VCAP * VBLK];
+    const int t = threadIdx.x;
+    const int i = blockIdx.x * VBLK + t;
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
-    dvec4 pi = d.pos[i];
-    float4 hi = d.posf[i], li = d.posLo[i];
-    float4 vh = d.velHi[i], vl = d.velLo[i];
-    SideDF sc = sideDF(d, i, pi);
-    df R2 = dfD(P.reL2);
-    RadiusDF RL = radiusDF(P.reL);
-    double mu = P.KNM_VS1 * P.DNS_FL1, rho = P.DNS_FL1;
-    df neuW = dfD((2.0 * mu) / rho), neuF = dfD((2.0 * mu * mu / (mu + mu)) / rho);
+    const dvec4 pi = d.pos[i];
+    const float4 hi = d.posf[i], li = d.posLo[i];
+    const float4 vh = d.velHi[i], vl = d.velLo[i];
+    const SideDF sc = sideDF(d, i, pi);
+    const df R2 = K(d.k.reL2), neuW = K(d.k.neuW), neuF = K(d.k.neuF);
+    const RadiusDF RL = {K(d.k.reL), K(d.k.invReL)};
+    const float band = d.bandHiL;
     df ax = dfF(0.f), ay = dfF(0.f), az = dfF(0.f);
-    forCellsDF(d, pi, hi, d.bandHiL, [&](int j, int s, float4 hj) {
-        if (j == i) return;
-        float4 lj = __ldg(&d.posLoCell[s]);
-        PairF q = pairDF(hj, lj, hi, li);
-        if (!inBallDF(d, q.d2, R2, d.mgL, P.reL2, i, j)) return;
-        if (!sideOkDF(d, sc, hj, lj, q.d2, i, j)) return;
-        WeightDF w = weightDF(q.d2, RL, P.weightType);
-        df c = w.w * ((d.type[j] == P.wall) ? neuW : neuF);
-        float4 vhj = d.velHi[j], vlj = d.velLo[j];
-        ax += diffDF(vhj.x, vlj.x, vh.x, vl.x) * c;
-        ay += diffDF(vhj.y, vlj.y, vh.y, vl.y) * c;
-        az += diffDF(vhj.z, vlj.z, vh.z, vl.z) * c;
-    });
+    int ix, iy, iz;
+    bucketCoords(P, pi.x, pi.y, pi.z, ix, iy, iz);
+    const int dz = (int)(P.dim - 2.0);
+    const int nbk = dz ? 27 : 9;
+    int bk = 0, s = 0, s1 = 0;
+    bool more = true;
+    while (more) {
+        int n = 0;
+        while (n < VCAP) {
+            if (s >= s1) {
+                if (bk >= nbk) { more = false; break; }
+                int kz = bk / 9, ky = (bk / 3) % 3, kx = bk % 3;
+                bk++;
+                long long jb = (long long)((iz - 1) * dz + kz) * P.numBucketsXY +
+                               (long long)(iy - 1 + ky) * P.numBucketsX + (ix - 1 + kx);
+                if (jb < 0 || jb >= d.nB) continue;
+                s = d.cellStart[jb];
+                s1 = d.cellStart[jb + 1];
+                continue;
+            }
+            float4 fj = __ldg(&d.posfCell[s]);
+            float ex = fj.x - hi.x, ey = fj.y - hi.y, ez = fj.z - hi.z;
+            if (ex * ex + ey * ey + ez * ez <= band) slots[n++ * VBLK + t] = s;
+            s++;
+        }
+        for (int k = 0; k < n; k++) {
+            const int sk = slots[k * VBLK + t];
+            const int j = __ldg(d.cellSorted + sk);
+            if (j == i) continue;
+            const float4 hj = __ldg(&d.posfCell[sk]), lj = __ldg(&d.posLoCell[sk]);
+            PairF q = pairDF(hj, lj, hi, li);
+            if (!inBallDF(d, q.d2, R2, d.mgL, P.reL2, i, j)) continue;
+            if (!sideOkDF(d, sc, hj, lj, q.d2, i, j)) continue;
+            WeightDF w = weightDF(q.d2, RL, P.weightType);
+            df c = w.w * ((d.type[j] == P.wall) ? neuW : neuF);
+            float4 vhj = d.velHi[j], vlj = d.velLo[j];
+            ax += diffDF(vhj.x, vlj.x, vh.x, vl.x) * c;
+            ay += diffDF(vhj.y, vlj.y, vh.y, vl.y) * c;
+            az += diffDF(vhj.z, vlj.z, vh.z, vl.z) * c;
+        }
+    }
     double cv = P.coeffViscMultiphase;
     d.acc[i] = make_dvec4(cv * dD(ax), cv * dD(ay), cv * dD(az), 0.0);
 }
 void launchViscosityDF(const Dev& d, cudaStream_t s) {
     launchVelDF(d, s);
-    k_visc_df<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+    k_visc_df<<<gridFor(d.N0, VBLK), VBLK, 0, s>>>(d);
 }
 
 // ------------------------------------------------------------------ collision
@@ -154,15 +189,12 @@ __global__ void __launch_bounds__(BLK) k_collision_df(Dev d) {
     df dvx = dfF(0.f), dvy = dfF(0.f), dvz = dfF(0.f);
     bool any = false;
     if (d.type[i] == P.fluid) {
-        double mi = P.DNS_FL1;
         dvec4 pi = d.pos[i];
         float4 hi = d.posf[i], li = d.posLo[i];
         float4 vh = d.velHi[i], vl = d.velLo[i];
         float vin = fabsf(vh.x) + fabsf(vh.y) + fabsf(vh.z);
         SideDF sc = sideDF(d, i, pi);
-        df R2 = dfD(P.distCollisionLimit2);
-        df cF = dfD(P.restitutionCollision * P.DNS_FL1 / (mi + P.DNS_FL1));
-        df cW = dfD(P.restitutionCollision * P.densityWall / (mi + P.densityWall));
+        const df R2 = K(d.k.coll2), cF = K(d.k.collF), cW = K(d.k.collW);
         forNbrs(d, i, [&](int j) {
             float4 hj = d.posf[j], lj = d.posLo[j];
             PairF q = pairDF(hj, lj, hi, li);
@@ -241,8 +273,8 @@ __global__ void __launch_bounds__(BLK) k_wall_npcd_df(Dev d) {
     ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
     float4 hi = d.posf[i], li = d.posLo[i];
     MirrorDF M = mirrorDF(d, mi);
-    df R2 = dfD(P.reS2);
-    RadiusDF RS = radiusDF(P.reS);
+    const df R2 = K(d.k.reS2);
+    const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
     df sx = dfF(0.f), sy = dfF(0.f), sz = dfF(0.f);
     forNbrs(d, i, [&](int j) {
         PairF m;
@@ -268,12 +300,23 @@ void launchWallNpcdDF(const Dev& d, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------ correction matrix
+// MpsVectorMatrix::correctionMatrix + inverseMatrix, src/MpsVectorMatrix.cpp:20-166: the
+// moment matrix sum w/r^2 r r^T is accumulated in float-float and inverted through its
+// adjugate in float-float (the reference eliminates without pivoting; both give the
+// inverse to rounding), identity when det <= eps or numNeigh < 4.  The FP64 copy is the
+// operator's output; the float-float copy feeds the DF32 pressure gradient.
+__device__ __forceinline__ df recipDF(df a) {
+    float y = 1.0f / a.h;
+    df t = a * y;                              // ~1
+    float e = fS(fS(1.0f, t.h), t.l);          // 1 - a y
+    return quick2(y, fM(y, e));
+}
 __global__ void __launch_bounds__(BLK) k_corr_matrix_df(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     float4 hi = d.posf[i], li = d.posLo[i];
-    RadiusDF RS = radiusDF(P.reS);
+    const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
     df m00 = dfF(0.f), m01 = m00, m02 = m00, m11 = m00, m12 = m00, m22 = m00;
     forMask(d, i, d.maskS[i], [&](int j, size_t) {
         PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
@@ -282,20 +325,47 @@ __global__ void __launch_bounds__(BLK) k_corr_matrix_df(Dev d) {
         m00 += t0 * q.v.x; m01 += t0 * q.v.y; m02 += t0 * q.v.z;
         m11 += t1 * q.v.y; m12 += t1 * q.v.z; m22 += t2 * q.v.z;
     });
-    double c = -P.coeffPressGrad;
-    double m[9];
-    m[0] = dD(m00) * c; m[1] = dD(m01) * c; m[2] = dD(m02) * c;
-    m[4] = dD(m11) * c; m[5] = dD(m12) * c; m[8] = dD(m22) * c;
-    m[3] = m[1]; m[6] = m[2]; m[7] = m[5];
-    invert3(m, (int)P.dim, P.epsilonZero);
-    if (d.numNeigh[i] < 4) {
+    const df c = K(d.k.negCPG);
+    df A[9];
+    A[0] = m00 * c; A[1] = m01 * c; A[2] = m02 * c;
+    A[4] = m11 * c; A[5] = m12 * c; A[8] = m22 * c;
+    A[3] = A[1]; A[6] = A[2]; A[7] = A[5];
+    if (P.dim == 2) { A[2] = A[5] = A[6] = A[7] = dfF(0.f); A[8] = dfF(1.f); }
+    df det = (A[0] * A[4] * A[8] + A[1] * A[5] * A[6] + A[2] * A[3] * A[7]) -
+             (A[2] * A[4] * A[6] + A[1] * A[3] * A[8] + A[0] * A[5] * A[7]);
+    df M[9];
+    bool ident = d.numNeigh[i] < 4 || !(det.h > (float)P.epsilonZero);
+    if (ident) {
 #pragma unroll
-        for (int k = 0; k < 9; k++) m[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        for (int k = 0; k < 9; k++) M[k] = dfF((k % 4 == 0) ? 1.f : 0.f);
+    } else {
+        df r = recipDF(det);
+        M[0] = (A[4] * A[8] - A[5] * A[7]) * r; M[1] = (A[2] * A[7] - A[1] * A[8]) * r;
+        M[2] = (A[1] * A[5] - A[2] * A[4]) * r; M[3] = (A[5] * A[6] - A[3] * A[8]) * r;
+        M[4] = (A[0] * A[8] - A[2] * A[6]) * r; M[5] = (A[2] * A[3] - A[0] * A[5]) * r;
+        M[6] = (A[3] * A[7] - A[4] * A[6]) * r; M[7] = (A[1] * A[6] - A[0] * A[7]) * r;
+        M[8] = (A[0] * A[4] - A[1] * A[3]) * r;
     }
-    d.c1[i] = make_dvec4(m[0], m[1], m[2], 0.0);
-    d.c2[i] = make_dvec4(m[3], m[4], m[5], 0.0);
-    d.c3[i] = make_dvec4(m[6], m[7], m[8], 0.0);
+#pragma unroll
+    for (int k = 0; k < 9; k++) d.corrDF[(size_t)k * d.N0 + i] = make_float2(M[k].h, M[k].l);
+    d.c1[i] = make_dvec4(dD(M[0]), dD(M[1]), dD(M[2]), 0.0);
+    d.c2[i] = make_dvec4(dD(M[3]), dD(M[4]), dD(M[5]), 0.0);
+    d.c3[i] = make_dvec4(dD(M[6]), dD(M[7]), dD(M[8]), 0.0);
 }
+// float-float copy of matrices written through the field interface
+__global__ void k_df_corr(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N0) return;
+    dvec4 r[3] = {d.c1[i], d.c2[i], d.c3[i]};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        df x = dfD(r[a].x), y = dfD(r[a].y), z = dfD(r[a].z);
+        d.corrDF[(size_t)(3 * a) * d.N0 + i] = make_float2(x.h, x.l);
+        d.corrDF[(size_t)(3 * a + 1) * d.N0 + i] = make_float2(y.h, y.l);
+        d.corrDF[(size_t)(3 * a + 2) * d.N0 + i] = make_float2(z.h, z.l);
+    }
+}
+void launchCorrDF(const Dev& d, cudaStream_t s) { k_df_corr<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
 void launchCorrectionMatrixDF(const Dev& d, cudaStream_t s) { k_corr_matrix_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
 
 // ------------------------------------------------------------------ PND / NPCD
@@ -305,7 +375,7 @@ __global__ void __launch_bounds__(BLK) k_pnd_npcd_df(Dev d) {
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     float4 hi = d.posf[i], li = d.posLo[i];
-    RadiusDF RS = radiusDF(P.reS);
+    const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
     unsigned long long mL = d.maskL[i];
     int nn = d.nNeighWall[i] + __popcll(mL);
     df ni = dfF(0.f), nx = ni, ny = ni, nz = ni;
@@ -347,10 +417,9 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
         return;
     }
     float4 hi = d.posf[i], li = d.posLo[i];
-    RadiusDF RL = radiusDF(P.reL);
-    df cP = dfD(P.coeffPPE);
-    df cG = dfD(P.coeffPPE * P.DNS_FL1);
-    df gx = dfD(P.gravity[0]), gy = dfD(P.gravity[1]), gz = dfD(P.gravity[2]);
+    const RadiusDF RL = {K(d.k.reL), K(d.k.invReL)};
+    const df cP = K(d.k.cPPE), cG = K(d.k.cPPEg);
+    const df gx = K(d.k.g[0]), gy = K(d.k.g[1]), gz = K(d.k.g[2]);
     df sum = dfF(0.f), src = dfF(0.f);
     int len = 0;
     forMask(d, i, d.maskL[i], [&](int j, size_t) {
@@ -387,7 +456,7 @@ __global__ void __launch_bounds__(BLK) k_press_grad_df(Dev d) {
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     float4 hi = d.posf[i], li = d.posLo[i];
-    RadiusDF RS = radiusDF(P.reS);
+    const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
     df Pi = loadDF(d.pressDF, i), pmin = Pi;
     double ni = d.pndi[i];
     int gt = P.gradientType;
@@ -400,10 +469,8 @@ __global__ void __launch_bounds__(BLK) k_press_grad_df(Dev d) {
     }
     df C[9];
     if (P.gradientCorrection) {
-        dvec4 C1 = d.c1[i], C2 = d.c2[i], C3 = d.c3[i];
-        C[0] = dfD(C1.x); C[1] = dfD(C1.y); C[2] = dfD(C1.z);
-        C[3] = dfD(C2.x); C[4] = dfD(C2.y); C[5] = dfD(C2.z);
-        C[6] = dfD(C3.x); C[7] = dfD(C3.y); C[8] = dfD(C3.z);
+#pragma unroll
+        for (int k = 0; k < 9; k++) C[k] = loadDF(d.corrDF + (size_t)k * d.N0, i);
     }
     df base = (gt == 0) ? -pmin : (gt == 1 ? Pi : Pi - pmin - pmin);
     df ax = dfF(0.f), ay = ax, az = ax;
@@ -441,8 +508,8 @@ __global__ void __launch_bounds__(BLK) k_wall_press_grad_df(Dev d) {
     dvec4 pi = d.pos[i], mi = d.mirror[i];
     float4 hi = d.posf[i], li = d.posLo[i];
     MirrorDF M = mirrorDF(d, mi);
-    df R2 = dfD(P.reS2);
-    RadiusDF RS = radiusDF(P.reS);
+    const df R2 = K(d.k.reS2);
+    const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
     double Pid = d.press[i], ni = d.pndi[i];
     df Pi = loadDF(d.pressDF, i), pmin = Pi;
     int gt = P.gradientType;
@@ -530,12 +597,11 @@ __global__ void __launch_bounds__(BLK) k_wall_visc_df(Dev d) {
     double vm2 = M[6] * vi.x + M[7] * vi.y + M[8] * vi.z;
     df vmx = dfD(vm0), vmy = dfD(vm1), vmz = dfD(vm2);
     double mu = P.KNM_VS1 * P.DNS_FL1;
-    double neu = ((mu + mu) > P.epsilonZero ? 2.0 * mu * mu / (mu + mu) : 0.0) / P.DNS_FL1;
-    df neuF = dfD(neu);
+    const df neuF = K(d.k.neuWall);
     float4 hi = d.posf[i], li = d.posLo[i];
     MirrorDF Mi = mirrorDF(d, mi);
-    df R2 = dfD(P.reL2);
-    RadiusDF RL = radiusDF(P.reL);
+    const df R2 = K(d.k.reL2);
+    const RadiusDF RL = {K(d.k.reL), K(d.k.invReL)};
     df sx = dfF(0.f), sy = sx, sz = sx;
     forNbrs(d, i, [&](int j) {
         PairF m;

@@ -262,12 +262,16 @@ def ppe_compare(g, abi, use_mlp):
         g.run_op(op)
     x_prev = g.get(abi.F_PRESSPPE)
     res = {}
-    variants = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS),
-                ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS)]
+    # single-launch solves, then the per-kernel launch path for reference
+    variants = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, True),
+                ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, True)]
     if use_mlp:
-        variants.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP))
-    for name, s, w in variants:
+        variants.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP, True))
+    variants += [("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, False),
+                 ("fp32_fp64_per_kernel_launch", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, False)]
+    for name, s, w, single in variants:
         best = None
+        g.set_ppe_launch(single)
         for rep in range(3):
             g.set(abi.F_PRESSPPE, x_prev)
             g.set_solver(s, w, 1e-8, 20000)
@@ -282,6 +286,7 @@ def ppe_compare(g, abi, use_mlp):
         else:
             p = g.get(abi.F_PRESSPPE)
             res[name]["rel_err_vs_fp64"] = float(np.linalg.norm(p - p_ref) / np.linalg.norm(p_ref))
+    g.set_ppe_launch(True)
     base = res["plain_fp64"]["ms"]
     for k in res:
         res[k]["speedup_vs_plain"] = round(base / res[k]["ms"], 3) if res[k]["ms"] > 0 else None

@@ -217,6 +217,12 @@ int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm_start, double tol, int ma
  * error margin; per-particle results differ from FP64 by ~1e-11 relative.  Operators
  * without a DF32 kernel (diffusive/mean PND, extrapolation, shifting, dummy velocity,
  * step-0 PND) run their FP64 kernels in either mode. */
+/* How the PPE solve is launched: 1 (default) the whole solve in one cooperative launch
+ * with device-side grid barriers when the device supports it, 0 one launch per kernel
+ * with the host polling convergence every few iterations.  Same algorithm and results to
+ * rounding; the single launch removes launch gaps and host round trips. */
+int mpsgpu_set_ppe_launch(mpsgpu_t h, int persistent);
+
 #define MPSGPU_PRECISION_FP64  0
 #define MPSGPU_PRECISION_DF32  1
 int mpsgpu_set_precision(mpsgpu_t h, int precision);
@@ -280,8 +286,9 @@ int mpsgpu_abi_sizes(int* params, int* stats, int* mesh);
 /* Device timing per operator with CUDA events on the handle's stream (the per-kernel
  * timer the reference lacks; it only prints wall time, src/MpsInputOutput.cpp:31-55).
  * Classes 0..MPS_OP_COUNT-1 are the MpsOp operators, followed by NEIGHBOR_LIST,
- * PPE_ASSEMBLE, PPE_SPMV, PPE_VECTOR, PPE_OTHER.  Enabling resets the totals. */
-#define MPSGPU_PROF_NCLASS (MPS_OP_COUNT + 5)
+ * PPE_ASSEMBLE, PPE_SPMV, PPE_VECTOR, PPE_OTHER, PPE_SOLVE (a whole solve in one launch).
+ * Enabling resets the totals. */
+#define MPSGPU_PROF_NCLASS (MPS_OP_COUNT + 6)
 int mpsgpu_profile(mpsgpu_t h, int enable);
 int mpsgpu_profile_get(mpsgpu_t h, int cls, double* ms, long long* calls);
 const char* mpsgpu_profile_name(int cls);

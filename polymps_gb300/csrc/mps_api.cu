@@ -34,6 +34,7 @@ struct mpsgpu_s {
     bool listValid = false;
     bool masksValid = false;
     bool cacheValid = false;   // per-entry FP64 weights of the current list
+    bool persistent = true;    // PPE solve in one cooperative launch when the device allows it
     double timeCurrent = 0.0;
     int numIter = 0;
     int lastOut = 0;
@@ -227,9 +228,16 @@ static int calcPress(mpsgpu_t h) {
     double rr = 0, rr0 = 0;
     int maxIt = h->maxIter > 0 ? h->maxIter : 2 * h->N0;
     int e;
-    if (h->solver == MPSGPU_SOLVER_MIXED)
+    const bool mixed = h->solver == MPSGPU_SOLVER_MIXED;
+    h->B.prepared = df32(h) ? 1 : 0;   // the DF32 assembly writes the FP32 copies itself
+    if (h->persistent && (mixed ? h->B.pgridMx : h->B.pgridCg) > 0) {
+        e = ppeSolvePersistent(h->d, h->B, mixed ? 1 : 0, h->tol, maxIt, h->s, &iters, &refine, &rr, &rr0, &h->prof);
+        if (e == MPSGPU_ERR_CUDA) g_lastError = "persistent PPE solve: launch failed or a grid-barrier wait ran out";
+    } else if (mixed) {
         e = ppeSolveMixed(h->d, h->B, h->tol, maxIt, h->s, &iters, &refine, &rr, &rr0, &h->prof);
-    else e = ppeSolvePlain(h->d, h->B, h->tol, maxIt, h->s, &iters, &rr, &rr0, &h->prof);
+    } else {
+        e = ppeSolvePlain(h->d, h->B, h->tol, maxIt, h->s, &iters, &rr, &rr0, &h->prof);
+    }
     cudaEventRecord(h->es1, h->s);
     if (h->mlp.recording && !e) {
         // features of this system with the previous solution, target = converged - previous
@@ -392,7 +400,7 @@ const char* mpsgpu_profile_name(int cls) {
                                 "PND_DIFFUSIVE", "PND_MEAN", "UPDATE_BC", "CALC_PRESS", "EXTRAPOLATE_PRESS",
                                 "PRESS_GRADIENT", "WALL_PRESS_GRADIENT", "WALL_VISCOSITY", "CORRECT", "SHIFTING",
                                 "DUMMY_VELOCITY", "INIT_PND"};
-    static const char* extra[] = {"NEIGHBOR_LIST", "PPE_ASSEMBLE", "PPE_SPMV", "PPE_VECTOR", "PPE_OTHER"};
+    static const char* extra[] = {"NEIGHBOR_LIST", "PPE_ASSEMBLE", "PPE_SPMV", "PPE_VECTOR", "PPE_OTHER", "PPE_SOLVE"};
     static_assert(sizeof(ops) / sizeof(ops[0]) == MPS_OP_COUNT, "operator names");
     if (cls >= 0 && cls < MPS_OP_COUNT) return ops[cls];
     if (cls >= MPS_OP_COUNT && cls < PROF_NCLASS) return extra[cls - MPS_OP_COUNT];
@@ -550,10 +558,14 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         A(B.rowLen, n);
         A(B.valf, (size_t)d.K * n);
         for (float** v : {&B.diagf, &B.diagInvf, &B.rf, &B.zf, &B.pf, &B.Apf, &B.xf}) A(*v, n);
+        B.pgridCg = ppePersistentGrid(0);
+        B.pgridMx = ppePersistentGrid(1);
         A(B.scal, 16);
-        A(B.partials, 4 * B.nblocks);
+        A(B.partials, 4 * std::max(B.nblocks, std::max(B.pgridCg, B.pgridMx)));
         A(B.counter, 1);
-        A(B.flag, 4);
+        A(B.flag, 8);
+        A(B.dinv, n);
+        A(B.bar, 96);   // three 128-byte lines of barrier words
     }
 #undef A
     // upload the particle state (src/MpsInputOutput.cpp:759-856 initial values)
@@ -651,6 +663,12 @@ int mpsgpu_set_precision(mpsgpu_t h, int precision) {
         h->masksValid = false;
         h->cacheValid = false;
     }
+    return 0;
+}
+
+int mpsgpu_set_ppe_launch(mpsgpu_t h, int persistent) {
+    if (!h) return MPSGPU_ERR_ARG;
+    h->persistent = persistent != 0;
     return 0;
 }
 

@@ -12,7 +12,7 @@ long long launchCount();
 // are the operators; the extra classes split the pressure solve.
 enum {
     PROF_NEIGHBOR_LIST = MPS_OP_COUNT, PROF_PPE_ASSEMBLE, PROF_PPE_SPMV, PROF_PPE_VECTOR,
-    PROF_PPE_OTHER, PROF_NCLASS
+    PROF_PPE_OTHER, PROF_PPE_SOLVE, PROF_NCLASS
 };
 struct Prof {
     bool on = false;
@@ -87,8 +87,12 @@ struct PpeBuffers {
     float *valf, *diagf, *diagInvf, *rf, *zf, *pf, *Apf, *xf;  // mixed-precision copies
     double* partials;
     unsigned int* counter;
-    int* flag;       // [0] = done, [1] = iterations
+    int* flag;       // [0] done, [1] iterations, [2] breakdown, [3] inner done, [4] refinements
     int nblocks;
+    double* dinv;            // FP64 inverse diagonal (persistent plain solver)
+    unsigned int* bar;       // grid barrier of the persistent solvers: arrivals, generation, abort
+    int pgridCg, pgridMx;    // co-resident grid sizes of the persistent solvers (0: unavailable)
+    int prepared;            // FP32 copies (valf, diagf, diagInvf) already written by the assembly
 };
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);
@@ -98,3 +102,7 @@ int ppeSolvePlain(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cu
                   int* iters, double* relres, double* relres0, Prof* prof);
 int ppeSolveMixed(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cudaStream_t s,
                   int* iters, int* refinements, double* relres, double* relres0, Prof* prof);
+// Whole solve in one cooperative launch (mixed = 1: FP32 inner CG under FP64 refinement).
+int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol, int maxIter, cudaStream_t s,
+                       int* iters, int* refinements, double* relres, double* relres0, Prof* prof);
+int ppePersistentGrid(int mixed);

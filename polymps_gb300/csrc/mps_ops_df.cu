@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
     const MpsParams& P = d.P;
     int bci = d.bc[i];
     if (bci == P.other || bci == P.surface) {
-        B.diag[i] = 1.0; B.rowLen[i] = 0; B.b[i] = 0.0;
+        B.diag[i] = 1.0; B.diagf[i] = 1.0f; B.diagInvf[i] = 1.0f; B.rowLen[i] = 0; B.b[i] = 0.0;
         warpCount(d.counters + 1, 0u);
         return;
     }
@@ -433,13 +433,17 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
             if (d.bc[j] == P.inner) {
                 size_t k = (size_t)len * B.N0 + i;
                 B.val[k] = dD(mij);
+                B.valf[k] = mij.h;   // the FP32 copy of the mixed solver (hi part = fl32)
                 B.col[k] = j;
                 len++;
             }
         }
     });
     double rho = P.DNS_FL1;
-    B.diag[i] = dD(sum) - P.alphaCompressibility * rho / (P.timeStep * P.timeStep);
+    double dg = dD(sum) - P.alphaCompressibility * rho / (P.timeStep * P.timeStep);
+    B.diag[i] = dg;
+    B.diagf[i] = (float)dg;
+    B.diagInvf[i] = 1.0f / (float)dg;
     B.rowLen[i] = len;
     B.b[i] = dD(src) + (-P.coeffPPESource * rho * (d.pndSmall[i] - P.pndSmallZero));
     warpCount(d.counters + 1, (unsigned)len);

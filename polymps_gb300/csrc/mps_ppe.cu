@@ -15,13 +15,13 @@
 //
 // The mixed solver keeps FP64 for the iterative-refinement residual r = b - Ax, its norm
 // and all dot products, and runs the inner CG on FP32 matrix values and vectors.
-#include "mps_common.cuh"
+#include "mps_df.cuh"
 #include "mps_internal.h"
 
 #define PBLK 256
 
 // solver scalars in B.scal[]
-enum { S_RZ = 0, S_RR, S_BB, S_ALPHA, S_BETA, S_PAP, S_THR, S_RZNEW, S_SCALE, S_COUNT };
+enum { S_RZ = 0, S_RR, S_BB, S_ALPHA, S_BETA, S_PAP, S_THR, S_RZNEW, S_SCALE, S_INV, S_SQRT, S_COUNT };
 
 // ------------------------------------------------------------------ assembly
 __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
@@ -136,26 +136,36 @@ __device__ __forceinline__ void gridSum(double (&v)[NV], const PpeBuffers& B, Fi
     if (threadIdx.x == 0) fin(acc);
 }
 
-// ------------------------------------------------------------------ plain FP64 PCG
-// One ELL row, four entries in flight (independent value/column/gather loads).
-__device__ __forceinline__ double spmvRow(const PpeBuffers& B, const double* x, int i) {
-    double s = B.diag[i] * x[i];
-    int len = B.rowLen[i];
-    const size_t N0 = B.N0;
-    const double* v = B.val + i;
-    const int* c = B.col + i;
-    int k = 0;
-    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
-    for (; k + 4 <= len; k += 4) {
-        int c0 = __ldg(c + k * N0), c1 = __ldg(c + (k + 1) * N0), c2 = __ldg(c + (k + 2) * N0), c3 = __ldg(c + (k + 3) * N0);
-        double v0 = __ldg(v + k * N0), v1 = __ldg(v + (k + 1) * N0), v2 = __ldg(v + (k + 2) * N0), v3 = __ldg(v + (k + 3) * N0);
-        s += v0 * __ldg(x + c0);
-        s1 += v1 * __ldg(x + c1);
-        s2 += v2 * __ldg(x + c2);
-        s3 += v3 * __ldg(x + c3);
+// ------------------------------------------------------------------ ELL rows
+// One ELL row, eight entries in flight: the column and value loads of a chunk are issued
+// together, then the eight gathers; the last chunk is masked (predicated loads, the row's
+// own index as a harmless column) instead of a serial remainder loop.  RO: the gathered
+// vector is read-only for the launch (non-coherent cache path); otherwise plain loads.
+#define ELL_U 8
+template <class T, bool RO>
+__device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col, const T* x, int i, int len, size_t N0) {
+    T acc[ELL_U];
+#pragma unroll
+    for (int u = 0; u < ELL_U; u++) acc[u] = T(0);
+    const T* v = val + i;
+    const int* c = col + i;
+    for (int k = 0; k < len; k += ELL_U) {
+        int cc[ELL_U];
+        T vv[ELL_U];
+#pragma unroll
+        for (int u = 0; u < ELL_U; u++) {
+            bool ok = k + u < len;
+            cc[u] = ok ? __ldg(c + (size_t)(k + u) * N0) : i;
+            vv[u] = ok ? __ldg(v + (size_t)(k + u) * N0) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < ELL_U; u++) acc[u] += vv[u] * (RO ? __ldg(x + cc[u]) : x[cc[u]]);
     }
-    for (; k < len; k++) s += __ldg(v + k * N0) * __ldg(x + __ldg(c + k * N0));
-    return s + ((s1 + s2) + s3);
+    T xi = RO ? __ldg(x + i) : x[i];
+    return __ldg(diag + i) * xi + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
+}
+__device__ __forceinline__ double spmvRow(const PpeBuffers& B, const double* x, int i) {
+    return ellRow<double, true>(B.diag, B.val, B.col, x, i, __ldg(B.rowLen + i), B.N0);
 }
 
 // r = b - A x, z = r / diag, p = z; sums r.z, r.r, b.b
@@ -330,23 +340,7 @@ __global__ void __launch_bounds__(PBLK) k_mx_inner_init(Dev d, PpeBuffers B) {
     gridSum<1>(v, B, [&](double* t) { B.scal[S_RZ] = t[0]; B.flag[3] = 0; });
 }
 __device__ __forceinline__ float spmvRowF(const PpeBuffers& B, const float* x, int i) {
-    float s = B.diagf[i] * x[i];
-    int len = B.rowLen[i];
-    const size_t N0 = B.N0;
-    const float* v = B.valf + i;
-    const int* c = B.col + i;
-    int k = 0;
-    float s1 = 0.f, s2 = 0.f, s3 = 0.f;
-    for (; k + 4 <= len; k += 4) {
-        int c0 = __ldg(c + k * N0), c1 = __ldg(c + (k + 1) * N0), c2 = __ldg(c + (k + 2) * N0), c3 = __ldg(c + (k + 3) * N0);
-        float v0 = __ldg(v + k * N0), v1 = __ldg(v + (k + 1) * N0), v2 = __ldg(v + (k + 2) * N0), v3 = __ldg(v + (k + 3) * N0);
-        s += v0 * __ldg(x + c0);
-        s1 += v1 * __ldg(x + c1);
-        s2 += v2 * __ldg(x + c2);
-        s3 += v3 * __ldg(x + c3);
-    }
-    for (; k < len; k++) s += __ldg(v + k * N0) * __ldg(x + __ldg(c + k * N0));
-    return s + ((s1 + s2) + s3);
+    return ellRow<float, true>(B.diagf, B.valf, B.col, x, i, __ldg(B.rowLen + i), B.N0);
 }
 __global__ void __launch_bounds__(PBLK) k_mx_spmv(Dev d, PpeBuffers B) {
     if (*(volatile int*)(B.flag + 3)) return;
@@ -450,4 +444,375 @@ int ppeSolveMixed(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cu
     *relres0 = sc[S_SCALE];
     if (hf[2] || !hf[0]) return MPSGPU_ERR_NOT_CONVERGED;
     return 0;
+}
+
+// ------------------------------------------------------------------ persistent solvers
+// The whole solve in one cooperative launch (every block co-resident): no host polling,
+// no per-iteration launches.  Each CG iteration is two grid-wide reductions in the form
+//   Ap = A z + beta Ap,  p = z + beta p            (one SpMV, on z: A p follows by linearity)
+//   x += alpha p, r -= alpha Ap, z = M^-1 r
+// so the only vector every block gathers (z) is complete at the reduction before it.  The
+// reductions are deterministic: per-block partials, the last block to arrive sums them in
+// block order, writes the scalars and releases the others.  Waits are bounded: a block that
+// waits longer than QSPIN polls sets the abort word and every block returns.
+#define QB 256
+#define QSPIN (1 << 21)
+// barrier words, each on its own 128-byte line (the pollers of the generation word must
+// not contend with the arrival atomics): arrivals, generation, abort
+#define QB_ARR 0
+#define QB_GEN 32
+#define QB_ABT 64
+#define QB_WORDS 96
+
+__device__ __forceinline__ double vd(const double* p) { return *(volatile const double*)p; }
+__device__ __forceinline__ int vi(const int* p) { return *(volatile const int*)p; }
+
+struct QCtl {
+    unsigned int gen;
+};
+
+// Release/wait half of the grid barrier (thread 0 of each block), after the block's partials
+// are written.  The last block to arrive runs fin() with the whole block first.
+template <class Fin>
+__device__ __forceinline__ bool qArrive(const PpeBuffers& B, QCtl& c, Fin fin) {
+    __shared__ int sLast, sOk;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned int a = atomicAdd(B.bar + QB_ARR, 1u) + 1u;
+        sLast = (a == gridDim.x);
+    }
+    __syncthreads();
+    c.gen++;
+    if (sLast) {
+        __threadfence();
+        fin();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            B.bar[QB_ARR] = 0u;
+            __threadfence();
+            atomicExch(B.bar + QB_GEN, c.gen);
+            sOk = 1;
+        }
+    } else if (threadIdx.x == 0) {
+        int ok = 1;
+        long long spins = 0;
+        while (*(volatile unsigned int*)(B.bar + QB_GEN) < c.gen) {
+            if (++spins > QSPIN) { atomicExch(B.bar + QB_ABT, 1u); ok = 0; break; }
+            if ((spins & 15) == 0 && *(volatile unsigned int*)(B.bar + QB_ABT)) { ok = 0; break; }
+            __nanosleep(100);
+        }
+        __threadfence();
+        sOk = ok;
+    }
+    __syncthreads();
+    return sOk;
+}
+__device__ __forceinline__ bool qBarrier(const PpeBuffers& B, QCtl& c) {
+    __syncthreads();
+    return qArrive(B, c, [] {});
+}
+// Grid sum of NV FP64 values per thread; fin(tot) runs on thread 0 of the last block.
+template <int NV, class Fin>
+__device__ __forceinline__ bool qSum(double (&v)[NV], const PpeBuffers& B, QCtl& c, Fin fin) {
+    __shared__ double sm[NV * 32];
+    blockSum<NV>(v, sm);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < NV; q++) B.partials[q * gridDim.x + blockIdx.x] = v[q];
+    return qArrive(B, c, [&] {
+        double acc[NV];
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            double s = 0.0;
+            for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+                s += ((volatile double*)B.partials)[q * gridDim.x + b];
+            acc[q] = s;
+        }
+        blockSum<NV>(acc, sm);
+        if (threadIdx.x == 0) fin(acc);
+    });
+}
+// The same with float-float per-thread partials (FP32 vectors): the warp reduces in
+// float-float, each warp's total is converted to FP64 once, the rest of the sum is FP64.
+template <int NV, class Fin>
+__device__ __forceinline__ bool qSumDF(df (&a)[NV], const PpeBuffers& B, QCtl& c, Fin fin) {
+    double v[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            df b = {__shfl_xor_sync(0xffffffffu, a[q].h, o), __shfl_xor_sync(0xffffffffu, a[q].l, o)};
+            a[q] = a[q] + b;
+        }
+        v[q] = ((threadIdx.x & 31) == 0) ? dD(a[q]) : 0.0;
+    }
+    return qSum<NV>(v, B, c, fin);
+}
+
+// Rows inside the persistent kernels: matrix arrays are read-only for the launch, the
+// gathered vector is written by other blocks during it (plain loads, made visible by the
+// barrier's fences).  forRows walks a thread's rows with the next row's length prefetched.
+template <class F>
+__device__ __forceinline__ void forRows(const PpeBuffers& B, int n, int t0, int T, F&& f) {
+    int i = t0;
+    int len = i < n ? __ldg(B.rowLen + i) : 0;
+    while (i < n) {
+        int in = i + T;
+        int ln = in < n ? __ldg(B.rowLen + in) : 0;
+        f(i, len);
+        i = in;
+        len = ln;
+    }
+}
+__device__ __forceinline__ double qRow(const PpeBuffers& B, const double* x, int i, int len) {
+    return ellRow<double, false>(B.diag, B.val, B.col, x, i, len, B.N0);
+}
+__device__ __forceinline__ float qRowF(const PpeBuffers& B, const float* x, int i, int len) {
+    return ellRow<float, false>(B.diagf, B.valf, B.col, x, i, len, B.N0);
+}
+
+// Mixed solver: FP64 residual r = b - A x and its norm, FP32 inner CG on r / ||r|| to
+// the relative tolerance eta, x += ||r|| d in FP64, repeated until ||r|| < tol ||b||.
+__global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
+    const int n = liveN(d);
+    const int T = gridDim.x * QB;
+    const int t0 = blockIdx.x * QB + threadIdx.x;
+    QCtl c = {0u};
+    {
+        double v[2] = {0.0, 0.0};
+        forRows(B, n, t0, T, [&](int i, int len) {
+            double r = B.b[i] - qRow(B, B.x, i, len);
+            B.r[i] = r;
+            v[0] += r * r;
+            v[1] += B.b[i] * B.b[i];
+        });
+        if (!qSum<2>(v, B, c, [&](const double* t) {
+                B.scal[S_RR] = t[0];
+                B.scal[S_BB] = t[1];
+                double thr = tol * tol * t[1];
+                if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
+                B.scal[S_THR] = thr;
+                B.scal[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
+                B.scal[S_SQRT] = sqrt(t[0]);
+                B.scal[S_INV] = 1.0 / sqrt(t[0]);
+                B.flag[0] = (t[1] == 0.0 || t[0] < thr) ? 1 : 0;
+                B.flag[1] = 0;
+                B.flag[3] = 0;
+                if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
+            }))
+            return;
+    }
+    int total = 0, refine = 0;
+    while (!vi(B.flag) && total < maxIter && refine <= 20) {
+        // inner start: rf = r / ||r||, z = M rf, x_f = 0
+        {
+            const double inv = vd(B.scal + S_INV);
+            df a[1] = {dfF(0.f)};
+            for (int i = t0; i < n; i += T) {
+                float r = (float)(B.r[i] * inv);
+                float z = r * __ldg(B.diagInvf + i);
+                B.rf[i] = r; B.zf[i] = z; B.xf[i] = 0.f;
+                a[0] += prod2(r, z);
+            }
+            if (!qSumDF<1>(a, B, c, [&](const double* t) { B.scal[S_RZ] = t[0]; B.flag[3] = 0; })) return;
+        }
+        int inner = 0;
+        while (true) {
+            {
+                const float beta = inner ? (float)vd(B.scal + S_BETA) : 0.f;
+                df a[1] = {dfF(0.f)};
+                forRows(B, n, t0, T, [&](int i, int len) {
+                    float q = qRowF(B, B.zf, i, len);
+                    float z = B.zf[i];
+                    float ap = inner ? q + beta * B.Apf[i] : q;
+                    float p = inner ? z + beta * B.pf[i] : z;
+                    B.Apf[i] = ap; B.pf[i] = p;
+                    a[0] += prod2(p, ap);
+                });
+                if (!qSumDF<1>(a, B, c, [&](const double* t) { B.scal[S_PAP] = t[0]; B.scal[S_ALPHA] = B.scal[S_RZ] / t[0]; }))
+                    return;
+            }
+            {
+                const float alpha = (float)vd(B.scal + S_ALPHA);
+                df a[2] = {dfF(0.f), dfF(0.f)};
+                for (int i = t0; i < n; i += T) {
+                    B.xf[i] += alpha * B.pf[i];
+                    float r = B.rf[i] - alpha * B.Apf[i];
+                    float z = r * __ldg(B.diagInvf + i);
+                    B.rf[i] = r; B.zf[i] = z;
+                    a[0] += prod2(r, z);
+                    a[1] += prod2(r, r);
+                }
+                if (!qSumDF<2>(a, B, c, [&](const double* t) {
+                        B.flag[1] += 1;
+                        B.scal[S_BETA] = t[0] / B.scal[S_RZ];
+                        B.scal[S_RZ] = t[0];
+                        if (t[1] < eta2 || !(t[1] == t[1])) B.flag[3] = 1;
+                    }))
+                    return;
+            }
+            inner++;
+            if (vi(B.flag + 3) || total + inner >= maxIter || inner >= 400) break;
+        }
+        total += inner;
+        {
+            const double sc = vd(B.scal + S_SQRT);
+            for (int i = t0; i < n; i += T) B.x[i] += sc * (double)B.xf[i];
+            if (!qBarrier(B, c)) return;
+        }
+        {
+            double v[1] = {0.0};
+            forRows(B, n, t0, T, [&](int i, int len) {
+                double r = B.b[i] - qRow(B, B.x, i, len);
+                B.r[i] = r;
+                v[0] += r * r;
+            });
+            if (!qSum<1>(v, B, c, [&](const double* t) {
+                    B.scal[S_RR] = t[0];
+                    B.scal[S_SQRT] = sqrt(t[0]);
+                    B.scal[S_INV] = 1.0 / sqrt(t[0]);
+                    if (t[0] < B.scal[S_THR]) B.flag[0] = 1;
+                    if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
+                    B.flag[4] += 1;
+                }))
+                return;
+        }
+        refine++;
+    }
+}
+
+// Plain FP64 Jacobi-PCG (Eigen's ConjugateGradient with its diagonal preconditioner,
+// src/MpsPressure.cpp:424-445): z = invdiag * r, stop when ||r||^2 < tol^2 ||b||^2.
+__global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double tol, int maxIter) {
+    const int n = liveN(d);
+    const int T = gridDim.x * QB;
+    const int t0 = blockIdx.x * QB + threadIdx.x;
+    QCtl c = {0u};
+    {
+        double v[3] = {0.0, 0.0, 0.0};
+        forRows(B, n, t0, T, [&](int i, int len) {
+            double di = 1.0 / __ldg(B.diag + i);
+            double r = B.b[i] - qRow(B, B.x, i, len);
+            double z = r * di;
+            B.dinv[i] = di; B.r[i] = r; B.z[i] = z;
+            v[0] += r * z; v[1] += r * r; v[2] += B.b[i] * B.b[i];
+        });
+        if (!qSum<3>(v, B, c, [&](const double* t) {
+                B.scal[S_RZ] = t[0]; B.scal[S_RR] = t[1]; B.scal[S_BB] = t[2];
+                double thr = tol * tol * t[2];
+                if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
+                B.scal[S_THR] = thr;
+                B.scal[S_SCALE] = sqrt(t[1] / (t[2] > 0 ? t[2] : 1.0));
+                B.flag[0] = (t[2] == 0.0 || t[1] < thr) ? 1 : 0;
+                B.flag[1] = 0;
+                if (!(t[0] == t[0]) || !(t[1] == t[1])) { B.flag[0] = 1; B.flag[2] = 1; }
+            }))
+            return;
+    }
+    int it = 0;
+    while (!vi(B.flag) && it < maxIter) {
+        {
+            const double beta = it ? vd(B.scal + S_BETA) : 0.0;
+            double v[1] = {0.0};
+            forRows(B, n, t0, T, [&](int i, int len) {
+                double q = qRow(B, B.z, i, len);
+                double z = B.z[i];
+                double ap = it ? q + beta * B.Ap[i] : q;
+                double p = it ? z + beta * B.p[i] : z;
+                B.Ap[i] = ap; B.p[i] = p;
+                v[0] += p * ap;
+            });
+            if (!qSum<1>(v, B, c, [&](const double* t) { B.scal[S_PAP] = t[0]; B.scal[S_ALPHA] = B.scal[S_RZ] / t[0]; }))
+                return;
+        }
+        {
+            const double alpha = vd(B.scal + S_ALPHA);
+            double v[2] = {0.0, 0.0};
+            for (int i = t0; i < n; i += T) {
+                B.x[i] += alpha * B.p[i];
+                double r = B.r[i] - alpha * B.Ap[i];
+                double z = r * B.dinv[i];
+                B.r[i] = r; B.z[i] = z;
+                v[0] += r * z; v[1] += r * r;
+            }
+            if (!qSum<2>(v, B, c, [&](const double* t) {
+                    B.flag[1] += 1;
+                    B.scal[S_RR] = t[1];
+                    B.scal[S_BETA] = t[0] / B.scal[S_RZ];
+                    B.scal[S_RZ] = t[0];
+                    if (t[1] < B.scal[S_THR]) B.flag[0] = 1;
+                    if (!(t[1] == t[1])) { B.flag[0] = 1; B.flag[2] = 1; }
+                }))
+                return;
+        }
+        it++;
+    }
+    if (!qBarrier(B, c)) return;
+    {
+        double v[1] = {0.0};
+        forRows(B, n, t0, T, [&](int i, int len) {
+            double r = B.b[i] - qRow(B, B.x, i, len);
+            v[0] += r * r;
+        });
+        qSum<1>(v, B, c, [&](const double* t) { B.scal[S_RR] = t[0]; });
+    }
+}
+
+int ppePersistentGrid(int kind) {
+    int dev = 0, sms = 0, coop = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) return 0;
+    cudaError_t e = kind ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve, QB, 0)
+                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_solve, QB, 0);
+    if (e != cudaSuccess || per <= 0) return 0;
+    return per * sms;
+}
+
+static int finishPersistent(const PpeBuffers& B, cudaStream_t s, int* iters, int* refinements, double* relres,
+                            double* relres0) {
+    int f[5];
+    unsigned int abortWord = 0;
+    double sc[S_COUNT];
+    if (cudaMemcpyAsync(f, B.flag, sizeof(f), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
+    if (cudaMemcpyAsync(&abortWord, B.bar + QB_ABT, sizeof(unsigned int), cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return MPSGPU_ERR_CUDA;
+    if (cudaMemcpyAsync(sc, B.scal, sizeof(sc), cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return MPSGPU_ERR_CUDA;
+    if (abortWord) return MPSGPU_ERR_CUDA;   // a grid-barrier wait ran out (reported by the caller)
+    *iters = f[1];
+    if (refinements) *refinements = f[4];
+    double bb = sc[S_BB] > 0 ? sc[S_BB] : 1.0;
+    *relres = (sc[S_BB] > 0) ? sqrt(sc[S_RR] / bb) : 0.0;
+    *relres0 = sc[S_SCALE];
+    if (f[2] || !f[0]) return MPSGPU_ERR_NOT_CONVERGED;
+    return 0;
+}
+
+int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol, int maxIter, cudaStream_t s,
+                       int* iters, int* refinements, double* relres, double* relres0, Prof* prof) {
+    int grid = mixed ? B.pgridMx : B.pgridCg;
+    if (grid <= 0) return MPSGPU_ERR_UNSUPPORTED;
+    bool pr = prof && prof->on;
+    cudaMemsetAsync(B.flag, 0, 5 * sizeof(int), s);
+    cudaMemsetAsync(B.bar, 0, QB_WORDS * sizeof(unsigned int), s);
+    if (mixed && !B.prepared) {
+        if (pr) prof->begin(PROF_PPE_OTHER, s);
+        k_mixed_prepare<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B);
+        if (pr) prof->end(s);
+        countLaunch(1);
+    }
+    Dev dd = d;
+    PpeBuffers bb = B;
+    double t = tol, eta2 = 2e-4 * 2e-4;
+    int mi = maxIter;
+    void* args[5] = {&dd, &bb, &t, &mi, &eta2};
+    if (pr) prof->begin(PROF_PPE_SOLVE, s);
+    cudaError_t e = mixed ? cudaLaunchCooperativeKernel((const void*)k_mx_solve, grid, QB, args, 0, s)
+                          : cudaLaunchCooperativeKernel((const void*)k_cg_solve, grid, QB, args, 0, s);
+    if (pr) prof->end(s);
+    if (e != cudaSuccess) return MPSGPU_ERR_CUDA;
+    countLaunch(1);
+    return finishPersistent(B, s, iters, refinements, relres, relres0);
 }

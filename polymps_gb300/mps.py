@@ -17,7 +17,7 @@ _lib = None
 
 EXPORTS = [
     "mpsgpu_params_derive", "mpsgpu_create", "mpsgpu_destroy", "mpsgpu_initialize", "mpsgpu_step",
-    "mpsgpu_run", "mpsgpu_run_op", "mpsgpu_set_solver", "mpsgpu_set_precision", "mpsgpu_get_field", "mpsgpu_set_field",
+    "mpsgpu_run", "mpsgpu_run_op", "mpsgpu_set_solver", "mpsgpu_set_precision", "mpsgpu_set_ppe_launch", "mpsgpu_get_field", "mpsgpu_set_field",
     "mpsgpu_num_particles", "mpsgpu_time", "mpsgpu_get_neighbors", "mpsgpu_get_ppe",
     "mpsgpu_mlp_set_weights", "mpsgpu_mlp_get_weights", "mpsgpu_ppe_features", "mpsgpu_mlp_record",
     "mpsgpu_mlp_num_records", "mpsgpu_mlp_fit_normalization", "mpsgpu_mlp_train", "mpsgpu_mlp_forward",
@@ -25,7 +25,7 @@ EXPORTS = [
     "mpsgpu_profile", "mpsgpu_profile_get", "mpsgpu_profile_name", "mpsgpu_launch_count",
     "mpsgpu_last_stats", "mpsgpu_pcg_solve_static", "mpsgpu_pcg_static_error",
 ]
-PROF_NCLASS = len(abi.OPS) + 5
+PROF_NCLASS = len(abi.OPS) + 6
 
 
 class MpsError(RuntimeError):
@@ -54,6 +54,7 @@ def lib(path=None):
     L.mpsgpu_run_op.argtypes = [vp, C.c_int]
     L.mpsgpu_set_solver.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int]
     L.mpsgpu_set_precision.argtypes = [vp, C.c_int]
+    L.mpsgpu_set_ppe_launch.argtypes = [vp, C.c_int]
     L.mpsgpu_get_field.argtypes = [vp, C.c_int, vp]
     L.mpsgpu_set_field.argtypes = [vp, C.c_int, vp]
     L.mpsgpu_num_particles.argtypes = [vp, P(C.c_int)]
@@ -161,6 +162,10 @@ class MpsGpu:
     def set_precision(self, precision=abi.PRECISION_FP64):
         """FP64 (reference arithmetic) or DF32 (float-float pair arithmetic, same decisions)."""
         _check("mpsgpu_set_precision", lib().mpsgpu_set_precision(self.h, precision), self.h)
+
+    def set_ppe_launch(self, persistent=True):
+        """Whole PPE solve in one cooperative launch (True) or one launch per kernel."""
+        _check("mpsgpu_set_ppe_launch", lib().mpsgpu_set_ppe_launch(self.h, int(bool(persistent))), self.h)
 
     def set_solver(self, solver=abi.SOLVER_PLAIN_FP64, warm=abi.WARM_PREVIOUS, tol=1e-8, max_iter=0):
         _check("mpsgpu_set_solver", lib().mpsgpu_set_solver(self.h, solver, warm, tol, max_iter), self.h)

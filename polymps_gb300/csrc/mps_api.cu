@@ -94,7 +94,7 @@ void Prof::destroy() {
 static int opLaunches(int op, const MpsParams& P, bool x) {
     switch (op) {
         case MPS_OP_UPDATE_BUCKETS: return 7;   // key, 3 scan, scatter, sort, bucket-ordered copy
-        case MPS_OP_VISCOSITY: return x ? 2 : 1;   // (DF32: velocity copy) + sweep
+        case MPS_OP_VISCOSITY: return x ? 3 : 1;   // (DF32: velocity copy) + sweep (+ unlisted particles)
         case MPS_OP_OUT_OF_DOMAIN: return 2;
         case MPS_OP_COLLISION: return x ? 3 : 2;
         case MPS_OP_WALL_DISTANCE: case MPS_OP_WALL_NPCD: return P.wallType == 1 ? 1 : 0;
@@ -158,7 +158,7 @@ static void ensureList(mpsgpu_t h) {
     if (df32(h)) launchNeighborListDF(h->d, h->s);
     else launchNeighborList(h->d, h->s);
     if (h->prof.on) h->prof.end(h->s);
-    countLaunch(3);   // FP32 copies (2), list build
+    countLaunch(df32(h) ? 4 : 3);   // FP32 copies (2), list build (DF32: + unlisted particles)
     h->listValid = true;
     h->masksValid = false;
     h->cacheValid = !df32(h);   // the FP64 list build stores the per-entry weights

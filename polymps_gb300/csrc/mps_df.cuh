@@ -186,6 +186,22 @@ __device__ __forceinline__ bool sideOkDF(const Dev& d, const SideDF& s, float4 h
     });
 }
 
+// Particle of thread t for the 27-bucket scans.  Threads walk the stale bucket list in
+// bucket order (STRAY = false), so the lanes of a warp share most of their candidate
+// buckets and their candidate loads coalesce; a live particle appears there once (an
+// out-of-domain removal moves the last particle into the freed index, which the list
+// still holds, and leaves the old last index beyond the live count).  STRAY = true
+// covers, in index order, the live particles the list does not hold (cellOf < 0).
+template <bool STRAY>
+__device__ __forceinline__ int scanParticle(const Dev& d) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = *d.nLive;
+    if (STRAY) return (t < n && d.cellOf[t] < 0) ? t : -1;
+    if (t >= d.cellStart[d.nB]) return -1;
+    int i = d.cellSorted[t];
+    return i < n ? i : -1;
+}
+
 // 27-bucket scan (reference order) over the stale bucket list with the FP32 prefilter on
 // the hi parts; f(j, s, hj) receives every candidate with FP32 squared distance <= hi
 // (s = its slot in bucket order, so posLoCell[s] is its lo part).

@@ -42,9 +42,10 @@ __device__ __forceinline__ df loadDF(const float2* p, int j) {
 // squared distance is below the band are members, those above it were never seen by the
 // prefilter, and only the band's few candidates are decided in float-float (and, inside
 // the float-float margin, in FP64).  No per-entry weights: the DF32 sweeps recompute them.
+template <bool STRAY>
 __global__ void __launch_bounds__(128) k_build_nbr_df(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
+    const int i = scanParticle<STRAY>(d);
+    if (i < 0) return;
     dvec4 pi = d.pos[i];
     float4 hi = d.posf[i], li = d.posLo[i];
     const df R2 = K(d.k.reMax2);
@@ -67,7 +68,8 @@ __global__ void __launch_bounds__(128) k_build_nbr_df(Dev d) {
 void launchNeighborListDF(const Dev& d, cudaStream_t s) {
     cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long), s);
     launchPosf(d, s);
-    k_build_nbr_df<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+    k_build_nbr_df<false><<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+    k_build_nbr_df<true><<<gridFor(d.N0, 128), 128, 0, s>>>(d);
 }
 
 // ------------------------------------------------------------------ entry masks
@@ -115,11 +117,12 @@ void launchSideMasksDF(const Dev& d, cudaStream_t s) {
 // the compacted slots, so the lanes of a warp stay converged through the expensive part.
 #define VCAP 48
 #define VBLK 128
+template <bool STRAY>
 __global__ void __launch_bounds__(VBLK) k_visc_df(Dev d) {
     __shared__ int slots[VCAP * VBLK];
     const int t = threadIdx.x;
-    const int i = blockIdx.x * VBLK + t;
-    if (i >= liveN(d)) return;
+    const int i = scanParticle<STRAY>(d);
+    if (i < 0) return;
     const MpsParams& P = d.P;
     const dvec4 pi = d.pos[i];
     const float4 hi = d.posf[i], li = d.posLo[i];
@@ -175,7 +178,8 @@ __global__ void __launch_bounds__(VBLK) k_visc_df(Dev d) {
 }
 void launchViscosityDF(const Dev& d, cudaStream_t s) {
     launchVelDF(d, s);
-    k_visc_df<<<gridFor(d.N0, VBLK), VBLK, 0, s>>>(d);
+    k_visc_df<false><<<gridFor(d.N0, VBLK), VBLK, 0, s>>>(d);
+    k_visc_df<true><<<gridFor(d.N0, VBLK), VBLK, 0, s>>>(d);
 }
 
 // ------------------------------------------------------------------ collision

@@ -150,6 +150,14 @@ __device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col,
     const T* v = val + i;
     const int* c = col + i;
     for (int k = 0; k < len; k += ELL_U) {
+        // ask L2 for the next chunk's column and value lines while this chunk's gathers run
+        if (k + ELL_U < len) {
+#pragma unroll
+            for (int u = 0; u < ELL_U; u++) {
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(c + (size_t)(k + ELL_U + u) * N0));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(v + (size_t)(k + ELL_U + u) * N0));
+            }
+        }
         int cc[ELL_U];
         T vv[ELL_U];
 #pragma unroll

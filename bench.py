@@ -119,7 +119,19 @@ class Clocks:
 # Algorithmic bytes per call of each timed class (each distinct element read or written
 # once; neighbour re-reads assumed cache resident).  N particles, E neighbour entries,
 # Z off-diagonal PPE non-zeros; df = float-float tier (hi/lo FP32 copies, no weight cache).
-def algo_bytes(cls, N, E, Z, mixed, df):
+def algo_bytes(cls, N, E, Z, mixed, df, st=None):
+    if cls == "PPE_SOLVE" and st is not None and st.runPpeSolves:
+        # one launch = one whole solve; per call averages of the timed run
+        it = st.runPpeIterations / st.runPpeSolves
+        rf = st.runPpeRefinements / st.runPpeSolves
+        if mixed:
+            # inner FP32 iteration: SpMV (valf + col per entry; diag, len, z, Ap, p per row)
+            # + update (x_f, p, r_f, Ap, M^-1, z per row); per refinement: FP64 residual
+            # (val + col per entry; b, r, x, diag, len per row), x update, inner start
+            return it * (60 * N + 8 * Z) + (rf + 1) * (80 * N + 12 * Z)
+        # FP64 iteration: SpMV (val + col; diag, len, z, Ap, p) + update (x, p, r, Ap, M^-1, z);
+        # setup and final residual
+        return it * (116 * N + 12 * Z) + 2 * (60 * N + 12 * Z)
     if cls == "PPE_SPMV":
         return N * (16 if mixed else 28) + Z * (8 if mixed else 12)
     if cls == "PPE_VECTOR":
@@ -213,7 +225,7 @@ def run_gb300(a, rank, world, local):
     roof = None
     if dom:
         ms, calls = leaf[dom]
-        b = algo_bytes(dom, N, E, Z, mixed, prec == abi.PRECISION_DF32)
+        b = algo_bytes(dom, N, E, Z, mixed, prec == abi.PRECISION_DF32, st)
         if b:
             ach = b / (ms / calls / 1e3) / 1e9
             roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
@@ -261,10 +273,13 @@ def ppe_compare(g, abi, use_mlp):
     for op in ops:
         g.run_op(op)
     x_prev = g.get(abi.F_PRESSPPE)
+    x_prev2 = g.get(abi.F_PRESSPPE_PREV)
     res = {}
     # single-launch solves, then the per-kernel launch path for reference
     variants = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, True),
-                ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, True)]
+                ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, True),
+                ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, True),
+                ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP, True)]
     if use_mlp:
         variants.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP, True))
     variants += [("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, False),
@@ -274,6 +289,7 @@ def ppe_compare(g, abi, use_mlp):
         g.set_ppe_launch(single)
         for rep in range(3):
             g.set(abi.F_PRESSPPE, x_prev)
+            g.set(abi.F_PRESSPPE_PREV, x_prev2)
             g.set_solver(s, w, 1e-8, 20000)
             g.run_op("CALC_PRESS")
             st = g.last_stats()

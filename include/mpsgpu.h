@@ -116,6 +116,10 @@ typedef struct MpsStepStats {
     double stepMs;              /* device time of the whole step                       */
     long long nbrEntries;       /* neighbour-list entries of the last list build       */
     long long ppeNnz;           /* non-zeros of the last PPE matrix (with diagonal)    */
+    int    runSteps;            /* steps of the last mpsgpu_run / mpsgpu_step call     */
+    int    runPpeSolves;        /* PPE solves in that call                             */
+    long long runPpeIterations; /* their SpMV iterations, summed                       */
+    long long runPpeRefinements;/* their FP64 refinements, summed                      */
 } MpsStepStats;
 
 /* Field identifiers for get/set.  Vector fields use the reference's interleaved host
@@ -128,6 +132,8 @@ enum MpsField {
     MPS_F_PRESS = 32, MPS_F_PRESSPPE, MPS_F_PNDI, MPS_F_PNDKI, MPS_F_PNDSKI, MPS_F_PNDSMALL,
     MPS_F_NPCD2, MPS_F_CONC, MPS_F_VELDIV, MPS_F_DIFFTERM, MPS_F_PNDWALL, MPS_F_RIW2,
     MPS_F_DEVDOT, MPS_F_SOURCE,
+    MPS_F_PRESSPPE_PREV,          /* solution of the solve before the last (no reference
+                                     array: the warm-start state of the extrapolation) */
     MPS_F_TYPE = 64, MPS_F_BC, MPS_F_NUMNEIGH, MPS_F_NNEIGHWALL, MPS_F_NEARWALL
 };
 
@@ -172,6 +178,7 @@ enum MpsOp {
 #define MPSGPU_WARM_PREVIOUS       0   /* previous-step unclamped pressure (reference)  */
 #define MPSGPU_WARM_MLP            1   /* learned per-particle MLP correction           */
 #define MPSGPU_WARM_ZERO           2
+#define MPSGPU_WARM_EXTRAPOLATE    3   /* 2 p_n - p_{n-1} of the unclamped solutions       */
 
 typedef struct mpsgpu_s* mpsgpu_t;
 
@@ -249,9 +256,12 @@ int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col,
 /* Learned warm start (N2): MLP 16->64->64->64->1, GELU, BF16 weights, FP32 accumulate.
  * Weights are the FP32 master copy in this packed order:
  * W1[64x16] b1[64] W2[64x64] b2[64] W3[64x64] b3[64] W4[1x64] b4[1]  (row-major [out][in]),
- * followed by 32 feature-normalisation floats (mean[16], inv_std[16]). */
+ * The normalisation vector holds MPSGPU_MLP_NNORM floats: feature means[16], feature
+ * inverse spreads[16], then the target's mean and inverse spread.  The network predicts
+ * the correction of the temporal extrapolation 2 p_n - p_{n-1} in target units. */
 #define MPSGPU_MLP_NPARAM (64*16 + 64 + 64*64 + 64 + 64*64 + 64 + 64 + 1)
 #define MPSGPU_MLP_NFEAT  16
+#define MPSGPU_MLP_NNORM  34
 int mpsgpu_mlp_set_weights(mpsgpu_t h, const float* params, const float* norm32);
 int mpsgpu_mlp_get_weights(mpsgpu_t h, float* params, float* norm32);
 /* Features of the current PPE system, N x 16 FP32 (host). */

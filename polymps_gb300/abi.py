@@ -82,6 +82,8 @@ class MpsStepStats(C.Structure):
         ("ppeRelResidual", C.c_double), ("ppeInitialRelResidual", C.c_double),
         ("ppeSolveMs", C.c_double), ("ppeAssembleMs", C.c_double), ("stepMs", C.c_double),
         ("nbrEntries", C.c_longlong), ("ppeNnz", C.c_longlong),
+        ("runSteps", C.c_int), ("runPpeSolves", C.c_int),
+        ("runPpeIterations", C.c_longlong), ("runPpeRefinements", C.c_longlong),
     ]
 
     def as_dict(self):
@@ -101,6 +103,7 @@ F_POS, F_VEL, F_ACC, F_ACCSTAR, F_NPCD, F_GRADC, F_CORR1, F_CORR2, F_CORR3, F_MI
 (F_PRESS, F_PRESSPPE, F_PNDI, F_PNDKI, F_PNDSKI, F_PNDSMALL, F_NPCD2, F_CONC, F_VELDIV,
  F_DIFFTERM, F_PNDWALL, F_RIW2, F_DEVDOT, F_SOURCE) = range(32, 46)
 F_TYPE, F_BC, F_NUMNEIGH, F_NNEIGHWALL, F_NEARWALL = range(64, 69)
+F_PRESSPPE_PREV = 46   # warm-start state (no reference array; not in SCALAR_FIELDS)
 
 VECTOR_FIELDS = set(range(13))
 SCALAR_FIELDS = set(range(32, 46))
@@ -129,10 +132,11 @@ OPS = [
 OP = {name: k for k, name in enumerate(OPS)}
 
 SOLVER_PLAIN_FP64, SOLVER_MIXED = 0, 1
-WARM_PREVIOUS, WARM_MLP, WARM_ZERO = 0, 1, 2
+WARM_PREVIOUS, WARM_MLP, WARM_ZERO, WARM_EXTRAP = 0, 1, 2, 3
 PRECISION_FP64, PRECISION_DF32 = 0, 1
 MLP_NPARAM = 64 * 16 + 64 + 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1
 MLP_NFEAT = 16
+MLP_NNORM = 2 * MLP_NFEAT + 2
 
 
 def params_from_dict(d):
@@ -159,7 +163,7 @@ def params_to_dict(p):
 def field_buffer(field, n):
     if field in VECTOR_FIELDS:
         return np.zeros((n, 3), dtype=np.float64)
-    if field in SCALAR_FIELDS:
+    if field in SCALAR_FIELDS or field == F_PRESSPPE_PREV:
         return np.zeros(n, dtype=np.float64)
     if field in INT_FIELDS:
         return np.zeros(n, dtype=np.int32)

@@ -214,6 +214,7 @@ static int calcPress(mpsgpu_t h) {
     cudaEventRecord(h->ea1, h->s);
     // warm start: previous unclamped solution (reference), zero, or the learned predictor
     if (h->warm == MPSGPU_WARM_ZERO) cudaMemsetAsync(h->B.x, 0, sizeof(double) * h->N0, h->s);
+    if (h->warm == MPSGPU_WARM_EXTRAPOLATE) { launchWarmExtrapolate(h->d, h->B, h->s); countLaunch(1); }
     cudaEventRecord(h->es0, h->s);
     if (h->warm == MPSGPU_WARM_MLP) {
         if (h->prof.on) h->prof.begin(PROF_PPE_OTHER, h->s);
@@ -221,7 +222,7 @@ static int calcPress(mpsgpu_t h) {
         if (h->prof.on) h->prof.end(h->s);
         countLaunch(3);
         if (e) return e;
-    } else if (h->warm != MPSGPU_WARM_ZERO) {
+    } else if (h->warm == MPSGPU_WARM_PREVIOUS) {
         cudaMemcpyAsync(h->B.x, h->d.pressPPE, sizeof(double) * h->N0, cudaMemcpyDeviceToDevice, h->s);
     }
     int iters = 0, refine = 0;
@@ -248,6 +249,9 @@ static int calcPress(mpsgpu_t h) {
     launchPpeCopyBack(h->d, h->B, h->s);
     h->last.ppeIterations = iters;
     h->last.ppeRefinements = refine;
+    h->last.runPpeSolves += 1;
+    h->last.runPpeIterations += iters;
+    h->last.runPpeRefinements += refine;
     h->last.ppeRelResidual = rr;
     h->last.ppeInitialRelResidual = rr0;
     CK(cudaEventSynchronize(h->es1));
@@ -450,6 +454,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         A(*v, n);
     for (int** v : {&d.type, &d.bc, &d.numNeigh, &d.nNeighWall, &d.nearWall}) A(*v, n);
     A(d.posf, n);
+    A(d.pressPPEprev, n);
     A(d.cellOf, n);
     A(d.cellStart, d.nB + 1);
     A(d.cellCount, d.nB + 1);
@@ -623,6 +628,7 @@ int mpsgpu_initialize(mpsgpu_t h) {
 int mpsgpu_step(mpsgpu_t h, MpsStepStats* stats) {
     if (!h) return MPSGPU_ERR_ARG;
     std::memset(&h->last, 0, sizeof(h->last));
+    h->last.runSteps = 1;
     cudaEventRecord(h->e0, h->s);
     int e = stepImpl(h);
     cudaEventRecord(h->e1, h->s);
@@ -636,6 +642,10 @@ int mpsgpu_step(mpsgpu_t h, MpsStepStats* stats) {
 int mpsgpu_run(mpsgpu_t h, int nsteps, MpsStepStats* stats) {
     if (!h || nsteps < 0) return MPSGPU_ERR_ARG;
     cudaEventRecord(h->e0, h->s);
+    h->last.runSteps = nsteps;
+    h->last.runPpeSolves = 0;
+    h->last.runPpeIterations = 0;
+    h->last.runPpeRefinements = 0;
     for (int k = 0; k < nsteps; k++) {
         int e = stepImpl(h);
         if (e) return e;
@@ -673,7 +683,7 @@ int mpsgpu_set_ppe_launch(mpsgpu_t h, int persistent) {
 }
 
 int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm, double tol, int max_iter) {
-    if (!h || (solver != MPSGPU_SOLVER_PLAIN_FP64 && solver != MPSGPU_SOLVER_MIXED) || warm < 0 || warm > 2 || !(tol > 0))
+    if (!h || (solver != MPSGPU_SOLVER_PLAIN_FP64 && solver != MPSGPU_SOLVER_MIXED) || warm < 0 || warm > 3 || !(tol > 0))
         return MPSGPU_ERR_ARG;
     if (warm == MPSGPU_WARM_MLP && !h->mlp.ready) { g_lastError = "MLP weights not set"; return MPSGPU_ERR_ARG; }
     h->solver = solver; h->warm = warm; h->tol = tol; h->maxIter = max_iter;
@@ -735,6 +745,7 @@ static void* fieldPtr(mpsgpu_t h, int f, int* kind) {
         case MPS_F_RIW2: return d.riw2;
         case MPS_F_DEVDOT: return d.devDot;
         case MPS_F_SOURCE: return d.source;
+        case MPS_F_PRESSPPE_PREV: return d.pressPPEprev;
         default: break;
     }
     *kind = 2;

@@ -44,6 +44,7 @@ struct Dev {
     double *pndWall, *riw2, *devDot, *source, *aux1, *aux2;
     int *type, *bc, *numNeigh, *nNeighWall, *nearWall;
     float4* posf;      // FP32 copy of pos - domainMin (neighbour prefilter, FP32 sums)
+    double* pressPPEprev;   // unclamped PPE solution of the solve before the last (warm start)
     // buckets (stale list of the step)
     int *cellOf, *cellStart, *cellCount, *cellSorted, *cellCursor;
     // FP32 positions in bucket order (posfCell[s] = posf[cellSorted[s]]): the prefilter of

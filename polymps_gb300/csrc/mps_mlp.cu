@@ -23,6 +23,7 @@
 
 #define H 64
 #define NF 16
+#define NNORM (2 * NF + 2)   // feature means, feature inverse spreads, target mean, target inverse spread
 // parameter offsets in the packed FP32 master vector
 #define OW1 0
 #define OB1 (OW1 + H * NF)
@@ -168,12 +169,20 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float* feat, int n, c
 }
 
 // ------------------------------------------------------------------ features
-// Raw features of row i of the assembled system (normalised inside the network):
-//  0 (n_i - n0)/n0      1 b_i/A_ii          2 numNeigh/N0       3 surface flag
-//  4 wall distance/reL  5-7 wall normal     8 previous pressure 9 |v|
-// 10 v along -g         11 A_ii             12 wall PND         13 height along -g
-// 14 (b - A p_prev)_i / A_ii (Jacobi step of the warm-start residual)
-// 15 (pndi - pndki)/n0
+// The network corrects the temporal extrapolation of the unclamped solutions,
+// x_e = 2 p_n - p_{n-1}: x0 = x_e + correction on the rows that carry an equation.
+// Raw features of row i of the new system (normalised inside the network); pressures in
+// Pa, lengths in m, velocities in m/s, so that the scales do not depend on the spacing:
+//  0 (n_i - n0)/n0          1 b_i / A_ii              2 numNeigh / N0
+//  3 row without pressure last solve (p_n == 0)       4 wall distance / reL (<= 1.5)
+//  5 p_n - p_{n-1}          6 x_e                     7 (b - A x_e)_i / A_ii (Jacobi step)
+//  8 p_n                    9 |v|                    10 v along -g
+// 11 A_ii / (coeffPPE n0)  12 wall PND               13 height along -g
+// 14 (b_i - b_i of the last solve) / A_ii            15 (pndi - pndki)/n0
+__device__ __forceinline__ double extrapBase(const Dev& d, int j) {
+    double p = d.pressPPE[j];
+    return (p + p) - d.pressPPEprev[j];
+}
 __global__ void k_mlp_features(Dev d, PpeBuffers B, float* feat) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
@@ -181,37 +190,33 @@ __global__ void k_mlp_features(Dev d, PpeBuffers B, float* feat) {
     double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
     double gn = sqrt(gx * gx + gy * gy + gz * gz);
     if (gn > 0) { gx /= gn; gy /= gn; gz /= gn; }
-    dvec4 x = d.pos[i], v = d.vel[i], m = d.mirror[i];
+    dvec4 x = d.pos[i], v = d.vel[i];
     double diag = B.diag[i];
-    double pprev = d.pressPPE[i];
-    double ax = diag * pprev;
+    double pn = d.pressPPE[i], pp = d.pressPPEprev[i];
+    double xe = (d.bc[i] == P.inner) ? (pn + pn) - pp : 0.0;
+    double ax = diag * xe;
     int len = B.rowLen[i];
     for (int k = 0; k < len; k++) {
         size_t e = (size_t)k * B.N0 + i;
-        ax += B.val[e] * d.pressPPE[B.col[e]];
+        ax += B.val[e] * extrapBase(d, B.col[e]);   // matrix columns are inner rows
     }
     double bi = B.b[i];
     float f[NF];
     f[0] = (float)((d.pndSmall[i] - P.pndSmallZero) / P.pndSmallZero);
     f[1] = (float)(bi / diag);
     f[2] = (float)(d.numNeigh[i] / P.numNeighZero);
-    f[3] = (d.bc[i] == P.surface) ? 1.f : 0.f;
-    double dw = sqrt(d.riw2[i]) / P.reL;
-    f[4] = (float)fmin(dw, 1.5);
-    double nx = 0, ny = 0, nz = 0;
-    if (d.nearWall[i]) {
-        nx = x.x - m.x; ny = x.y - m.y; nz = x.z - m.z;
-        double l = sqrt(nx * nx + ny * ny + nz * nz);
-        if (l > 0) { nx /= l; ny /= l; nz /= l; }
-    }
-    f[5] = (float)nx; f[6] = (float)ny; f[7] = (float)nz;
-    f[8] = (float)pprev;
+    f[3] = (pn == 0.0) ? 1.f : 0.f;
+    f[4] = (float)fmin(sqrt(d.riw2[i]) / P.reL, 1.5);
+    f[5] = (float)(pn - pp);
+    f[6] = (float)xe;
+    f[7] = (float)((bi - ax) / diag);
+    f[8] = (float)pn;
     f[9] = (float)sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
     f[10] = (float)-(v.x * gx + v.y * gy + v.z * gz);
-    f[11] = (float)diag;
+    f[11] = (float)(diag / (P.coeffPPE * P.pndSmallZero));
     f[12] = (float)d.pndWall[i];
     f[13] = (float)-(x.x * gx + x.y * gy + x.z * gz);
-    f[14] = (float)((bi - ax) / diag);
+    f[14] = (float)((bi - d.source[i]) / diag);
     f[15] = (float)((d.pndi[i] - d.pndki[i]) / P.pndSmallZero);
     float4* o = (float4*)(feat + (size_t)i * NF);
     o[0] = make_float4(f[0], f[1], f[2], f[3]);
@@ -220,11 +225,13 @@ __global__ void k_mlp_features(Dev d, PpeBuffers B, float* feat) {
     o[3] = make_float4(f[12], f[13], f[14], f[15]);
 }
 
+// x0 = x_e + (out / target_inv_std + target_mean) on equation rows, 0 on identity rows
 __global__ void k_mlp_combine(Dev d, PpeBuffers B, const float* out, const float* norm) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     double x0 = 0.0;
-    if (d.bc[i] == d.P.inner) x0 = d.pressPPE[i] + (double)out[i] / (double)norm[NF + 8];
+    if (d.bc[i] == d.P.inner)
+        x0 = extrapBase(d, i) + (double)out[i] / (double)norm[2 * NF + 1] + (double)norm[2 * NF];
     B.x[i] = x0;
 }
 
@@ -267,7 +274,7 @@ int mlpInit(MlpState& m, int n0, cudaStream_t s) {
     auto al = [&](void** p, size_t b) { bytes += b; return cudaMalloc(p, b) == cudaSuccess; };
     bool ok = al((void**)&m.master, sizeof(float) * NPARAM) && al((void**)&m.adam_m, sizeof(float) * NPARAM) &&
               al((void**)&m.adam_v, sizeof(float) * NPARAM) && al((void**)&m.grad, sizeof(float) * NPARAM) &&
-              al((void**)&m.wbf, sizeof(__nv_bfloat16) * NBF) && al((void**)&m.norm, sizeof(float) * 2 * NF) &&
+              al((void**)&m.wbf, sizeof(__nv_bfloat16) * NBF) && al((void**)&m.norm, sizeof(float) * NNORM) &&
               al((void**)&m.feat, sizeof(float) * NF * (size_t)n0) && al((void**)&m.out, sizeof(float) * (size_t)n0) &&
               al((void**)&m.lossAcc, sizeof(float) * 4);
     if (!ok) return MPSGPU_ERR_NOMEM;
@@ -288,7 +295,7 @@ void mlpFree(MlpState& m) {
 
 int mlpSetWeights(MlpState& m, const float* params, const float* norm32, cudaStream_t s) {
     if (cudaMemcpyAsync(m.master, params, sizeof(float) * NPARAM, cudaMemcpyHostToDevice, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
-    if (cudaMemcpyAsync(m.norm, norm32, sizeof(float) * 2 * NF, cudaMemcpyHostToDevice, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
+    if (cudaMemcpyAsync(m.norm, norm32, sizeof(float) * NNORM, cudaMemcpyHostToDevice, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
     k_to_bf16<<<gridFor(H * H, 256), 256, 0, s>>>(m.master, m.wbf);
     cudaMemsetAsync(m.adam_m, 0, sizeof(float) * NPARAM, s);
     cudaMemsetAsync(m.adam_v, 0, sizeof(float) * NPARAM, s);
@@ -300,7 +307,7 @@ int mlpSetWeights(MlpState& m, const float* params, const float* norm32, cudaStr
 
 int mlpGetWeights(MlpState& m, float* params, float* norm32, cudaStream_t s) {
     if (cudaMemcpyAsync(params, m.master, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
-    if (cudaMemcpyAsync(norm32, m.norm, sizeof(float) * 2 * NF, cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
+    if (cudaMemcpyAsync(norm32, m.norm, sizeof(float) * NNORM, cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
     return cudaStreamSynchronize(s) == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
 }
 
@@ -319,7 +326,7 @@ __global__ void k_mlp_record(Dev d, PpeBuffers B, const float* feat, float* recF
     const float4* src = (const float4*)(feat + (size_t)i * NF);
     float4* dst = (float4*)(recFeat + slot * NF);
     dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
-    recTarget[slot] = (float)(B.x[i] - d.pressPPE[i]);
+    recTarget[slot] = (float)(B.x[i] - extrapBase(d, i));
 }
 int mlpRecordTargets(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s) {
     if (!m.recFeat) {
@@ -364,17 +371,17 @@ int mlpFitNormalization(MlpState& m, cudaStream_t s) {
     cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     cudaFree(acc);
-    float norm[2 * NF];
+    float norm[NNORM];
     double nn = (double)m.recCount;
     for (int k = 0; k < NF; k++) {
         double mu = h[k] / nn, var = h[NF + 1 + k] / nn - mu * mu;
         norm[k] = (float)mu;
         norm[NF + k] = (float)(var > 1e-20 ? 1.0 / sqrt(var) : 1.0);
     }
-    // the output is the pressure change in units of the target spread
+    // the network output is the correction in units of the target spread about its mean
     double my = h[NF] / nn, vy = h[2 * NF + 1] / nn - my * my;
-    norm[NF + 8] = (float)(vy > 1e-20 ? 1.0 / sqrt(vy) : 1.0);
-    norm[8] = norm[8];  // mean of the previous pressure stays a feature offset
+    norm[2 * NF] = (float)my;
+    norm[2 * NF + 1] = (float)(vy > 1e-20 ? 1.0 / sqrt(vy) : 1.0);
     if (cudaMemcpyAsync(m.norm, norm, sizeof(norm), cudaMemcpyHostToDevice, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
     return cudaStreamSynchronize(s) == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
 }
@@ -450,7 +457,7 @@ __global__ void __launch_bounds__(128) k_mlp_train(const float* recFeat, const f
     if (threadIdx.x == 0) { T.b4g = 0.f; T.loss = 0.f; }
     __syncthreads();
     int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, w = threadIdx.x >> 5;
-    float ysc = norm[NF + 8];
+    float ysc = norm[2 * NF + 1], ymu = norm[2 * NF];
     float inv_b = 1.0f / (float)batch;
     float acc3[8][4], acc2[8][4], acc1[2][4];
 #pragma unroll
@@ -470,7 +477,7 @@ __global__ void __launch_bounds__(128) k_mlp_train(const float* recFeat, const f
         long long r1 = seed ? hash32(seed * 2654435761u + (uint32_t)(base + g + 8)) % (uint32_t)nrec : (base + g + 8) % nrec;
         const float* f0 = recFeat + r0 * NF;
         const float* f1 = recFeat + r1 * NF;
-        float y0 = recTarget[r0] * ysc, y1 = recTarget[r1] * ysc;
+        float y0 = (recTarget[r0] - ymu) * ysc, y1 = (recTarget[r1] - ymu) * ysc;
         uint32_t ax[1][4], a1[4][4], a2[4][4];
         float z1[8][4], z2[8][4], z3[8][4];
         loadInput(s, f0, f1, ax[0]);

@@ -111,7 +111,7 @@ __global__ void k_out_serial(Dev d, const int* flags, int* counter) {
         mv(d.pndki, i, L); mv(d.pndski, i, L); mv(d.pndSmall, i, L); mv(d.npcd2, i, L); mv(d.conc, i, L);
         mv(d.velDiv, i, L); mv(d.diffTerm, i, L); mv(d.nearWall, i, L); mv(d.nNeighWall, i, L);
         mv(d.pndWall, i, L); mv(d.devDot, i, L); mv(d.riw2, i, L);
-        if (P.mpsType == 2 || P.mpsType == 3) { mv(d.pressPPE, i, L); mv(d.source, i, L); }
+        if (P.mpsType == 2 || P.mpsType == 3) { mv(d.pressPPE, i, L); mv(d.source, i, L); mv(d.pressPPEprev, i, L); }
         mv(d.acc, i, L); mv(d.accStar, i, L); mv(d.pos, i, L); mv(d.vel, i, L); mv(d.npcd, i, L);
         mv(d.gradC, i, L); mv(d.c1, i, L); mv(d.c2, i, L); mv(d.c3, i, L); mv(d.dvel, i, L);
         mv(d.wallPos, i, L); mv(d.mirror, i, L); mv(d.polyNormal, i, L); mv(d.forceWall, i, L);

@@ -21,7 +21,7 @@
 #define PBLK 256
 
 // solver scalars in B.scal[]
-enum { S_RZ = 0, S_RR, S_BB, S_ALPHA, S_BETA, S_PAP, S_THR, S_RZNEW, S_SCALE, S_INV, S_SQRT, S_COUNT };
+enum { S_RZ = 0, S_RR, S_BB, S_ALPHA, S_BETA, S_PAP, S_THR, S_RZNEW, S_SCALE, S_INV, S_SQRT, S_ETA2, S_COUNT };
 
 // ------------------------------------------------------------------ assembly
 __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
@@ -74,9 +74,21 @@ __global__ void k_ppe_copy_back(Dev d, PpeBuffers B) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     double x = B.x[i];
+    d.pressPPEprev[i] = d.pressPPE[i];
     d.pressPPE[i] = x;
     d.source[i] = B.b[i];
     d.press[i] = x < 0.0 ? 0.0 : x;
+}
+// Warm start by linear extrapolation in time of the unclamped solutions, x0 = 2 p_n - p_{n-1},
+// on the rows of the new system that carry an equation (zero on the identity rows).
+__global__ void k_warm_extrap(Dev d, PpeBuffers B) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    double p = d.pressPPE[i];
+    B.x[i] = (d.bc[i] == d.P.inner) ? (p + p) - d.pressPPEprev[i] : 0.0;
+}
+void launchWarmExtrapolate(const Dev& d, const PpeBuffers& B, cudaStream_t s) {
+    k_warm_extrap<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B);
 }
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s) {
     k_ppe_copy_back<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B);
@@ -580,7 +592,9 @@ __device__ __forceinline__ float qRowF(const PpeBuffers& B, const float* x, int 
 }
 
 // Mixed solver: FP64 residual r = b - A x and its norm, FP32 inner CG on r / ||r|| to
-// the relative tolerance eta, x += ||r|| d in FP64, repeated until ||r|| < tol ||b||.
+// the relative tolerance eta_k, x += ||r|| d in FP64, repeated until ||r|| < tol ||b||.
+// eta_k = max(eta, tol ||b|| / (2 ||r_k||)): an inner solve stops once its correction
+// brings the outer residual to half the tolerance, so the last one does not over-solve.
 __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
     const int n = liveN(d);
     const int T = gridDim.x * QB;
@@ -603,6 +617,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                 B.scal[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
                 B.scal[S_SQRT] = sqrt(t[0]);
                 B.scal[S_INV] = 1.0 / sqrt(t[0]);
+                B.scal[S_ETA2] = fmax(eta2, 0.25 * thr / t[0]);
                 B.flag[0] = (t[1] == 0.0 || t[0] < thr) ? 1 : 0;
                 B.flag[1] = 0;
                 B.flag[3] = 0;
@@ -655,7 +670,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                         B.flag[1] += 1;
                         B.scal[S_BETA] = t[0] / B.scal[S_RZ];
                         B.scal[S_RZ] = t[0];
-                        if (t[1] < eta2 || !(t[1] == t[1])) B.flag[3] = 1;
+                        if (t[1] < B.scal[S_ETA2] || !(t[1] == t[1])) B.flag[3] = 1;
                     }))
                     return;
             }
@@ -679,6 +694,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                     B.scal[S_RR] = t[0];
                     B.scal[S_SQRT] = sqrt(t[0]);
                     B.scal[S_INV] = 1.0 / sqrt(t[0]);
+                    B.scal[S_ETA2] = fmax(eta2, 0.25 * B.scal[S_THR] / t[0]);
                     if (t[0] < B.scal[S_THR]) B.flag[0] = 1;
                     if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
                     B.flag[4] += 1;

@@ -239,12 +239,12 @@ class MpsGpu:
     def mlp_set_weights(self, params, norm):
         params = np.ascontiguousarray(params, dtype=np.float32)
         norm = np.ascontiguousarray(norm, dtype=np.float32)
-        assert params.size == abi.MLP_NPARAM and norm.size == 2 * abi.MLP_NFEAT
+        assert params.size == abi.MLP_NPARAM and norm.size == abi.MLP_NNORM
         _check("mpsgpu_mlp_set_weights", lib().mpsgpu_mlp_set_weights(self.h, abi.fptr(params), abi.fptr(norm)), self.h)
 
     def mlp_get_weights(self):
         params = np.zeros(abi.MLP_NPARAM, dtype=np.float32)
-        norm = np.zeros(2 * abi.MLP_NFEAT, dtype=np.float32)
+        norm = np.zeros(abi.MLP_NNORM, dtype=np.float32)
         _check("mpsgpu_mlp_get_weights", lib().mpsgpu_mlp_get_weights(self.h, abi.fptr(params), abi.fptr(norm)), self.h)
         return params, norm
 

@@ -3,11 +3,13 @@
 1. Run the 3D incompressible polygon dam break at l0 = 0.01 m (108,000 particles) with the
    plain FP64 solver (previous-step warm start, tolerance 1e-10) and record, for every
    inner row of every recorded step, the 16 features of the assembled system and the
-   change of the converged pressure relative to the previous step's solution.
+   difference between the converged pressure and the temporal extrapolation
+   2 p_n - p_{n-1} of the two previous solutions (the network learns that correction).
 2. Fit the feature normalisation on the recorded set, then run Adam on mini-batches with
    the fused BF16 tensor-core forward/backward kernel.
 3. Evaluate on the l0 = 0.005 case (864,000 particles): PPE iterations and time to 1e-8
-   with the learned warm start against the previous-step warm start, same systems.
+   with the learned warm start against the previous-step and the extrapolated warm
+   starts, same systems.
 
     python -m polymps_gb300.train_warmstart [--steps 600] [--iters 3000] [--out PATH]
 """
@@ -37,7 +39,7 @@ def init_params(rng):
 
 def record(steps, every, tol, scale=1.0, warmup=20):
     c = cases.config(4, scale=scale)
-    g = mps.MpsGpu(c, solver=abi.SOLVER_PLAIN_FP64, tol=tol, max_iter=20000)
+    g = mps.MpsGpu(c, solver=abi.SOLVER_PLAIN_FP64, tol=tol, max_iter=20000, precision=abi.PRECISION_DF32)
     g.initialize()
     g.run(warmup)
     t0 = time.perf_counter()
@@ -49,10 +51,10 @@ def record(steps, every, tol, scale=1.0, warmup=20):
 
 
 def evaluate(params, norm, scale=1.0, steps=30, warmup=10, tol=1e-8):
-    """Same systems, three solves each: previous-step vs learned warm start (both with the
-    FP32/FP64 refinement solver) and the plain FP64 CG."""
+    """Same systems, six solves each: the plain FP64 CG and the FP32/FP64 refinement solver,
+    each from the previous-step, the extrapolated and the learned warm start."""
     c = cases.config(3, scale=scale)
-    g = mps.MpsGpu(c, solver=abi.SOLVER_PLAIN_FP64, tol=tol, max_iter=20000)
+    g = mps.MpsGpu(c, solver=abi.SOLVER_PLAIN_FP64, tol=tol, max_iter=20000, precision=abi.PRECISION_DF32)
     g.mlp_set_weights(params, norm)
     g.initialize()
     g.run(warmup)
@@ -63,12 +65,16 @@ def evaluate(params, norm, scale=1.0, steps=30, warmup=10, tol=1e-8):
         for op in ops:
             g.run_op(op)
         x_prev = g.get(abi.F_PRESSPPE)
+        x_prev2 = g.get(abi.F_PRESSPPE_PREV)
         res = {}
         for name, solver, warm in (("plain_prev", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS),
+                                   ("plain_extrap", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP),
+                                   ("plain_mlp", abi.SOLVER_PLAIN_FP64, abi.WARM_MLP),
                                    ("mixed_prev", abi.SOLVER_MIXED, abi.WARM_PREVIOUS),
-                                   ("mixed_mlp", abi.SOLVER_MIXED, abi.WARM_MLP),
-                                   ("plain_mlp", abi.SOLVER_PLAIN_FP64, abi.WARM_MLP)):
+                                   ("mixed_extrap", abi.SOLVER_MIXED, abi.WARM_EXTRAP),
+                                   ("mixed_mlp", abi.SOLVER_MIXED, abi.WARM_MLP)):
             g.set(abi.F_PRESSPPE, x_prev)
+            g.set(abi.F_PRESSPPE_PREV, x_prev2)
             g.set_solver(solver, warm, tol, 20000)
             g.run_op("CALC_PRESS")
             st = g.last_stats()
@@ -76,6 +82,7 @@ def evaluate(params, norm, scale=1.0, steps=30, warmup=10, tol=1e-8):
         rows.append(res)
         # finish the step with the reference solution (plain FP64 from the previous warm start)
         g.set(abi.F_PRESSPPE, x_prev)
+        g.set(abi.F_PRESSPPE_PREV, x_prev2)
         g.set_solver(abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, tol, 20000)
         g.run_op("CALC_PRESS")
         for op in ["CORRECTION_MATRIX", "PRESS_GRADIENT", "WALL_PRESS_GRADIENT", "WALL_VISCOSITY",
@@ -107,7 +114,7 @@ def main():
     rng = np.random.default_rng(a.seed)
     g, c, t_rec = record(a.steps, a.every, tol=1e-10)
     nrec = g.mlp_num_records()
-    g.mlp_set_weights(init_params(rng), np.concatenate([np.zeros(16), np.ones(16)]).astype(np.float32))
+    g.mlp_set_weights(init_params(rng), np.concatenate([np.zeros(16), np.ones(16), [0.0, 1.0]]).astype(np.float32))
     g.mlp_fit_normalization()
     p0, norm = g.mlp_get_weights()
     g.mlp_set_weights(p0, norm)

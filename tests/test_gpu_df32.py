@@ -139,3 +139,30 @@ def test_df32_free_running_steps(oracle_mod, mps_lib, name):
     assert relerr(g.get(abi.F_POS), o.get(abi.F_POS)) < 1e-9
     assert relerr(g.get(abi.F_VEL), o.get(abi.F_VEL)) < 1e-5
     assert relerr(g.get(abi.F_PRESS), o.get(abi.F_PRESS)) < 1e-5
+
+
+@pytest.mark.parametrize("solver", [abi.SOLVER_PLAIN_FP64, abi.SOLVER_MIXED])
+def test_extrapolated_warm_start(oracle_mod, mps_lib, solver):
+    """Warm start 2 p_n - p_{n-1}: the same system solved from it reaches the tolerance in
+    fewer iterations than from p_n, and the two solutions agree to the tolerance."""
+    from polymps_gb300 import mps
+    c = CASES["cfg3_3d_inc_polygon"]()
+    g = mps.MpsGpu(c, solver=solver, tol=1e-10, precision=abi.PRECISION_DF32)
+    g.initialize()
+    g.run(8)
+    for op in step_ops(g.params)[: step_ops(g.params).index("CALC_PRESS")]:
+        g.run_op(op)
+    pn, pp = g.get(abi.F_PRESSPPE), g.get(abi.F_PRESSPPE_PREV)
+    out = {}
+    for warm in (abi.WARM_PREVIOUS, abi.WARM_EXTRAP):
+        g.set(abi.F_PRESSPPE, pn)
+        g.set(abi.F_PRESSPPE_PREV, pp)
+        g.set_solver(solver, warm, 1e-10, 20000)
+        g.run_op("CALC_PRESS")
+        st = g.last_stats()
+        assert st.ppeRelResidual <= 1e-10
+        out[warm] = (g.get(abi.F_PRESSPPE), st.ppeIterations, st.ppeInitialRelResidual)
+    assert out[abi.WARM_EXTRAP][2] < out[abi.WARM_PREVIOUS][2]
+    assert out[abi.WARM_EXTRAP][1] <= out[abi.WARM_PREVIOUS][1]
+    assert relerr(out[abi.WARM_EXTRAP][0], out[abi.WARM_PREVIOUS][0]) < 1e-7
+    g.close()

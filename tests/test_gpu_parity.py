@@ -256,7 +256,7 @@ def _mlp_ref(params, norm, feat, want_grad=False, target=None):
     W4 = params[o:o + H]; o += H
     b4 = params[o]
     g = lambda z: 0.5 * z * (1 + erf(z / np.sqrt(2)))
-    x = _bf16((feat - norm[:16]) * norm[16:]).astype(np.float64)
+    x = _bf16((feat - norm[:16]) * norm[16:32]).astype(np.float64)
     z1 = x @ _bf16(W1).T.astype(np.float64) + b1
     h1 = _bf16(g(z1))
     z2 = h1 @ _bf16(W2).T.astype(np.float64) + b2
@@ -273,7 +273,7 @@ def test_mlp_forward_matches_cpu(mps_lib, seed):
     c = cases.config(3, scale=8.0)
     g = mps.MpsGpu(c)
     params = (rng.normal(size=abi.MLP_NPARAM) * 0.2).astype(np.float32)
-    norm = np.concatenate([rng.normal(size=16), 0.5 + rng.random(16)]).astype(np.float32)
+    norm = np.concatenate([rng.normal(size=16), 0.5 + rng.random(16), [0.0, 1.0]]).astype(np.float32)
     g.mlp_set_weights(params, norm)
     feat = rng.normal(size=(1000, 16)).astype(np.float32)
     out = g.mlp_forward(feat)
@@ -328,7 +328,7 @@ def test_mlp_gradient_matches_cpu(mps_lib):
     c = cases.config(3, scale=8.0)
     g = mps.MpsGpu(c)
     params = (rng.normal(size=abi.MLP_NPARAM) * 0.3).astype(np.float32)
-    norm = np.concatenate([np.zeros(16), np.ones(16)]).astype(np.float32)
+    norm = np.concatenate([np.zeros(16), np.ones(16), [0.0, 1.0]]).astype(np.float32)
     g.mlp_set_weights(params, norm)
     n = 512
     feat = rng.normal(size=(n, 16)).astype(np.float32)

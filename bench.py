@@ -36,10 +36,11 @@ def args_():
     a.add_argument("--steps", type=int, default=20)
     a.add_argument("--warmup", type=int, default=5)
     a.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    a.add_argument("--solver", default="mixed", choices=["mixed", "plain"])
+    a.add_argument("--solver", default="mixed", choices=["mixed", "plain", "matfree"])
     a.add_argument("--precision", default="df32", choices=["df32", "fp64"],
                    help="neighbour-sweep arithmetic: float-float (df32) or FP64")
-    a.add_argument("--warm", default="auto", choices=["auto", "prev", "mlp"])
+    a.add_argument("--warm", default="auto", choices=["auto", "prev", "mlp", "extrap"],
+                   help="auto: learned if weights are present, else extrapolated")
     a.add_argument("--scale", type=float, default=1.0, help="l0 multiplier (1 = 864k particles)")
     a.add_argument("--e2e-steps", type=int, default=3)
     a.add_argument("--no-cpu-baseline", action="store_true")
@@ -119,11 +120,15 @@ class Clocks:
 # Algorithmic bytes per call of each timed class (each distinct element read or written
 # once; neighbour re-reads assumed cache resident).  N particles, E neighbour entries,
 # Z off-diagonal PPE non-zeros; df = float-float tier (hi/lo FP32 copies, no weight cache).
-def algo_bytes(cls, N, E, Z, mixed, df, st=None):
+def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False):
     if cls == "PPE_SOLVE" and st is not None and st.runPpeSolves:
         # one launch = one whole solve; per call averages of the timed run
         it = st.runPpeIterations / st.runPpeSolves
         rf = st.runPpeRefinements / st.runPpeSolves
+        if mixed and matfree:
+            # inner iteration with the matrix-free operator: neighbour index per entry; mask,
+            # diagonal, own hi/lo position, z, Ap, p per row; update as below
+            return it * (96 * N + 4 * Z) + (rf + 1) * (80 * N + 12 * Z)
         if mixed:
             # inner FP32 iteration: SpMV (valf + col per entry; diag, len, z, Ap, p per row)
             # + update (x_f, p, r_f, Ap, M^-1, z per row); per refinement: FP64 residual
@@ -165,15 +170,17 @@ def run_gb300(a, rank, world, local):
     build.build()
     case = cases.config(3, scale=a.scale)
     N = case.n
-    solver = abi.SOLVER_MIXED if a.solver == "mixed" else abi.SOLVER_PLAIN_FP64
+    solver = {"mixed": abi.SOLVER_MIXED, "plain": abi.SOLVER_PLAIN_FP64, "matfree": abi.SOLVER_MIXED_MATFREE}[a.solver]
     mlp_path = os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz")
     use_mlp = a.warm == "mlp" or (a.warm == "auto" and os.path.exists(mlp_path))
     prec = abi.PRECISION_DF32 if a.precision == "df32" else abi.PRECISION_FP64
     g = mps.MpsGpu(case, solver=solver, tol=1e-8, max_iter=20000, precision=prec)
+    warm = abi.WARM_PREVIOUS if a.warm == "prev" else abi.WARM_EXTRAP
     if use_mlp:
         w = np.load(mlp_path)
         g.mlp_set_weights(w["params"], w["norm"])
-        g.set_solver(solver, abi.WARM_MLP, 1e-8, 20000)
+        warm = abi.WARM_MLP
+    g.set_solver(solver, warm, 1e-8, 20000)
     g.initialize()
     g.run(a.warmup)
     torch.cuda.synchronize()
@@ -199,9 +206,15 @@ def run_gb300(a, rank, world, local):
         torch.distributed.barrier()
     value = N * a.steps * world / dev_s
 
+    # state of the end of the timed run, uploaded every step of the end-to-end section
+    host = {f: g.get(f) for f in (abi.F_POS, abi.F_VEL, abi.F_PRESS, abi.F_PRESSPPE)}
+    # PPE time-to-1e-8 on identical systems: plain FP64 vs mixed vs warm starts (before the
+    # end-to-end section, which re-uploads the state and resets the warm-start history)
+    ppe = None
+    if a.ppe_compare and rank == 0:
+        ppe = ppe_compare(g, abi, use_mlp)
     # e2e through the C ABI with host arrays: upload the state from pinned host memory,
     # step, download the result, every step
-    host = {f: g.get(f) for f in (abi.F_POS, abi.F_VEL, abi.F_PRESS, abi.F_PRESSPPE)}
     h2d = sum(v.nbytes for v in host.values())
     d2h = host[abi.F_POS].nbytes + host[abi.F_VEL].nbytes + host[abi.F_PRESS].nbytes
     torch.cuda.synchronize()
@@ -219,13 +232,13 @@ def run_gb300(a, rank, world, local):
     # dominant class and its roofline
     hbm, hbm_src = peaks()
     E, Z = st.nbrEntries, max(st.ppeNnz - N, 0)
-    mixed = solver == abi.SOLVER_MIXED
+    mixed = solver != abi.SOLVER_PLAIN_FP64
     leaf = {k: v for k, v in prof.items() if k not in ("CALC_PRESS",)}
     dom = max(leaf, key=lambda k: leaf[k][0]) if leaf else None
     roof = None
     if dom:
         ms, calls = leaf[dom]
-        b = algo_bytes(dom, N, E, Z, mixed, prec == abi.PRECISION_DF32, st)
+        b = algo_bytes(dom, N, E, Z, mixed, prec == abi.PRECISION_DF32, st, solver == abi.SOLVER_MIXED_MATFREE)
         if b:
             ach = b / (ms / calls / 1e3) / 1e9
             roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
@@ -233,10 +246,6 @@ def run_gb300(a, rank, world, local):
                     "algo_bytes_per_launch": int(b), "launch_ms": round(ms / calls, 4),
                     "share_of_step": round(ms / st.stepMs, 3)}
 
-    # PPE time-to-1e-8 on identical systems: plain FP64 vs mixed vs learned + mixed
-    ppe = None
-    if a.ppe_compare and rank == 0:
-        ppe = ppe_compare(g, abi, use_mlp)
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": "particle-steps/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(st.stepMs / a.steps, 3),
@@ -245,7 +254,8 @@ def run_gb300(a, rank, world, local):
         "data": "synthetic",
         "config": {"workload": "3D incompressible polygon dam break (cfg3)", "particles": N,
                    "l0": case.params["partDist"], "dt": case.params["timeStep"],
-                   "ppe_tol": 1e-8, "solver": a.solver, "precision": a.precision, "warm_start": "mlp" if use_mlp else "previous",
+                   "ppe_tol": 1e-8, "solver": a.solver, "precision": a.precision,
+                   "warm_start": {abi.WARM_MLP: "learned", abi.WARM_EXTRAP: "extrapolated", abi.WARM_PREVIOUS: "previous"}[warm],
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "working set > L2 (no flush needed)", "wall_s": round(wall, 3)},
         "e2e": {"value": round(e2e, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
@@ -279,7 +289,9 @@ def ppe_compare(g, abi, use_mlp):
     variants = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, True),
                 ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, True),
                 ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, True),
-                ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP, True)]
+                ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP, True),
+                ("matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_PREVIOUS, True),
+                ("extrapolated_matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_EXTRAP, True)]
     if use_mlp:
         variants.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP, True))
     variants += [("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, False),

@@ -175,6 +175,11 @@ enum MpsOp {
  * solves under FP64 iterative refinement (FP64 residual r=b-Ax, FP64 dots). */
 #define MPSGPU_SOLVER_PLAIN_FP64   0
 #define MPSGPU_SOLVER_MIXED        1
+/* MIXED with a matrix-free inner operator: the FP32 off-diagonals are recomputed from the
+ * particle positions in every inner SpMV (coeffPPE w(r_ij), entries marked at assembly)
+ * instead of streamed from the assembled matrix; FP64 residuals use the assembled matrix.
+ * Needs the single-launch PPE solve (mpsgpu_set_ppe_launch). */
+#define MPSGPU_SOLVER_MIXED_MATFREE 2
 #define MPSGPU_WARM_PREVIOUS       0   /* previous-step unclamped pressure (reference)  */
 #define MPSGPU_WARM_MLP            1   /* learned per-particle MLP correction           */
 #define MPSGPU_WARM_ZERO           2

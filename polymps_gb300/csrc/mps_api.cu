@@ -229,9 +229,14 @@ static int calcPress(mpsgpu_t h) {
     double rr = 0, rr0 = 0;
     int maxIt = h->maxIter > 0 ? h->maxIter : 2 * h->N0;
     int e;
-    const bool mixed = h->solver == MPSGPU_SOLVER_MIXED;
+    const bool mixed = h->solver != MPSGPU_SOLVER_PLAIN_FP64;
     h->B.prepared = df32(h) ? 1 : 0;   // the DF32 assembly writes the FP32 copies itself
-    if (h->persistent && (mixed ? h->B.pgridMx : h->B.pgridCg) > 0) {
+    h->B.matfree = h->solver == MPSGPU_SOLVER_MIXED_MATFREE ? 1 : 0;
+    if (h->B.matfree && (!h->persistent || h->B.pgridMf <= 0)) {
+        g_lastError = "matrix-free mixed solver needs the single-launch (cooperative) PPE solve";
+        return MPSGPU_ERR_UNSUPPORTED;
+    }
+    if (h->persistent && (h->B.matfree ? h->B.pgridMf : (mixed ? h->B.pgridMx : h->B.pgridCg)) > 0) {
         e = ppeSolvePersistent(h->d, h->B, mixed ? 1 : 0, h->tol, maxIt, h->s, &iters, &refine, &rr, &rr0, &h->prof);
         if (e == MPSGPU_ERR_CUDA) g_lastError = "persistent PPE solve: launch failed or a grid-barrier wait ran out";
     } else if (mixed) {
@@ -566,10 +571,12 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         B.pgridCg = ppePersistentGrid(0);
         B.pgridMx = ppePersistentGrid(1);
         A(B.scal, 16);
-        A(B.partials, 4 * std::max(B.nblocks, std::max(B.pgridCg, B.pgridMx)));
+        A(B.partials, 4 * std::max(B.nblocks, std::max(B.pgridCg, std::max(B.pgridMx, ppePersistentGrid(2)))));
         A(B.counter, 1);
         A(B.flag, 8);
         A(B.dinv, n);
+        A(B.mfMask, n);
+        B.pgridMf = ppePersistentGrid(2);
         A(B.bar, 96);   // three 128-byte lines of barrier words
     }
 #undef A
@@ -683,7 +690,7 @@ int mpsgpu_set_ppe_launch(mpsgpu_t h, int persistent) {
 }
 
 int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm, double tol, int max_iter) {
-    if (!h || (solver != MPSGPU_SOLVER_PLAIN_FP64 && solver != MPSGPU_SOLVER_MIXED) || warm < 0 || warm > 3 || !(tol > 0))
+    if (!h || (solver != MPSGPU_SOLVER_PLAIN_FP64 && solver != MPSGPU_SOLVER_MIXED && solver != MPSGPU_SOLVER_MIXED_MATFREE) || warm < 0 || warm > 3 || !(tol > 0))
         return MPSGPU_ERR_ARG;
     if (warm == MPSGPU_WARM_MLP && !h->mlp.ready) { g_lastError = "MLP weights not set"; return MPSGPU_ERR_ARG; }
     h->solver = solver; h->warm = warm; h->tol = tol; h->maxIter = max_iter;

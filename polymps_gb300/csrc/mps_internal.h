@@ -93,6 +93,9 @@ struct PpeBuffers {
     unsigned int* bar;       // grid barrier of the persistent solvers: arrivals, generation, abort
     int pgridCg, pgridMx;    // co-resident grid sizes of the persistent solvers (0: unavailable)
     int prepared;            // FP32 copies (valf, diagf, diagInvf) already written by the assembly
+    unsigned long long* mfMask;   // per row: neighbour-list entries that are matrix entries
+    int matfree;             // mixed solver: recompute the FP32 off-diagonals from positions
+    int pgridMf;             // co-resident grid of the matrix-free mixed solver
 };
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);

@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
     const MpsParams& P = d.P;
     int bci = d.bc[i];
     if (bci == P.other || bci == P.surface) {
-        B.diag[i] = 1.0; B.diagf[i] = 1.0f; B.diagInvf[i] = 1.0f; B.rowLen[i] = 0; B.b[i] = 0.0;
+        B.diag[i] = 1.0; B.diagf[i] = 1.0f; B.diagInvf[i] = 1.0f; B.rowLen[i] = 0; B.b[i] = 0.0; B.mfMask[i] = 0ull;
         warpCount(d.counters + 1, 0u);
         return;
     }
@@ -426,7 +426,8 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
     const df gx = K(d.k.g[0]), gy = K(d.k.g[1]), gz = K(d.k.g[2]);
     df sum = dfF(0.f), src = dfF(0.f);
     int len = 0;
-    forMask(d, i, d.maskL[i], [&](int j, size_t) {
+    unsigned long long mm = 0ull;
+    forMask(d, i, d.maskL[i], [&](int j, size_t e) {
         PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
         df wL = weightDF(q.d2, RL, P.weightType).w;
         if (d.type[j] == P.dummyWall) {
@@ -440,9 +441,11 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
                 B.valf[k] = mij.h;   // the FP32 copy of the mixed solver (hi part = fl32)
                 B.col[k] = j;
                 len++;
+                mm |= 1ull << ((e - i) / B.N0);
             }
         }
     });
+    B.mfMask[i] = mm;
     double rho = P.DNS_FL1;
     double dg = dD(sum) - P.alphaCompressibility * rho / (P.timeStep * P.timeStep);
     B.diag[i] = dg;

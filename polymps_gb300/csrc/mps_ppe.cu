@@ -30,13 +30,14 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
     const MpsParams& P = d.P;
     int bci = d.bc[i];
     if (bci == P.other || bci == P.surface) {
-        B.diag[i] = 1.0; B.rowLen[i] = 0; B.b[i] = 0.0;
+        B.diag[i] = 1.0; B.rowLen[i] = 0; B.b[i] = 0.0; B.mfMask[i] = 0ull;
         warpCount(d.counters + 1, 0u);
         return;
     }
     dvec4 pi = d.pos[i];
     double sum = 0.0, src = 0.0;
     int len = 0;
+    unsigned long long mm = 0ull;
     const double* wLc = d.cwL ? d.cwL : d.cw;
     forMask(d, i, d.maskL[i], [&](int j, size_t e) {
         double wL = wLc[e];
@@ -53,6 +54,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
                 B.val[k] = mij;
                 B.col[k] = j;
                 len++;
+                mm |= 1ull << ((e - i) / B.N0);
             }
         }
     });
@@ -60,6 +62,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
     sum -= P.alphaCompressibility * rho / (P.timeStep * P.timeStep);
     B.diag[i] = sum;
     B.rowLen[i] = len;
+    B.mfMask[i] = mm;
     B.b[i] = src + (-P.coeffPPESource * rho * (d.pndSmall[i] - P.pndSmallZero));
     warpCount(d.counters + 1, (unsigned)len);
 }
@@ -591,12 +594,61 @@ __device__ __forceinline__ float qRowF(const PpeBuffers& B, const float* x, int 
     return ellRow<float, false>(B.diagf, B.valf, B.col, x, i, len, B.N0);
 }
 
+// Matrix-free FP32 row of the mixed solver's inner operator: the off-diagonal entries
+// a_ij = coeffPPE w(r_ij; reL) are recomputed from the hi/lo position copies for the list
+// entries that the assembly marked as matrix entries (mfMask), eight neighbours in flight;
+// the diagonal is the assembled one.  Only the 4-byte neighbour indices are streamed.
+__device__ __forceinline__ float mfWeight(float r2, float re, float invRe, int t) {
+    float rinv = rsqrtf(r2);
+    switch (t) {
+        case 1: { float r = r2 * rinv; return re * rinv + r * invRe - 2.0f; }
+        case 2: { float r = r2 * rinv; return re * rinv - r * invRe; }
+        case 3: { float a = 1.0f - r2 * rinv * invRe; return a * a * a; }
+        case 4: { float a = 1.0f - r2 * rinv * invRe; return a * a; }
+        default: return re * rinv - 1.0f;
+    }
+}
+__device__ __forceinline__ float mfRowF(const Dev& d, const PpeBuffers& B, const float* z, int i, float cP, float re,
+                                       float invRe, int wt) {
+    unsigned long long m = __ldg(B.mfMask + i);
+    const float4 hi = __ldg(d.posf + i), li = __ldg(d.posLo + i);
+    const int* row = d.nbr + i;
+    const size_t N0 = d.N0;
+    float acc[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++) acc[u] = 0.f;
+    while (m) {
+        int jj[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            int k = __ffsll((long long)m) - 1;
+            jj[u] = (m != 0ull) ? __ldg(row + (size_t)k * N0) : -1;
+            m &= m - 1ull;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            if (jj[u] < 0) continue;
+            const int j = jj[u];
+            const float4 hj = __ldg(d.posf + j), lj = __ldg(d.posLo + j);
+            float dx = (hj.x - hi.x) + (lj.x - li.x);
+            float dy = (hj.y - hi.y) + (lj.y - li.y);
+            float dz = (hj.z - hi.z) + (lj.z - li.z);
+            float w = mfWeight(dx * dx + dy * dy + dz * dz, re, invRe, wt);
+            acc[u] += (cP * w) * z[j];
+        }
+    }
+    return __ldg(B.diagf + i) * z[i] + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
+}
+
 // Mixed solver: FP64 residual r = b - A x and its norm, FP32 inner CG on r / ||r|| to
 // the relative tolerance eta_k, x += ||r|| d in FP64, repeated until ||r|| < tol ||b||.
 // eta_k = max(eta, tol ||b|| / (2 ||r_k||)): an inner solve stops once its correction
 // brings the outer residual to half the tolerance, so the last one does not over-solve.
+template <bool MF>
 __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
     const int n = liveN(d);
+    const float cP = (float)d.P.coeffPPE, re = (float)d.P.reL, invRe = (float)(1.0 / d.P.reL);
+    const int wt = d.P.weightType;
     const int T = gridDim.x * QB;
     const int t0 = blockIdx.x * QB + threadIdx.x;
     QCtl c = {0u};
@@ -645,7 +697,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                 const float beta = inner ? (float)vd(B.scal + S_BETA) : 0.f;
                 df a[1] = {dfF(0.f)};
                 forRows(B, n, t0, T, [&](int i, int len) {
-                    float q = qRowF(B, B.zf, i, len);
+                    float q = MF ? mfRowF(d, B, B.zf, i, cP, re, invRe, wt) : qRowF(B, B.zf, i, len);
                     float z = B.zf[i];
                     float ap = inner ? q + beta * B.Apf[i] : q;
                     float p = inner ? z + beta * B.pf[i] : z;
@@ -782,14 +834,16 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
     }
 }
 
+// kind: 0 plain FP64, 1 mixed, 2 mixed with the matrix-free inner operator
 int ppePersistentGrid(int kind) {
     int dev = 0, sms = 0, coop = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return 0;
-    cudaError_t e = kind ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve, QB, 0)
-                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_solve, QB, 0);
+    cudaError_t e = kind == 2   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<true>, QB, 0)
+                    : kind == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<false>, QB, 0)
+                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_solve, QB, 0);
     if (e != cudaSuccess || per <= 0) return 0;
     return per * sms;
 }
@@ -816,7 +870,7 @@ static int finishPersistent(const PpeBuffers& B, cudaStream_t s, int* iters, int
 
 int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol, int maxIter, cudaStream_t s,
                        int* iters, int* refinements, double* relres, double* relres0, Prof* prof) {
-    int grid = mixed ? B.pgridMx : B.pgridCg;
+    int grid = mixed ? (B.matfree ? B.pgridMf : B.pgridMx) : B.pgridCg;
     if (grid <= 0) return MPSGPU_ERR_UNSUPPORTED;
     bool pr = prof && prof->on;
     cudaMemsetAsync(B.flag, 0, 5 * sizeof(int), s);
@@ -833,8 +887,9 @@ int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol,
     int mi = maxIter;
     void* args[5] = {&dd, &bb, &t, &mi, &eta2};
     if (pr) prof->begin(PROF_PPE_SOLVE, s);
-    cudaError_t e = mixed ? cudaLaunchCooperativeKernel((const void*)k_mx_solve, grid, QB, args, 0, s)
-                          : cudaLaunchCooperativeKernel((const void*)k_cg_solve, grid, QB, args, 0, s);
+    const void* fn = !mixed ? (const void*)k_cg_solve
+                            : (B.matfree ? (const void*)k_mx_solve<true> : (const void*)k_mx_solve<false>);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, grid, QB, args, 0, s);
     if (pr) prof->end(s);
     if (e != cudaSuccess) return MPSGPU_ERR_CUDA;
     countLaunch(1);

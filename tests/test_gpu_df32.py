@@ -166,3 +166,20 @@ def test_extrapolated_warm_start(oracle_mod, mps_lib, solver):
     assert out[abi.WARM_EXTRAP][1] <= out[abi.WARM_PREVIOUS][1]
     assert relerr(out[abi.WARM_EXTRAP][0], out[abi.WARM_PREVIOUS][0]) < 1e-7
     g.close()
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_DF32])
+def test_matrix_free_mixed_solver(oracle_mod, mps_lib, precision):
+    """The mixed solver with the matrix-free FP32 inner operator reaches the FP64 residual
+    of the assembled system and agrees with the plain FP64 CG within 1e-6."""
+    from polymps_gb300 import mps
+    c = CASES["cfg3_3d_inc_polygon"]()
+    out = {}
+    for solver in (abi.SOLVER_PLAIN_FP64, abi.SOLVER_MIXED_MATFREE):
+        g = mps.MpsGpu(c, solver=solver, tol=1e-10, precision=precision)
+        g.initialize()
+        st = g.run(4)
+        assert st.ppeRelResidual <= 1e-10
+        out[solver] = g.get(abi.F_PRESS)
+        g.close()
+    assert relerr(out[abi.SOLVER_MIXED_MATFREE], out[abi.SOLVER_PLAIN_FP64]) < 1e-6

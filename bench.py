@@ -36,7 +36,7 @@ def args_():
     a.add_argument("--steps", type=int, default=20)
     a.add_argument("--warmup", type=int, default=5)
     a.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    a.add_argument("--solver", default="mixed", choices=["mixed", "plain", "matfree"])
+    a.add_argument("--solver", default="mixed", choices=["mixed", "plain", "matfree", "compact"])
     a.add_argument("--precision", default="df32", choices=["df32", "fp64"],
                    help="neighbour-sweep arithmetic: float-float (df32) or FP64")
     a.add_argument("--warm", default="auto", choices=["auto", "prev", "mlp", "extrap"],
@@ -120,11 +120,16 @@ class Clocks:
 # Algorithmic bytes per call of each timed class (each distinct element read or written
 # once; neighbour re-reads assumed cache resident).  N particles, E neighbour entries,
 # Z off-diagonal PPE non-zeros; df = float-float tier (hi/lo FP32 copies, no weight cache).
-def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False):
+def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False, compact=False):
     if cls == "PPE_SOLVE" and st is not None and st.runPpeSolves:
         # one launch = one whole solve; per call averages of the timed run
         it = st.runPpeIterations / st.runPpeSolves
         rf = st.runPpeRefinements / st.runPpeSolves
+        if mixed and compact:
+            # compact inner iteration: FP16 value + 16-bit offset per entry; wide flag, y, Ap,
+            # p per row; update (x_f, p, r_f, Ap, z); once per solve the compact copy (FP32
+            # value + column read, FP16 value + offset written) and the scaling
+            return it * (49 * N + 4 * Z) + (rf + 1) * (84 * N + 12 * Z) + 12 * Z + 17 * N
         if mixed and matfree:
             # inner iteration with the matrix-free operator: neighbour index per entry; mask,
             # diagonal, own hi/lo position, z, Ap, p per row; update as below
@@ -170,7 +175,8 @@ def run_gb300(a, rank, world, local):
     build.build()
     case = cases.config(3, scale=a.scale)
     N = case.n
-    solver = {"mixed": abi.SOLVER_MIXED, "plain": abi.SOLVER_PLAIN_FP64, "matfree": abi.SOLVER_MIXED_MATFREE}[a.solver]
+    solver = {"mixed": abi.SOLVER_MIXED, "plain": abi.SOLVER_PLAIN_FP64, "matfree": abi.SOLVER_MIXED_MATFREE,
+              "compact": abi.SOLVER_MIXED_COMPACT}[a.solver]
     mlp_path = os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz")
     use_mlp = a.warm == "mlp" or (a.warm == "auto" and os.path.exists(mlp_path))
     prec = abi.PRECISION_DF32 if a.precision == "df32" else abi.PRECISION_FP64
@@ -238,7 +244,8 @@ def run_gb300(a, rank, world, local):
     roof = None
     if dom:
         ms, calls = leaf[dom]
-        b = algo_bytes(dom, N, E, Z, mixed, prec == abi.PRECISION_DF32, st, solver == abi.SOLVER_MIXED_MATFREE)
+        b = algo_bytes(dom, N, E, Z, mixed, prec == abi.PRECISION_DF32, st, solver == abi.SOLVER_MIXED_MATFREE,
+                       solver == abi.SOLVER_MIXED_COMPACT)
         if b:
             ach = b / (ms / calls / 1e3) / 1e9
             roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
@@ -291,7 +298,8 @@ def ppe_compare(g, abi, use_mlp):
                 ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, True),
                 ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP, True),
                 ("matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_PREVIOUS, True),
-                ("extrapolated_matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_EXTRAP, True)]
+                ("compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_PREVIOUS, True),
+                ("extrapolated_compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_EXTRAP, True)]
     if use_mlp:
         variants.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP, True))
     variants += [("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, False),

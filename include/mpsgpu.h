@@ -180,6 +180,11 @@ enum MpsOp {
  * instead of streamed from the assembled matrix; FP64 residuals use the assembled matrix.
  * Needs the single-launch PPE solve (mpsgpu_set_ppe_launch). */
 #define MPSGPU_SOLVER_MIXED_MATFREE 2
+/* MIXED with a compact inner operator: the FP32 inner CG runs on the symmetrically scaled
+ * matrix diag(sign(A_ii)/sqrt|A_ii|) A diag(1/sqrt|A_ii|) (unit diagonal, no
+ * preconditioner), stored as FP16 values with 16-bit column offsets (4 bytes per entry);
+ * FP64 residuals use the assembled FP64 matrix.  Needs the single-launch PPE solve. */
+#define MPSGPU_SOLVER_MIXED_COMPACT 3
 #define MPSGPU_WARM_PREVIOUS       0   /* previous-step unclamped pressure (reference)  */
 #define MPSGPU_WARM_MLP            1   /* learned per-particle MLP correction           */
 #define MPSGPU_WARM_ZERO           2

@@ -131,7 +131,7 @@ OPS = [
 ]
 OP = {name: k for k, name in enumerate(OPS)}
 
-SOLVER_PLAIN_FP64, SOLVER_MIXED, SOLVER_MIXED_MATFREE = 0, 1, 2
+SOLVER_PLAIN_FP64, SOLVER_MIXED, SOLVER_MIXED_MATFREE, SOLVER_MIXED_COMPACT = 0, 1, 2, 3
 WARM_PREVIOUS, WARM_MLP, WARM_ZERO, WARM_EXTRAP = 0, 1, 2, 3
 PRECISION_FP64, PRECISION_DF32 = 0, 1
 MLP_NPARAM = 64 * 16 + 64 + 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1

@@ -231,12 +231,13 @@ static int calcPress(mpsgpu_t h) {
     int e;
     const bool mixed = h->solver != MPSGPU_SOLVER_PLAIN_FP64;
     h->B.prepared = df32(h) ? 1 : 0;   // the DF32 assembly writes the FP32 copies itself
-    h->B.matfree = h->solver == MPSGPU_SOLVER_MIXED_MATFREE ? 1 : 0;
-    if (h->B.matfree && (!h->persistent || h->B.pgridMf <= 0)) {
-        g_lastError = "matrix-free mixed solver needs the single-launch (cooperative) PPE solve";
+    h->B.matfree = h->solver == MPSGPU_SOLVER_MIXED_MATFREE ? 1 : (h->solver == MPSGPU_SOLVER_MIXED_COMPACT ? 2 : 0);
+    int pgrid = !mixed ? h->B.pgridCg : (h->B.matfree == 2 ? h->B.pgridH16 : (h->B.matfree ? h->B.pgridMf : h->B.pgridMx));
+    if (h->B.matfree && (!h->persistent || pgrid <= 0)) {
+        g_lastError = "this mixed inner operator needs the single-launch (cooperative) PPE solve";
         return MPSGPU_ERR_UNSUPPORTED;
     }
-    if (h->persistent && (h->B.matfree ? h->B.pgridMf : (mixed ? h->B.pgridMx : h->B.pgridCg)) > 0) {
+    if (h->persistent && pgrid > 0) {
         e = ppeSolvePersistent(h->d, h->B, mixed ? 1 : 0, h->tol, maxIt, h->s, &iters, &refine, &rr, &rr0, &h->prof);
         if (e == MPSGPU_ERR_CUDA) g_lastError = "persistent PPE solve: launch failed or a grid-barrier wait ran out";
     } else if (mixed) {
@@ -571,12 +572,19 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         B.pgridCg = ppePersistentGrid(0);
         B.pgridMx = ppePersistentGrid(1);
         A(B.scal, 16);
-        A(B.partials, 4 * std::max(B.nblocks, std::max(B.pgridCg, std::max(B.pgridMx, ppePersistentGrid(2)))));
+        A(B.partials, 4 * std::max(std::max(B.nblocks, ppePersistentGrid(3)),
+                                   std::max(B.pgridCg, std::max(B.pgridMx, ppePersistentGrid(2)))));
         A(B.counter, 1);
         A(B.flag, 8);
         A(B.dinv, n);
         A(B.mfMask, n);
         B.pgridMf = ppePersistentGrid(2);
+        B.pgridH16 = ppePersistentGrid(3);
+        A(B.valh, (size_t)d.K * n);
+        A(B.col16, (size_t)d.K * n);
+        A(B.sclf, n);
+        A(B.sgs, n);
+        A(B.wideRow, n);
         A(B.bar, 96);   // three 128-byte lines of barrier words
     }
 #undef A
@@ -690,7 +698,8 @@ int mpsgpu_set_ppe_launch(mpsgpu_t h, int persistent) {
 }
 
 int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm, double tol, int max_iter) {
-    if (!h || (solver != MPSGPU_SOLVER_PLAIN_FP64 && solver != MPSGPU_SOLVER_MIXED && solver != MPSGPU_SOLVER_MIXED_MATFREE) || warm < 0 || warm > 3 || !(tol > 0))
+    if (!h || (solver != MPSGPU_SOLVER_PLAIN_FP64 && solver != MPSGPU_SOLVER_MIXED && solver != MPSGPU_SOLVER_MIXED_MATFREE &&
+               solver != MPSGPU_SOLVER_MIXED_COMPACT) || warm < 0 || warm > 3 || !(tol > 0))
         return MPSGPU_ERR_ARG;
     if (warm == MPSGPU_WARM_MLP && !h->mlp.ready) { g_lastError = "MLP weights not set"; return MPSGPU_ERR_ARG; }
     h->solver = solver; h->warm = warm; h->tol = tol; h->maxIter = max_iter;

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <vector>
+#include <cuda_fp16.h>
 #include "mps_common.cuh"
 
 // Kernel-launch counter (all launches of this library, process-wide).
@@ -94,8 +95,13 @@ struct PpeBuffers {
     int pgridCg, pgridMx;    // co-resident grid sizes of the persistent solvers (0: unavailable)
     int prepared;            // FP32 copies (valf, diagf, diagInvf) already written by the assembly
     unsigned long long* mfMask;   // per row: neighbour-list entries that are matrix entries
-    int matfree;             // mixed solver: recompute the FP32 off-diagonals from positions
+    int matfree;             // mixed inner operator: 0 assembled FP32, 1 matrix-free, 2 compact scaled
     int pgridMf;             // co-resident grid of the matrix-free mixed solver
+    __half* valh;            // compact scaled operator: FP16 off-diagonals of diag(sigma s) A diag(s)
+    short* col16;            // and their column offsets j - i
+    float *sclf, *sgs;       // s_i = 1/sqrt|A_ii| and sigma_i s_i
+    unsigned char* wideRow;  // rows with an offset outside 16 bits (read the 32-bit columns)
+    int pgridH16;
 };
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);

@@ -21,7 +21,7 @@
 #define PBLK 256
 
 // solver scalars in B.scal[]
-enum { S_RZ = 0, S_RR, S_BB, S_ALPHA, S_BETA, S_PAP, S_THR, S_RZNEW, S_SCALE, S_INV, S_SQRT, S_ETA2, S_COUNT };
+enum { S_RZ = 0, S_RR, S_BB, S_ALPHA, S_BETA, S_PAP, S_THR, S_RZNEW, S_SCALE, S_INV, S_SQRT, S_ETA2, S_RR0, S_COUNT };
 
 // ------------------------------------------------------------------ assembly
 __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
@@ -640,11 +640,65 @@ __device__ __forceinline__ float mfRowF(const Dev& d, const PpeBuffers& B, const
     return __ldg(B.diagf + i) * z[i] + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
 }
 
+// Compact inner operator: with s_i = 1/sqrt|A_ii| and sigma_i = sign(A_ii), the system
+// A d = r is M y = c with M = diag(sigma s) A diag(s), c_i = sigma_i s_i r_i, d = s y.  M is
+// symmetric (coupled rows are all equation rows, sigma = -1), has a unit diagonal and
+// off-diagonals in (-1, 0): they are stored in FP16 (FP32 arithmetic), the columns as
+// 16-bit offsets j - i (rows with a farther neighbour keep the 32-bit columns), 4 bytes
+// per entry instead of 8, and CG on M needs no preconditioner.
+__device__ __forceinline__ float h16Row(const PpeBuffers& B, const float* y, int i, int len) {
+    const size_t N0 = B.N0;
+    const __half* v = B.valh + i;
+    float acc[ELL_U];
+#pragma unroll
+    for (int u = 0; u < ELL_U; u++) acc[u] = 0.f;
+    if (!__ldg(B.wideRow + i)) {
+        const short* c = B.col16 + i;
+        for (int k = 0; k < len; k += ELL_U) {
+            if (k + ELL_U < len) {
+#pragma unroll
+                for (int u = 0; u < ELL_U; u += 2) {
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(c + (size_t)(k + ELL_U + u) * N0));
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(v + (size_t)(k + ELL_U + u) * N0));
+                }
+            }
+            int cc[ELL_U];
+            float vv[ELL_U];
+#pragma unroll
+            for (int u = 0; u < ELL_U; u++) {
+                bool ok = k + u < len;
+                cc[u] = ok ? i + (int)__ldg(c + (size_t)(k + u) * N0) : i;
+                vv[u] = ok ? __half2float(__ldg(v + (size_t)(k + u) * N0)) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < ELL_U; u++) acc[u] += vv[u] * y[cc[u]];
+        }
+    } else {
+        const int* c = B.col + i;
+        for (int k = 0; k < len; k += ELL_U) {
+            int cc[ELL_U];
+            float vv[ELL_U];
+#pragma unroll
+            for (int u = 0; u < ELL_U; u++) {
+                bool ok = k + u < len;
+                cc[u] = ok ? __ldg(c + (size_t)(k + u) * N0) : i;
+                vv[u] = ok ? __half2float(__ldg(v + (size_t)(k + u) * N0)) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < ELL_U; u++) acc[u] += vv[u] * y[cc[u]];
+        }
+    }
+    return y[i] + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
+}
+
 // Mixed solver: FP64 residual r = b - A x and its norm, FP32 inner CG on r / ||r|| to
 // the relative tolerance eta_k, x += ||r|| d in FP64, repeated until ||r|| < tol ||b||.
 // eta_k = max(eta, tol ||b|| / (2 ||r_k||)): an inner solve stops once its correction
 // brings the outer residual to half the tolerance, so the last one does not over-solve.
-template <bool MF>
+// Inner operator of k_mx_solve: the assembled FP32 ELL matrix with Jacobi preconditioning,
+// the matrix-free FP32 operator with Jacobi preconditioning, or the compact scaled operator.
+enum { OP_ELL32 = 0, OP_MATFREE = 1, OP_H16 = 2 };
+template <int OP>
 __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
     const int n = liveN(d);
     const float cP = (float)d.P.coeffPPE, re = (float)d.P.reL, invRe = (float)(1.0 / d.P.reL);
@@ -652,6 +706,30 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
     const int T = gridDim.x * QB;
     const int t0 = blockIdx.x * QB + threadIdx.x;
     QCtl c = {0u};
+    if (OP == OP_H16) {
+        // scaling, then the compact copy of the FP32 matrix
+        for (int i = t0; i < n; i += T) {
+            double dd = __ldg(B.diag + i);
+            double sc = 1.0 / sqrt(fabs(dd));
+            B.sclf[i] = (float)sc;
+            B.sgs[i] = (float)(dd < 0.0 ? -sc : sc);
+        }
+        if (!qBarrier(B, c)) return;
+        forRows(B, n, t0, T, [&](int i, int len) {
+            const float si = B.sgs[i];
+            unsigned char wide = 0;
+            for (int k = 0; k < len; k++) {
+                size_t e = (size_t)k * B.N0 + i;
+                int j = __ldg(B.col + e);
+                B.valh[e] = __float2half_rn(si * __ldg(B.valf + e) * B.sclf[j]);
+                int off = j - i;
+                if (off < -32768 || off > 32767) wide = 1;
+                B.col16[e] = (short)off;
+            }
+            B.wideRow[i] = wide;
+        });
+        if (!qBarrier(B, c)) return;
+    }
     {
         double v[2] = {0.0, 0.0};
         forRows(B, n, t0, T, [&](int i, int len) {
@@ -679,17 +757,20 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
     }
     int total = 0, refine = 0;
     while (!vi(B.flag) && total < maxIter && refine <= 20) {
-        // inner start: rf = r / ||r||, z = M rf, x_f = 0
+        // inner start: rf = r / ||r|| (compact operator: sigma s r / ||r||), z = M^-1 rf, x_f = 0
         {
             const double inv = vd(B.scal + S_INV);
-            df a[1] = {dfF(0.f)};
+            df a[2] = {dfF(0.f), dfF(0.f)};
             for (int i = t0; i < n; i += T) {
                 float r = (float)(B.r[i] * inv);
-                float z = r * __ldg(B.diagInvf + i);
+                if (OP == OP_H16) r *= B.sgs[i];
+                float z = (OP == OP_H16) ? r : r * __ldg(B.diagInvf + i);
                 B.rf[i] = r; B.zf[i] = z; B.xf[i] = 0.f;
                 a[0] += prod2(r, z);
+                a[1] += prod2(r, r);
             }
-            if (!qSumDF<1>(a, B, c, [&](const double* t) { B.scal[S_RZ] = t[0]; B.flag[3] = 0; })) return;
+            if (!qSumDF<2>(a, B, c, [&](const double* t) { B.scal[S_RZ] = t[0]; B.scal[S_RR0] = t[1]; B.flag[3] = 0; }))
+                return;
         }
         int inner = 0;
         while (true) {
@@ -697,7 +778,9 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                 const float beta = inner ? (float)vd(B.scal + S_BETA) : 0.f;
                 df a[1] = {dfF(0.f)};
                 forRows(B, n, t0, T, [&](int i, int len) {
-                    float q = MF ? mfRowF(d, B, B.zf, i, cP, re, invRe, wt) : qRowF(B, B.zf, i, len);
+                    float q = (OP == OP_MATFREE) ? mfRowF(d, B, B.zf, i, cP, re, invRe, wt)
+                            : (OP == OP_H16)   ? h16Row(B, B.zf, i, len)
+                                               : qRowF(B, B.zf, i, len);
                     float z = B.zf[i];
                     float ap = inner ? q + beta * B.Apf[i] : q;
                     float p = inner ? z + beta * B.pf[i] : z;
@@ -713,7 +796,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                 for (int i = t0; i < n; i += T) {
                     B.xf[i] += alpha * B.pf[i];
                     float r = B.rf[i] - alpha * B.Apf[i];
-                    float z = r * __ldg(B.diagInvf + i);
+                    float z = (OP == OP_H16) ? r : r * __ldg(B.diagInvf + i);
                     B.rf[i] = r; B.zf[i] = z;
                     a[0] += prod2(r, z);
                     a[1] += prod2(r, r);
@@ -722,7 +805,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                         B.flag[1] += 1;
                         B.scal[S_BETA] = t[0] / B.scal[S_RZ];
                         B.scal[S_RZ] = t[0];
-                        if (t[1] < B.scal[S_ETA2] || !(t[1] == t[1])) B.flag[3] = 1;
+                        if (t[1] < B.scal[S_ETA2] * B.scal[S_RR0] || !(t[1] == t[1])) B.flag[3] = 1;
                     }))
                     return;
             }
@@ -732,7 +815,8 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
         total += inner;
         {
             const double sc = vd(B.scal + S_SQRT);
-            for (int i = t0; i < n; i += T) B.x[i] += sc * (double)B.xf[i];
+            for (int i = t0; i < n; i += T)
+                B.x[i] += sc * (double)((OP == OP_H16) ? B.xf[i] * B.sclf[i] : B.xf[i]);
             if (!qBarrier(B, c)) return;
         }
         {
@@ -834,15 +918,17 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
     }
 }
 
-// kind: 0 plain FP64, 1 mixed, 2 mixed with the matrix-free inner operator
+// kind: 0 plain FP64, 1 mixed, 2 mixed with the matrix-free inner operator, 3 mixed with
+// the compact scaled inner operator
 int ppePersistentGrid(int kind) {
     int dev = 0, sms = 0, coop = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return 0;
-    cudaError_t e = kind == 2   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<true>, QB, 0)
-                    : kind == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<false>, QB, 0)
+    cudaError_t e = kind == 3   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_H16>, QB, 0)
+                    : kind == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_MATFREE>, QB, 0)
+                    : kind == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_ELL32>, QB, 0)
                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_solve, QB, 0);
     if (e != cudaSuccess || per <= 0) return 0;
     return per * sms;
@@ -870,7 +956,7 @@ static int finishPersistent(const PpeBuffers& B, cudaStream_t s, int* iters, int
 
 int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol, int maxIter, cudaStream_t s,
                        int* iters, int* refinements, double* relres, double* relres0, Prof* prof) {
-    int grid = mixed ? (B.matfree ? B.pgridMf : B.pgridMx) : B.pgridCg;
+    int grid = !mixed ? B.pgridCg : (B.matfree == 2 ? B.pgridH16 : (B.matfree ? B.pgridMf : B.pgridMx));
     if (grid <= 0) return MPSGPU_ERR_UNSUPPORTED;
     bool pr = prof && prof->on;
     cudaMemsetAsync(B.flag, 0, 5 * sizeof(int), s);
@@ -887,8 +973,10 @@ int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol,
     int mi = maxIter;
     void* args[5] = {&dd, &bb, &t, &mi, &eta2};
     if (pr) prof->begin(PROF_PPE_SOLVE, s);
-    const void* fn = !mixed ? (const void*)k_cg_solve
-                            : (B.matfree ? (const void*)k_mx_solve<true> : (const void*)k_mx_solve<false>);
+    const void* fn = !mixed              ? (const void*)k_cg_solve
+                     : B.matfree == 2    ? (const void*)k_mx_solve<OP_H16>
+                     : B.matfree == 1    ? (const void*)k_mx_solve<OP_MATFREE>
+                                         : (const void*)k_mx_solve<OP_ELL32>;
     cudaError_t e = cudaLaunchCooperativeKernel(fn, grid, QB, args, 0, s);
     if (pr) prof->end(s);
     if (e != cudaSuccess) return MPSGPU_ERR_CUDA;

@@ -169,17 +169,19 @@ def test_extrapolated_warm_start(oracle_mod, mps_lib, solver):
 
 
 @pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_DF32])
-def test_matrix_free_mixed_solver(oracle_mod, mps_lib, precision):
-    """The mixed solver with the matrix-free FP32 inner operator reaches the FP64 residual
-    of the assembled system and agrees with the plain FP64 CG within 1e-6."""
+@pytest.mark.parametrize("inner", [abi.SOLVER_MIXED_MATFREE, abi.SOLVER_MIXED_COMPACT])
+def test_mixed_inner_operators(oracle_mod, mps_lib, precision, inner):
+    """The mixed solver with the matrix-free FP32 or the compact FP16-stored inner operator
+    reaches the FP64 residual of the assembled system and agrees with the plain FP64 CG
+    within 1e-6."""
     from polymps_gb300 import mps
     c = CASES["cfg3_3d_inc_polygon"]()
     out = {}
-    for solver in (abi.SOLVER_PLAIN_FP64, abi.SOLVER_MIXED_MATFREE):
+    for solver in (abi.SOLVER_PLAIN_FP64, inner):
         g = mps.MpsGpu(c, solver=solver, tol=1e-10, precision=precision)
         g.initialize()
         st = g.run(4)
         assert st.ppeRelResidual <= 1e-10
         out[solver] = g.get(abi.F_PRESS)
         g.close()
-    assert relerr(out[abi.SOLVER_MIXED_MATFREE], out[abi.SOLVER_PLAIN_FP64]) < 1e-6
+    assert relerr(out[inner], out[abi.SOLVER_PLAIN_FP64]) < 1e-6

@@ -46,6 +46,8 @@ def args_():
     a.add_argument("--no-cpu-baseline", action="store_true")
     a.add_argument("--cpu-steps", type=int, default=1)
     a.add_argument("--ppe-compare", type=int, default=1)
+    a.add_argument("--presort", action="store_true",
+                   help="number the input particles in bucket order (input renumbering only)")
     return a.parse_args()
 
 
@@ -175,6 +177,12 @@ def run_gb300(a, rank, world, local):
     build.build()
     case = cases.config(3, scale=a.scale)
     N = case.n
+    if a.presort:
+        p0 = mps.derive(case.mps_params(), case.n, case.pos)
+        b = np.floor((case.pos - np.array(p0.domainMin[:3])) / p0.bucketSide).astype(np.int64)
+        key = (b[:, 2] * p0.numBucketsY + b[:, 1]) * p0.numBucketsX + b[:, 0]
+        perm = np.argsort(key, kind="stable")
+        case = cases.Case(case.name, case.params, case.type[perm], case.pos[perm], case.mesh)
     solver = {"mixed": abi.SOLVER_MIXED, "plain": abi.SOLVER_PLAIN_FP64, "matfree": abi.SOLVER_MIXED_MATFREE,
               "compact": abi.SOLVER_MIXED_COMPACT}[a.solver]
     mlp_path = os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz")

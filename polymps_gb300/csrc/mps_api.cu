@@ -26,6 +26,10 @@ struct mpsgpu_s {
     int* scanScratch = nullptr;
     int* outFlags = nullptr;
     int* outCounter = nullptr;
+    int* perm = nullptr;          // storage renumbering: permutation and gather scratch
+    void* permScratch = nullptr;
+    int renumberEvery = 20;       // bucket rebuilds between storage renumberings (0: never)
+    int renumberCountdown = 0;    // 0: renumber at the next bucket rebuild
     // solver controls
     int solver = MPSGPU_SOLVER_PLAIN_FP64, warm = MPSGPU_WARM_PREVIOUS;
     double tol = 1e-8;
@@ -93,7 +97,7 @@ void Prof::destroy() {
 // Kernels launched by one operator (fixed by the configuration; the solvers count theirs).
 static int opLaunches(int op, const MpsParams& P, bool x) {
     switch (op) {
-        case MPS_OP_UPDATE_BUCKETS: return 7;   // key, 3 scan, scatter, sort, bucket-ordered copy
+        case MPS_OP_UPDATE_BUCKETS: return 8;   // key, 3 scan, scatter, sort, list positions, bucket-ordered copy
         case MPS_OP_VISCOSITY: return x ? 3 : 1;   // (DF32: velocity copy) + sweep (+ unlisted particles)
         case MPS_OP_OUT_OF_DOMAIN: return 2;
         case MPS_OP_COLLISION: return x ? 3 : 2;
@@ -288,7 +292,14 @@ static int runOpBody(mpsgpu_t h, int op) {
     auto invalidate = [&]() { h->listValid = false; h->masksValid = false; h->cacheValid = false; };
     const bool x = df32(h);
     switch (op) {
-        case MPS_OP_UPDATE_BUCKETS: launchBuckets(d, h->scanScratch, s); invalidate(); break;
+        case MPS_OP_UPDATE_BUCKETS: {
+            bool rn = h->renumberEvery > 0 && h->renumberCountdown <= 0;
+            launchBuckets(d, h->scanScratch, s, rn ? h->perm : nullptr, h->permScratch);
+            if (rn) { h->renumberCountdown = h->renumberEvery; countLaunch(renumberLaunches()); }
+            h->renumberCountdown--;
+            invalidate();
+            break;
+        }
         case MPS_OP_VISCOSITY: if (x) launchViscosityDF(d, s); else launchViscosity(d, s); break;
         case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
         case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
@@ -373,6 +384,32 @@ static int finishStats(mpsgpu_t h, MpsStepStats* st, float stepMs) {
     h->last.stepMs = stepMs;
     if (st) *st = h->last;
     return 0;
+}
+
+// Field transfers are in reference order; storage is in bucket order (mps_common.cuh).
+template <class T>
+__global__ void k_to_ref(const T* src, T* dst, const int* slotOf, int n) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) dst[r] = src[slotOf[r]];
+}
+template <class T>
+__global__ void k_from_ref(const T* src, T* dst, const int* slotOf, int n) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) dst[slotOf[r]] = src[r];
+}
+static void toRef(mpsgpu_t h, int kind, const void* p, int n) {
+    void* sc = h->permScratch;
+    if (kind == 0) k_to_ref<dvec4><<<gridFor(n, 256), 256, 0, h->s>>>((const dvec4*)p, (dvec4*)sc, h->d.slotOf, n);
+    else if (kind == 1) k_to_ref<double><<<gridFor(n, 256), 256, 0, h->s>>>((const double*)p, (double*)sc, h->d.slotOf, n);
+    else k_to_ref<int><<<gridFor(n, 256), 256, 0, h->s>>>((const int*)p, (int*)sc, h->d.slotOf, n);
+    countLaunch(1);
+}
+static void fromRef(mpsgpu_t h, int kind, void* p, int n) {
+    const void* sc = h->permScratch;
+    if (kind == 0) k_from_ref<dvec4><<<gridFor(n, 256), 256, 0, h->s>>>((const dvec4*)sc, (dvec4*)p, h->d.slotOf, n);
+    else if (kind == 1) k_from_ref<double><<<gridFor(n, 256), 256, 0, h->s>>>((const double*)sc, (double*)p, h->d.slotOf, n);
+    else k_from_ref<int><<<gridFor(n, 256), 256, 0, h->s>>>((const int*)sc, (int*)p, h->d.slotOf, n);
+    countLaunch(1);
 }
 
 extern "C" {
@@ -462,9 +499,18 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.posf, n);
     A(d.pressPPEprev, n);
     A(d.cellOf, n);
-    A(d.cellStart, d.nB + 1);
-    A(d.cellCount, d.nB + 1);
-    A(d.cellCursor, d.nB + 1);
+    A(d.cellStart, d.nB + 2);
+    A(d.cellCount, d.nB + 2);
+    A(d.cellCursor, d.nB + 2);
+    A(d.orig, n);
+    A(d.slotOf, n);
+    A(d.cellPos, n);
+    A(h->perm, n);
+    {
+        double* sc = nullptr;   // 32 bytes per particle: the widest per-particle element
+        A(sc, (size_t)4 * n);
+        h->permScratch = sc;
+    }
     A(d.cellSorted, n);
     A(d.posfCell, n);
     A(d.posLo, n);
@@ -485,7 +531,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.velMax, 1);
     A(d.err, 1);
     A(d.counters, 4);
-    A(h->scanScratch, scanScratchInts(std::max(d.nB, n)));
+    A(h->scanScratch, scanScratchInts(std::max(d.nB + 1, n)));
     A(h->outFlags, n);
     A(h->outCounter, 1);
     // FP32 prefilter band (see k_build_nbr): |d2f - d2| <= 3.47 delta re + 3 delta^2 + 3.1 u re^2
@@ -603,6 +649,12 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     std::vector<double> big(n, 10e8 * p->partDist);
     cudaMemcpy(d.riw2, big.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
     cudaMemcpy(d.nLive, &n, sizeof(int), cudaMemcpyHostToDevice);
+    {
+        std::vector<int> id(n);
+        for (int i = 0; i < n; i++) id[i] = i;   // storage starts in reference order
+        cudaMemcpy(d.orig, id.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+        cudaMemcpy(d.slotOf, id.data(), sizeof(int) * n, cudaMemcpyHostToDevice);
+    }
     if (cudaDeviceSynchronize() != cudaSuccess || launchStatus()) { mpsgpu_destroy(h); return MPSGPU_ERR_CUDA; }
     h->maxIter = 0;
     if (cudaMallocHost(&h->pinned, sizeof(dvec4) * (size_t)n) != cudaSuccess) { mpsgpu_destroy(h); return MPSGPU_ERR_NOMEM; }
@@ -784,15 +836,16 @@ int mpsgpu_get_field(mpsgpu_t h, int f, void* host) {
     int n = 0;
     int e = mpsgpu_num_particles(h, &n);
     if (e) return e;
+    toRef(h, kind, p, n);
     if (kind == 0) {
         dvec4* v = (dvec4*)h->pinned;
-        CK(cudaMemcpyAsync(v, p, sizeof(dvec4) * n, cudaMemcpyDeviceToHost, h->s));
+        CK(cudaMemcpyAsync(v, h->permScratch, sizeof(dvec4) * n, cudaMemcpyDeviceToHost, h->s));
         CK(cudaStreamSynchronize(h->s));
         double* o = (double*)host;
         for (int i = 0; i < n; i++) { o[3 * i] = v[i].x; o[3 * i + 1] = v[i].y; o[3 * i + 2] = v[i].z; }
     } else {
         size_t sz = (kind == 1) ? sizeof(double) : sizeof(int);
-        CK(cudaMemcpyAsync(h->pinned, p, sz * n, cudaMemcpyDeviceToHost, h->s));
+        CK(cudaMemcpyAsync(h->pinned, h->permScratch, sz * n, cudaMemcpyDeviceToHost, h->s));
         CK(cudaStreamSynchronize(h->s));
         std::memcpy(host, h->pinned, sz * n);
     }
@@ -817,12 +870,13 @@ int mpsgpu_set_field(mpsgpu_t h, int f, const void* host) {
         dvec4* v = (dvec4*)h->pinned;
         const double* in = (const double*)host;
         for (int i = 0; i < n; i++) v[i] = make_dvec4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0);
-        CK(cudaMemcpyAsync(p, v, sizeof(dvec4) * n, cudaMemcpyHostToDevice, h->s));
+        CK(cudaMemcpyAsync(h->permScratch, v, sizeof(dvec4) * n, cudaMemcpyHostToDevice, h->s));
     } else {
         size_t sz = (kind == 1) ? sizeof(double) : sizeof(int);
         std::memcpy(h->pinned, host, sz * n);
-        CK(cudaMemcpyAsync(p, h->pinned, sz * n, cudaMemcpyHostToDevice, h->s));
+        CK(cudaMemcpyAsync(h->permScratch, h->pinned, sz * n, cudaMemcpyHostToDevice, h->s));
     }
+    fromRef(h, kind, p, n);
     // any state change can alter list membership, masks or the near-wall set
     h->listValid = false;
     h->masksValid = false;
@@ -840,18 +894,25 @@ int mpsgpu_get_neighbors(mpsgpu_t h, int* counts, int* nbr, long long cap) {
     if (e) return e;
     int n = 0;
     if ((e = mpsgpu_num_particles(h, &n))) return e;
-    CK(cudaMemcpyAsync(counts, h->d.nbrCount, sizeof(int) * n, cudaMemcpyDeviceToHost, h->s));
+    // rows and entries in reference indices (storage is in bucket order)
+    std::vector<int> cnt(n), orig(h->N0), slot(h->N0);
+    CK(cudaMemcpyAsync(cnt.data(), h->d.nbrCount, sizeof(int) * n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaMemcpyAsync(orig.data(), h->d.orig, sizeof(int) * h->N0, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaMemcpyAsync(slot.data(), h->d.slotOf, sizeof(int) * h->N0, cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
+    for (int r = 0; r < n; r++) counts[r] = cnt[slot[r]];
     if (!nbr) return 0;
     std::vector<int> ell((size_t)h->d.K * h->N0);
     CK(cudaMemcpyAsync(ell.data(), h->d.nbr, sizeof(int) * ell.size(), cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
     long long k = 0;
-    for (int i = 0; i < n; i++)
-        for (int c = 0; c < counts[i]; c++) {
+    for (int r = 0; r < n; r++) {
+        int i = slot[r];
+        for (int c = 0; c < counts[r]; c++) {
             if (k >= cap) return MPSGPU_ERR_CAPACITY;
-            nbr[k++] = ell[(size_t)c * h->N0 + i];
+            nbr[k++] = orig[ell[(size_t)c * h->N0 + i]];
         }
+    }
     return 0;
 }
 
@@ -861,10 +922,12 @@ int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col, 
     int n = 0;
     int e = mpsgpu_num_particles(h, &n);
     if (e) return e;
-    std::vector<int> len(n);
-    std::vector<double> diag(n);
+    std::vector<int> len(n), orig(h->N0), slot(h->N0);
+    std::vector<double> diag(n), bst(n);
     CK(cudaMemcpyAsync(len.data(), h->B.rowLen, sizeof(int) * n, cudaMemcpyDeviceToHost, h->s));
     CK(cudaMemcpyAsync(diag.data(), h->B.diag, sizeof(double) * n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaMemcpyAsync(orig.data(), h->d.orig, sizeof(int) * h->N0, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaMemcpyAsync(slot.data(), h->d.slotOf, sizeof(int) * h->N0, cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
     long long nnz = n;
     for (int i = 0; i < n; i++) nnz += len[i];
@@ -875,18 +938,20 @@ int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col, 
     std::vector<double> ev(ellN);
     CK(cudaMemcpyAsync(ec.data(), h->B.col, sizeof(int) * ellN, cudaMemcpyDeviceToHost, h->s));
     CK(cudaMemcpyAsync(ev.data(), h->B.val, sizeof(double) * ellN, cudaMemcpyDeviceToHost, h->s));
-    if (rhs) CK(cudaMemcpyAsync(rhs, h->B.b, sizeof(double) * n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaMemcpyAsync(bst.data(), h->B.b, sizeof(double) * n, cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
     long long k = 0;
     rowptr[0] = 0;
     std::vector<std::pair<int, double>> row;
-    for (int i = 0; i < n; i++) {
+    for (int r = 0; r < n; r++) {   // reference rows and columns
+        int i = slot[r];
+        if (rhs) rhs[r] = bst[i];
         row.clear();
-        row.push_back({i, diag[i]});
-        for (int c = 0; c < len[i]; c++) row.push_back({ec[(size_t)c * h->N0 + i], ev[(size_t)c * h->N0 + i]});
+        row.push_back({r, diag[i]});
+        for (int c = 0; c < len[i]; c++) row.push_back({orig[ec[(size_t)c * h->N0 + i]], ev[(size_t)c * h->N0 + i]});
         std::sort(row.begin(), row.end(), [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
         for (auto& pr : row) { col[k] = pr.first; val[k] = pr.second; k++; }
-        rowptr[i + 1] = k;
+        rowptr[r + 1] = k;
     }
     return 0;
 }
@@ -905,7 +970,15 @@ int mpsgpu_ppe_features(mpsgpu_t h, float* feat) {
     int n = 0;
     int e = mpsgpu_num_particles(h, &n);
     if (e) return e;
-    return mlpFeatures(h->mlp, h->d, h->B, feat, n, h->s);
+    std::vector<float> st((size_t)MPSGPU_MLP_NFEAT * n);
+    if ((e = mlpFeatures(h->mlp, h->d, h->B, st.data(), n, h->s))) return e;
+    std::vector<int> slot(n);
+    CK(cudaMemcpyAsync(slot.data(), h->d.slotOf, sizeof(int) * n, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    for (int r = 0; r < n; r++)   // rows in reference order
+        std::memcpy(feat + (size_t)r * MPSGPU_MLP_NFEAT, st.data() + (size_t)slot[r] * MPSGPU_MLP_NFEAT,
+                    sizeof(float) * MPSGPU_MLP_NFEAT);
+    return 0;
 }
 
 int mpsgpu_mlp_record(mpsgpu_t h, int enable) {

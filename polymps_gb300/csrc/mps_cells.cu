@@ -23,7 +23,10 @@ __global__ void k_cell_key(Dev d) {
     if (i >= d.N0) return;
     int n = liveN(d);
     int key = -1;
-    if (i < n && d.type[i] != d.P.ghost) {
+    if (i < n && d.type[i] == d.P.ghost) {
+        key = d.nB;   // live, in no bucket: listed after the buckets, never scanned
+        atomicAdd(d.cellCount + key, 1);
+    } else if (i < n) {
         const MpsParams& P = d.P;
         dvec4 p = d.pos[i];
         int ix, iy, iz = 0;
@@ -36,11 +39,13 @@ __global__ void k_cell_key(Dev d) {
             iz = (int)xmul(xsub(p.z, P.domainMin[2]), P.invBucketSide);
         }
         long long ib = (long long)iz * P.numBucketsXY + (long long)iy * P.numBucketsX + ix;
-        if (ib < 0 || ib >= d.nB) setErr(d, MPSE_DOMAIN);
-        else {
+        if (ib < 0 || ib >= d.nB) {
+            setErr(d, MPSE_DOMAIN);
+            key = d.nB;
+        } else {
             key = (int)ib;
-            atomicAdd(d.cellCount + key, 1);
         }
+        atomicAdd(d.cellCount + key, 1);
         // FP32 copy of the start-of-step positions for the prefiltered scans
         float4 hi = make_float4((float)(p.x - P.domainMin[0]), (float)(p.y - P.domainMin[1]),
                                 (float)(p.z - P.domainMin[2]), 0.f);
@@ -59,15 +64,17 @@ __global__ void k_cell_scatter(Dev d) {
     d.cellSorted[slot] = i;
 }
 
-// Restore ascending particle order inside each bucket (buckets hold ~16 particles).
+// Order each bucket by reference index (the reference's linked-list order; buckets hold
+// ~16 particles).  The range after the last bucket is ordered the same way.
 __global__ void k_cell_sort(Dev d) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= d.nB) return;
+    if (c > d.nB) return;
     int s0 = d.cellStart[c], s1 = d.cellStart[c + 1];
     for (int a = s0 + 1; a < s1; a++) {
         int v = d.cellSorted[a];
+        int ov = d.orig[v];
         int b = a - 1;
-        while (b >= s0 && d.cellSorted[b] > v) { d.cellSorted[b + 1] = d.cellSorted[b]; b--; }
+        while (b >= s0 && d.orig[d.cellSorted[b]] > ov) { d.cellSorted[b + 1] = d.cellSorted[b]; b--; }
         d.cellSorted[b + 1] = v;
     }
 }
@@ -147,13 +154,70 @@ void scanExclusive(const int* in, int* out, int n, int* scratch, cudaStream_t s)
 }
 int scanScratchInts(int n) { return 2 * ((n + SCAN_TILE - 1) / SCAN_TILE) + 4; }
 
-void launchBuckets(const Dev& d, int* scanScratch, cudaStream_t s) {
-    cudaMemsetAsync(d.cellCount, 0, sizeof(int) * (d.nB + 1), s);
-    cudaMemsetAsync(d.cellCursor, 0, sizeof(int) * (d.nB + 1), s);
+// ------------------------------------------------------------------ renumbering
+// Storage renumbering into the order of the bucket list just built: slot s receives the
+// particle listed at s (live particles; slots beyond the live count keep theirs), every
+// per-particle array is gathered through a scratch buffer, the reference-index maps follow,
+// and the list becomes the identity.  Neighbours are then stored next to each other, which
+// is what the gathers of every sweep and the coalescing of the bucket-order scans want.
+__global__ void k_perm_build(Dev d, int* perm) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.N0) return;
+    perm[s] = (s < *d.nLive) ? d.cellSorted[s] : s;
+}
+template <class T>
+__global__ void k_gather(const T* src, T* dst, const int* perm, int n) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) dst[s] = src[perm[s]];
+}
+__global__ void k_perm_maps(Dev d, const int* perm, const int* origOld) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= d.N0) return;
+    int r = origOld[perm[s]];
+    d.orig[s] = r;
+    d.slotOf[r] = s;
+    if (s < *d.nLive) d.cellSorted[s] = s;
+}
+template <class T>
+static void permute(T* a, const int* perm, void* scratch, int n, cudaStream_t s) {
+    if (!a) return;
+    k_gather<T><<<gridFor(n, 256), 256, 0, s>>>(a, (T*)scratch, perm, n);
+    cudaMemcpyAsync(a, scratch, sizeof(T) * n, cudaMemcpyDeviceToDevice, s);
+}
+int renumberLaunches() { return 1 + (15 + 17 + 5 + 3) + 1; }
+static void launchRenumber(const Dev& d, int* perm, void* scratch, cudaStream_t s) {
+    const int n = d.N0;
+    k_perm_build<<<gridFor(n, 256), 256, 0, s>>>(d, perm);
+    for (dvec4* v : {d.pos, d.vel, d.acc, d.accStar, d.mirror, d.wallPos, d.polyNormal, d.npcd, d.gradC,
+                     d.forceWall, d.c1, d.c2, d.c3, d.dvel, d.shift})
+        permute(v, perm, scratch, n, s);
+    for (double* v : {d.press, d.pressPPE, d.pressPPEprev, d.pndi, d.pndki, d.pndski, d.pndSmall, d.npcd2, d.conc,
+                      d.velDiv, d.diffTerm, d.pndWall, d.riw2, d.devDot, d.source, d.aux1, d.aux2})
+        permute(v, perm, scratch, n, s);
+    for (int* v : {d.type, d.bc, d.numNeigh, d.nNeighWall, d.nearWall}) permute(v, perm, scratch, n, s);
+    permute(d.posf, perm, scratch, n, s);
+    permute(d.posLo, perm, scratch, n, s);
+    permute(d.cellOf, perm, scratch, n, s);
+    // maps: the old orig goes through the scratch (the gather reads it while writing orig)
+    cudaMemcpyAsync(scratch, d.orig, sizeof(int) * n, cudaMemcpyDeviceToDevice, s);
+    k_perm_maps<<<gridFor(n, 256), 256, 0, s>>>(d, perm, (const int*)scratch);
+}
+
+__global__ void k_cell_pos(Dev d) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < d.cellStart[d.nB + 1]) d.cellPos[d.cellSorted[p]] = p;
+}
+
+void launchBuckets(const Dev& d, int* scanScratch, cudaStream_t s, int* perm, void* permScratch) {
+    cudaMemsetAsync(d.cellCount, 0, sizeof(int) * (d.nB + 2), s);
+    cudaMemsetAsync(d.cellCursor, 0, sizeof(int) * (d.nB + 2), s);
     k_cell_key<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
-    scanExclusive(d.cellCount, d.cellStart, d.nB, scanScratch, s);
+    scanExclusive(d.cellCount, d.cellStart, d.nB + 1, scanScratch, s);
     k_cell_scatter<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
-    k_cell_sort<<<gridFor(d.nB, 256), 256, 0, s>>>(d);
+    k_cell_sort<<<gridFor(d.nB + 1, 256), 256, 0, s>>>(d);
+    if (perm) launchRenumber(d, perm, permScratch, s);
+    cudaMemsetAsync(d.cellPos, 0xff, sizeof(int) * d.N0, s);
+    k_cell_pos<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
     k_posf_cell<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
 }
 

@@ -45,8 +45,17 @@ struct Dev {
     int *type, *bc, *numNeigh, *nNeighWall, *nearWall;
     float4* posf;      // FP32 copy of pos - domainMin (neighbour prefilter, FP32 sums)
     double* pressPPEprev;   // unclamped PPE solution of the solve before the last (warm start)
-    // buckets (stale list of the step)
+    // Storage numbering: particles are stored in bucket order (renumbered when the buckets
+    // are rebuilt every few steps) and identified by their reference index at the API:
+    // orig[s] = reference index of the particle stored in slot s, slotOf[r] = its slot.
+    // Inside a bucket the stored particles are ordered by reference index, so every scan
+    // visits them in the reference's order.
+    int *orig, *slotOf;
+    // buckets (stale list of the step): cellOf[i] = bucket, nB for a live particle in no
+    // bucket (ghost type), -1 beyond the live count; cellStart has nB + 2 entries, the
+    // range [cellStart[nB], cellStart[nB+1]) lists the live particles in no bucket
     int *cellOf, *cellStart, *cellCount, *cellSorted, *cellCursor;
+    int* cellPos;      // inverse of cellSorted over the list (-1: slot not listed)
     // FP32 positions in bucket order (posfCell[s] = posf[cellSorted[s]]): the prefilter of
     // the 27-bucket scans reads contiguous 16-byte records and fetches the particle index
     // only for candidates that pass it

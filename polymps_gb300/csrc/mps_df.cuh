@@ -191,12 +191,12 @@ __device__ __forceinline__ bool sideOkDF(const Dev& d, const SideDF& s, float4 h
 // buckets and their candidate loads coalesce; a live particle appears there once (an
 // out-of-domain removal moves the last particle into the freed index, which the list
 // still holds, and leaves the old last index beyond the live count).  STRAY = true
-// covers, in index order, the live particles the list does not hold (cellOf < 0).
+// covers, in index order, the live particles the list does not hold (cellOf == nB).
 template <bool STRAY>
 __device__ __forceinline__ int scanParticle(const Dev& d) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     int n = *d.nLive;
-    if (STRAY) return (t < n && d.cellOf[t] < 0) ? t : -1;
+    if (STRAY) return (t < n && d.cellOf[t] >= d.nB) ? t : -1;
     if (t >= d.cellStart[d.nB]) return -1;
     int i = d.cellSorted[t];
     return i < n ? i : -1;

@@ -33,7 +33,9 @@ struct Prof {
 // mps_cells.cu
 void scanExclusive(const int* in, int* out, int n, int* scratch, cudaStream_t s);
 int scanScratchInts(int n);
-void launchBuckets(const Dev& d, int* scanScratch, cudaStream_t s);
+// perm != NULL: renumber the storage into bucket order (perm: N0 ints, permScratch: 32 N0 bytes)
+void launchBuckets(const Dev& d, int* scanScratch, cudaStream_t s, int* perm, void* permScratch);
+int renumberLaunches();
 void launchNeighborList(const Dev& d, cudaStream_t s);
 void launchPosf(const Dev& d, cudaStream_t s);       // FP32 copy, then its bucket-ordered copy
 void launchPosfCell(const Dev& d, cudaStream_t s);   // bucket-ordered copy only

@@ -79,10 +79,13 @@ void launchPredict(const Dev& d, cudaStream_t s) { k_predict<<<gridFor(d.N0, 256
 
 // ------------------------------------------------------------------ out of domain
 // MpsParticle::checkParticleOutDomain, src/MpsParticle.cpp:270-396.  A parallel pass flags
-// fluid particles outside [min + bucket, max - bucket]; when any is flagged, a single
-// thread replays the reference's serial swap-with-last loop over the flagged slots in
-// ascending order (untouched slots keep valid flags: a swap only writes the current slot
-// and the last live slot, which leaves the loop range).
+// fluid particles outside [min + bucket, max - bucket] by reference index; when any is
+// flagged, a single thread replays the reference's serial swap-with-last loop on reference
+// indices: the data of the last live index is copied onto the removed one (the arrays the
+// reference copies) and the last index becomes a ghost, exactly as in the reference, on
+// the storage slots of those indices.  Live storage is then kept contiguous: the ghost's
+// slot trades places with the last live slot (all arrays, the index maps and the two
+// entries of the step's bucket list, so the list keeps pointing at the same data).
 __device__ __forceinline__ bool outside(const Dev& d, dvec4 p) {
     const MpsParams& P = d.P;
     double b = P.bucketSide;
@@ -90,36 +93,60 @@ __device__ __forceinline__ bool outside(const Dev& d, dvec4 p) {
            p.y < P.domainMin[1] + b || (P.dim == 3 && (p.z > P.domainMax[2] - b || p.z < P.domainMin[2] + b));
 }
 __global__ void k_out_flag(Dev d, int* flags, int* counter) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
     int n = liveN(d);
-    int f = 0;
-    if (i < n && d.type[i] == d.P.fluid && outside(d, d.pos[i])) f = 1;
-    if (i < d.N0) flags[i] = f;
+    if (s >= n) return;
+    int f = (d.type[s] == d.P.fluid && outside(d, d.pos[s])) ? 1 : 0;
+    flags[d.orig[s]] = f;
     if (f) atomicAdd(counter, 1);
 }
 template <class T> __device__ __forceinline__ void mv(T* a, int i, int L) { a[i] = a[L]; }
+template <class T> __device__ __forceinline__ void sw(T* a, int i, int j) { T t = a[i]; a[i] = a[j]; a[j] = t; }
+// every per-particle array that lives across operators: a pure relocation of two slots
+__device__ void swapSlots(const Dev& d, int a, int b) {
+    for (dvec4* v : {d.pos, d.vel, d.acc, d.accStar, d.mirror, d.wallPos, d.polyNormal, d.npcd, d.gradC,
+                     d.forceWall, d.c1, d.c2, d.c3, d.dvel, d.shift})
+        sw(v, a, b);
+    for (double* v : {d.press, d.pressPPE, d.pressPPEprev, d.pndi, d.pndki, d.pndski, d.pndSmall, d.npcd2, d.conc,
+                      d.velDiv, d.diffTerm, d.pndWall, d.riw2, d.devDot, d.source, d.aux1, d.aux2})
+        sw(v, a, b);
+    for (int* v : {d.type, d.bc, d.numNeigh, d.nNeighWall, d.nearWall, d.cellOf}) sw(v, a, b);
+    sw(d.posf, a, b);
+    sw(d.posLo, a, b);
+    int ra = d.orig[a], rb = d.orig[b];
+    d.orig[a] = rb; d.orig[b] = ra;
+    d.slotOf[ra] = b; d.slotOf[rb] = a;
+    int pa = d.cellPos[a], pb = d.cellPos[b];
+    if (pa >= 0) d.cellSorted[pa] = b;
+    if (pb >= 0) d.cellSorted[pb] = a;
+    d.cellPos[a] = pb; d.cellPos[b] = pa;
+}
 __global__ void k_out_serial(Dev d, const int* flags, int* counter) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     if (*counter == 0) return;
     const MpsParams& P = d.P;
     int newN = *d.nLive;
     int removed = 0;
-    for (int i = 0; i < newN; i++) {
-        if (!flags[i]) continue;
-        int L = newN - 1;
-        mv(d.type, i, L); mv(d.bc, i, L); mv(d.numNeigh, i, L); mv(d.press, i, L); mv(d.pndi, i, L);
-        mv(d.pndki, i, L); mv(d.pndski, i, L); mv(d.pndSmall, i, L); mv(d.npcd2, i, L); mv(d.conc, i, L);
-        mv(d.velDiv, i, L); mv(d.diffTerm, i, L); mv(d.nearWall, i, L); mv(d.nNeighWall, i, L);
-        mv(d.pndWall, i, L); mv(d.devDot, i, L); mv(d.riw2, i, L);
-        if (P.mpsType == 2 || P.mpsType == 3) { mv(d.pressPPE, i, L); mv(d.source, i, L); mv(d.pressPPEprev, i, L); }
-        mv(d.acc, i, L); mv(d.accStar, i, L); mv(d.pos, i, L); mv(d.vel, i, L); mv(d.npcd, i, L);
-        mv(d.gradC, i, L); mv(d.c1, i, L); mv(d.c2, i, L); mv(d.c3, i, L); mv(d.dvel, i, L);
-        mv(d.wallPos, i, L); mv(d.mirror, i, L); mv(d.polyNormal, i, L); mv(d.forceWall, i, L);
-        d.type[L] = P.ghost; d.bc[L] = P.other; d.nearWall[L] = 0; d.riw2[L] = 10e8 * P.partDist;
-        d.vel[L] = make_dvec4(0, 0, 0, 0);
-        d.press[L] = 0.0;
-        d.pos[L] = make_dvec4(P.domainMax[0] - P.partDist, P.domainMax[1] - P.partDist,
-                                (P.dim == 2) ? 0.0 : P.domainMax[2] - P.partDist, 0.0);
+    for (int r = 0; r < newN; r++) {
+        if (!flags[r]) continue;
+        const int L = newN - 1;
+        const int i = d.slotOf[r], l = d.slotOf[L];
+        if (i != l) {
+            mv(d.type, i, l); mv(d.bc, i, l); mv(d.numNeigh, i, l); mv(d.press, i, l); mv(d.pndi, i, l);
+            mv(d.pndki, i, l); mv(d.pndski, i, l); mv(d.pndSmall, i, l); mv(d.npcd2, i, l); mv(d.conc, i, l);
+            mv(d.velDiv, i, l); mv(d.diffTerm, i, l); mv(d.nearWall, i, l); mv(d.nNeighWall, i, l);
+            mv(d.pndWall, i, l); mv(d.devDot, i, l); mv(d.riw2, i, l);
+            if (P.mpsType == 2 || P.mpsType == 3) { mv(d.pressPPE, i, l); mv(d.source, i, l); mv(d.pressPPEprev, i, l); }
+            mv(d.acc, i, l); mv(d.accStar, i, l); mv(d.pos, i, l); mv(d.vel, i, l); mv(d.npcd, i, l);
+            mv(d.gradC, i, l); mv(d.c1, i, l); mv(d.c2, i, l); mv(d.c3, i, l); mv(d.dvel, i, l);
+            mv(d.wallPos, i, l); mv(d.mirror, i, l); mv(d.polyNormal, i, l); mv(d.forceWall, i, l);
+        }
+        d.type[l] = P.ghost; d.bc[l] = P.other; d.nearWall[l] = 0; d.riw2[l] = 10e8 * P.partDist;
+        d.vel[l] = make_dvec4(0, 0, 0, 0);
+        d.press[l] = 0.0;
+        d.pos[l] = make_dvec4(P.domainMax[0] - P.partDist, P.domainMax[1] - P.partDist,
+                              (P.dim == 2) ? 0.0 : P.domainMax[2] - P.partDist, 0.0);
+        if (l != newN - 1) swapSlots(d, l, newN - 1);
         newN--;
         removed++;
     }

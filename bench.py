@@ -220,8 +220,18 @@ def run_gb300(a, rank, world, local):
         torch.distributed.barrier()
     value = N * a.steps * world / dev_s
 
-    # state of the end of the timed run, uploaded every step of the end-to-end section
-    host = {f: g.get(f) for f in (abi.F_POS, abi.F_VEL, abi.F_PRESS, abi.F_PRESSPPE)}
+    # state of the end of the timed run, uploaded every step of the end-to-end section from
+    # page-locked host arrays (and the results read back into page-locked arrays)
+    def pinned_like(a):
+        t = torch.empty(a.size, dtype=torch.float64).pin_memory()
+        v = t.numpy().reshape(a.shape)
+        v[...] = a
+        return v, t
+    host, keep = {}, []
+    for f in (abi.F_POS, abi.F_VEL, abi.F_PRESS, abi.F_PRESSPPE):
+        v, t = pinned_like(g.get(f))
+        host[f] = v
+        keep.append(t)
     # PPE time-to-1e-8 on identical systems: plain FP64 vs mixed vs warm starts (before the
     # end-to-end section, which re-uploads the state and resets the warm-start history)
     ppe = None
@@ -237,9 +247,9 @@ def run_gb300(a, rank, world, local):
         for f, v in host.items():
             g.set(f, v)
         g.step()
-        host[abi.F_POS] = g.get(abi.F_POS)
-        host[abi.F_VEL] = g.get(abi.F_VEL)
-        host[abi.F_PRESS] = g.get(abi.F_PRESS)
+        g.get(abi.F_POS, out=host[abi.F_POS])
+        g.get(abi.F_VEL, out=host[abi.F_VEL])
+        g.get(abi.F_PRESS, out=host[abi.F_PRESS])
     e2e_s = time.perf_counter() - t0
     e2e = N * a.e2e_steps * world / e2e_s
 

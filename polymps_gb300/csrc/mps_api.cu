@@ -47,7 +47,6 @@ struct mpsgpu_s {
     std::string err;
     MlpState mlp;
     Prof prof;
-    void* pinned = nullptr;       // host staging for field transfers (N0 x 32 bytes, page-locked)
 };
 
 // ------------------------------------------------------------------ profiler
@@ -397,16 +396,28 @@ __global__ void k_from_ref(const T* src, T* dst, const int* slotOf, int n) {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r < n) dst[slotOf[r]] = src[r];
 }
+// vector fields: storage dvec4 <-> the reference's interleaved N x 3 doubles, in one pass
+__global__ void k_vec_to_ref(const dvec4* src, double* dst, const int* slotOf, int n) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    dvec4 v = src[slotOf[r]];
+    dst[3 * r] = v.x; dst[3 * r + 1] = v.y; dst[3 * r + 2] = v.z;
+}
+__global__ void k_vec_from_ref(const double* src, dvec4* dst, const int* slotOf, int n) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    dst[slotOf[r]] = make_dvec4(src[3 * r], src[3 * r + 1], src[3 * r + 2], 0.0);
+}
 static void toRef(mpsgpu_t h, int kind, const void* p, int n) {
     void* sc = h->permScratch;
-    if (kind == 0) k_to_ref<dvec4><<<gridFor(n, 256), 256, 0, h->s>>>((const dvec4*)p, (dvec4*)sc, h->d.slotOf, n);
+    if (kind == 0) k_vec_to_ref<<<gridFor(n, 256), 256, 0, h->s>>>((const dvec4*)p, (double*)sc, h->d.slotOf, n);
     else if (kind == 1) k_to_ref<double><<<gridFor(n, 256), 256, 0, h->s>>>((const double*)p, (double*)sc, h->d.slotOf, n);
     else k_to_ref<int><<<gridFor(n, 256), 256, 0, h->s>>>((const int*)p, (int*)sc, h->d.slotOf, n);
     countLaunch(1);
 }
 static void fromRef(mpsgpu_t h, int kind, void* p, int n) {
     const void* sc = h->permScratch;
-    if (kind == 0) k_from_ref<dvec4><<<gridFor(n, 256), 256, 0, h->s>>>((const dvec4*)sc, (dvec4*)p, h->d.slotOf, n);
+    if (kind == 0) k_vec_from_ref<<<gridFor(n, 256), 256, 0, h->s>>>((const double*)sc, (dvec4*)p, h->d.slotOf, n);
     else if (kind == 1) k_from_ref<double><<<gridFor(n, 256), 256, 0, h->s>>>((const double*)sc, (double*)p, h->d.slotOf, n);
     else k_from_ref<int><<<gridFor(n, 256), 256, 0, h->s>>>((const int*)sc, (int*)p, h->d.slotOf, n);
     countLaunch(1);
@@ -657,7 +668,6 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     }
     if (cudaDeviceSynchronize() != cudaSuccess || launchStatus()) { mpsgpu_destroy(h); return MPSGPU_ERR_CUDA; }
     h->maxIter = 0;
-    if (cudaMallocHost(&h->pinned, sizeof(dvec4) * (size_t)n) != cudaSuccess) { mpsgpu_destroy(h); return MPSGPU_ERR_NOMEM; }
     if ((e = mlpInit(h->mlp, n, h->s))) { mpsgpu_destroy(h); return e; }
     *out = h;
     return 0;
@@ -668,7 +678,6 @@ int mpsgpu_destroy(mpsgpu_t h) {
     if (h->s) cudaStreamSynchronize(h->s);
     mlpFree(h->mlp);
     h->prof.destroy();
-    if (h->pinned) cudaFreeHost(h->pinned);
     for (void* p : h->allocs) cudaFree(p);
     for (cudaEvent_t ev : {h->e0, h->e1, h->ea0, h->ea1, h->es0, h->es1}) if (ev) cudaEventDestroy(ev);
     if (h->s) cudaStreamDestroy(h->s);
@@ -836,19 +845,11 @@ int mpsgpu_get_field(mpsgpu_t h, int f, void* host) {
     int n = 0;
     int e = mpsgpu_num_particles(h, &n);
     if (e) return e;
+    // reorder (and de-pad vectors) on the device, then one copy into the caller's array
     toRef(h, kind, p, n);
-    if (kind == 0) {
-        dvec4* v = (dvec4*)h->pinned;
-        CK(cudaMemcpyAsync(v, h->permScratch, sizeof(dvec4) * n, cudaMemcpyDeviceToHost, h->s));
-        CK(cudaStreamSynchronize(h->s));
-        double* o = (double*)host;
-        for (int i = 0; i < n; i++) { o[3 * i] = v[i].x; o[3 * i + 1] = v[i].y; o[3 * i + 2] = v[i].z; }
-    } else {
-        size_t sz = (kind == 1) ? sizeof(double) : sizeof(int);
-        CK(cudaMemcpyAsync(h->pinned, h->permScratch, sz * n, cudaMemcpyDeviceToHost, h->s));
-        CK(cudaStreamSynchronize(h->s));
-        std::memcpy(host, h->pinned, sz * n);
-    }
+    size_t bytes = (kind == 0) ? 3 * sizeof(double) * n : ((kind == 1) ? sizeof(double) : sizeof(int)) * n;
+    CK(cudaMemcpyAsync(host, h->permScratch, bytes, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
     return 0;
 }
 
@@ -866,16 +867,9 @@ int mpsgpu_set_field(mpsgpu_t h, int f, const void* host) {
     int n = 0;
     int e = mpsgpu_num_particles(h, &n);
     if (e) return e;
-    if (kind == 0) {
-        dvec4* v = (dvec4*)h->pinned;
-        const double* in = (const double*)host;
-        for (int i = 0; i < n; i++) v[i] = make_dvec4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0);
-        CK(cudaMemcpyAsync(h->permScratch, v, sizeof(dvec4) * n, cudaMemcpyHostToDevice, h->s));
-    } else {
-        size_t sz = (kind == 1) ? sizeof(double) : sizeof(int);
-        std::memcpy(h->pinned, host, sz * n);
-        CK(cudaMemcpyAsync(h->permScratch, h->pinned, sz * n, cudaMemcpyHostToDevice, h->s));
-    }
+    // one copy of the caller's array, then reorder (and pad vectors) on the device
+    size_t bytes = (kind == 0) ? 3 * sizeof(double) * n : ((kind == 1) ? sizeof(double) : sizeof(int)) * n;
+    CK(cudaMemcpyAsync(h->permScratch, host, bytes, cudaMemcpyHostToDevice, h->s));
     fromRef(h, kind, p, n);
     // any state change can alter list membership, masks or the near-wall set
     h->listValid = false;

@@ -182,8 +182,9 @@ class MpsGpu:
         lib().mpsgpu_time(self.h, C.byref(t), C.byref(it))
         return t.value, it.value
 
-    def get(self, field):
-        buf = abi.field_buffer(field, self.n)
+    def get(self, field, out=None):
+        """Field in the reference's host layout; out: a preallocated (e.g. page-locked) array."""
+        buf = abi.field_buffer(field, self.n) if out is None else out
         _check("mpsgpu_get_field", lib().mpsgpu_get_field(self.h, field, buf.ctypes.data), self.h)
         return buf
 

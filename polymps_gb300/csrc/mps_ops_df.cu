@@ -478,12 +478,9 @@ __global__ void __launch_bounds__(BLK) k_press_grad_df(Dev d) {
             if (pmin > pj) pmin = pj;
         });
     }
-    df C[9];
-    if (P.gradientCorrection) {
-#pragma unroll
-        for (int k = 0; k < 9; k++) C[k] = loadDF(d.corrDF + (size_t)k * d.N0, i);
-    }
     df base = (gt == 0) ? -pmin : (gt == 1 ? Pi : Pi - pmin - pmin);
+    // sum of r_ij f_ij; with gradient correction C (constant per particle) is applied to
+    // the sum once: sum (C r) f = C (sum r f)
     df ax = dfF(0.f), ay = ax, az = ax;
     forMask(d, i, mS, [&](int j, size_t) {
         PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
@@ -494,13 +491,17 @@ __global__ void __launch_bounds__(BLK) k_press_grad_df(Dev d) {
             double nj = d.pndi[j], Pj = d.press[j], Pid = d.press[i];
             f = (ni > P.epsilonZero && nj > P.epsilonZero) ? dfD(ni * Pj / nj + nj * Pid / ni) * w.wr2 : w.w;
         }
-        if (!P.gradientCorrection) { ax += q.v.x * f; ay += q.v.y * f; az += q.v.z * f; }
-        else {
-            ax += (q.v.x * C[0] + q.v.y * C[1] + q.v.z * C[2]) * f;
-            ay += (q.v.x * C[3] + q.v.y * C[4] + q.v.z * C[5]) * f;
-            az += (q.v.x * C[6] + q.v.y * C[7] + q.v.z * C[8]) * f;
-        }
+        ax += q.v.x * f; ay += q.v.y * f; az += q.v.z * f;
     });
+    if (P.gradientCorrection) {
+        df C[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) C[k] = loadDF(d.corrDF + (size_t)k * d.N0, i);
+        df bx = C[0] * ax + C[1] * ay + C[2] * az;
+        df by = C[3] * ax + C[4] * ay + C[5] * az;
+        df bz = C[6] * ax + C[7] * ay + C[8] * az;
+        ax = bx; ay = by; az = bz;
+    }
     double c = P.relaxPress * P.coeffPressGrad / P.DNS_FL1;
     d.acc[i] = make_dvec4(dD(ax) * c, dD(ay) * c, dD(az) * c, 0.0);
 }

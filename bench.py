@@ -311,20 +311,22 @@ def ppe_compare(g, abi, use_mlp):
     x_prev2 = g.get(abi.F_PRESSPPE_PREV)
     res = {}
     # single-launch solves, then the per-kernel launch path for reference
-    variants = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, True),
-                ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, True),
-                ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, True),
-                ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP, True),
-                ("matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_PREVIOUS, True),
-                ("compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_PREVIOUS, True),
-                ("extrapolated_compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_EXTRAP, True)]
+    # launch mode: 1 single launch (default), 2 single launch with staged ELL tiles, 0 per kernel
+    variants = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 1),
+                ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 1),
+                ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, 1),
+                ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 1),
+                ("extrapolated_fp32_fp64_staged_tiles", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 2),
+                ("matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_PREVIOUS, 1),
+                ("compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_PREVIOUS, 1),
+                ("extrapolated_compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_EXTRAP, 1)]
     if use_mlp:
-        variants.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP, True))
-    variants += [("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, False),
-                 ("fp32_fp64_per_kernel_launch", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, False)]
-    for name, s, w, single in variants:
+        variants.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP, 1))
+    variants += [("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 0),
+                 ("fp32_fp64_per_kernel_launch", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 0)]
+    for name, s, w, mode in variants:
         best = None
-        g.set_ppe_launch(single)
+        g.set_ppe_launch(mode)
         for rep in range(3):
             g.set(abi.F_PRESSPPE, x_prev)
             g.set(abi.F_PRESSPPE_PREV, x_prev2)
@@ -340,7 +342,7 @@ def ppe_compare(g, abi, use_mlp):
         else:
             p = g.get(abi.F_PRESSPPE)
             res[name]["rel_err_vs_fp64"] = float(np.linalg.norm(p - p_ref) / np.linalg.norm(p_ref))
-    g.set_ppe_launch(True)
+    g.set_ppe_launch(1)
     base = res["plain_fp64"]["ms"]
     for k in res:
         res[k]["speedup_vs_plain"] = round(base / res[k]["ms"], 3) if res[k]["ms"] > 0 else None

@@ -234,11 +234,14 @@ int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm_start, double tol, int ma
  * error margin; per-particle results differ from FP64 by ~1e-11 relative.  Operators
  * without a DF32 kernel (diffusive/mean PND, extrapolation, shifting, dummy velocity,
  * step-0 PND) run their FP64 kernels in either mode. */
-/* How the PPE solve is launched: 1 (default) the whole solve in one cooperative launch
- * with device-side grid barriers when the device supports it, 0 one launch per kernel
- * with the host polling convergence every few iterations.  Same algorithm and results to
- * rounding; the single launch removes launch gaps and host round trips. */
-int mpsgpu_set_ppe_launch(mpsgpu_t h, int persistent);
+/* How the PPE solve is launched: 0 one launch per kernel with the host polling
+ * convergence every few iterations; 1 (default) the whole solve in one cooperative launch
+ * with device-side grid barriers; 2 as 1, with the mixed solver's FP32 matrix streamed
+ * through shared memory by bulk copies (measured slower than 1 at 864k rows: the SpMV
+ * is bound by the neighbour gathers of z, not by the matrix stream).  Same algorithm
+ * and results to rounding.
+ * Modes 1 and 2 fall back to the previous mode where the device does not support them. */
+int mpsgpu_set_ppe_launch(mpsgpu_t h, int mode);
 
 #define MPSGPU_PRECISION_FP64  0
 #define MPSGPU_PRECISION_DF32  1

@@ -38,7 +38,7 @@ struct mpsgpu_s {
     bool listValid = false;
     bool masksValid = false;
     bool cacheValid = false;   // per-entry FP64 weights of the current list
-    bool persistent = true;    // PPE solve in one cooperative launch when the device allows it
+    int persistent = 1;        // PPE launch: 0 per kernel, 1 single cooperative launch, 2 + staged ELL tiles
     double timeCurrent = 0.0;
     int numIter = 0;
     int lastOut = 0;
@@ -235,7 +235,10 @@ static int calcPress(mpsgpu_t h) {
     const bool mixed = h->solver != MPSGPU_SOLVER_PLAIN_FP64;
     h->B.prepared = df32(h) ? 1 : 0;   // the DF32 assembly writes the FP32 copies itself
     h->B.matfree = h->solver == MPSGPU_SOLVER_MIXED_MATFREE ? 1 : (h->solver == MPSGPU_SOLVER_MIXED_COMPACT ? 2 : 0);
-    int pgrid = !mixed ? h->B.pgridCg : (h->B.matfree == 2 ? h->B.pgridH16 : (h->B.matfree ? h->B.pgridMf : h->B.pgridMx));
+    if (h->solver == MPSGPU_SOLVER_MIXED && h->persistent == 2 && h->B.pgridTs > 0) h->B.matfree = 3;
+    int pgrid = !mixed ? h->B.pgridCg
+                       : (h->B.matfree == 3 ? h->B.pgridTs
+                                            : (h->B.matfree == 2 ? h->B.pgridH16 : (h->B.matfree ? h->B.pgridMf : h->B.pgridMx)));
     if (h->B.matfree && (!h->persistent || pgrid <= 0)) {
         g_lastError = "this mixed inner operator needs the single-launch (cooperative) PPE solve";
         return MPSGPU_ERR_UNSUPPORTED;
@@ -614,22 +617,25 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     // PPE buffers
     PpeBuffers& B = h->B;
     std::memset(&B, 0, sizeof(B));
-    B.N0 = n; B.K = d.K;
+    // ELL leading dimension padded to whole 256-row tiles: every slice of a tile is a
+    // 16-byte aligned, in-bounds range for the bulk copies of the staged SpMV
+    B.N0 = (n + 255) / 256 * 256; B.K = d.K;
+    const size_t ell = (size_t)d.K * B.N0;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     B.nblocks = std::max(1, sms) * 8;
     if (p->mpsType == 2) {
         for (double** v : {&B.diag, &B.x, &B.b, &B.r, &B.z, &B.p, &B.Ap}) A(*v, n);
-        A(B.val, (size_t)d.K * n);
-        A(B.col, (size_t)d.K * n);
+        A(B.val, ell);
+        A(B.col, ell);
         A(B.rowLen, n);
-        A(B.valf, (size_t)d.K * n);
+        A(B.valf, ell);
         for (float** v : {&B.diagf, &B.diagInvf, &B.rf, &B.zf, &B.pf, &B.Apf, &B.xf}) A(*v, n);
         B.pgridCg = ppePersistentGrid(0);
         B.pgridMx = ppePersistentGrid(1);
         A(B.scal, 16);
-        A(B.partials, 4 * std::max(std::max(B.nblocks, ppePersistentGrid(3)),
+        A(B.partials, 4 * std::max(std::max(std::max(B.nblocks, ppePersistentGrid(4)), ppePersistentGrid(3)),
                                    std::max(B.pgridCg, std::max(B.pgridMx, ppePersistentGrid(2)))));
         A(B.counter, 1);
         A(B.flag, 8);
@@ -637,8 +643,11 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         A(B.mfMask, n);
         B.pgridMf = ppePersistentGrid(2);
         B.pgridH16 = ppePersistentGrid(3);
-        A(B.valh, (size_t)d.K * n);
-        A(B.col16, (size_t)d.K * n);
+        B.pgridTs = ppePersistentGrid(4);
+        // the staged tiles keep up to 128 tile lengths per block in shared memory
+        if (B.pgridTs > 0 && (n + 255) / 256 > 128 * B.pgridTs) B.pgridTs = 0;
+        A(B.valh, ell);
+        A(B.col16, ell);
         A(B.sclf, n);
         A(B.sgs, n);
         A(B.wideRow, n);
@@ -752,9 +761,9 @@ int mpsgpu_set_precision(mpsgpu_t h, int precision) {
     return 0;
 }
 
-int mpsgpu_set_ppe_launch(mpsgpu_t h, int persistent) {
-    if (!h) return MPSGPU_ERR_ARG;
-    h->persistent = persistent != 0;
+int mpsgpu_set_ppe_launch(mpsgpu_t h, int mode) {
+    if (!h || mode < 0 || mode > 2) return MPSGPU_ERR_ARG;
+    h->persistent = mode;
     return 0;
 }
 
@@ -927,7 +936,8 @@ int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col, 
     for (int i = 0; i < n; i++) nnz += len[i];
     *nnz_out = nnz;
     if (!col) return 0;
-    size_t ellN = (size_t)h->d.K * h->N0;
+    const size_t ld = h->B.N0;
+    size_t ellN = (size_t)h->d.K * ld;
     std::vector<int> ec(ellN);
     std::vector<double> ev(ellN);
     CK(cudaMemcpyAsync(ec.data(), h->B.col, sizeof(int) * ellN, cudaMemcpyDeviceToHost, h->s));
@@ -942,7 +952,7 @@ int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col, 
         if (rhs) rhs[r] = bst[i];
         row.clear();
         row.push_back({r, diag[i]});
-        for (int c = 0; c < len[i]; c++) row.push_back({orig[ec[(size_t)c * h->N0 + i]], ev[(size_t)c * h->N0 + i]});
+        for (int c = 0; c < len[i]; c++) row.push_back({orig[ec[(size_t)c * ld + i]], ev[(size_t)c * ld + i]});
         std::sort(row.begin(), row.end(), [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
         for (auto& pr : row) { col[k] = pr.first; val[k] = pr.second; k++; }
         rowptr[r + 1] = k;

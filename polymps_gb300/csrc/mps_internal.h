@@ -83,7 +83,7 @@ void launchWallDistance(const Dev& d, cudaStream_t s);
 
 // mps_ppe.cu
 struct PpeBuffers {
-    int N0, K;
+    int N0, K;       // N0: leading dimension of the ELL arrays (rows padded to a multiple of 256)
     double *diag, *val, *x, *b, *r, *z, *p, *Ap, *scal;  // scal: solver scalars (device)
     int* col;
     int* rowLen;
@@ -104,6 +104,7 @@ struct PpeBuffers {
     float *sclf, *sgs;       // s_i = 1/sqrt|A_ii| and sigma_i s_i
     unsigned char* wideRow;  // rows with an offset outside 16 bits (read the 32-bit columns)
     int pgridH16;
+    int pgridTs;             // co-resident grid of the mixed solver with the staged ELL tiles (0: none)
 };
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);

@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
                 B.valf[k] = mij.h;   // the FP32 copy of the mixed solver (hi part = fl32)
                 B.col[k] = j;
                 len++;
-                mm |= 1ull << ((e - i) / B.N0);
+                mm |= 1ull << ((e - i) / d.N0);
             }
         }
     });

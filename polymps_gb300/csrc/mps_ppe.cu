@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
                 B.val[k] = mij;
                 B.col[k] = j;
                 len++;
-                mm |= 1ull << ((e - i) / B.N0);
+                mm |= 1ull << ((e - i) / d.N0);
             }
         }
     });
@@ -514,7 +514,7 @@ __device__ __forceinline__ bool qArrive(const PpeBuffers& B, QCtl& c, Fin fin) {
             B.bar[QB_ARR] = 0u;
             __threadfence();
             atomicExch(B.bar + QB_GEN, c.gen);
-            sOk = 1;
+            sOk = *(volatile unsigned int*)(B.bar + QB_ABT) == 0u;
         }
     } else if (threadIdx.x == 0) {
         int ok = 1;
@@ -525,6 +525,7 @@ __device__ __forceinline__ bool qArrive(const PpeBuffers& B, QCtl& c, Fin fin) {
             __nanosleep(100);
         }
         __threadfence();
+        if (ok && *(volatile unsigned int*)(B.bar + QB_ABT)) ok = 0;
         sOk = ok;
     }
     __syncthreads();
@@ -691,21 +692,184 @@ __device__ __forceinline__ float h16Row(const PpeBuffers& B, const float* y, int
     return y[i] + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
 }
 
+// ------------------------------------------------------------------ staged ELL tiles
+// The FP32 inner SpMV with the matrix streamed through shared memory: a block owns the
+// 256-row tiles t = blockIdx.x + m gridDim.x (the rows its threads own in every other
+// phase); each tile's column and value slices (1 KB each, column-major ELL) are copied by
+// the bulk-copy engine (cp.async.bulk, completion counted on an mbarrier) in chunks of
+// TS_CH slices into a TS_NS-stage ring, up to TS_NS - 1 chunks ahead of the threads, which
+// read their row's entries from shared memory and gather z.  The engine keeps the HBM
+// stream in flight independently of the threads' gather latencies.  Every mbarrier wait
+// is bounded; a wait that runs out sets the abort word (see qArrive) and the block stops
+// consuming, drains the copies it issued (again bounded) and returns at the next barrier.
+#define TS_CH 8
+#define TS_NS 3
+#define TS_SPIN (1 << 20)
+struct TsStage {
+    int col[TS_CH][QB];
+    float val[TS_CH][QB];
+};
+#define TS_MAXT 128   // tiles per block held in shared memory
+struct TsSmem {
+    TsStage st[TS_NS];
+    unsigned long long full[TS_NS], empty[TS_NS];
+    int tlen[TS_MAXT];
+};
+__device__ __forceinline__ unsigned smemAddr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbarInit(unsigned long long* b, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbarExpectTx(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbarArrive(unsigned long long* b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(b)) : "memory");
+}
+__device__ __forceinline__ bool mbarTry(unsigned long long* b, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smemAddr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait; false when it ran out
+__device__ __forceinline__ bool mbarWait(unsigned long long* b, unsigned parity) {
+    for (int k = 0; k < TS_SPIN; k++)
+        if (mbarTry(b, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulkG2S(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smemAddr(dst)),
+                 "l"(src), "r"(bytes), "r"(smemAddr(bar))
+                 : "memory");
+}
+// Chunk walk of a block: its tiles in order (m-th tile = blockIdx.x + m gridDim.x, length
+// tlen[m] = longest row), ceil(len / TS_CH) chunks each.
+struct TsWalk {
+    int m, chunk;
+};
+__device__ __forceinline__ bool tsNext(const TsSmem& sm, int mt, TsWalk& w) {
+    while (w.m < mt) {
+        if (w.chunk * TS_CH < sm.tlen[w.m]) return true;
+        w.m++;
+        w.chunk = 0;
+    }
+    return false;
+}
+// issue one chunk (thread 0): slices [c TS_CH, min(L, (c+1) TS_CH)) of the walk's tile
+__device__ __forceinline__ void tsIssue(TsSmem& sm, const PpeBuffers& B, const TsWalk& w, unsigned q, bool& ok) {
+    const int s = q % TS_NS;
+    const unsigned use = q / TS_NS;
+    if (use > 0 && !mbarWait(&sm.empty[s], (use - 1) & 1)) { ok = false; return; }
+    const int L = sm.tlen[w.m];
+    const int k0 = w.chunk * TS_CH, nsl = min(TS_CH, L - k0);
+    const size_t r0 = (size_t)(blockIdx.x + w.m * gridDim.x) * QB;
+    mbarExpectTx(&sm.full[s], (unsigned)(nsl * QB * (sizeof(int) + sizeof(float))));
+    for (int u = 0; u < nsl; u++) {
+        size_t e = (size_t)(k0 + u) * B.N0 + r0;
+        bulkG2S(sm.st[s].col[u], B.col + e, QB * sizeof(int), &sm.full[s]);
+        bulkG2S(sm.st[s].val[u], B.valf + e, QB * sizeof(float), &sm.full[s]);
+    }
+}
+
+// One staged SpMV pass over the block's tiles: y_i = A_ii z_i + sum_k valf z[col] for the
+// thread's row of every tile, then rowDone(i, y_i) (rows below the live count only).
+// gq counts the chunks consumed, the same in every thread; returns false when a wait ran
+// out (the abort word is then set; the copies issued are drained, bounded, before return).
+template <class F>
+__device__ __forceinline__ bool tsSpmv(TsSmem& sm, const PpeBuffers& B, const float* z, int n, int mt, unsigned& gq,
+                                       F&& rowDone) {
+    bool ok = true;
+    TsWalk prod = {0, 0};
+    unsigned qp = gq, q = gq;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < TS_NS - 1 && ok && tsNext(sm, mt, prod); k++) { tsIssue(sm, B, prod, qp, ok); qp++; prod.chunk++; }
+    for (int m = 0; m < mt; m++) {
+        const int row = (blockIdx.x + m * gridDim.x) * QB + threadIdx.x;
+        const int len = (row < n) ? __ldg(B.rowLen + row) : 0;
+        const int L = sm.tlen[m];
+        float acc[TS_CH];
+#pragma unroll
+        for (int u = 0; u < TS_CH; u++) acc[u] = 0.f;
+        for (int c = 0; c * TS_CH < L; c++) {
+            if (threadIdx.x == 0 && ok && tsNext(sm, mt, prod)) { tsIssue(sm, B, prod, qp, ok); qp++; prod.chunk++; }
+            const int st = q % TS_NS;
+            bool got = ok && mbarWait(&sm.full[st], (q / TS_NS) & 1);
+            got = __all_sync(0xffffffffu, got);
+            if (got) {
+                const int k0 = c * TS_CH;
+#pragma unroll
+                for (int u = 0; u < TS_CH; u++)
+                    if (k0 + u < len) acc[u] += sm.st[st].val[u][threadIdx.x] * z[sm.st[st].col[u][threadIdx.x]];
+            } else {
+                ok = false;
+            }
+            __syncwarp();
+            if ((threadIdx.x & 31) == 0) mbarArrive(&sm.empty[st]);
+            q++;
+        }
+        if (row < n)
+            rowDone(row, __ldg(B.diagf + row) * z[row] +
+                             (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]))));
+    }
+    // a wait that ran out: stop, and let the copies this block issued land before leaving
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+            atomicExch(B.bar + QB_ABT, 1u);
+            for (unsigned k = q; k < qp; k++) mbarWait(&sm.full[k % TS_NS], (k / TS_NS) & 1);
+        }
+        __syncthreads();
+        return false;
+    }
+    gq = q;
+    return true;
+}
+
 // Mixed solver: FP64 residual r = b - A x and its norm, FP32 inner CG on r / ||r|| to
 // the relative tolerance eta_k, x += ||r|| d in FP64, repeated until ||r|| < tol ||b||.
 // eta_k = max(eta, tol ||b|| / (2 ||r_k||)): an inner solve stops once its correction
 // brings the outer residual to half the tolerance, so the last one does not over-solve.
 // Inner operator of k_mx_solve: the assembled FP32 ELL matrix with Jacobi preconditioning,
 // the matrix-free FP32 operator with Jacobi preconditioning, or the compact scaled operator.
-enum { OP_ELL32 = 0, OP_MATFREE = 1, OP_H16 = 2 };
+enum { OP_ELL32 = 0, OP_MATFREE = 1, OP_H16 = 2, OP_TILED = 3 };
 template <int OP>
 __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
+    extern __shared__ __align__(128) unsigned char dynSmem[];
     const int n = liveN(d);
     const float cP = (float)d.P.coeffPPE, re = (float)d.P.reL, invRe = (float)(1.0 / d.P.reL);
     const int wt = d.P.weightType;
     const int T = gridDim.x * QB;
     const int t0 = blockIdx.x * QB + threadIdx.x;
     QCtl c = {0u};
+    // staged tiles: the block's tile lengths and the mbarriers of the ring
+    TsSmem& sm = *reinterpret_cast<TsSmem*>(dynSmem);
+    const int ntiles = (n + QB - 1) / QB;
+    const int mt = (ntiles > (int)blockIdx.x) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    unsigned gq = 0u;   // chunks consumed so far (the same count in every thread of the block)
+    if (OP == OP_TILED) {
+        if (threadIdx.x == 0) {
+            for (int st = 0; st < TS_NS; st++) {
+                mbarInit(&sm.full[st], 1u);
+                mbarInit(&sm.empty[st], QB / 32);
+            }
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        for (int m = threadIdx.x; m < TS_MAXT; m += QB) sm.tlen[m] = 0;
+        __syncthreads();
+        for (int m = 0; m < mt; m++) {
+            const int row = (blockIdx.x + m * gridDim.x) * QB + threadIdx.x;
+            int len = (row < n) ? __ldg(B.rowLen + row) : 0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
+            if ((threadIdx.x & 31) == 0) atomicMax(&sm.tlen[m], len);
+        }
+        __syncthreads();
+    }
     if (OP == OP_H16) {
         // scaling, then the compact copy of the FP32 matrix
         for (int i = t0; i < n; i += T) {
@@ -777,7 +941,16 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
             {
                 const float beta = inner ? (float)vd(B.scal + S_BETA) : 0.f;
                 df a[1] = {dfF(0.f)};
-                forRows(B, n, t0, T, [&](int i, int len) {
+                if (OP == OP_TILED) {
+                    bool okp = tsSpmv(sm, B, B.zf, n, mt, gq, [&](int i, float q) {
+                        float z = B.zf[i];
+                        float ap = inner ? q + beta * B.Apf[i] : q;
+                        float p = inner ? z + beta * B.pf[i] : z;
+                        B.Apf[i] = ap; B.pf[i] = p;
+                        a[0] += prod2(p, ap);
+                    });
+                    (void)okp;   // an ran-out wait sets the abort word: the reduction below returns false
+                } else forRows(B, n, t0, T, [&](int i, int len) {
                     float q = (OP == OP_MATFREE) ? mfRowF(d, B, B.zf, i, cP, re, invRe, wt)
                             : (OP == OP_H16)   ? h16Row(B, B.zf, i, len)
                                                : qRowF(B, B.zf, i, len);
@@ -919,13 +1092,22 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
 }
 
 // kind: 0 plain FP64, 1 mixed, 2 mixed with the matrix-free inner operator, 3 mixed with
-// the compact scaled inner operator
+// the compact scaled inner operator, 4 mixed with the staged tiles
 int ppePersistentGrid(int kind) {
     int dev = 0, sms = 0, coop = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return 0;
+    if (kind == 4) {
+        if (cudaFuncSetAttribute(k_mx_solve<OP_TILED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(TsSmem)) != cudaSuccess)
+            return 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_TILED>, QB, sizeof(TsSmem)) != cudaSuccess ||
+            per <= 0)
+            return 0;
+        return per * sms;
+    }
     cudaError_t e = kind == 3   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_H16>, QB, 0)
                     : kind == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_MATFREE>, QB, 0)
                     : kind == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_ELL32>, QB, 0)
@@ -956,7 +1138,8 @@ static int finishPersistent(const PpeBuffers& B, cudaStream_t s, int* iters, int
 
 int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol, int maxIter, cudaStream_t s,
                        int* iters, int* refinements, double* relres, double* relres0, Prof* prof) {
-    int grid = !mixed ? B.pgridCg : (B.matfree == 2 ? B.pgridH16 : (B.matfree ? B.pgridMf : B.pgridMx));
+    int grid = !mixed ? B.pgridCg
+                      : (B.matfree == 3 ? B.pgridTs : (B.matfree == 2 ? B.pgridH16 : (B.matfree ? B.pgridMf : B.pgridMx)));
     if (grid <= 0) return MPSGPU_ERR_UNSUPPORTED;
     bool pr = prof && prof->on;
     cudaMemsetAsync(B.flag, 0, 5 * sizeof(int), s);
@@ -974,10 +1157,12 @@ int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol,
     void* args[5] = {&dd, &bb, &t, &mi, &eta2};
     if (pr) prof->begin(PROF_PPE_SOLVE, s);
     const void* fn = !mixed              ? (const void*)k_cg_solve
+                     : B.matfree == 3    ? (const void*)k_mx_solve<OP_TILED>
                      : B.matfree == 2    ? (const void*)k_mx_solve<OP_H16>
                      : B.matfree == 1    ? (const void*)k_mx_solve<OP_MATFREE>
                                          : (const void*)k_mx_solve<OP_ELL32>;
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, grid, QB, args, 0, s);
+    size_t dyn = (mixed && B.matfree == 3) ? sizeof(TsSmem) : 0;
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, grid, QB, args, dyn, s);
     if (pr) prof->end(s);
     if (e != cudaSuccess) return MPSGPU_ERR_CUDA;
     countLaunch(1);

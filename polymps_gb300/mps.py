@@ -163,9 +163,10 @@ class MpsGpu:
         """FP64 (reference arithmetic) or DF32 (float-float pair arithmetic, same decisions)."""
         _check("mpsgpu_set_precision", lib().mpsgpu_set_precision(self.h, precision), self.h)
 
-    def set_ppe_launch(self, persistent=True):
-        """Whole PPE solve in one cooperative launch (True) or one launch per kernel."""
-        _check("mpsgpu_set_ppe_launch", lib().mpsgpu_set_ppe_launch(self.h, int(bool(persistent))), self.h)
+    def set_ppe_launch(self, mode=1):
+        """PPE launch: 0 one launch per kernel, 1 (default) one cooperative launch per solve,
+        2 as 1 with the FP32 matrix streamed through shared memory by bulk copies."""
+        _check("mpsgpu_set_ppe_launch", lib().mpsgpu_set_ppe_launch(self.h, int(mode)), self.h)
 
     def set_solver(self, solver=abi.SOLVER_PLAIN_FP64, warm=abi.WARM_PREVIOUS, tol=1e-8, max_iter=0):
         _check("mpsgpu_set_solver", lib().mpsgpu_set_solver(self.h, solver, warm, tol, max_iter), self.h)

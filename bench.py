@@ -169,7 +169,7 @@ def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False, compact=False):
 
 def run_gb300(a, rank, world, local):
     import torch
-    from polymps_gb300 import abi, build, cases, mps
+    from polymps_gb300 import abi, build, cases, mps, replicas
     if world > 1:
         import torch.distributed as dist_
         dist_.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
@@ -212,13 +212,10 @@ def run_gb300(a, rank, world, local):
     g.profile(False)
     clk = clocks.stop()
     torch.cuda.synchronize()
-    dev_s = st.stepMs / 1e3
-    if world > 1:
-        t = torch.tensor([dev_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s = float(t.item())
-        torch.distributed.barrier()
-    value = N * a.steps * world / dev_s
+    # replicas: particle-steps of all ranks over the slowest rank's device time
+    units, dev_s = replicas.aggregate(N * a.steps, st.stepMs / 1e3, world, device="cuda")
+    replicas.barrier(world)
+    value = units / dev_s
 
     # state of the end of the timed run, uploaded every step of the end-to-end section from
     # page-locked host arrays (and the results read back into page-locked arrays)
@@ -251,7 +248,8 @@ def run_gb300(a, rank, world, local):
         g.get(abi.F_VEL, out=host[abi.F_VEL])
         g.get(abi.F_PRESS, out=host[abi.F_PRESS])
     e2e_s = time.perf_counter() - t0
-    e2e = N * a.e2e_steps * world / e2e_s
+    e2e_units, e2e_s = replicas.aggregate(N * a.e2e_steps, e2e_s, world, device="cuda")
+    e2e = e2e_units / e2e_s
 
     # dominant class and its roofline
     hbm, hbm_src = peaks()
@@ -380,13 +378,19 @@ def run_reference(a, rank, world):
     o = oracle.Oracle(case, threads=cores)
     o.set_solver(1e-8)
     o.initialize()
-    w = min(a.warmup, 1)
-    k = max(1, min(a.steps, 2))
-    for _ in range(w):
-        o.step()
+    # W warm-up and up to K timed steps of the full workload, capped so the run stays within
+    # a few minutes (each step of the 864k-particle case takes seconds on the host cores)
+    budget = 150.0
     t0 = time.perf_counter()
-    for _ in range(k):
+    w = 0
+    while w < a.warmup and time.perf_counter() - t0 < budget / 4:
         o.step()
+        w += 1
+    t0 = time.perf_counter()
+    k = 0
+    while k < a.steps and (k == 0 or time.perf_counter() - t0 < budget):
+        o.step()
+        k += 1
     dt = time.perf_counter() - t0
     v = case.n * k / dt
     return {"metric": METRIC, "value": round(v, 1), "unit": "particle-steps/s", "n_gpus": world, "steps": k,

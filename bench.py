@@ -27,6 +27,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s"
+WORKLOADS = {2: "3D weakly compressible polygon dam break (cfg2)",
+             3: "3D incompressible polygon dam break (cfg3)",
+             5: "3D incompressible dam break with obstacle, collision and shifting (cfg5)"}
 HBM_FALLBACK = 6800.0
 
 
@@ -42,6 +45,9 @@ def args_():
     a.add_argument("--warm", default="auto", choices=["auto", "prev", "mlp", "extrap"],
                    help="auto: learned if weights are present, else extrapolated")
     a.add_argument("--scale", type=float, default=1.0, help="l0 multiplier (1 = 864k particles)")
+    a.add_argument("--config", type=int, default=3, choices=[2, 3, 5],
+                   help="workload: 3 = 864k-particle incompressible dam break (the headline), "
+                        "5 = 9.375M particles with obstacle and shifting, 2 = 108k weakly compressible")
     a.add_argument("--e2e-steps", type=int, default=3)
     a.add_argument("--no-cpu-baseline", action="store_true")
     a.add_argument("--cpu-steps", type=int, default=1)
@@ -175,7 +181,7 @@ def run_gb300(a, rank, world, local):
         dist_.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     build.build()
-    case = cases.config(3, scale=a.scale)
+    case = cases.config(a.config, scale=a.scale)
     N = case.n
     if a.presort:
         p0 = mps.derive(case.mps_params(), case.n, case.pos)
@@ -275,7 +281,7 @@ def run_gb300(a, rank, world, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": ("df32" if prec == abi.PRECISION_DF32 else "f64") + ("+f32/f64 PPE" if mixed else "+f64 PPE"),
         "data": "synthetic",
-        "config": {"workload": "3D incompressible polygon dam break (cfg3)", "particles": N,
+        "config": {"workload": WORKLOADS[a.config], "particles": N,
                    "l0": case.params["partDist"], "dt": case.params["timeStep"],
                    "ppe_tol": 1e-8, "solver": a.solver, "precision": a.precision,
                    "warm_start": {abi.WARM_MLP: "learned", abi.WARM_EXTRAP: "extrapolated", abi.WARM_PREVIOUS: "previous"}[warm],
@@ -373,7 +379,7 @@ def run_reference(a, rank, world):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
-    case = cases.config(3, scale=a.scale)
+    case = cases.config(a.config, scale=a.scale)
     cores = os.cpu_count() or 1
     o = oracle.Oracle(case, threads=cores)
     o.set_solver(1e-8)
@@ -396,7 +402,7 @@ def run_reference(a, rank, world):
     return {"metric": METRIC, "value": round(v, 1), "unit": "particle-steps/s", "n_gpus": world, "steps": k,
             "warmup": w, "ms_per_step": round(dt / k * 1e3, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "3D incompressible polygon dam break (cfg3)", "particles": case.n,
+            "config": {"workload": WORKLOADS[a.config], "particles": case.n,
                        "ppe_tol": 1e-8},
             "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
                              "sample": "%d timed step(s) after %d warm-up step(s)" % (k, w)},

@@ -107,7 +107,8 @@ static int opLaunches(int op, const MpsParams& P, bool x) {
         case MPS_OP_PND_MEAN: return P.wallType == 1 ? 3 : 2;
         case MPS_OP_INIT_PND: return 2 + (P.wallType == 1 ? 3 : 2);
         case MPS_OP_CALC_PRESS: return (P.mpsType == 2) ? 2 : 1;   // assemble + copy back | EOS
-        case MPS_OP_SHIFTING:   // FP32 copies (2) + scans + apply kernels
+        case MPS_OP_SHIFTING:   // FP32 copies (2) + scans + apply kernels (DF32: two scans per sweep + copies)
+            if (x) return P.shiftingType == 1 ? 6 : (P.shiftingType == 2 ? (P.wallType == 1 ? 11 : 8) : 0);
             return P.shiftingType == 1 ? 4 : (P.shiftingType == 2 ? (P.wallType == 1 ? 8 : 5) : 0);
         case MPS_OP_DUMMY_VELOCITY: return P.wallType == 0 ? 3 : 0;
         default: return 1;
@@ -326,7 +327,10 @@ static int runOpBody(mpsgpu_t h, int op) {
             break;
         case MPS_OP_WALL_VISCOSITY: ensureMasks(h); if (x) launchWallViscosityDF(d, s); else launchWallViscosity(d, s); break;
         case MPS_OP_CORRECT: launchCorrect(d, s); invalidate(); break;
-        case MPS_OP_SHIFTING: launchShifting(d, s); if (P.shiftingType == 2) invalidate(); break;
+        case MPS_OP_SHIFTING:
+            if (x) launchShiftingDF(d, s); else launchShifting(d, s);
+            if (P.shiftingType == 2) invalidate();
+            break;
         case MPS_OP_DUMMY_VELOCITY: launchDummyVelocity(d, s); break;
         case MPS_OP_INIT_PND: ensureMasks(h); ensureCache(h); launchInitPnd(d, s); break;
         default: g_lastError = "unknown operator"; return MPSGPU_ERR_ARG;
@@ -532,6 +536,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.velHi, n);
     A(d.velLo, n);
     A(d.pressDF, n);
+    A(d.concDF, n);
     A(d.corrDF, (size_t)9 * n);
     A(d.nbrCount, n);
     A(d.nbr, (size_t)d.K * n);

@@ -67,6 +67,7 @@ struct Dev {
     int prec;                       // MPSGPU_PRECISION_*
     float4 *posLo, *posLoCell, *velHi, *velLo;
     float2* pressDF;
+    float2* concDF;                 // shifting concentration as a float-float pair
     float mgS, mgL, mgMax, mgColl, mgSide;
     // float-float (hi, lo) constants of the DF32 sweeps, converted once on the host
     struct DfK {

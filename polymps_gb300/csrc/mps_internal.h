@@ -77,6 +77,9 @@ void launchPndNeighNpcdDF(const Dev& d, cudaStream_t s);
 void launchPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallViscosityDF(const Dev& d, cudaStream_t s);
+void launchShiftingDF(const Dev& d, cudaStream_t s);
+void launchShiftVelApply(const Dev& d, cudaStream_t s);
+void launchApplyShift(const Dev& d, cudaStream_t s);
 
 // mps_wall.cu
 void launchWallDistance(const Dev& d, cudaStream_t s);

@@ -932,6 +932,8 @@ __global__ void k_apply_shift(Dev d) {
     d.posf[i] = hi;
     d.posLo[i] = posLoOf(x, hi, d.P);
 }
+void launchShiftVelApply(const Dev& d, cudaStream_t s) { k_shift_vel_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
+void launchApplyShift(const Dev& d, cudaStream_t s) { k_apply_shift<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
 void launchShifting(const Dev& d, cudaStream_t s) {
     const MpsParams& P = d.P;
     if (P.shiftingType != 1 && P.shiftingType != 2) return;

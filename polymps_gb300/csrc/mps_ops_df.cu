@@ -649,3 +649,185 @@ void launchWallViscosityDF(const Dev& d, cudaStream_t s) {
     launchVelDF(d, s);
     k_wall_visc_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
 }
+
+// ------------------------------------------------------------------ shifting
+// MpsShifting (src/MpsShifting.cpp:23-101 type 1, :432-691 type 2) at the post-corrector
+// positions through the 27 buckets.  Each sweep runs in bucket order over the listed
+// particles and once more over the unlisted ones; entries are the reS ball minus the
+// mirror side, decided exactly as in the FP64 tier.
+template <class Op, bool STRAY>
+__global__ void __launch_bounds__(BLK) k_shift_scan_df(Dev d, Op op) {
+    const int i = scanParticle<STRAY>(d);
+    if (i < 0) return;
+    typename Op::State st;
+    const bool on = op.begin(d, i, st);
+    if (on) {
+        const MpsParams& P = d.P;
+        const dvec4 pi = d.pos[i];
+        const float4 hi = d.posf[i], li = d.posLo[i];
+        const SideDF sc = sideDF(d, i, pi);
+        const df R2 = K(d.k.reS2);
+        forCellsDF(d, pi, hi, d.bandHiS, [&](int j, int s, float4 hj) {
+            if (j == i) return;
+            const float4 lj = __ldg(&d.posLoCell[s]);
+            PairF q = pairDF(hj, lj, hi, li);
+            if (!inBallDF(d, q.d2, R2, d.mgS, P.reS2, i, j)) return;
+            if (!sideOkDF(d, sc, hj, lj, q.d2, i, j)) return;
+            op.visit(d, st, j, q);
+        });
+    }
+    op.end(d, i, st, on);
+}
+template <class Op>
+static void launchShiftScanDF(const Dev& d, const Op& op, cudaStream_t s) {
+    k_shift_scan_df<Op, false><<<gridFor(d.N0, BLK), BLK, 0, s>>>(d, op);
+    k_shift_scan_df<Op, true><<<gridFor(d.N0, BLK), BLK, 0, s>>>(d, op);
+}
+
+// dw/dr of MpsParticle::delWeight (src/MpsParticle.cpp) from r^2, float-float
+__device__ __forceinline__ df dweightDF(df d2, const RadiusDF& R, int t) {
+    df rinv = rsqrtDF(d2);
+    switch (t) {
+        case 1: return -(R.re * (rinv * rinv)) + R.invRe;
+        case 2: return -(R.re * (rinv * rinv)) - R.invRe;
+        case 3: { df a = -(d2 * rinv * R.invRe) + 1.0f; return (a * a) * (R.invRe * -3.0f); }
+        case 4: { df a = -(d2 * rinv * R.invRe) + 1.0f; return a * (R.invRe * -2.0f); }
+        default: return -(R.re * (rinv * rinv));
+    }
+}
+
+// type 1: dv_i = sum dw(r_ij) (v_j - v_i) over fluid particles, applied to inner ones
+struct ShiftVelDF {
+    struct State { float4 vh, vl; df ux, uy, uz; };
+    __device__ bool begin(const Dev& d, int i, State& st) const {
+        st.vh = d.velHi[i]; st.vl = d.velLo[i];
+        st.ux = st.uy = st.uz = dfF(0.f);
+        return d.type[i] == d.P.fluid;
+    }
+    __device__ void visit(const Dev& d, State& st, int j, const PairF& q) const {
+        const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
+        df dw = dweightDF(q.d2, RS, d.P.weightType);
+        float4 vhj = d.velHi[j], vlj = d.velLo[j];
+        st.ux += diffDF(vhj.x, vlj.x, st.vh.x, st.vl.x) * dw;
+        st.uy += diffDF(vhj.y, vlj.y, st.vh.y, st.vl.y) * dw;
+        st.uz += diffDF(vhj.z, vlj.z, st.vh.z, st.vl.z) * dw;
+    }
+    __device__ void end(const Dev& d, int i, State& st, bool on) const {
+        bool apply = on && d.bc[i] == d.P.inner;
+        d.shift[i] = apply ? make_dvec4(dD(st.ux), dD(st.uy), dD(st.uz), 0.0) : make_dvec4(0, 0, 0, 0);
+    }
+};
+// type 2, concentration: C_i = (sum w(r_ij) + wall PND) / pndSmallZero, every particle
+struct ConcDF {
+    struct State { df sum; };
+    __device__ bool begin(const Dev&, int, State& st) const { st.sum = dfF(0.f); return true; }
+    __device__ void visit(const Dev& d, State& st, int, const PairF& q) const {
+        const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
+        st.sum += weightDF(q.d2, RS, d.P.weightType).w;
+    }
+    __device__ void end(const Dev& d, int i, State& st, bool) const {
+        d.conc[i] = (dD(st.sum) + d.pndWall[i]) / d.P.pndSmallZero;
+    }
+};
+__global__ void k_df_conc(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.N0) return;
+    df c = dfD(d.conc[i]);
+    d.concDF[i] = make_float2(c.h, c.l);
+}
+// type 2, gradient: grad C_i = -coeffPressGrad sum (C_i + C_j) w/r^2 r_ij over fluid
+// particles; the shift of inner particles is -coeffShifting2 grad C_i
+struct GradConcDF {
+    struct State { df ci, gx, gy, gz; };
+    __device__ bool begin(const Dev& d, int i, State& st) const {
+        st.ci = loadDF(d.concDF, i);
+        st.gx = st.gy = st.gz = dfF(0.f);
+        return d.type[i] == d.P.fluid;
+    }
+    __device__ void visit(const Dev& d, State& st, int j, const PairF& q) const {
+        const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
+        df cc = (st.ci + loadDF(d.concDF, j)) * weightDF(q.d2, RS, d.P.weightType).wr2;
+        st.gx += q.v.x * cc; st.gy += q.v.y * cc; st.gz += q.v.z * cc;
+    }
+    __device__ void end(const Dev& d, int i, State& st, bool on) const {
+        const MpsParams& P = d.P;
+        dvec4 sh = make_dvec4(0, 0, 0, 0);
+        if (on) {
+            double gx = dD(st.gx) * -P.coeffPressGrad, gy = dD(st.gy) * -P.coeffPressGrad,
+                   gz = dD(st.gz) * -P.coeffPressGrad;
+            d.gradC[i] = make_dvec4(gx, gy, gz, 0.0);
+            if (d.bc[i] == P.inner)
+                sh = make_dvec4(-P.coeffShifting2 * gx, -P.coeffShifting2 * gy, -P.coeffShifting2 * gz, 0.0);
+        }
+        d.shift[i] = sh;
+    }
+};
+// type 2, wall contribution (src/MpsShifting.cpp:578-691) at the shifted positions:
+// mirror entries of near-wall fluid particles, reflected by the wall plane of i.
+__global__ void __launch_bounds__(BLK) k_wall_grad_conc_df(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 sh = make_dvec4(0, 0, 0, 0);
+    if (d.type[i] == P.fluid && d.nearWall[i]) {
+        dvec4 pi = d.pos[i], mi = d.mirror[i];
+        ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
+        const float4 hi = d.posf[i], li = d.posLo[i];
+        const MirrorDF M = mirrorDF(d, mi);
+        const df R2 = K(d.k.reS2);
+        const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
+        const df ci = loadDF(d.concDF, i);
+        df sx = dfF(0.f), sy = dfF(0.f), sz = dfF(0.f);
+        forCellsDF(d, pi, hi, d.bandHiS, [&](int j, int s, float4 hj) {
+            if (j == i) return;
+            const float4 lj = __ldg(&d.posLoCell[s]);
+            PairF q = pairDF(hj, lj, hi, li);
+            if (!inBallDF(d, q.d2, R2, d.mgS, P.reS2, i, j)) return;
+            PairF m = pairDF(hj, lj, M.mh, M.ml);
+            if (!lessDF(m.d2, R2, d.mgS, [&] { return pairMirror(d.pos[j], mi).dm2 < P.reS2; })) return;
+            if (!lessDF(q.d2, m.d2, d.mgSide, [&] {
+                    dvec4 pj = d.pos[j];
+                    return pairOf(pj, pi).d2 < pairMirror(pj, mi).dm2;
+                }))
+                return;
+            df cc = (ci + loadDF(d.concDF, j)) * weightDF(m.d2, RS, P.weightType).wr2;
+            sx += m.v.x * cc; sy += m.v.y * cc; sz += m.v.z * cc;
+        });
+        double dx = dD(sx), dy = dD(sy), dz = dD(sz);
+        double cI = d.conc[i];
+        PairM s = pairMirror(pi, mi);
+        if (s.dm2 < P.reS2) {
+            double wS = wfun(sqrt(s.dm2), P.reS, P.weightType);
+            dx += (cI + cI) * s.m0 * wS / s.dm2; dy += (cI + cI) * s.m1 * wS / s.dm2; dz += (cI + cI) * s.m2 * wS / s.dm2;
+        }
+        double g0 = -(r.R[0] * dx + r.R[1] * dy + r.R[2] * dz) * P.coeffPressGrad;
+        double g1 = -(r.R[3] * dx + r.R[4] * dy + r.R[5] * dz) * P.coeffPressGrad;
+        double g2 = -(r.R[6] * dx + r.R[7] * dy + r.R[8] * dz) * P.coeffPressGrad;
+        dvec4 g = d.gradC[i];
+        g.x += g0; g.y += g1; g.z += g2;
+        d.gradC[i] = g;
+        if (d.bc[i] == P.inner)
+            sh = make_dvec4(-P.coeffShifting2 * g0, -P.coeffShifting2 * g1, -P.coeffShifting2 * g2, 0.0);
+    }
+    d.shift[i] = sh;
+}
+void launchShiftingDF(const Dev& d, cudaStream_t s) {
+    const MpsParams& P = d.P;
+    if (P.shiftingType != 1 && P.shiftingType != 2) return;
+    launchPosf(d, s);   // post-corrector positions (hi/lo, particle and bucket order)
+    if (P.shiftingType == 1) {
+        launchVelDF(d, s);
+        launchShiftScanDF(d, ShiftVelDF(), s);
+        launchShiftVelApply(d, s);
+        return;
+    }
+    launchShiftScanDF(d, ConcDF(), s);
+    k_df_conc<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    launchShiftScanDF(d, GradConcDF(), s);
+    launchApplyShift(d, s);
+    if (P.wallType == 1) {
+        launchPosfCell(d, s);   // the wall sweep sees the shifted positions
+        k_wall_grad_conc_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+        launchApplyShift(d, s);
+    }
+}

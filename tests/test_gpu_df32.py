@@ -185,3 +185,36 @@ def test_mixed_inner_operators(oracle_mod, mps_lib, precision, inner):
         out[solver] = g.get(abi.F_PRESS)
         g.close()
     assert relerr(out[inner], out[abi.SOLVER_PLAIN_FP64]) < 1e-6
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_DF32])
+@pytest.mark.parametrize("stype", [1, 2])
+def test_shifting_parity(oracle_mod, mps_lib, stype, precision):
+    """Particle shifting (type 1: velocity correction; type 2: concentration gradient with
+    the polygon-wall term) from an identical post-corrector state, tank with obstacle."""
+    from polymps_gb300 import mps
+    c = cases.config(5, jitter=0.02, scale=6.0)
+    c.params.update(shiftingType=stype)
+    o = oracle_mod.Oracle(c)
+    g = mps.MpsGpu(c, tol=1e-12, precision=precision)
+    o.set_solver(1e-12)
+    o.initialize()
+    for _ in range(4):
+        o.step()
+    ops = step_ops(o.params)
+    # both sides scan the bucket list of the start-of-step positions
+    sync(o, g)
+    o.run_op("UPDATE_BUCKETS")
+    g.run_op("UPDATE_BUCKETS")
+    for op in ops[1: ops.index("SHIFTING")]:
+        o.run_op(op)
+    assert o.n == g.n
+    sync(o, g)
+    f = abi.F_POS if stype == 2 else abi.F_VEL
+    before = o.get(f)
+    o.run_op("SHIFTING")
+    g.run_op("SHIFTING")
+    assert np.abs(o.get(f) - before).max() > 0.0   # the sweep moved something
+    compare(o, g, "shifting %d" % stype, rtol=DF_RTOL if precision == abi.PRECISION_DF32 else 1e-10)
+    g.close()
+    o.close()

@@ -24,6 +24,7 @@ CASES = {
     "cfg1_2d_particle_walls": lambda: cases.config(1, jitter=0.02),
     "cfg2_3d_wc_polygon": lambda: cases.config(2, jitter=0.02, scale=3.0),
     "cfg3_3d_inc_polygon": lambda: cases.config(3, jitter=0.02, scale=5.0),
+    "cfg5_3d_obstacle_shifting": lambda: cases.config(5, jitter=0.02, scale=6.0),
 }
 
 

@@ -315,12 +315,15 @@ def ppe_compare(g, abi, use_mlp):
     x_prev2 = g.get(abi.F_PRESSPPE_PREV)
     res = {}
     # single-launch solves, then the per-kernel launch path for reference
-    # launch mode: 1 single launch (default), 2 single launch with staged ELL tiles, 0 per kernel
+    # launch mode: 1 single launch (default), 2 single launch with staged ELL tiles, 3 single
+    # launch with the pipelined inner CG, 0 per kernel
     variants = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 1),
                 ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 1),
                 ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, 1),
                 ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 1),
                 ("extrapolated_fp32_fp64_staged_tiles", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 2),
+                ("fp32_fp64_pipelined", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 3),
+                ("extrapolated_fp32_fp64_pipelined", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 3),
                 ("matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_PREVIOUS, 1),
                 ("compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_PREVIOUS, 1),
                 ("extrapolated_compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_EXTRAP, 1)]

@@ -232,15 +232,17 @@ int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm_start, double tol, int ma
  * and keeps every discrete decision (neighbour radius, mirror side, collision sign) equal
  * to the reference's by deciding in FP64 whenever the float-float value lies within its
  * error margin; per-particle results differ from FP64 by ~1e-11 relative.  Operators
- * without a DF32 kernel (diffusive/mean PND, extrapolation, shifting, dummy velocity,
- * step-0 PND) run their FP64 kernels in either mode. */
+ * without a DF32 kernel (diffusive/mean PND, extrapolation, dummy velocity, step-0 PND)
+ * run their FP64 kernels in either mode. */
 /* How the PPE solve is launched: 0 one launch per kernel with the host polling
  * convergence every few iterations; 1 (default) the whole solve in one cooperative launch
  * with device-side grid barriers; 2 as 1, with the mixed solver's FP32 matrix streamed
  * through shared memory by bulk copies (measured slower than 1 at 864k rows: the SpMV
- * is bound by the neighbour gathers of z, not by the matrix stream).  Same algorithm
- * and results to rounding.
- * Modes 1 and 2 fall back to the previous mode where the device does not support them. */
+ * is bound by the neighbour gathers of z, not by the matrix stream); 3 as 1, with the
+ * mixed solver's inner CG in the pipelined form (one grid reduction per iteration instead
+ * of two, Ghysels & Vanroose 2014) and the refinement residual formed in the same pass as
+ * the iterate update.  Same method and results to the solver tolerance.
+ * Modes 1 to 3 fall back to the previous modes where the device does not support them. */
 int mpsgpu_set_ppe_launch(mpsgpu_t h, int mode);
 
 #define MPSGPU_PRECISION_FP64  0

@@ -237,9 +237,11 @@ static int calcPress(mpsgpu_t h) {
     h->B.prepared = df32(h) ? 1 : 0;   // the DF32 assembly writes the FP32 copies itself
     h->B.matfree = h->solver == MPSGPU_SOLVER_MIXED_MATFREE ? 1 : (h->solver == MPSGPU_SOLVER_MIXED_COMPACT ? 2 : 0);
     if (h->solver == MPSGPU_SOLVER_MIXED && h->persistent == 2 && h->B.pgridTs > 0) h->B.matfree = 3;
+    if (h->solver == MPSGPU_SOLVER_MIXED && h->persistent == 3 && h->B.pgridPipe > 0) h->B.matfree = 4;
     int pgrid = !mixed ? h->B.pgridCg
-                       : (h->B.matfree == 3 ? h->B.pgridTs
-                                            : (h->B.matfree == 2 ? h->B.pgridH16 : (h->B.matfree ? h->B.pgridMf : h->B.pgridMx)));
+                       : (h->B.matfree == 4 ? h->B.pgridPipe
+                          : h->B.matfree == 3 ? h->B.pgridTs
+                                              : (h->B.matfree == 2 ? h->B.pgridH16 : (h->B.matfree ? h->B.pgridMf : h->B.pgridMx)));
     if (h->B.matfree && (!h->persistent || pgrid <= 0)) {
         g_lastError = "this mixed inner operator needs the single-launch (cooperative) PPE solve";
         return MPSGPU_ERR_UNSUPPORTED;
@@ -636,12 +638,13 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         A(B.col, ell);
         A(B.rowLen, n);
         A(B.valf, ell);
-        for (float** v : {&B.diagf, &B.diagInvf, &B.rf, &B.zf, &B.pf, &B.Apf, &B.xf}) A(*v, n);
+        for (float** v : {&B.diagf, &B.diagInvf, &B.rf, &B.zf, &B.pf, &B.Apf, &B.xf, &B.wf, &B.qzf, &B.mf2}) A(*v, n);
+        A(B.xalt, n);
         B.pgridCg = ppePersistentGrid(0);
         B.pgridMx = ppePersistentGrid(1);
         A(B.scal, 16);
-        A(B.partials, 4 * std::max(std::max(std::max(B.nblocks, ppePersistentGrid(4)), ppePersistentGrid(3)),
-                                   std::max(B.pgridCg, std::max(B.pgridMx, ppePersistentGrid(2)))));
+            A(B.partials, 4 * std::max(std::max(std::max(B.nblocks, ppePersistentGrid(4)), ppePersistentGrid(3)),
+                                   std::max(std::max(B.pgridCg, ppePersistentGrid(5)), std::max(B.pgridMx, ppePersistentGrid(2)))));
         A(B.counter, 1);
         A(B.flag, 8);
         A(B.dinv, n);
@@ -649,6 +652,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         B.pgridMf = ppePersistentGrid(2);
         B.pgridH16 = ppePersistentGrid(3);
         B.pgridTs = ppePersistentGrid(4);
+        B.pgridPipe = ppePersistentGrid(5);
         // the staged tiles keep up to 128 tile lengths per block in shared memory
         if (B.pgridTs > 0 && (n + 255) / 256 > 128 * B.pgridTs) B.pgridTs = 0;
         A(B.valh, ell);
@@ -767,7 +771,7 @@ int mpsgpu_set_precision(mpsgpu_t h, int precision) {
 }
 
 int mpsgpu_set_ppe_launch(mpsgpu_t h, int mode) {
-    if (!h || mode < 0 || mode > 2) return MPSGPU_ERR_ARG;
+    if (!h || mode < 0 || mode > 3) return MPSGPU_ERR_ARG;
     h->persistent = mode;
     return 0;
 }

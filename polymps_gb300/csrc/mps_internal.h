@@ -100,7 +100,8 @@ struct PpeBuffers {
     int pgridCg, pgridMx;    // co-resident grid sizes of the persistent solvers (0: unavailable)
     int prepared;            // FP32 copies (valf, diagf, diagInvf) already written by the assembly
     unsigned long long* mfMask;   // per row: neighbour-list entries that are matrix entries
-    int matfree;             // mixed inner operator: 0 assembled FP32, 1 matrix-free, 2 compact scaled
+    int matfree;             // mixed inner operator: 0 assembled FP32, 1 matrix-free, 2 compact scaled,
+                             // 3 staged tiles, 4 assembled FP32 with the pipelined inner CG
     int pgridMf;             // co-resident grid of the matrix-free mixed solver
     __half* valh;            // compact scaled operator: FP16 off-diagonals of diag(sigma s) A diag(s)
     short* col16;            // and their column offsets j - i
@@ -108,6 +109,11 @@ struct PpeBuffers {
     unsigned char* wideRow;  // rows with an offset outside 16 bits (read the 32-bit columns)
     int pgridH16;
     int pgridTs;             // co-resident grid of the mixed solver with the staged ELL tiles (0: none)
+    // pipelined inner CG: w = A u and z = A q recurrences, second buffer of m = M w, and the
+    // second FP64 iterate of the refinement
+    float *wf, *qzf, *mf2;
+    double* xalt;
+    int pgridPipe;
 };
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);

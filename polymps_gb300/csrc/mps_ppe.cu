@@ -156,6 +156,23 @@ __device__ __forceinline__ void gridSum(double (&v)[NV], const PpeBuffers& B, Fi
 // together, then the eight gathers; the last chunk is masked (predicated loads, the row's
 // own index as a harmless column) instead of a serial remainder loop.  RO: the gathered
 // vector is read-only for the launch (non-coherent cache path); otherwise plain loads.
+// Matrix streams are read once per SpMV: loaded without L1 allocation, so L1 keeps the
+// lines of the gathered vector (the neighbours of a block's rows reuse them).
+__device__ __forceinline__ int ldStream(const int* p) {
+    int v;
+    asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ float ldStream(const float* p) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ double ldStream(const double* p) {
+    double v;
+    asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+}
 #define ELL_U 8
 template <class T, bool RO>
 __device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col, const T* x, int i, int len, size_t N0) {
@@ -178,8 +195,8 @@ __device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col,
 #pragma unroll
         for (int u = 0; u < ELL_U; u++) {
             bool ok = k + u < len;
-            cc[u] = ok ? __ldg(c + (size_t)(k + u) * N0) : i;
-            vv[u] = ok ? __ldg(v + (size_t)(k + u) * N0) : T(0);
+            cc[u] = ok ? ldStream(c + (size_t)(k + u) * N0) : i;
+            vv[u] = ok ? ldStream(v + (size_t)(k + u) * N0) : T(0);
         }
 #pragma unroll
         for (int u = 0; u < ELL_U; u++) acc[u] += vv[u] * (RO ? __ldg(x + cc[u]) : x[cc[u]]);
@@ -843,8 +860,11 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
     const int n = liveN(d);
     const float cP = (float)d.P.coeffPPE, re = (float)d.P.reL, invRe = (float)(1.0 / d.P.reL);
     const int wt = d.P.weightType;
+    // grid-stride rows: at any moment the blocks work on one contiguous window of rows,
+    // so the column slices of the ELL arrays stream through DRAM pages in order
     const int T = gridDim.x * QB;
     const int t0 = blockIdx.x * QB + threadIdx.x;
+    const int r1 = n;
     QCtl c = {0u};
     // staged tiles: the block's tile lengths and the mbarriers of the ring
     TsSmem& sm = *reinterpret_cast<TsSmem*>(dynSmem);
@@ -872,14 +892,14 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
     }
     if (OP == OP_H16) {
         // scaling, then the compact copy of the FP32 matrix
-        for (int i = t0; i < n; i += T) {
+        for (int i = t0; i < r1; i += T) {
             double dd = __ldg(B.diag + i);
             double sc = 1.0 / sqrt(fabs(dd));
             B.sclf[i] = (float)sc;
             B.sgs[i] = (float)(dd < 0.0 ? -sc : sc);
         }
         if (!qBarrier(B, c)) return;
-        forRows(B, n, t0, T, [&](int i, int len) {
+        forRows(B, r1, t0, T, [&](int i, int len) {
             const float si = B.sgs[i];
             unsigned char wide = 0;
             for (int k = 0; k < len; k++) {
@@ -896,7 +916,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
     }
     {
         double v[2] = {0.0, 0.0};
-        forRows(B, n, t0, T, [&](int i, int len) {
+        forRows(B, r1, t0, T, [&](int i, int len) {
             double r = B.b[i] - qRow(B, B.x, i, len);
             B.r[i] = r;
             v[0] += r * r;
@@ -925,7 +945,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
         {
             const double inv = vd(B.scal + S_INV);
             df a[2] = {dfF(0.f), dfF(0.f)};
-            for (int i = t0; i < n; i += T) {
+            for (int i = t0; i < r1; i += T) {
                 float r = (float)(B.r[i] * inv);
                 if (OP == OP_H16) r *= B.sgs[i];
                 float z = (OP == OP_H16) ? r : r * __ldg(B.diagInvf + i);
@@ -950,7 +970,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                         a[0] += prod2(p, ap);
                     });
                     (void)okp;   // an ran-out wait sets the abort word: the reduction below returns false
-                } else forRows(B, n, t0, T, [&](int i, int len) {
+                } else forRows(B, r1, t0, T, [&](int i, int len) {
                     float q = (OP == OP_MATFREE) ? mfRowF(d, B, B.zf, i, cP, re, invRe, wt)
                             : (OP == OP_H16)   ? h16Row(B, B.zf, i, len)
                                                : qRowF(B, B.zf, i, len);
@@ -966,7 +986,7 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
             {
                 const float alpha = (float)vd(B.scal + S_ALPHA);
                 df a[2] = {dfF(0.f), dfF(0.f)};
-                for (int i = t0; i < n; i += T) {
+                for (int i = t0; i < r1; i += T) {
                     B.xf[i] += alpha * B.pf[i];
                     float r = B.rf[i] - alpha * B.Apf[i];
                     float z = (OP == OP_H16) ? r : r * __ldg(B.diagInvf + i);
@@ -988,13 +1008,13 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
         total += inner;
         {
             const double sc = vd(B.scal + S_SQRT);
-            for (int i = t0; i < n; i += T)
+            for (int i = t0; i < r1; i += T)
                 B.x[i] += sc * (double)((OP == OP_H16) ? B.xf[i] * B.sclf[i] : B.xf[i]);
             if (!qBarrier(B, c)) return;
         }
         {
             double v[1] = {0.0};
-            forRows(B, n, t0, T, [&](int i, int len) {
+            forRows(B, r1, t0, T, [&](int i, int len) {
                 double r = B.b[i] - qRow(B, B.x, i, len);
                 B.r[i] = r;
                 v[0] += r * r;
@@ -1014,16 +1034,191 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
     }
 }
 
-// Plain FP64 Jacobi-PCG (Eigen's ConjugateGradient with its diagonal preconditioner,
-// src/MpsPressure.cpp:424-445): z = invdiag * r, stop when ||r||^2 < tol^2 ||b||^2.
-__global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double tol, int maxIter) {
+// FP64 residual row of the refinement without a pass in between: x_j + d_j is formed from
+// the FP64 iterate and the FP32 correction of the inner solve as the owner of j forms it.
+__device__ __forceinline__ double qRowPlus(const PpeBuffers& B, const double* x, const float* dx, int i, int len) {
+    double acc[ELL_U];
+#pragma unroll
+    for (int u = 0; u < ELL_U; u++) acc[u] = 0.0;
+    const double* v = B.val + i;
+    const int* c = B.col + i;
+    const size_t N0 = B.N0;
+    for (int k = 0; k < len; k += ELL_U) {
+        int cc[ELL_U];
+        double vv[ELL_U];
+#pragma unroll
+        for (int u = 0; u < ELL_U; u++) {
+            bool ok = k + u < len;
+            cc[u] = ok ? ldStream(c + (size_t)(k + u) * N0) : i;
+            vv[u] = ok ? ldStream(v + (size_t)(k + u) * N0) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < ELL_U; u++) acc[u] += vv[u] * (x[cc[u]] + (double)dx[cc[u]]);
+    }
+    return __ldg(B.diag + i) * (x[i] + (double)dx[i]) +
+           (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
+}
+
+// Mixed solver with the pipelined inner CG (Ghysels & Vanroose, "Hiding global
+// synchronization latency in the preconditioned Conjugate Gradient algorithm", Parallel
+// Computing 40, 2014, Alg. 3), Jacobi M = diag^-1 applied on the fly: with u = M r,
+// q = M s and m = M w recomputed from r, s and w, the recurrences kept are
+//   z = A m + beta z,  s = w + beta s,  p = M r + beta p,  x += alpha p,
+//   r -= alpha s,      w -= alpha z,    m' = M w
+// and the three dot products (r.u, w.u, r.r) of the next iteration are summed in the same
+// pass: one grid barrier per inner iteration (the standard form needs two).  m is double
+// buffered (its owner writes m' while neighbours gather m).  The FP64 refinement forms
+// r = b - A (x + d) in the pass that stores x + d into the other FP64 buffer, and starts
+// the next inner solve there (u0 = M r), so a refinement costs two barriers.
+__global__ void __launch_bounds__(QB, 4) k_mx_pipe(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
     const int n = liveN(d);
     const int T = gridDim.x * QB;
     const int t0 = blockIdx.x * QB + threadIdx.x;
     QCtl c = {0u};
+    double* xa = B.x;      // current FP64 iterate
+    double* xb = B.xalt;   // the next one
+    float* mA = B.zf;      // u0, then m of odd iterations
+    float* mB = B.mf2;     // m of even iterations
+    {
+        double v[2] = {0.0, 0.0};
+        forRows(B, n, t0, T, [&](int i, int len) {
+            double r = B.b[i] - qRow(B, xa, i, len);
+            B.r[i] = r;
+            float rf = (float)r;
+            B.rf[i] = rf;
+            mA[i] = rf * __ldg(B.diagInvf + i);
+            v[0] += r * r;
+            v[1] += B.b[i] * B.b[i];
+        });
+        if (!qSum<2>(v, B, c, [&](const double* t) {
+                B.scal[S_RR] = t[0];
+                B.scal[S_BB] = t[1];
+                double thr = tol * tol * t[1];
+                if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
+                B.scal[S_THR] = thr;
+                B.scal[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
+                B.scal[S_ETA2] = fmax(eta2, 0.25 * thr / t[0]);
+                B.flag[0] = (t[1] == 0.0 || t[0] < thr) ? 1 : 0;
+                B.flag[1] = 0;
+                if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
+            }))
+            return;
+    }
+    int total = 0, refine = 0;
+    while (!vi(B.flag) && total < maxIter && refine <= 20) {
+        // inner start: w0 = A u0, m0 = M w0; gamma0 = r.u, delta0 = w.u, rho0 = r.r
+        {
+            df a[3] = {dfF(0.f), dfF(0.f), dfF(0.f)};
+            forRows(B, n, t0, T, [&](int i, int len) {
+                const float w = qRowF(B, mA, i, len);
+                const float u = mA[i], r = B.rf[i];
+                B.wf[i] = w;
+                mB[i] = w * __ldg(B.diagInvf + i);
+                a[0] += prod2(r, u);
+                a[1] += prod2(w, u);
+                a[2] += prod2(r, r);
+            });
+            if (!qSumDF<3>(a, B, c, [&](const double* t) {
+                    B.flag[3] = 0;
+                    B.scal[S_RZ] = t[0];
+                    B.scal[S_RR0] = t[2];
+                    B.scal[S_BETA] = 0.0;
+                    // the PPE matrix and its Jacobi preconditioner are negative definite:
+                    // r.u and w.u share their sign and alpha > 0
+                    const double al = t[0] / t[1];
+                    if (al > 0.0 && al < 1e300) B.scal[S_ALPHA] = al;
+                    else B.flag[3] = 1;   // zero residual or breakdown: nothing to solve
+                }))
+                return;
+        }
+        int inner = 0;
+        while (!vi(B.flag + 3) && total + inner < maxIter && inner < 400) {
+            const float alpha = (float)vd(B.scal + S_ALPHA), beta = (float)vd(B.scal + S_BETA);
+            const float* mc = (inner & 1) ? mA : mB;
+            float* mn = (inner & 1) ? mB : mA;
+            const bool first = inner == 0;
+            df a[3] = {dfF(0.f), dfF(0.f), dfF(0.f)};
+            forRows(B, n, t0, T, [&](int i, int len) {
+                const float an = qRowF(B, mc, i, len);   // A m
+                const float di = __ldg(B.diagInvf + i);
+                float w = B.wf[i], r = B.rf[i];
+                float z = first ? an : an + beta * B.qzf[i];
+                float sv = first ? w : w + beta * B.Apf[i];
+                float p = first ? r * di : r * di + beta * B.pf[i];
+                float x = first ? alpha * p : B.xf[i] + alpha * p;
+                r -= alpha * sv;
+                w -= alpha * z;
+                B.qzf[i] = z; B.Apf[i] = sv; B.pf[i] = p; B.xf[i] = x;
+                B.rf[i] = r; B.wf[i] = w;
+                const float u = r * di;
+                mn[i] = w * di;
+                a[0] += prod2(r, u);
+                a[1] += prod2(w, u);
+                a[2] += prod2(r, r);
+            });
+            if (!qSumDF<3>(a, B, c, [&](const double* t) {
+                    B.flag[1] += 1;
+                    if (t[2] < B.scal[S_ETA2] * B.scal[S_RR0] || !(t[2] == t[2])) { B.flag[3] = 1; return; }
+                    const double g0 = B.scal[S_RZ], al = B.scal[S_ALPHA];
+                    const double bt = t[0] / g0;
+                    const double aln = t[0] / (t[1] - bt * t[0] / al);
+                    if (!(aln > 0.0 && aln < 1e300 && bt >= 0.0)) { B.flag[3] = 1; return; }
+                    B.scal[S_BETA] = bt;
+                    B.scal[S_ALPHA] = aln;
+                    B.scal[S_RZ] = t[0];
+                }))
+                return;
+            inner++;
+        }
+        total += inner;
+        // refinement: x' = x + d into the other buffer, r = b - A x', next inner start u0
+        {
+            const bool any = inner > 0;
+            double v[1] = {0.0};
+            forRows(B, n, t0, T, [&](int i, int len) {
+                double r;
+                if (any) {
+                    xb[i] = xa[i] + (double)B.xf[i];
+                    r = B.b[i] - qRowPlus(B, xa, B.xf, i, len);
+                } else {
+                    xb[i] = xa[i];
+                    r = B.r[i];
+                }
+                B.r[i] = r;
+                float rf = (float)r;
+                B.rf[i] = rf;
+                mA[i] = rf * __ldg(B.diagInvf + i);
+                v[0] += r * r;
+            });
+            if (!qSum<1>(v, B, c, [&](const double* t) {
+                    B.scal[S_RR] = t[0];
+                    B.scal[S_ETA2] = fmax(eta2, 0.25 * B.scal[S_THR] / t[0]);
+                    if (t[0] < B.scal[S_THR]) B.flag[0] = 1;
+                    if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
+                    B.flag[4] += 1;
+                }))
+                return;
+            double* tx = xa; xa = xb; xb = tx;
+        }
+        refine++;
+    }
+    if (xa != B.x)
+        for (int i = t0; i < n; i += T) B.x[i] = xa[i];
+}
+
+// Plain FP64 Jacobi-PCG (Eigen's ConjugateGradient with its diagonal preconditioner,
+// src/MpsPressure.cpp:424-445): z = invdiag * r, stop when ||r||^2 < tol^2 ||b||^2.
+__global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double tol, int maxIter) {
+    const int n = liveN(d);
+    // grid-stride rows: at any moment the blocks work on one contiguous window of rows,
+    // so the column slices of the ELL arrays stream through DRAM pages in order
+    const int T = gridDim.x * QB;
+    const int t0 = blockIdx.x * QB + threadIdx.x;
+    const int r1 = n;
+    QCtl c = {0u};
     {
         double v[3] = {0.0, 0.0, 0.0};
-        forRows(B, n, t0, T, [&](int i, int len) {
+        forRows(B, r1, t0, T, [&](int i, int len) {
             double di = 1.0 / __ldg(B.diag + i);
             double r = B.b[i] - qRow(B, B.x, i, len);
             double z = r * di;
@@ -1047,7 +1242,7 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
         {
             const double beta = it ? vd(B.scal + S_BETA) : 0.0;
             double v[1] = {0.0};
-            forRows(B, n, t0, T, [&](int i, int len) {
+            forRows(B, r1, t0, T, [&](int i, int len) {
                 double q = qRow(B, B.z, i, len);
                 double z = B.z[i];
                 double ap = it ? q + beta * B.Ap[i] : q;
@@ -1061,7 +1256,7 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
         {
             const double alpha = vd(B.scal + S_ALPHA);
             double v[2] = {0.0, 0.0};
-            for (int i = t0; i < n; i += T) {
+            for (int i = t0; i < r1; i += T) {
                 B.x[i] += alpha * B.p[i];
                 double r = B.r[i] - alpha * B.Ap[i];
                 double z = r * B.dinv[i];
@@ -1083,7 +1278,7 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
     if (!qBarrier(B, c)) return;
     {
         double v[1] = {0.0};
-        forRows(B, n, t0, T, [&](int i, int len) {
+        forRows(B, r1, t0, T, [&](int i, int len) {
             double r = B.b[i] - qRow(B, B.x, i, len);
             v[0] += r * r;
         });
@@ -1092,7 +1287,8 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
 }
 
 // kind: 0 plain FP64, 1 mixed, 2 mixed with the matrix-free inner operator, 3 mixed with
-// the compact scaled inner operator, 4 mixed with the staged tiles
+// the compact scaled inner operator, 4 mixed with the staged tiles, 5 mixed with the
+// pipelined inner CG
 int ppePersistentGrid(int kind) {
     int dev = 0, sms = 0, coop = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
@@ -1108,7 +1304,8 @@ int ppePersistentGrid(int kind) {
             return 0;
         return per * sms;
     }
-    cudaError_t e = kind == 3   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_H16>, QB, 0)
+    cudaError_t e = kind == 5   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_pipe, QB, 0)
+                    : kind == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_H16>, QB, 0)
                     : kind == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_MATFREE>, QB, 0)
                     : kind == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_ELL32>, QB, 0)
                                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_solve, QB, 0);
@@ -1139,7 +1336,9 @@ static int finishPersistent(const PpeBuffers& B, cudaStream_t s, int* iters, int
 int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol, int maxIter, cudaStream_t s,
                        int* iters, int* refinements, double* relres, double* relres0, Prof* prof) {
     int grid = !mixed ? B.pgridCg
-                      : (B.matfree == 3 ? B.pgridTs : (B.matfree == 2 ? B.pgridH16 : (B.matfree ? B.pgridMf : B.pgridMx)));
+                      : (B.matfree == 4 ? B.pgridPipe
+                                        : (B.matfree == 3 ? B.pgridTs
+                                                          : (B.matfree == 2 ? B.pgridH16 : (B.matfree ? B.pgridMf : B.pgridMx))));
     if (grid <= 0) return MPSGPU_ERR_UNSUPPORTED;
     bool pr = prof && prof->on;
     cudaMemsetAsync(B.flag, 0, 5 * sizeof(int), s);
@@ -1157,6 +1356,7 @@ int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol,
     void* args[5] = {&dd, &bb, &t, &mi, &eta2};
     if (pr) prof->begin(PROF_PPE_SOLVE, s);
     const void* fn = !mixed              ? (const void*)k_cg_solve
+                     : B.matfree == 4    ? (const void*)k_mx_pipe
                      : B.matfree == 3    ? (const void*)k_mx_solve<OP_TILED>
                      : B.matfree == 2    ? (const void*)k_mx_solve<OP_H16>
                      : B.matfree == 1    ? (const void*)k_mx_solve<OP_MATFREE>

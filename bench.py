@@ -43,7 +43,8 @@ def args_():
     a.add_argument("--precision", default="df32", choices=["df32", "fp64"],
                    help="neighbour-sweep arithmetic: float-float (df32) or FP64")
     a.add_argument("--warm", default="auto", choices=["auto", "prev", "mlp", "extrap"],
-                   help="auto: learned if weights are present, else extrapolated")
+                   help="auto: extrapolated (the fastest measured); the learned start is timed in the "
+                        "PPE comparison when its weights are present")
     a.add_argument("--scale", type=float, default=1.0, help="l0 multiplier (1 = 864k particles)")
     a.add_argument("--config", type=int, default=3, choices=[2, 3, 5],
                    help="workload: 3 = 864k-particle incompressible dam break (the headline), "
@@ -192,13 +193,15 @@ def run_gb300(a, rank, world, local):
     solver = {"mixed": abi.SOLVER_MIXED, "plain": abi.SOLVER_PLAIN_FP64, "matfree": abi.SOLVER_MIXED_MATFREE,
               "compact": abi.SOLVER_MIXED_COMPACT}[a.solver]
     mlp_path = os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz")
-    use_mlp = a.warm == "mlp" or (a.warm == "auto" and os.path.exists(mlp_path))
+    have_mlp = os.path.exists(mlp_path)
+    use_mlp = a.warm == "mlp"
     prec = abi.PRECISION_DF32 if a.precision == "df32" else abi.PRECISION_FP64
     g = mps.MpsGpu(case, solver=solver, tol=1e-8, max_iter=20000, precision=prec)
     warm = abi.WARM_PREVIOUS if a.warm == "prev" else abi.WARM_EXTRAP
-    if use_mlp:
+    if have_mlp:
         w = np.load(mlp_path)
         g.mlp_set_weights(w["params"], w["norm"])
+    if use_mlp:
         warm = abi.WARM_MLP
     g.set_solver(solver, warm, 1e-8, 20000)
     g.initialize()
@@ -239,7 +242,7 @@ def run_gb300(a, rank, world, local):
     # end-to-end section, which re-uploads the state and resets the warm-start history)
     ppe = None
     if a.ppe_compare and rank == 0:
-        ppe = ppe_compare(g, abi, use_mlp)
+        ppe = ppe_compare(g, abi, have_mlp)
     # e2e through the C ABI with host arrays: upload the state from pinned host memory,
     # step, download the result, every step
     h2d = sum(v.nbytes for v in host.values())

@@ -273,17 +273,21 @@ int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col,
  * W1[64x16] b1[64] W2[64x64] b2[64] W3[64x64] b3[64] W4[1x64] b4[1]  (row-major [out][in]),
  * The normalisation vector holds MPSGPU_MLP_NNORM floats: feature means[16], feature
  * inverse spreads[16], then the target's mean and inverse spread.  The network predicts
- * the correction of the temporal extrapolation 2 p_n - p_{n-1} in target units. */
+ * the correction c of the temporal extrapolation x_e = 2 p_n - p_{n-1}; features 1, 5, 7,
+ * 14 (pressure differences) and the target are in units of the system scale sigma (RMS
+ * over the equation rows of feature 7, the Jacobi step of the extrapolation residual).
+ * The warm start is x_e + theta c with theta = argmin ||b - A (x_e + theta c)||, so the
+ * start is never worse than the extrapolation in the residual norm. */
 #define MPSGPU_MLP_NPARAM (64*16 + 64 + 64*64 + 64 + 64*64 + 64 + 64 + 1)
 #define MPSGPU_MLP_NFEAT  16
 #define MPSGPU_MLP_NNORM  34
 int mpsgpu_mlp_set_weights(mpsgpu_t h, const float* params, const float* norm32);
 int mpsgpu_mlp_get_weights(mpsgpu_t h, float* params, float* norm32);
-/* Features of the current PPE system, N x 16 FP32 (host). */
+/* Raw features of the current PPE system, N x 16 FP32 (host; before the sigma scaling). */
 int mpsgpu_ppe_features(mpsgpu_t h, float* feat);
 /* Training on the GPU with the library's own forward/backward/Adam kernels.  While
  * recording is enabled, every PPE solve appends (features, converged pressure minus
- * previous pressure) of its inner rows to a device-resident training set. */
+ * x_e, both scaled by sigma) of its equation rows to a device-resident training set. */
 int mpsgpu_mlp_record(mpsgpu_t h, int enable);
 int mpsgpu_mlp_num_records(mpsgpu_t h, long long* n);
 int mpsgpu_mlp_fit_normalization(mpsgpu_t h);

@@ -220,11 +220,14 @@ static int calcPress(mpsgpu_t h) {
     if (h->warm == MPSGPU_WARM_ZERO) cudaMemsetAsync(h->B.x, 0, sizeof(double) * h->N0, h->s);
     if (h->warm == MPSGPU_WARM_EXTRAPOLATE) { launchWarmExtrapolate(h->d, h->B, h->s); countLaunch(1); }
     cudaEventRecord(h->es0, h->s);
+    h->B.prepared = df32(h) ? 1 : 0;   // the DF32 assembly writes the FP32 copies itself
     if (h->warm == MPSGPU_WARM_MLP) {
         if (h->prof.on) h->prof.begin(PROF_PPE_OTHER, h->s);
+        // the learned start reads the FP32 copy of the matrix
+        if (!h->B.prepared) { launchMixedPrepare(h->d, h->B, h->s); h->B.prepared = 1; countLaunch(1); }
         int e = mlpWarmStart(h->mlp, h->d, h->B, h->s);
         if (h->prof.on) h->prof.end(h->s);
-        countLaunch(3);
+        countLaunch(8);   // x_e copy, features, scale, forward, correction, step dot products, step, apply
         if (e) return e;
     } else if (h->warm == MPSGPU_WARM_PREVIOUS) {
         cudaMemcpyAsync(h->B.x, h->d.pressPPE, sizeof(double) * h->N0, cudaMemcpyDeviceToDevice, h->s);
@@ -234,7 +237,6 @@ static int calcPress(mpsgpu_t h) {
     int maxIt = h->maxIter > 0 ? h->maxIter : 2 * h->N0;
     int e;
     const bool mixed = h->solver != MPSGPU_SOLVER_PLAIN_FP64;
-    h->B.prepared = df32(h) ? 1 : 0;   // the DF32 assembly writes the FP32 copies itself
     h->B.matfree = h->solver == MPSGPU_SOLVER_MIXED_MATFREE ? 1 : (h->solver == MPSGPU_SOLVER_MIXED_COMPACT ? 2 : 0);
     if (h->solver == MPSGPU_SOLVER_MIXED && h->persistent == 2 && h->B.pgridTs > 0) h->B.matfree = 3;
     if (h->solver == MPSGPU_SOLVER_MIXED && h->persistent == 3 && h->B.pgridPipe > 0) h->B.matfree = 4;
@@ -257,6 +259,7 @@ static int calcPress(mpsgpu_t h) {
     cudaEventRecord(h->es1, h->s);
     if (h->mlp.recording && !e) {
         // features of this system with the previous solution, target = converged - previous
+        if (!h->B.prepared) { launchMixedPrepare(h->d, h->B, h->s); h->B.prepared = 1; }   // features read valf
         int er = mlpRecordFeatures(h->mlp, h->d, h->B, h->s);
         if (!er) er = mlpRecordTargets(h->mlp, h->d, h->B, h->s);
         if (er) return er;
@@ -984,6 +987,7 @@ int mpsgpu_ppe_features(mpsgpu_t h, float* feat) {
     int e = mpsgpu_num_particles(h, &n);
     if (e) return e;
     std::vector<float> st((size_t)MPSGPU_MLP_NFEAT * n);
+    if (!h->B.prepared) { launchMixedPrepare(h->d, h->B, h->s); h->B.prepared = 1; }   // features read valf
     if ((e = mlpFeatures(h->mlp, h->d, h->B, st.data(), n, h->s))) return e;
     std::vector<int> slot(n);
     CK(cudaMemcpyAsync(slot.data(), h->d.slotOf, sizeof(int) * n, cudaMemcpyDeviceToHost, h->s));

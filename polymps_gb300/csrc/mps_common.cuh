@@ -200,11 +200,29 @@ __device__ __forceinline__ bool sideOK(const SideCtx& s, dvec4 pj, double d2) {
 __device__ __forceinline__ int liveN(const Dev& d) { return *d.nLive; }
 
 // Iterate the ELL neighbour row of i (scan order of the reference).
+// Streams read once per sweep (neighbour-list columns, matrix columns): loaded without L1
+// allocation, so L1 keeps the lines of the gathered per-particle records.
+__device__ __forceinline__ int ldStream(const int* p) {
+    int v;
+    asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ float ldStream(const float* p) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ double ldStream(const double* p) {
+    double v;
+    asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+}
+
 template <class F>
 __device__ __forceinline__ void forNbrs(const Dev& d, int i, F&& f) {
     int c = d.nbrCount[i];
     const int* row = d.nbr + i;
-    for (int k = 0; k < c; k++) f(__ldg(row + (size_t)k * d.N0));
+    for (int k = 0; k < c; k++) f(ldStream(row + (size_t)k * d.N0));
 }
 
 // Iterate the set bits of an entry mask in ascending entry order (the scan order).
@@ -215,7 +233,7 @@ __device__ __forceinline__ void forMask(const Dev& d, int i, unsigned long long 
         int k = __ffsll((long long)m) - 1;
         m &= m - 1;
         size_t e = (size_t)k * d.N0 + i;
-        f(__ldg(row + (size_t)k * d.N0), e);
+        f(ldStream(row + (size_t)k * d.N0), e);
     }
 }
 

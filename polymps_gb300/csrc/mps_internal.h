@@ -119,6 +119,8 @@ void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeAssembleDF(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchWarmExtrapolate(const Dev& d, const PpeBuffers& B, cudaStream_t s);
+// FP32 copies of the assembled matrix (valf, diagf, diagInvf) for the FP64 assembly
+void launchMixedPrepare(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 // Returns iterations and final relative residual through host pointers (synchronises).
 int ppeSolvePlain(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cudaStream_t s,
                   int* iters, double* relres, double* relres0, Prof* prof);

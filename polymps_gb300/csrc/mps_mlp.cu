@@ -5,9 +5,10 @@
 // at a time; the FP32 accumulator fragment of one layer is re-packed in registers as the
 // BF16 A fragment of the next (the m16n8 C layout of two adjacent n-tiles is the m16k16 A
 // layout), so activations never leave the register file.  The network predicts the
-// change of the unclamped pressure since the previous step, normalised by the pressure
-// scale: x0 = p_prev + out / inv_std[8] on inner rows, and x0 = 0 on the identity rows
-// of surface/dummy particles (their exact solution).
+// correction c of the temporal extrapolation x_e = 2 p_n - p_{n-1} of the unclamped
+// pressure on equation rows (in target units, de-normalised on output); the warm start is
+// x0 = x_e + theta c with the residual-minimising step theta, and x0 = 0 on the identity
+// rows of surface/dummy particles (their exact solution).
 //
 // Training runs on the same machinery: a fused forward/backward kernel over blocks of 64
 // recorded samples (activation gradients on the tensor cores, weight gradients dW = dZ^T H
@@ -86,14 +87,20 @@ __device__ void loadWeights(SmemW& s, const __nv_bfloat16* wbf, const float* mas
     if (threadIdx.x == 0) s.b4 = master[OB4];
 }
 
-// A fragment of 16 samples x 16 normalised features (rows g and g+8 of the tile)
-__device__ __forceinline__ void loadInput(const SmemW& s, const float* f0, const float* f1, uint32_t* a) {
+// A fragment of 16 samples x 16 normalised features (rows g and g+8 of the tile); q scales
+// the pressure-difference features 1, 5, 7 and 14 (1/sigma for raw features, 1 otherwise)
+__device__ __forceinline__ float fin(const SmemW& s, const float* f, int c, float q) {
+    float v = f[c];
+    if (c == 1 || c == 5 || c == 7 || c == 14) v *= q;
+    return (v - s.mean[c]) * s.istd[c];
+}
+__device__ __forceinline__ void loadInput(const SmemW& s, const float* f0, const float* f1, uint32_t* a, float q = 1.f) {
     int t = threadIdx.x & 3;
     int c0 = 2 * t, c1 = 2 * t + 8;
-    a[0] = pack2((f0[c0] - s.mean[c0]) * s.istd[c0], (f0[c0 + 1] - s.mean[c0 + 1]) * s.istd[c0 + 1]);
-    a[1] = pack2((f1[c0] - s.mean[c0]) * s.istd[c0], (f1[c0 + 1] - s.mean[c0 + 1]) * s.istd[c0 + 1]);
-    a[2] = pack2((f0[c1] - s.mean[c1]) * s.istd[c1], (f0[c1 + 1] - s.mean[c1 + 1]) * s.istd[c1 + 1]);
-    a[3] = pack2((f1[c1] - s.mean[c1]) * s.istd[c1], (f1[c1 + 1] - s.mean[c1 + 1]) * s.istd[c1 + 1]);
+    a[0] = pack2(fin(s, f0, c0, q), fin(s, f0, c0 + 1, q));
+    a[1] = pack2(fin(s, f1, c0, q), fin(s, f1, c0 + 1, q));
+    a[2] = pack2(fin(s, f0, c1, q), fin(s, f0, c1 + 1, q));
+    a[3] = pack2(fin(s, f1, c1, q), fin(s, f1, c1 + 1, q));
 }
 
 // z[8][4] = A(16 x K) W^T + b, W row-major [64][K] in smem with stride S
@@ -138,10 +145,12 @@ __device__ __forceinline__ void headOut(const SmemW& s, const float (*z)[4], flo
 
 // ------------------------------------------------------------------ inference
 __global__ void __launch_bounds__(128) k_mlp_forward(const float* feat, int n, const __nv_bfloat16* wbf,
-                                                     const float* master, const float* norm, float* out) {
+                                                     const float* master, const float* norm, const double* sig,
+                                                     float* out) {
     __shared__ SmemW s;
     loadWeights(s, wbf, master, norm);
     __syncthreads();
+    const float q = sig ? (float)(1.0 / sig[0]) : 1.f;
     int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -153,7 +162,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float* feat, int n, c
         const float* f1 = (r1 < n) ? feat + (size_t)r1 * NF : zero;
         uint32_t a0[1][4], a[4][4];
         float z[8][4];
-        loadInput(s, f0, f1, a0[0]);
+        loadInput(s, f0, f1, a0[0], q);
         layer<1, S1>(a0, s.w1, s.b1, z);
         activate(z, a);
         layer<4, S2>(a, s.w2, s.b2, z);
@@ -172,7 +181,8 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float* feat, int n, c
 // The network corrects the temporal extrapolation of the unclamped solutions,
 // x_e = 2 p_n - p_{n-1}: x0 = x_e + correction on the rows that carry an equation.
 // Raw features of row i of the new system (normalised inside the network); pressures in
-// Pa, lengths in m, velocities in m/s, so that the scales do not depend on the spacing:
+// Pa (1, 5, 7 and 14 then in units of the system scale sigma below), lengths in m,
+// velocities in m/s:
 //  0 (n_i - n0)/n0          1 b_i / A_ii              2 numNeigh / N0
 //  3 row without pressure last solve (p_n == 0)       4 wall distance / reL (<= 1.5)
 //  5 p_n - p_{n-1}          6 x_e                     7 (b - A x_e)_i / A_ii (Jacobi step)
@@ -183,79 +193,206 @@ __device__ __forceinline__ double extrapBase(const Dev& d, int j) {
     double p = d.pressPPE[j];
     return (p + p) - d.pressPPEprev[j];
 }
-__global__ void k_mlp_features(Dev d, PpeBuffers B, float* feat) {
+// Block sums of two FP64 values per thread into part[block] and part[gridDim + block].
+__device__ __forceinline__ void blockPartials2(double s0, double s1, double* part) {
+    __shared__ double sm[2][32];
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sm[0][threadIdx.x >> 5] = s0; sm[1][threadIdx.x >> 5] = s1; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) { a += sm[0][k]; b += sm[1][k]; }
+        part[blockIdx.x] = a;
+        part[gridDim.x + blockIdx.x] = b;
+    }
+}
+// Totals of nblk block partials (fixed order for a fixed block size), in every thread.
+__device__ __forceinline__ void sumPartials2(const double* part, int nblk, double& a, double& b) {
+    __shared__ double sm[2][32];
+    double s0 = 0.0, s1 = 0.0;
+    for (int k = threadIdx.x; k < nblk; k += blockDim.x) { s0 += part[k]; s1 += part[nblk + k]; }
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    }
+    if ((threadIdx.x & 31) == 0) { sm[0][threadIdx.x >> 5] = s0; sm[1][threadIdx.x >> 5] = s1; }
+    __syncthreads();
+    a = 0.0; b = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) { a += sm[0][k]; b += sm[1][k]; }
+    __syncthreads();
+}
+
+// Features 1, 5, 7 and 14 (pressure differences, Pa) and the target are taken in units of
+// the system scale sigma = RMS of feature 7 over the equation rows: their spread shrinks
+// with the particle spacing, in units of sigma it does not, so a network trained at one
+// spacing applies at another.  The features kernel leaves block partials of sum f7^2 and
+// of the row count; sigma is formed once from them, and the network input, the recorded
+// samples and the correction apply it.
+#define FSIG 7
+// x_e in FP32 for the neighbour gathers of the features (the features are FP32 numbers;
+// GB300 runs FP64 at 1/64 of the FP32 rate, so the per-entry work stays in FP32)
+__global__ void k_mlp_xe32(Dev d, float* xe32) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
+    if (i >= d.N0) return;
+    xe32[i] = (i < liveN(d) && d.bc[i] == d.P.inner) ? (float)extrapBase(d, i) : 0.f;
+}
+__global__ void __launch_bounds__(256) k_mlp_features(Dev d, PpeBuffers B, const float* xe32, float* feat, float* re,
+                                                      double* part) {
     const MpsParams& P = d.P;
     double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
     double gn = sqrt(gx * gx + gy * gy + gz * gz);
     if (gn > 0) { gx /= gn; gy /= gn; gz /= gn; }
-    dvec4 x = d.pos[i], v = d.vel[i];
-    double diag = B.diag[i];
-    double pn = d.pressPPE[i], pp = d.pressPPEprev[i];
-    double xe = (d.bc[i] == P.inner) ? (pn + pn) - pp : 0.0;
-    double ax = diag * xe;
-    int len = B.rowLen[i];
-    for (int k = 0; k < len; k++) {
-        size_t e = (size_t)k * B.N0 + i;
-        ax += B.val[e] * extrapBase(d, B.col[e]);   // matrix columns are inner rows
+    const float ggx = (float)gx, ggy = (float)gy, ggz = (float)gz;
+    const float in0 = (float)(1.0 / P.pndSmallZero), iN0 = (float)(1.0 / P.numNeighZero), iRe = (float)(1.0 / P.reL);
+    const float iA = (float)(1.0 / (P.coeffPPE * P.pndSmallZero));
+    const int n = liveN(d);
+    const size_t N0 = B.N0;
+    double q0 = 0.0, q1 = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const dvec4 x = d.pos[i], v = d.vel[i];
+        const float diag = (float)B.diag[i], idg = 1.f / diag;
+        const float pn = (float)d.pressPPE[i], pp = (float)d.pressPPEprev[i];
+        const bool eq = d.bc[i] == P.inner;
+        const float xe = xe32[i];
+        // (A x_e)_i in FP32 from the FP32 copy of the matrix, eight entries in flight
+        float acc[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) acc[u] = 0.f;
+        const int len = B.rowLen[i];
+        for (int k = 0; k < len; k += 8) {
+            int cc[8];
+            float vv[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                bool ok = k + u < len;
+                cc[u] = ok ? ldStream(B.col + (size_t)(k + u) * N0 + i) : i;
+                vv[u] = ok ? ldStream(B.valf + (size_t)(k + u) * N0 + i) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) acc[u] += vv[u] * xe32[cc[u]];
+        }
+        const float ax = diag * xe + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
+        const float bi = (float)B.b[i];
+        if (re) re[i] = bi - ax;   // residual of the extrapolated start
+        const float vx = (float)v.x, vy = (float)v.y, vz = (float)v.z;
+        float f[NF];
+        f[0] = ((float)d.pndSmall[i] - (float)P.pndSmallZero) * in0;
+        f[1] = bi * idg;
+        f[2] = (float)d.numNeigh[i] * iN0;
+        f[3] = (d.pressPPE[i] == 0.0) ? 1.f : 0.f;
+        f[4] = fminf(sqrtf((float)d.riw2[i]) * iRe, 1.5f);
+        f[5] = pn - pp;
+        f[6] = xe;
+        f[7] = (bi - ax) * idg;
+        f[8] = pn;
+        f[9] = sqrtf(vx * vx + vy * vy + vz * vz);
+        f[10] = -(vx * ggx + vy * ggy + vz * ggz);
+        f[11] = diag * iA;
+        f[12] = (float)d.pndWall[i];
+        f[13] = -((float)x.x * ggx + (float)x.y * ggy + (float)x.z * ggz);
+        f[14] = (bi - (float)d.source[i]) * idg;
+        f[15] = ((float)d.pndi[i] - (float)d.pndki[i]) * in0;
+        float4* o = (float4*)(feat + (size_t)i * NF);
+        o[0] = make_float4(f[0], f[1], f[2], f[3]);
+        o[1] = make_float4(f[4], f[5], f[6], f[7]);
+        o[2] = make_float4(f[8], f[9], f[10], f[11]);
+        o[3] = make_float4(f[12], f[13], f[14], f[15]);
+        if (eq) { q0 += (double)(f[FSIG] * f[FSIG]); q1 += 1.0; }
     }
-    double bi = B.b[i];
-    float f[NF];
-    f[0] = (float)((d.pndSmall[i] - P.pndSmallZero) / P.pndSmallZero);
-    f[1] = (float)(bi / diag);
-    f[2] = (float)(d.numNeigh[i] / P.numNeighZero);
-    f[3] = (pn == 0.0) ? 1.f : 0.f;
-    f[4] = (float)fmin(sqrt(d.riw2[i]) / P.reL, 1.5);
-    f[5] = (float)(pn - pp);
-    f[6] = (float)xe;
-    f[7] = (float)((bi - ax) / diag);
-    f[8] = (float)pn;
-    f[9] = (float)sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
-    f[10] = (float)-(v.x * gx + v.y * gy + v.z * gz);
-    f[11] = (float)(diag / (P.coeffPPE * P.pndSmallZero));
-    f[12] = (float)d.pndWall[i];
-    f[13] = (float)-(x.x * gx + x.y * gy + x.z * gz);
-    f[14] = (float)((bi - d.source[i]) / diag);
-    f[15] = (float)((d.pndi[i] - d.pndki[i]) / P.pndSmallZero);
-    float4* o = (float4*)(feat + (size_t)i * NF);
-    o[0] = make_float4(f[0], f[1], f[2], f[3]);
-    o[1] = make_float4(f[4], f[5], f[6], f[7]);
-    o[2] = make_float4(f[8], f[9], f[10], f[11]);
-    o[3] = make_float4(f[12], f[13], f[14], f[15]);
+    blockPartials2(q0, q1, part);
+}
+__global__ void __launch_bounds__(256) k_mlp_sig(const double* part, int nblk, double* sig) {
+    double a, b;
+    sumPartials2(part, nblk, a, b);
+    if (threadIdx.x == 0) sig[0] = (b > 0.0 && a > 0.0) ? sqrt(a / b) : 1.0;
+}
+static void mlpFeatureLaunch(MlpState& m, const Dev& d, const PpeBuffers& B, float* re, cudaStream_t s) {
+    k_mlp_xe32<<<gridFor(d.N0, 256), 256, 0, s>>>(d, m.xe32);
+    k_mlp_features<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.feat, re, m.part);
+    k_mlp_sig<<<1, 256, 0, s>>>(m.part, m.nblk, m.sig);
 }
 
-// x0 = x_e + (out / target_inv_std + target_mean) on equation rows, 0 on identity rows
-__global__ void k_mlp_combine(Dev d, PpeBuffers B, const float* out, const float* norm) {
+// The network's correction c = out / target_inv_std + target_mean of the extrapolation
+// x_e on equation rows (identity rows: x = 0).  The start is x0 = x_e + theta c with the
+// step theta = (r_e . A c) / (A c . A c) that minimises ||b - A x0||: a pointwise
+// prediction error is rough, and A amplifies rough errors, so the full step can leave a
+// larger residual than x_e even when it lowers the error; with the minimising step the
+// start is never worse than the extrapolation (theta = 0) in the residual norm.
+__global__ void k_mlp_combine(Dev d, PpeBuffers B, const float* out, const float* norm, const double* sig,
+                              float* cdir) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
-    double x0 = 0.0;
-    if (d.bc[i] == d.P.inner)
-        x0 = extrapBase(d, i) + (double)out[i] / (double)norm[2 * NF + 1] + (double)norm[2 * NF];
-    B.x[i] = x0;
+    if (i >= d.N0) return;
+    const bool eq = i < liveN(d) && d.bc[i] == d.P.inner;
+    B.x[i] = eq ? extrapBase(d, i) : 0.0;
+    cdir[i] = eq ? (out[i] / norm[2 * NF + 1] + norm[2 * NF]) * (float)sig[0] : 0.f;
+}
+__global__ void __launch_bounds__(256) k_mlp_step_dots(Dev d, PpeBuffers B, const float* cdir, const float* re,
+                                                       double* part) {
+    double s0 = 0.0, s1 = 0.0;
+    const int n = liveN(d);
+    const size_t N0 = B.N0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float acc[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) acc[u] = 0.f;
+        const int len = B.rowLen[i];
+        for (int k = 0; k < len; k += 8) {
+            int cc[8];
+            float vv[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                bool ok = k + u < len;
+                cc[u] = ok ? ldStream(B.col + (size_t)(k + u) * N0 + i) : i;
+                vv[u] = ok ? ldStream(B.valf + (size_t)(k + u) * N0 + i) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) acc[u] += vv[u] * cdir[cc[u]];
+        }
+        const float ac = __ldg(B.diagf + i) * cdir[i] + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
+        s0 += (double)(re[i] * ac);
+        s1 += (double)(ac * ac);
+    }
+    blockPartials2(s0, s1, part);
+}
+// theta from the block partials (one block, fixed order), then x0 += theta c
+__global__ void __launch_bounds__(256) k_mlp_theta(const double* part, int nblk, double* theta) {
+    double a, b;
+    sumPartials2(part, nblk, a, b);
+    if (threadIdx.x == 0) theta[0] = (b > 0.0 && a == a) ? a / b : 0.0;
+}
+__global__ void k_mlp_step_apply(Dev d, PpeBuffers B, const float* cdir, const double* theta) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < d.N0) B.x[i] += theta[0] * (double)cdir[i];
 }
 
-static int mlpForwardLaunch(MlpState& m, const float* feat, int n, float* out, cudaStream_t s) {
+// sig: system scale of the raw features (nullptr: the features are network inputs as given)
+static int mlpForwardLaunch(MlpState& m, const float* feat, int n, const double* sig, float* out, cudaStream_t s) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int tiles = (n + 15) / 16;
     int blocks = std::min((tiles + 3) / 4, std::max(1, sms) * 8);
-    k_mlp_forward<<<blocks, 128, 0, s>>>(feat, n, m.wbf, m.master, m.norm, out);
+    k_mlp_forward<<<blocks, 128, 0, s>>>(feat, n, m.wbf, m.master, m.norm, sig, out);
     return cudaGetLastError() == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
 }
 
 int mlpWarmStart(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s) {
     if (!m.ready) return MPSGPU_ERR_ARG;
-    k_mlp_features<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.feat);
-    int e = mlpForwardLaunch(m, m.feat, d.N0, m.out, s);
+    mlpFeatureLaunch(m, d, B, m.re, s);
+    int e = mlpForwardLaunch(m, m.feat, d.N0, m.sig, m.out, s);
     if (e) return e;
-    k_mlp_combine<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.out, m.norm);
+    k_mlp_combine<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.out, m.norm, m.sig, m.cdir);
+    k_mlp_step_dots<<<m.nblk, 256, 0, s>>>(d, B, m.cdir, m.re, m.part);
+    k_mlp_theta<<<1, 256, 0, s>>>(m.part, m.nblk, m.sig + 1);
+    k_mlp_step_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.cdir, m.sig + 1);
     return cudaGetLastError() == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
 }
 
 int mlpFeatures(MlpState& m, const Dev& d, const PpeBuffers& B, float* hostFeat, int n, cudaStream_t s) {
-    k_mlp_features<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.feat);
+    mlpFeatureLaunch(m, d, B, nullptr, s);
     if (cudaMemcpyAsync(hostFeat, m.feat, sizeof(float) * NF * n, cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
     return cudaStreamSynchronize(s) == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
 }
@@ -278,6 +415,16 @@ int mlpInit(MlpState& m, int n0, cudaStream_t s) {
               al((void**)&m.feat, sizeof(float) * NF * (size_t)n0) && al((void**)&m.out, sizeof(float) * (size_t)n0) &&
               al((void**)&m.lossAcc, sizeof(float) * 4);
     if (!ok) return MPSGPU_ERR_NOMEM;
+    {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        m.nblk = std::max(1, sms) * 8;
+    }
+    ok = al((void**)&m.re, sizeof(float) * (size_t)n0) && al((void**)&m.cdir, sizeof(float) * (size_t)n0) &&
+         al((void**)&m.xe32, sizeof(float) * (size_t)n0) &&
+         al((void**)&m.part, sizeof(double) * 2 * (size_t)m.nblk) && al((void**)&m.sig, 2 * sizeof(double));
+    if (!ok) return MPSGPU_ERR_NOMEM;
     cudaMemsetAsync(m.master, 0, sizeof(float) * NPARAM, s);
     cudaMemsetAsync(m.adam_m, 0, sizeof(float) * NPARAM, s);
     cudaMemsetAsync(m.adam_v, 0, sizeof(float) * NPARAM, s);
@@ -288,7 +435,8 @@ int mlpInit(MlpState& m, int n0, cudaStream_t s) {
 
 void mlpFree(MlpState& m) {
     for (void* p : {(void*)m.master, (void*)m.adam_m, (void*)m.adam_v, (void*)m.grad, (void*)m.wbf, (void*)m.norm,
-                    (void*)m.feat, (void*)m.out, (void*)m.recFeat, (void*)m.recTarget, (void*)m.lossAcc})
+                    (void*)m.feat, (void*)m.out, (void*)m.recFeat, (void*)m.recTarget, (void*)m.lossAcc,
+                    (void*)m.re, (void*)m.cdir, (void*)m.part, (void*)m.sig, (void*)m.xe32})
         if (p) cudaFree(p);
     m = MlpState();
 }
@@ -313,11 +461,11 @@ int mlpGetWeights(MlpState& m, float* params, float* norm32, cudaStream_t s) {
 
 // ------------------------------------------------------------------ recording
 int mlpRecordFeatures(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s) {
-    k_mlp_features<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.feat);
+    mlpFeatureLaunch(m, d, B, nullptr, s);
     return cudaGetLastError() == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
 }
-__global__ void k_mlp_record(Dev d, PpeBuffers B, const float* feat, float* recFeat, float* recTarget,
-                             unsigned long long* count, long long cap) {
+__global__ void k_mlp_record(Dev d, PpeBuffers B, const float* feat, const double* sig, float* recFeat,
+                             float* recTarget, unsigned long long* count, long long cap) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     if (d.bc[i] != d.P.inner) return;
@@ -325,8 +473,12 @@ __global__ void k_mlp_record(Dev d, PpeBuffers B, const float* feat, float* recF
     if ((long long)slot >= cap) return;
     const float4* src = (const float4*)(feat + (size_t)i * NF);
     float4* dst = (float4*)(recFeat + slot * NF);
-    dst[0] = src[0]; dst[1] = src[1]; dst[2] = src[2]; dst[3] = src[3];
-    recTarget[slot] = (float)(B.x[i] - extrapBase(d, i));
+    const double sg = sig[0];
+    const float q = (float)(1.0 / sg);
+    float4 a = src[0], b = src[1], c = src[2], e = src[3];
+    a.y *= q; b.y *= q; b.w *= q; e.z *= q;   // features 1, 5, 7, 14 in units of sigma
+    dst[0] = a; dst[1] = b; dst[2] = c; dst[3] = e;
+    recTarget[slot] = (float)((B.x[i] - extrapBase(d, i)) / sg);
 }
 int mlpRecordTargets(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s) {
     if (!m.recFeat) {
@@ -337,7 +489,7 @@ int mlpRecordTargets(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_
     }
     unsigned long long* cnt = (unsigned long long*)((char*)m.recTarget + sizeof(float) * m.recCap);
     cudaMemcpyAsync(cnt, &m.recCount, sizeof(unsigned long long), cudaMemcpyHostToDevice, s);
-    k_mlp_record<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.feat, m.recFeat, m.recTarget, cnt, m.recCap);
+    k_mlp_record<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.feat, m.sig, m.recFeat, m.recTarget, cnt, m.recCap);
     unsigned long long c = 0;
     cudaMemcpyAsync(&c, cnt, sizeof(c), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return MPSGPU_ERR_CUDA;
@@ -654,7 +806,7 @@ int mlpForwardHost(MlpState& m, const float* hfeat, int n, float* hout, cudaStre
     if (cudaMalloc(&df, sizeof(float) * NF * n) != cudaSuccess) return MPSGPU_ERR_NOMEM;
     if (cudaMalloc(&dout, sizeof(float) * n) != cudaSuccess) { cudaFree(df); return MPSGPU_ERR_NOMEM; }
     cudaMemcpyAsync(df, hfeat, sizeof(float) * NF * n, cudaMemcpyHostToDevice, s);
-    int e = mlpForwardLaunch(m, df, n, dout, s);
+    int e = mlpForwardLaunch(m, df, n, nullptr, dout, s);
     if (!e) cudaMemcpyAsync(hout, dout, sizeof(float) * n, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) e = MPSGPU_ERR_CUDA;
     cudaFree(df); cudaFree(dout);

@@ -17,6 +17,16 @@ struct MlpState {
     float* norm = nullptr;         // mean[16], inv_std[16]
     float* feat = nullptr;         // N0 x 16 raw features of the current system
     float* out = nullptr;          // N0 outputs
+    // step along the network's correction: residual of the extrapolation, the correction
+    // (Pa), block partials of the two dot products and the step length
+    float* re = nullptr;
+    float* cdir = nullptr;
+    float* xe32 = nullptr;         // x_e in FP32 (gathered by the features)
+    double* part = nullptr;
+    int nblk = 0;
+    // system scale: RMS over equation rows of the Jacobi step of the extrapolation residual
+    // (pressure-difference features and the target are in its units)
+    double* sig = nullptr;         // [0] sigma, [1] step theta
     // training record: features and targets of recorded steps
     float* recFeat = nullptr;
     float* recTarget = nullptr;

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(128) k_side_masks_df(Dev d) {
         const df RS = K(d.k.reS2), RL = K(d.k.reL2);
         const int* row = d.nbr + i;
         for (int k = 0; k < c; k++) {
-            int j = __ldg(row + (size_t)k * d.N0);
+            int j = ldStream(row + (size_t)k * d.N0);
             float4 hj = d.posf[j], lj = d.posLo[j];
             df d2 = norm2(diff3(hj, lj, hi, li));
             if (!sideOkDF(d, sc, hj, lj, d2, i, j)) continue;

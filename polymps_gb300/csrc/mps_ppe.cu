@@ -156,23 +156,6 @@ __device__ __forceinline__ void gridSum(double (&v)[NV], const PpeBuffers& B, Fi
 // together, then the eight gathers; the last chunk is masked (predicated loads, the row's
 // own index as a harmless column) instead of a serial remainder loop.  RO: the gathered
 // vector is read-only for the launch (non-coherent cache path); otherwise plain loads.
-// Matrix streams are read once per SpMV: loaded without L1 allocation, so L1 keeps the
-// lines of the gathered vector (the neighbours of a block's rows reuse them).
-__device__ __forceinline__ int ldStream(const int* p) {
-    int v;
-    asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
-    return v;
-}
-__device__ __forceinline__ float ldStream(const float* p) {
-    float v;
-    asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
-    return v;
-}
-__device__ __forceinline__ double ldStream(const double* p) {
-    double v;
-    asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
-    return v;
-}
 #define ELL_U 8
 template <class T, bool RO>
 __device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col, const T* x, int i, int len, size_t N0) {
@@ -342,6 +325,9 @@ __global__ void k_mixed_prepare(Dev d, PpeBuffers B) {
     }
     B.diagf[i] = (float)B.diag[i];
     B.diagInvf[i] = (float)(1.0 / B.diag[i]);
+}
+void launchMixedPrepare(const Dev& d, const PpeBuffers& B, cudaStream_t s) {
+    k_mixed_prepare<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B);
 }
 // FP64 residual r = b - A x (FP64 values), sums r.r (and b.b on the first call)
 __global__ void __launch_bounds__(PBLK) k_mx_residual(Dev d, PpeBuffers B, int first, double tol) {
@@ -640,7 +626,7 @@ __device__ __forceinline__ float mfRowF(const Dev& d, const PpeBuffers& B, const
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             int k = __ffsll((long long)m) - 1;
-            jj[u] = (m != 0ull) ? __ldg(row + (size_t)k * N0) : -1;
+            jj[u] = (m != 0ull) ? ldStream(row + (size_t)k * N0) : -1;
             m &= m - 1ull;
         }
 #pragma unroll
@@ -699,7 +685,7 @@ __device__ __forceinline__ float h16Row(const PpeBuffers& B, const float* y, int
 #pragma unroll
             for (int u = 0; u < ELL_U; u++) {
                 bool ok = k + u < len;
-                cc[u] = ok ? __ldg(c + (size_t)(k + u) * N0) : i;
+                cc[u] = ok ? ldStream(c + (size_t)(k + u) * N0) : i;
                 vv[u] = ok ? __half2float(__ldg(v + (size_t)(k + u) * N0)) : 0.f;
             }
 #pragma unroll

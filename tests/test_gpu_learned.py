@@ -1,0 +1,81 @@
+"""What the trained warm-start network gains over the method without it.
+
+The network is trained on the GPU by the library's own kernels (records of the plain FP64
+solver on the 3D incompressible dam break, fused BF16 forward/backward, Adam), then the
+same held-out PPE systems are solved by the FP32/FP64 refinement solver from three
+starts: the previous-step pressure (the reference's warm start), the temporal
+extrapolation 2 p_n - p_{n-1} (the learned start without the network), and the learned
+start x_e + theta c (network correction c, residual-minimising step theta).
+"""
+import numpy as np
+import pytest
+
+from polymps_gb300 import abi, cases
+
+pytestmark = pytest.mark.gpu
+
+OPS_BEFORE = ["UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT", "OUT_OF_DOMAIN", "COLLISION",
+              "WALL_DISTANCE", "WALL_NPCD", "PND_NEIGH_NPCD", "UPDATE_BC"]
+OPS_AFTER = ["CORRECTION_MATRIX", "PRESS_GRADIENT", "WALL_PRESS_GRADIENT", "WALL_VISCOSITY", "CORRECT",
+             "OUT_OF_DOMAIN"]
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def test_learned_warm_start_gain(mps_lib):
+    from polymps_gb300 import mps, train_warmstart as tw
+    c = cases.config(4, scale=2.0)   # l0 = 0.02 m
+    g = mps.MpsGpu(c, solver=abi.SOLVER_PLAIN_FP64, tol=1e-10, max_iter=20000, precision=abi.PRECISION_DF32)
+    g.initialize()
+    g.run(10)
+    for s in range(80):
+        g.mlp_record(s % 2 == 0)
+        g.step()
+    g.mlp_record(False)
+    assert g.mlp_num_records() > 100000
+    rng = np.random.default_rng(5)
+    g.mlp_set_weights(tw.init_params(rng), np.concatenate([np.zeros(16), np.ones(16), [0.0, 1.0]]).astype(np.float32))
+    g.mlp_fit_normalization()
+    p0, norm = g.mlp_get_weights()
+    g.mlp_set_weights(p0, norm)
+    first = float(np.mean(g.mlp_train(200, 4096, 2e-3, seed=1)))
+    last = float(np.mean(g.mlp_train(800, 4096, 1e-3, seed=2)))
+    assert last < first   # the network learns the correction on its own kernels
+
+    rows = []
+    for s in range(8):   # held-out systems: later steps of the same run
+        for op in OPS_BEFORE:
+            g.run_op(op)
+        xp, xq = g.get(abi.F_PRESSPPE), g.get(abi.F_PRESSPPE_PREV)
+        out = {}
+        for name, solver, warm, tol in (("reference", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 1e-12),
+                                        ("previous", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 1e-8),
+                                        ("extrapolated", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 1e-8),
+                                        ("learned", abi.SOLVER_MIXED, abi.WARM_MLP, 1e-8)):
+            g.set(abi.F_PRESSPPE, xp)
+            g.set(abi.F_PRESSPPE_PREV, xq)
+            g.set_solver(solver, warm, tol, 20000)
+            g.run_op("CALC_PRESS")
+            st = g.last_stats()
+            assert st.ppeRelResidual <= tol
+            out[name] = (st.ppeInitialRelResidual, st.ppeIterations, g.get(abi.F_PRESS))
+        for name in ("previous", "extrapolated", "learned"):
+            assert _rel(out[name][2], out["reference"][2]) < 1e-6
+        rows.append({k: v[:2] for k, v in out.items()})
+        for op in OPS_AFTER:
+            g.run_op(op)
+    g.close()
+    r0 = {k: np.array([r[k][0] for r in rows]) for k in ("previous", "extrapolated", "learned")}
+    it = {k: np.array([r[k][1] for r in rows]) for k in ("previous", "extrapolated", "learned")}
+    print("initial relative residual (mean): previous %.3e  extrapolated %.3e  learned %.3e"
+          % (r0["previous"].mean(), r0["extrapolated"].mean(), r0["learned"].mean()))
+    print("inner iterations (mean): previous %.2f  extrapolated %.2f  learned %.2f"
+          % (it["previous"].mean(), it["extrapolated"].mean(), it["learned"].mean()))
+    print("network gain over the extrapolated start: residual x%.3f, iterations %+.2f"
+          % (r0["extrapolated"].mean() / r0["learned"].mean(), it["extrapolated"].mean() - it["learned"].mean()))
+    # the residual-minimising step never leaves a larger residual than the extrapolation
+    assert np.all(r0["learned"] <= r0["extrapolated"] * (1.0 + 1e-6))
+    # and the learned start beats the reference's previous-step start
+    assert r0["learned"].mean() < r0["previous"].mean()

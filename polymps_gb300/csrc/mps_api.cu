@@ -37,6 +37,8 @@ struct mpsgpu_s {
     // host mirrors of a few scalars
     bool listValid = false;
     bool masksValid = false;
+    bool skinValid = false;    // the nbr rows hold the start-of-step skin list of this bucket list
+    int skinOn = 1;            // DF32 tier: viscosity and the post-prediction list from the skin list
     bool cacheValid = false;   // per-entry FP64 weights of the current list
     int persistent = 1;        // PPE launch: 0 per kernel, 1 single cooperative launch, 2 + staged ELL tiles
     double timeCurrent = 0.0;
@@ -50,7 +52,7 @@ struct mpsgpu_s {
 };
 
 // ------------------------------------------------------------------ profiler
-void Prof::begin(int c, cudaStream_t s) {
+void Prof::begin(int c, cudaStream_t s, bool count) {
     if (2 * used + 2 > ev.size()) {
         for (int k = 0; k < 64; k++) {
             cudaEvent_t e;
@@ -59,7 +61,7 @@ void Prof::begin(int c, cudaStream_t s) {
         }
         cls.resize(ev.size() / 2);
     }
-    cls[used] = c;
+    cls[used] = count ? c : (c | 0x10000);   // 0x10000: time only, no call counted
     cudaEventRecord(ev[2 * used], s);
     open.push_back(used);
     used++;
@@ -78,8 +80,9 @@ int Prof::flush() {
     for (size_t k = 0; k < used; k++) {
         float ms = 0;
         cudaEventElapsedTime(&ms, ev[2 * k], ev[2 * k + 1]);
-        this->ms[cls[k]] += ms;
-        calls[cls[k]]++;
+        const int c = cls[k] & 0xffff;
+        this->ms[c] += ms;
+        if (!(cls[k] & 0x10000)) calls[c]++;
     }
     used = 0;
     return 0;
@@ -159,10 +162,16 @@ static bool df32(mpsgpu_t h) { return h->d.prec == MPSGPU_PRECISION_DF32; }
 static void ensureList(mpsgpu_t h) {
     if (h->listValid) return;
     if (h->prof.on) h->prof.begin(PROF_NEIGHBOR_LIST, h->s);
-    if (df32(h)) launchNeighborListDF(h->d, h->s);
-    else launchNeighborList(h->d, h->s);
+    if (df32(h) && h->skinValid) {
+        launchNeighborFilterDF(h->d, h->s);
+        countLaunch(5);   // FP32 copies (2), skin check, filter (listed + unlisted particles)
+    } else {
+        if (df32(h)) launchNeighborListDF(h->d, h->s);
+        else launchNeighborList(h->d, h->s);
+        countLaunch(df32(h) ? 4 : 3);   // FP32 copies (2), list build (DF32: + unlisted particles)
+    }
+    h->skinValid = false;
     if (h->prof.on) h->prof.end(h->s);
-    countLaunch(df32(h) ? 4 : 3);   // FP32 copies (2), list build (DF32: + unlisted particles)
     h->listValid = true;
     h->masksValid = false;
     h->cacheValid = !df32(h);   // the FP64 list build stores the per-entry weights
@@ -306,9 +315,23 @@ static int runOpBody(mpsgpu_t h, int op) {
             if (rn) { h->renumberCountdown = h->renumberEvery; countLaunch(renumberLaunches()); }
             h->renumberCountdown--;
             invalidate();
+            h->skinValid = false;
             break;
         }
-        case MPS_OP_VISCOSITY: if (x) launchViscosityDF(d, s); else launchViscosity(d, s); break;
+        case MPS_OP_VISCOSITY:
+            if (x && h->skinOn) {
+                // start-of-step list with a skin: the viscosity sweep reads it, and the list of
+                // the predicted positions is filtered from it (ensureList)
+                if (h->prof.on) { h->prof.end(s); h->prof.begin(PROF_NEIGHBOR_LIST, s, false); }
+                launchSkinListDF(d, s);
+                if (h->prof.on) { h->prof.end(s); h->prof.begin(MPS_OP_VISCOSITY, s, false); }
+                launchViscosityListDF(d, s);
+                invalidate();
+                h->skinValid = true;
+                countLaunch(2);   // skin list (listed + unlisted particles); the sweep is counted below
+            } else if (x) launchViscosityDF(d, s);
+            else launchViscosity(d, s);
+            break;
         case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
         case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
         case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); invalidate(); break;
@@ -542,6 +565,9 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.velLo, n);
     A(d.pressDF, n);
     A(d.concDF, n);
+    A(d.posSkin, n);
+    A(d.skinCell, n);
+    A(d.skinFlag, 2);
     A(d.corrDF, (size_t)9 * n);
     A(d.nbrCount, n);
     A(d.nbr, (size_t)d.K * n);
@@ -575,6 +601,15 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         d.bandHi = (float)(d.reMax2 + band(d.reMax2));
         d.bandHiS = (float)(p->reS2 + band(p->reS2));
         d.bandHiL = (float)(p->reL2 + band(p->reL2));
+        // start-of-step skin list: reMax + 0.15 l0 (covers steps that move no particle by
+        // more than 0.075 l0 from its start position; otherwise the list is rebuilt)
+        {
+            double skin = 0.15 * p->partDist;
+            double rs = std::sqrt(d.reMax2) + skin;
+            d.skinR2 = (float)(rs * rs + band(rs * rs));
+            double mv = 0.5 * skin - 8.0 * std::ldexp(1.0, -24) * X;   // FP32 hi-part error of both copies
+            d.skinMove2 = (float)(mv > 0.0 ? mv * mv : 0.0);
+        }
         // float-float squared distances: each coordinate difference is within
         // 4 * 2^-48 * X of the FP64 one (storage of both lo parts, the rounded lo difference
         // and the reference's own rounding), the float-float products and sums add about
@@ -767,6 +802,7 @@ int mpsgpu_set_precision(mpsgpu_t h, int precision) {
     if (precision != h->d.prec) {
         h->d.prec = precision;
         h->listValid = false;
+        h->skinValid = false;
         h->masksValid = false;
         h->cacheValid = false;
     }
@@ -894,6 +930,7 @@ int mpsgpu_set_field(mpsgpu_t h, int f, const void* host) {
     fromRef(h, kind, p, n);
     // any state change can alter list membership, masks or the near-wall set
     h->listValid = false;
+    h->skinValid = false;
     h->masksValid = false;
     h->cacheValid = false;
     if (f == MPS_F_POS) launchPosf(h->d, h->s);

@@ -68,6 +68,15 @@ struct Dev {
     float4 *posLo, *posLoCell, *velHi, *velLo;
     float2* pressDF;
     float2* concDF;                 // shifting concentration as a float-float pair
+    // start-of-step neighbour list with a skin (DF32 tier): candidates within reL + skin of
+    // the start positions, in scan order; the viscosity sweep reads it, and the list of the
+    // predicted positions is filtered from it while every particle stays within half the
+    // skin of its start, no particle was removed and its bucket is unchanged
+    float4* posSkin;                // start positions (hi parts)
+    long long* skinCell;            // bucket coordinates of the start position (scan window)
+    int* skinFlag;                  // [0] set: the skin list no longer covers the list
+    float skinR2;                   // FP32 squared radius of the skin list (with the band)
+    float skinMove2;                // FP32 squared displacement bound (half the skin, less the band)
     float mgS, mgL, mgMax, mgColl, mgSide;
     // float-float (hi, lo) constants of the DF32 sweeps, converted once on the host
     struct DfK {

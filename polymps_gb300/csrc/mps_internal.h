@@ -23,7 +23,7 @@ struct Prof {
     size_t used = 0;
     double ms[PROF_NCLASS] = {0};
     long long calls[PROF_NCLASS] = {0};
-    void begin(int c, cudaStream_t s);
+    void begin(int c, cudaStream_t s, bool count = true);
     void end(cudaStream_t s);
     int flush();                      // synchronises on the last event, accumulates
     void reset();
@@ -78,6 +78,11 @@ void launchPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallViscosityDF(const Dev& d, cudaStream_t s);
 void launchShiftingDF(const Dev& d, cudaStream_t s);
+// start-of-step list with a skin: build, viscosity over it, and the list of the current
+// positions filtered from it
+void launchSkinListDF(const Dev& d, cudaStream_t s);
+void launchViscosityListDF(const Dev& d, cudaStream_t s);
+void launchNeighborFilterDF(const Dev& d, cudaStream_t s);
 void launchShiftVelApply(const Dev& d, cudaStream_t s);
 void launchApplyShift(const Dev& d, cudaStream_t s);
 

@@ -152,6 +152,7 @@ __global__ void k_out_serial(Dev d, const int* flags, int* counter) {
     }
     *d.nLive = newN;
     *counter = removed;
+    if (removed) d.skinFlag[0] = 1;   // indices moved: the start-of-step list is stale
 }
 void launchOutOfDomain(const Dev& d, int* flags, int* counter, cudaStream_t s) {
     cudaMemsetAsync(counter, 0, sizeof(int), s);

@@ -831,3 +831,138 @@ void launchShiftingDF(const Dev& d, cudaStream_t s) {
         launchApplyShift(d, s);
     }
 }
+
+// ------------------------------------------------------------------ start-of-step list
+// Scan window key of a position: its three bucket coordinates (out-of-grid included).
+__device__ __forceinline__ long long cellKeyOf(const Dev& d, dvec4 p) {
+    int ix, iy, iz;
+    bucketCoords(d.P, p.x, p.y, p.z, ix, iy, iz);
+    return ((long long)(iz & 0x1fffff) << 42) | ((long long)(iy & 0x1fffff) << 21) | (long long)(ix & 0x1fffff);
+}
+// Candidates of the 27-bucket scan within reMax + skin of the start positions (FP32 test
+// against a radius that includes the rounding band: a superset of every list the step's
+// sweeps can need while the particles stay within half the skin), in scan order.
+template <bool STRAY>
+__global__ void __launch_bounds__(128) k_build_skin_df(Dev d) {
+    const int i = scanParticle<STRAY>(d);
+    if (i < 0) return;
+    const dvec4 pi = d.pos[i];
+    const float4 hi = d.posf[i];
+    int cnt = 0;
+    const size_t N0 = d.N0;
+    forCellsDF(d, pi, hi, d.skinR2, [&](int j, int, float4) {
+        if (j == i) return;
+        if (cnt < d.K) d.nbr[(size_t)cnt * N0 + i] = j;
+        cnt++;
+    });
+    d.nbrCount[i] = cnt > d.K ? d.K + 1 : cnt;   // K + 1: the row overflowed, rescanned where read
+    d.posSkin[i] = hi;
+    d.skinCell[i] = cellKeyOf(d, pi);
+}
+void launchSkinListDF(const Dev& d, cudaStream_t s) {
+    cudaMemsetAsync(d.skinFlag, 0, sizeof(int), s);
+    k_build_skin_df<false><<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+    k_build_skin_df<true><<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}
+
+// Viscosity (the sweep of k_visc_df: same entries in the same scan order, same float-float
+// arithmetic, so the same sums) over the start-of-step list instead of the 27 buckets.
+__global__ void __launch_bounds__(128) k_visc_list_df(Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    const dvec4 pi = d.pos[i];
+    const float4 hi = d.posf[i], li = d.posLo[i];
+    const float4 vh = d.velHi[i], vl = d.velLo[i];
+    const SideDF sc = sideDF(d, i, pi);
+    const df R2 = K(d.k.reL2), neuW = K(d.k.neuW), neuF = K(d.k.neuF);
+    const RadiusDF RL = {K(d.k.reL), K(d.k.invReL)};
+    df ax = dfF(0.f), ay = dfF(0.f), az = dfF(0.f);
+    auto pair = [&](int j, float4 hj, float4 lj) {
+        PairF q = pairDF(hj, lj, hi, li);
+        if (!inBallDF(d, q.d2, R2, d.mgL, P.reL2, i, j)) return;
+        if (!sideOkDF(d, sc, hj, lj, q.d2, i, j)) return;
+        WeightDF w = weightDF(q.d2, RL, P.weightType);
+        df c = w.w * ((d.type[j] == P.wall) ? neuW : neuF);
+        float4 vhj = d.velHi[j], vlj = d.velLo[j];
+        ax += diffDF(vhj.x, vlj.x, vh.x, vl.x) * c;
+        ay += diffDF(vhj.y, vlj.y, vh.y, vl.y) * c;
+        az += diffDF(vhj.z, vlj.z, vh.z, vl.z) * c;
+    };
+    const int c = d.nbrCount[i];
+    if (c <= d.K) {
+        const int* row = d.nbr + i;
+        for (int k = 0; k < c; k++) {
+            const int j = ldStream(row + (size_t)k * d.N0);
+            const float4 hj = d.posf[j];
+            float ex = hj.x - hi.x, ey = hj.y - hi.y, ez = hj.z - hi.z;
+            if (ex * ex + ey * ey + ez * ez > d.bandHiL) continue;   // outside the reL band
+            pair(j, hj, d.posLo[j]);
+        }
+    } else {
+        forCellsDF(d, pi, hi, d.bandHiL, [&](int j, int s, float4 hj) {
+            if (j != i) pair(j, hj, __ldg(&d.posLoCell[s]));
+        });
+    }
+    double cv = P.coeffViscMultiphase;
+    d.acc[i] = make_dvec4(cv * dD(ax), cv * dD(ay), cv * dD(az), 0.0);
+}
+void launchViscosityListDF(const Dev& d, cudaStream_t s) {
+    launchVelDF(d, s);
+    k_visc_list_df<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}
+
+// The skin list covers the list of the current positions while every particle is within
+// half the skin of its start position (FP32 test with margin).
+__global__ void k_skin_check(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    float4 a = d.posf[i], b = d.posSkin[i];
+    float ex = a.x - b.x, ey = a.y - b.y, ez = a.z - b.z;
+    if (!(ex * ex + ey * ey + ez * ez <= d.skinMove2)) d.skinFlag[0] = 1;
+}
+// List of the current positions (the set and order of k_build_nbr_df) filtered from the
+// skin list; a particle whose scan window changed, whose skin row overflowed, or any
+// particle after the skin list went stale, scans the 27 buckets as k_build_nbr_df does.
+template <bool STRAY>
+__global__ void __launch_bounds__(128) k_filter_nbr_df(Dev d) {
+    const int i = scanParticle<STRAY>(d);
+    if (i < 0) return;
+    const dvec4 pi = d.pos[i];
+    const float4 hi = d.posf[i], li = d.posLo[i];
+    const df R2 = K(d.k.reMax2);
+    const size_t N0 = d.N0;
+    int cnt = 0;
+    auto keep = [&](int j, float4 hj, float4 lj) {
+        float ex = hj.x - hi.x, ey = hj.y - hi.y, ez = hj.z - hi.z;
+        float d2f = ex * ex + ey * ey + ez * ez;
+        if (d2f > d.bandHi) return;
+        if (!(d2f < d.bandLo)) {
+            PairF q = pairDF(hj, lj, hi, li);
+            if (!inBallDF(d, q.d2, R2, d.mgMax, d.reMax2, i, j)) return;
+        }
+        if (cnt < d.K) d.nbr[(size_t)cnt * N0 + i] = j;
+        cnt++;
+    };
+    const int c = d.nbrCount[i];
+    if (!*(volatile int*)d.skinFlag && c <= d.K && d.skinCell[i] == cellKeyOf(d, pi)) {
+        for (int k = 0; k < c; k++) {   // compacted in place: the write index never passes the read index
+            const int j = d.nbr[(size_t)k * N0 + i];
+            keep(j, d.posf[j], d.posLo[j]);
+        }
+    } else {
+        forCellsDF(d, pi, hi, d.bandHi, [&](int j, int s, float4 hj) {
+            if (j != i) keep(j, hj, __ldg(&d.posLoCell[s]));
+        });
+    }
+    if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }
+    d.nbrCount[i] = cnt;
+    warpCount(d.counters, (unsigned)cnt);
+}
+void launchNeighborFilterDF(const Dev& d, cudaStream_t s) {
+    cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long), s);
+    launchPosf(d, s);
+    k_skin_check<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    k_filter_nbr_df<false><<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+    k_filter_nbr_df<true><<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}

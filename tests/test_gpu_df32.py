@@ -65,6 +65,32 @@ def test_df32_neighbor_sets_bit_exact(oracle_mod, mps_lib, name):
     assert np.array_equal(no, ng)
 
 
+@pytest.mark.parametrize("kick", [0.0, 40.0])
+@pytest.mark.parametrize("name", list(CASES))
+def test_df32_skin_list_bit_exact(oracle_mod, mps_lib, name, kick):
+    """The list of the predicted positions filtered from the start-of-step skin list (no
+    kick) or, when particles move beyond half the skin (random velocities of 40 m/s), rebuilt
+    by the fallback scan, equals the oracle's scan of the same positions through the same
+    stale buckets."""
+    from polymps_gb300 import mps
+    o, g = _pair(oracle_mod, mps, CASES[name]())
+    o.initialize()
+    for _ in range(3):
+        o.step()
+    v = o.get(abi.F_VEL)
+    o.set(abi.F_VEL, v + kick * np.random.default_rng(2).standard_normal(v.shape))
+    sync(o, g)
+    for ob in (o, g):
+        for op in ("UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT"):
+            ob.run_op(op)
+    compare(o, g, "after prediction", fields=[abi.F_ACC, abi.F_POS], rtol=1e-8)
+    o.set(abi.F_POS, g.get(abi.F_POS))   # no field set on the GPU side since the skin list
+    co, no = o.neighbors()
+    cg, ng = g.neighbors()
+    assert np.array_equal(co, cg)
+    assert np.array_equal(no, ng)
+
+
 def test_df32_neighbor_sets_adversarial(oracle_mod, mps_lib):
     """Pairs at r^2 = reL^2 and within a few ulps of it: decided by the FP64 fallback."""
     from polymps_gb300 import mps

@@ -42,9 +42,9 @@ def args_():
     a.add_argument("--solver", default="mixed", choices=["mixed", "plain", "matfree", "compact"])
     a.add_argument("--precision", default="df32", choices=["df32", "fp64"],
                    help="neighbour-sweep arithmetic: float-float (df32) or FP64")
-    a.add_argument("--warm", default="auto", choices=["auto", "prev", "mlp", "extrap"],
-                   help="auto: extrapolated (the fastest measured); the learned start is timed in the "
-                        "PPE comparison when its weights are present")
+    a.add_argument("--warm", default="auto", choices=["auto", "prev", "mlp", "extrap", "extrap2"],
+                   help="auto: quadratic extrapolation (the fastest measured); the learned start is "
+                        "timed in the PPE comparison when its weights are present")
     a.add_argument("--scale", type=float, default=1.0, help="l0 multiplier (1 = 864k particles)")
     a.add_argument("--config", type=int, default=3, choices=[2, 3, 5],
                    help="workload: 3 = 864k-particle incompressible dam break (the headline), "
@@ -53,6 +53,7 @@ def args_():
     a.add_argument("--no-cpu-baseline", action="store_true")
     a.add_argument("--cpu-steps", type=int, default=1)
     a.add_argument("--ppe-compare", type=int, default=1)
+    a.add_argument("--ppe-steps", type=int, default=40, help="steps sampled by the PPE comparison")
     a.add_argument("--presort", action="store_true",
                    help="number the input particles in bucket order (input renumbering only)")
     return a.parse_args()
@@ -197,7 +198,7 @@ def run_gb300(a, rank, world, local):
     use_mlp = a.warm == "mlp"
     prec = abi.PRECISION_DF32 if a.precision == "df32" else abi.PRECISION_FP64
     g = mps.MpsGpu(case, solver=solver, tol=1e-8, max_iter=20000, precision=prec)
-    warm = abi.WARM_PREVIOUS if a.warm == "prev" else abi.WARM_EXTRAP
+    warm = {"prev": abi.WARM_PREVIOUS, "extrap": abi.WARM_EXTRAP}.get(a.warm, abi.WARM_EXTRAP2)
     if have_mlp:
         w = np.load(mlp_path)
         g.mlp_set_weights(w["params"], w["norm"])
@@ -238,11 +239,11 @@ def run_gb300(a, rank, world, local):
         v, t = pinned_like(g.get(f))
         host[f] = v
         keep.append(t)
-    # PPE time-to-1e-8 on identical systems: plain FP64 vs mixed vs warm starts (before the
-    # end-to-end section, which re-uploads the state and resets the warm-start history)
+    # PPE time-to-1e-8 on identical systems along further steps: plain FP64 vs mixed vs warm
+    # starts (before the end-to-end section, which re-uploads the state)
     ppe = None
     if a.ppe_compare and rank == 0:
-        ppe = ppe_compare(g, abi, have_mlp)
+        ppe = ppe_compare(g, abi, have_mlp, g.params, (solver, warm, 1e-8, 20000), steps=a.ppe_steps)
     # e2e through the C ABI with host arrays: upload the state from pinned host memory,
     # step, download the result, every step
     h2d = sum(v.nbytes for v in host.values())
@@ -287,7 +288,8 @@ def run_gb300(a, rank, world, local):
         "config": {"workload": WORKLOADS[a.config], "particles": N,
                    "l0": case.params["partDist"], "dt": case.params["timeStep"],
                    "ppe_tol": 1e-8, "solver": a.solver, "precision": a.precision,
-                   "warm_start": {abi.WARM_MLP: "learned", abi.WARM_EXTRAP: "extrapolated", abi.WARM_PREVIOUS: "previous"}[warm],
+                   "warm_start": {abi.WARM_MLP: "learned", abi.WARM_EXTRAP: "extrapolated",
+                                  abi.WARM_EXTRAP2: "quadratic extrapolation", abi.WARM_PREVIOUS: "previous"}[warm],
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "working set > L2 (no flush needed)", "wall_s": round(wall, 3)},
         "e2e": {"value": round(e2e, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
@@ -307,55 +309,101 @@ def run_gb300(a, rank, world, local):
     return out
 
 
-def ppe_compare(g, abi, use_mlp):
-    """Solve the current step's PPE three ways from the same state and warm start."""
-    # advance to the system of the next step: run the ops up to the pressure solve
-    ops = ["UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT", "OUT_OF_DOMAIN", "COLLISION",
-           "WALL_DISTANCE", "WALL_NPCD", "PND_NEIGH_NPCD", "UPDATE_BC"]
-    for op in ops:
-        g.run_op(op)
-    x_prev = g.get(abi.F_PRESSPPE)
-    x_prev2 = g.get(abi.F_PRESSPPE_PREV)
-    res = {}
-    # single-launch solves, then the per-kernel launch path for reference
-    # launch mode: 1 single launch (default), 2 single launch with staged ELL tiles, 3 single
-    # launch with the pipelined inner CG, 0 per kernel
-    variants = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 1),
-                ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 1),
-                ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, 1),
-                ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 1),
-                ("extrapolated_fp32_fp64_staged_tiles", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 2),
-                ("fp32_fp64_pipelined", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 3),
-                ("extrapolated_fp32_fp64_pipelined", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 3),
-                ("matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_PREVIOUS, 1),
-                ("compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_PREVIOUS, 1),
-                ("extrapolated_compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_EXTRAP, 1)]
+def _hist_get(g, abi):
+    return [g.get(f) for f in (abi.F_PRESSPPE, abi.F_PRESSPPE_PREV, abi.F_PRESSPPE_PREV2)]
+
+
+def _hist_set(g, abi, h):
+    for f, v in zip((abi.F_PRESSPPE, abi.F_PRESSPPE_PREV, abi.F_PRESSPPE_PREV2), h):
+        g.set(f, v)
+
+
+def _solve(g, abi, hist, solver, warm, mode=1):
+    g.set_ppe_launch(mode)
+    _hist_set(g, abi, hist)
+    g.set_solver(solver, warm, 1e-8, 20000)
+    g.run_op("CALC_PRESS")
+    st = g.last_stats()
+    return {"ms": st.ppeSolveMs, "iters": st.ppeIterations, "refinements": st.ppeRefinements,
+            "relres": st.ppeRelResidual, "relres0": st.ppeInitialRelResidual}
+
+
+def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4):
+    """PPE time-to-1e-8 of the solvers and warm starts on the same systems, sampled along
+    `steps` further steps of the run (every `every`-th system): each sampled system is
+    solved by every variant from the same warm-start state, then the step is finished
+    with the bench's own solver."""
+    before = ["UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT", "OUT_OF_DOMAIN", "COLLISION"]
+    if params.wallType == 1:
+        before += ["WALL_DISTANCE", "WALL_NPCD"]
+    before += ["PND_NEIGH_NPCD", "UPDATE_BC"]
+    after = ["CORRECTION_MATRIX", "PRESS_GRADIENT"] if params.gradientCorrection else ["PRESS_GRADIENT"]
+    if params.wallType == 1:
+        after += ["WALL_PRESS_GRADIENT", "WALL_VISCOSITY"]
+    after += ["CORRECT", "OUT_OF_DOMAIN"] + (["SHIFTING"] if params.shiftingType else []) + ["OUT_OF_DOMAIN"]
+    main = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS),
+            ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP),
+            ("plain_fp64_quadratic_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP2),
+            ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS),
+            ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP),
+            ("quadratic_extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP2)]
     if use_mlp:
-        variants.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP, 1))
-    variants += [("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 0),
-                 ("fp32_fp64_per_kernel_launch", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 0)]
-    for name, s, w, mode in variants:
-        best = None
-        g.set_ppe_launch(mode)
-        for rep in range(3):
-            g.set(abi.F_PRESSPPE, x_prev)
-            g.set(abi.F_PRESSPPE_PREV, x_prev2)
-            g.set_solver(s, w, 1e-8, 20000)
-            g.run_op("CALC_PRESS")
-            st = g.last_stats()
-            if best is None or st.ppeSolveMs < best["ms"]:
-                best = {"ms": round(st.ppeSolveMs, 3), "iters": st.ppeIterations, "refinements": st.ppeRefinements,
-                        "relres": st.ppeRelResidual, "relres0": st.ppeInitialRelResidual}
-        res[name] = best
-        if name == "plain_fp64":
-            p_ref = g.get(abi.F_PRESSPPE)
-        else:
-            p = g.get(abi.F_PRESSPPE)
-            res[name]["rel_err_vs_fp64"] = float(np.linalg.norm(p - p_ref) / np.linalg.norm(p_ref))
-    g.set_ppe_launch(1)
+        main.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP))
+    # launch-form and inner-operator options: first sampled system only (best of three)
+    alt = [("quadratic_fp32_fp64_staged_tiles", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 2),
+           ("quadratic_fp32_fp64_pipelined", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 3),
+           ("quadratic_compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_EXTRAP2, 1),
+           ("quadratic_matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_EXTRAP2, 1),
+           ("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 0),
+           ("quadratic_fp32_fp64_per_kernel_launch", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 0)]
+    samples = {k: [] for k, _, _ in main}
+    alt_res = {}
+    err = {k: 0.0 for k, _, _ in main}
+    first = None
+    for s in range(steps):
+        for op in before:
+            g.run_op(op)
+        hist = _hist_get(g, abi)
+        if s % every == 0:
+            if first is None:
+                first = s
+            p_ref = None
+            for name, solver, warm in main:
+                r = _solve(g, abi, hist, solver, warm)
+                samples[name].append(r)
+                p = g.get(abi.F_PRESSPPE)
+                if p_ref is None:
+                    p_ref = p
+                else:
+                    err[name] = max(err[name], float(np.linalg.norm(p - p_ref) / np.linalg.norm(p_ref)))
+            if s == first:
+                for name, solver, warm, mode in alt:
+                    best = min((_solve(g, abi, hist, solver, warm, mode) for _ in range(3)), key=lambda r: r["ms"])
+                    alt_res[name] = {k: (round(v, 3) if k == "ms" else v) for k, v in best.items()}
+            g.set_ppe_launch(1)
+        _hist_set(g, abi, hist)
+        g.set_solver(*default)
+        g.run_op("CALC_PRESS")
+        for op in after:
+            g.run_op(op)
+    res = {}
+    for name, _, _ in main:
+        v = samples[name]
+        res[name] = {"ms": round(float(np.mean([r["ms"] for r in v])), 3),
+                     "iters": round(float(np.mean([r["iters"] for r in v])), 2),
+                     "refinements": round(float(np.mean([r["refinements"] for r in v])), 2),
+                     "relres0": float(np.mean([r["relres0"] for r in v])),
+                     "relres_max": float(max(r["relres"] for r in v))}
+        if name != "plain_fp64":
+            res[name]["rel_err_vs_fp64_max"] = err[name]
     base = res["plain_fp64"]["ms"]
     for k in res:
         res[k]["speedup_vs_plain"] = round(base / res[k]["ms"], 3) if res[k]["ms"] > 0 else None
+    for k, v in alt_res.items():
+        v["speedup_vs_plain"] = round(samples["plain_fp64"][0]["ms"] / v["ms"], 3) if v["ms"] > 0 else None
+    res["options_first_system"] = alt_res
+    res["systems"] = len(samples["plain_fp64"])
+    res["steps_sampled"] = "every %d-th of %d steps after the timed run" % (every, steps)
     res["assemble_ms"] = round(g.last_stats().ppeAssembleMs, 3)
     return res
 

@@ -134,6 +134,7 @@ enum MpsField {
     MPS_F_DEVDOT, MPS_F_SOURCE,
     MPS_F_PRESSPPE_PREV,          /* solution of the solve before the last (no reference
                                      array: the warm-start state of the extrapolation) */
+    MPS_F_PRESSPPE_PREV2,         /* and the one before it (quadratic extrapolation) */
     MPS_F_TYPE = 64, MPS_F_BC, MPS_F_NUMNEIGH, MPS_F_NNEIGHWALL, MPS_F_NEARWALL
 };
 
@@ -189,6 +190,7 @@ enum MpsOp {
 #define MPSGPU_WARM_MLP            1   /* learned per-particle MLP correction           */
 #define MPSGPU_WARM_ZERO           2
 #define MPSGPU_WARM_EXTRAPOLATE    3   /* 2 p_n - p_{n-1} of the unclamped solutions       */
+#define MPSGPU_WARM_EXTRAPOLATE2   4   /* 3 p_n - 3 p_{n-1} + p_{n-2} (quadratic)         */
 
 typedef struct mpsgpu_s* mpsgpu_t;
 
@@ -268,12 +270,12 @@ int mpsgpu_get_neighbors(mpsgpu_t h, int* counts, int* nbr, long long nbr_capaci
 int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col,
                    double* val, double* rhs);
 
-/* Learned warm start (N2): MLP 16->64->64->64->1, GELU, BF16 weights, FP32 accumulate.
+/* Learned warm start (N2): MLP 16->64->64->64->1, GELU (tanh form), BF16 weights, FP32 accumulate.
  * Weights are the FP32 master copy in this packed order:
  * W1[64x16] b1[64] W2[64x64] b2[64] W3[64x64] b3[64] W4[1x64] b4[1]  (row-major [out][in]),
  * The normalisation vector holds MPSGPU_MLP_NNORM floats: feature means[16], feature
  * inverse spreads[16], then the target's mean and inverse spread.  The network predicts
- * the correction c of the temporal extrapolation x_e = 2 p_n - p_{n-1}; features 1, 5, 7,
+ * the correction c of the quadratic extrapolation x_e = 3 p_n - 3 p_{n-1} + p_{n-2}; features 1, 5, 7,
  * 14 (pressure differences) and the target are in units of the system scale sigma (RMS
  * over the equation rows of feature 7, the Jacobi step of the extrapolation residual).
  * The warm start is x_e + theta c with theta = argmin ||b - A (x_e + theta c)||, so the

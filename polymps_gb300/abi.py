@@ -104,6 +104,7 @@ F_POS, F_VEL, F_ACC, F_ACCSTAR, F_NPCD, F_GRADC, F_CORR1, F_CORR2, F_CORR3, F_MI
  F_DIFFTERM, F_PNDWALL, F_RIW2, F_DEVDOT, F_SOURCE) = range(32, 46)
 F_TYPE, F_BC, F_NUMNEIGH, F_NNEIGHWALL, F_NEARWALL = range(64, 69)
 F_PRESSPPE_PREV = 46   # warm-start state (no reference array; not in SCALAR_FIELDS)
+F_PRESSPPE_PREV2 = 47
 
 VECTOR_FIELDS = set(range(13))
 SCALAR_FIELDS = set(range(32, 46))
@@ -132,7 +133,7 @@ OPS = [
 OP = {name: k for k, name in enumerate(OPS)}
 
 SOLVER_PLAIN_FP64, SOLVER_MIXED, SOLVER_MIXED_MATFREE, SOLVER_MIXED_COMPACT = 0, 1, 2, 3
-WARM_PREVIOUS, WARM_MLP, WARM_ZERO, WARM_EXTRAP = 0, 1, 2, 3
+WARM_PREVIOUS, WARM_MLP, WARM_ZERO, WARM_EXTRAP, WARM_EXTRAP2 = 0, 1, 2, 3, 4
 PRECISION_FP64, PRECISION_DF32 = 0, 1
 MLP_NPARAM = 64 * 16 + 64 + 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1
 MLP_NFEAT = 16
@@ -163,7 +164,7 @@ def params_to_dict(p):
 def field_buffer(field, n):
     if field in VECTOR_FIELDS:
         return np.zeros((n, 3), dtype=np.float64)
-    if field in SCALAR_FIELDS or field == F_PRESSPPE_PREV:
+    if field in SCALAR_FIELDS or field in (F_PRESSPPE_PREV, F_PRESSPPE_PREV2):
         return np.zeros(n, dtype=np.float64)
     if field in INT_FIELDS:
         return np.zeros(n, dtype=np.int32)

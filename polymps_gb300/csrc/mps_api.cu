@@ -227,7 +227,10 @@ static int calcPress(mpsgpu_t h) {
     cudaEventRecord(h->ea1, h->s);
     // warm start: previous unclamped solution (reference), zero, or the learned predictor
     if (h->warm == MPSGPU_WARM_ZERO) cudaMemsetAsync(h->B.x, 0, sizeof(double) * h->N0, h->s);
-    if (h->warm == MPSGPU_WARM_EXTRAPOLATE) { launchWarmExtrapolate(h->d, h->B, h->s); countLaunch(1); }
+    if (h->warm == MPSGPU_WARM_EXTRAPOLATE || h->warm == MPSGPU_WARM_EXTRAPOLATE2) {
+        launchWarmExtrapolate(h->d, h->B, h->s, h->warm == MPSGPU_WARM_EXTRAPOLATE2);
+        countLaunch(1);
+    }
     cudaEventRecord(h->es0, h->s);
     h->B.prepared = df32(h) ? 1 : 0;   // the DF32 assembly writes the FP32 copies itself
     if (h->warm == MPSGPU_WARM_MLP) {
@@ -544,6 +547,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     for (int** v : {&d.type, &d.bc, &d.numNeigh, &d.nNeighWall, &d.nearWall}) A(*v, n);
     A(d.posf, n);
     A(d.pressPPEprev, n);
+    A(d.pressPPEprev2, n);
     A(d.cellOf, n);
     A(d.cellStart, d.nB + 2);
     A(d.cellCount, d.nB + 2);
@@ -817,7 +821,7 @@ int mpsgpu_set_ppe_launch(mpsgpu_t h, int mode) {
 
 int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm, double tol, int max_iter) {
     if (!h || (solver != MPSGPU_SOLVER_PLAIN_FP64 && solver != MPSGPU_SOLVER_MIXED && solver != MPSGPU_SOLVER_MIXED_MATFREE &&
-               solver != MPSGPU_SOLVER_MIXED_COMPACT) || warm < 0 || warm > 3 || !(tol > 0))
+               solver != MPSGPU_SOLVER_MIXED_COMPACT) || warm < 0 || warm > 4 || !(tol > 0))
         return MPSGPU_ERR_ARG;
     if (warm == MPSGPU_WARM_MLP && !h->mlp.ready) { g_lastError = "MLP weights not set"; return MPSGPU_ERR_ARG; }
     h->solver = solver; h->warm = warm; h->tol = tol; h->maxIter = max_iter;
@@ -880,6 +884,7 @@ static void* fieldPtr(mpsgpu_t h, int f, int* kind) {
         case MPS_F_DEVDOT: return d.devDot;
         case MPS_F_SOURCE: return d.source;
         case MPS_F_PRESSPPE_PREV: return d.pressPPEprev;
+        case MPS_F_PRESSPPE_PREV2: return d.pressPPEprev2;
         default: break;
     }
     *kind = 2;

@@ -191,7 +191,7 @@ static void launchRenumber(const Dev& d, int* perm, void* scratch, cudaStream_t 
     for (dvec4* v : {d.pos, d.vel, d.acc, d.accStar, d.mirror, d.wallPos, d.polyNormal, d.npcd, d.gradC,
                      d.forceWall, d.c1, d.c2, d.c3, d.dvel, d.shift})
         permute(v, perm, scratch, n, s);
-    for (double* v : {d.press, d.pressPPE, d.pressPPEprev, d.pndi, d.pndki, d.pndski, d.pndSmall, d.npcd2, d.conc,
+    for (double* v : {d.press, d.pressPPE, d.pressPPEprev, d.pressPPEprev2, d.pndi, d.pndki, d.pndski, d.pndSmall, d.npcd2, d.conc,
                       d.velDiv, d.diffTerm, d.pndWall, d.riw2, d.devDot, d.source, d.aux1, d.aux2})
         permute(v, perm, scratch, n, s);
     for (int* v : {d.type, d.bc, d.numNeigh, d.nNeighWall, d.nearWall}) permute(v, perm, scratch, n, s);

@@ -45,6 +45,7 @@ struct Dev {
     int *type, *bc, *numNeigh, *nNeighWall, *nearWall;
     float4* posf;      // FP32 copy of pos - domainMin (neighbour prefilter, FP32 sums)
     double* pressPPEprev;   // unclamped PPE solution of the solve before the last (warm start)
+    double* pressPPEprev2;  // and the one before it
     // Storage numbering: particles are stored in bucket order (renumbered when the buckets
     // are rebuilt every few steps) and identified by their reference index at the API:
     // orig[s] = reference index of the particle stored in slot s, slotOf[r] = its slot.

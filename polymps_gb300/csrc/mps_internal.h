@@ -123,7 +123,7 @@ struct PpeBuffers {
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeAssembleDF(const Dev& d, const PpeBuffers& B, cudaStream_t s);
-void launchWarmExtrapolate(const Dev& d, const PpeBuffers& B, cudaStream_t s);
+void launchWarmExtrapolate(const Dev& d, const PpeBuffers& B, cudaStream_t s, bool quadratic = false);
 // FP32 copies of the assembled matrix (valf, diagf, diagInvf) for the FP64 assembly
 void launchMixedPrepare(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 // Returns iterations and final relative residual through host pointers (synchronises).

@@ -5,7 +5,7 @@
 // at a time; the FP32 accumulator fragment of one layer is re-packed in registers as the
 // BF16 A fragment of the next (the m16n8 C layout of two adjacent n-tiles is the m16k16 A
 // layout), so activations never leave the register file.  The network predicts the
-// correction c of the temporal extrapolation x_e = 2 p_n - p_{n-1} of the unclamped
+// correction c of the temporal extrapolation x_e = 3 p_n - 3 p_{n-1} + p_{n-2} of the unclamped
 // pressure on equation rows (in target units, de-normalised on output); the warm start is
 // x0 = x_e + theta c with the residual-minimising step theta, and x0 = 0 on the identity
 // rows of surface/dummy particles (their exact solution).
@@ -46,9 +46,26 @@ static_assert(NPARAM == MPSGPU_MLP_NPARAM, "parameter packing");
 #define S1 24
 #define S2 72
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks & Gimpel, "Gaussian Error Linear Units", 2016):
+// gelu(x) = x/2 (1 + tanh(k0 (x + k1 x^3))), k0 = sqrt(2/pi), k1 = 0.044715, with the
+// hardware tanh (tanh.approx.f32, one MUFU op); the network is trained with the same
+// function, so the approximation is part of its definition.
+#define GELU_K0 0.7978845608028654f
+#define GELU_K1 0.044715f
+__device__ __forceinline__ float tanhHw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float gelu(float x) {
+    const float t = tanhHw(GELU_K0 * x * fmaf(GELU_K1 * x, x, 1.0f));
+    return 0.5f * x * (1.0f + t);
+}
+// d gelu / dx = (1 + t)/2 + x/2 (1 - t^2) k0 (1 + 3 k1 x^2)
 __device__ __forceinline__ float gelud(float x) {
-    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+    const float x2 = x * x;
+    const float t = tanhHw(GELU_K0 * x * fmaf(GELU_K1, x2, 1.0f));
+    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_K0 * fmaf(3.0f * GELU_K1, x2, 1.0f);
 }
 
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
@@ -179,7 +196,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float* feat, int n, c
 
 // ------------------------------------------------------------------ features
 // The network corrects the temporal extrapolation of the unclamped solutions,
-// x_e = 2 p_n - p_{n-1}: x0 = x_e + correction on the rows that carry an equation.
+// x_e = 3 p_n - 3 p_{n-1} + p_{n-2}: x0 = x_e + correction on the rows that carry an equation.
 // Raw features of row i of the new system (normalised inside the network); pressures in
 // Pa (1, 5, 7 and 14 then in units of the system scale sigma below), lengths in m,
 // velocities in m/s:
@@ -190,8 +207,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float* feat, int n, c
 // 11 A_ii / (coeffPPE n0)  12 wall PND               13 height along -g
 // 14 (b_i - b_i of the last solve) / A_ii            15 (pndi - pndki)/n0
 __device__ __forceinline__ double extrapBase(const Dev& d, int j) {
-    double p = d.pressPPE[j];
-    return (p + p) - d.pressPPEprev[j];
+    return 3.0 * (d.pressPPE[j] - d.pressPPEprev[j]) + d.pressPPEprev2[j];
 }
 // Block sums of two FP64 values per thread into part[block] and part[gridDim + block].
 __device__ __forceinline__ void blockPartials2(double s0, double s1, double* part) {

@@ -107,7 +107,7 @@ __device__ void swapSlots(const Dev& d, int a, int b) {
     for (dvec4* v : {d.pos, d.vel, d.acc, d.accStar, d.mirror, d.wallPos, d.polyNormal, d.npcd, d.gradC,
                      d.forceWall, d.c1, d.c2, d.c3, d.dvel, d.shift})
         sw(v, a, b);
-    for (double* v : {d.press, d.pressPPE, d.pressPPEprev, d.pndi, d.pndki, d.pndski, d.pndSmall, d.npcd2, d.conc,
+    for (double* v : {d.press, d.pressPPE, d.pressPPEprev, d.pressPPEprev2, d.pndi, d.pndki, d.pndski, d.pndSmall, d.npcd2, d.conc,
                       d.velDiv, d.diffTerm, d.pndWall, d.riw2, d.devDot, d.source, d.aux1, d.aux2})
         sw(v, a, b);
     for (int* v : {d.type, d.bc, d.numNeigh, d.nNeighWall, d.nearWall, d.cellOf}) sw(v, a, b);
@@ -136,7 +136,7 @@ __global__ void k_out_serial(Dev d, const int* flags, int* counter) {
             mv(d.pndki, i, l); mv(d.pndski, i, l); mv(d.pndSmall, i, l); mv(d.npcd2, i, l); mv(d.conc, i, l);
             mv(d.velDiv, i, l); mv(d.diffTerm, i, l); mv(d.nearWall, i, l); mv(d.nNeighWall, i, l);
             mv(d.pndWall, i, l); mv(d.devDot, i, l); mv(d.riw2, i, l);
-            if (P.mpsType == 2 || P.mpsType == 3) { mv(d.pressPPE, i, l); mv(d.source, i, l); mv(d.pressPPEprev, i, l); }
+            if (P.mpsType == 2 || P.mpsType == 3) { mv(d.pressPPE, i, l); mv(d.source, i, l); mv(d.pressPPEprev, i, l); mv(d.pressPPEprev2, i, l); }
             mv(d.acc, i, l); mv(d.accStar, i, l); mv(d.pos, i, l); mv(d.vel, i, l); mv(d.npcd, i, l);
             mv(d.gradC, i, l); mv(d.c1, i, l); mv(d.c2, i, l); mv(d.c3, i, l); mv(d.dvel, i, l);
             mv(d.wallPos, i, l); mv(d.mirror, i, l); mv(d.polyNormal, i, l); mv(d.forceWall, i, l);

@@ -77,21 +77,24 @@ __global__ void k_ppe_copy_back(Dev d, PpeBuffers B) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     double x = B.x[i];
+    d.pressPPEprev2[i] = d.pressPPEprev[i];
     d.pressPPEprev[i] = d.pressPPE[i];
     d.pressPPE[i] = x;
     d.source[i] = B.b[i];
     d.press[i] = x < 0.0 ? 0.0 : x;
 }
-// Warm start by linear extrapolation in time of the unclamped solutions, x0 = 2 p_n - p_{n-1},
-// on the rows of the new system that carry an equation (zero on the identity rows).
-__global__ void k_warm_extrap(Dev d, PpeBuffers B) {
+// Warm start by extrapolation in time of the unclamped solutions on the rows of the new
+// system that carry an equation (zero on the identity rows): linear x0 = 2 p_n - p_{n-1}
+// or quadratic x0 = 3 p_n - 3 p_{n-1} + p_{n-2}.
+__global__ void k_warm_extrap(Dev d, PpeBuffers B, int quad) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
-    double p = d.pressPPE[i];
-    B.x[i] = (d.bc[i] == d.P.inner) ? (p + p) - d.pressPPEprev[i] : 0.0;
+    double p = d.pressPPE[i], q = d.pressPPEprev[i];
+    double x = quad ? 3.0 * (p - q) + d.pressPPEprev2[i] : (p + p) - q;
+    B.x[i] = (d.bc[i] == d.P.inner) ? x : 0.0;
 }
-void launchWarmExtrapolate(const Dev& d, const PpeBuffers& B, cudaStream_t s) {
-    k_warm_extrap<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B);
+void launchWarmExtrapolate(const Dev& d, const PpeBuffers& B, cudaStream_t s, bool quadratic) {
+    k_warm_extrap<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, quadratic ? 1 : 0);
 }
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s) {
     k_ppe_copy_back<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B);

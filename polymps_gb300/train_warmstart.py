@@ -4,7 +4,8 @@
    plain FP64 solver (previous-step warm start, tolerance 1e-10) and record, for every
    inner row of every recorded step, the 16 features of the assembled system and the
    difference between the converged pressure and the temporal extrapolation
-   2 p_n - p_{n-1} of the two previous solutions (the network learns that correction).
+   3 p_n - 3 p_{n-1} + p_{n-2} of the three previous solutions (the network learns that
+   correction).
 2. Fit the feature normalisation on the recorded set, then run Adam on mini-batches with
    the fused BF16 tensor-core forward/backward kernel.
 3. Evaluate on the l0 = 0.005 case (864,000 particles): PPE iterations and time to 1e-8
@@ -51,11 +52,13 @@ def record(steps, every, tol, scale=1.0, warmup=20):
 
 
 def evaluate(params, norm, scale=1.0, steps=30, warmup=10, tol=1e-8):
-    """Same systems, six solves each: the plain FP64 CG and the FP32/FP64 refinement solver,
-    each from the previous-step, the extrapolated and the learned warm start."""
+    """Same systems, eight solves each: the plain FP64 CG and the FP32/FP64 refinement
+    solver, each from the previous-step, the linear and quadratic extrapolation and the
+    learned warm start."""
     c = cases.config(3, scale=scale)
-    g = mps.MpsGpu(c, solver=abi.SOLVER_PLAIN_FP64, tol=tol, max_iter=20000, precision=abi.PRECISION_DF32)
+    g = mps.MpsGpu(c, solver=abi.SOLVER_MIXED, tol=tol, max_iter=20000, precision=abi.PRECISION_DF32)
     g.mlp_set_weights(params, norm)
+    g.set_solver(abi.SOLVER_MIXED, abi.WARM_EXTRAP2, tol, 20000)
     g.initialize()
     g.run(warmup)
     ops = ["UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT", "OUT_OF_DOMAIN", "COLLISION",
@@ -64,29 +67,26 @@ def evaluate(params, norm, scale=1.0, steps=30, warmup=10, tol=1e-8):
     for s in range(steps):
         for op in ops:
             g.run_op(op)
-        x_prev = g.get(abi.F_PRESSPPE)
-        x_prev2 = g.get(abi.F_PRESSPPE_PREV)
+        hist = [g.get(f) for f in (abi.F_PRESSPPE, abi.F_PRESSPPE_PREV, abi.F_PRESSPPE_PREV2)]
         res = {}
-        for name, solver, warm in (("plain_prev", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS),
-                                   ("plain_extrap", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP),
-                                   ("plain_mlp", abi.SOLVER_PLAIN_FP64, abi.WARM_MLP),
-                                   ("mixed_prev", abi.SOLVER_MIXED, abi.WARM_PREVIOUS),
-                                   ("mixed_extrap", abi.SOLVER_MIXED, abi.WARM_EXTRAP),
-                                   ("mixed_mlp", abi.SOLVER_MIXED, abi.WARM_MLP)):
-            g.set(abi.F_PRESSPPE, x_prev)
-            g.set(abi.F_PRESSPPE_PREV, x_prev2)
-            g.set_solver(solver, warm, tol, 20000)
-            g.run_op("CALC_PRESS")
-            st = g.last_stats()
-            res[name] = (st.ppeIterations, st.ppeSolveMs, st.ppeInitialRelResidual, st.ppeRelResidual)
+        for solver, sname in ((abi.SOLVER_PLAIN_FP64, "plain"), (abi.SOLVER_MIXED, "mixed")):
+            for warm, wname in ((abi.WARM_PREVIOUS, "prev"), (abi.WARM_EXTRAP, "extrap"),
+                                (abi.WARM_EXTRAP2, "extrap2"), (abi.WARM_MLP, "mlp")):
+                for f, h in zip((abi.F_PRESSPPE, abi.F_PRESSPPE_PREV, abi.F_PRESSPPE_PREV2), hist):
+                    g.set(f, h)
+                g.set_solver(solver, warm, tol, 20000)
+                g.run_op("CALC_PRESS")
+                st = g.last_stats()
+                res[sname + "_" + wname] = (st.ppeIterations, st.ppeSolveMs, st.ppeInitialRelResidual,
+                                            st.ppeRelResidual)
         rows.append(res)
-        # finish the step with the reference solution (plain FP64 from the previous warm start)
-        g.set(abi.F_PRESSPPE, x_prev)
-        g.set(abi.F_PRESSPPE_PREV, x_prev2)
-        g.set_solver(abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, tol, 20000)
+        # finish the step from the quadratic extrapolation with the refinement solver
+        for f, h in zip((abi.F_PRESSPPE, abi.F_PRESSPPE_PREV, abi.F_PRESSPPE_PREV2), hist):
+            g.set(f, h)
+        g.set_solver(abi.SOLVER_MIXED, abi.WARM_EXTRAP2, tol, 20000)
         g.run_op("CALC_PRESS")
-        for op in ["CORRECTION_MATRIX", "PRESS_GRADIENT", "WALL_PRESS_GRADIENT", "WALL_VISCOSITY",
-                   "CORRECT", "OUT_OF_DOMAIN"]:
+        for op in ["CORRECTION_MATRIX", "PRESS_GRADIENT", "WALL_PRESS_GRADIENT", "WALL_VISCOSITY", "CORRECT",
+                   "OUT_OF_DOMAIN"]:
             g.run_op(op)
     g.close()
     summ = {}

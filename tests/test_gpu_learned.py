@@ -3,9 +3,9 @@
 The network is trained on the GPU by the library's own kernels (records of the plain FP64
 solver on the 3D incompressible dam break, fused BF16 forward/backward, Adam), then the
 same held-out PPE systems are solved by the FP32/FP64 refinement solver from three
-starts: the previous-step pressure (the reference's warm start), the temporal
-extrapolation 2 p_n - p_{n-1} (the learned start without the network), and the learned
-start x_e + theta c (network correction c, residual-minimising step theta).
+starts: the previous-step pressure (the reference's warm start), the quadratic
+extrapolation x_e = 3 p_n - 3 p_{n-1} + p_{n-2} (the learned start without the network),
+and the learned start x_e + theta c (network correction c, residual-minimising step theta).
 """
 import numpy as np
 import pytest
@@ -48,14 +48,15 @@ def test_learned_warm_start_gain(mps_lib):
     for s in range(8):   # held-out systems: later steps of the same run
         for op in OPS_BEFORE:
             g.run_op(op)
-        xp, xq = g.get(abi.F_PRESSPPE), g.get(abi.F_PRESSPPE_PREV)
+        xp, xq, xr = g.get(abi.F_PRESSPPE), g.get(abi.F_PRESSPPE_PREV), g.get(abi.F_PRESSPPE_PREV2)
         out = {}
         for name, solver, warm, tol in (("reference", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 1e-12),
                                         ("previous", abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 1e-8),
-                                        ("extrapolated", abi.SOLVER_MIXED, abi.WARM_EXTRAP, 1e-8),
+                                        ("extrapolated", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 1e-8),
                                         ("learned", abi.SOLVER_MIXED, abi.WARM_MLP, 1e-8)):
             g.set(abi.F_PRESSPPE, xp)
             g.set(abi.F_PRESSPPE_PREV, xq)
+            g.set(abi.F_PRESSPPE_PREV2, xr)
             g.set_solver(solver, warm, tol, 20000)
             g.run_op("CALC_PRESS")
             st = g.last_stats()

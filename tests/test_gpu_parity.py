@@ -244,8 +244,20 @@ def _bf16(x):
     return r.astype(np.uint32).view(np.float32)
 
 
+# GELU in its tanh form, as the kernels evaluate it (with the hardware tanh)
+_K0, _K1 = np.sqrt(2.0 / np.pi), 0.044715
+
+
+def _gelu(z):
+    return 0.5 * z * (1.0 + np.tanh(_K0 * (z + _K1 * z ** 3)))
+
+
+def _gelud(z):
+    t = np.tanh(_K0 * (z + _K1 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _K0 * (1.0 + 3.0 * _K1 * z * z)
+
+
 def _mlp_ref(params, norm, feat, want_grad=False, target=None):
-    from scipy.special import erf
     H, NF = 64, 16
     o = 0
     W1 = params[o:o + H * NF].reshape(H, NF); o += H * NF
@@ -256,7 +268,7 @@ def _mlp_ref(params, norm, feat, want_grad=False, target=None):
     b3 = params[o:o + H]; o += H
     W4 = params[o:o + H]; o += H
     b4 = params[o]
-    g = lambda z: 0.5 * z * (1 + erf(z / np.sqrt(2)))
+    g = _gelu
     x = _bf16((feat - norm[:16]) * norm[16:32]).astype(np.float64)
     z1 = x @ _bf16(W1).T.astype(np.float64) + b1
     h1 = _bf16(g(z1))
@@ -286,7 +298,6 @@ def test_mlp_forward_matches_cpu(mps_lib, seed):
 def _mlp_grad_ref(params, feat, target):
     """Exact backprop (FP64) of the network with BF16-rounded weights and hidden inputs,
     as the tensor-core kernels evaluate it; mean squared error over the samples."""
-    from scipy.special import erf
     H, NF = 64, 16
     sl = {}
     o = 0
@@ -297,8 +308,7 @@ def _mlp_grad_ref(params, feat, target):
     W3 = _bf16(params[sl["W3"]]).astype(np.float64).reshape(H, H)
     W4 = _bf16(params[sl["W4"]]).astype(np.float64)
     b1, b2, b3, b4 = (params[sl[k]].astype(np.float64) for k in ("b1", "b2", "b3", "b4"))
-    g = lambda z: 0.5 * z * (1 + erf(z / np.sqrt(2)))
-    gd = lambda z: 0.5 * (1 + erf(z / np.sqrt(2))) + z * np.exp(-0.5 * z * z) / np.sqrt(2 * np.pi)
+    g, gd = _gelu, _gelud
     x = _bf16(feat).astype(np.float64)
     z1 = x @ W1.T + b1; h1 = _bf16(g(z1)).astype(np.float64)
     z2 = h1 @ W2.T + b2; h2 = _bf16(g(z2)).astype(np.float64)

@@ -36,7 +36,7 @@ HBM_FALLBACK = 6800.0
 def args_():
     a = argparse.ArgumentParser()
     a.add_argument("--gpus", type=int, default=1)
-    a.add_argument("--steps", type=int, default=20)
+    a.add_argument("--steps", type=int, default=100)
     a.add_argument("--warmup", type=int, default=5)
     a.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     a.add_argument("--solver", default="mixed", choices=["mixed", "plain", "matfree", "compact"])
@@ -89,7 +89,7 @@ class Clocks:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()

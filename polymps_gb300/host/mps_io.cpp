@@ -264,7 +264,11 @@ int readInputFile(const std::string& jsonPath, CaseInput& c, std::string& err) {
         std::string s = text(g, "solver", "plain");
         c.gpu.solver = (s == "mixed") ? MPSGPU_SOLVER_MIXED : MPSGPU_SOLVER_PLAIN_FP64;
         std::string w = text(g, "warm_start", "previous");
-        c.gpu.warmStart = (w == "mlp") ? MPSGPU_WARM_MLP : (w == "zero") ? MPSGPU_WARM_ZERO : MPSGPU_WARM_PREVIOUS;
+        c.gpu.warmStart = (w == "mlp")            ? MPSGPU_WARM_MLP
+                          : (w == "zero")         ? MPSGPU_WARM_ZERO
+                          : (w == "extrapolate")  ? MPSGPU_WARM_EXTRAPOLATE
+                          : (w == "extrapolate2") ? MPSGPU_WARM_EXTRAPOLATE2
+                                                  : MPSGPU_WARM_PREVIOUS;
         c.gpu.tol = num(g, "tol", 1e-8);
         c.gpu.maxIter = (int)num(g, "max_iter", 0);
         c.gpu.mlpWeights = text(g, "mlp_weights", "");

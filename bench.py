@@ -53,7 +53,8 @@ def args_():
     a.add_argument("--no-cpu-baseline", action="store_true")
     a.add_argument("--cpu-steps", type=int, default=1)
     a.add_argument("--ppe-compare", type=int, default=1)
-    a.add_argument("--ppe-steps", type=int, default=40, help="steps sampled by the PPE comparison")
+    a.add_argument("--ppe-steps", type=int, default=0,
+                   help="steps the PPE comparison runs on (0: to the workload's configured length)")
     a.add_argument("--presort", action="store_true",
                    help="number the input particles in bucket order (input renumbering only)")
     return a.parse_args()
@@ -243,7 +244,10 @@ def run_gb300(a, rank, world, local):
     # starts (before the end-to-end section, which re-uploads the state)
     ppe = None
     if a.ppe_compare and rank == 0:
-        ppe = ppe_compare(g, abi, have_mlp, g.params, (solver, warm, 1e-8, 20000), steps=a.ppe_steps)
+        done = a.warmup + a.steps   # steps taken so far (initialisation is step 0)
+        steps = a.ppe_steps if a.ppe_steps > 0 else max(getattr(case, "steps", 1000) - done, 40)
+        ppe = ppe_compare(g, abi, have_mlp, g.params, (solver, warm, 1e-8, 20000), steps=steps,
+                          every=max(1, steps // 36), start=done)
     # e2e through the C ABI with host arrays: upload the state from pinned host memory,
     # step, download the result, every step
     h2d = sum(v.nbytes for v in host.values())
@@ -328,7 +332,7 @@ def _solve(g, abi, hist, solver, warm, mode=1):
             "relres": st.ppeRelResidual, "relres0": st.ppeInitialRelResidual}
 
 
-def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4):
+def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4, start=0):
     """PPE time-to-1e-8 of the solvers and warm starts on the same systems, sampled along
     `steps` further steps of the run (every `every`-th system): each sampled system is
     solved by every variant from the same warm-start state, then the step is finished
@@ -357,6 +361,7 @@ def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4):
            ("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 0),
            ("quadratic_fp32_fp64_per_kernel_launch", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 0)]
     samples = {k: [] for k, _, _ in main}
+    trace = []
     alt_res = {}
     err = {k: 0.0 for k, _, _ in main}
     first = None
@@ -368,14 +373,17 @@ def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4):
             if first is None:
                 first = s
             p_ref = None
+            row = {"step": start + s}
             for name, solver, warm in main:
                 r = _solve(g, abi, hist, solver, warm)
                 samples[name].append(r)
+                row[name] = round(r["ms"], 3)
                 p = g.get(abi.F_PRESSPPE)
                 if p_ref is None:
                     p_ref = p
                 else:
                     err[name] = max(err[name], float(np.linalg.norm(p - p_ref) / np.linalg.norm(p_ref)))
+            trace.append(row)
             if s == first:
                 for name, solver, warm, mode in alt:
                     best = min((_solve(g, abi, hist, solver, warm, mode) for _ in range(3)), key=lambda r: r["ms"])
@@ -403,7 +411,15 @@ def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4):
         v["speedup_vs_plain"] = round(samples["plain_fp64"][0]["ms"] / v["ms"], 3) if v["ms"] > 0 else None
     res["options_first_system"] = alt_res
     res["systems"] = len(samples["plain_fp64"])
-    res["steps_sampled"] = "every %d-th of %d steps after the timed run" % (every, steps)
+    res["steps_sampled"] = "every %d-th step of steps %d-%d of the run" % (every, start, start + steps - 1)
+    # the flow's phases differ: early systems are smooth in time (extrapolated starts gain
+    # most), later ones carry particle-scale pressure noise
+    half = len(trace) // 2
+    for tag, part in (("first_half", trace[:half]), ("second_half", trace[half:])):
+        if part:
+            res[tag] = {k: round(float(np.mean([r[k] for r in part])), 3) for k in part[0] if k != "step"}
+            res[tag]["steps"] = "%d-%d" % (part[0]["step"], part[-1]["step"])
+    res["trace_ms"] = trace
     res["assemble_ms"] = round(g.last_stats().ppeAssembleMs, 3)
     return res
 

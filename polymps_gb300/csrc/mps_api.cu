@@ -39,6 +39,8 @@ struct mpsgpu_s {
     bool masksValid = false;
     bool skinValid = false;    // the nbr rows hold the start-of-step skin list of this bucket list
     int skinOn = 1;            // DF32 tier: viscosity and the post-prediction list from the skin list
+    bool corrFresh = false;    // the correction matrix of the current positions and masks is written
+    bool opSkipped = false;    // the last operator had nothing left to launch
     bool cacheValid = false;   // per-entry FP64 weights of the current list
     int persistent = 1;        // PPE launch: 0 per kernel, 1 single cooperative launch, 2 + staged ELL tiles
     double timeCurrent = 0.0;
@@ -302,14 +304,17 @@ static int runOpImpl(mpsgpu_t h, int op) {
     if (pr) h->prof.begin(op, h->s);
     int e = runOpBody(h, op);
     if (pr) h->prof.end(h->s);
-    countLaunch(opLaunches(op, h->d.P, h->d.prec == MPSGPU_PRECISION_DF32));
+    if (!h->opSkipped) countLaunch(opLaunches(op, h->d.P, h->d.prec == MPSGPU_PRECISION_DF32));
+    h->opSkipped = false;
     return e;
 }
 static int runOpBody(mpsgpu_t h, int op) {
     Dev& d = h->d;
     const MpsParams& P = d.P;
     cudaStream_t s = h->s;
-    auto invalidate = [&]() { h->listValid = false; h->masksValid = false; h->cacheValid = false; };
+    auto invalidate = [&]() {
+        h->listValid = false; h->masksValid = false; h->cacheValid = false; h->corrFresh = false;
+    };
     const bool x = df32(h);
     switch (op) {
         case MPS_OP_UPDATE_BUCKETS: {
@@ -339,13 +344,28 @@ static int runOpBody(mpsgpu_t h, int op) {
         case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
         case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); invalidate(); break;
         case MPS_OP_COLLISION: ensureList(h); if (x) launchCollisionDF(d, s); else launchCollision(d, s); break;
-        case MPS_OP_WALL_DISTANCE: launchWallDistance(d, s); h->masksValid = false; break;
+        case MPS_OP_WALL_DISTANCE: launchWallDistance(d, s); h->masksValid = false; h->corrFresh = false; break;
         case MPS_OP_WALL_NPCD: ensureMasks(h); if (x) launchWallNpcdDF(d, s); else launchWallNpcd(d, s); break;
         case MPS_OP_CORRECTION_MATRIX:
             ensureMasks(h);
+            if (x && h->corrFresh && h->masksValid) {   // formed by the PND sweep: publish it
+                std::swap(d.c1, d.c1n); std::swap(d.c2, d.c2n); std::swap(d.c3, d.c3n);
+                std::swap(d.corrDF, d.corrDFn);
+                h->corrFresh = false;
+                h->opSkipped = true;
+                break;
+            }
             if (x) launchCorrectionMatrixDF(d, s); else launchCorrectionMatrix(d, s);
             break;
-        case MPS_OP_PND_NEIGH_NPCD: ensureMasks(h); if (x) launchPndNeighNpcdDF(d, s); else launchPndNeighNpcd(d, s); break;
+        case MPS_OP_PND_NEIGH_NPCD: {
+            ensureMasks(h);
+            // the correction matrix of the step (read after the pressure solve, positions and
+            // masks unchanged in between) is formed in the same pass
+            bool corr = x && P.gradientCorrection && P.pndType != 2;
+            if (x) launchPndNeighNpcdDF(d, s, corr); else launchPndNeighNpcd(d, s);
+            h->corrFresh = corr;
+            break;
+        }
         case MPS_OP_PND_DIFFUSIVE: ensureMasks(h); ensureCache(h); launchPndDiffusive(d, s); break;
         case MPS_OP_PND_MEAN: ensureMasks(h); ensureCache(h); launchPndMean(d, s); break;
         case MPS_OP_UPDATE_BC: launchUpdateBC(d, s); break;
@@ -533,6 +553,13 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     std::memset(&d, 0, sizeof(d));
     d.P = *p;
     d.N0 = n;
+    d.invSidef = (float)p->invBucketSide;
+    d.epsf = (float)p->epsilonZero;
+    d.dz3 = (int)(p->dim - 2.0);
+    for (int k = 0; k < 3; k++) {
+        d.oodLo[k] = p->domainMin[k] + p->bucketSide;
+        d.oodHi[k] = p->domainMax[k] - p->bucketSide;
+    }
     d.nB = p->numBucketsXYZ;
     d.K = ((int)p->dim == 3) ? 64 : 32;
     int e = 0;
@@ -573,6 +600,10 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.skinCell, n);
     A(d.skinFlag, 2);
     A(d.corrDF, (size_t)9 * n);
+    A(d.corrDFn, (size_t)9 * n);
+    A(d.c1n, n);
+    A(d.c2n, n);
+    A(d.c3n, n);
     A(d.nbrCount, n);
     A(d.nbr, (size_t)d.K * n);
     A(d.cw, (size_t)d.K * n);
@@ -587,6 +618,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.counters, 4);
     A(h->scanScratch, scanScratchInts(std::max(d.nB + 1, n)));
     A(h->outFlags, n);
+    cudaMemsetAsync(h->outFlags, 0, sizeof(int) * n, h->s);
     A(h->outCounter, 1);
     // FP32 prefilter band (see k_build_nbr): |d2f - d2| <= 3.47 delta re + 3 delta^2 + 3.1 u re^2
     {
@@ -807,6 +839,7 @@ int mpsgpu_set_precision(mpsgpu_t h, int precision) {
         h->d.prec = precision;
         h->listValid = false;
         h->skinValid = false;
+        h->corrFresh = false;
         h->masksValid = false;
         h->cacheValid = false;
     }
@@ -936,6 +969,7 @@ int mpsgpu_set_field(mpsgpu_t h, int f, const void* host) {
     // any state change can alter list membership, masks or the near-wall set
     h->listValid = false;
     h->skinValid = false;
+    h->corrFresh = false;
     h->masksValid = false;
     h->cacheValid = false;
     if (f == MPS_F_POS) launchPosf(h->d, h->s);

@@ -67,6 +67,8 @@ struct Dev {
     // squared distances for the reS, reL, list and collision radii
     int prec;                       // MPSGPU_PRECISION_*
     float4 *posLo, *posLoCell, *velHi, *velLo;
+    dvec4 *c1n, *c2n, *c3n;         // correction matrix formed by the PND sweep, published by the
+    float2* corrDFn;                // correction-matrix operator (pointer swap)
     float2* pressDF;
     float2* concDF;                 // shifting concentration as a float-float pair
     // start-of-step neighbour list with a skin (DF32 tier): candidates within reL + skin of
@@ -78,6 +80,10 @@ struct Dev {
     int* skinFlag;                  // [0] set: the skin list no longer covers the list
     float skinR2;                   // FP32 squared radius of the skin list (with the band)
     float skinMove2;                // FP32 squared displacement bound (half the skin, less the band)
+    float invSidef, epsf;           // FP32 copies of invBucketSide and epsilonZero (bucket fast path)
+    int dz3;                        // (int)(dim - 2): 1 in 3D (27 buckets), 0 in 2D (9)
+    // out-of-domain bounds [min + bucket, max - bucket] (FP64, formed once as the reference does)
+    double oodLo[3], oodHi[3];
     float mgS, mgL, mgMax, mgColl, mgSide;
     // float-float (hi, lo) constants of the DF32 sweeps, converted once on the host
     struct DfK {
@@ -141,6 +147,23 @@ __device__ __forceinline__ void bucketCoords(const MpsParams& P, double x, doubl
     bx = (int)xadd(xmul(xsub(x, P.domainMin[0]), P.invBucketSide), P.epsilonZero);
     by = (int)xadd(xmul(xsub(y, P.domainMin[1]), P.invBucketSide), P.epsilonZero);
     bz = (int)xadd(xmul(xsub(z, P.domainMin[2]), P.invBucketSide), P.epsilonZero);
+}
+
+// The same coordinates from hi = fl32(x - min) (the particle's current FP32 copy): the FP32
+// quotient is within 4 * 2^-24 relative of the FP64 one, so its truncation is exact unless
+// it lies within a margin of an integer (or below it), where the FP64 expression decides.
+__device__ __forceinline__ int bucketCoord1(float h, double x, double mn, const MpsParams& P, float inv, float eps) {
+    const float q = fmaf(h, inv, eps);
+    const float m = 5e-7f * fabsf(q) + 1e-6f;
+    const float f = q - floorf(q);
+    if (q > m && f > m && f < 1.0f - m) return (int)q;
+    return (int)xadd(xmul(xsub(x, mn), P.invBucketSide), P.epsilonZero);
+}
+__device__ __forceinline__ void bucketCoordsHi(const Dev& d, dvec4 p, float4 hi, int& bx, int& by, int& bz) {
+    const MpsParams& P = d.P;
+    bx = bucketCoord1(hi.x, p.x, P.domainMin[0], P, d.invSidef, d.epsf);
+    by = bucketCoord1(hi.y, p.y, P.domainMin[1], P, d.invSidef, d.epsf);
+    bz = bucketCoord1(hi.z, p.z, P.domainMin[2], P, d.invSidef, d.epsf);
 }
 
 // ------------------------------------------------------------------ weights

@@ -204,13 +204,14 @@ __device__ __forceinline__ int scanParticle(const Dev& d) {
 
 // 27-bucket scan (reference order) over the stale bucket list with the FP32 prefilter on
 // the hi parts; f(j, s, hj) receives every candidate with FP32 squared distance <= hi
-// (s = its slot in bucket order, so posLoCell[s] is its lo part).
+// (s = its slot in bucket order, so posLoCell[s] is its lo part).  fi is the particle's
+// current FP32 copy (the window comes from it, exactly, with the FP64 fallback).
 template <class F>
 __device__ __forceinline__ void forCellsDF(const Dev& d, dvec4 pi, float4 fi, float hi, F&& f) {
     const MpsParams& P = d.P;
     int ix, iy, iz;
-    bucketCoords(P, pi.x, pi.y, pi.z, ix, iy, iz);
-    int dz = (int)(P.dim - 2.0);
+    bucketCoordsHi(d, pi, fi, ix, iy, iz);
+    int dz = d.dz3;
     int minZ = (iz - 1) * dz, maxZ = (iz + 1) * dz;
 #pragma unroll 1
     for (int jz = minZ; jz <= maxZ; jz++)

@@ -73,7 +73,8 @@ void launchCollisionDF(const Dev& d, cudaStream_t s);
 void launchWallNpcdDF(const Dev& d, cudaStream_t s);
 void launchCorrectionMatrixDF(const Dev& d, cudaStream_t s);
 void launchCorrDF(const Dev& d, cudaStream_t s);
-void launchPndNeighNpcdDF(const Dev& d, cudaStream_t s);
+// withCorrection: also the correction matrix of the same positions and masks
+void launchPndNeighNpcdDF(const Dev& d, cudaStream_t s, bool withCorrection = false);
 void launchPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallViscosityDF(const Dev& d, cudaStream_t s);

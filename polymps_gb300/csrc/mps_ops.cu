@@ -87,18 +87,19 @@ void launchPredict(const Dev& d, cudaStream_t s) { k_predict<<<gridFor(d.N0, 256
 // slot trades places with the last live slot (all arrays, the index maps and the two
 // entries of the step's bucket list, so the list keeps pointing at the same data).
 __device__ __forceinline__ bool outside(const Dev& d, dvec4 p) {
-    const MpsParams& P = d.P;
-    double b = P.bucketSide;
-    return p.x > P.domainMax[0] - b || p.x < P.domainMin[0] + b || p.y > P.domainMax[1] - b ||
-           p.y < P.domainMin[1] + b || (P.dim == 3 && (p.z > P.domainMax[2] - b || p.z < P.domainMin[2] + b));
+    return p.x > d.oodHi[0] || p.x < d.oodLo[0] || p.y > d.oodHi[1] || p.y < d.oodLo[1] ||
+           (d.dz3 && (p.z > d.oodHi[2] || p.z < d.oodLo[2]));
 }
+// flags (by reference index) are zero between calls: only flagged particles write theirs,
+// and the serial pass clears what it read
 __global__ void k_out_flag(Dev d, int* flags, int* counter) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     int n = liveN(d);
     if (s >= n) return;
-    int f = (d.type[s] == d.P.fluid && outside(d, d.pos[s])) ? 1 : 0;
-    flags[d.orig[s]] = f;
-    if (f) atomicAdd(counter, 1);
+    if (d.type[s] == d.P.fluid && outside(d, d.pos[s])) {
+        flags[d.orig[s]] = 1;
+        atomicAdd(counter, 1);
+    }
 }
 template <class T> __device__ __forceinline__ void mv(T* a, int i, int L) { a[i] = a[L]; }
 template <class T> __device__ __forceinline__ void sw(T* a, int i, int j) { T t = a[i]; a[i] = a[j]; a[j] = t; }
@@ -121,11 +122,12 @@ __device__ void swapSlots(const Dev& d, int a, int b) {
     if (pb >= 0) d.cellSorted[pb] = a;
     d.cellPos[a] = pb; d.cellPos[b] = pa;
 }
-__global__ void k_out_serial(Dev d, const int* flags, int* counter) {
+__global__ void k_out_serial(Dev d, int* flags, int* counter) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     if (*counter == 0) return;
     const MpsParams& P = d.P;
-    int newN = *d.nLive;
+    const int oldN = *d.nLive;
+    int newN = oldN;
     int removed = 0;
     for (int r = 0; r < newN; r++) {
         if (!flags[r]) continue;
@@ -153,6 +155,7 @@ __global__ void k_out_serial(Dev d, const int* flags, int* counter) {
     *d.nLive = newN;
     *counter = removed;
     if (removed) d.skinFlag[0] = 1;   // indices moved: the start-of-step list is stale
+    for (int r = 0; r < oldN; r++) flags[r] = 0;
 }
 void launchOutOfDomain(const Dev& d, int* flags, int* counter, cudaStream_t s) {
     cudaMemsetAsync(counter, 0, sizeof(int), s);

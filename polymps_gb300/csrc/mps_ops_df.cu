@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(VBLK) k_visc_df(Dev d) {
     const float band = d.bandHiL;
     df ax = dfF(0.f), ay = dfF(0.f), az = dfF(0.f);
     int ix, iy, iz;
-    bucketCoords(P, pi.x, pi.y, pi.z, ix, iy, iz);
+    bucketCoordsHi(d, pi, hi, ix, iy, iz);
     const int dz = (int)(P.dim - 2.0);
     const int nbk = dz ? 27 : 9;
     int bk = 0, s = 0, s1 = 0;
@@ -315,6 +315,8 @@ __device__ __forceinline__ df recipDF(df a) {
     float e = fS(fS(1.0f, t.h), t.l);          // 1 - a y
     return quick2(y, fM(y, e));
 }
+__device__ __forceinline__ void corrFinish(const Dev& d, int i, int numNeigh, df m00, df m01, df m02, df m11,
+                                           df m12, df m22, dvec4* c1, dvec4* c2, dvec4* c3, float2* cdf);
 __global__ void __launch_bounds__(BLK) k_corr_matrix_df(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
@@ -329,6 +331,13 @@ __global__ void __launch_bounds__(BLK) k_corr_matrix_df(Dev d) {
         m00 += t0 * q.v.x; m01 += t0 * q.v.y; m02 += t0 * q.v.z;
         m11 += t1 * q.v.y; m12 += t1 * q.v.z; m22 += t2 * q.v.z;
     });
+    corrFinish(d, i, d.numNeigh[i], m00, m01, m02, m11, m12, m22, d.c1, d.c2, d.c3, d.corrDF);
+}
+// inverse of -coeffPressGrad * the moment matrix (identity when det <= eps or fewer than
+// four neighbours), written as the FP64 rows and the float-float copy
+__device__ __forceinline__ void corrFinish(const Dev& d, int i, int numNeigh, df m00, df m01, df m02, df m11,
+                                           df m12, df m22, dvec4* c1, dvec4* c2, dvec4* c3, float2* cdf) {
+    const MpsParams& P = d.P;
     const df c = K(d.k.negCPG);
     df A[9];
     A[0] = m00 * c; A[1] = m01 * c; A[2] = m02 * c;
@@ -338,7 +347,7 @@ __global__ void __launch_bounds__(BLK) k_corr_matrix_df(Dev d) {
     df det = (A[0] * A[4] * A[8] + A[1] * A[5] * A[6] + A[2] * A[3] * A[7]) -
              (A[2] * A[4] * A[6] + A[1] * A[3] * A[8] + A[0] * A[5] * A[7]);
     df M[9];
-    bool ident = d.numNeigh[i] < 4 || !(det.h > (float)P.epsilonZero);
+    bool ident = numNeigh < 4 || !(det.h > (float)P.epsilonZero);
     if (ident) {
 #pragma unroll
         for (int k = 0; k < 9; k++) M[k] = dfF((k % 4 == 0) ? 1.f : 0.f);
@@ -351,10 +360,10 @@ __global__ void __launch_bounds__(BLK) k_corr_matrix_df(Dev d) {
         M[8] = (A[0] * A[4] - A[1] * A[3]) * r;
     }
 #pragma unroll
-    for (int k = 0; k < 9; k++) d.corrDF[(size_t)k * d.N0 + i] = make_float2(M[k].h, M[k].l);
-    d.c1[i] = make_dvec4(dD(M[0]), dD(M[1]), dD(M[2]), 0.0);
-    d.c2[i] = make_dvec4(dD(M[3]), dD(M[4]), dD(M[5]), 0.0);
-    d.c3[i] = make_dvec4(dD(M[6]), dD(M[7]), dD(M[8]), 0.0);
+    for (int k = 0; k < 9; k++) cdf[(size_t)k * d.N0 + i] = make_float2(M[k].h, M[k].l);
+    c1[i] = make_dvec4(dD(M[0]), dD(M[1]), dD(M[2]), 0.0);
+    c2[i] = make_dvec4(dD(M[3]), dD(M[4]), dD(M[5]), 0.0);
+    c3[i] = make_dvec4(dD(M[6]), dD(M[7]), dD(M[8]), 0.0);
 }
 // float-float copy of matrices written through the field interface
 __global__ void k_df_corr(Dev d) {
@@ -374,6 +383,10 @@ void launchCorrectionMatrixDF(const Dev& d, cudaStream_t s) { k_corr_matrix_df<<
 
 // ------------------------------------------------------------------ PND / NPCD
 // MpsPndNeigh::calcPndnNeighNPCD, src/MpsPndNeigh.cpp:199-331
+// CORR: the correction matrix's moment sums over the reS entries in the same pass (one
+// pair evaluation serves both; the PND sums take the entries also inside reL, in the same
+// ascending order as the plain sweep, so both results equal the separate kernels').
+template <bool CORR>
 __global__ void __launch_bounds__(BLK) k_pnd_npcd_df(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
@@ -383,12 +396,32 @@ __global__ void __launch_bounds__(BLK) k_pnd_npcd_df(Dev d) {
     unsigned long long mL = d.maskL[i];
     int nn = d.nNeighWall[i] + __popcll(mL);
     df ni = dfF(0.f), nx = ni, ny = ni, nz = ni;
-    forMask(d, i, mL & d.maskS[i], [&](int j, size_t) {
-        PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
-        df wS = weightDF(q.d2, RS, P.weightType).w;
-        ni += wS;
-        nx += q.v.x * wS; ny += q.v.y * wS; nz += q.v.z * wS;
-    });
+    df m00 = dfF(0.f), m01 = m00, m02 = m00, m11 = m00, m12 = m00, m22 = m00;
+    if (CORR) {
+        unsigned long long m = d.maskS[i];
+        const int* row = d.nbr + i;
+        while (m) {
+            const int k = __ffsll((long long)m) - 1;
+            m &= m - 1;
+            const int j = ldStream(row + (size_t)k * d.N0);
+            PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
+            WeightDF w = weightDF(q.d2, RS, P.weightType);
+            df t0 = q.v.x * w.wr2, t1 = q.v.y * w.wr2, t2 = q.v.z * w.wr2;
+            m00 += t0 * q.v.x; m01 += t0 * q.v.y; m02 += t0 * q.v.z;
+            m11 += t1 * q.v.y; m12 += t1 * q.v.z; m22 += t2 * q.v.z;
+            if ((mL >> k) & 1ull) {
+                ni += w.w;
+                nx += q.v.x * w.w; ny += q.v.y * w.w; nz += q.v.z * w.w;
+            }
+        }
+    } else {
+        forMask(d, i, mL & d.maskS[i], [&](int j, size_t) {
+            PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
+            df wS = weightDF(q.d2, RS, P.weightType).w;
+            ni += wS;
+            nx += q.v.x * wS; ny += q.v.y * wS; nz += q.v.z * wS;
+        });
+    }
     double nd = dD(ni);
     dvec4 np = d.npcd[i];
     np.x += dD(nx); np.y += dD(ny); np.z += dD(nz);
@@ -404,8 +437,14 @@ __global__ void __launch_bounds__(BLK) k_pnd_npcd_df(Dev d) {
     d.npcd2[i] = np.x * np.x + np.y * np.y + np.z * np.z;
     dvec4 nw = d.polyNormal[i];
     d.devDot[i] = (np.x * nw.x + np.y * nw.y + np.z * nw.z < 0.0) ? 1.0 : -1.0;
+    // into the staging arrays: the correction-matrix operator publishes them (the reference
+    // writes the matrix there, not in this sweep)
+    if (CORR) corrFinish(d, i, nn, m00, m01, m02, m11, m12, m22, d.c1n, d.c2n, d.c3n, d.corrDFn);
 }
-void launchPndNeighNpcdDF(const Dev& d, cudaStream_t s) { k_pnd_npcd_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
+void launchPndNeighNpcdDF(const Dev& d, cudaStream_t s, bool withCorrection) {
+    if (withCorrection) k_pnd_npcd_df<true><<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    else k_pnd_npcd_df<false><<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
 
 // ------------------------------------------------------------------ PPE assembly
 // MpsPressure::solvePressurePoissonPnd, src/MpsPressure.cpp:169-286 (matrix values are
@@ -834,9 +873,9 @@ void launchShiftingDF(const Dev& d, cudaStream_t s) {
 
 // ------------------------------------------------------------------ start-of-step list
 // Scan window key of a position: its three bucket coordinates (out-of-grid included).
-__device__ __forceinline__ long long cellKeyOf(const Dev& d, dvec4 p) {
+__device__ __forceinline__ long long cellKeyOf(const Dev& d, dvec4 p, float4 hi) {
     int ix, iy, iz;
-    bucketCoords(d.P, p.x, p.y, p.z, ix, iy, iz);
+    bucketCoordsHi(d, p, hi, ix, iy, iz);
     return ((long long)(iz & 0x1fffff) << 42) | ((long long)(iy & 0x1fffff) << 21) | (long long)(ix & 0x1fffff);
 }
 // Candidates of the 27-bucket scan within reMax + skin of the start positions (FP32 test
@@ -857,7 +896,7 @@ __global__ void __launch_bounds__(128) k_build_skin_df(Dev d) {
     });
     d.nbrCount[i] = cnt > d.K ? d.K + 1 : cnt;   // K + 1: the row overflowed, rescanned where read
     d.posSkin[i] = hi;
-    d.skinCell[i] = cellKeyOf(d, pi);
+    d.skinCell[i] = cellKeyOf(d, pi, hi);
 }
 void launchSkinListDF(const Dev& d, cudaStream_t s) {
     cudaMemsetAsync(d.skinFlag, 0, sizeof(int), s);
@@ -945,7 +984,7 @@ __global__ void __launch_bounds__(128) k_filter_nbr_df(Dev d) {
         cnt++;
     };
     const int c = d.nbrCount[i];
-    if (!*(volatile int*)d.skinFlag && c <= d.K && d.skinCell[i] == cellKeyOf(d, pi)) {
+    if (!*(volatile int*)d.skinFlag && c <= d.K && d.skinCell[i] == cellKeyOf(d, pi, hi)) {
         for (int k = 0; k < c; k++) {   // compacted in place: the write index never passes the read index
             const int j = d.nbr[(size_t)k * N0 + i];
             keep(j, d.posf[j], d.posLo[j]);

@@ -91,6 +91,27 @@ def test_df32_skin_list_bit_exact(oracle_mod, mps_lib, name, kick):
     assert np.array_equal(no, ng)
 
 
+def test_df32_fused_correction_matrix(oracle_mod, mps_lib):
+    """The correction matrix formed inside the PND sweep equals the separate kernel's, bit for
+    bit (same entries, same order, same float-float arithmetic)."""
+    from polymps_gb300 import mps
+    c = CASES["cfg3_3d_inc_polygon"]()
+    g = mps.MpsGpu(c, tol=1e-10, precision=abi.PRECISION_DF32)
+    g.initialize()
+    g.run(3)
+    ops = step_ops(g.params)
+    for op in ops[: ops.index("CORRECTION_MATRIX") + 1]:
+        g.run_op(op)   # no field set since the PND sweep: the fused matrix is kept
+    fused = [g.get(f) for f in (abi.F_CORR1, abi.F_CORR2, abi.F_CORR3)]
+    g.set(abi.F_PRESS, g.get(abi.F_PRESS))   # any field set: the operator recomputes
+    g.run_op("CORRECTION_MATRIX")
+    sep = [g.get(f) for f in (abi.F_CORR1, abi.F_CORR2, abi.F_CORR3)]
+    for a, b in zip(fused, sep):
+        assert np.array_equal(a, b)
+    assert np.abs(fused[0]).max() > 0
+    g.close()
+
+
 def test_df32_neighbor_sets_adversarial(oracle_mod, mps_lib):
     """Pairs at r^2 = reL^2 and within a few ulps of it: decided by the FP64 fallback."""
     from polymps_gb300 import mps

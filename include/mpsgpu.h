@@ -314,6 +314,19 @@ const char* mpsgpu_last_error(mpsgpu_t h);
 /* ABI check for bindings: sizeof(MpsParams), sizeof(MpsStepStats), sizeof(MpsMesh). */
 int mpsgpu_abi_sizes(int* params, int* stats, int* mesh);
 
+/* Binary .vtu output written from device buffers (replaces MpsInputOutput::writeVtuAscii,
+ * src/MpsInputOutput.cpp:1313-1580, and its non-working binary variant :921-1310): the same
+ * arrays, names and types as the ASCII writer (Float32 values, Int32 flags, UInt8 cell
+ * types), converted and reordered into the reference's particle order on the device and
+ * copied to the host as one block, written as raw appended data with UInt32 headers.
+ * groups: the optional arrays of the JSON's output_VTU section. */
+#define MPSGPU_VTU_PND            1u   /* pnd, pndSmall */
+#define MPSGPU_VTU_NEIGH          2u   /* nNeigh */
+#define MPSGPU_VTU_DEVIATION      4u   /* npcdDeviation, polygonNormal */
+#define MPSGPU_VTU_CONCENTRATION  8u   /* concentration, GradCi */
+#define MPSGPU_VTU_AUXILIAR      16u   /* ParticleType (+ nearMeshType with polygon walls) */
+int mpsgpu_write_vtu(mpsgpu_t h, const char* path, unsigned int groups);
+
 /* Device timing per operator with CUDA events on the handle's stream (the per-kernel
  * timer the reference lacks; it only prints wall time, src/MpsInputOutput.cpp:31-55).
  * Classes 0..MPS_OP_COUNT-1 are the MpsOp operators, followed by NEIGHBOR_LIST,

@@ -194,3 +194,6 @@ def make_mesh(tri):
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libmpsgpu.so")
+
+# optional array groups of mpsgpu_write_vtu
+VTU_PND, VTU_NEIGH, VTU_DEVIATION, VTU_CONCENTRATION, VTU_AUXILIAR = 1, 2, 4, 8, 16

@@ -107,12 +107,13 @@ class Case:
                 nrm = nrm / (np.linalg.norm(nrm) or 1.0)
                 f.write(struct.pack("<12fH", *nrm, *t[0], *t[1], *t[2], 0))
 
-    def write_json(self, path, grid_path, stl_path, out_dir):
-        """JSON input in the reference schema (radii in units of l0, as in the examples)."""
+    def write_json(self, path, grid_path, stl_path, out_dir, vtu_type=0):
+        """JSON input in the reference schema (radii in units of l0, as in the examples);
+        vtu_type 0 ASCII output, 1 binary."""
         p = self.params
         js = {
             "flags": {"wall_type": p["wallType"], "fem_MESH": False, "forced_MESH": False,
-                      "output_VTU": {"type": 0, "only_freeSurface": False, "pnd": True,
+                      "output_VTU": {"type": vtu_type, "only_freeSurface": False, "pnd": True,
                                      "neigh": True, "deviation": False, "concentration": False,
                                      "auxiliar": False, "non_newtonian": False}},
             "pathNames": {"particle_grid_file": grid_path, "mesh_rigid_file": stl_path,

@@ -41,6 +41,9 @@ struct mpsgpu_s {
     int skinOn = 1;            // DF32 tier: viscosity and the post-prediction list from the skin list
     bool corrFresh = false;    // the correction matrix of the current positions and masks is written
     bool opSkipped = false;    // the last operator had nothing left to launch
+    void* vtuDev = nullptr;    // staging of the binary .vtu block (device, page-locked host)
+    void* vtuHost = nullptr;
+    size_t vtuCap = 0;
     bool cacheValid = false;   // per-entry FP64 weights of the current list
     int persistent = 1;        // PPE launch: 0 per kernel, 1 single cooperative launch, 2 + staged ELL tiles
     double timeCurrent = 0.0;
@@ -481,6 +484,28 @@ static void fromRef(mpsgpu_t h, int kind, void* p, int n) {
     countLaunch(1);
 }
 
+// ------------------------------------------------------------------ binary .vtu output
+// Arrays of the appended block in the reference's particle order (slotOf maps a reference
+// index to its storage slot), converted as the ASCII writer converts them ((float) casts).
+__global__ void k_vtu_vec(const dvec4* src, const int* slotOf, int n, float* dst) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    dvec4 v = src[slotOf[r]];
+    dst[3 * r] = (float)v.x; dst[3 * r + 1] = (float)v.y; dst[3 * r + 2] = (float)v.z;
+}
+__global__ void k_vtu_sca(const double* src, const int* slotOf, int n, float* dst) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) dst[r] = (float)src[slotOf[r]];
+}
+__global__ void k_vtu_int(const int* src, const int* slotOf, int n, int* dst, int add) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) dst[r] = src ? src[slotOf[r]] : r + add;   // src == NULL: r + add (connectivity, offsets)
+}
+__global__ void k_vtu_u8(int n, unsigned char* dst, unsigned char v) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < n) dst[r] = v;
+}
+
 extern "C" {
 
 int mpsgpu_params_derive(MpsParams* p, int n, const double* pos3) {
@@ -771,6 +796,8 @@ int mpsgpu_destroy(mpsgpu_t h) {
     mlpFree(h->mlp);
     h->prof.destroy();
     for (void* p : h->allocs) cudaFree(p);
+    if (h->vtuDev) cudaFree(h->vtuDev);
+    if (h->vtuHost) cudaFreeHost(h->vtuHost);
     for (cudaEvent_t ev : {h->e0, h->e1, h->ea0, h->ea1, h->es0, h->es1}) if (ev) cudaEventDestroy(ev);
     if (h->s) cudaStreamDestroy(h->s);
     delete h;
@@ -945,6 +972,100 @@ int mpsgpu_get_field(mpsgpu_t h, int f, void* host) {
     size_t bytes = (kind == 0) ? 3 * sizeof(double) * n : ((kind == 1) ? sizeof(double) : sizeof(int)) * n;
     CK(cudaMemcpyAsync(host, h->permScratch, bytes, cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
+    return 0;
+}
+
+int mpsgpu_write_vtu(mpsgpu_t h, const char* path, unsigned int groups) {
+    if (!h || !path) return MPSGPU_ERR_ARG;
+    int n = 0;
+    int e = mpsgpu_num_particles(h, &n);
+    if (e) return e;
+    Dev& d = h->d;
+    // the arrays of writeVtuAscii, in its order: 0 FP64 vector, 1 FP64 scalar, 2 int,
+    // 3 generated int (r + add), 4 UInt8 constant, 5 Int32 zeros
+    struct Arr { const char* name; int kind; const void* src; int add; };
+    std::vector<Arr> pts = {{"Position", 0, d.pos, 0}};
+    std::vector<Arr> pd = {{"Velocity", 0, d.vel, 0}, {"pressure", 1, d.press, 0}, {"BC", 2, d.bc, 0}};
+    if (groups & MPSGPU_VTU_PND) { pd.push_back({"pnd", 1, d.pndi, 0}); pd.push_back({"pndSmall", 1, d.pndSmall, 0}); }
+    if (groups & MPSGPU_VTU_NEIGH) pd.push_back({"nNeigh", 2, d.numNeigh, 0});
+    if (groups & MPSGPU_VTU_DEVIATION) { pd.push_back({"npcdDeviation", 0, d.npcd, 0}); pd.push_back({"polygonNormal", 0, d.polyNormal, 0}); }
+    if (groups & MPSGPU_VTU_CONCENTRATION) { pd.push_back({"concentration", 1, d.conc, 0}); pd.push_back({"GradCi", 0, d.gradC, 0}); }
+    if (groups & MPSGPU_VTU_AUXILIAR) {
+        pd.push_back({"ParticleType", 2, d.type, 0});
+        if (d.P.wallType == 1) pd.push_back({"nearMeshType", 5, nullptr, 0});
+    }
+    std::vector<Arr> cells = {{"connectivity", 3, nullptr, 0}, {"offsets", 3, nullptr, 1}, {"types", 4, nullptr, 1}};
+    auto bytesOf = [&](const Arr& a) -> size_t { return a.kind == 0 ? 12ull * n : (a.kind == 4 ? (size_t)n : 4ull * n); };
+    size_t total = 0;
+    for (auto* g : {&pts, &pd, &cells})
+        for (auto& a : *g) total += 4 + bytesOf(a);
+    if (total > h->vtuCap) {
+        if (h->vtuDev) cudaFree(h->vtuDev);
+        if (h->vtuHost) cudaFreeHost(h->vtuHost);
+        h->vtuDev = h->vtuHost = nullptr;
+        h->vtuCap = 0;
+        CK(cudaMalloc(&h->vtuDev, total));
+        CK(cudaMallocHost(&h->vtuHost, total));
+        h->vtuCap = total;
+    }
+    // pack: each array is a UInt32 byte count followed by its data (4-byte aligned: the one
+    // UInt8 array is the last)
+    char* base = (char*)h->vtuDev;
+    size_t off = 0;
+    std::vector<size_t> offs;
+    std::vector<unsigned int> heads;
+    for (auto* g : {&pts, &pd, &cells})
+        for (auto& a : *g) {
+            offs.push_back(off);
+            heads.push_back((unsigned int)bytesOf(a));
+            char* dst = base + off + 4;
+            int gr = gridFor(n, 256);
+            if (n > 0) {
+                if (a.kind == 0) k_vtu_vec<<<gr, 256, 0, h->s>>>((const dvec4*)a.src, d.slotOf, n, (float*)dst);
+                else if (a.kind == 1) k_vtu_sca<<<gr, 256, 0, h->s>>>((const double*)a.src, d.slotOf, n, (float*)dst);
+                else if (a.kind == 2) k_vtu_int<<<gr, 256, 0, h->s>>>((const int*)a.src, d.slotOf, n, (int*)dst, 0);
+                else if (a.kind == 3) k_vtu_int<<<gr, 256, 0, h->s>>>(nullptr, d.slotOf, n, (int*)dst, a.add);
+                else if (a.kind == 4) k_vtu_u8<<<gr, 256, 0, h->s>>>(n, (unsigned char*)dst, (unsigned char)a.add);
+                else CK(cudaMemsetAsync(dst, 0, 4ull * n, h->s));
+                countLaunch(a.kind == 5 ? 0 : 1);
+            }
+            off += 4 + bytesOf(a);
+        }
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->vtuHost, h->vtuDev, total, cudaMemcpyDeviceToHost, h->s));
+    CK(cudaStreamSynchronize(h->s));
+    char* hb = (char*)h->vtuHost;
+    for (size_t k = 0; k < offs.size(); k++) std::memcpy(hb + offs[k], &heads[k], 4);
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) { g_lastError = std::string("cannot open ") + path; return MPSGPU_ERR_ARG; }
+    size_t k = 0;
+    auto arr = [&](const Arr& a, const char* indent) {
+        const char* ty = a.kind == 4 ? "UInt8" : (a.kind >= 2 ? "Int32" : "Float32");
+        if (a.kind == 0)
+            std::fprintf(fp, "%s<DataArray type='%s' Name='%s' NumberOfComponents='3' format='appended' offset='%zu'/>\n",
+                         indent, ty, a.name, offs[k]);
+        else
+            std::fprintf(fp, "%s<DataArray type='%s' Name='%s' format='appended' offset='%zu'/>\n", indent, ty, a.name,
+                         offs[k]);
+        k++;
+    };
+    std::fprintf(fp, "<?xml version='1.0' encoding='UTF-8'?>\n");
+    std::fprintf(fp, "<VTKFile xmlns='VTK' byte_order='LittleEndian' version='0.1' type='UnstructuredGrid' "
+                     "header_type='UInt32'>\n");
+    std::fprintf(fp, "  <UnstructuredGrid>\n");
+    std::fprintf(fp, "    <Piece NumberOfCells='%d' NumberOfPoints='%d'>\n", n, n);
+    std::fprintf(fp, "      <Points>\n");
+    for (auto& a : pts) arr(a, "        ");
+    std::fprintf(fp, "      </Points>\n      <PointData>\n");
+    for (auto& a : pd) arr(a, "        ");
+    std::fprintf(fp, "      </PointData>\n      <Cells>\n");
+    for (auto& a : cells) arr(a, "        ");
+    std::fprintf(fp, "      </Cells>\n    </Piece>\n  </UnstructuredGrid>\n");
+    std::fprintf(fp, "  <AppendedData encoding='raw'>\n_");
+    size_t wr = std::fwrite(hb, 1, total, fp);
+    std::fprintf(fp, "\n  </AppendedData>\n</VTKFile>\n");
+    std::fclose(fp);
+    if (wr != total) { g_lastError = std::string("short write to ") + path; return MPSGPU_ERR_ARG; }
     return 0;
 }
 

@@ -86,7 +86,17 @@ int main(int argc, char** argv) {
             if (P.mpsType == 2) std::printf(" Solver iterations: %3d Estimated error: %.2e", st.ppeIterations, st.ppeRelResidual);
             std::printf(" RunTime: %02dh%02dm%02dsec\n", sec / 3600, (sec / 60) % 60, sec % 60);
         }
-        if (output && iter % P.iterOutput == 0) {
+        if (output && iter % P.iterOutput == 0 && c.out.vtuType == 1) {
+            // binary: formatted from the device buffers by the library
+            char name[1024];
+            std::snprintf(name, sizeof(name), "%s/output%05d.vtu", c.vtuFolder.c_str(), fileNumber);
+            unsigned int groups = (c.out.pnd ? MPSGPU_VTU_PND : 0u) | (c.out.neigh ? MPSGPU_VTU_NEIGH : 0u) |
+                                  (c.out.deviation ? MPSGPU_VTU_DEVIATION : 0u) |
+                                  (c.out.concentration ? MPSGPU_VTU_CONCENTRATION : 0u) |
+                                  (c.out.auxiliar ? MPSGPU_VTU_AUXILIAR : 0u);
+            TRY(mpsgpu_write_vtu(h, name, groups));
+            fileNumber++;
+        } else if (output && iter % P.iterOutput == 0) {
             int cur = 0;
             TRY(mpsgpu_num_particles(h, &cur));
             v.n = cur;

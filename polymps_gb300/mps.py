@@ -23,7 +23,7 @@ EXPORTS = [
     "mpsgpu_mlp_num_records", "mpsgpu_mlp_fit_normalization", "mpsgpu_mlp_train", "mpsgpu_mlp_forward",
     "mpsgpu_mlp_gradient", "mpsgpu_stream", "mpsgpu_last_error", "mpsgpu_abi_sizes",
     "mpsgpu_profile", "mpsgpu_profile_get", "mpsgpu_profile_name", "mpsgpu_launch_count",
-    "mpsgpu_last_stats", "mpsgpu_pcg_solve_static", "mpsgpu_pcg_static_error",
+    "mpsgpu_last_stats", "mpsgpu_pcg_solve_static", "mpsgpu_pcg_static_error", "mpsgpu_write_vtu",
 ]
 PROF_NCLASS = len(abi.OPS) + 6
 
@@ -55,6 +55,7 @@ def lib(path=None):
     L.mpsgpu_set_solver.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int]
     L.mpsgpu_set_precision.argtypes = [vp, C.c_int]
     L.mpsgpu_set_ppe_launch.argtypes = [vp, C.c_int]
+    L.mpsgpu_write_vtu.argtypes = [vp, C.c_char_p, C.c_uint]
     L.mpsgpu_get_field.argtypes = [vp, C.c_int, vp]
     L.mpsgpu_set_field.argtypes = [vp, C.c_int, vp]
     L.mpsgpu_num_particles.argtypes = [vp, P(C.c_int)]
@@ -165,8 +166,13 @@ class MpsGpu:
 
     def set_ppe_launch(self, mode=1):
         """PPE launch: 0 one launch per kernel, 1 (default) one cooperative launch per solve,
-        2 as 1 with the FP32 matrix streamed through shared memory by bulk copies."""
+        2 as 1 with the FP32 matrix streamed through shared memory by bulk copies, 3 as 1 with
+        the pipelined inner CG."""
         _check("mpsgpu_set_ppe_launch", lib().mpsgpu_set_ppe_launch(self.h, int(mode)), self.h)
+
+    def write_vtu(self, path, groups=0):
+        """Binary .vtu of the current state (abi.VTU_* optional array groups)."""
+        _check("mpsgpu_write_vtu", lib().mpsgpu_write_vtu(self.h, str(path).encode(), int(groups)), self.h)
 
     def set_solver(self, solver=abi.SOLVER_PLAIN_FP64, warm=abi.WARM_PREVIOUS, tol=1e-8, max_iter=0):
         _check("mpsgpu_set_solver", lib().mpsgpu_set_solver(self.h, solver, warm, tol, max_iter), self.h)

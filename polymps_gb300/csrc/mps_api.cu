@@ -566,7 +566,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     if (!p || !p->derived || n <= 0 || !type || !pos3 || !out) { g_lastError = "bad argument"; return MPSGPU_ERR_ARG; }
     if (unsupported(*p)) { g_lastError = "configuration outside the implemented path"; return MPSGPU_ERR_UNSUPPORTED; }
     if (p->wallType == 1 && (!mesh || mesh->ntri <= 0 || !mesh->tri_xyz)) { g_lastError = "polygon walls need a mesh"; return MPSGPU_ERR_ARG; }
-    if (mesh && mesh->ntri > MPS_MAX_TRI) { g_lastError = "mesh larger than the brute-force wall kernel supports"; return MPSGPU_ERR_UNSUPPORTED; }
+    if (mesh && mesh->ntri > (1 << 26)) { g_lastError = "mesh too large"; return MPSGPU_ERR_UNSUPPORTED; }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { g_lastError = "no CUDA device"; return MPSGPU_ERR_NOGPU; }
     mpsgpu_t h = new mpsgpu_s();
@@ -718,6 +718,24 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         cudaMemcpyAsync(dn, nrm.data(), sizeof(double) * nrm.size(), cudaMemcpyHostToDevice, h->s);
         cudaMemcpyAsync(dtab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, h->s);
         d.tri = dt; d.triNormal = dn; d.tab = dtab; d.ntri = mesh->ntri;
+        if (mesh->ntri > MPS_MAX_TRI) {
+            // large mesh: triangle BVH (host build, FP32 boxes) and FP32 triangle copies
+            std::vector<float> lo4, hi4, tf(9 * (size_t)mesh->ntri);
+            std::vector<int> order;
+            hostBuildBvh(mesh->ntri, mesh->tri_xyz, p->domainMin, lo4, hi4, order);
+            for (size_t k = 0; k < tf.size(); k++) tf[k] = (float)(mesh->tri_xyz[k] - p->domainMin[k % 3]);
+            float *blo = nullptr, *bhi = nullptr, *btf = nullptr;
+            int* bord = nullptr;
+            A(blo, lo4.size());
+            A(bhi, hi4.size());
+            A(bord, order.size());
+            A(btf, tf.size());
+            cudaMemcpyAsync(blo, lo4.data(), sizeof(float) * lo4.size(), cudaMemcpyHostToDevice, h->s);
+            cudaMemcpyAsync(bhi, hi4.data(), sizeof(float) * hi4.size(), cudaMemcpyHostToDevice, h->s);
+            cudaMemcpyAsync(bord, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, h->s);
+            cudaMemcpyAsync(btf, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice, h->s);
+            d.bvhLo = (const float4*)blo; d.bvhHi = (const float4*)bhi; d.bvhOrder = bord; d.triF = btf;
+        }
         cudaStreamSynchronize(h->s);
     }
     // PPE buffers

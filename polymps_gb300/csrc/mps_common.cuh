@@ -111,6 +111,11 @@ struct Dev {
     const double* tri;          // ntri * 9
     const double* triNormal;    // ntri * 3
     const double* tab;          // xPND[50], Z[50], xNeigh[50], nNeigh[50] (as double)
+    // meshes above MPS_MAX_TRI triangles: BVH nodes (FP32 boxes relative to domainMin, the
+    // .w words hold child indices or leaf ranges), leaf order, FP32 triangle copies
+    const float4 *bvhLo, *bvhHi;
+    const int* bvhOrder;
+    const float* triF;          // ntri * 9, relative to domainMin
     // prefilter band for the FP32 distance test (|d2f - reL2| <= band -> exact FP64)
     float reL2f, bandLo, bandHi;
     // scalars

@@ -197,3 +197,72 @@ void hostTriNormals(int ntri, const double* tri, double* nrm) {
         for (int k = 0; k < 3; k++) nrm[3 * t + k] = (l > 0) ? c[k] / l : 0.0;
     }
 }
+
+// ------------------------------------------------------------------ triangle BVH
+namespace {
+struct BvhBuild {
+    const double* tri;
+    const double* origin;
+    std::vector<float> cen;   // centroid (FP32, relative), 3 per triangle
+    std::vector<float>& lo4;
+    std::vector<float>& hi4;
+    std::vector<int>& order;
+    float vlo(int t, int k) const {   // smallest FP32 vertex coordinate, widened down
+        double m = std::min(tri[9 * t + k], std::min(tri[9 * t + 3 + k], tri[9 * t + 6 + k])) - origin[k];
+        return std::nextafter((float)m, -3.0e38f);
+    }
+    float vhi(int t, int k) const {
+        double m = std::max(tri[9 * t + k], std::max(tri[9 * t + 3 + k], tri[9 * t + 6 + k])) - origin[k];
+        return std::nextafter((float)m, 3.0e38f);
+    }
+    int build(int first, int count) {
+        int node = (int)(lo4.size() / 4);
+        lo4.resize(lo4.size() + 4);
+        hi4.resize(hi4.size() + 4);
+        float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        float clo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, chi[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+        for (int q = first; q < first + count; q++) {
+            int t = order[q];
+            for (int k = 0; k < 3; k++) {
+                lo[k] = std::min(lo[k], vlo(t, k));
+                hi[k] = std::max(hi[k], vhi(t, k));
+                clo[k] = std::min(clo[k], cen[3 * t + k]);
+                chi[k] = std::max(chi[k], cen[3 * t + k]);
+            }
+        }
+        for (int k = 0; k < 3; k++) { lo4[4 * node + k] = lo[k]; hi4[4 * node + k] = hi[k]; }
+        if (count <= 4) {
+            int leaf[2] = {-(first + 1), count};
+            std::memcpy(&lo4[4 * node + 3], &leaf[0], 4);
+            std::memcpy(&hi4[4 * node + 3], &leaf[1], 4);
+            return node;
+        }
+        int ax = 0;
+        for (int k = 1; k < 3; k++)
+            if (chi[k] - clo[k] > chi[ax] - clo[ax]) ax = k;
+        int half = count / 2;
+        std::nth_element(order.begin() + first, order.begin() + first + half, order.begin() + first + count,
+                         [&](int a, int b) {
+                             float ca = cen[3 * a + ax], cb = cen[3 * b + ax];
+                             return ca < cb || (ca == cb && a < b);
+                         });
+        int l = build(first, half);
+        int r = build(first + half, count - half);
+        std::memcpy(&lo4[4 * node + 3], &l, 4);
+        std::memcpy(&hi4[4 * node + 3], &r, 4);
+        return node;
+    }
+};
+}  // namespace
+
+void hostBuildBvh(int ntri, const double* tri, const double* origin, std::vector<float>& lo4,
+                  std::vector<float>& hi4, std::vector<int>& order) {
+    lo4.clear(); hi4.clear();
+    order.resize(ntri);
+    for (int t = 0; t < ntri; t++) order[t] = t;
+    BvhBuild b{tri, origin, std::vector<float>(3 * (size_t)ntri), lo4, hi4, order};
+    for (int t = 0; t < ntri; t++)
+        for (int k = 0; k < 3; k++)
+            b.cen[3 * t + k] = (float)((tri[9 * t + k] + tri[9 * t + 3 + k] + tri[9 * t + 6 + k]) / 3.0 - origin[k]);
+    if (ntri > 0) b.build(0, ntri);
+}

@@ -153,7 +153,119 @@ __global__ void __launch_bounds__(128) k_wall_distance(Dev d) {
     d.nNeighWall[i] = nw;
 }
 
+// Meshes above MPS_MAX_TRI triangles (libigl's AABB query for large meshes): depth-first
+// walk of the triangle BVH in FP32, nearer child first, pruning boxes whose FP32 distance
+// exceeds the band of the best FP32 triangle distance so far; the triangles inside the band
+// of the final best are then decided exactly as by the brute-force kernel (FP64 Ericson,
+// smallest squared distance, ties to the lowest triangle index).
+#define BVH_STACK 64
+#define BVH_CAND 32
+__device__ __forceinline__ float boxDist2(float4 lo, float4 hi, float px, float py, float pz) {
+    float dx = fmaxf(fmaxf(lo.x - px, px - hi.x), 0.f);
+    float dy = fmaxf(fmaxf(lo.y - py, py - hi.y), 0.f);
+    float dz = fmaxf(fmaxf(lo.z - pz, pz - hi.z), 0.f);
+    return dx * dx + dy * dy + dz * dz;
+}
+__device__ __forceinline__ float bandOf(float bestf) { return bestf + 1e-4f + 1e-5f * bestf; }
+__global__ void __launch_bounds__(128) k_wall_distance_bvh(Dev d) {
+    __shared__ double sTab[4 * MPS_TAB];
+    for (int k = threadIdx.x; k < 4 * MPS_TAB; k += blockDim.x) sTab[k] = d.tab[k];
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    dvec4 p = d.pos[i];
+    const float px = (float)(p.x - P.domainMin[0]), py = (float)(p.y - P.domainMin[1]), pz = (float)(p.z - P.domainMin[2]);
+    int stack[BVH_STACK];
+    int cand[BVH_CAND];
+    float candD[BVH_CAND];
+    int nc = 0;
+    bool overflow = false;
+    float bestf = 3.0e38f;
+    // pass 1: best FP32 distance, keeping the triangles within the band of the best so far
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const int nd = stack[--sp];
+        const float4 lo = __ldg(d.bvhLo + nd), hi = __ldg(d.bvhHi + nd);
+        if (boxDist2(lo, hi, px, py, pz) > bandOf(bestf)) continue;
+        const int a = __float_as_int(lo.w), b = __float_as_int(hi.w);
+        if (a < 0) {
+            for (int q = -a - 1; q < -a - 1 + b; q++) {
+                const int t = __ldg(d.bvhOrder + q);
+                const float df = sqDistTriF(px, py, pz, d.triF + 9 * t);
+                bestf = fminf(bestf, df);
+                if (df <= bandOf(bestf)) {
+                    if (nc < BVH_CAND) { cand[nc] = t; candD[nc] = df; nc++; }
+                    else overflow = true;
+                }
+            }
+        } else if (sp + 2 <= BVH_STACK) {
+            const float da = boxDist2(__ldg(d.bvhLo + a), __ldg(d.bvhHi + a), px, py, pz);
+            const float db = boxDist2(__ldg(d.bvhLo + b), __ldg(d.bvhHi + b), px, py, pz);
+            if (da <= db) { stack[sp++] = b; stack[sp++] = a; }
+            else { stack[sp++] = a; stack[sp++] = b; }
+        } else {
+            overflow = true;   // deeper than the stack: never for a median-split tree of < 2^60 leaves
+        }
+    }
+    const float lim = bandOf(bestf);
+    double best = 1.0 / 0.0;
+    int bt = -1;
+    double bx = 0, by = 0, bz = 0;
+    auto exact = [&](int t) {
+        double qx, qy, qz;
+        closestPtTriX(p.x, p.y, p.z, d.tri + 9 * t, qx, qy, qz);
+        double dx = xsub(p.x, qx), dy = xsub(p.y, qy), dz = xsub(p.z, qz);
+        double d2 = xnorm2(dx, dy, dz);
+        if (d2 < best || (d2 == best && t < bt)) { best = d2; bt = t; bx = qx; by = qy; bz = qz; }
+    };
+    if (!overflow) {
+        for (int c = 0; c < nc; c++)
+            if (candD[c] <= lim) exact(cand[c]);
+    } else {
+        // pass 2 (many near-ties): every triangle within the final band, by a second walk
+        sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            const int nd = stack[--sp];
+            const float4 lo = __ldg(d.bvhLo + nd), hi = __ldg(d.bvhHi + nd);
+            if (boxDist2(lo, hi, px, py, pz) > lim) continue;
+            const int a = __float_as_int(lo.w), b = __float_as_int(hi.w);
+            if (a < 0) {
+                for (int q = -a - 1; q < -a - 1 + b; q++) {
+                    const int t = __ldg(d.bvhOrder + q);
+                    if (sqDistTriF(px, py, pz, d.triF + 9 * t) <= lim) exact(t);
+                }
+            } else if (sp + 2 <= BVH_STACK) {
+                stack[sp++] = a;
+                stack[sp++] = b;
+            }
+        }
+    }
+    double riw2 = d.riw2[i];
+    if (bt >= 0 && best < riw2) {
+        riw2 = best;
+        d.riw2[i] = best;
+        d.wallPos[i] = make_dvec4(bx, by, bz, 0.0);
+        d.mirror[i] = make_dvec4(xadd(p.x, xmul(2.0, xsub(bx, p.x))), xadd(p.y, xmul(2.0, xsub(by, p.y))),
+                                   xadd(p.z, xmul(2.0, xsub(bz, p.z))), 0.0);
+        d.polyNormal[i] = make_dvec4(d.triNormal[bt * 3], d.triNormal[bt * 3 + 1], d.triNormal[bt * 3 + 2], 0.0);
+    }
+    double pw = 0.0;
+    int nw = 0;
+    if (riw2 < P.reL2) {
+        d.nearWall[i] = 1;
+        double x = sqrt(riw2);
+        pw = interpTab(sTab, sTab + MPS_TAB, sqrt(P.reS2), x);
+        nw = (int)interpTab(sTab + 2 * MPS_TAB, sTab + 3 * MPS_TAB, sqrt(P.reL2), x);
+    }
+    d.pndWall[i] = pw;
+    d.nNeighWall[i] = nw;
+}
+
 void launchWallDistance(const Dev& d, cudaStream_t s) {
     if (d.P.wallType != 1 || d.ntri <= 0) return;
-    k_wall_distance<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+    if (d.ntri > MPS_MAX_TRI) k_wall_distance_bvh<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+    else k_wall_distance<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
 }

@@ -1165,6 +1165,157 @@ void pcg(Orc& o) {
     o.solverError = std::sqrt(rn2 / bn2);
 }
 
+// Jacobi-preconditioned BiCGSTAB (van der Vorst 1992, preconditioner applied on the right)
+// with Eigen's documented stopping rule ||r||^2 < tol^2 ||b||^2 and restart of the shadow
+// residual when rho vanishes, standing in for Eigen::BiCGSTAB<SparseMatrix>
+// (src/MpsPressure.cpp:448-468).  Single-threaded.
+void bicgstab(Orc& o) {
+    int n = o.N;
+    const std::vector<long long>& R = o.Arow;
+    std::vector<double> diag(n, 1.0), r(n), r0(n), p(n, 0.0), v(n, 0.0), y(n), s(n), zz(n), t(n);
+    auto spmv = [&](const std::vector<double>& x, std::vector<double>& yv) {
+        for (int i = 0; i < n; i++) {
+            double acc = 0.0;
+            for (long long k = R[i]; k < R[i + 1]; k++) acc += o.Aval[k] * x[o.Acol[k]];
+            yv[i] = acc;
+        }
+    };
+    auto dot = [&](const std::vector<double>& a, const std::vector<double>& b) {
+        double acc = 0.0;
+        for (int i = 0; i < n; i++) acc += a[i] * b[i];
+        return acc;
+    };
+    for (int i = 0; i < n; i++)
+        for (long long k = R[i]; k < R[i + 1]; k++)
+            if (o.Acol[k] == i) diag[i] = o.Aval[k];
+    std::vector<double>& x = o.pressurePPE;
+    const std::vector<double>& b = o.sourceTerm;
+    double bn2 = dot(b, b);
+    o.solverIter = 0;
+    if (bn2 == 0.0) {
+        for (int i = 0; i < n; i++) x[i] = 0.0;
+        o.solverError = 0.0; o.initialError = 0.0;
+        return;
+    }
+    spmv(x, t);
+    for (int i = 0; i < n; i++) { r[i] = b[i] - t[i]; r0[i] = r[i]; }
+    double rn2 = dot(r, r);
+    o.initialError = std::sqrt(rn2 / bn2);
+    double thr = std::max(o.tol * o.tol * bn2, (double)std::numeric_limits<double>::min());
+    double rho = 1.0, alpha = 1.0, w = 1.0;
+    double r0n2 = rn2;
+    int maxIt = (o.maxIter > 0) ? o.maxIter : 2 * n;
+    int it = 0;
+    const double eps = std::numeric_limits<double>::epsilon();
+    while (rn2 > thr && it < maxIt) {
+        double rhoOld = rho;
+        rho = dot(r0, r);
+        if (std::abs(rho) < eps * eps * r0n2) {   // the shadow residual went orthogonal: restart
+            spmv(x, t);
+            for (int i = 0; i < n; i++) { r[i] = b[i] - t[i]; r0[i] = r[i]; }
+            rho = r0n2 = rn2 = dot(r, r);
+            if (rn2 <= thr) break;
+            for (int i = 0; i < n; i++) { p[i] = 0.0; v[i] = 0.0; }
+            rhoOld = alpha = w = 1.0;
+        }
+        double beta = (rho / rhoOld) * (alpha / w);
+        for (int i = 0; i < n; i++) p[i] = r[i] + beta * (p[i] - w * v[i]);
+        for (int i = 0; i < n; i++) y[i] = p[i] / diag[i];
+        spmv(y, v);
+        alpha = rho / dot(r0, v);
+        for (int i = 0; i < n; i++) s[i] = r[i] - alpha * v[i];
+        for (int i = 0; i < n; i++) zz[i] = s[i] / diag[i];
+        spmv(zz, t);
+        double tt = dot(t, t);
+        w = (tt > 0.0) ? dot(t, s) / tt : 0.0;
+        for (int i = 0; i < n; i++) { x[i] += alpha * y[i] + w * zz[i]; r[i] = s[i] - w * t[i]; }
+        rn2 = dot(r, r);
+        it++;
+    }
+    o.solverIter = it;
+    o.solverError = std::sqrt(rn2 / bn2);
+}
+
+// MpsPressure::calcVelDivergence, src/MpsPressure.cpp:479-557 (fluid particles; reS ball off
+// the mirror side; with the correction matrix when gradient correction is on)
+void calcVelDivergence(Orc& o) {
+    const MpsParams& P = o.P;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < o.N; i++) {
+        o.velDiv[i] = 0.0;
+        if (o.type[i] != P.fluid) continue;
+        double DivV = 0.0;
+        double ni = o.pndi[i];
+        const double* xi = &o.pos[i * 3];
+        const double* mi = &o.mirror[i * 3];
+        const double* vi = &o.vel[i * 3];
+        const double MC[9] = {o.c1[i * 3], o.c1[i * 3 + 1], o.c1[i * 3 + 2], o.c2[i * 3], o.c2[i * 3 + 1],
+                              o.c2[i * 3 + 2], o.c3[i * 3], o.c3[i * 3 + 1], o.c3[i * 3 + 2]};
+        forCandidates(o, xi[0], xi[1], xi[2], [&](int j) {
+            Pair q = pairOf(o, j, xi, mi);
+            if (q.d2 < P.reS2 && sideOK(o, q) && j != i) {
+                double vx = o.vel[j * 3] - vi[0], vy = o.vel[j * 3 + 1] - vi[1], vz = o.vel[j * 3 + 2] - vi[2];
+                double wS = weight(std::sqrt(q.d2), P.reS, P.weightType);
+                if (!P.gradientCorrection) {
+                    if (ni > P.epsilonZero)
+                        DivV += (P.dim / P.pndSmallZero) * (o.pndi[j] / ni) * (vx * q.v0 + vy * q.v1 + vz * q.v2) * wS / q.d2;
+                } else {
+                    double c0 = q.v0 * MC[0] + q.v1 * MC[1] + q.v2 * MC[2];
+                    double c1 = q.v0 * MC[3] + q.v1 * MC[4] + q.v2 * MC[5];
+                    double c2 = q.v0 * MC[6] + q.v1 * MC[7] + q.v2 * MC[8];
+                    DivV += (P.dim / P.pndSmallZero) * (vx * c0 + vy * c1 + vz * c2) * wS / q.d2;
+                }
+            }
+        });
+        o.velDiv[i] = DivV;
+    }
+}
+
+// MpsPressure::calcWallSlipVelDivergence / calcWallNoSlipVelDivergence,
+// src/MpsPressure.cpp:560-645 / :648-790 (rigid mesh: wall velocity 0): mirror particles of the
+// fluid near the wall, velocities mirrored (slip: R v_i; no-slip: -v_i), the no-slip pair
+// vectors reflected by R.
+void calcWallVelDivergence(Orc& o) {
+    const MpsParams& P = o.P;
+    const bool noslip = (P.slipCondition == 0);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < o.N; i++) {
+        double ni = o.pndi[i];
+        if (!(o.type[i] == P.fluid && o.nearWall[i] && ni > P.epsilonZero)) continue;
+        const double* xi = &o.pos[i * 3];
+        const double* mi = &o.mirror[i * 3];
+        const double* vi = &o.vel[i * 3];
+        // both variants normalise with the normalMod2 > eps test (src/MpsPressure.cpp:575-588)
+        Refl r = reflMod2(xi, mi, P.epsilonZero);
+        double vm[3];
+        if (noslip) { vm[0] = -vi[0]; vm[1] = -vi[1]; vm[2] = -vi[2]; }
+        else
+            for (int a = 0; a < 3; a++) vm[a] = r.R[a * 3] * vi[0] + r.R[a * 3 + 1] * vi[1] + r.R[a * 3 + 2] * vi[2];
+        double DivV = 0.0;
+        auto term = [&](double vx, double vy, double vz, double m0, double m1, double m2, double dm2, double pj) {
+            double wS = weight(std::sqrt(dm2), P.reS, P.weightType);
+            if (noslip) {
+                vx = -vx; vy = -vy; vz = -vz;
+                double a0 = r.R[0] * m0 + r.R[1] * m1 + r.R[2] * m2;
+                double a1 = r.R[3] * m0 + r.R[4] * m1 + r.R[5] * m2;
+                double a2 = r.R[6] * m0 + r.R[7] * m1 + r.R[8] * m2;
+                m0 = a0; m1 = a1; m2 = a2;
+            }
+            DivV += (P.dim / P.pndSmallZero) * (pj / ni) * (vx * m0 + vy * m1 + vz * m2) * wS / dm2;
+        };
+        forCandidates(o, xi[0], xi[1], xi[2], [&](int j) {
+            Pair q = pairOf(o, j, xi, mi);
+            if (q.d2 < P.reS2 && q.dm2 < P.reS2 && q.d2 < q.dm2 && j != i)
+                term(o.vel[j * 3] - vm[0], o.vel[j * 3 + 1] - vm[1], o.vel[j * 3 + 2] - vm[2], q.m0, q.m1, q.m2, q.dm2,
+                     o.pndi[j]);
+        });
+        double a0 = xi[0] - mi[0], a1 = xi[1] - mi[1], a2 = xi[2] - mi[2];
+        double dii = a0 * a0 + a1 * a1 + a2 * a2;
+        if (dii < P.reS2) term(vi[0] - vm[0], vi[1] - vm[1], vi[2] - vm[2], a0, a1, a2, dii, o.pndi[i]);
+        o.velDiv[i] += DivV;
+    }
+}
+
 // MpsPressure::solvePressurePoissonPnd (src/MpsPressure.cpp:169-286): serial row assembly;
 // the N*n_size zero padding triplets at (0,0) add nothing and are not materialised.
 void assemblePPE(Orc& o) {
@@ -1207,7 +1358,11 @@ void assemblePPE(Orc& o) {
         std::sort(idx.begin(), idx.end(), [&](int a, int b) { return cols[a] < cols[b]; });
         for (int k : idx) { o.Acol.push_back(cols[k]); o.Aval.push_back(vals[k]); }
         o.Arow[i + 1] = (long long)o.Acol.size();
-        o.sourceTerm[i] += -P.coeffPPESource * density * (ni - P.pndSmallZero);
+        if (P.mpsType == 3)   // PND + div u source (src/MpsPressure.cpp:388): the previous PND
+            o.sourceTerm[i] += -P.coeffPPESource * density * (o.pndki[i] - P.pndSmallZero) +
+                               (1.0 - P.relaxPND) * density * o.velDiv[i] / P.timeStep;
+        else
+            o.sourceTerm[i] += -P.coeffPPESource * density * (ni - P.pndSmallZero);
     }
 }
 
@@ -1218,8 +1373,13 @@ void calcPress(Orc& o) {
     if (P.mpsType == 0 || P.mpsType == 1) { pressExplicit(o); return; }
     if ((int)o.pressurePPE.size() != o.N) o.sizeMismatch = 1;
     o.pressurePPE.resize(o.N, 0.0);
+    if (P.mpsType == 3) {   // src/MpsPressure.cpp:44-56
+        calcVelDivergence(o);
+        if (P.wallType == 1) calcWallVelDivergence(o);
+    }
     assemblePPE(o);
-    pcg(o);
+    if (P.solverType == 1) bicgstab(o);
+    else pcg(o);
     for (int i = 0; i < o.N; i++) o.press[i] = o.pressurePPE[i];
     for (int i = 0; i < o.N; i++) if (o.press[i] < 0) o.press[i] = 0.0;
 }

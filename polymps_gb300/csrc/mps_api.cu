@@ -114,7 +114,8 @@ static int opLaunches(int op, const MpsParams& P, bool x) {
         case MPS_OP_PND_DIFFUSIVE: return P.wallType == 1 ? 5 : 4;
         case MPS_OP_PND_MEAN: return P.wallType == 1 ? 3 : 2;
         case MPS_OP_INIT_PND: return 2 + (P.wallType == 1 ? 3 : 2);
-        case MPS_OP_CALC_PRESS: return (P.mpsType == 2) ? 2 : 1;   // assemble + copy back | EOS
+        case MPS_OP_CALC_PRESS:   // (velocity divergence) + assemble + copy back | EOS
+            return (P.mpsType == 2) ? 2 : (P.mpsType == 3 ? (P.wallType == 1 ? 4 : 3) : 1);
         case MPS_OP_SHIFTING:   // FP32 copies (2) + scans + apply kernels (DF32: two scans per sweep + copies)
             if (x) return P.shiftingType == 1 ? 6 : (P.shiftingType == 2 ? (P.wallType == 1 ? 11 : 8) : 0);
             return P.shiftingType == 1 ? 4 : (P.shiftingType == 2 ? (P.wallType == 1 ? 8 : 5) : 0);
@@ -210,8 +211,7 @@ static int unsupported(const MpsParams& P) {
     if (P.fluidType != 0) return 1;
     if (P.freeSurfType == 2) return 1;
     if (P.collisionType != 0) return 1;
-    if (P.mpsType == 3) return 1;
-    if (P.mpsType == 2 && P.solverType != 0) return 1;
+    if (P.solverType != 0 && P.solverType != 1) return 1;
     if (P.relaxPress < 1.0) return 1;
     return 0;
 }
@@ -226,6 +226,8 @@ static int calcPress(mpsgpu_t h) {
     ensureMasks(h);
     cudaEventRecord(h->ea0, h->s);
     if (h->prof.on) h->prof.begin(PROF_PPE_ASSEMBLE, h->s);
+    // PND + div u source: velocity divergence of the predicted velocities (src/MpsPressure.cpp:44-56)
+    if (P.mpsType == 3) launchVelDivergence(h->d, h->s);
     if (df32(h)) launchPpeAssembleDF(h->d, h->B, h->s);
     else launchPpeAssemble(h->d, h->B, h->s);
     if (h->prof.on) h->prof.end(h->s);
@@ -265,7 +267,11 @@ static int calcPress(mpsgpu_t h) {
         g_lastError = "this mixed inner operator needs the single-launch (cooperative) PPE solve";
         return MPSGPU_ERR_UNSUPPORTED;
     }
-    if (h->persistent && pgrid > 0) {
+    if (P.solverType == 1) {   // BiCGSTAB (the reference's solver_type 1), FP64
+        e = ppeSolveBicgstab(h->d, h->B, h->tol, maxIt, h->s, &iters, &rr, &rr0, &h->prof);
+        if (e == MPSGPU_ERR_CUDA) g_lastError = "BiCGSTAB: launch failed or a grid-barrier wait ran out";
+        if (e == MPSGPU_ERR_UNSUPPORTED) g_lastError = "BiCGSTAB needs cooperative launches";
+    } else if (h->persistent && pgrid > 0) {
         e = ppeSolvePersistent(h->d, h->B, mixed ? 1 : 0, h->tol, maxIt, h->s, &iters, &refine, &rr, &rr0, &h->prof);
         if (e == MPSGPU_ERR_CUDA) g_lastError = "persistent PPE solve: launch failed or a grid-barrier wait ran out";
     } else if (mixed) {
@@ -405,8 +411,9 @@ static int stepImpl(mpsgpu_t h) {
     RUN(MPS_OP_COLLISION);
     if (P.wallType == 1) { RUN(MPS_OP_WALL_DISTANCE); RUN(MPS_OP_WALL_NPCD); }
     // The first correctionMatrix call (src/main.cpp:317-319) is read only by the diffusive
-    // PND; otherwise the second call (src/main.cpp:375-377, same positions) overwrites it.
-    if (P.gradientCorrection && P.pndType == 2) RUN(MPS_OP_CORRECTION_MATRIX);
+    // PND and the velocity divergence of the PND + div u source; otherwise the second call
+    // (src/main.cpp:375-377, same positions) overwrites it.
+    if (P.gradientCorrection && (P.pndType == 2 || P.mpsType == 3)) RUN(MPS_OP_CORRECTION_MATRIX);
     RUN(MPS_OP_PND_NEIGH_NPCD);
     if (P.pndType == 2) RUN(MPS_OP_PND_DIFFUSIVE);
     else if (P.pndType == 1) RUN(MPS_OP_PND_MEAN);
@@ -437,7 +444,7 @@ static int finishStats(mpsgpu_t h, MpsStepStats* st, float stepMs) {
     CK(cudaMemcpyAsync(cnt, h->d.counters, sizeof(cnt), cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
     h->last.nbrEntries = (long long)cnt[0];
-    h->last.ppeNnz = (h->d.P.mpsType == 2) ? (long long)cnt[1] + n : 0;
+    h->last.ppeNnz = (h->d.P.mpsType == 2 || h->d.P.mpsType == 3) ? (long long)cnt[1] + n : 0;
     h->last.velMax = vmax;
     h->last.CFLcurrent = h->d.P.timeStep * vmax / h->d.P.partDist;
     h->last.numParticles = n;
@@ -749,8 +756,9 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     B.nblocks = std::max(1, sms) * 8;
-    if (p->mpsType == 2) {
-        for (double** v : {&B.diag, &B.x, &B.b, &B.r, &B.z, &B.p, &B.Ap}) A(*v, n);
+    if (p->mpsType == 2 || p->mpsType == 3) {
+        for (double** v : {&B.diag, &B.x, &B.b, &B.r, &B.z, &B.p, &B.Ap, &B.bs[0], &B.bs[1], &B.bs[2], &B.bs[3]})
+            A(*v, n);
         A(B.val, ell);
         A(B.col, ell);
         A(B.rowLen, n);
@@ -759,9 +767,10 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         A(B.xalt, n);
         B.pgridCg = ppePersistentGrid(0);
         B.pgridMx = ppePersistentGrid(1);
-        A(B.scal, 16);
+        A(B.scal, 32);
             A(B.partials, 4 * std::max(std::max(std::max(B.nblocks, ppePersistentGrid(4)), ppePersistentGrid(3)),
-                                   std::max(std::max(B.pgridCg, ppePersistentGrid(5)), std::max(B.pgridMx, ppePersistentGrid(2)))));
+                                   std::max(std::max(B.pgridCg, std::max(ppePersistentGrid(5), ppePersistentGrid(6))),
+                                            std::max(B.pgridMx, ppePersistentGrid(2)))));
         A(B.counter, 1);
         A(B.flag, 8);
         A(B.dinv, n);
@@ -770,6 +779,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         B.pgridH16 = ppePersistentGrid(3);
         B.pgridTs = ppePersistentGrid(4);
         B.pgridPipe = ppePersistentGrid(5);
+        B.pgridBi = ppePersistentGrid(6);
         // the staged tiles keep up to 128 tile lengths per block in shared memory
         if (B.pgridTs > 0 && (n + 255) / 256 > 128 * B.pgridTs) B.pgridTs = 0;
         A(B.valh, ell);
@@ -1148,7 +1158,7 @@ int mpsgpu_get_neighbors(mpsgpu_t h, int* counts, int* nbr, long long cap) {
 
 int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col, double* val, double* rhs) {
     if (!h || !nnz_out) return MPSGPU_ERR_ARG;
-    if (h->d.P.mpsType != 2) return MPSGPU_ERR_UNSUPPORTED;
+    if (h->d.P.mpsType != 2 && h->d.P.mpsType != 3) return MPSGPU_ERR_UNSUPPORTED;
     int n = 0;
     int e = mpsgpu_num_particles(h, &n);
     if (e) return e;
@@ -1197,7 +1207,7 @@ int mpsgpu_mlp_get_weights(mpsgpu_t h, float* params, float* norm32) {
 }
 int mpsgpu_ppe_features(mpsgpu_t h, float* feat) {
     if (!h || !feat) return MPSGPU_ERR_ARG;
-    if (h->d.P.mpsType != 2) return MPSGPU_ERR_UNSUPPORTED;
+    if (h->d.P.mpsType != 2 && h->d.P.mpsType != 3) return MPSGPU_ERR_UNSUPPORTED;
     int n = 0;
     int e = mpsgpu_num_particles(h, &n);
     if (e) return e;
@@ -1215,7 +1225,7 @@ int mpsgpu_ppe_features(mpsgpu_t h, float* feat) {
 
 int mpsgpu_mlp_record(mpsgpu_t h, int enable) {
     if (!h) return MPSGPU_ERR_ARG;
-    if (h->d.P.mpsType != 2) return MPSGPU_ERR_UNSUPPORTED;
+    if (h->d.P.mpsType != 2 && h->d.P.mpsType != 3) return MPSGPU_ERR_UNSUPPORTED;
     h->mlp.recording = enable != 0;
     return 0;
 }

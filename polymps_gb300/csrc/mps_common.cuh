@@ -171,6 +171,16 @@ __device__ __forceinline__ void bucketCoordsHi(const Dev& d, dvec4 p, float4 hi,
     bz = bucketCoord1(hi.z, p.z, P.domainMin[2], P, d.invSidef, d.epsf);
 }
 
+// PPE source of an equation row: PND deviation (src/MpsPressure.cpp:256), or with the
+// velocity divergence and the previous PND for the PND + div u formulation (:388)
+__device__ __forceinline__ double ppeSource(const Dev& d, int i, double rho) {
+    const MpsParams& P = d.P;
+    if (P.mpsType == 3)
+        return -P.coeffPPESource * rho * (d.pndki[i] - P.pndSmallZero) +
+               (1.0 - P.relaxPND) * rho * d.velDiv[i] / P.timeStep;
+    return -P.coeffPPESource * rho * (d.pndSmall[i] - P.pndSmallZero);
+}
+
 // ------------------------------------------------------------------ weights
 // MpsParticle::weight / delWeight, src/MpsParticle.cpp:57-108
 __device__ __forceinline__ double wfun(double dst, double re, int t) {

@@ -79,6 +79,8 @@ void launchPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallViscosityDF(const Dev& d, cudaStream_t s);
 void launchShiftingDF(const Dev& d, cudaStream_t s);
+// velocity divergence of the PND + div u source (list based, FP64; + the polygon-wall term)
+void launchVelDivergence(const Dev& d, cudaStream_t s);
 // start-of-step list with a skin: build, viscosity over it, and the list of the current
 // positions filtered from it
 void launchSkinListDF(const Dev& d, cudaStream_t s);
@@ -120,6 +122,8 @@ struct PpeBuffers {
     float *wf, *qzf, *mf2;
     double* xalt;
     int pgridPipe;
+    double* bs[4];           // BiCGSTAB: shadow residual r0, s, M^-1 s, A M^-1 s
+    int pgridBi;             // co-resident grid of the BiCGSTAB solver
 };
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);
@@ -136,3 +140,6 @@ int ppeSolveMixed(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cu
 int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol, int maxIter, cudaStream_t s,
                        int* iters, int* refinements, double* relres, double* relres0, Prof* prof);
 int ppePersistentGrid(int mixed);
+// BiCGSTAB (solver_type 1) in one cooperative launch
+int ppeSolveBicgstab(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cudaStream_t s, int* iters,
+                     double* relres, double* relres0, Prof* prof);

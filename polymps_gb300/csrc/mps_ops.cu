@@ -252,6 +252,88 @@ void launchWallNpcd(const Dev& d, cudaStream_t s) {
     k_wall_npcd<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
 }
 
+// ------------------------------------------------------------------ velocity divergence
+// MpsPressure::calcVelDivergence, src/MpsPressure.cpp:479-557: fluid particles over the reS
+// entries off the mirror side; PND-weighted, or through the correction matrix.
+__global__ void __launch_bounds__(BLK) k_vel_div(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    double div = 0.0;
+    if (d.type[i] == P.fluid) {
+        const double ni = d.pndi[i];
+        const dvec4 pi = d.pos[i], vi = d.vel[i];
+        const dvec4 c1 = d.c1[i], c2 = d.c2[i], c3 = d.c3[i];
+        const double f = P.dim / P.pndSmallZero;
+        forMask(d, i, d.maskS[i], [&](int j, size_t) {
+            dvec4 pj = d.pos[j], vj = d.vel[j];
+            PairG q = pairOf(pj, pi);
+            double vx = vj.x - vi.x, vy = vj.y - vi.y, vz = vj.z - vi.z;
+            double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+            if (!P.gradientCorrection) {
+                if (ni > P.epsilonZero) div += f * (d.pndi[j] / ni) * (vx * q.v0 + vy * q.v1 + vz * q.v2) * wS / q.d2;
+            } else {
+                double a0 = q.v0 * c1.x + q.v1 * c1.y + q.v2 * c1.z;
+                double a1 = q.v0 * c2.x + q.v1 * c2.y + q.v2 * c2.z;
+                double a2 = q.v0 * c3.x + q.v1 * c3.y + q.v2 * c3.z;
+                div += f * (vx * a0 + vy * a1 + vz * a2) * wS / q.d2;
+            }
+        });
+    }
+    d.velDiv[i] = div;
+}
+// calcWallSlipVelDivergence / calcWallNoSlipVelDivergence, src/MpsPressure.cpp:560-790
+// (rigid mesh: wall velocity 0): mirror velocity R v_i (slip) or -v_i (no-slip), the no-slip
+// pair vectors reflected by R, over the near-wall fluid with n_i > eps.
+__global__ void __launch_bounds__(BLK) k_wall_vel_div(Dev d) {
+    int i = nearIndex(d);
+    if (i < 0) return;
+    const MpsParams& P = d.P;
+    const double ni = d.pndi[i];
+    if (!(ni > P.epsilonZero)) return;
+    const bool noslip = P.slipCondition == 0;
+    const dvec4 pi = d.pos[i], mi = d.mirror[i], vi = d.vel[i];
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, false);
+    double vm[3];
+    if (noslip) { vm[0] = -vi.x; vm[1] = -vi.y; vm[2] = -vi.z; }
+    else {
+        vm[0] = r.R[0] * vi.x + r.R[1] * vi.y + r.R[2] * vi.z;
+        vm[1] = r.R[3] * vi.x + r.R[4] * vi.y + r.R[5] * vi.z;
+        vm[2] = r.R[6] * vi.x + r.R[7] * vi.y + r.R[8] * vi.z;
+    }
+    const double f = P.dim / P.pndSmallZero;
+    double div = 0.0;
+    auto term = [&](double vx, double vy, double vz, double m0, double m1, double m2, double dm2, double pj) {
+        double wS = wfun(sqrt(dm2), P.reS, P.weightType);
+        if (noslip) {
+            vx = -vx; vy = -vy; vz = -vz;
+            double a0 = r.R[0] * m0 + r.R[1] * m1 + r.R[2] * m2;
+            double a1 = r.R[3] * m0 + r.R[4] * m1 + r.R[5] * m2;
+            double a2 = r.R[6] * m0 + r.R[7] * m1 + r.R[8] * m2;
+            m0 = a0; m1 = a1; m2 = a2;
+        }
+        div += f * (pj / ni) * (vx * m0 + vy * m1 + vz * m2) * wS / dm2;
+    };
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2) {
+            PairM m = pairMirror(pj, mi);
+            if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
+                dvec4 vj = d.vel[j];
+                term(vj.x - vm[0], vj.y - vm[1], vj.z - vm[2], m.m0, m.m1, m.m2, m.dm2, d.pndi[j]);
+            }
+        }
+    });
+    PairM s = pairMirror(pi, mi);
+    if (s.dm2 < P.reS2) term(vi.x - vm[0], vi.y - vm[1], vi.z - vm[2], s.m0, s.m1, s.m2, s.dm2, ni);
+    d.velDiv[i] += div;
+}
+void launchVelDivergence(const Dev& d, cudaStream_t s) {
+    k_vel_div<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    if (d.P.wallType == 1) k_wall_vel_div<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
+
 // ------------------------------------------------------------------ correction matrix
 // MpsVectorMatrix::correctionMatrix + inverseMatrix (Gauss-Jordan without pivoting,
 // identity when det <= eps or numNeigh < 4), src/MpsVectorMatrix.cpp:20-166

@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
     B.diagf[i] = (float)dg;
     B.diagInvf[i] = 1.0f / (float)dg;
     B.rowLen[i] = len;
-    B.b[i] = dD(src) + (-P.coeffPPESource * rho * (d.pndSmall[i] - P.pndSmallZero));
+    B.b[i] = dD(src) + ppeSource(d, i, rho);
     warpCount(d.counters + 1, (unsigned)len);
 }
 void launchPpeAssembleDF(const Dev& d, const PpeBuffers& B, cudaStream_t s) {

@@ -21,7 +21,8 @@
 #define PBLK 256
 
 // solver scalars in B.scal[]
-enum { S_RZ = 0, S_RR, S_BB, S_ALPHA, S_BETA, S_PAP, S_THR, S_RZNEW, S_SCALE, S_INV, S_SQRT, S_ETA2, S_RR0, S_COUNT };
+enum { S_RZ = 0, S_RR, S_BB, S_ALPHA, S_BETA, S_PAP, S_THR, S_RZNEW, S_SCALE, S_INV, S_SQRT, S_ETA2, S_RR0,
+       S_RHO, S_RHOOLD, S_OMEGA, S_R0N2, S_COUNT };
 
 // ------------------------------------------------------------------ assembly
 __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
@@ -63,7 +64,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
     B.diag[i] = sum;
     B.rowLen[i] = len;
     B.mfMask[i] = mm;
-    B.b[i] = src + (-P.coeffPPESource * rho * (d.pndSmall[i] - P.pndSmallZero));
+    B.b[i] = src + ppeSource(d, i, rho);
     warpCount(d.counters + 1, (unsigned)len);
 }
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s) {
@@ -1276,9 +1277,133 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
     }
 }
 
+// Jacobi-preconditioned BiCGSTAB (solver_type 1: Eigen::BiCGSTAB, src/MpsPressure.cpp:448-468;
+// van der Vorst 1992 with the preconditioner on the right), in one cooperative launch: per
+// iteration two SpMVs and five grid synchronisations (y and z must be complete before their
+// SpMVs; (r0, v), (t, t) and (t, s), (r, r) and (r0, r) are grid sums).  The shadow residual
+// is restarted when (r0, r) vanishes relative to its start, the stopping rule is
+// ||r||^2 < tol^2 ||b||^2 on the recurrence residual, and the FP64 residual of the result is
+// reported.
+__global__ void __launch_bounds__(QB, 3) k_bicgstab(Dev d, PpeBuffers B, double tol, int maxIter) {
+    const int n = liveN(d);
+    const int T = gridDim.x * QB;
+    const int t0 = blockIdx.x * QB + threadIdx.x;
+    const int r1 = n;
+    QCtl c = {0u};
+    double *r0 = B.bs[0], *sv = B.bs[1], *zz = B.bs[2], *tv = B.bs[3], *y = B.z, *v = B.Ap;
+    auto restart = [&](bool first) -> bool {
+        double a[2] = {0.0, 0.0};
+        forRows(B, r1, t0, T, [&](int i, int len) {
+            if (first) B.dinv[i] = 1.0 / __ldg(B.diag + i);
+            double r = B.b[i] - qRow(B, B.x, i, len);
+            B.r[i] = r; r0[i] = r; B.p[i] = 0.0; v[i] = 0.0;
+            a[0] += r * r;
+            if (first) a[1] += B.b[i] * B.b[i];
+        });
+        return qSum<2>(a, B, c, [&](const double* t) {
+            if (first) {
+                B.scal[S_BB] = t[1];
+                double thr = tol * tol * t[1];
+                if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
+                B.scal[S_THR] = thr;
+                B.scal[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
+                B.flag[1] = 0;
+                if (t[1] == 0.0) B.flag[0] = 1;
+            }
+            B.scal[S_RR] = B.scal[S_RHO] = B.scal[S_R0N2] = t[0];
+            B.scal[S_RHOOLD] = B.scal[S_ALPHA] = B.scal[S_OMEGA] = 1.0;
+            B.flag[5] = 0;
+            if (t[0] < B.scal[S_THR]) B.flag[0] = 1;
+            if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
+        });
+    };
+    if (!restart(true)) return;
+    int it = 0;
+    while (!vi(B.flag) && it < maxIter) {
+        {   // p = r + beta (p - w v), y = M^-1 p
+            const double rho = vd(B.scal + S_RHO), w = vd(B.scal + S_OMEGA);
+            const double beta = (rho / vd(B.scal + S_RHOOLD)) * (vd(B.scal + S_ALPHA) / w);
+            for (int i = t0; i < r1; i += T) {
+                double p = B.r[i] + beta * (B.p[i] - w * v[i]);
+                B.p[i] = p;
+                y[i] = p * B.dinv[i];
+            }
+            if (!qBarrier(B, c)) return;
+        }
+        {   // v = A y, alpha = rho / (r0, v)
+            double a[1] = {0.0};
+            forRows(B, r1, t0, T, [&](int i, int len) {
+                double q = qRow(B, y, i, len);
+                v[i] = q;
+                a[0] += r0[i] * q;
+            });
+            if (!qSum<1>(a, B, c, [&](const double* t) {
+                    double al = B.scal[S_RHO] / t[0];
+                    B.scal[S_ALPHA] = al;
+                    if (!(al == al) || t[0] == 0.0) { B.flag[0] = 1; B.flag[2] = 1; }
+                }))
+                return;
+        }
+        if (vi(B.flag)) break;
+        {   // s = r - alpha v, z = M^-1 s
+            const double alpha = vd(B.scal + S_ALPHA);
+            for (int i = t0; i < r1; i += T) {
+                double s = B.r[i] - alpha * v[i];
+                sv[i] = s;
+                zz[i] = s * B.dinv[i];
+            }
+            if (!qBarrier(B, c)) return;
+        }
+        {   // t = A z, w = (t, s) / (t, t)
+            double a[2] = {0.0, 0.0};
+            forRows(B, r1, t0, T, [&](int i, int len) {
+                double q = qRow(B, zz, i, len);
+                tv[i] = q;
+                a[0] += q * q;
+                a[1] += q * sv[i];
+            });
+            if (!qSum<2>(a, B, c, [&](const double* t) { B.scal[S_OMEGA] = (t[0] > 0.0) ? t[1] / t[0] : 0.0; }))
+                return;
+        }
+        {   // x += alpha y + w z, r = s - w t; (r, r) and the next rho = (r0, r)
+            const double alpha = vd(B.scal + S_ALPHA), w = vd(B.scal + S_OMEGA);
+            double a[2] = {0.0, 0.0};
+            for (int i = t0; i < r1; i += T) {
+                B.x[i] += alpha * y[i] + w * zz[i];
+                double r = sv[i] - w * tv[i];
+                B.r[i] = r;
+                a[0] += r * r;
+                a[1] += r0[i] * r;
+            }
+            if (!qSum<2>(a, B, c, [&](const double* t) {
+                    B.flag[1] += 1;
+                    B.scal[S_RR] = t[0];
+                    B.scal[S_RHOOLD] = B.scal[S_RHO];
+                    B.scal[S_RHO] = t[1];
+                    if (t[0] < B.scal[S_THR]) B.flag[0] = 1;
+                    else if (fabs(t[1]) < 4.930380657631324e-32 * B.scal[S_R0N2]) B.flag[5] = 1;   // eps^2
+                    if (!(t[0] == t[0]) || B.scal[S_OMEGA] == 0.0) { B.flag[0] = 1; B.flag[2] = 1; }
+                }))
+                return;
+        }
+        it++;
+        if (vi(B.flag + 5) && !vi(B.flag))
+            if (!restart(false)) return;
+    }
+    if (!qBarrier(B, c)) return;
+    {
+        double a[1] = {0.0};
+        forRows(B, r1, t0, T, [&](int i, int len) {
+            double r = B.b[i] - qRow(B, B.x, i, len);
+            a[0] += r * r;
+        });
+        qSum<1>(a, B, c, [&](const double* t) { B.scal[S_RR] = t[0]; });
+    }
+}
+
 // kind: 0 plain FP64, 1 mixed, 2 mixed with the matrix-free inner operator, 3 mixed with
 // the compact scaled inner operator, 4 mixed with the staged tiles, 5 mixed with the
-// pipelined inner CG
+// pipelined inner CG, 6 BiCGSTAB
 int ppePersistentGrid(int kind) {
     int dev = 0, sms = 0, coop = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
@@ -1294,7 +1419,8 @@ int ppePersistentGrid(int kind) {
             return 0;
         return per * sms;
     }
-    cudaError_t e = kind == 5   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_pipe, QB, 0)
+    cudaError_t e = kind == 6   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bicgstab, QB, 0)
+                    : kind == 5 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_pipe, QB, 0)
                     : kind == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_H16>, QB, 0)
                     : kind == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_MATFREE>, QB, 0)
                     : kind == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_ELL32>, QB, 0)
@@ -1321,6 +1447,25 @@ static int finishPersistent(const PpeBuffers& B, cudaStream_t s, int* iters, int
     *relres0 = sc[S_SCALE];
     if (f[2] || !f[0]) return MPSGPU_ERR_NOT_CONVERGED;
     return 0;
+}
+
+int ppeSolveBicgstab(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cudaStream_t s, int* iters,
+                     double* relres, double* relres0, Prof* prof) {
+    if (B.pgridBi <= 0) return MPSGPU_ERR_UNSUPPORTED;
+    bool pr = prof && prof->on;
+    cudaMemsetAsync(B.flag, 0, 8 * sizeof(int), s);
+    cudaMemsetAsync(B.bar, 0, QB_WORDS * sizeof(unsigned int), s);
+    Dev dd = d;
+    PpeBuffers bb = B;
+    double t = tol;
+    int mi = maxIter;
+    void* args[4] = {&dd, &bb, &t, &mi};
+    if (pr) prof->begin(PROF_PPE_SOLVE, s);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_bicgstab, B.pgridBi, QB, args, 0, s);
+    if (pr) prof->end(s);
+    if (e != cudaSuccess) return MPSGPU_ERR_CUDA;
+    countLaunch(1);
+    return finishPersistent(B, s, iters, nullptr, relres, relres0);
 }
 
 int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol, int maxIter, cudaStream_t s,

@@ -83,7 +83,7 @@ int main(int argc, char** argv) {
             int sec = (int)(now() - t0);
             std::printf("Iteration: %5dth Time: %lfsec Num. Particles: %d Max Velocity: %lfm/s Courant: %lf", iter, time,
                         st.numParticles, st.velMax, st.CFLcurrent);
-            if (P.mpsType == 2) std::printf(" Solver iterations: %3d Estimated error: %.2e", st.ppeIterations, st.ppeRelResidual);
+            if (P.mpsType == 2 || P.mpsType == 3) std::printf(" Solver iterations: %3d Estimated error: %.2e", st.ppeIterations, st.ppeRelResidual);
             std::printf(" RunTime: %02dh%02dm%02dsec\n", sec / 3600, (sec / 60) % 60, sec % 60);
         }
         if (output && iter % P.iterOutput == 0 && c.out.vtuType == 1) {

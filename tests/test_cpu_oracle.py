@@ -142,6 +142,31 @@ def test_oracle_pcg_vs_scipy(oracle_mod):
     assert asym < 1.0
 
 
+@pytest.mark.parametrize("mps_type,solver", [(3, 0), (3, 1), (2, 1)])
+def test_oracle_divu_and_bicgstab(oracle_mod, mps_type, solver):
+    """The PND + div u source (mps_type 3) and the BiCGSTAB solver (solver_type 1): the
+    oracle's solution of its assembled system against a direct solve."""
+    sp = pytest.importorskip("scipy.sparse")
+    spla = pytest.importorskip("scipy.sparse.linalg")
+    c = cases.config(3, scale=5.0)
+    c.params.update(mpsType=mps_type, solverType=solver)
+    o = oracle_mod.Oracle(c)
+    o.set_solver(1e-12)
+    o.initialize()
+    for _ in range(3):
+        o.step()
+    rowptr, col, val, rhs = o.ppe()
+    A = sp.csr_matrix((val, col, rowptr), shape=(len(rhs), len(rhs)))
+    x_ref = spla.spsolve(A.tocsc(), rhs)
+    x = o.get(abi.F_PRESSPPE)
+    assert np.linalg.norm(x - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+    dv = o.get(abi.F_VELDIV)
+    if mps_type == 3:
+        assert np.abs(dv).max() > 0
+        fl = o.get(abi.F_TYPE) == 0
+        assert np.all(dv[~fl] == 0)
+
+
 def test_oracle_dam_break_sanity(oracle_mod):
     """cfg1 (2D, particle walls): the front advances and the bottom pressure approaches
     the hydrostatic scale; every PPE solve reaches 1e-8."""

@@ -69,7 +69,7 @@ def step_ops(p):
     ops = ["UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT", "OUT_OF_DOMAIN", "COLLISION"]
     if p.wallType == 1:
         ops += ["WALL_DISTANCE", "WALL_NPCD"]
-    if p.gradientCorrection and p.pndType == 2:
+    if p.gradientCorrection and (p.pndType == 2 or p.mpsType == 3):
         ops += ["CORRECTION_MATRIX"]
     ops += ["PND_NEIGH_NPCD"]
     if p.pndType == 2:

@@ -1026,6 +1026,68 @@ void collision(Orc& o) {
     }
 }
 
+// MpsParticleCollision::checkDynamicParticleCollisions (DPC), src/MpsParticleCollision.cpp:
+// 120-292: pairs closer than l0 off the mirror side; approaching pairs exchange momentum
+// with coefficient kappa (1 below l0/2, else chi = sqrt(W_ij / W(l0/2)) of the Wendland-type
+// kernel (1 - r/l0)^4 (4 r/l0 + 1)), separating pairs get a dynamic background-pressure
+// repulsion; then v += dv and x += dv dt for fluid particles.  (The wall pressure maximum
+// the reference computes first is not used.)
+void collisionDPC(Orc& o) {
+    const MpsParams& P = o.P;
+    const double Wij5 = 0.5 * 0.5 * 0.5 * 0.5 * 3.0;
+    const double gMod = std::sqrt(P.gravity[0] * P.gravity[0] + P.gravity[1] * P.gravity[1] + P.gravity[2] * P.gravity[2]);
+    const double l02 = P.partDist * P.partDist;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < o.N; i++) {
+        if (o.type[i] != P.fluid) continue;
+        double mi = (o.PTYPE[i] == 1) ? P.DNS_FL1 : P.DNS_FL2;
+        const double* xi = &o.pos[i * 3];
+        const double* vi = &o.vel[i * 3];
+        const double* mr = &o.mirror[i * 3];
+        double dv[3] = {0, 0, 0};
+        forCandidates(o, xi[0], xi[1], xi[2], [&](int j) {
+            Pair q = pairOf(o, j, xi, mr);
+            if (q.d2 < l02 && sideOK(o, q) && j != i) {
+                double mj;
+                if (o.type[j] == P.fluid) mj = (o.PTYPE[j] == 1) ? P.DNS_FL1 : P.DNS_FL2;
+                else mj = o.Dns[1];
+                double dst = std::sqrt(q.d2);
+                double Wij = 0.0;
+                if (dst > P.epsilonZero) {
+                    double w1 = 1.0 - dst * P.invPartDist;
+                    double w2 = 4.0 * dst * P.invPartDist + 1.0;
+                    Wij = w1 * w1 * w1 * w1 * w2;
+                }
+                double chi = std::sqrt(Wij / Wij5);
+                double kappa = (dst < 0.5 * P.partDist) ? 1.0 : chi;
+                double fDT = (vi[0] - o.vel[j * 3]) * q.v0 + (vi[1] - o.vel[j * 3 + 1]) * q.v1 + (vi[2] - o.vel[j * 3 + 2]) * q.v2;
+                double f2 = (o.type[j] == P.fluid) ? 1.0 : 2.0;
+                if (fDT > 0.0) {
+                    fDT *= kappa * 2.0 * mj / (mi + mj) / q.d2;
+                    dv[0] -= f2 * q.v0 * fDT; dv[1] -= f2 * q.v1 * fDT; dv[2] -= f2 * q.v2 * fDT;
+                } else {
+                    double pmax = 2.0 / 3.0 * o.RHO[i] * gMod * 0.2;
+                    double pmin = o.RHO[i] * gMod * P.partDist;
+                    double ptil = std::max(std::min(P.lambdaCollision * std::fabs(o.press[i] + o.press[j]),
+                                                    P.lambdaCollision * pmax), pmin);
+                    double pb = ptil * chi;
+                    double rep = P.timeStep / mi * chi * pb / q.d2;
+                    dv[0] -= f2 * q.v0 * rep; dv[1] -= f2 * q.v1 * rep; dv[2] -= f2 * q.v2 * rep;
+                }
+            }
+        });
+        for (int k = 0; k < 3; k++) o.dvel[i * 3 + k] = dv[k];
+    }
+    for (int i = 0; i < o.N; i++) {
+        if (o.type[i] == P.fluid)
+            for (int k = 0; k < 3; k++) {
+                o.vel[i * 3 + k] += o.dvel[i * 3 + k];
+                o.pos[i * 3 + k] += o.dvel[i * 3 + k] * P.timeStep;
+            }
+        for (int k = 0; k < 3; k++) o.dvel[i * 3 + k] = 0.0;
+    }
+}
+
 // ------------------------------------------------------------------ correction matrix
 // MpsVectorMatrix::detMatrix / inverseMatrix, src/MpsVectorMatrix.cpp:96-166
 double detMatrix(double a, double b, double c, double d, double e, double f, double g, double h, double k) {
@@ -1630,7 +1692,7 @@ int runOp(Orc& o, int op) {
         case MPS_OP_ADD_GRAVITY: addGravity(o); return 0;
         case MPS_OP_PREDICT: predict(o); return 0;
         case MPS_OP_OUT_OF_DOMAIN: checkParticleOutDomain(o); return 0;
-        case MPS_OP_COLLISION: collision(o); return 0;
+        case MPS_OP_COLLISION: if (P.collisionType == 1) collisionDPC(o); else collision(o); return 0;
         case MPS_OP_WALL_DISTANCE: if (P.wallType == 1) wallDistance(o); return 0;
         case MPS_OP_WALL_NPCD: if (P.wallType == 1) calcWallNPCD(o); return 0;
         case MPS_OP_CORRECTION_MATRIX: correctionMatrix(o); return 0;
@@ -1691,7 +1753,8 @@ int step(Orc& o) {
     addGravity(o);
     predict(o);
     checkParticleOutDomain(o);
-    collision(o);
+    if (P.collisionType == 1) collisionDPC(o);
+    else collision(o);
     if (P.wallType == 1) { wallDistance(o); calcWallNPCD(o); }
     if (P.gradientCorrection) correctionMatrix(o);
     calcPndnNeighNPCD(o);

@@ -107,7 +107,7 @@ static int opLaunches(int op, const MpsParams& P, bool x) {
         case MPS_OP_UPDATE_BUCKETS: return 8;   // key, 3 scan, scatter, sort, list positions, bucket-ordered copy
         case MPS_OP_VISCOSITY: return x ? 3 : 1;   // (DF32: velocity copy) + sweep (+ unlisted particles)
         case MPS_OP_OUT_OF_DOMAIN: return 2;
-        case MPS_OP_COLLISION: return x ? 3 : 2;
+        case MPS_OP_COLLISION: return P.collisionType == 1 ? 2 : (x ? 3 : 2);
         case MPS_OP_WALL_DISTANCE: case MPS_OP_WALL_NPCD: return P.wallType == 1 ? 1 : 0;
         case MPS_OP_WALL_PRESS_GRADIENT: case MPS_OP_WALL_VISCOSITY: return P.wallType == 1 ? (x ? 2 : 1) : 0;
         case MPS_OP_PRESS_GRADIENT: return x ? 2 : 1;
@@ -210,7 +210,7 @@ static int unsupported(const MpsParams& P) {
     if (P.domainTypeBC != 0) return 1;
     if (P.fluidType != 0) return 1;
     if (P.freeSurfType == 2) return 1;
-    if (P.collisionType != 0) return 1;
+    if (P.collisionType != 0 && P.collisionType != 1) return 1;
     if (P.solverType != 0 && P.solverType != 1) return 1;
     if (P.relaxPress < 1.0) return 1;
     return 0;
@@ -352,7 +352,14 @@ static int runOpBody(mpsgpu_t h, int op) {
         case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
         case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
         case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); invalidate(); break;
-        case MPS_OP_COLLISION: ensureList(h); if (x) launchCollisionDF(d, s); else launchCollision(d, s); break;
+        case MPS_OP_COLLISION:
+            ensureList(h);
+            if (P.collisionType == 1) {   // DPC moves the positions: every list is stale
+                launchCollisionDPC(d, s);
+                invalidate();
+            } else if (x) launchCollisionDF(d, s);
+            else launchCollision(d, s);
+            break;
         case MPS_OP_WALL_DISTANCE: launchWallDistance(d, s); h->masksValid = false; h->corrFresh = false; break;
         case MPS_OP_WALL_NPCD: ensureMasks(h); if (x) launchWallNpcdDF(d, s); else launchWallNpcd(d, s); break;
         case MPS_OP_CORRECTION_MATRIX:

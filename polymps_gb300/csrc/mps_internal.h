@@ -79,6 +79,8 @@ void launchPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallViscosityDF(const Dev& d, cudaStream_t s);
 void launchShiftingDF(const Dev& d, cudaStream_t s);
+// dynamic particle collision (collision type 1, FP64, list based; moves positions)
+void launchCollisionDPC(const Dev& d, cudaStream_t s);
 // velocity divergence of the PND + div u source (list based, FP64; + the polygon-wall term)
 void launchVelDivergence(const Dev& d, cudaStream_t s);
 // start-of-step list with a skin: build, viscosity over it, and the list of the current

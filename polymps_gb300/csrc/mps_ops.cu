@@ -211,6 +211,74 @@ void launchCollision(const Dev& d, cudaStream_t s) {
     launchCollisionApply(d, s);
 }
 
+// MpsParticleCollision::checkDynamicParticleCollisions (DPC, collision type 1),
+// src/MpsParticleCollision.cpp:120-292: list entries closer than l0 off the mirror side;
+// approaching pairs exchange momentum with kappa (1 below l0/2, else chi =
+// sqrt(W_ij / W(l0/2)), W = (1 - r/l0)^4 (4 r/l0 + 1)), separating pairs get the dynamic
+// background-pressure repulsion; then v += dv, x += dv dt for fluid particles.
+__global__ void __launch_bounds__(BLK) k_collision_dpc(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    dvec4 dv = make_dvec4(0, 0, 0, 0);
+    const MpsParams& P = d.P;
+    if (d.type[i] == P.fluid) {
+        const double mi = P.DNS_FL1;   // PTYPE == 1 for every Newtonian particle
+        const double Wij5 = 0.5 * 0.5 * 0.5 * 0.5 * 3.0;
+        const double gMod = sqrt(P.gravity[0] * P.gravity[0] + P.gravity[1] * P.gravity[1] + P.gravity[2] * P.gravity[2]);
+        const double l02 = P.partDist * P.partDist;
+        const double pmax = 2.0 / 3.0 * P.DNS_FL1 * gMod * 0.2, pmin = P.DNS_FL1 * gMod * P.partDist;
+        const dvec4 pi = d.pos[i], vi = d.vel[i];
+        const double pri = d.press[i];
+        SideCtx sc = sideCtx(d, i, pi);
+        forNbrs(d, i, [&](int j) {
+            dvec4 pj = d.pos[j];
+            PairG q = pairOf(pj, pi);
+            if (!(q.d2 < l02 && sideOK(sc, pj, q.d2))) return;
+            const bool jf = d.type[j] == P.fluid;
+            const double mj = jf ? P.DNS_FL1 : P.densityWall;
+            const double dst = sqrt(q.d2);
+            double Wij = 0.0;
+            if (dst > P.epsilonZero) {
+                double w1 = 1.0 - dst * P.invPartDist;
+                double w2 = 4.0 * dst * P.invPartDist + 1.0;
+                Wij = w1 * w1 * w1 * w1 * w2;
+            }
+            const double chi = sqrt(Wij / Wij5);
+            const double kappa = (dst < 0.5 * P.partDist) ? 1.0 : chi;
+            const dvec4 vj = d.vel[j];
+            double fDT = (vi.x - vj.x) * q.v0 + (vi.y - vj.y) * q.v1 + (vi.z - vj.z) * q.v2;
+            const double f2 = jf ? 1.0 : 2.0;
+            double k;
+            if (fDT > 0.0) {
+                k = fDT * kappa * 2.0 * mj / (mi + mj) / q.d2;
+            } else {
+                double ptil = fmax(fmin(P.lambdaCollision * fabs(pri + d.press[j]), P.lambdaCollision * pmax), pmin);
+                double pb = ptil * chi;
+                k = P.timeStep / mi * chi * pb / q.d2;
+            }
+            dv.x -= f2 * q.v0 * k; dv.y -= f2 * q.v1 * k; dv.z -= f2 * q.v2 * k;
+        });
+    }
+    d.dvel[i] = dv;
+}
+__global__ void k_collision_dpc_apply(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    if (d.type[i] == d.P.fluid) {
+        dvec4 v = d.vel[i], x = d.pos[i], dv = d.dvel[i];
+        const double dt = d.P.timeStep;
+        v.x += dv.x; v.y += dv.y; v.z += dv.z;
+        x.x += dv.x * dt; x.y += dv.y * dt; x.z += dv.z * dt;
+        d.vel[i] = v;
+        d.pos[i] = x;
+    }
+    d.dvel[i] = make_dvec4(0, 0, 0, 0);
+}
+void launchCollisionDPC(const Dev& d, cudaStream_t s) {
+    k_collision_dpc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    k_collision_dpc_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+}
+
 // ------------------------------------------------------------------ wall NPCD
 // Wall-only sweeps run over the compacted list of fluid particles near the wall.
 __device__ __forceinline__ int nearIndex(const Dev& d) {

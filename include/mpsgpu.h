@@ -129,6 +129,7 @@ enum MpsField {
     MPS_F_POS = 0, MPS_F_VEL, MPS_F_ACC, MPS_F_ACCSTAR, MPS_F_NPCD, MPS_F_GRADC,
     MPS_F_CORR1, MPS_F_CORR2, MPS_F_CORR3, MPS_F_MIRROR, MPS_F_WALLPOS, MPS_F_POLYNORMAL,
     MPS_F_FORCEWALL,
+    MPS_F_NORMAL,                 /* fluid normal of the ARC free-surface test (MpsParticle::normal) */
     MPS_F_PRESS = 32, MPS_F_PRESSPPE, MPS_F_PNDI, MPS_F_PNDKI, MPS_F_PNDSKI, MPS_F_PNDSMALL,
     MPS_F_NPCD2, MPS_F_CONC, MPS_F_VELDIV, MPS_F_DIFFTERM, MPS_F_PNDWALL, MPS_F_RIW2,
     MPS_F_DEVDOT, MPS_F_SOURCE,

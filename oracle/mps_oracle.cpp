@@ -38,7 +38,7 @@ struct Orc {
         aux1, aux2, pndWall, devDot, riw2, RHO, MEU;
     // vectors, interleaved xyz
     std::vector<double> pos, vel, acc, accStar, npcd, gradC, c1, c2, c3, dvel, wallPos, mirror,
-        polyNormal, forceWall;
+        polyNormal, forceWall, normal;
     std::vector<double> pressurePPE, sourceTerm;
     // buckets (include/MpsParticle.h:138-141)
     std::vector<int> first, last, next;
@@ -1140,8 +1140,70 @@ void correctionMatrix(Orc& o) {
 
 // ------------------------------------------------------------------ boundary condition
 // MpsBoundaryCondition::updateParticleBC (types 0 and 1), src/MpsBoundaryCondition.cpp:173-204
+// MpsShifting::calcNormalParticles, src/MpsShifting.cpp:106-166: n_i = -sum r_ij w / |r_ij| / n0
+// over the reS ball off the mirror side (every particle)
+void calcNormalParticles(Orc& o) {
+    const MpsParams& P = o.P;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < o.N; i++) {
+        const double* xi = &o.pos[i * 3];
+        const double* mi = &o.mirror[i * 3];
+        double d[3] = {0, 0, 0};
+        forCandidates(o, xi[0], xi[1], xi[2], [&](int j) {
+            Pair q = pairOf(o, j, xi, mi);
+            if (q.d2 < P.reS2 && sideOK(o, q) && j != i) {
+                double dst = std::sqrt(q.d2);
+                double wS = weight(dst, P.reS, P.weightType);
+                d[0] += q.v0 * wS / dst; d[1] += q.v1 * wS / dst; d[2] += q.v2 * wS / dst;
+            }
+        });
+        for (int k = 0; k < 3; k++) o.normal[i * 3 + k] = -d[k] / P.pndSmallZero;
+    }
+}
+// MpsShifting::calcWallNormalParticles, src/MpsShifting.cpp:319-420: mirror entries of the
+// fluid near the wall and i itself as a neighbour of its mirror, reflected by R
+void calcWallNormalParticles(Orc& o) {
+    const MpsParams& P = o.P;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < o.N; i++) {
+        if (!(o.type[i] == P.fluid && o.nearWall[i])) continue;
+        const double* xi = &o.pos[i * 3];
+        const double* mi = &o.mirror[i * 3];
+        Refl r = reflSqrt(xi, mi, P.epsilonZero);
+        double d[3] = {0, 0, 0};
+        forCandidates(o, xi[0], xi[1], xi[2], [&](int j) {
+            Pair q = pairOf(o, j, xi, mi);
+            if (q.d2 < P.reS2 && q.dm2 < P.reS2 && q.d2 < q.dm2 && j != i) {
+                double dst = std::sqrt(q.dm2);
+                double wS = weight(dst, P.reS, P.weightType);
+                d[0] += q.m0 * wS / dst; d[1] += q.m1 * wS / dst; d[2] += q.m2 * wS / dst;
+            }
+        });
+        double a0 = xi[0] - mi[0], a1 = xi[1] - mi[1], a2 = xi[2] - mi[2];
+        double dii = a0 * a0 + a1 * a1 + a2 * a2;
+        if (dii < P.reS2) {
+            double dst = std::sqrt(dii);
+            double wS = weight(dst, P.reS, P.weightType);
+            d[0] += a0 * wS / dst; d[1] += a1 * wS / dst; d[2] += a2 * wS / dst;
+        }
+        for (int k = 0; k < 3; k++)
+            o.normal[i * 3 + k] += -(r.R[k * 3] * d[0] + r.R[k * 3 + 1] * d[1] + r.R[k * 3 + 2] * d[2]) / P.pndSmallZero;
+    }
+}
+// the normals the ARC test reads, computed right before it (src/main.cpp:169-175, :351-357)
+void normalsForBC(Orc& o) {
+    if (o.P.freeSurfType != 2) return;
+    calcNormalParticles(o);
+    if (o.P.wallType == 1) calcWallNormalParticles(o);
+}
+// MpsBoundaryCondition::updateParticleBC, src/MpsBoundaryCondition.cpp:66-400: types 0
+// (PND + neighbours), 1 (NPCD) and 2 (ARC: inner when PND, neighbour count and normal allow
+// it, else by the first neighbour in scan order, real or (polygon) mirrored, whose position
+// relative to the normal satisfies the distance / angle tests; surface when some neighbour
+// was tested and none passed)
 void updateParticleBC(Orc& o) {
     const MpsParams& P = o.P;
+#pragma omp parallel for schedule(dynamic, 64)
     for (int i = 0; i < o.N; i++) {
         if (o.type[i] == P.dummyWall) { o.bc[i] = P.other; continue; }
         o.bc[i] = (o.pndSmall[i] < P.betaPnd) ? P.surface : P.inner;
@@ -1150,6 +1212,56 @@ void updateParticleBC(Orc& o) {
             else o.bc[i] = P.inner;
         } else if (P.freeSurfType == 1) {
             if (o.bc[i] == P.surface && o.numNeigh[i] > 4 && o.npcd2[i] < P.delta2) o.bc[i] = P.inner;
+        } else if (P.freeSurfType == 2) {
+            double n[3] = {o.normal[i * 3], o.normal[i * 3 + 1], o.normal[i * 3 + 2]};
+            double norm2 = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+            if (o.pndi[i] >= P.betaPnd && o.numNeigh[i] >= P.betaNeigh && norm2 <= P.normThreshold2) {
+                o.bc[i] = P.inner;
+                continue;
+            }
+            const double* xi = &o.pos[i * 3];
+            const double* mi = &o.mirror[i * 3];
+            if (norm2 > P.epsilonZero) { double nn = std::sqrt(norm2); n[0] /= nn; n[1] /= nn; n[2] /= nn; }
+            else n[0] = n[1] = n[2] = 0.0;
+            Refl r = reflMod2(xi, mi, P.epsilonZero);
+            double nm[3];
+            for (int a = 0; a < 3; a++) nm[a] = r.R[a * 3] * n[0] + r.R[a * 3 + 1] * n[1] + r.R[a * 3 + 2] * n[2];
+            double nm2 = nm[0] * nm[0] + nm[1] * nm[1] + nm[2] * nm[2];
+            if (nm2 > P.epsilonZero) { double q = std::sqrt(nm2); nm[0] /= q; nm[1] /= q; nm[2] /= q; }
+            else nm[0] = nm[1] = nm[2] = 0.0;
+            bool done = false;
+            int bcv = o.bc[i];
+            forCandidates(o, xi[0], xi[1], xi[2], [&](int j) {
+                if (done) return;
+                Pair q = pairOf(o, j, xi, mi);
+                if (q.d2 < P.reS2 && sideOK(o, q) && j != i) {
+                    const double* pj = &o.pos[j * 3];
+                    double c0 = pj[0] - (xi[0] + P.partDist * n[0]);
+                    double c1 = pj[1] - (xi[1] + P.partDist * n[1]);
+                    double c2 = pj[2] - (xi[2] + P.partDist * n[2]);
+                    double dinj2 = c0 * c0 + c1 * c1 + c2 * c2;
+                    double rijn = q.v0 * n[0] + q.v1 * n[1] + q.v2 * n[2];
+                    double ang = std::acos(rijn / std::sqrt(q.d2));
+                    if ((q.d2 >= P.dstThreshold2 && dinj2 < P.hThreshold2) || (q.d2 < P.dstThreshold2 && ang < P.thetaArc)) {
+                        bcv = P.inner; done = true; return;
+                    }
+                    bcv = P.surface;
+                }
+                if (P.wallType == 1 && q.d2 < P.reS2 && q.dm2 < P.reS2 && q.d2 < q.dm2 && j != i) {
+                    const double* pj = &o.pos[j * 3];
+                    double c0 = pj[0] - (mi[0] + P.partDist * nm[0]);
+                    double c1 = pj[1] - (mi[1] + P.partDist * nm[1]);
+                    double c2 = pj[2] - (mi[2] + P.partDist * nm[2]);
+                    double dimnj2 = c0 * c0 + c1 * c1 + c2 * c2;
+                    double rimjn = q.m0 * nm[0] + q.m1 * nm[1] + q.m2 * nm[2];
+                    double angm = std::acos(rimjn / std::sqrt(q.dm2));
+                    if ((q.dm2 >= P.dstThreshold2 && dimnj2 < P.hThreshold2) || (q.dm2 < P.dstThreshold2 && angm < P.thetaArc)) {
+                        bcv = P.inner; done = true; return;
+                    }
+                    bcv = P.surface;
+                }
+            });
+            o.bc[i] = bcv;
         }
     }
 }
@@ -1707,7 +1819,7 @@ int runOp(Orc& o, int op) {
             if (P.wallType == 1) meanWallPnd(o);
             meanPnd(o);
             return 0;
-        case MPS_OP_UPDATE_BC: updateParticleBC(o); return 0;
+        case MPS_OP_UPDATE_BC: normalsForBC(o); updateParticleBC(o); return 0;
         case MPS_OP_CALC_PRESS: calcPress(o); return o.sizeMismatch ? MPSGPU_ERR_SIZE_MISMATCH : 0;
         case MPS_OP_EXTRAPOLATE_PRESS: extrapolatePress(o); return 0;
         case MPS_OP_PRESS_GRADIENT: pressGradient(o); return 0;
@@ -1738,6 +1850,7 @@ int initialize(Orc& o) {
     if (P.wallType == 1) { wallDistance(o); calcWallNPCD(o); }
     if (P.mpsType == 2 || P.mpsType == 3) o.pressurePPE.assign(o.N, 0.0);
     runOp(o, MPS_OP_INIT_PND);
+    normalsForBC(o);
     updateParticleBC(o);
     calcPress(o);
     return 0;
@@ -1760,6 +1873,7 @@ int step(Orc& o) {
     calcPndnNeighNPCD(o);
     if (P.pndType == 2) runOp(o, MPS_OP_PND_DIFFUSIVE);
     else if (P.pndType == 1) runOp(o, MPS_OP_PND_MEAN);
+    normalsForBC(o);
     updateParticleBC(o);
     calcPress(o);
     if (P.wallType == 0) extrapolatePress(o);
@@ -1794,6 +1908,7 @@ FieldRef fieldRef(Orc& o, int f) {
         case MPS_F_WALLPOS: return {KV, o.wallPos.data()};
         case MPS_F_POLYNORMAL: return {KV, o.polyNormal.data()};
         case MPS_F_FORCEWALL: return {KV, o.forceWall.data()};
+        case MPS_F_NORMAL: return {KV, o.normal.data()};
         case MPS_F_PRESS: return {KS, o.press.data()};
         case MPS_F_PRESSPPE: return {KS, o.pressurePPE.data()};
         case MPS_F_PNDI: return {KS, o.pndi.data()};
@@ -1841,7 +1956,7 @@ int orc_create(const MpsParams* p, int n, const int* type, const double* pos3, c
     // Newtonian: RHO = DNS_FL1, PTYPE = 1, MEU = KNM_VS1*DNS_FL1 (src/MpsInputOutput.cpp:833-838)
     S(o->RHO, p->DNS_FL1); S(o->MEU, p->KNM_VS1 * p->DNS_FL1);
     V(o->pos); V(o->vel); V(o->acc); V(o->accStar); V(o->npcd); V(o->gradC); V(o->c1); V(o->c2); V(o->c3);
-    V(o->dvel); V(o->wallPos); V(o->mirror); V(o->polyNormal); V(o->forceWall);
+    V(o->dvel); V(o->wallPos); V(o->mirror); V(o->polyNormal); V(o->forceWall); V(o->normal);
     std::memcpy(o->pos.data(), pos3, sizeof(double) * n * 3);
     if (vel3) std::memcpy(o->vel.data(), vel3, sizeof(double) * n * 3);
     if (press) std::memcpy(o->press.data(), press, sizeof(double) * n);

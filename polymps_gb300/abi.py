@@ -99,21 +99,21 @@ STATIC_MAX_ROWS = 1 << 17
 
 # fields (enum MpsField)
 F_POS, F_VEL, F_ACC, F_ACCSTAR, F_NPCD, F_GRADC, F_CORR1, F_CORR2, F_CORR3, F_MIRROR, \
-    F_WALLPOS, F_POLYNORMAL, F_FORCEWALL = range(13)
+    F_WALLPOS, F_POLYNORMAL, F_FORCEWALL, F_NORMAL = range(14)
 (F_PRESS, F_PRESSPPE, F_PNDI, F_PNDKI, F_PNDSKI, F_PNDSMALL, F_NPCD2, F_CONC, F_VELDIV,
  F_DIFFTERM, F_PNDWALL, F_RIW2, F_DEVDOT, F_SOURCE) = range(32, 46)
 F_TYPE, F_BC, F_NUMNEIGH, F_NNEIGHWALL, F_NEARWALL = range(64, 69)
 F_PRESSPPE_PREV = 46   # warm-start state (no reference array; not in SCALAR_FIELDS)
 F_PRESSPPE_PREV2 = 47
 
-VECTOR_FIELDS = set(range(13))
+VECTOR_FIELDS = set(range(14))
 SCALAR_FIELDS = set(range(32, 46))
 INT_FIELDS = set(range(64, 69))
 
 FIELD_NAMES = {
     F_POS: "pos", F_VEL: "vel", F_ACC: "acc", F_ACCSTAR: "accStar", F_NPCD: "npcd",
     F_GRADC: "gradC", F_CORR1: "corr1", F_CORR2: "corr2", F_CORR3: "corr3", F_MIRROR: "mirror",
-    F_WALLPOS: "wallPos", F_POLYNORMAL: "polyNormal", F_FORCEWALL: "forceWall",
+    F_WALLPOS: "wallPos", F_POLYNORMAL: "polyNormal", F_FORCEWALL: "forceWall", F_NORMAL: "normal",
     F_PRESS: "press", F_PRESSPPE: "pressPPE", F_PNDI: "pndi", F_PNDKI: "pndki",
     F_PNDSKI: "pndski", F_PNDSMALL: "pndSmall", F_NPCD2: "npcd2", F_CONC: "conc",
     F_VELDIV: "velDiv", F_DIFFTERM: "diffTerm", F_PNDWALL: "pndWall", F_RIW2: "riw2",

@@ -120,6 +120,7 @@ static int opLaunches(int op, const MpsParams& P, bool x) {
             if (x) return P.shiftingType == 1 ? 6 : (P.shiftingType == 2 ? (P.wallType == 1 ? 11 : 8) : 0);
             return P.shiftingType == 1 ? 4 : (P.shiftingType == 2 ? (P.wallType == 1 ? 8 : 5) : 0);
         case MPS_OP_DUMMY_VELOCITY: return P.wallType == 0 ? 3 : 0;
+        case MPS_OP_UPDATE_BC: return P.freeSurfType == 2 ? (P.wallType == 1 ? 3 : 2) : 1;   // (normals) + flags
         default: return 1;
     }
 }
@@ -209,7 +210,6 @@ static int unsupported(const MpsParams& P) {
     if (P.femOn || P.forcedOn) return 1;
     if (P.domainTypeBC != 0) return 1;
     if (P.fluidType != 0) return 1;
-    if (P.freeSurfType == 2) return 1;
     if (P.collisionType != 0 && P.collisionType != 1) return 1;
     if (P.solverType != 0 && P.solverType != 1) return 1;
     if (P.relaxPress < 1.0) return 1;
@@ -384,7 +384,10 @@ static int runOpBody(mpsgpu_t h, int op) {
         }
         case MPS_OP_PND_DIFFUSIVE: ensureMasks(h); ensureCache(h); launchPndDiffusive(d, s); break;
         case MPS_OP_PND_MEAN: ensureMasks(h); ensureCache(h); launchPndMean(d, s); break;
-        case MPS_OP_UPDATE_BC: launchUpdateBC(d, s); break;
+        case MPS_OP_UPDATE_BC:
+            if (P.freeSurfType == 2) { ensureMasks(h); launchUpdateBCArc(d, s); }
+            else launchUpdateBC(d, s);
+            break;
         case MPS_OP_CALC_PRESS: { int e = calcPress(h); if (e) return e; break; }
         case MPS_OP_EXTRAPOLATE_PRESS: ensureMasks(h); ensureCache(h); launchExtrapolatePress(d, s); break;
         case MPS_OP_PRESS_GRADIENT: ensureMasks(h); if (x) launchPressGradientDF(d, s); else launchPressGradient(d, s); break;
@@ -635,6 +638,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.velLo, n);
     A(d.pressDF, n);
     A(d.concDF, n);
+    A(d.normal, n);
     A(d.posSkin, n);
     A(d.skinCell, n);
     A(d.skinFlag, 2);
@@ -960,6 +964,7 @@ static void* fieldPtr(mpsgpu_t h, int f, int* kind) {
         case MPS_F_WALLPOS: return d.wallPos;
         case MPS_F_POLYNORMAL: return d.polyNormal;
         case MPS_F_FORCEWALL: return d.forceWall;
+        case MPS_F_NORMAL: return d.normal;
         default: break;
     }
     *kind = 1;

@@ -188,7 +188,7 @@ int renumberLaunches() { return 1 + (15 + 17 + 5 + 3) + 1; }
 static void launchRenumber(const Dev& d, int* perm, void* scratch, cudaStream_t s) {
     const int n = d.N0;
     k_perm_build<<<gridFor(n, 256), 256, 0, s>>>(d, perm);
-    for (dvec4* v : {d.pos, d.vel, d.acc, d.accStar, d.mirror, d.wallPos, d.polyNormal, d.npcd, d.gradC,
+    for (dvec4* v : {d.pos, d.vel, d.acc, d.accStar, d.mirror, d.wallPos, d.polyNormal, d.normal, d.npcd, d.gradC,
                      d.forceWall, d.c1, d.c2, d.c3, d.dvel, d.shift})
         permute(v, perm, scratch, n, s);
     for (double* v : {d.press, d.pressPPE, d.pressPPEprev, d.pressPPEprev2, d.pndi, d.pndki, d.pndski, d.pndSmall, d.npcd2, d.conc,

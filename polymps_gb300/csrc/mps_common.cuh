@@ -71,6 +71,7 @@ struct Dev {
     float2* corrDFn;                // correction-matrix operator (pointer swap)
     float2* pressDF;
     float2* concDF;                 // shifting concentration as a float-float pair
+    dvec4* normal;                  // fluid normal of the ARC free-surface test
     // start-of-step neighbour list with a skin (DF32 tier): candidates within reL + skin of
     // the start positions, in scan order; the viscosity sweep reads it, and the list of the
     // predicted positions is filtered from it while every particle stays within half the

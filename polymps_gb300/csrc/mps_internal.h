@@ -79,6 +79,8 @@ void launchPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallViscosityDF(const Dev& d, cudaStream_t s);
 void launchShiftingDF(const Dev& d, cudaStream_t s);
+// ARC free surface (free-surface type 2): fluid normals (+ wall term), then the BC test
+void launchUpdateBCArc(const Dev& d, cudaStream_t s);
 // dynamic particle collision (collision type 1, FP64, list based; moves positions)
 void launchCollisionDPC(const Dev& d, cudaStream_t s);
 // velocity divergence of the PND + div u source (list based, FP64; + the polygon-wall term)

@@ -105,7 +105,7 @@ template <class T> __device__ __forceinline__ void mv(T* a, int i, int L) { a[i]
 template <class T> __device__ __forceinline__ void sw(T* a, int i, int j) { T t = a[i]; a[i] = a[j]; a[j] = t; }
 // every per-particle array that lives across operators: a pure relocation of two slots
 __device__ void swapSlots(const Dev& d, int a, int b) {
-    for (dvec4* v : {d.pos, d.vel, d.acc, d.accStar, d.mirror, d.wallPos, d.polyNormal, d.npcd, d.gradC,
+    for (dvec4* v : {d.pos, d.vel, d.acc, d.accStar, d.mirror, d.wallPos, d.polyNormal, d.normal, d.npcd, d.gradC,
                      d.forceWall, d.c1, d.c2, d.c3, d.dvel, d.shift})
         sw(v, a, b);
     for (double* v : {d.press, d.pressPPE, d.pressPPEprev, d.pressPPEprev2, d.pndi, d.pndki, d.pndski, d.pndSmall, d.npcd2, d.conc,
@@ -704,6 +704,125 @@ __global__ void k_update_bc(Dev d) {
     d.bc[i] = bc;
 }
 void launchUpdateBC(const Dev& d, cudaStream_t s) { k_update_bc<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
+
+// ------------------------------------------------------------------ ARC free surface
+// MpsShifting::calcNormalParticles, src/MpsShifting.cpp:106-166: n_i = -sum r_ij w / |r_ij| / n0
+// over the reS entries off the mirror side
+__global__ void __launch_bounds__(BLK) k_normal(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    const dvec4 pi = d.pos[i];
+    double nx = 0, ny = 0, nz = 0;
+    forMask(d, i, d.maskS[i], [&](int j, size_t) {
+        PairG q = pairOf(d.pos[j], pi);
+        double dst = sqrt(q.d2);
+        double wS = wfun(dst, P.reS, P.weightType);
+        nx += q.v0 * wS / dst; ny += q.v1 * wS / dst; nz += q.v2 * wS / dst;
+    });
+    d.normal[i] = make_dvec4(-nx / P.pndSmallZero, -ny / P.pndSmallZero, -nz / P.pndSmallZero, 0.0);
+}
+// calcWallNormalParticles, src/MpsShifting.cpp:319-420: mirror entries of the near-wall fluid
+// and i as a neighbour of its mirror, reflected by R
+__global__ void __launch_bounds__(BLK) k_wall_normal(Dev d) {
+    int i = nearIndex(d);
+    if (i < 0) return;
+    const MpsParams& P = d.P;
+    const dvec4 pi = d.pos[i], mi = d.mirror[i];
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
+    double dx = 0, dy = 0, dz = 0;
+    forNbrs(d, i, [&](int j) {
+        dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (q.d2 < P.reS2) {
+            PairM m = pairMirror(pj, mi);
+            if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
+                double dst = sqrt(m.dm2);
+                double wS = wfun(dst, P.reS, P.weightType);
+                dx += m.m0 * wS / dst; dy += m.m1 * wS / dst; dz += m.m2 * wS / dst;
+            }
+        }
+    });
+    PairM s = pairMirror(pi, mi);
+    if (s.dm2 < P.reS2) {
+        double dst = sqrt(s.dm2);
+        double wS = wfun(dst, P.reS, P.weightType);
+        dx += s.m0 * wS / dst; dy += s.m1 * wS / dst; dz += s.m2 * wS / dst;
+    }
+    dvec4 n = d.normal[i];
+    n.x += -(r.R[0] * dx + r.R[1] * dy + r.R[2] * dz) / P.pndSmallZero;
+    n.y += -(r.R[3] * dx + r.R[4] * dy + r.R[5] * dz) / P.pndSmallZero;
+    n.z += -(r.R[6] * dx + r.R[7] * dy + r.R[8] * dz) / P.pndSmallZero;
+    d.normal[i] = n;
+}
+// MpsBoundaryCondition::updateParticleBC type 2 (ARC), src/MpsBoundaryCondition.cpp:205-395:
+// inner when PND, neighbour count and normal allow it; otherwise the list entries in scan
+// order (the reference's bucket scan order) decide: the first real or (polygon) mirrored
+// neighbour that passes the distance / angle test makes the particle inner, a tested one
+// that fails makes it surface (until a later one passes); untested: the PND flag stays.
+__global__ void __launch_bounds__(BLK) k_update_bc_arc(Dev d) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    if (d.type[i] == P.dummyWall) { d.bc[i] = P.other; return; }
+    int bc = (d.pndSmall[i] < P.betaPnd) ? P.surface : P.inner;
+    dvec4 nv = d.normal[i];
+    double n[3] = {nv.x, nv.y, nv.z};
+    double norm2 = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+    if (d.pndi[i] >= P.betaPnd && d.numNeigh[i] >= P.betaNeigh && norm2 <= P.normThreshold2) {
+        d.bc[i] = P.inner;
+        return;
+    }
+    const dvec4 pi = d.pos[i], mi = d.mirror[i];
+    if (norm2 > P.epsilonZero) { double q = sqrt(norm2); n[0] /= q; n[1] /= q; n[2] /= q; }
+    else n[0] = n[1] = n[2] = 0.0;
+    ReflG r = makeRefl(pi, mi, P.epsilonZero, false);
+    double nm[3];
+    for (int a = 0; a < 3; a++) nm[a] = r.R[a * 3] * n[0] + r.R[a * 3 + 1] * n[1] + r.R[a * 3 + 2] * n[2];
+    double nm2 = nm[0] * nm[0] + nm[1] * nm[1] + nm[2] * nm[2];
+    if (nm2 > P.epsilonZero) { double q = sqrt(nm2); nm[0] /= q; nm[1] /= q; nm[2] /= q; }
+    else nm[0] = nm[1] = nm[2] = 0.0;
+    const double ax = pi.x + P.partDist * n[0], ay = pi.y + P.partDist * n[1], az = pi.z + P.partDist * n[2];
+    const double bx = mi.x + P.partDist * nm[0], by = mi.y + P.partDist * nm[1], bz = mi.z + P.partDist * nm[2];
+    SideCtx sc = sideCtx(d, i, pi);
+    const int c = d.nbrCount[i];
+    const int* row = d.nbr + i;
+    for (int k = 0; k < c; k++) {
+        const int j = ldStream(row + (size_t)k * d.N0);
+        const dvec4 pj = d.pos[j];
+        PairG q = pairOf(pj, pi);
+        if (!(q.d2 < P.reS2)) continue;
+        if (sideOK(sc, pj, q.d2)) {
+            double c0 = pj.x - ax, c1 = pj.y - ay, c2 = pj.z - az;
+            double dinj2 = c0 * c0 + c1 * c1 + c2 * c2;
+            double ang = acos((q.v0 * n[0] + q.v1 * n[1] + q.v2 * n[2]) / sqrt(q.d2));
+            if ((q.d2 >= P.dstThreshold2 && dinj2 < P.hThreshold2) || (q.d2 < P.dstThreshold2 && ang < P.thetaArc)) {
+                bc = P.inner;
+                break;
+            }
+            bc = P.surface;
+        }
+        if (P.wallType == 1) {
+            PairM m = pairMirror(pj, mi);
+            if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
+                double c0 = pj.x - bx, c1 = pj.y - by, c2 = pj.z - bz;
+                double dimnj2 = c0 * c0 + c1 * c1 + c2 * c2;
+                double angm = acos((m.m0 * nm[0] + m.m1 * nm[1] + m.m2 * nm[2]) / sqrt(m.dm2));
+                if ((m.dm2 >= P.dstThreshold2 && dimnj2 < P.hThreshold2) || (m.dm2 < P.dstThreshold2 && angm < P.thetaArc)) {
+                    bc = P.inner;
+                    break;
+                }
+                bc = P.surface;
+            }
+        }
+    }
+    d.bc[i] = bc;
+}
+void launchUpdateBCArc(const Dev& d, cudaStream_t s) {
+    k_normal<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    if (d.P.wallType == 1) k_wall_normal<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+    k_update_bc_arc<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
 
 // ------------------------------------------------------------------ EOS
 // MpsPressure::calcPressEMPS / calcPressWCMPS, src/MpsPressure.cpp:62-163

@@ -439,8 +439,34 @@ def cpu_baseline(case, steps):
         o.step()
     dt = time.perf_counter() - t0
     o.close()
-    return {"value": round(case.n * steps / dt, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
-            "sample": "%d step(s) of the %d-particle workload after initialisation (%.1f s)" % (steps, case.n, dt)}
+    out = {"value": round(case.n * steps / dt, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
+           "sample": "%d step(s) of the %d-particle workload after initialisation (%.1f s)" % (steps, case.n, dt)}
+    # the same sample on one host thread
+    o = oracle.Oracle(case, threads=1)
+    o.set_solver(1e-8)
+    o.initialize()
+    t0 = time.perf_counter()
+    o.step()
+    d1 = time.perf_counter() - t0
+    o.close()
+    out["single_thread"] = {"value": round(case.n / d1, 1), "cores": 1,
+                            "sample": "1 step of the %d-particle workload (%.1f s)" % (case.n, d1)}
+    # the 2D particle-wall dam break (1,922 particles) run to its configured 200 steps
+    from polymps_gb300 import cases
+    c1 = cases.config(1)
+    full = {}
+    for th in (cores, 1):
+        o = oracle.Oracle(c1, threads=th)
+        o.set_solver(1e-8)
+        o.initialize()
+        t0 = time.perf_counter()
+        for _ in range(c1.steps):
+            o.step()
+        d = time.perf_counter() - t0
+        o.close()
+        full["threads_%d" % th] = {"s": round(d, 3), "value": round(c1.n * c1.steps / d, 1)}
+    out["full_run_2d_particle_walls"] = {"particles": c1.n, "steps": c1.steps, **full}
+    return out
 
 
 def run_reference(a, rank, world):

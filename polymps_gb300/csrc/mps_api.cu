@@ -779,7 +779,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         B.pgridCg = ppePersistentGrid(0);
         B.pgridMx = ppePersistentGrid(1);
         A(B.scal, 32);
-            A(B.partials, 4 * std::max(std::max(std::max(B.nblocks, ppePersistentGrid(4)), ppePersistentGrid(3)),
+            A(B.partials, 8 * std::max(std::max(std::max(B.nblocks, ppePersistentGrid(4)), ppePersistentGrid(3)),
                                    std::max(std::max(B.pgridCg, std::max(ppePersistentGrid(5), ppePersistentGrid(6))),
                                             std::max(B.pgridMx, ppePersistentGrid(2)))));
         A(B.counter, 1);

@@ -481,16 +481,27 @@ int ppeSolveMixed(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cu
 // no per-iteration launches.  Each CG iteration is two grid-wide reductions in the form
 //   Ap = A z + beta Ap,  p = z + beta p            (one SpMV, on z: A p follows by linearity)
 //   x += alpha p, r -= alpha Ap, z = M^-1 r
-// so the only vector every block gathers (z) is complete at the reduction before it.  The
-// reductions are deterministic: per-block partials, the last block to arrive sums them in
-// block order, writes the scalars and releases the others.  Waits are bounded: a block that
-// waits longer than QSPIN polls sets the abort word and every block returns.
+// so the only vector every block gathers (z) is complete at the reduction before it.
+// A reduction is one barrier: every block stores its partial sums, adds one to the
+// arrival counter (release) and waits until the counter reaches the generation's target
+// (acquire); then every block sums all partials in block order and derives the solver's
+// scalars itself.  Identical inputs in identical order give every block identical
+// scalars, so no block has to publish them and release the others (that serial tail cost
+// ~12 us of the ~16 us a reduction took at 608 blocks).  The scalars and flags live in
+// shared memory per block; block 0 stores its copy for the host at the end.  Waits are
+// bounded: a block that waits longer than QSPIN polls sets the abort word and every
+// block returns.
+// Block sizes: one block per SM (1024 threads for the mixed solvers at <= 64 registers,
+// 768 for the FP64 solvers at <= 80), so a reduction reads 152 partials per value
+// instead of 608 (every block reads them all: measured 12 -> 7 us per reduction); the
+// staged-tile operator keeps 256-thread blocks (its tiles are one row per thread).
 #define QB 256
+#define QBX 1024
+#define QBC 768
 #define QSPIN (1 << 21)
-// barrier words, each on its own 128-byte line (the pollers of the generation word must
-// not contend with the arrival atomics): arrivals, generation, abort
+// barrier words, each on its own 128-byte line (the arrival counter is 64-bit and only
+// grows within a launch; it is zeroed before each launch): arrivals, unused, abort
 #define QB_ARR 0
-#define QB_GEN 32
 #define QB_ABT 64
 #define QB_WORDS 96
 
@@ -500,36 +511,43 @@ __device__ __forceinline__ int vi(const int* p) { return *(volatile const int*)p
 struct QCtl {
     unsigned int gen;
 };
-
-// Release/wait half of the grid barrier (thread 0 of each block), after the block's partials
-// are written.  The last block to arrive runs fin() with the whole block first.
-template <class Fin>
-__device__ __forceinline__ bool qArrive(const PpeBuffers& B, QCtl& c, Fin fin) {
-    __shared__ int sLast, sOk;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        unsigned int a = atomicAdd(B.bar + QB_ARR, 1u) + 1u;
-        sLast = (a == gridDim.x);
+// block-local solver scalars and flags
+struct QLocal {
+    double scal[32];
+    int flag[8];
+};
+__device__ __forceinline__ void qInit(QLocal& L) {
+    for (int t = threadIdx.x; t < 32; t += blockDim.x) L.scal[t] = 0.0;
+    for (int t = threadIdx.x; t < 8; t += blockDim.x) L.flag[t] = 0;
+    __syncthreads();
+}
+// block 0's scalars and flags to the global words the host reads
+__device__ __forceinline__ void qStore(const PpeBuffers& B, const QLocal& L) {
+    __syncthreads();
+    if (blockIdx.x == 0) {
+        for (int t = threadIdx.x; t < 32; t += blockDim.x) B.scal[t] = L.scal[t];
+        for (int t = threadIdx.x; t < 8; t += blockDim.x) B.flag[t] = L.flag[t];
     }
+}
+
+// Grid barrier: all writes of the block before it are visible to every block after it.
+__device__ __forceinline__ bool qBarrier(const PpeBuffers& B, QCtl& c) {
+    __shared__ int sOk;
     __syncthreads();
     c.gen++;
-    if (sLast) {
-        __threadfence();
-        fin();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            B.bar[QB_ARR] = 0u;
-            __threadfence();
-            atomicExch(B.bar + QB_GEN, c.gen);
-            sOk = *(volatile unsigned int*)(B.bar + QB_ABT) == 0u;
-        }
-    } else if (threadIdx.x == 0) {
+    if (threadIdx.x == 0) {
+        unsigned long long* cnt = reinterpret_cast<unsigned long long*>(B.bar + QB_ARR);
+        const unsigned long long target = (unsigned long long)c.gen * gridDim.x;
+        asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(cnt) : "memory");
         int ok = 1;
         long long spins = 0;
-        while (*(volatile unsigned int*)(B.bar + QB_GEN) < c.gen) {
+        while (true) {
+            unsigned long long v;
+            asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(cnt) : "memory");
+            if (v >= target) break;
             if (++spins > QSPIN) { atomicExch(B.bar + QB_ABT, 1u); ok = 0; break; }
             if ((spins & 15) == 0 && *(volatile unsigned int*)(B.bar + QB_ABT)) { ok = 0; break; }
-            __nanosleep(100);
+            if (spins > 4) __nanosleep(32);
         }
         __threadfence();
         if (ok && *(volatile unsigned int*)(B.bar + QB_ABT)) ok = 0;
@@ -538,30 +556,33 @@ __device__ __forceinline__ bool qArrive(const PpeBuffers& B, QCtl& c, Fin fin) {
     __syncthreads();
     return sOk;
 }
-__device__ __forceinline__ bool qBarrier(const PpeBuffers& B, QCtl& c) {
-    __syncthreads();
-    return qArrive(B, c, [] {});
-}
-// Grid sum of NV FP64 values per thread; fin(tot) runs on thread 0 of the last block.
+// Grid sum of NV (<= 4) FP64 values per thread; fin(tot) runs on thread 0 of every block
+// with the same totals, and its writes to the block-local scalars are visible to the
+// block's threads on return.  The partials of consecutive reductions alternate between
+// two buffers: a block can be at most one reduction ahead of the slowest block's reads.
 template <int NV, class Fin>
 __device__ __forceinline__ bool qSum(double (&v)[NV], const PpeBuffers& B, QCtl& c, Fin fin) {
     __shared__ double sm[NV * 32];
     blockSum<NV>(v, sm);
+    double* part = B.partials + (size_t)(c.gen & 1u) * 4u * gridDim.x;
     if (threadIdx.x == 0)
 #pragma unroll
-        for (int q = 0; q < NV; q++) B.partials[q * gridDim.x + blockIdx.x] = v[q];
-    return qArrive(B, c, [&] {
+        for (int q = 0; q < NV; q++) part[q * gridDim.x + blockIdx.x] = v[q];
+    if (!qBarrier(B, c)) return false;
+    if (threadIdx.x < 32) {   // warp 0: lane-strided partial sums, then a fixed shuffle tree
         double acc[NV];
 #pragma unroll
         for (int q = 0; q < NV; q++) {
             double s = 0.0;
-            for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-                s += ((volatile double*)B.partials)[q * gridDim.x + b];
+            for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) s += ((volatile double*)part)[q * gridDim.x + b];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             acc[q] = s;
         }
-        blockSum<NV>(acc, sm);
         if (threadIdx.x == 0) fin(acc);
-    });
+    }
+    __syncthreads();
+    return true;
 }
 // The same with float-float per-thread partials (FP32 vectors): the warp reduces in
 // float-float, each warp's total is converted to FP64 once, the rest of the sum is FP64.
@@ -707,7 +728,7 @@ __device__ __forceinline__ float h16Row(const PpeBuffers& B, const float* y, int
 // TS_CH slices into a TS_NS-stage ring, up to TS_NS - 1 chunks ahead of the threads, which
 // read their row's entries from shared memory and gather z.  The engine keeps the HBM
 // stream in flight independently of the threads' gather latencies.  Every mbarrier wait
-// is bounded; a wait that runs out sets the abort word (see qArrive) and the block stops
+// is bounded; a wait that runs out sets the abort word (see qBarrier) and the block stops
 // consuming, drains the copies it issued (again bounded) and returns at the next barrier.
 #define TS_CH 8
 #define TS_NS 3
@@ -846,15 +867,20 @@ __device__ __forceinline__ bool tsSpmv(TsSmem& sm, const PpeBuffers& B, const fl
 // the matrix-free FP32 operator with Jacobi preconditioning, or the compact scaled operator.
 enum { OP_ELL32 = 0, OP_MATFREE = 1, OP_H16 = 2, OP_TILED = 3 };
 template <int OP>
-__global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
+__global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solve(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
+    __shared__ QLocal qL;   // this block's copy of the solver scalars and flags
+    qInit(qL);
+    double* const qS = qL.scal;
+    int* const qF = qL.flag;
     extern __shared__ __align__(128) unsigned char dynSmem[];
     const int n = liveN(d);
     const float cP = (float)d.P.coeffPPE, re = (float)d.P.reL, invRe = (float)(1.0 / d.P.reL);
     const int wt = d.P.weightType;
     // grid-stride rows: at any moment the blocks work on one contiguous window of rows,
     // so the column slices of the ELL arrays stream through DRAM pages in order
-    const int T = gridDim.x * QB;
-    const int t0 = blockIdx.x * QB + threadIdx.x;
+    constexpr int BS = (OP == OP_TILED) ? QB : QBX;
+    const int T = gridDim.x * BS;
+    const int t0 = blockIdx.x * BS + threadIdx.x;
     const int r1 = n;
     QCtl c = {0u};
     // staged tiles: the block's tile lengths and the mbarriers of the ring
@@ -914,27 +940,27 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
             v[1] += B.b[i] * B.b[i];
         });
         if (!qSum<2>(v, B, c, [&](const double* t) {
-                B.scal[S_RR] = t[0];
-                B.scal[S_BB] = t[1];
+                qS[S_RR] = t[0];
+                qS[S_BB] = t[1];
                 double thr = tol * tol * t[1];
                 if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
-                B.scal[S_THR] = thr;
-                B.scal[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
-                B.scal[S_SQRT] = sqrt(t[0]);
-                B.scal[S_INV] = 1.0 / sqrt(t[0]);
-                B.scal[S_ETA2] = fmax(eta2, 0.25 * thr / t[0]);
-                B.flag[0] = (t[1] == 0.0 || t[0] < thr) ? 1 : 0;
-                B.flag[1] = 0;
-                B.flag[3] = 0;
-                if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
+                qS[S_THR] = thr;
+                qS[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
+                qS[S_SQRT] = sqrt(t[0]);
+                qS[S_INV] = 1.0 / sqrt(t[0]);
+                qS[S_ETA2] = fmax(eta2, 0.25 * thr / t[0]);
+                qF[0] = (t[1] == 0.0 || t[0] < thr) ? 1 : 0;
+                qF[1] = 0;
+                qF[3] = 0;
+                if (!(t[0] == t[0])) { qF[0] = 1; qF[2] = 1; }
             }))
             return;
     }
     int total = 0, refine = 0;
-    while (!vi(B.flag) && total < maxIter && refine <= 20) {
+    while (!vi(qF) && total < maxIter && refine <= 20) {
         // inner start: rf = r / ||r|| (compact operator: sigma s r / ||r||), z = M^-1 rf, x_f = 0
         {
-            const double inv = vd(B.scal + S_INV);
+            const double inv = vd(qS + S_INV);
             df a[2] = {dfF(0.f), dfF(0.f)};
             for (int i = t0; i < r1; i += T) {
                 float r = (float)(B.r[i] * inv);
@@ -944,13 +970,13 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                 a[0] += prod2(r, z);
                 a[1] += prod2(r, r);
             }
-            if (!qSumDF<2>(a, B, c, [&](const double* t) { B.scal[S_RZ] = t[0]; B.scal[S_RR0] = t[1]; B.flag[3] = 0; }))
+            if (!qSumDF<2>(a, B, c, [&](const double* t) { qS[S_RZ] = t[0]; qS[S_RR0] = t[1]; qF[3] = 0; }))
                 return;
         }
         int inner = 0;
         while (true) {
             {
-                const float beta = inner ? (float)vd(B.scal + S_BETA) : 0.f;
+                const float beta = inner ? (float)vd(qS + S_BETA) : 0.f;
                 df a[1] = {dfF(0.f)};
                 if (OP == OP_TILED) {
                     bool okp = tsSpmv(sm, B, B.zf, n, mt, gq, [&](int i, float q) {
@@ -971,11 +997,11 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                     B.Apf[i] = ap; B.pf[i] = p;
                     a[0] += prod2(p, ap);
                 });
-                if (!qSumDF<1>(a, B, c, [&](const double* t) { B.scal[S_PAP] = t[0]; B.scal[S_ALPHA] = B.scal[S_RZ] / t[0]; }))
+                if (!qSumDF<1>(a, B, c, [&](const double* t) { qS[S_PAP] = t[0]; qS[S_ALPHA] = qS[S_RZ] / t[0]; }))
                     return;
             }
             {
-                const float alpha = (float)vd(B.scal + S_ALPHA);
+                const float alpha = (float)vd(qS + S_ALPHA);
                 df a[2] = {dfF(0.f), dfF(0.f)};
                 for (int i = t0; i < r1; i += T) {
                     B.xf[i] += alpha * B.pf[i];
@@ -986,19 +1012,19 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                     a[1] += prod2(r, r);
                 }
                 if (!qSumDF<2>(a, B, c, [&](const double* t) {
-                        B.flag[1] += 1;
-                        B.scal[S_BETA] = t[0] / B.scal[S_RZ];
-                        B.scal[S_RZ] = t[0];
-                        if (t[1] < B.scal[S_ETA2] * B.scal[S_RR0] || !(t[1] == t[1])) B.flag[3] = 1;
+                        qF[1] += 1;
+                        qS[S_BETA] = t[0] / qS[S_RZ];
+                        qS[S_RZ] = t[0];
+                        if (t[1] < qS[S_ETA2] * qS[S_RR0] || !(t[1] == t[1])) qF[3] = 1;
                     }))
                     return;
             }
             inner++;
-            if (vi(B.flag + 3) || total + inner >= maxIter || inner >= 400) break;
+            if (vi(qF + 3) || total + inner >= maxIter || inner >= 400) break;
         }
         total += inner;
         {
-            const double sc = vd(B.scal + S_SQRT);
+            const double sc = vd(qS + S_SQRT);
             for (int i = t0; i < r1; i += T)
                 B.x[i] += sc * (double)((OP == OP_H16) ? B.xf[i] * B.sclf[i] : B.xf[i]);
             if (!qBarrier(B, c)) return;
@@ -1011,18 +1037,19 @@ __global__ void __launch_bounds__(QB, 4) k_mx_solve(Dev d, PpeBuffers B, double 
                 v[0] += r * r;
             });
             if (!qSum<1>(v, B, c, [&](const double* t) {
-                    B.scal[S_RR] = t[0];
-                    B.scal[S_SQRT] = sqrt(t[0]);
-                    B.scal[S_INV] = 1.0 / sqrt(t[0]);
-                    B.scal[S_ETA2] = fmax(eta2, 0.25 * B.scal[S_THR] / t[0]);
-                    if (t[0] < B.scal[S_THR]) B.flag[0] = 1;
-                    if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
-                    B.flag[4] += 1;
+                    qS[S_RR] = t[0];
+                    qS[S_SQRT] = sqrt(t[0]);
+                    qS[S_INV] = 1.0 / sqrt(t[0]);
+                    qS[S_ETA2] = fmax(eta2, 0.25 * qS[S_THR] / t[0]);
+                    if (t[0] < qS[S_THR]) qF[0] = 1;
+                    if (!(t[0] == t[0])) { qF[0] = 1; qF[2] = 1; }
+                    qF[4] += 1;
                 }))
                 return;
         }
         refine++;
     }
+    qStore(B, qL);
 }
 
 // FP64 residual row of the refinement without a pass in between: x_j + d_j is formed from
@@ -1061,10 +1088,14 @@ __device__ __forceinline__ double qRowPlus(const PpeBuffers& B, const double* x,
 // buffered (its owner writes m' while neighbours gather m).  The FP64 refinement forms
 // r = b - A (x + d) in the pass that stores x + d into the other FP64 buffer, and starts
 // the next inner solve there (u0 = M r), so a refinement costs two barriers.
-__global__ void __launch_bounds__(QB, 4) k_mx_pipe(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
+__global__ void __launch_bounds__(QBX, 1) k_mx_pipe(Dev d, PpeBuffers B, double tol, int maxIter, double eta2) {
+    __shared__ QLocal qL;   // this block's copy of the solver scalars and flags
+    qInit(qL);
+    double* const qS = qL.scal;
+    int* const qF = qL.flag;
     const int n = liveN(d);
-    const int T = gridDim.x * QB;
-    const int t0 = blockIdx.x * QB + threadIdx.x;
+    const int T = gridDim.x * QBX;
+    const int t0 = blockIdx.x * QBX + threadIdx.x;
     QCtl c = {0u};
     double* xa = B.x;      // current FP64 iterate
     double* xb = B.xalt;   // the next one
@@ -1082,21 +1113,21 @@ __global__ void __launch_bounds__(QB, 4) k_mx_pipe(Dev d, PpeBuffers B, double t
             v[1] += B.b[i] * B.b[i];
         });
         if (!qSum<2>(v, B, c, [&](const double* t) {
-                B.scal[S_RR] = t[0];
-                B.scal[S_BB] = t[1];
+                qS[S_RR] = t[0];
+                qS[S_BB] = t[1];
                 double thr = tol * tol * t[1];
                 if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
-                B.scal[S_THR] = thr;
-                B.scal[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
-                B.scal[S_ETA2] = fmax(eta2, 0.25 * thr / t[0]);
-                B.flag[0] = (t[1] == 0.0 || t[0] < thr) ? 1 : 0;
-                B.flag[1] = 0;
-                if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
+                qS[S_THR] = thr;
+                qS[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
+                qS[S_ETA2] = fmax(eta2, 0.25 * thr / t[0]);
+                qF[0] = (t[1] == 0.0 || t[0] < thr) ? 1 : 0;
+                qF[1] = 0;
+                if (!(t[0] == t[0])) { qF[0] = 1; qF[2] = 1; }
             }))
             return;
     }
     int total = 0, refine = 0;
-    while (!vi(B.flag) && total < maxIter && refine <= 20) {
+    while (!vi(qF) && total < maxIter && refine <= 20) {
         // inner start: w0 = A u0, m0 = M w0; gamma0 = r.u, delta0 = w.u, rho0 = r.r
         {
             df a[3] = {dfF(0.f), dfF(0.f), dfF(0.f)};
@@ -1110,21 +1141,21 @@ __global__ void __launch_bounds__(QB, 4) k_mx_pipe(Dev d, PpeBuffers B, double t
                 a[2] += prod2(r, r);
             });
             if (!qSumDF<3>(a, B, c, [&](const double* t) {
-                    B.flag[3] = 0;
-                    B.scal[S_RZ] = t[0];
-                    B.scal[S_RR0] = t[2];
-                    B.scal[S_BETA] = 0.0;
+                    qF[3] = 0;
+                    qS[S_RZ] = t[0];
+                    qS[S_RR0] = t[2];
+                    qS[S_BETA] = 0.0;
                     // the PPE matrix and its Jacobi preconditioner are negative definite:
                     // r.u and w.u share their sign and alpha > 0
                     const double al = t[0] / t[1];
-                    if (al > 0.0 && al < 1e300) B.scal[S_ALPHA] = al;
-                    else B.flag[3] = 1;   // zero residual or breakdown: nothing to solve
+                    if (al > 0.0 && al < 1e300) qS[S_ALPHA] = al;
+                    else qF[3] = 1;   // zero residual or breakdown: nothing to solve
                 }))
                 return;
         }
         int inner = 0;
-        while (!vi(B.flag + 3) && total + inner < maxIter && inner < 400) {
-            const float alpha = (float)vd(B.scal + S_ALPHA), beta = (float)vd(B.scal + S_BETA);
+        while (!vi(qF + 3) && total + inner < maxIter && inner < 400) {
+            const float alpha = (float)vd(qS + S_ALPHA), beta = (float)vd(qS + S_BETA);
             const float* mc = (inner & 1) ? mA : mB;
             float* mn = (inner & 1) ? mB : mA;
             const bool first = inner == 0;
@@ -1148,15 +1179,15 @@ __global__ void __launch_bounds__(QB, 4) k_mx_pipe(Dev d, PpeBuffers B, double t
                 a[2] += prod2(r, r);
             });
             if (!qSumDF<3>(a, B, c, [&](const double* t) {
-                    B.flag[1] += 1;
-                    if (t[2] < B.scal[S_ETA2] * B.scal[S_RR0] || !(t[2] == t[2])) { B.flag[3] = 1; return; }
-                    const double g0 = B.scal[S_RZ], al = B.scal[S_ALPHA];
+                    qF[1] += 1;
+                    if (t[2] < qS[S_ETA2] * qS[S_RR0] || !(t[2] == t[2])) { qF[3] = 1; return; }
+                    const double g0 = qS[S_RZ], al = qS[S_ALPHA];
                     const double bt = t[0] / g0;
                     const double aln = t[0] / (t[1] - bt * t[0] / al);
-                    if (!(aln > 0.0 && aln < 1e300 && bt >= 0.0)) { B.flag[3] = 1; return; }
-                    B.scal[S_BETA] = bt;
-                    B.scal[S_ALPHA] = aln;
-                    B.scal[S_RZ] = t[0];
+                    if (!(aln > 0.0 && aln < 1e300 && bt >= 0.0)) { qF[3] = 1; return; }
+                    qS[S_BETA] = bt;
+                    qS[S_ALPHA] = aln;
+                    qS[S_RZ] = t[0];
                 }))
                 return;
             inner++;
@@ -1182,11 +1213,11 @@ __global__ void __launch_bounds__(QB, 4) k_mx_pipe(Dev d, PpeBuffers B, double t
                 v[0] += r * r;
             });
             if (!qSum<1>(v, B, c, [&](const double* t) {
-                    B.scal[S_RR] = t[0];
-                    B.scal[S_ETA2] = fmax(eta2, 0.25 * B.scal[S_THR] / t[0]);
-                    if (t[0] < B.scal[S_THR]) B.flag[0] = 1;
-                    if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
-                    B.flag[4] += 1;
+                    qS[S_RR] = t[0];
+                    qS[S_ETA2] = fmax(eta2, 0.25 * qS[S_THR] / t[0]);
+                    if (t[0] < qS[S_THR]) qF[0] = 1;
+                    if (!(t[0] == t[0])) { qF[0] = 1; qF[2] = 1; }
+                    qF[4] += 1;
                 }))
                 return;
             double* tx = xa; xa = xb; xb = tx;
@@ -1195,16 +1226,21 @@ __global__ void __launch_bounds__(QB, 4) k_mx_pipe(Dev d, PpeBuffers B, double t
     }
     if (xa != B.x)
         for (int i = t0; i < n; i += T) B.x[i] = xa[i];
+    qStore(B, qL);
 }
 
 // Plain FP64 Jacobi-PCG (Eigen's ConjugateGradient with its diagonal preconditioner,
 // src/MpsPressure.cpp:424-445): z = invdiag * r, stop when ||r||^2 < tol^2 ||b||^2.
-__global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double tol, int maxIter) {
+__global__ void __launch_bounds__(QBC, 1) k_cg_solve(Dev d, PpeBuffers B, double tol, int maxIter) {
+    __shared__ QLocal qL;   // this block's copy of the solver scalars and flags
+    qInit(qL);
+    double* const qS = qL.scal;
+    int* const qF = qL.flag;
     const int n = liveN(d);
     // grid-stride rows: at any moment the blocks work on one contiguous window of rows,
     // so the column slices of the ELL arrays stream through DRAM pages in order
-    const int T = gridDim.x * QB;
-    const int t0 = blockIdx.x * QB + threadIdx.x;
+    const int T = gridDim.x * QBC;
+    const int t0 = blockIdx.x * QBC + threadIdx.x;
     const int r1 = n;
     QCtl c = {0u};
     {
@@ -1217,21 +1253,21 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
             v[0] += r * z; v[1] += r * r; v[2] += B.b[i] * B.b[i];
         });
         if (!qSum<3>(v, B, c, [&](const double* t) {
-                B.scal[S_RZ] = t[0]; B.scal[S_RR] = t[1]; B.scal[S_BB] = t[2];
+                qS[S_RZ] = t[0]; qS[S_RR] = t[1]; qS[S_BB] = t[2];
                 double thr = tol * tol * t[2];
                 if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
-                B.scal[S_THR] = thr;
-                B.scal[S_SCALE] = sqrt(t[1] / (t[2] > 0 ? t[2] : 1.0));
-                B.flag[0] = (t[2] == 0.0 || t[1] < thr) ? 1 : 0;
-                B.flag[1] = 0;
-                if (!(t[0] == t[0]) || !(t[1] == t[1])) { B.flag[0] = 1; B.flag[2] = 1; }
+                qS[S_THR] = thr;
+                qS[S_SCALE] = sqrt(t[1] / (t[2] > 0 ? t[2] : 1.0));
+                qF[0] = (t[2] == 0.0 || t[1] < thr) ? 1 : 0;
+                qF[1] = 0;
+                if (!(t[0] == t[0]) || !(t[1] == t[1])) { qF[0] = 1; qF[2] = 1; }
             }))
             return;
     }
     int it = 0;
-    while (!vi(B.flag) && it < maxIter) {
+    while (!vi(qF) && it < maxIter) {
         {
-            const double beta = it ? vd(B.scal + S_BETA) : 0.0;
+            const double beta = it ? vd(qS + S_BETA) : 0.0;
             double v[1] = {0.0};
             forRows(B, r1, t0, T, [&](int i, int len) {
                 double q = qRow(B, B.z, i, len);
@@ -1241,11 +1277,11 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
                 B.Ap[i] = ap; B.p[i] = p;
                 v[0] += p * ap;
             });
-            if (!qSum<1>(v, B, c, [&](const double* t) { B.scal[S_PAP] = t[0]; B.scal[S_ALPHA] = B.scal[S_RZ] / t[0]; }))
+            if (!qSum<1>(v, B, c, [&](const double* t) { qS[S_PAP] = t[0]; qS[S_ALPHA] = qS[S_RZ] / t[0]; }))
                 return;
         }
         {
-            const double alpha = vd(B.scal + S_ALPHA);
+            const double alpha = vd(qS + S_ALPHA);
             double v[2] = {0.0, 0.0};
             for (int i = t0; i < r1; i += T) {
                 B.x[i] += alpha * B.p[i];
@@ -1255,12 +1291,12 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
                 v[0] += r * z; v[1] += r * r;
             }
             if (!qSum<2>(v, B, c, [&](const double* t) {
-                    B.flag[1] += 1;
-                    B.scal[S_RR] = t[1];
-                    B.scal[S_BETA] = t[0] / B.scal[S_RZ];
-                    B.scal[S_RZ] = t[0];
-                    if (t[1] < B.scal[S_THR]) B.flag[0] = 1;
-                    if (!(t[1] == t[1])) { B.flag[0] = 1; B.flag[2] = 1; }
+                    qF[1] += 1;
+                    qS[S_RR] = t[1];
+                    qS[S_BETA] = t[0] / qS[S_RZ];
+                    qS[S_RZ] = t[0];
+                    if (t[1] < qS[S_THR]) qF[0] = 1;
+                    if (!(t[1] == t[1])) { qF[0] = 1; qF[2] = 1; }
                 }))
                 return;
         }
@@ -1273,8 +1309,9 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
             double r = B.b[i] - qRow(B, B.x, i, len);
             v[0] += r * r;
         });
-        qSum<1>(v, B, c, [&](const double* t) { B.scal[S_RR] = t[0]; });
+        qSum<1>(v, B, c, [&](const double* t) { qS[S_RR] = t[0]; });
     }
+    qStore(B, qL);
 }
 
 // Jacobi-preconditioned BiCGSTAB (solver_type 1: Eigen::BiCGSTAB, src/MpsPressure.cpp:448-468;
@@ -1284,10 +1321,14 @@ __global__ void __launch_bounds__(QB, 3) k_cg_solve(Dev d, PpeBuffers B, double 
 // is restarted when (r0, r) vanishes relative to its start, the stopping rule is
 // ||r||^2 < tol^2 ||b||^2 on the recurrence residual, and the FP64 residual of the result is
 // reported.
-__global__ void __launch_bounds__(QB, 3) k_bicgstab(Dev d, PpeBuffers B, double tol, int maxIter) {
+__global__ void __launch_bounds__(QBC, 1) k_bicgstab(Dev d, PpeBuffers B, double tol, int maxIter) {
+    __shared__ QLocal qL;   // this block's copy of the solver scalars and flags
+    qInit(qL);
+    double* const qS = qL.scal;
+    int* const qF = qL.flag;
     const int n = liveN(d);
-    const int T = gridDim.x * QB;
-    const int t0 = blockIdx.x * QB + threadIdx.x;
+    const int T = gridDim.x * QBC;
+    const int t0 = blockIdx.x * QBC + threadIdx.x;
     const int r1 = n;
     QCtl c = {0u};
     double *r0 = B.bs[0], *sv = B.bs[1], *zz = B.bs[2], *tv = B.bs[3], *y = B.z, *v = B.Ap;
@@ -1302,27 +1343,27 @@ __global__ void __launch_bounds__(QB, 3) k_bicgstab(Dev d, PpeBuffers B, double 
         });
         return qSum<2>(a, B, c, [&](const double* t) {
             if (first) {
-                B.scal[S_BB] = t[1];
+                qS[S_BB] = t[1];
                 double thr = tol * tol * t[1];
                 if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
-                B.scal[S_THR] = thr;
-                B.scal[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
-                B.flag[1] = 0;
-                if (t[1] == 0.0) B.flag[0] = 1;
+                qS[S_THR] = thr;
+                qS[S_SCALE] = sqrt(t[0] / (t[1] > 0 ? t[1] : 1.0));
+                qF[1] = 0;
+                if (t[1] == 0.0) qF[0] = 1;
             }
-            B.scal[S_RR] = B.scal[S_RHO] = B.scal[S_R0N2] = t[0];
-            B.scal[S_RHOOLD] = B.scal[S_ALPHA] = B.scal[S_OMEGA] = 1.0;
-            B.flag[5] = 0;
-            if (t[0] < B.scal[S_THR]) B.flag[0] = 1;
-            if (!(t[0] == t[0])) { B.flag[0] = 1; B.flag[2] = 1; }
+            qS[S_RR] = qS[S_RHO] = qS[S_R0N2] = t[0];
+            qS[S_RHOOLD] = qS[S_ALPHA] = qS[S_OMEGA] = 1.0;
+            qF[5] = 0;
+            if (t[0] < qS[S_THR]) qF[0] = 1;
+            if (!(t[0] == t[0])) { qF[0] = 1; qF[2] = 1; }
         });
     };
     if (!restart(true)) return;
     int it = 0;
-    while (!vi(B.flag) && it < maxIter) {
+    while (!vi(qF) && it < maxIter) {
         {   // p = r + beta (p - w v), y = M^-1 p
-            const double rho = vd(B.scal + S_RHO), w = vd(B.scal + S_OMEGA);
-            const double beta = (rho / vd(B.scal + S_RHOOLD)) * (vd(B.scal + S_ALPHA) / w);
+            const double rho = vd(qS + S_RHO), w = vd(qS + S_OMEGA);
+            const double beta = (rho / vd(qS + S_RHOOLD)) * (vd(qS + S_ALPHA) / w);
             for (int i = t0; i < r1; i += T) {
                 double p = B.r[i] + beta * (B.p[i] - w * v[i]);
                 B.p[i] = p;
@@ -1338,15 +1379,15 @@ __global__ void __launch_bounds__(QB, 3) k_bicgstab(Dev d, PpeBuffers B, double 
                 a[0] += r0[i] * q;
             });
             if (!qSum<1>(a, B, c, [&](const double* t) {
-                    double al = B.scal[S_RHO] / t[0];
-                    B.scal[S_ALPHA] = al;
-                    if (!(al == al) || t[0] == 0.0) { B.flag[0] = 1; B.flag[2] = 1; }
+                    double al = qS[S_RHO] / t[0];
+                    qS[S_ALPHA] = al;
+                    if (!(al == al) || t[0] == 0.0) { qF[0] = 1; qF[2] = 1; }
                 }))
                 return;
         }
-        if (vi(B.flag)) break;
+        if (vi(qF)) break;
         {   // s = r - alpha v, z = M^-1 s
-            const double alpha = vd(B.scal + S_ALPHA);
+            const double alpha = vd(qS + S_ALPHA);
             for (int i = t0; i < r1; i += T) {
                 double s = B.r[i] - alpha * v[i];
                 sv[i] = s;
@@ -1362,11 +1403,11 @@ __global__ void __launch_bounds__(QB, 3) k_bicgstab(Dev d, PpeBuffers B, double 
                 a[0] += q * q;
                 a[1] += q * sv[i];
             });
-            if (!qSum<2>(a, B, c, [&](const double* t) { B.scal[S_OMEGA] = (t[0] > 0.0) ? t[1] / t[0] : 0.0; }))
+            if (!qSum<2>(a, B, c, [&](const double* t) { qS[S_OMEGA] = (t[0] > 0.0) ? t[1] / t[0] : 0.0; }))
                 return;
         }
         {   // x += alpha y + w z, r = s - w t; (r, r) and the next rho = (r0, r)
-            const double alpha = vd(B.scal + S_ALPHA), w = vd(B.scal + S_OMEGA);
+            const double alpha = vd(qS + S_ALPHA), w = vd(qS + S_OMEGA);
             double a[2] = {0.0, 0.0};
             for (int i = t0; i < r1; i += T) {
                 B.x[i] += alpha * y[i] + w * zz[i];
@@ -1376,18 +1417,18 @@ __global__ void __launch_bounds__(QB, 3) k_bicgstab(Dev d, PpeBuffers B, double 
                 a[1] += r0[i] * r;
             }
             if (!qSum<2>(a, B, c, [&](const double* t) {
-                    B.flag[1] += 1;
-                    B.scal[S_RR] = t[0];
-                    B.scal[S_RHOOLD] = B.scal[S_RHO];
-                    B.scal[S_RHO] = t[1];
-                    if (t[0] < B.scal[S_THR]) B.flag[0] = 1;
-                    else if (fabs(t[1]) < 4.930380657631324e-32 * B.scal[S_R0N2]) B.flag[5] = 1;   // eps^2
-                    if (!(t[0] == t[0]) || B.scal[S_OMEGA] == 0.0) { B.flag[0] = 1; B.flag[2] = 1; }
+                    qF[1] += 1;
+                    qS[S_RR] = t[0];
+                    qS[S_RHOOLD] = qS[S_RHO];
+                    qS[S_RHO] = t[1];
+                    if (t[0] < qS[S_THR]) qF[0] = 1;
+                    else if (fabs(t[1]) < 4.930380657631324e-32 * qS[S_R0N2]) qF[5] = 1;   // eps^2
+                    if (!(t[0] == t[0]) || qS[S_OMEGA] == 0.0) { qF[0] = 1; qF[2] = 1; }
                 }))
                 return;
         }
         it++;
-        if (vi(B.flag + 5) && !vi(B.flag))
+        if (vi(qF + 5) && !vi(qF))
             if (!restart(false)) return;
     }
     if (!qBarrier(B, c)) return;
@@ -1397,8 +1438,9 @@ __global__ void __launch_bounds__(QB, 3) k_bicgstab(Dev d, PpeBuffers B, double 
             double r = B.b[i] - qRow(B, B.x, i, len);
             a[0] += r * r;
         });
-        qSum<1>(a, B, c, [&](const double* t) { B.scal[S_RR] = t[0]; });
+        qSum<1>(a, B, c, [&](const double* t) { qS[S_RR] = t[0]; });
     }
+    qStore(B, qL);
 }
 
 // kind: 0 plain FP64, 1 mixed, 2 mixed with the matrix-free inner operator, 3 mixed with
@@ -1419,12 +1461,12 @@ int ppePersistentGrid(int kind) {
             return 0;
         return per * sms;
     }
-    cudaError_t e = kind == 6   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bicgstab, QB, 0)
-                    : kind == 5 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_pipe, QB, 0)
-                    : kind == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_H16>, QB, 0)
-                    : kind == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_MATFREE>, QB, 0)
-                    : kind == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_ELL32>, QB, 0)
-                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_solve, QB, 0);
+    cudaError_t e = kind == 6   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bicgstab, QBC, 0)
+                    : kind == 5 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_pipe, QBX, 0)
+                    : kind == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_H16>, QBX, 0)
+                    : kind == 2 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_MATFREE>, QBX, 0)
+                    : kind == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_solve<OP_ELL32>, QBX, 0)
+                                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_solve, QBC, 0);
     if (e != cudaSuccess || per <= 0) return 0;
     return per * sms;
 }
@@ -1461,7 +1503,7 @@ int ppeSolveBicgstab(const Dev& d, const PpeBuffers& B, double tol, int maxIter,
     int mi = maxIter;
     void* args[4] = {&dd, &bb, &t, &mi};
     if (pr) prof->begin(PROF_PPE_SOLVE, s);
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_bicgstab, B.pgridBi, QB, args, 0, s);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_bicgstab, B.pgridBi, QBC, args, 0, s);
     if (pr) prof->end(s);
     if (e != cudaSuccess) return MPSGPU_ERR_CUDA;
     countLaunch(1);
@@ -1500,7 +1542,8 @@ int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol,
                      : B.matfree == 1    ? (const void*)k_mx_solve<OP_MATFREE>
                                          : (const void*)k_mx_solve<OP_ELL32>;
     size_t dyn = (mixed && B.matfree == 3) ? sizeof(TsSmem) : 0;
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, grid, QB, args, dyn, s);
+    const int bs = !mixed ? QBC : (B.matfree == 3 ? QB : QBX);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, grid, bs, args, dyn, s);
     if (pr) prof->end(s);
     if (e != cudaSuccess) return MPSGPU_ERR_CUDA;
     countLaunch(1);

@@ -616,6 +616,55 @@ __device__ __forceinline__ void forRows(const PpeBuffers& B, int n, int t0, int 
         len = ln;
     }
 }
+// Balanced rows of one thread in the persistent kernels: full rounds of the grid (row =
+// m T + b BS + t, T = G BS), then the remainder n - full T split evenly over the blocks, so
+// every block gets the same number of rows (+-1 per thread).  A plain grid stride gives
+// the first blocks one round more: at 864k rows and 152 x 1024 threads, 84 blocks did 6
+// rounds and 68 did 5, and every grid sum waited for the 6-round blocks.
+struct RowSet {
+    int first, T, full, last;   // rows first + m T (m < full), then last (-1: none)
+};
+__device__ __forceinline__ RowSet rowSet(int n, int BS) {
+    RowSet s;
+    const int G = gridDim.x;
+    s.T = G * BS;
+    s.full = n / s.T;
+    s.first = blockIdx.x * BS + threadIdx.x;
+    const int rem = n - s.full * s.T;
+    const int share = (rem + G - 1) / G;
+    const int j = s.full * s.T + blockIdx.x * share + (int)threadIdx.x;
+    s.last = ((int)threadIdx.x < share && j < n) ? j : -1;
+    return s;
+}
+__device__ __forceinline__ int rowCount(const RowSet& s) { return s.full + (s.last >= 0 ? 1 : 0); }
+__device__ __forceinline__ int rowAt(const RowSet& s, int m) { return m < s.full ? s.first + m * s.T : s.last; }
+template <class F>
+__device__ __forceinline__ void forOwn(const RowSet& s, F&& f) {
+    int i = s.first;
+    for (int m = 0; m < s.full; m++, i += s.T) f(i);
+    if (s.last >= 0) f(s.last);
+}
+// the same two rows at a time (i1 = -1: none), so a body can issue both rows' loads
+// before its stores (the compiler cannot move a load above a store that may alias it)
+template <class F>
+__device__ __forceinline__ void forOwn2(const RowSet& s, F&& f) {
+    const int cnt = rowCount(s);
+    for (int m = 0; m < cnt; m += 2) f(rowAt(s, m), m + 1 < cnt ? rowAt(s, m + 1) : -1);
+}
+// ELL rows with the next row's length prefetched
+template <class F>
+__device__ __forceinline__ void forRows(const PpeBuffers& B, const RowSet& s, F&& f) {
+    const int cnt = rowCount(s);
+    int i = cnt > 0 ? rowAt(s, 0) : 0;
+    int len = cnt > 0 ? __ldg(B.rowLen + i) : 0;
+    for (int m = 0; m < cnt; m++) {
+        const int in = (m + 1 < cnt) ? rowAt(s, m + 1) : -1;
+        const int ln = in >= 0 ? __ldg(B.rowLen + in) : 0;
+        f(i, len);
+        i = in;
+        len = ln;
+    }
+}
 __device__ __forceinline__ double qRow(const PpeBuffers& B, const double* x, int i, int len) {
     return ellRow<double, false>(B.diag, B.val, B.col, x, i, len, B.N0);
 }
@@ -876,11 +925,11 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
     const int n = liveN(d);
     const float cP = (float)d.P.coeffPPE, re = (float)d.P.reL, invRe = (float)(1.0 / d.P.reL);
     const int wt = d.P.weightType;
-    // grid-stride rows: at any moment the blocks work on one contiguous window of rows,
-    // so the column slices of the ELL arrays stream through DRAM pages in order
+    // grid-stride rounds (at any moment the blocks work on one contiguous window of rows,
+    // so the column slices of the ELL arrays stream through DRAM pages in order), the
+    // remainder split evenly over the blocks
     constexpr int BS = (OP == OP_TILED) ? QB : QBX;
-    const int T = gridDim.x * BS;
-    const int t0 = blockIdx.x * BS + threadIdx.x;
+    const RowSet rs = rowSet(n, BS);   // this thread's rows
     const int r1 = n;
     QCtl c = {0u};
     // staged tiles: the block's tile lengths and the mbarriers of the ring
@@ -909,14 +958,14 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
     }
     if (OP == OP_H16) {
         // scaling, then the compact copy of the FP32 matrix
-        for (int i = t0; i < r1; i += T) {
+        forOwn(rs, [&](int i) {
             double dd = __ldg(B.diag + i);
             double sc = 1.0 / sqrt(fabs(dd));
             B.sclf[i] = (float)sc;
             B.sgs[i] = (float)(dd < 0.0 ? -sc : sc);
-        }
+        });
         if (!qBarrier(B, c)) return;
-        forRows(B, r1, t0, T, [&](int i, int len) {
+        forRows(B, rs, [&](int i, int len) {
             const float si = B.sgs[i];
             unsigned char wide = 0;
             for (int k = 0; k < len; k++) {
@@ -933,7 +982,7 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
     }
     {
         double v[2] = {0.0, 0.0};
-        forRows(B, r1, t0, T, [&](int i, int len) {
+        forRows(B, rs, [&](int i, int len) {
             double r = B.b[i] - qRow(B, B.x, i, len);
             B.r[i] = r;
             v[0] += r * r;
@@ -962,14 +1011,14 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
         {
             const double inv = vd(qS + S_INV);
             df a[2] = {dfF(0.f), dfF(0.f)};
-            for (int i = t0; i < r1; i += T) {
+            forOwn(rs, [&](int i) {
                 float r = (float)(B.r[i] * inv);
                 if (OP == OP_H16) r *= B.sgs[i];
                 float z = (OP == OP_H16) ? r : r * __ldg(B.diagInvf + i);
                 B.rf[i] = r; B.zf[i] = z; B.xf[i] = 0.f;
                 a[0] += prod2(r, z);
                 a[1] += prod2(r, r);
-            }
+            });
             if (!qSumDF<2>(a, B, c, [&](const double* t) { qS[S_RZ] = t[0]; qS[S_RR0] = t[1]; qF[3] = 0; }))
                 return;
         }
@@ -987,7 +1036,7 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
                         a[0] += prod2(p, ap);
                     });
                     (void)okp;   // an ran-out wait sets the abort word: the reduction below returns false
-                } else forRows(B, r1, t0, T, [&](int i, int len) {
+                } else forRows(B, rs, [&](int i, int len) {
                     float q = (OP == OP_MATFREE) ? mfRowF(d, B, B.zf, i, cP, re, invRe, wt)
                             : (OP == OP_H16)   ? h16Row(B, B.zf, i, len)
                                                : qRowF(B, B.zf, i, len);
@@ -1003,14 +1052,24 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
             {
                 const float alpha = (float)vd(qS + S_ALPHA);
                 df a[2] = {dfF(0.f), dfF(0.f)};
-                for (int i = t0; i < r1; i += T) {
-                    B.xf[i] += alpha * B.pf[i];
-                    float r = B.rf[i] - alpha * B.Apf[i];
-                    float z = (OP == OP_H16) ? r : r * __ldg(B.diagInvf + i);
-                    B.rf[i] = r; B.zf[i] = z;
-                    a[0] += prod2(r, z);
-                    a[1] += prod2(r, r);
-                }
+                forOwn2(rs, [&](int i0, int i1) {   // both rows' loads before the stores
+                    const bool h1 = i1 >= 0;
+                    const int j1 = h1 ? i1 : i0;
+                    const float xa = B.xf[i0], pa = B.pf[i0], ra = B.rf[i0], qa = B.Apf[i0];
+                    const float xb = B.xf[j1], pb = B.pf[j1], rb = B.rf[j1], qb = B.Apf[j1];
+                    const float ma = (OP == OP_H16) ? 1.f : __ldg(B.diagInvf + i0);
+                    const float mb = (OP == OP_H16) ? 1.f : __ldg(B.diagInvf + j1);
+                    const float r0 = ra - alpha * qa, r1b = rb - alpha * qb;
+                    const float z0 = (OP == OP_H16) ? r0 : r0 * ma, z1 = (OP == OP_H16) ? r1b : r1b * mb;
+                    B.xf[i0] = xa + alpha * pa; B.rf[i0] = r0; B.zf[i0] = z0;
+                    a[0] += prod2(r0, z0);
+                    a[1] += prod2(r0, r0);
+                    if (h1) {
+                        B.xf[i1] = xb + alpha * pb; B.rf[i1] = r1b; B.zf[i1] = z1;
+                        a[0] += prod2(r1b, z1);
+                        a[1] += prod2(r1b, r1b);
+                    }
+                });
                 if (!qSumDF<2>(a, B, c, [&](const double* t) {
                         qF[1] += 1;
                         qS[S_BETA] = t[0] / qS[S_RZ];
@@ -1025,13 +1084,14 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
         total += inner;
         {
             const double sc = vd(qS + S_SQRT);
-            for (int i = t0; i < r1; i += T)
+            forOwn(rs, [&](int i) {
                 B.x[i] += sc * (double)((OP == OP_H16) ? B.xf[i] * B.sclf[i] : B.xf[i]);
+            });
             if (!qBarrier(B, c)) return;
         }
         {
             double v[1] = {0.0};
-            forRows(B, r1, t0, T, [&](int i, int len) {
+            forRows(B, rs, [&](int i, int len) {
                 double r = B.b[i] - qRow(B, B.x, i, len);
                 B.r[i] = r;
                 v[0] += r * r;
@@ -1094,8 +1154,7 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_pipe(Dev d, PpeBuffers B, double 
     double* const qS = qL.scal;
     int* const qF = qL.flag;
     const int n = liveN(d);
-    const int T = gridDim.x * QBX;
-    const int t0 = blockIdx.x * QBX + threadIdx.x;
+    const RowSet rs = rowSet(n, QBX);   // this thread's rows
     QCtl c = {0u};
     double* xa = B.x;      // current FP64 iterate
     double* xb = B.xalt;   // the next one
@@ -1103,7 +1162,7 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_pipe(Dev d, PpeBuffers B, double 
     float* mB = B.mf2;     // m of even iterations
     {
         double v[2] = {0.0, 0.0};
-        forRows(B, n, t0, T, [&](int i, int len) {
+        forRows(B, rs, [&](int i, int len) {
             double r = B.b[i] - qRow(B, xa, i, len);
             B.r[i] = r;
             float rf = (float)r;
@@ -1131,7 +1190,7 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_pipe(Dev d, PpeBuffers B, double 
         // inner start: w0 = A u0, m0 = M w0; gamma0 = r.u, delta0 = w.u, rho0 = r.r
         {
             df a[3] = {dfF(0.f), dfF(0.f), dfF(0.f)};
-            forRows(B, n, t0, T, [&](int i, int len) {
+            forRows(B, rs, [&](int i, int len) {
                 const float w = qRowF(B, mA, i, len);
                 const float u = mA[i], r = B.rf[i];
                 B.wf[i] = w;
@@ -1160,7 +1219,7 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_pipe(Dev d, PpeBuffers B, double 
             float* mn = (inner & 1) ? mB : mA;
             const bool first = inner == 0;
             df a[3] = {dfF(0.f), dfF(0.f), dfF(0.f)};
-            forRows(B, n, t0, T, [&](int i, int len) {
+            forRows(B, rs, [&](int i, int len) {
                 const float an = qRowF(B, mc, i, len);   // A m
                 const float di = __ldg(B.diagInvf + i);
                 float w = B.wf[i], r = B.rf[i];
@@ -1197,7 +1256,7 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_pipe(Dev d, PpeBuffers B, double 
         {
             const bool any = inner > 0;
             double v[1] = {0.0};
-            forRows(B, n, t0, T, [&](int i, int len) {
+            forRows(B, rs, [&](int i, int len) {
                 double r;
                 if (any) {
                     xb[i] = xa[i] + (double)B.xf[i];
@@ -1225,7 +1284,7 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_pipe(Dev d, PpeBuffers B, double 
         refine++;
     }
     if (xa != B.x)
-        for (int i = t0; i < n; i += T) B.x[i] = xa[i];
+        forOwn(rs, [&](int i) { B.x[i] = xa[i]; });
     qStore(B, qL);
 }
 
@@ -1237,15 +1296,15 @@ __global__ void __launch_bounds__(QBC, 1) k_cg_solve(Dev d, PpeBuffers B, double
     double* const qS = qL.scal;
     int* const qF = qL.flag;
     const int n = liveN(d);
-    // grid-stride rows: at any moment the blocks work on one contiguous window of rows,
-    // so the column slices of the ELL arrays stream through DRAM pages in order
-    const int T = gridDim.x * QBC;
-    const int t0 = blockIdx.x * QBC + threadIdx.x;
+    // grid-stride rounds (at any moment the blocks work on one contiguous window of rows,
+    // so the column slices of the ELL arrays stream through DRAM pages in order), the
+    // remainder split evenly over the blocks
+    const RowSet rs = rowSet(n, QBC);   // this thread's rows
     const int r1 = n;
     QCtl c = {0u};
     {
         double v[3] = {0.0, 0.0, 0.0};
-        forRows(B, r1, t0, T, [&](int i, int len) {
+        forRows(B, rs, [&](int i, int len) {
             double di = 1.0 / __ldg(B.diag + i);
             double r = B.b[i] - qRow(B, B.x, i, len);
             double z = r * di;
@@ -1269,7 +1328,7 @@ __global__ void __launch_bounds__(QBC, 1) k_cg_solve(Dev d, PpeBuffers B, double
         {
             const double beta = it ? vd(qS + S_BETA) : 0.0;
             double v[1] = {0.0};
-            forRows(B, r1, t0, T, [&](int i, int len) {
+            forRows(B, rs, [&](int i, int len) {
                 double q = qRow(B, B.z, i, len);
                 double z = B.z[i];
                 double ap = it ? q + beta * B.Ap[i] : q;
@@ -1283,13 +1342,20 @@ __global__ void __launch_bounds__(QBC, 1) k_cg_solve(Dev d, PpeBuffers B, double
         {
             const double alpha = vd(qS + S_ALPHA);
             double v[2] = {0.0, 0.0};
-            for (int i = t0; i < r1; i += T) {
-                B.x[i] += alpha * B.p[i];
-                double r = B.r[i] - alpha * B.Ap[i];
-                double z = r * B.dinv[i];
-                B.r[i] = r; B.z[i] = z;
-                v[0] += r * z; v[1] += r * r;
-            }
+            forOwn2(rs, [&](int i0, int i1) {   // both rows' loads before the stores
+                const bool h1 = i1 >= 0;
+                const int j1 = h1 ? i1 : i0;
+                const double xa = B.x[i0], pa = B.p[i0], ra = B.r[i0], qa = B.Ap[i0], ma = B.dinv[i0];
+                const double xb = B.x[j1], pb = B.p[j1], rb = B.r[j1], qb = B.Ap[j1], mb = B.dinv[j1];
+                const double r0 = ra - alpha * qa, r1b = rb - alpha * qb;
+                const double z0 = r0 * ma, z1 = r1b * mb;
+                B.x[i0] = xa + alpha * pa; B.r[i0] = r0; B.z[i0] = z0;
+                v[0] += r0 * z0; v[1] += r0 * r0;
+                if (h1) {
+                    B.x[i1] = xb + alpha * pb; B.r[i1] = r1b; B.z[i1] = z1;
+                    v[0] += r1b * z1; v[1] += r1b * r1b;
+                }
+            });
             if (!qSum<2>(v, B, c, [&](const double* t) {
                     qF[1] += 1;
                     qS[S_RR] = t[1];
@@ -1305,7 +1371,7 @@ __global__ void __launch_bounds__(QBC, 1) k_cg_solve(Dev d, PpeBuffers B, double
     if (!qBarrier(B, c)) return;
     {
         double v[1] = {0.0};
-        forRows(B, r1, t0, T, [&](int i, int len) {
+        forRows(B, rs, [&](int i, int len) {
             double r = B.b[i] - qRow(B, B.x, i, len);
             v[0] += r * r;
         });
@@ -1327,14 +1393,13 @@ __global__ void __launch_bounds__(QBC, 1) k_bicgstab(Dev d, PpeBuffers B, double
     double* const qS = qL.scal;
     int* const qF = qL.flag;
     const int n = liveN(d);
-    const int T = gridDim.x * QBC;
-    const int t0 = blockIdx.x * QBC + threadIdx.x;
+    const RowSet rs = rowSet(n, QBC);   // this thread's rows
     const int r1 = n;
     QCtl c = {0u};
     double *r0 = B.bs[0], *sv = B.bs[1], *zz = B.bs[2], *tv = B.bs[3], *y = B.z, *v = B.Ap;
     auto restart = [&](bool first) -> bool {
         double a[2] = {0.0, 0.0};
-        forRows(B, r1, t0, T, [&](int i, int len) {
+        forRows(B, rs, [&](int i, int len) {
             if (first) B.dinv[i] = 1.0 / __ldg(B.diag + i);
             double r = B.b[i] - qRow(B, B.x, i, len);
             B.r[i] = r; r0[i] = r; B.p[i] = 0.0; v[i] = 0.0;
@@ -1364,16 +1429,16 @@ __global__ void __launch_bounds__(QBC, 1) k_bicgstab(Dev d, PpeBuffers B, double
         {   // p = r + beta (p - w v), y = M^-1 p
             const double rho = vd(qS + S_RHO), w = vd(qS + S_OMEGA);
             const double beta = (rho / vd(qS + S_RHOOLD)) * (vd(qS + S_ALPHA) / w);
-            for (int i = t0; i < r1; i += T) {
+            forOwn(rs, [&](int i) {
                 double p = B.r[i] + beta * (B.p[i] - w * v[i]);
                 B.p[i] = p;
                 y[i] = p * B.dinv[i];
-            }
+            });
             if (!qBarrier(B, c)) return;
         }
         {   // v = A y, alpha = rho / (r0, v)
             double a[1] = {0.0};
-            forRows(B, r1, t0, T, [&](int i, int len) {
+            forRows(B, rs, [&](int i, int len) {
                 double q = qRow(B, y, i, len);
                 v[i] = q;
                 a[0] += r0[i] * q;
@@ -1388,16 +1453,16 @@ __global__ void __launch_bounds__(QBC, 1) k_bicgstab(Dev d, PpeBuffers B, double
         if (vi(qF)) break;
         {   // s = r - alpha v, z = M^-1 s
             const double alpha = vd(qS + S_ALPHA);
-            for (int i = t0; i < r1; i += T) {
+            forOwn(rs, [&](int i) {
                 double s = B.r[i] - alpha * v[i];
                 sv[i] = s;
                 zz[i] = s * B.dinv[i];
-            }
+            });
             if (!qBarrier(B, c)) return;
         }
         {   // t = A z, w = (t, s) / (t, t)
             double a[2] = {0.0, 0.0};
-            forRows(B, r1, t0, T, [&](int i, int len) {
+            forRows(B, rs, [&](int i, int len) {
                 double q = qRow(B, zz, i, len);
                 tv[i] = q;
                 a[0] += q * q;
@@ -1409,13 +1474,13 @@ __global__ void __launch_bounds__(QBC, 1) k_bicgstab(Dev d, PpeBuffers B, double
         {   // x += alpha y + w z, r = s - w t; (r, r) and the next rho = (r0, r)
             const double alpha = vd(qS + S_ALPHA), w = vd(qS + S_OMEGA);
             double a[2] = {0.0, 0.0};
-            for (int i = t0; i < r1; i += T) {
+            forOwn(rs, [&](int i) {
                 B.x[i] += alpha * y[i] + w * zz[i];
                 double r = sv[i] - w * tv[i];
                 B.r[i] = r;
                 a[0] += r * r;
                 a[1] += r0[i] * r;
-            }
+            });
             if (!qSum<2>(a, B, c, [&](const double* t) {
                     qF[1] += 1;
                     qS[S_RR] = t[0];
@@ -1434,7 +1499,7 @@ __global__ void __launch_bounds__(QBC, 1) k_bicgstab(Dev d, PpeBuffers B, double
     if (!qBarrier(B, c)) return;
     {
         double a[1] = {0.0};
-        forRows(B, r1, t0, T, [&](int i, int len) {
+        forRows(B, rs, [&](int i, int len) {
             double r = B.b[i] - qRow(B, B.x, i, len);
             a[0] += r * r;
         });

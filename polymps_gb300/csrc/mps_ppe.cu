@@ -644,12 +644,24 @@ __device__ __forceinline__ void forOwn(const RowSet& s, F&& f) {
     for (int m = 0; m < s.full; m++, i += s.T) f(i);
     if (s.last >= 0) f(s.last);
 }
-// the same two rows at a time (i1 = -1: none), so a body can issue both rows' loads
-// before its stores (the compiler cannot move a load above a store that may alias it)
-template <class F>
-__device__ __forceinline__ void forOwn2(const RowSet& s, F&& f) {
+// The thread's rows in groups of RB: ld(i) for every row of a group (all loads in flight),
+// then st(i, v) for each (a load cannot move above a store that may alias it, so a plain
+// loop waits one memory latency per row)
+template <int RB, class St, class LoadF, class StoreF>
+__device__ __forceinline__ void forOwnGroup(const RowSet& s, LoadF&& ld, StoreF&& st) {
     const int cnt = rowCount(s);
-    for (int m = 0; m < cnt; m += 2) f(rowAt(s, m), m + 1 < cnt ? rowAt(s, m + 1) : -1);
+    for (int m0 = 0; m0 < cnt; m0 += RB) {
+        St v[RB];
+        int ii[RB];
+#pragma unroll
+        for (int u = 0; u < RB; u++) {
+            ii[u] = (m0 + u < cnt) ? rowAt(s, m0 + u) : -1;
+            v[u] = ld(ii[u] >= 0 ? ii[u] : rowAt(s, m0));   // a valid row either way
+        }
+#pragma unroll
+        for (int u = 0; u < RB; u++)
+            if (ii[u] >= 0) st(ii[u], v[u]);
+    }
 }
 // ELL rows with the next row's length prefetched
 template <class F>
@@ -1052,23 +1064,18 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
             {
                 const float alpha = (float)vd(qS + S_ALPHA);
                 df a[2] = {dfF(0.f), dfF(0.f)};
-                forOwn2(rs, [&](int i0, int i1) {   // both rows' loads before the stores
-                    const bool h1 = i1 >= 0;
-                    const int j1 = h1 ? i1 : i0;
-                    const float xa = B.xf[i0], pa = B.pf[i0], ra = B.rf[i0], qa = B.Apf[i0];
-                    const float xb = B.xf[j1], pb = B.pf[j1], rb = B.rf[j1], qb = B.Apf[j1];
-                    const float ma = (OP == OP_H16) ? 1.f : __ldg(B.diagInvf + i0);
-                    const float mb = (OP == OP_H16) ? 1.f : __ldg(B.diagInvf + j1);
-                    const float r0 = ra - alpha * qa, r1b = rb - alpha * qb;
-                    const float z0 = (OP == OP_H16) ? r0 : r0 * ma, z1 = (OP == OP_H16) ? r1b : r1b * mb;
-                    B.xf[i0] = xa + alpha * pa; B.rf[i0] = r0; B.zf[i0] = z0;
-                    a[0] += prod2(r0, z0);
-                    a[1] += prod2(r0, r0);
-                    if (h1) {
-                        B.xf[i1] = xb + alpha * pb; B.rf[i1] = r1b; B.zf[i1] = z1;
-                        a[0] += prod2(r1b, z1);
-                        a[1] += prod2(r1b, r1b);
-                    }
+                struct VR { float x, p, r, q, m; };
+                forOwnGroup<3, VR>(rs, [&](int i) {
+                    VR v;
+                    v.x = B.xf[i]; v.p = B.pf[i]; v.r = B.rf[i]; v.q = B.Apf[i];
+                    v.m = (OP == OP_H16) ? 1.f : __ldg(B.diagInvf + i);
+                    return v;
+                }, [&](int i, const VR& v) {
+                    const float r = v.r - alpha * v.q;
+                    const float z = (OP == OP_H16) ? r : r * v.m;
+                    B.xf[i] = v.x + alpha * v.p; B.rf[i] = r; B.zf[i] = z;
+                    a[0] += prod2(r, z);
+                    a[1] += prod2(r, r);
                 });
                 if (!qSumDF<2>(a, B, c, [&](const double* t) {
                         qF[1] += 1;
@@ -1342,19 +1349,16 @@ __global__ void __launch_bounds__(QBC, 1) k_cg_solve(Dev d, PpeBuffers B, double
         {
             const double alpha = vd(qS + S_ALPHA);
             double v[2] = {0.0, 0.0};
-            forOwn2(rs, [&](int i0, int i1) {   // both rows' loads before the stores
-                const bool h1 = i1 >= 0;
-                const int j1 = h1 ? i1 : i0;
-                const double xa = B.x[i0], pa = B.p[i0], ra = B.r[i0], qa = B.Ap[i0], ma = B.dinv[i0];
-                const double xb = B.x[j1], pb = B.p[j1], rb = B.r[j1], qb = B.Ap[j1], mb = B.dinv[j1];
-                const double r0 = ra - alpha * qa, r1b = rb - alpha * qb;
-                const double z0 = r0 * ma, z1 = r1b * mb;
-                B.x[i0] = xa + alpha * pa; B.r[i0] = r0; B.z[i0] = z0;
-                v[0] += r0 * z0; v[1] += r0 * r0;
-                if (h1) {
-                    B.x[i1] = xb + alpha * pb; B.r[i1] = r1b; B.z[i1] = z1;
-                    v[0] += r1b * z1; v[1] += r1b * r1b;
-                }
+            struct VR { double x, p, r, q, m; };
+            forOwnGroup<4, VR>(rs, [&](int i) {
+                VR w;
+                w.x = B.x[i]; w.p = B.p[i]; w.r = B.r[i]; w.q = B.Ap[i]; w.m = B.dinv[i];
+                return w;
+            }, [&](int i, const VR& w) {
+                const double r = w.r - alpha * w.q;
+                const double z = r * w.m;
+                B.x[i] = w.x + alpha * w.p; B.r[i] = r; B.z[i] = z;
+                v[0] += r * z; v[1] += r * r;
             });
             if (!qSum<2>(v, B, c, [&](const double* t) {
                     qF[1] += 1;

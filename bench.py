@@ -33,6 +33,12 @@ WORKLOADS = {2: "3D weakly compressible polygon dam break (cfg2)",
 HBM_FALLBACK = 6800.0
 
 
+# DRAM bytes (read + write) per launch of the single-launch PPE solve over the 100 timed
+# steps of the default workload, from one ncu capture of exactly those launches
+# (dram__bytes_read.sum + dram__bytes_write.sum, profiles/k_mx_solve_cfg3-864k.md).
+MX_SOLVE_TRAFFIC = 4.814e9
+
+
 def args_():
     a = argparse.ArgumentParser()
     a.add_argument("--gpus", type=int, default=1)
@@ -279,8 +285,12 @@ def run_gb300(a, rank, world, local):
                        solver == abi.SOLVER_MIXED_COMPACT)
         if b:
             ach = b / (ms / calls / 1e3) / 1e9
+            traffic = None
+            if (dom == "PPE_SOLVE" and a.config == 3 and a.scale == 1.0 and a.solver == "mixed"
+                    and a.precision == "df32" and a.warm in ("auto", "extrap2") and a.steps == 100 and a.warmup == 5):
+                traffic = MX_SOLVE_TRAFFIC
             roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
-                    "frac": round(ach / hbm, 4), "peak_source": hbm_src, "traffic": None,
+                    "frac": round(ach / hbm, 4), "peak_source": hbm_src, "traffic": traffic,
                     "algo_bytes_per_launch": int(b), "launch_ms": round(ms / calls, 4),
                     "share_of_step": round(ms / st.stepMs, 3)}
 

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <string>
 #include <vector>
+#include <utility>
 #include <algorithm>
 #include "mps_common.cuh"
 #include "mps_internal.h"
@@ -37,7 +38,9 @@ struct mpsgpu_s {
     // host mirrors of a few scalars
     bool listValid = false;
     bool masksValid = false;
-    bool skinValid = false;    // the nbr rows hold the start-of-step skin list of this bucket list
+    bool skinValid = false;    // the skin list of this bucket list is built and not yet filtered
+    bool skinShift = false;    // ... and still intact for the shifting sweeps of the step
+    int *nbrAlt = nullptr, *cntAlt = nullptr;   // second list arrays (the skin list keeps its own)
     int skinOn = 1;            // DF32 tier: viscosity and the post-prediction list from the skin list
     bool corrFresh = false;    // the correction matrix of the current positions and masks is written
     bool opSkipped = false;    // the last operator had nothing left to launch
@@ -333,6 +336,7 @@ static int runOpBody(mpsgpu_t h, int op) {
             h->renumberCountdown--;
             invalidate();
             h->skinValid = false;
+            h->skinShift = false;
             break;
         }
         case MPS_OP_VISCOSITY:
@@ -344,7 +348,13 @@ static int runOpBody(mpsgpu_t h, int op) {
                 if (h->prof.on) { h->prof.end(s); h->prof.begin(MPS_OP_VISCOSITY, s, false); }
                 launchViscosityListDF(d, s);
                 invalidate();
+                // the skin list keeps its arrays; the lists filtered from it go to the others
+                d.skinNbr = d.nbr;
+                d.skinCnt = d.nbrCount;
+                std::swap(d.nbr, h->nbrAlt);
+                std::swap(d.nbrCount, h->cntAlt);
                 h->skinValid = true;
+                h->skinShift = true;
                 countLaunch(2);   // skin list (listed + unlisted particles); the sweep is counted below
             } else if (x) launchViscosityDF(d, s);
             else launchViscosity(d, s);
@@ -398,8 +408,23 @@ static int runOpBody(mpsgpu_t h, int op) {
         case MPS_OP_WALL_VISCOSITY: ensureMasks(h); if (x) launchWallViscosityDF(d, s); else launchWallViscosity(d, s); break;
         case MPS_OP_CORRECT: launchCorrect(d, s); invalidate(); break;
         case MPS_OP_SHIFTING:
-            if (x) launchShiftingDF(d, s); else launchShifting(d, s);
-            if (P.shiftingType == 2) invalidate();
+            if (x && h->skinShift && (P.shiftingType == 1 || P.shiftingType == 2)) {
+                // the list of the post-corrector positions filtered from the skin list (a
+                // particle that moved out of its skin or scan window, or any particle after a
+                // removal, scans the buckets), its masks, then list sweeps
+                if (h->prof.on) { h->prof.end(s); h->prof.begin(PROF_NEIGHBOR_LIST, s, false); }
+                launchNeighborFilterDF(d, s);
+                launchSideMasksDF(d, s);
+                if (h->prof.on) { h->prof.end(s); h->prof.begin(MPS_OP_SHIFTING, s, false); }
+                launchShiftingListDF(d, s);
+                invalidate();
+                // posf + cell copy, skin check, filter (2), masks; then the sweeps and applies
+                countLaunch(6 + (P.shiftingType == 1 ? 3 : (P.wallType == 1 ? 7 : 4)));
+                h->opSkipped = true;
+            } else {
+                if (x) launchShiftingDF(d, s); else launchShifting(d, s);
+                if (P.shiftingType == 2) invalidate();
+            }
             break;
         case MPS_OP_DUMMY_VELOCITY: launchDummyVelocity(d, s); break;
         case MPS_OP_INIT_PND: ensureMasks(h); ensureCache(h); launchInitPnd(d, s); break;
@@ -649,6 +674,10 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     A(d.c3n, n);
     A(d.nbrCount, n);
     A(d.nbr, (size_t)d.K * n);
+    A(h->cntAlt, n);
+    A(h->nbrAlt, (size_t)d.K * n);
+    d.skinCnt = d.nbrCount;
+    d.skinNbr = d.nbr;
     A(d.cw, (size_t)d.K * n);
     A(d.cwd, (size_t)d.K * n);
     if (p->reS2 != p->reL2) A(d.cwL, (size_t)d.K * n);
@@ -1127,7 +1156,9 @@ int mpsgpu_set_field(mpsgpu_t h, int f, const void* host) {
     size_t bytes = (kind == 0) ? 3 * sizeof(double) * n : ((kind == 1) ? sizeof(double) : sizeof(int)) * n;
     CK(cudaMemcpyAsync(h->permScratch, host, bytes, cudaMemcpyHostToDevice, h->s));
     fromRef(h, kind, p, n);
-    // any state change can alter list membership, masks or the near-wall set
+    // any state change can alter list membership, masks or the near-wall set (the shifting
+    // filter keeps the skin list: it re-checks every position against its start position and
+    // scan window, so set positions fall back to the bucket scan where they must)
     h->listValid = false;
     h->skinValid = false;
     h->corrFresh = false;

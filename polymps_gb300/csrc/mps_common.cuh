@@ -100,6 +100,7 @@ struct Dev {
     // neighbour list (ELL) and its per-entry cache for the epoch: w(r; reS), w/r^2,
     // w(r; reL) (only when reL != reS)
     int *nbrCount, *nbr;
+    int *skinCnt, *skinNbr;         // the start-of-step skin list (its own arrays once built)
     double *cw, *cwd, *cwL;
     // per-particle entry masks after the wall pass: bit k set when entry k is inside the
     // reS (maskS) / reL (maskL) ball and not on the mirror side

@@ -79,6 +79,8 @@ void launchPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallPressGradientDF(const Dev& d, cudaStream_t s);
 void launchWallViscosityDF(const Dev& d, cudaStream_t s);
 void launchShiftingDF(const Dev& d, cudaStream_t s);
+// the same from the list of the current positions (filtered from the skin list, masks built)
+void launchShiftingListDF(const Dev& d, cudaStream_t s);
 // ARC free surface (free-surface type 2): fluid normals (+ wall term), then the BC test
 void launchUpdateBCArc(const Dev& d, cudaStream_t s);
 // dynamic particle collision (collision type 1, FP64, list based; moves positions)

@@ -850,6 +850,43 @@ __global__ void __launch_bounds__(BLK) k_wall_grad_conc_df(Dev d) {
     }
     d.shift[i] = sh;
 }
+// The shifting sums over the list of the post-corrector positions (filtered from the skin
+// list) instead of the 27-bucket scan: the reS-ball entries off the mirror side are the
+// maskS entries of that list, in scan order, so the sums are those of k_shift_scan_df.
+template <class Op>
+__global__ void __launch_bounds__(BLK) k_shift_list_df(Dev d, Op op) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    typename Op::State st;
+    const bool on = op.begin(d, i, st);
+    if (on) {
+        const float4 hi = d.posf[i], li = d.posLo[i];
+        forMask(d, i, d.maskS[i], [&](int j, size_t) {
+            const PairF q = pairDF(__ldg(d.posf + j), __ldg(d.posLo + j), hi, li);
+            op.visit(d, st, j, q);
+        });
+    }
+    op.end(d, i, st, on);
+}
+// Shifting from the list of the current positions (built by the caller: filter + masks).
+void launchShiftingListDF(const Dev& d, cudaStream_t s) {
+    const MpsParams& P = d.P;
+    if (P.shiftingType == 1) {
+        launchVelDF(d, s);
+        k_shift_list_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d, ShiftVelDF());
+        launchShiftVelApply(d, s);
+        return;
+    }
+    k_shift_list_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d, ConcDF());
+    k_df_conc<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
+    k_shift_list_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d, GradConcDF());
+    launchApplyShift(d, s);
+    if (P.wallType == 1) {
+        launchPosfCell(d, s);
+        k_wall_grad_conc_df<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+        launchApplyShift(d, s);
+    }
+}
 void launchShiftingDF(const Dev& d, cudaStream_t s) {
     const MpsParams& P = d.P;
     if (P.shiftingType != 1 && P.shiftingType != 2) return;
@@ -983,10 +1020,10 @@ __global__ void __launch_bounds__(128) k_filter_nbr_df(Dev d) {
         if (cnt < d.K) d.nbr[(size_t)cnt * N0 + i] = j;
         cnt++;
     };
-    const int c = d.nbrCount[i];
+    const int c = d.skinCnt[i];
     if (!*(volatile int*)d.skinFlag && c <= d.K && d.skinCell[i] == cellKeyOf(d, pi, hi)) {
-        for (int k = 0; k < c; k++) {   // compacted in place: the write index never passes the read index
-            const int j = d.nbr[(size_t)k * N0 + i];
+        for (int k = 0; k < c; k++) {   // the skin list stays intact (a later sweep filters it again)
+            const int j = ldStream(d.skinNbr + (size_t)k * N0 + i);
             keep(j, d.posf[j], d.posLo[j]);
         }
     } else {

@@ -265,3 +265,39 @@ def test_shifting_parity(oracle_mod, mps_lib, stype, precision):
     compare(o, g, "shifting %d" % stype, rtol=DF_RTOL if precision == abi.PRECISION_DF32 else 1e-10)
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("stype", [1, 2])
+def test_shifting_list_parity(oracle_mod, mps_lib, stype):
+    """DF32 shifting over the list of the post-corrector positions filtered from the
+    start-of-step skin list (the path of a full step) equals the oracle's scan from the
+    same post-corrector state, tank with obstacle."""
+    from polymps_gb300 import mps
+    c = cases.config(5, jitter=0.02, scale=6.0)
+    c.params.update(shiftingType=stype)
+    o = oracle_mod.Oracle(c)
+    g = mps.MpsGpu(c, tol=1e-12, precision=abi.PRECISION_DF32)
+    o.set_solver(1e-12)
+    o.initialize()
+    g.initialize()
+    for _ in range(4):
+        o.step()
+    ops = step_ops(o.params)
+    sync(o, g)
+    k = ops.index("SHIFTING")
+    for op in ops[:k]:   # the GPU builds its skin list in VISCOSITY, as in a step
+        o.run_op(op)
+        g.run_op(op)
+    assert o.n == g.n
+    sync(o, g)   # identical post-corrector state (moves within the skin keep the list usable)
+    f = abi.F_POS if stype == 2 else abi.F_VEL
+    before = o.get(f)
+    o.run_op("SHIFTING")
+    l0 = mps.MpsGpu.launch_count()
+    g.run_op("SHIFTING")
+    # filter path: positions (2), skin check, filter (2), masks, then the sweeps
+    assert mps.MpsGpu.launch_count() - l0 == 6 + (3 if stype == 1 else 7)
+    assert np.abs(o.get(f) - before).max() > 0.0
+    compare(o, g, "shifting list %d" % stype, rtol=DF_RTOL)
+    g.close()
+    o.close()

@@ -374,6 +374,43 @@ def test_ppe_launch_modes_agree(oracle_mod, mps_lib, solver):
 
 
 @pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_DF32])
+def test_mixed_solver_storage_orders(mps_lib, precision):
+    """108k particles in random storage order (matrix columns anywhere in the index range)
+    and, after the bucket-order renumbering of the 20th rebuild, in bucket order: the mixed
+    solution reaches the FP64 residual 1e-8 and stays within 1e-6 (normwise) of the FP64
+    solve of the same system to 1e-12."""
+    from polymps_gb300 import mps
+    c = cases.config(3, jitter=0.02, scale=2.0)
+    perm = np.random.default_rng(7).permutation(c.n)
+    c = cases.Case(c.name, c.params, c.type[perm], c.pos[perm], c.mesh)
+    g = mps.MpsGpu(c, precision=precision, solver=abi.SOLVER_MIXED, tol=1e-8)
+    g.initialize()
+    ops = step_ops(g.params)
+    k = ops.index("CALC_PRESS")
+    hist_f = (abi.F_PRESSPPE, abi.F_PRESSPPE_PREV, abi.F_PRESSPPE_PREV2)
+    done = 0
+    for upto in (2, 23):   # steps before the checked one
+        g.run(upto - done)
+        done = upto + 1
+        for op in ops[:k]:
+            g.run_op(op)
+        hist = [g.get(f) for f in hist_f]
+        g.set_solver(abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 1e-12, 20000)
+        g.run_op("CALC_PRESS")
+        p_ref = g.get(abi.F_PRESSPPE)
+        for f, v in zip(hist_f, hist):
+            g.set(f, v)
+        g.set_solver(abi.SOLVER_MIXED, abi.WARM_PREVIOUS, 1e-8, 20000)
+        g.run_op("CALC_PRESS")
+        st = g.last_stats()
+        assert st.ppeRelResidual <= 1e-8
+        assert relerr(g.get(abi.F_PRESSPPE), p_ref) < 1e-6
+        for op in ops[k + 1:]:
+            g.run_op(op)
+    g.close()
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_DF32])
 @pytest.mark.parametrize("name", ["cfg1_2d_particle_walls", "cfg3_3d_inc_polygon"])
 def test_out_of_domain_removal(oracle_mod, mps_lib, name, precision):
     """Fluid particles pushed outside the domain margin (one of them the last index) are

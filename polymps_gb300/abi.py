@@ -161,6 +161,17 @@ def params_to_dict(p):
     return out
 
 
+def field_spec(field, n):
+    """(shape, dtype) of a field in the reference's host layout."""
+    if field in VECTOR_FIELDS:
+        return (n, 3), np.float64
+    if field in SCALAR_FIELDS or field in (F_PRESSPPE_PREV, F_PRESSPPE_PREV2):
+        return (n,), np.float64
+    if field in INT_FIELDS:
+        return (n,), np.int32
+    raise ValueError(f"unknown field {field}")
+
+
 def field_buffer(field, n):
     if field in VECTOR_FIELDS:
         return np.zeros((n, 3), dtype=np.float64)

@@ -40,6 +40,7 @@ struct mpsgpu_s {
     bool masksValid = false;
     bool skinValid = false;    // the skin list of this bucket list is built and not yet filtered
     bool skinShift = false;    // ... and still intact for the shifting sweeps of the step
+    int nHost = -1;            // live count known on the host (-1: read it from the device)
     int *nbrAlt = nullptr, *cntAlt = nullptr;   // second list arrays (the skin list keeps its own)
     int skinOn = 1;            // DF32 tier: viscosity and the post-prediction list from the skin list
     bool corrFresh = false;    // the correction matrix of the current positions and masks is written
@@ -361,7 +362,11 @@ static int runOpBody(mpsgpu_t h, int op) {
             break;
         case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
         case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
-        case MPS_OP_OUT_OF_DOMAIN: launchOutOfDomain(d, h->outFlags, h->outCounter, s); invalidate(); break;
+        case MPS_OP_OUT_OF_DOMAIN:
+            launchOutOfDomain(d, h->outFlags, h->outCounter, s);
+            invalidate();
+            h->nHost = -1;   // removals change the live count on the device
+            break;
         case MPS_OP_COLLISION:
             ensureList(h);
             if (P.collisionType == 1) {   // DPC moves the positions: every list is stale
@@ -483,6 +488,7 @@ static int finishStats(mpsgpu_t h, MpsStepStats* st, float stepMs) {
     h->last.velMax = vmax;
     h->last.CFLcurrent = h->d.P.timeStep * vmax / h->d.P.partDist;
     h->last.numParticles = n;
+    h->nHost = n;
     h->last.stepMs = stepMs;
     if (st) *st = h->last;
     return 0;
@@ -958,8 +964,13 @@ int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm, double tol, int max_iter
 
 int mpsgpu_num_particles(mpsgpu_t h, int* n) {
     if (!h || !n) return MPSGPU_ERR_ARG;
+    if (h->nHost >= 0) {   // unchanged since the last read (only removals change it)
+        *n = h->nHost;
+        return 0;
+    }
     CK(cudaMemcpyAsync(n, h->d.nLive, sizeof(int), cudaMemcpyDeviceToHost, h->s));
     CK(cudaStreamSynchronize(h->s));
+    h->nHost = *n;
     return 0;
 }
 

@@ -196,8 +196,8 @@ class MpsGpu:
         return buf
 
     def set(self, field, arr):
-        ref = abi.field_buffer(field, self.n)
-        arr = np.ascontiguousarray(arr, dtype=ref.dtype).reshape(ref.shape)
+        shape, dtype = abi.field_spec(field, self.n)
+        arr = np.ascontiguousarray(arr, dtype=dtype).reshape(shape)   # no copy for a matching array
         _check("mpsgpu_set_field", lib().mpsgpu_set_field(self.h, field, arr.ctypes.data), self.h)
 
     def neighbors(self):

@@ -250,7 +250,7 @@ static int calcPress(mpsgpu_t h) {
         if (!h->B.prepared) { launchMixedPrepare(h->d, h->B, h->s); h->B.prepared = 1; countLaunch(1); }
         int e = mlpWarmStart(h->mlp, h->d, h->B, h->s);
         if (h->prof.on) h->prof.end(h->s);
-        countLaunch(8);   // x_e copy, features, scale, forward, correction, step dot products, step, apply
+        countLaunch(9);   // x_e copy, residual, features, scale, forward, correction, step dot products, step, apply
         if (e) return e;
     } else if (h->warm == MPSGPU_WARM_PREVIOUS) {
         cudaMemcpyAsync(h->B.x, h->d.pressPPE, sizeof(double) * h->N0, cudaMemcpyDeviceToDevice, h->s);

@@ -276,6 +276,43 @@ __device__ __forceinline__ void forNbrs(const Dev& d, int i, F&& f) {
 }
 
 // Iterate the set bits of an entry mask in ascending entry order (the scan order).
+// ELL matrix rows (PPE solvers, learned warm start)
+// One ELL row, eight entries in flight: the column and value loads of a chunk are issued
+// together, then the eight gathers; the last chunk is masked (predicated loads, the row's
+// own index as a harmless column) instead of a serial remainder loop.  RO: the gathered
+// vector is read-only for the launch (non-coherent cache path); otherwise plain loads.
+#define ELL_U 8
+template <class T, bool RO>
+__device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col, const T* x, int i, int len, size_t N0) {
+    T acc[ELL_U];
+#pragma unroll
+    for (int u = 0; u < ELL_U; u++) acc[u] = T(0);
+    const T* v = val + i;
+    const int* c = col + i;
+    for (int k = 0; k < len; k += ELL_U) {
+        // ask L2 for the next chunk's column and value lines while this chunk's gathers run
+        if (k + ELL_U < len) {
+#pragma unroll
+            for (int u = 0; u < ELL_U; u++) {
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(c + (size_t)(k + ELL_U + u) * N0));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(v + (size_t)(k + ELL_U + u) * N0));
+            }
+        }
+        int cc[ELL_U];
+        T vv[ELL_U];
+#pragma unroll
+        for (int u = 0; u < ELL_U; u++) {
+            bool ok = k + u < len;
+            cc[u] = ok ? ldStream(c + (size_t)(k + u) * N0) : i;
+            vv[u] = ok ? ldStream(v + (size_t)(k + u) * N0) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < ELL_U; u++) acc[u] += vv[u] * (RO ? __ldg(x + cc[u]) : x[cc[u]]);
+    }
+    T xi = RO ? __ldg(x + i) : x[i];
+    return __ldg(diag + i) * xi + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
+}
+
 template <class F>
 __device__ __forceinline__ void forMask(const Dev& d, int i, unsigned long long m, F&& f) {
     const int* row = d.nbr + i;

@@ -255,8 +255,15 @@ __global__ void k_mlp_xe32(Dev d, float* xe32) {
     if (i >= d.N0) return;
     xe32[i] = (i < liveN(d) && d.bc[i] == d.P.inner) ? (float)extrapBase(d, i) : 0.f;
 }
-__global__ void __launch_bounds__(256) k_mlp_features(Dev d, PpeBuffers B, const float* xe32, float* feat, float* re,
-                                                      double* part) {
+// r_e = b - A x_e (FP32 copy of the matrix) for the features and the step: one row per
+// thread, eight entries in flight with the next chunk's lines prefetched (ellRow)
+__global__ void __launch_bounds__(256) k_mlp_resid(Dev d, PpeBuffers B, const float* xe32, float* re) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    re[i] = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), B.N0);
+}
+__global__ void __launch_bounds__(256) k_mlp_features(Dev d, PpeBuffers B, const float* xe32, const float* re,
+                                                      float* feat, double* part) {
     const MpsParams& P = d.P;
     double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
     double gn = sqrt(gx * gx + gy * gy + gz * gz);
@@ -265,7 +272,6 @@ __global__ void __launch_bounds__(256) k_mlp_features(Dev d, PpeBuffers B, const
     const float in0 = (float)(1.0 / P.pndSmallZero), iN0 = (float)(1.0 / P.numNeighZero), iRe = (float)(1.0 / P.reL);
     const float iA = (float)(1.0 / (P.coeffPPE * P.pndSmallZero));
     const int n = liveN(d);
-    const size_t N0 = B.N0;
     double q0 = 0.0, q1 = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const dvec4 x = d.pos[i], v = d.vel[i];
@@ -273,26 +279,8 @@ __global__ void __launch_bounds__(256) k_mlp_features(Dev d, PpeBuffers B, const
         const float pn = (float)d.pressPPE[i], pp = (float)d.pressPPEprev[i];
         const bool eq = d.bc[i] == P.inner;
         const float xe = xe32[i];
-        // (A x_e)_i in FP32 from the FP32 copy of the matrix, eight entries in flight
-        float acc[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) acc[u] = 0.f;
-        const int len = B.rowLen[i];
-        for (int k = 0; k < len; k += 8) {
-            int cc[8];
-            float vv[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                bool ok = k + u < len;
-                cc[u] = ok ? ldStream(B.col + (size_t)(k + u) * N0 + i) : i;
-                vv[u] = ok ? ldStream(B.valf + (size_t)(k + u) * N0 + i) : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < 8; u++) acc[u] += vv[u] * xe32[cc[u]];
-        }
-        const float ax = diag * xe + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
         const float bi = (float)B.b[i];
-        if (re) re[i] = bi - ax;   // residual of the extrapolated start
+        const float rei = re[i];   // b_i - (A x_e)_i
         const float vx = (float)v.x, vy = (float)v.y, vz = (float)v.z;
         float f[NF];
         f[0] = ((float)d.pndSmall[i] - (float)P.pndSmallZero) * in0;
@@ -302,7 +290,7 @@ __global__ void __launch_bounds__(256) k_mlp_features(Dev d, PpeBuffers B, const
         f[4] = fminf(sqrtf((float)d.riw2[i]) * iRe, 1.5f);
         f[5] = pn - pp;
         f[6] = xe;
-        f[7] = (bi - ax) * idg;
+        f[7] = rei * idg;
         f[8] = pn;
         f[9] = sqrtf(vx * vx + vy * vy + vz * vz);
         f[10] = -(vx * ggx + vy * ggy + vz * ggz);
@@ -325,9 +313,10 @@ __global__ void __launch_bounds__(256) k_mlp_sig(const double* part, int nblk, d
     sumPartials2(part, nblk, a, b);
     if (threadIdx.x == 0) sig[0] = (b > 0.0 && a > 0.0) ? sqrt(a / b) : 1.0;
 }
-static void mlpFeatureLaunch(MlpState& m, const Dev& d, const PpeBuffers& B, float* re, cudaStream_t s) {
+static void mlpFeatureLaunch(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s) {
     k_mlp_xe32<<<gridFor(d.N0, 256), 256, 0, s>>>(d, m.xe32);
-    k_mlp_features<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.feat, re, m.part);
+    k_mlp_resid<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.xe32, m.re);
+    k_mlp_features<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.re, m.feat, m.part);
     k_mlp_sig<<<1, 256, 0, s>>>(m.part, m.nblk, m.sig);
 }
 
@@ -351,23 +340,7 @@ __global__ void __launch_bounds__(256) k_mlp_step_dots(Dev d, PpeBuffers B, cons
     const int n = liveN(d);
     const size_t N0 = B.N0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        float acc[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) acc[u] = 0.f;
-        const int len = B.rowLen[i];
-        for (int k = 0; k < len; k += 8) {
-            int cc[8];
-            float vv[8];
-#pragma unroll
-            for (int u = 0; u < 8; u++) {
-                bool ok = k + u < len;
-                cc[u] = ok ? ldStream(B.col + (size_t)(k + u) * N0 + i) : i;
-                vv[u] = ok ? ldStream(B.valf + (size_t)(k + u) * N0 + i) : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < 8; u++) acc[u] += vv[u] * cdir[cc[u]];
-        }
-        const float ac = __ldg(B.diagf + i) * cdir[i] + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
+        const float ac = ellRow<float, true>(B.diagf, B.valf, B.col, cdir, i, __ldg(B.rowLen + i), N0);
         s0 += (double)(re[i] * ac);
         s1 += (double)(ac * ac);
     }
@@ -397,7 +370,7 @@ static int mlpForwardLaunch(MlpState& m, const float* feat, int n, const double*
 
 int mlpWarmStart(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s) {
     if (!m.ready) return MPSGPU_ERR_ARG;
-    mlpFeatureLaunch(m, d, B, m.re, s);
+    mlpFeatureLaunch(m, d, B, s);
     int e = mlpForwardLaunch(m, m.feat, d.N0, m.sig, m.out, s);
     if (e) return e;
     k_mlp_combine<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.out, m.norm, m.sig, m.cdir);
@@ -408,7 +381,7 @@ int mlpWarmStart(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s)
 }
 
 int mlpFeatures(MlpState& m, const Dev& d, const PpeBuffers& B, float* hostFeat, int n, cudaStream_t s) {
-    mlpFeatureLaunch(m, d, B, nullptr, s);
+    mlpFeatureLaunch(m, d, B, s);
     if (cudaMemcpyAsync(hostFeat, m.feat, sizeof(float) * NF * n, cudaMemcpyDeviceToHost, s) != cudaSuccess) return MPSGPU_ERR_CUDA;
     return cudaStreamSynchronize(s) == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
 }
@@ -477,7 +450,7 @@ int mlpGetWeights(MlpState& m, float* params, float* norm32, cudaStream_t s) {
 
 // ------------------------------------------------------------------ recording
 int mlpRecordFeatures(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s) {
-    mlpFeatureLaunch(m, d, B, nullptr, s);
+    mlpFeatureLaunch(m, d, B, s);
     return cudaGetLastError() == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
 }
 __global__ void k_mlp_record(Dev d, PpeBuffers B, const float* feat, const double* sig, float* recFeat,

@@ -155,42 +155,7 @@ __device__ __forceinline__ void gridSum(double (&v)[NV], const PpeBuffers& B, Fi
     if (threadIdx.x == 0) fin(acc);
 }
 
-// ------------------------------------------------------------------ ELL rows
-// One ELL row, eight entries in flight: the column and value loads of a chunk are issued
-// together, then the eight gathers; the last chunk is masked (predicated loads, the row's
-// own index as a harmless column) instead of a serial remainder loop.  RO: the gathered
-// vector is read-only for the launch (non-coherent cache path); otherwise plain loads.
-#define ELL_U 8
-template <class T, bool RO>
-__device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col, const T* x, int i, int len, size_t N0) {
-    T acc[ELL_U];
-#pragma unroll
-    for (int u = 0; u < ELL_U; u++) acc[u] = T(0);
-    const T* v = val + i;
-    const int* c = col + i;
-    for (int k = 0; k < len; k += ELL_U) {
-        // ask L2 for the next chunk's column and value lines while this chunk's gathers run
-        if (k + ELL_U < len) {
-#pragma unroll
-            for (int u = 0; u < ELL_U; u++) {
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(c + (size_t)(k + ELL_U + u) * N0));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(v + (size_t)(k + ELL_U + u) * N0));
-            }
-        }
-        int cc[ELL_U];
-        T vv[ELL_U];
-#pragma unroll
-        for (int u = 0; u < ELL_U; u++) {
-            bool ok = k + u < len;
-            cc[u] = ok ? ldStream(c + (size_t)(k + u) * N0) : i;
-            vv[u] = ok ? ldStream(v + (size_t)(k + u) * N0) : T(0);
-        }
-#pragma unroll
-        for (int u = 0; u < ELL_U; u++) acc[u] += vv[u] * (RO ? __ldg(x + cc[u]) : x[cc[u]]);
-    }
-    T xi = RO ? __ldg(x + i) : x[i];
-    return __ldg(diag + i) * xi + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
-}
+// ------------------------------------------------------------------ ELL rows (ellRow: mps_common.cuh)
 __device__ __forceinline__ double spmvRow(const PpeBuffers& B, const double* x, int i) {
     return ellRow<double, true>(B.diag, B.val, B.col, x, i, __ldg(B.rowLen + i), B.N0);
 }
@@ -942,7 +907,6 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
     // remainder split evenly over the blocks
     constexpr int BS = (OP == OP_TILED) ? QB : QBX;
     const RowSet rs = rowSet(n, BS);   // this thread's rows
-    const int r1 = n;
     QCtl c = {0u};
     // staged tiles: the block's tile lengths and the mbarriers of the ring
     TsSmem& sm = *reinterpret_cast<TsSmem*>(dynSmem);
@@ -1307,7 +1271,6 @@ __global__ void __launch_bounds__(QBC, 1) k_cg_solve(Dev d, PpeBuffers B, double
     // so the column slices of the ELL arrays stream through DRAM pages in order), the
     // remainder split evenly over the blocks
     const RowSet rs = rowSet(n, QBC);   // this thread's rows
-    const int r1 = n;
     QCtl c = {0u};
     {
         double v[3] = {0.0, 0.0, 0.0};
@@ -1398,7 +1361,6 @@ __global__ void __launch_bounds__(QBC, 1) k_bicgstab(Dev d, PpeBuffers B, double
     int* const qF = qL.flag;
     const int n = liveN(d);
     const RowSet rs = rowSet(n, QBC);   // this thread's rows
-    const int r1 = n;
     QCtl c = {0u};
     double *r0 = B.bs[0], *sv = B.bs[1], *zz = B.bs[2], *tv = B.bs[3], *y = B.z, *v = B.Ap;
     auto restart = [&](bool first) -> bool {

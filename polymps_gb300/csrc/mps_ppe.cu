@@ -451,9 +451,8 @@ int ppeSolveMixed(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cu
 // arrival counter (release) and waits until the counter reaches the generation's target
 // (acquire); then every block sums all partials in block order and derives the solver's
 // scalars itself.  Identical inputs in identical order give every block identical
-// scalars, so no block has to publish them and release the others (that serial tail cost
-// ~12 us of the ~16 us a reduction took at 608 blocks).  The scalars and flags live in
-// shared memory per block; block 0 stores its copy for the host at the end.  Waits are
+// scalars, so no block has to publish them and release the others.  The scalars and flags
+// live in shared memory per block; block 0 stores its copy for the host at the end.  Waits are
 // bounded: a block that waits longer than QSPIN polls sets the abort word and every
 // block returns.
 // Block sizes: one block per SM (1024 threads for the mixed solvers at <= 64 registers,

@@ -476,6 +476,18 @@ def cpu_baseline(case, steps):
         o.close()
         full["threads_%d" % th] = {"s": round(d, 3), "value": round(c1.n * c1.steps / d, 1)}
     out["full_run_2d_particle_walls"] = {"particles": c1.n, "steps": c1.steps, **full}
+    # a fixed window of the 3D weakly compressible dam break (108,000 particles), all threads
+    c2 = cases.config(2)
+    o = oracle.Oracle(c2, threads=cores)
+    o.set_solver(1e-8)
+    o.initialize()
+    t0 = time.perf_counter()
+    for _ in range(5):
+        o.step()
+    d = time.perf_counter() - t0
+    o.close()
+    out["window_3d_weakly_compressible"] = {"particles": c2.n, "steps": 5, "s": round(d, 3),
+                                            "value": round(c2.n * 5 / d, 1), "cores": cores}
     return out
 
 

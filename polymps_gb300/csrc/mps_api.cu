@@ -634,7 +634,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         d.oodHi[k] = p->domainMax[k] - p->bucketSide;
     }
     d.nB = p->numBucketsXYZ;
-    d.K = ((int)p->dim == 3) ? 64 : 32;
+    d.K = ((int)p->dim == 3) ? 128 : 64;   // entries per neighbour row (compressed flows reach ~2x the rest count)
     int e = 0;
 #define A(ptr, cnt) do { if ((e = dalloc(h, &(ptr), (cnt)))) { mpsgpu_destroy(h); return e; } } while (0)
     A(d.nLive, 1);
@@ -757,7 +757,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         k.collW = hd(p->restitutionCollision * p->densityWall / (p->DNS_FL1 + p->densityWall));
         k.negCPG = hd(-p->coeffPressGrad);
     }
-    if (d.K > 64) { g_lastError = "neighbour row capacity above the 64-bit entry masks"; mpsgpu_destroy(h); return MPSGPU_ERR_UNSUPPORTED; }
+    if (d.K > 128) { g_lastError = "neighbour row capacity above the 128-entry masks"; mpsgpu_destroy(h); return MPSGPU_ERR_UNSUPPORTED; }
     // mesh and wall tables
     if (p->wallType == 1) {
         std::vector<double> nrm(3 * mesh->ntri), tab(4 * MPS_TAB);

@@ -320,20 +320,20 @@ __global__ void __launch_bounds__(128) k_side_masks(Dev d) {
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     int c = d.nbrCount[i];
-    unsigned long long all = (c >= 64) ? ~0ull : ((1ull << c) - 1ull);
+    const Mask all = maskFirst(c);
     dvec4 pi = d.pos[i];
     SideCtx sc = sideCtx(d, i, pi);
     bool fullS = P.reS2 >= d.reMax2, fullL = P.reL2 >= d.reMax2;
-    unsigned long long mS = all, mL = all;
+    Mask mS = all, mL = all;
     if (sc.check || !fullS || !fullL) {
-        mS = 0; mL = 0;
+        mS = maskNone(); mL = maskNone();
         const int* row = d.nbr + i;
         for (int k = 0; k < c; k++) {
             dvec4 pj = d.pos[__ldg(row + (size_t)k * d.N0)];
             PairG q = pairOf(pj, pi);
             bool side = sideOK(sc, pj, q.d2);
-            if (side && q.d2 < P.reS2) mS |= 1ull << k;
-            if (side && q.d2 < P.reL2) mL |= 1ull << k;
+            if (side && q.d2 < P.reS2) maskSet(mS, k);
+            if (side && q.d2 < P.reL2) maskSet(mL, k);
         }
     }
     d.maskS[i] = mS;

@@ -30,6 +30,35 @@ __host__ __device__ __forceinline__ dvec4 make_dvec4(double x, double y, double 
 #define MPSE_NOTCONV    4u   // PPE iteration cap reached
 #define MPSE_NAN        8u   // non-finite value in a reduction
 
+// Entry masks of a neighbour row (bit k: entry k of the row; rows hold up to 128 entries).
+struct Mask {
+    unsigned long long lo, hi;
+};
+__host__ __device__ __forceinline__ Mask operator&(const Mask& a, const Mask& b) { return {a.lo & b.lo, a.hi & b.hi}; }
+#ifdef __CUDACC__
+__device__ __forceinline__ Mask maskNone() { return {0ull, 0ull}; }
+__device__ __forceinline__ Mask maskFirst(int c) {   // entries 0 .. c - 1
+    Mask m;
+    m.lo = c >= 64 ? ~0ull : ((1ull << c) - 1ull);
+    m.hi = c >= 128 ? ~0ull : (c > 64 ? ((1ull << (c - 64)) - 1ull) : 0ull);
+    return m;
+}
+__device__ __forceinline__ void maskSet(Mask& m, int k) {
+    if (k < 64) m.lo |= 1ull << k;
+    else m.hi |= 1ull << (k - 64);
+}
+__device__ __forceinline__ bool maskHas(const Mask& m, int k) {
+    return k < 64 ? ((m.lo >> k) & 1ull) != 0ull : ((m.hi >> (k - 64)) & 1ull) != 0ull;
+}
+__device__ __forceinline__ int maskCount(const Mask& m) { return __popcll(m.lo) + __popcll(m.hi); }
+// removes and returns the lowest entry (-1: none left)
+__device__ __forceinline__ int maskPop(Mask& m) {
+    if (m.lo) { const int k = __ffsll((long long)m.lo) - 1; m.lo &= m.lo - 1ull; return k; }
+    if (m.hi) { const int k = __ffsll((long long)m.hi) - 1; m.hi &= m.hi - 1ull; return k + 64; }
+    return -1;
+}
+#endif
+
 struct Dev {
     MpsParams P;
     int N0;            // capacity
@@ -104,7 +133,7 @@ struct Dev {
     double *cw, *cwd, *cwL;
     // per-particle entry masks after the wall pass: bit k set when entry k is inside the
     // reS (maskS) / reL (maskL) ball and not on the mirror side
-    unsigned long long *maskS, *maskL;
+    Mask *maskS, *maskL;
     int *nearList, *nearCount;      // fluid particles near the polygon wall (compacted)
     double reMax2;                  // list radius^2 = max(reS^2, reL^2)
     float bandHiS, bandHiL;         // FP32 prefilter upper bounds for the reS / reL balls
@@ -314,13 +343,21 @@ __device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col,
 }
 
 template <class F>
-__device__ __forceinline__ void forMask(const Dev& d, int i, unsigned long long m, F&& f) {
+__device__ __forceinline__ void forMask(const Dev& d, int i, Mask m, F&& f) {
     const int* row = d.nbr + i;
-    while (m) {
-        int k = __ffsll((long long)m) - 1;
-        m &= m - 1;
-        size_t e = (size_t)k * d.N0 + i;
-        f(ldStream(row + (size_t)k * d.N0), e);
+    unsigned long long w = m.lo;   // entries 0..63, then 64..127 (rarely any)
+    while (w) {
+        const int k = __ffsll((long long)w) - 1;
+        w &= w - 1ull;
+        const size_t e = (size_t)k * d.N0 + i;
+        f(ldStream(row + e - i), e);
+    }
+    w = m.hi;
+    while (w) {
+        const int k = __ffsll((long long)w) + 63;
+        w &= w - 1ull;
+        const size_t e = (size_t)k * d.N0 + i;
+        f(ldStream(row + e - i), e);
     }
 }
 

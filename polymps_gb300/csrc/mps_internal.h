@@ -113,7 +113,7 @@ struct PpeBuffers {
     unsigned int* bar;       // grid barrier of the persistent solvers: arrivals, generation, abort
     int pgridCg, pgridMx;    // co-resident grid sizes of the persistent solvers (0: unavailable)
     int prepared;            // FP32 copies (valf, diagf, diagInvf) already written by the assembly
-    unsigned long long* mfMask;   // per row: neighbour-list entries that are matrix entries
+    Mask* mfMask;            // per row: neighbour-list entries that are matrix entries
     int matfree;             // mixed inner operator: 0 assembled FP32, 1 matrix-free, 2 compact scaled,
                              // 3 staged tiles, 4 assembled FP32 with the pipelined inner CG
     int pgridMf;             // co-resident grid of the matrix-free mixed solver

@@ -443,8 +443,8 @@ __global__ void __launch_bounds__(BLK) k_pnd_npcd(Dev d) {
     const MpsParams& P = d.P;
     dvec4 pi = d.pos[i];
     double ni = 0.0, wSum = 0.0;
-    unsigned long long mL = d.maskL[i];
-    int nn = (INIT ? 0 : d.nNeighWall[i]) + __popcll(mL);
+    const Mask mL = d.maskL[i];
+    int nn = (INIT ? 0 : d.nNeighWall[i]) + maskCount(mL);
     dvec4 np = INIT ? make_dvec4(0, 0, 0, 0) : d.npcd[i];
     forMask(d, i, mL & d.maskS[i], [&](int j, size_t e) {
         dvec4 pj = d.pos[j];
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(BLK) k_pnd_diffusive(Dev d) {
     double Di = 0.0, DivV = 0.0;
     double cdiv = P.dim / P.pndSmallZero;
     double invNi = 1.0 / ni;
-    unsigned long long mL = d.maskL[i], mS = d.maskS[i] & mL;
+    const Mask mL = d.maskL[i], mS = d.maskS[i] & mL;
     const double* wLc = d.cwL ? d.cwL : d.cw;
     forMask(d, i, mL, [&](int j, size_t e) {
         dvec4 pj = d.pos[j];
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(BLK) k_pnd_diffusive(Dev d) {
             Di += P.timeStep / rho * P.coeffViscMultiphase * (d.press[j] - Pi - pgh) * wL;
         }
         int k = (int)((e - i) / d.N0);
-        if ((mS >> k) & 1ull) {
+        if (maskHas(mS, k)) {
             dvec4 vj = d.vel[j];
             double vx = vj.x - vi.x, vy = vj.y - vi.y, vz = vj.z - vi.z;
             double wd = d.cwd[e];   // wS / r^2
@@ -872,7 +872,7 @@ __global__ void __launch_bounds__(BLK) k_press_grad(Dev d) {
     dvec4 pi = d.pos[i];
     double Pi = d.press[i], pmin = Pi, ni = d.pndi[i];
     int gt = P.gradientType;
-    unsigned long long mS = d.maskS[i];
+    const Mask mS = d.maskS[i];
     if (gt == 0 || gt == 2) {
         forMask(d, i, mS, [&](int j, size_t e) {
             double pj_ = d.press[j];

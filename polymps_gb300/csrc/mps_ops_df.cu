@@ -78,13 +78,13 @@ __global__ void __launch_bounds__(128) k_side_masks_df(Dev d) {
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     int c = d.nbrCount[i];
-    unsigned long long all = (c >= 64) ? ~0ull : ((1ull << c) - 1ull);
+    const Mask all = maskFirst(c);
     dvec4 pi = d.pos[i];
     SideDF sc = sideDF(d, i, pi);
     bool fullS = P.reS2 >= d.reMax2, fullL = P.reL2 >= d.reMax2;
-    unsigned long long mS = all, mL = all;
+    Mask mS = all, mL = all;
     if (sc.check || !fullS || !fullL) {
-        mS = 0; mL = 0;
+        mS = maskNone(); mL = maskNone();
         float4 hi = d.posf[i], li = d.posLo[i];
         const df RS = K(d.k.reS2), RL = K(d.k.reL2);
         const int* row = d.nbr + i;
@@ -93,8 +93,8 @@ __global__ void __launch_bounds__(128) k_side_masks_df(Dev d) {
             float4 hj = d.posf[j], lj = d.posLo[j];
             df d2 = norm2(diff3(hj, lj, hi, li));
             if (!sideOkDF(d, sc, hj, lj, d2, i, j)) continue;
-            if (fullS || inBallDF(d, d2, RS, d.mgS, P.reS2, i, j)) mS |= 1ull << k;
-            if (fullL || inBallDF(d, d2, RL, d.mgL, P.reL2, i, j)) mL |= 1ull << k;
+            if (fullS || inBallDF(d, d2, RS, d.mgS, P.reS2, i, j)) maskSet(mS, k);
+            if (fullL || inBallDF(d, d2, RL, d.mgL, P.reL2, i, j)) maskSet(mL, k);
         }
     }
     d.maskS[i] = mS;
@@ -393,23 +393,22 @@ __global__ void __launch_bounds__(BLK) k_pnd_npcd_df(Dev d) {
     const MpsParams& P = d.P;
     float4 hi = d.posf[i], li = d.posLo[i];
     const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
-    unsigned long long mL = d.maskL[i];
-    int nn = d.nNeighWall[i] + __popcll(mL);
+    const Mask mL = d.maskL[i];
+    int nn = d.nNeighWall[i] + maskCount(mL);
     df ni = dfF(0.f), nx = ni, ny = ni, nz = ni;
     df m00 = dfF(0.f), m01 = m00, m02 = m00, m11 = m00, m12 = m00, m22 = m00;
     if (CORR) {
-        unsigned long long m = d.maskS[i];
+        Mask m = d.maskS[i];
         const int* row = d.nbr + i;
-        while (m) {
-            const int k = __ffsll((long long)m) - 1;
-            m &= m - 1;
+        int k;
+        while ((k = maskPop(m)) >= 0) {
             const int j = ldStream(row + (size_t)k * d.N0);
             PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
             WeightDF w = weightDF(q.d2, RS, P.weightType);
             df t0 = q.v.x * w.wr2, t1 = q.v.y * w.wr2, t2 = q.v.z * w.wr2;
             m00 += t0 * q.v.x; m01 += t0 * q.v.y; m02 += t0 * q.v.z;
             m11 += t1 * q.v.y; m12 += t1 * q.v.z; m22 += t2 * q.v.z;
-            if ((mL >> k) & 1ull) {
+            if (maskHas(mL, k)) {
                 ni += w.w;
                 nx += q.v.x * w.w; ny += q.v.y * w.w; nz += q.v.z * w.w;
             }
@@ -455,7 +454,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
     const MpsParams& P = d.P;
     int bci = d.bc[i];
     if (bci == P.other || bci == P.surface) {
-        B.diag[i] = 1.0; B.diagf[i] = 1.0f; B.diagInvf[i] = 1.0f; B.rowLen[i] = 0; B.b[i] = 0.0; B.mfMask[i] = 0ull;
+        B.diag[i] = 1.0; B.diagf[i] = 1.0f; B.diagInvf[i] = 1.0f; B.rowLen[i] = 0; B.b[i] = 0.0; B.mfMask[i] = maskNone();
         warpCount(d.counters + 1, 0u);
         return;
     }
@@ -465,7 +464,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
     const df gx = K(d.k.g[0]), gy = K(d.k.g[1]), gz = K(d.k.g[2]);
     df sum = dfF(0.f), src = dfF(0.f);
     int len = 0;
-    unsigned long long mm = 0ull;
+    Mask mm = maskNone();
     forMask(d, i, d.maskL[i], [&](int j, size_t e) {
         PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
         df wL = weightDF(q.d2, RL, P.weightType).w;
@@ -480,7 +479,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
                 B.valf[k] = mij.h;   // the FP32 copy of the mixed solver (hi part = fl32)
                 B.col[k] = j;
                 len++;
-                mm |= 1ull << ((e - i) / d.N0);
+                maskSet(mm, (int)((e - i) / d.N0));
             }
         }
     });
@@ -510,7 +509,7 @@ __global__ void __launch_bounds__(BLK) k_press_grad_df(Dev d) {
     df Pi = loadDF(d.pressDF, i), pmin = Pi;
     double ni = d.pndi[i];
     int gt = P.gradientType;
-    unsigned long long mS = d.maskS[i];
+    const Mask mS = d.maskS[i];
     if (gt == 0 || gt == 2) {
         forMask(d, i, mS, [&](int j, size_t) {
             df pj = loadDF(d.pressDF, j);

@@ -31,14 +31,14 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
     const MpsParams& P = d.P;
     int bci = d.bc[i];
     if (bci == P.other || bci == P.surface) {
-        B.diag[i] = 1.0; B.rowLen[i] = 0; B.b[i] = 0.0; B.mfMask[i] = 0ull;
+        B.diag[i] = 1.0; B.rowLen[i] = 0; B.b[i] = 0.0; B.mfMask[i] = maskNone();
         warpCount(d.counters + 1, 0u);
         return;
     }
     dvec4 pi = d.pos[i];
     double sum = 0.0, src = 0.0;
     int len = 0;
-    unsigned long long mm = 0ull;
+    Mask mm = maskNone();
     const double* wLc = d.cwL ? d.cwL : d.cw;
     forMask(d, i, d.maskL[i], [&](int j, size_t e) {
         double wL = wLc[e];
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
                 B.val[k] = mij;
                 B.col[k] = j;
                 len++;
-                mm |= 1ull << ((e - i) / d.N0);
+                maskSet(mm, (int)((e - i) / d.N0));
             }
         }
     });
@@ -664,20 +664,19 @@ __device__ __forceinline__ float mfWeight(float r2, float re, float invRe, int t
 }
 __device__ __forceinline__ float mfRowF(const Dev& d, const PpeBuffers& B, const float* z, int i, float cP, float re,
                                        float invRe, int wt) {
-    unsigned long long m = __ldg(B.mfMask + i);
+    Mask m = B.mfMask[i];
     const float4 hi = __ldg(d.posf + i), li = __ldg(d.posLo + i);
     const int* row = d.nbr + i;
     const size_t N0 = d.N0;
     float acc[8];
 #pragma unroll
     for (int u = 0; u < 8; u++) acc[u] = 0.f;
-    while (m) {
+    while (m.lo | m.hi) {
         int jj[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
-            int k = __ffsll((long long)m) - 1;
-            jj[u] = (m != 0ull) ? ldStream(row + (size_t)k * N0) : -1;
-            m &= m - 1ull;
+            const int k = maskPop(m);
+            jj[u] = (k >= 0) ? ldStream(row + (size_t)k * N0) : -1;
         }
 #pragma unroll
         for (int u = 0; u < 8; u++) {

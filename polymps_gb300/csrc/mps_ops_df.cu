@@ -73,7 +73,7 @@ void launchNeighborListDF(const Dev& d, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------ entry masks
-__global__ void __launch_bounds__(128) k_side_masks_df(Dev d) {
+__global__ void __launch_bounds__(128, 10) k_side_masks_df(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
@@ -387,7 +387,7 @@ void launchCorrectionMatrixDF(const Dev& d, cudaStream_t s) { k_corr_matrix_df<<
 // pair evaluation serves both; the PND sums take the entries also inside reL, in the same
 // ascending order as the plain sweep, so both results equal the separate kernels').
 template <bool CORR>
-__global__ void __launch_bounds__(BLK) k_pnd_npcd_df(Dev d) {
+__global__ void __launch_bounds__(BLK, 9) k_pnd_npcd_df(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
@@ -448,7 +448,7 @@ void launchPndNeighNpcdDF(const Dev& d, cudaStream_t s, bool withCorrection) {
 // ------------------------------------------------------------------ PPE assembly
 // MpsPressure::solvePressurePoissonPnd, src/MpsPressure.cpp:169-286 (matrix values are
 // assembled in float-float and stored in FP64)
-__global__ void __launch_bounds__(128) k_ppe_assemble_df(Dev d, PpeBuffers B) {
+__global__ void __launch_bounds__(128, 12) k_ppe_assemble_df(Dev d, PpeBuffers B) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
@@ -500,7 +500,7 @@ void launchPpeAssembleDF(const Dev& d, const PpeBuffers& B, cudaStream_t s) {
 
 // ------------------------------------------------------------------ pressure gradient
 // MpsPressure::calcPressGradient, src/MpsPressure.cpp:1217-1338
-__global__ void __launch_bounds__(BLK) k_press_grad_df(Dev d) {
+__global__ void __launch_bounds__(BLK, 9) k_press_grad_df(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;

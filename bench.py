@@ -316,9 +316,22 @@ def run_gb300(a, rank, world, local):
         "profile_ms": {k: round(v[0], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
         "last_step": {"ppe_iters": st.ppeIterations, "ppe_relres": st.ppeRelResidual, "velMax": st.velMax},
     }
+    g.close()
+    # the smooth start of the flow (steps 7-86, every second system) on a fresh simulation:
+    # extrapolated and learned starts gain most there
+    if a.ppe_compare and rank == 0 and a.ppe_steps == 0:
+        g2 = mps.MpsGpu(case, solver=solver, tol=1e-8, max_iter=20000, precision=prec)
+        if have_mlp:
+            w = np.load(mlp_path)
+            g2.mlp_set_weights(w["params"], w["norm"])
+        g2.set_solver(solver, warm, 1e-8, 20000)
+        g2.initialize()
+        g2.run(6)
+        out["ppe_early"] = ppe_compare(g2, abi, have_mlp, g2.params, (solver, warm, 1e-8, 20000), steps=80,
+                                       every=2, start=7)
+        g2.close()
     if rank == 0 and not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(case, a.cpu_steps)
-    g.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return out

@@ -301,3 +301,42 @@ def test_shifting_list_parity(oracle_mod, mps_lib, stype):
     compare(o, g, "shifting list %d" % stype, rtol=DF_RTOL)
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_DF32])
+def test_dense_rows_over_64_entries(oracle_mod, mps_lib, precision):
+    """Fluid compressed to 0.75 of its spacing (about 75 neighbours per particle, the second
+    word of the entry masks in use): bit-exact neighbour sets and one teacher-forced step
+    of every operator against the oracle."""
+    from polymps_gb300 import mps
+    from test_gpu_parity import FP64_RTOL
+    c = cases.config(3, jitter=0.02, scale=5.0)
+    o0 = oracle_mod.Oracle(c)
+    fluid = c.type == o0.params.fluid
+    o0.close()
+    pos = c.pos.copy()
+    ctr = pos[fluid].mean(axis=0)
+    pos[fluid] = ctr + 0.75 * (pos[fluid] - ctr)
+    c2 = cases.Case(c.name, c.params, c.type, pos, c.mesh)
+    o = oracle_mod.Oracle(c2)
+    g = mps.MpsGpu(c2, tol=1e-12, precision=precision)
+    o.set_solver(1e-12)
+    for ob in (o, g):
+        ob.run_op("UPDATE_BUCKETS")
+    co, no = o.neighbors()
+    cg, ng = g.neighbors()
+    assert co.max() > 64
+    assert np.array_equal(co, cg)
+    assert np.array_equal(no, ng)
+    o.initialize()
+    g.initialize()
+    o.set_velmax(0.0)
+    sync(o, g)
+    rtol = FP64_RTOL if precision == abi.PRECISION_FP64 else DF_RTOL
+    for op in step_ops(o.params):
+        o.run_op(op)
+        g.run_op(op)
+        compare(o, g, "dense op %s" % op, rtol=rtol)
+        sync(o, g)
+    g.close()
+    o.close()

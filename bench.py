@@ -10,12 +10,18 @@ the FP32/FP64 refinement solver and the learned warm start on the same systems.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
+The last stdout line is one JSON object of about 1.5 KB at most; the per-system PPE
+traces, the per-class profile and the longer CPU baseline go to the --detail file.
+
 Multi-GPU: the path is run as N independent replicas (one per rank, no collective on
-the data path); value = sum of particle-steps over ranks / max time over ranks.
+the data path); value = sum of particle-steps over ranks / max time over ranks.  With
+--gpus N > 1 and no torchrun environment, bench.py starts the N ranks itself (torchrun
+on 127.0.0.1, one GPU per rank).
 """
 import argparse
 import json
 import os
+import socket
 import subprocess
 import sys
 import threading
@@ -31,15 +37,10 @@ WORKLOADS = {2: "3D weakly compressible polygon dam break (cfg2)",
              3: "3D incompressible polygon dam break (cfg3)",
              5: "3D incompressible dam break with obstacle, collision and shifting (cfg5)"}
 HBM_FALLBACK = 6800.0
+LINE_MAX = 1500
 
 
-# DRAM bytes (read + write) per launch of the single-launch PPE solve over the 100 timed
-# steps of the default workload, from one ncu capture of exactly those launches
-# (dram__bytes_read.sum + dram__bytes_write.sum, profiles/k_mx_solve_cfg3-864k.md).
-MX_SOLVE_TRAFFIC = 4.814e9
-
-
-def args_():
+def args_(argv=None):
     a = argparse.ArgumentParser()
     a.add_argument("--gpus", type=int, default=1)
     a.add_argument("--steps", type=int, default=100)
@@ -55,15 +56,21 @@ def args_():
     a.add_argument("--config", type=int, default=3, choices=[2, 3, 5],
                    help="workload: 3 = 864k-particle incompressible dam break (the headline), "
                         "5 = 9.375M particles with obstacle and shifting, 2 = 108k weakly compressible")
-    a.add_argument("--e2e-steps", type=int, default=3)
+    a.add_argument("--e2e-steps", type=int, default=10)
+    a.add_argument("--fp64-steps", type=int, default=0,
+                   help="timed steps of the FP64 drop-in tier (0: as --steps)")
     a.add_argument("--no-cpu-baseline", action="store_true")
     a.add_argument("--cpu-steps", type=int, default=1)
     a.add_argument("--ppe-compare", type=int, default=1)
     a.add_argument("--ppe-steps", type=int, default=0,
                    help="steps the PPE comparison runs on (0: to the workload's configured length)")
+    a.add_argument("--ppe-options", action="store_true",
+                   help="also time the measured-and-rejected launch forms and inner operators")
+    a.add_argument("--detail", default=os.path.join(ROOT, "bench_detail.json"),
+                   help="file for the per-system PPE traces, the per-class profile and the long CPU baseline")
     a.add_argument("--presort", action="store_true",
                    help="number the input particles in bucket order (input renumbering only)")
-    return a.parse_args()
+    return a.parse_args(argv)
 
 
 def dist():
@@ -71,6 +78,22 @@ def dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def launch_ranks(n, argv):
+    """Re-run this script as n ranks under torchrun on this node (127.0.0.1); returns the
+    launcher's exit status.  Rank 0 prints the line."""
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(n),
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), os.path.abspath(__file__)] + argv
+    return subprocess.call(cmd)
 
 
 def peaks():
@@ -182,13 +205,34 @@ def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False, compact=False):
     return None
 
 
+def _timed_run(g, steps, world, rank, clocks=None):
+    """K steps bracketed by a barrier and a device synchronise on both sides; returns
+    (stats, wall seconds, launches)."""
+    import torch
+    from polymps_gb300 import mps, replicas
+    torch.cuda.synchronize()
+    replicas.barrier(world)
+    if clocks:
+        clocks.start()
+    l0 = mps.MpsGpu.launch_count()
+    t0 = time.perf_counter()
+    st = g.run(steps)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    launches = mps.MpsGpu.launch_count() - l0
+    replicas.barrier(world)
+    return st, wall, launches
+
+
 def run_gb300(a, rank, world, local):
     import torch
     from polymps_gb300 import abi, build, cases, mps, replicas
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device visible (the GB300 path has no CPU fallback)")
+    torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist_
-        dist_.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local)
+        dist_.init_process_group("nccl", device_id=torch.device("cuda", local))
     build.build()
     case = cases.config(a.config, scale=a.scale)
     N = case.n
@@ -202,77 +246,58 @@ def run_gb300(a, rank, world, local):
               "compact": abi.SOLVER_MIXED_COMPACT}[a.solver]
     mlp_path = os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz")
     have_mlp = os.path.exists(mlp_path)
-    use_mlp = a.warm == "mlp"
     prec = abi.PRECISION_DF32 if a.precision == "df32" else abi.PRECISION_FP64
-    g = mps.MpsGpu(case, solver=solver, tol=1e-8, max_iter=20000, precision=prec)
-    warm = {"prev": abi.WARM_PREVIOUS, "extrap": abi.WARM_EXTRAP}.get(a.warm, abi.WARM_EXTRAP2)
-    if have_mlp:
-        w = np.load(mlp_path)
-        g.mlp_set_weights(w["params"], w["norm"])
-    if use_mlp:
-        warm = abi.WARM_MLP
-    g.set_solver(solver, warm, 1e-8, 20000)
-    g.initialize()
+    warm = {"prev": abi.WARM_PREVIOUS, "extrap": abi.WARM_EXTRAP, "mlp": abi.WARM_MLP}.get(a.warm, abi.WARM_EXTRAP2)
+
+    def handle(precision, solver_, warm_):
+        g = mps.MpsGpu(case, solver=solver_, tol=1e-8, max_iter=20000, precision=precision)
+        if have_mlp:
+            w = np.load(mlp_path)
+            g.mlp_set_weights(w["params"], w["norm"])
+        g.set_solver(solver_, warm_, 1e-8, 20000)
+        g.initialize()
+        return g
+
+    g = handle(prec, solver, warm)
     g.run(a.warmup)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
     clocks = Clocks(local)
-    clocks.start()
     g.profile(True)
-    l0 = mps.MpsGpu.launch_count()
-    t0 = time.perf_counter()
-    st = g.run(a.steps)
-    wall = time.perf_counter() - t0
-    launches = mps.MpsGpu.launch_count() - l0
+    st, wall, launches = _timed_run(g, a.steps, world, rank, clocks)
+    clk = clocks.stop()
     prof = g.profile_get()
     g.profile(False)
-    clk = clocks.stop()
-    torch.cuda.synchronize()
     # replicas: particle-steps of all ranks over the slowest rank's device time
     units, dev_s = replicas.aggregate(N * a.steps, st.stepMs / 1e3, world, device="cuda")
-    replicas.barrier(world)
     value = units / dev_s
 
-    # state of the end of the timed run, uploaded every step of the end-to-end section from
-    # page-locked host arrays (and the results read back into page-locked arrays)
-    def pinned_like(a):
-        t = torch.empty(a.size, dtype=torch.float64).pin_memory()
-        v = t.numpy().reshape(a.shape)
-        v[...] = a
+    # e2e through the C ABI with host arrays: the state of the end of the timed run is
+    # uploaded every step from page-locked host arrays, stepped, and read back into them
+    def pinned_like(x):
+        t = torch.empty(x.size, dtype=torch.float64).pin_memory()
+        v = t.numpy().reshape(x.shape)
+        v[...] = x
         return v, t
     host, keep = {}, []
     for f in (abi.F_POS, abi.F_VEL, abi.F_PRESS, abi.F_PRESSPPE):
         v, t = pinned_like(g.get(f))
         host[f] = v
         keep.append(t)
-    # e2e through the C ABI with host arrays: upload the state from pinned host memory,
-    # step, download the result, every step
     h2d = sum(v.nbytes for v in host.values())
     d2h = h2d   # the step's state comes back: positions, velocities, pressure and the unclamped solution
     torch.cuda.synchronize()
+    replicas.barrier(world)
     t0 = time.perf_counter()
     for _ in range(a.e2e_steps):
         for f, v in host.items():
             g.set(f, v)
         g.step()
-        g.get(abi.F_POS, out=host[abi.F_POS])
-        g.get(abi.F_VEL, out=host[abi.F_VEL])
-        g.get(abi.F_PRESS, out=host[abi.F_PRESS])
-        g.get(abi.F_PRESSPPE, out=host[abi.F_PRESSPPE])
+        for f in host:
+            g.get(f, out=host[f])
     e2e_s = time.perf_counter() - t0
     e2e_units, e2e_s = replicas.aggregate(N * a.e2e_steps, e2e_s, world, device="cuda")
     e2e = e2e_units / e2e_s
 
-    # PPE time-to-1e-8 on identical systems along the rest of the run: plain FP64 vs mixed vs
-    # warm starts
-    ppe = None
-    if a.ppe_compare and rank == 0:
-        done = a.warmup + a.steps + a.e2e_steps   # steps taken so far (initialisation is step 0)
-        steps = a.ppe_steps if a.ppe_steps > 0 else max(getattr(case, "steps", 1000) - done, 40)
-        ppe = ppe_compare(g, abi, have_mlp, g.params, (solver, warm, 1e-8, 20000), steps=steps,
-                          every=max(1, steps // 36), start=done)
-    # dominant class and its roofline
+    # dominant class of the per-class profile and its roofline
     hbm, hbm_src = peaks()
     E, Z = st.nbrEntries, max(st.ppeNnz - N, 0)
     mixed = solver != abi.SOLVER_PLAIN_FP64
@@ -285,14 +310,50 @@ def run_gb300(a, rank, world, local):
                        solver == abi.SOLVER_MIXED_COMPACT)
         if b:
             ach = b / (ms / calls / 1e3) / 1e9
-            traffic = None
-            if (dom == "PPE_SOLVE" and a.config == 3 and a.scale == 1.0 and a.solver == "mixed"
-                    and a.precision == "df32" and a.warm in ("auto", "extrap2") and a.steps == 100 and a.warmup == 5):
-                traffic = MX_SOLVE_TRAFFIC
             roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
-                    "frac": round(ach / hbm, 4), "peak_source": hbm_src, "traffic": traffic,
-                    "algo_bytes_per_launch": int(b), "launch_ms": round(ms / calls, 4),
-                    "share_of_step": round(ms / st.stepMs, 3)}
+                    "frac": round(ach / hbm, 4), "peak_source": hbm_src, "traffic": None,
+                    "algo_bytes": int(b), "launch_ms": round(ms / calls, 4),
+                    "share": round(ms / st.stepMs, 3)}
+    iters = st.runPpeIterations / max(st.runPpeSolves, 1)
+    detail = {"profile_ms": {k: [round(v[0], 3), v[1]] for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
+              "timed_run": {"wall_s": round(wall, 3), "ppe_iters_per_solve": round(iters, 2),
+                            "ppe_refinements_per_solve": round(st.runPpeRefinements / max(st.runPpeSolves, 1), 2),
+                            "last_relres": st.ppeRelResidual, "velMax": st.velMax}}
+
+    # the FP64 drop-in tier (every pair in FP64, plain FP64 PPE from the previous solution)
+    # on the same workload
+    ppe_done = a.warmup + a.steps + a.e2e_steps
+    fp64 = None
+    if not (a.precision == "fp64" and a.solver == "plain"):
+        g64 = handle(abi.PRECISION_FP64, abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS)
+        g64.run(max(3, min(a.warmup, 5)))
+        k64 = a.fp64_steps or a.steps
+        st64, _, _ = _timed_run(g64, k64, world, rank)
+        u64, s64 = replicas.aggregate(N * k64, st64.stepMs / 1e3, world, device="cuda")
+        fp64 = {"value": round(u64 / s64, 1), "ms_per_step": round(st64.stepMs / k64, 3), "steps": k64}
+        g64.close()
+
+    # PPE time-to-1e-8 on identical systems along the rest of the run
+    ppe = ppe_early = None
+    if a.ppe_compare and rank == 0 and case.params.get("mpsType", 2) == 2:
+        steps = a.ppe_steps if a.ppe_steps > 0 else max(getattr(case, "steps", 1000) - ppe_done, 40)
+        ppe = ppe_compare(g, abi, have_mlp, g.params, (solver, warm, 1e-8, 20000), steps=steps,
+                          every=max(1, steps // 36), start=ppe_done, options=a.ppe_options)
+    g.close()
+    # the smooth start of the flow (steps 7-86, every second system) on a fresh simulation:
+    # extrapolated and learned starts gain most there
+    if a.ppe_compare and rank == 0 and a.ppe_steps == 0 and case.params.get("mpsType", 2) == 2:
+        g2 = handle(prec, solver, warm)
+        g2.run(6)
+        ppe_early = ppe_compare(g2, abi, have_mlp, g2.params, (solver, warm, 1e-8, 20000), steps=80, every=2,
+                                start=7)
+        g2.close()
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        cpu, cpu_more = cpu_baseline(case, a.cpu_steps)
+        detail["cpu_baseline_more"] = cpu_more
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": "particle-steps/s", "n_gpus": world,
@@ -300,41 +361,46 @@ def run_gb300(a, rank, world, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": ("df32" if prec == abi.PRECISION_DF32 else "f64") + ("+f32/f64 PPE" if mixed else "+f64 PPE"),
         "data": "synthetic",
-        "config": {"workload": WORKLOADS[a.config], "particles": N,
-                   "l0": case.params["partDist"], "dt": case.params["timeStep"],
+        "config": {"workload": WORKLOADS[a.config], "particles": N, "l0": case.params["partDist"],
                    "ppe_tol": 1e-8, "solver": a.solver, "precision": a.precision,
-                   "warm_start": {abi.WARM_MLP: "learned", abi.WARM_EXTRAP: "extrapolated",
-                                  abi.WARM_EXTRAP2: "quadratic extrapolation", abi.WARM_PREVIOUS: "previous"}[warm],
+                   "warm_start": {abi.WARM_MLP: "learned", abi.WARM_EXTRAP: "linear", abi.WARM_EXTRAP2: "quadratic",
+                                  abi.WARM_PREVIOUS: "previous"}[warm],
                    "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "working set > L2 (no flush needed)", "wall_s": round(wall, 3)},
+                   "l2": "working set > L2, no flush"},
         "e2e": {"value": round(e2e, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "steps": a.e2e_steps},
+                "d2h_bytes_per_step": int(d2h)},
+        "value_fp64": fp64,
         "roofline": roof,
         "clocks": clk,
         "gpu_launches": int(launches),
-        "ppe": ppe,
-        "profile_ms": {k: round(v[0], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
-        "last_step": {"ppe_iters": st.ppeIterations, "ppe_relres": st.ppeRelResidual, "velMax": st.velMax},
+        "ppe": _ppe_summary(ppe, ppe_early),
+        "cpu_baseline": cpu,
     }
-    g.close()
-    # the smooth start of the flow (steps 7-86, every second system) on a fresh simulation:
-    # extrapolated and learned starts gain most there
-    if a.ppe_compare and rank == 0 and a.ppe_steps == 0:
-        g2 = mps.MpsGpu(case, solver=solver, tol=1e-8, max_iter=20000, precision=prec)
-        if have_mlp:
-            w = np.load(mlp_path)
-            g2.mlp_set_weights(w["params"], w["norm"])
-        g2.set_solver(solver, warm, 1e-8, 20000)
-        g2.initialize()
-        g2.run(6)
-        out["ppe_early"] = ppe_compare(g2, abi, have_mlp, g2.params, (solver, warm, 1e-8, 20000), steps=80,
-                                       every=2, start=7)
-        g2.close()
-    if rank == 0 and not a.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(case, a.cpu_steps)
-    if world > 1:
-        torch.distributed.destroy_process_group()
+    if rank == 0:
+        detail.update({"line": out, "ppe": ppe, "ppe_early": ppe_early})
+        try:
+            with open(a.detail, "w") as f:
+                json.dump(detail, f, indent=1)
+            out["detail"] = os.path.relpath(a.detail, ROOT)
+        except OSError:
+            pass
     return out
+
+
+def _ppe_summary(ppe, early):
+    """Mean PPE time-to-1e-8 of the plain FP64 CG and each variant's speed-up over it."""
+    if not ppe:
+        return None
+    keep = ("quadratic_extrapolated_fp32_fp64", "learned_fp32_fp64", "fp32_fp64_refinement",
+            "extrapolated_fp32_fp64")
+    s = {"systems": ppe["systems"], "steps": ppe["steps_sampled"], "plain_fp64_ms": ppe["plain_fp64"]["ms"],
+         "plain_fp64_iters": ppe["plain_fp64"]["iters"],
+         "speedup_vs_plain": {k: ppe[k]["speedup_vs_plain"] for k in keep if k in ppe},
+         "max_rel_err_vs_plain": max(ppe[k].get("rel_err_vs_fp64_max", 0.0) for k in keep if k in ppe)}
+    if early:
+        s["early"] = {"systems": early["systems"], "plain_fp64_ms": early["plain_fp64"]["ms"],
+                      "speedup_vs_plain": {k: early[k]["speedup_vs_plain"] for k in keep if k in early}}
+    return s
 
 
 def _hist_get(g, abi):
@@ -356,7 +422,7 @@ def _solve(g, abi, hist, solver, warm, mode=1):
             "relres": st.ppeRelResidual, "relres0": st.ppeInitialRelResidual}
 
 
-def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4, start=0):
+def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4, start=0, options=False):
     """PPE time-to-1e-8 of the solvers and warm starts on the same systems, sampled along
     `steps` further steps of the run (every `every`-th system): each sampled system is
     solved by every variant from the same warm-start state, then the step is finished
@@ -370,20 +436,21 @@ def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4, start=0):
         after += ["WALL_PRESS_GRADIENT", "WALL_VISCOSITY"]
     after += ["CORRECT", "OUT_OF_DOMAIN"] + (["SHIFTING"] if params.shiftingType else []) + ["OUT_OF_DOMAIN"]
     main = [("plain_fp64", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS),
-            ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP),
-            ("plain_fp64_quadratic_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP2),
             ("fp32_fp64_refinement", abi.SOLVER_MIXED, abi.WARM_PREVIOUS),
             ("extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP),
             ("quadratic_extrapolated_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_EXTRAP2)]
     if use_mlp:
         main.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP))
-    # launch-form and inner-operator options: first sampled system only (best of three)
-    alt = [("quadratic_fp32_fp64_staged_tiles", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 2),
+    # launch-form and inner-operator options (measured and not the default): first sampled
+    # system only (best of three), with --ppe-options
+    alt = [("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, 1),
+           ("plain_fp64_quadratic_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP2, 1),
+           ("quadratic_fp32_fp64_staged_tiles", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 2),
            ("quadratic_fp32_fp64_pipelined", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 3),
            ("quadratic_compact_fp32_fp64", abi.SOLVER_MIXED_COMPACT, abi.WARM_EXTRAP2, 1),
            ("quadratic_matfree_fp32_fp64", abi.SOLVER_MIXED_MATFREE, abi.WARM_EXTRAP2, 1),
            ("plain_fp64_per_kernel_launch", abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, 0),
-           ("quadratic_fp32_fp64_per_kernel_launch", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 0)]
+           ("quadratic_fp32_fp64_per_kernel_launch", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 0)] if options else []
     samples = {k: [] for k, _, _ in main}
     trace = []
     alt_res = {}
@@ -433,9 +500,10 @@ def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4, start=0):
         res[k]["speedup_vs_plain"] = round(base / res[k]["ms"], 3) if res[k]["ms"] > 0 else None
     for k, v in alt_res.items():
         v["speedup_vs_plain"] = round(samples["plain_fp64"][0]["ms"] / v["ms"], 3) if v["ms"] > 0 else None
-    res["options_first_system"] = alt_res
+    if alt_res:
+        res["options_first_system"] = alt_res
     res["systems"] = len(samples["plain_fp64"])
-    res["steps_sampled"] = "every %d-th step of steps %d-%d of the run" % (every, start, start + steps - 1)
+    res["steps_sampled"] = "every %d-th of steps %d-%d" % (every, start, start + steps - 1)
     # the flow's phases differ: early systems are smooth in time (extrapolated starts gain
     # most), later ones carry particle-scale pressure noise
     half = len(trace) // 2
@@ -448,63 +516,51 @@ def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4, start=0):
     return res
 
 
-def cpu_baseline(case, steps):
-    """The FP64 CPU oracle (a restatement of the reference path; the reference itself
-    cannot be built here) on the host cores: a bounded sample of `steps` steps."""
+def _oracle_steps(case, threads, steps, tol=1e-8):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # the checker / CPU baseline
-    cores = os.cpu_count() or 1
-    o = oracle.Oracle(case, threads=cores)
-    o.set_solver(1e-8)
+    o = oracle.Oracle(case, threads=threads)
+    o.set_solver(tol)
     o.initialize()
     t0 = time.perf_counter()
     for _ in range(steps):
         o.step()
     dt = time.perf_counter() - t0
     o.close()
-    out = {"value": round(case.n * steps / dt, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
-           "sample": "%d step(s) of the %d-particle workload after initialisation (%.1f s)" % (steps, case.n, dt)}
-    # the same sample on one host thread
-    o = oracle.Oracle(case, threads=1)
-    o.set_solver(1e-8)
-    o.initialize()
-    t0 = time.perf_counter()
-    o.step()
-    d1 = time.perf_counter() - t0
-    o.close()
-    out["single_thread"] = {"value": round(case.n / d1, 1), "cores": 1,
-                            "sample": "1 step of the %d-particle workload (%.1f s)" % (case.n, d1)}
-    # the 2D particle-wall dam break (1,922 particles) run to its configured 200 steps
+    return dt
+
+
+def cpu_baseline(case, steps):
+    """The FP64 CPU oracle (a restatement of the reference path; the reference itself
+    cannot be built here) on the host cores: a bounded sample of `steps` steps of the same
+    workload on all cores, and one step on one core.  Returns (line entry, longer record)."""
     from polymps_gb300 import cases
+    cores = os.cpu_count() or 1
+    dt = _oracle_steps(case, cores, steps)
+    d1 = _oracle_steps(case, 1, 1)
+    out = {"value": round(case.n * steps / dt, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
+           "sample": "%d step(s) of the %d-particle workload after initialisation (%.1f s)" % (steps, case.n, dt),
+           "single_thread": round(case.n / d1, 1)}
+    more = {"single_thread_sample": "1 step (%.1f s)" % d1}
+    # the 2D particle-wall dam break run to its configured 200 steps, and a window of the
+    # 3D weakly compressible dam break (108,000 particles)
     c1 = cases.config(1)
-    full = {}
+    more["full_run_2d_particle_walls"] = {"particles": c1.n, "steps": c1.steps}
     for th in (cores, 1):
-        o = oracle.Oracle(c1, threads=th)
-        o.set_solver(1e-8)
-        o.initialize()
-        t0 = time.perf_counter()
-        for _ in range(c1.steps):
-            o.step()
-        d = time.perf_counter() - t0
-        o.close()
-        full["threads_%d" % th] = {"s": round(d, 3), "value": round(c1.n * c1.steps / d, 1)}
-    out["full_run_2d_particle_walls"] = {"particles": c1.n, "steps": c1.steps, **full}
-    # a fixed window of the 3D weakly compressible dam break (108,000 particles), all threads
+        d = _oracle_steps(c1, th, c1.steps)
+        more["full_run_2d_particle_walls"]["threads_%d" % th] = {"s": round(d, 3),
+                                                                 "value": round(c1.n * c1.steps / d, 1)}
     c2 = cases.config(2)
-    o = oracle.Oracle(c2, threads=cores)
-    o.set_solver(1e-8)
-    o.initialize()
-    t0 = time.perf_counter()
-    for _ in range(5):
-        o.step()
-    d = time.perf_counter() - t0
-    o.close()
-    out["window_3d_weakly_compressible"] = {"particles": c2.n, "steps": 5, "s": round(d, 3),
-                                            "value": round(c2.n * 5 / d, 1), "cores": cores}
-    return out
+    d = _oracle_steps(c2, cores, 5)
+    more["window_3d_weakly_compressible"] = {"particles": c2.n, "steps": 5, "s": round(d, 3),
+                                             "value": round(c2.n * 5 / d, 1), "cores": cores}
+    return out, more
 
 
 def run_reference(a, rank, world):
+    """The reference arm: the reference's own CPU implementation of the path cannot be
+    built here (its Eigen, libigl and nlohmann/json submodules are empty), so its FP64
+    restatement (the oracle port) is timed on all host cores, rank 0 only."""
     if rank != 0:
         return None
     from polymps_gb300 import cases
@@ -534,23 +590,41 @@ def run_reference(a, rank, world):
     return {"metric": METRIC, "value": round(v, 1), "unit": "particle-steps/s", "n_gpus": world, "steps": k,
             "warmup": w, "ms_per_step": round(dt / k * 1e3, 1), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": WORKLOADS[a.config], "particles": case.n,
-                       "ppe_tol": 1e-8},
+            "config": {"workload": WORKLOADS[a.config], "particles": case.n, "ppe_tol": 1e-8},
             "cpu_baseline": {"value": round(v, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
                              "sample": "%d timed step(s) after %d warm-up step(s)" % (k, w)},
             "e2e": {"value": round(v, 1), "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 
 
-def main():
-    a = args_()
+def compact(out):
+    """The printed line: drop optional detail until it fits in LINE_MAX bytes."""
+    s = json.dumps(out, separators=(",", ":"))
+    for key in (("ppe", "early"), ("clocks", "samples"), ("cpu_baseline", "sample"), ("roofline", "peak_source")):
+        if len(s) <= LINE_MAX:
+            break
+        d = out.get(key[0])
+        if isinstance(d, dict):
+            d.pop(key[1], None)
+        s = json.dumps(out, separators=(",", ":"))
+    return s
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    a = args_(argv)
     rank, world, local = dist()
+    if "WORLD_SIZE" not in os.environ and a.gpus > 1:
+        sys.exit(launch_ranks(a.gpus, argv))
+    if "WORLD_SIZE" in os.environ and world != a.gpus:
+        sys.exit("bench.py: --gpus %d but WORLD_SIZE=%d: launch one rank per GPU (torchrun --nproc-per-node %d)"
+                 % (a.gpus, world, a.gpus))
     if a.impl == "reference":
         out = run_reference(a, rank, world)
     else:
         out = run_gb300(a, rank, world, local)
     if rank == 0 and out is not None:
-        print(json.dumps(out))
+        print(compact(out), flush=True)
 
 
 if __name__ == "__main__":

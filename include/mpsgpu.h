@@ -75,9 +75,9 @@ typedef struct MpsParams {
     double reRepulsiveForce, expectMaxVelocity;
     double repForceCoefMitsume, repForceCoefLennardJones, repForceCoefMonaghanKajtar;
     double EPS_RE;
-    int    freeSurfType;        /* 0 PND+neigh, 1 PND+NPCD (2 ARC: not supported)     */
+    int    freeSurfType;        /* 0 PND+neigh, 1 PND+NPCD, 2 ARC (normals + arc test) */
     double pndThreshold, neighThreshold, npcdThreshold, thetaThreshold, normThreshold;
-    int    collisionType;       /* 0 PC (1 DPC: not supported)                         */
+    int    collisionType;       /* 0 PC, 1 DPC (src/main.cpp:285-290); others rejected */
     double collisionRatio, distLimitRatio, lambdaCollision;
     int    ghost, fluid, wall, dummyWall;   /* particle type IDs                        */
     int    surface, inner, other;           /* boundary type IDs                        */
@@ -200,6 +200,14 @@ typedef struct mpsgpu_s* mpsgpu_t;
  * Host only (no GPU needed).  pos3 (N x 3) is only read for particle walls
  * (calcDomainLimits with limitTypeBC 0). */
 int mpsgpu_params_derive(MpsParams* p, int n, const double* pos3);
+
+/* Host-only check (no GPU needed) of the input switches against the implemented path:
+ * 0, or MPSGPU_ERR_UNSUPPORTED with mpsgpu_last_error(NULL) naming the JSON switch and
+ * the reason (deformable/forced meshes, periodic domains, non-Newtonian rheology,
+ * relax_fact < 1, unknown solver/collision/wall types).  mpsgpu_create makes the same
+ * check.  Replaces the reference's silent acceptance of switches it marks "NOT WORKING"
+ * (input/InputDamINC.json flags). */
+int mpsgpu_check_params(const MpsParams* p);
 
 /* Upload a particle system: replaces MpsInputOutput::readMpsParticleFile's arrays
  * (src/MpsInputOutput.cpp:645-857) plus PolygonMesh::initPolygonMesh/readPolygonMeshFile
@@ -348,8 +356,12 @@ int mpsgpu_launch_count(long long* n);
  * system whose arrays (rowptr[n+1], col/val[nnz], b[n], x[n]) are DEVICE pointers; x holds
  * the initial guess on entry and the solution on return.  All work vectors live in one
  * file-scope device array of MPSGPU_STATIC_MAX_ROWS rows (about 5.3 MB per device),
- * reserved at library load: the call makes no device allocation.  Rules:
+ * reserved when the library's device code is loaded on a device (at the latest by the
+ * first call there): the call itself makes no device allocation.  Rules:
  *  - n must be 1..MPSGPU_STATIC_MAX_ROWS, otherwise MPSGPU_ERR_ARG;
+ *  - every row needs a stored non-zero diagonal entry (Jacobi scaling); otherwise the
+ *    call returns MPSGPU_ERR_ARG naming the first such row, with x untouched;
+ *  - b = 0 gives x = 0, 0 iterations and relres 0 (Eigen's CG returns the same);
  *  - each call clears the array's control words itself; nothing needs zeroing first;
  *  - the array is shared by every call on a device: calls that overlap on the GPU
  *    (two streams, two host threads) race and corrupt each other;

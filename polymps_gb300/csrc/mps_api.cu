@@ -210,13 +210,28 @@ static void ensureMasks(mpsgpu_t h) {
     h->masksValid = true;
 }
 
-static int unsupported(const MpsParams& P) {
-    if (P.femOn || P.forcedOn) return 1;
-    if (P.domainTypeBC != 0) return 1;
-    if (P.fluidType != 0) return 1;
-    if (P.collisionType != 0 && P.collisionType != 1) return 1;
-    if (P.solverType != 0 && P.solverType != 1) return 1;
-    if (P.relaxPress < 1.0) return 1;
+// Switches of the reference outside the implemented path, each with the reason.
+static const char* unsupportedReason(const MpsParams& P) {
+    if (P.femOn || P.forcedOn) return "fem_MESH / forced_MESH: deformable and forced meshes are not supported";
+    if (P.domainTypeBC != 0) return "domain.boundary.type != 0: periodic domains are not supported";
+    if (P.fluidType != 0) return "physical.fluid_type != 0: non-Newtonian rheology is not supported";
+    if (P.collisionType != 0 && P.collisionType != 1)
+        return "particle_collision.type: only 0 (PC) and 1 (DPC) are supported";
+    if (P.solverType != 0 && P.solverType != 1)
+        return "semi_implicit_mps.solver_type: only 0 (CG) and 1 (BiCGSTAB) are supported";
+    if (P.relaxPress < 1.0)
+        return "gradient.relax_fact < 1: the prediction-step pressure gradient is not supported";
+    if (P.wallType != 0 && P.wallType != 1) return "wall_type: only 0 (particles) and 1 (polygon) are supported";
+    if (P.mpsType < 0 || P.mpsType > 3) return "mps_type: only 0 to 3 are supported";
+    return nullptr;
+}
+
+int mpsgpu_check_params(const MpsParams* p) {
+    if (!p) { g_lastError = "bad argument"; return MPSGPU_ERR_ARG; }
+    if (const char* why = unsupportedReason(*p)) {
+        g_lastError = std::string("configuration outside the implemented path: ") + why;
+        return MPSGPU_ERR_UNSUPPORTED;
+    }
     return 0;
 }
 
@@ -612,7 +627,7 @@ int mpsgpu_abi_sizes(int* params, int* stats, int* mesh) {
 int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3, const double* vel3,
                   const double* press, const MpsMesh* mesh, mpsgpu_t* out) {
     if (!p || !p->derived || n <= 0 || !type || !pos3 || !out) { g_lastError = "bad argument"; return MPSGPU_ERR_ARG; }
-    if (unsupported(*p)) { g_lastError = "configuration outside the implemented path"; return MPSGPU_ERR_UNSUPPORTED; }
+    if (int e = mpsgpu_check_params(p)) return e;
     if (p->wallType == 1 && (!mesh || mesh->ntri <= 0 || !mesh->tri_xyz)) { g_lastError = "polygon walls need a mesh"; return MPSGPU_ERR_ARG; }
     if (mesh && mesh->ntri > (1 << 26)) { g_lastError = "mesh too large"; return MPSGPU_ERR_UNSUPPORTED; }
     int ndev = 0;

@@ -27,7 +27,7 @@
 #define SMAX MPSGPU_STATIC_MAX_ROWS
 
 // layout in doubles: r, z, p, Ap, inverse diagonal (SMAX each), block partials (3 per block),
-// scalars (16), control words (counter, flags) as unsigned ints in the last 4 doubles
+// scalars (16), control words (counter, flags; 8 unsigned ints) in the last 4 doubles
 #define OFF_R 0
 #define OFF_Z (1ull * SMAX)
 #define OFF_P (2ull * SMAX)
@@ -47,7 +47,8 @@ namespace {
 
 struct View {
     double *r, *z, *p, *Ap, *dinv, *part, *scal;
-    unsigned int* ctrl;   // [0] block counter, [1] done, [2] iterations, [3] breakdown
+    unsigned int* ctrl;   // [0] block counter, [1] done, [2] iterations, [3] breakdown,
+                          // [4] UINT_MAX - (lowest row without a usable diagonal), 0 if none
 };
 __host__ __device__ inline View viewOf(double* S) {
     View v;
@@ -102,10 +103,15 @@ __global__ void __launch_bounds__(SBLK) k_s_init(int n, const int* rowptr, const
     View w = viewOf(S);
     double v[3] = {0, 0, 0};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double diag = 1.0;
+        double diag = 0.0;
         for (int k = rowptr[i]; k < rowptr[i + 1]; k++)
             if (col[k] == i) diag = val[k];
-        double di = 1.0 / diag;
+        // a row without a stored non-zero diagonal cannot be Jacobi-scaled: record the
+        // lowest such row (as UINT_MAX - row, so atomicMax keeps the lowest) and leave the
+        // solve to the host, which rejects the system before any iteration runs
+        double di = 0.0;
+        if (diag != 0.0 && diag == diag) di = 1.0 / diag;
+        else atomicMax(&w.ctrl[4], 0xFFFFFFFFu - (unsigned int)i);
         double r = b[i] - rowDot(rowptr, col, val, x, i);
         double z = r * di;
         w.dinv[i] = di; w.r[i] = r; w.z[i] = z; w.p[i] = z;
@@ -119,6 +125,7 @@ __global__ void __launch_bounds__(SBLK) k_s_init(int n, const int* rowptr, const
         w.ctrl[1] = (t[2] == 0.0 || t[1] < thr) ? 1u : 0u;
         w.ctrl[2] = 0u;
         if (!(t[0] == t[0]) || !(t[1] == t[1])) { w.ctrl[1] = 1u; w.ctrl[3] = 1u; }
+        if (*(volatile unsigned int*)&w.ctrl[4]) w.ctrl[1] = 1u;   // malformed system: no iteration
     });
 }
 __global__ void __launch_bounds__(SBLK) k_s_spmv(int n, const int* rowptr, const int* col, const double* val, double* S) {
@@ -213,37 +220,60 @@ extern "C" int mpsgpu_pcg_solve_static(int n, const int* rowptr, const int* col,
     if (e) return e;
     cudaStream_t s = (cudaStream_t)stream;
     View w = viewOf(S);
+    auto fail = [](const char* what, cudaError_t err) {
+        g_msg = std::string("mpsgpu_pcg_solve_static: ") + what + ": " + cudaGetErrorString(err);
+        return MPSGPU_ERR_CUDA;
+    };
     // the array keeps the previous call's contents: reset the block counter and flags
-    if (cudaMemsetAsync(w.ctrl, 0, 4 * sizeof(unsigned int), s) != cudaSuccess) { g_msg = "memset"; return MPSGPU_ERR_CUDA; }
+    cudaError_t ce = cudaMemsetAsync(w.ctrl, 0, 8 * sizeof(unsigned int), s);
+    if (ce != cudaSuccess) return fail("clearing the control words", ce);
     int nb = (n + SBLK - 1) / SBLK;
     if (nb > SBLOCKS) nb = SBLOCKS;
     k_s_init<<<nb, SBLK, 0, s>>>(n, rowptr, col, val, b, x, S, tol);
-    unsigned int ctrl[4] = {0, 0, 0, 0};
+    if ((ce = cudaGetLastError()) != cudaSuccess) return fail("launch", ce);
+    unsigned int ctrl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double scal[16];
+    // the set-up's verdict before any iteration: a malformed system is rejected with x
+    // untouched; a zero right-hand side has the solution x = 0 (as Eigen's CG returns)
+    if ((ce = cudaMemcpyAsync(ctrl, w.ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(scal, w.scal, sizeof(scal), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (ce = cudaStreamSynchronize(s)) != cudaSuccess)
+        return fail("set-up", ce);
+    if (ctrl[4]) {
+        g_msg = "mpsgpu_pcg_solve_static: row " + std::to_string(0xFFFFFFFFu - ctrl[4]) +
+                " has no stored non-zero diagonal entry (Jacobi preconditioning needs one in every row)";
+        return MPSGPU_ERR_ARG;
+    }
+    if (scal[SC_BB] == 0.0) {
+        if ((ce = cudaMemsetAsync(x, 0, sizeof(double) * (size_t)n, s)) != cudaSuccess ||
+            (ce = cudaStreamSynchronize(s)) != cudaSuccess)
+            return fail("zeroing x", ce);
+        if (iters) *iters = 0;
+        if (relres) *relres = 0.0;
+        return 0;
+    }
     int launched = 0;
     const int batch = 8;
-    while (true) {
+    while (!ctrl[1]) {
         for (int k = 0; k < batch; k++) {
             k_s_spmv<<<nb, SBLK, 0, s>>>(n, rowptr, col, val, S);
             k_s_update<<<nb, SBLK, 0, s>>>(n, x, S, (unsigned int)max_iter);
             k_s_p<<<nb, SBLK, 0, s>>>(n, S);
         }
         launched += batch;
-        if (cudaMemcpyAsync(ctrl, w.ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-            cudaStreamSynchronize(s) != cudaSuccess) {
-            g_msg = std::string("mpsgpu_pcg_solve_static: ") + cudaGetErrorString(cudaGetLastError());
-            return MPSGPU_ERR_CUDA;
-        }
-        if (ctrl[1] || launched >= max_iter) break;
+        if ((ce = cudaGetLastError()) != cudaSuccess) return fail("launch", ce);
+        if ((ce = cudaMemcpyAsync(ctrl, w.ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+            (ce = cudaStreamSynchronize(s)) != cudaSuccess)
+            return fail("polling", ce);
+        if (launched >= max_iter) break;
     }
     k_s_residual<<<nb, SBLK, 0, s>>>(n, rowptr, col, val, b, x, S);
-    double scal[16];
-    if (cudaMemcpyAsync(scal, w.scal, sizeof(scal), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-        g_msg = "mpsgpu_pcg_solve_static: residual";
-        return MPSGPU_ERR_CUDA;
-    }
+    if ((ce = cudaGetLastError()) != cudaSuccess) return fail("launch", ce);
+    if ((ce = cudaMemcpyAsync(scal, w.scal, sizeof(scal), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (ce = cudaStreamSynchronize(s)) != cudaSuccess)
+        return fail("residual read-back", ce);
     if (iters) *iters = (int)ctrl[2];
-    if (relres) *relres = scal[SC_BB] > 0 ? std::sqrt(scal[SC_RR0] / scal[SC_BB]) : 0.0;
+    if (relres) *relres = std::sqrt(scal[SC_RR0] / scal[SC_BB]);
     if (ctrl[3] || ctrl[1] != 1u) { g_msg = "mpsgpu_pcg_solve_static: did not reach the tolerance"; return MPSGPU_ERR_NOT_CONVERGED; }
     return 0;
 }

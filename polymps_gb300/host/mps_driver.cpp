@@ -4,7 +4,10 @@
 // progress line of displayInfo every 100 iterations and writes .vtu/.pvd output every
 // iter_output iterations.
 //
-//   mps_gb300 <input.json> [--max-steps N] [--no-output]
+//   mps_gb300 <input.json> [--max-steps N] [--no-output] [--check-input params.bin]
+// --check-input parses the JSON, .grid and .stl, derives the constants and checks the
+// switches on the host only (no GPU), writes the MpsParams as read (before derivation)
+// as raw bytes to the given file, prints one status line and exits with the status code.
 // Without an argument the input name is read from stdin relative to input/ with .json
 // appended, as the reference does (src/MpsInputOutput.cpp:89-109).
 #include <chrono>
@@ -33,9 +36,11 @@ int main(int argc, char** argv) {
     std::string json;
     long long maxSteps = -1;
     bool output = true;
+    std::string checkPath;
     for (int a = 1; a < argc; a++) {
         if (!std::strcmp(argv[a], "--max-steps") && a + 1 < argc) maxSteps = std::atoll(argv[++a]);
         else if (!std::strcmp(argv[a], "--no-output")) output = false;
+        else if (!std::strcmp(argv[a], "--check-input") && a + 1 < argc) checkPath = argv[++a];
         else json = argv[a];
     }
     if (json.empty()) {
@@ -47,11 +52,25 @@ int main(int argc, char** argv) {
     CaseInput c;
     std::string err;
     double t0 = now();
-    if (int e = readInputFile(json, c, err)) {
-        std::fprintf(stderr, "%s\n", err.c_str());
-        return e;
-    }
+    int rc = readInputFile(json, c, err);
     int n = (int)c.type.size();
+    if (!checkPath.empty()) {
+        // the parameters as read (before derivation scales the radii and sets the domain)
+        if (FILE* f = std::fopen(checkPath.c_str(), "wb")) {
+            std::fwrite(&c.params, sizeof(MpsParams), 1, f);
+            std::fclose(f);
+        }
+        MpsParams d = c.params;
+        if (!rc && (rc = mpsgpu_params_derive(&d, n, c.pos.data())) != 0) err = mpsgpu_last_error(nullptr);
+        if (!rc && (rc = mpsgpu_check_params(&d)) != 0) err = mpsgpu_last_error(nullptr);
+        std::printf("check-input status %d particles %d triangles %d: %s\n", rc, n, (int)(c.tri.size() / 9),
+                    rc ? err.c_str() : "ok");
+        return rc;
+    }
+    if (rc) {
+        std::fprintf(stderr, "%s\n", err.c_str());
+        return rc;
+    }
     mpsgpu_t h = nullptr;
     TRY(mpsgpu_params_derive(&c.params, n, c.pos.data()));
     MpsMesh mesh{(int)(c.tri.size() / 9), c.tri.data()};

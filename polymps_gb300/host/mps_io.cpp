@@ -269,7 +269,11 @@ int readInputFile(const std::string& jsonPath, CaseInput& c, std::string& err) {
                           : (w == "extrapolate")  ? MPSGPU_WARM_EXTRAPOLATE
                           : (w == "extrapolate2") ? MPSGPU_WARM_EXTRAPOLATE2
                                                   : MPSGPU_WARM_PREVIOUS;
-        c.gpu.tol = num(g, "tol", 1e-8);
+        const JVal* t = g->at("tol");
+        if (t && t->kind == JVal::STR && t->str == "eigen")
+            c.gpu.tol = 2.220446049250313e-16;   // Eigen's default: the machine epsilon
+        else
+            c.gpu.tol = num(g, "tol", 1e-8);
         c.gpu.maxIter = (int)num(g, "max_iter", 0);
         c.gpu.mlpWeights = text(g, "mlp_weights", "");
     }

@@ -17,6 +17,9 @@ struct OutputFlags {
 struct GpuOptions {               // optional "gpu" section (new knobs, no reference counterpart)
     int solver = MPSGPU_SOLVER_PLAIN_FP64;
     int warmStart = MPSGPU_WARM_PREVIOUS;
+    // PPE relative tolerance: 1e-8 unless the JSON says otherwise; "eigen" selects Eigen's
+    // default, the machine epsilon, which the reference runs with (it never calls
+    // setTolerance: src/MpsPressure.cpp:427 is commented out)
     double tol = 1e-8;
     int maxIter = 0;
     std::string mlpWeights;       // .bin: MPSGPU_MLP_NPARAM + 32 floats

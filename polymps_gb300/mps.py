@@ -24,6 +24,7 @@ EXPORTS = [
     "mpsgpu_mlp_gradient", "mpsgpu_stream", "mpsgpu_last_error", "mpsgpu_abi_sizes",
     "mpsgpu_profile", "mpsgpu_profile_get", "mpsgpu_profile_name", "mpsgpu_launch_count",
     "mpsgpu_last_stats", "mpsgpu_pcg_solve_static", "mpsgpu_pcg_static_error", "mpsgpu_write_vtu",
+    "mpsgpu_check_params",
 ]
 PROF_NCLASS = len(abi.OPS) + 6
 
@@ -45,6 +46,7 @@ def lib(path=None):
     L = C.CDLL(path)
     vp, P = C.c_void_p, C.POINTER
     L.mpsgpu_params_derive.argtypes = [P(abi.MpsParams), C.c_int, P(C.c_double)]
+    L.mpsgpu_check_params.argtypes = [P(abi.MpsParams)]
     L.mpsgpu_create.argtypes = [P(abi.MpsParams), C.c_int, P(C.c_int), P(C.c_double), P(C.c_double),
                                 P(C.c_double), P(abi.MpsMesh), P(vp)]
     for f in ("mpsgpu_destroy", "mpsgpu_initialize", "mpsgpu_mlp_fit_normalization"):

@@ -231,9 +231,13 @@ def test_mixed_precision_solver(oracle_mod, mps_lib):
         o.run_op(op); g.run_op(op); sync(o, g)
     o.run_op("CALC_PRESS")
     g.run_op("CALC_PRESS")
-    st = g.step()   # a full mixed step must also converge
+    st = g.last_stats()
     assert st.ppeRelResidual <= 1e-8
     assert st.ppeRefinements >= 1
+    assert relerr(g.get(abi.F_PRESSPPE), o.get(abi.F_PRESSPPE)) < 1e-6
+    assert relerr(g.get(abi.F_PRESS), o.get(abi.F_PRESS)) < 1e-6
+    st = g.step()   # a full mixed step must also converge
+    assert st.ppeRelResidual <= 1e-8
 
 
 def _bf16(x):

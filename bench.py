@@ -33,9 +33,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s"
-WORKLOADS = {2: "3D weakly compressible polygon dam break (cfg2)",
-             3: "3D incompressible polygon dam break (cfg3)",
-             5: "3D incompressible dam break with obstacle, collision and shifting (cfg5)"}
+WORKLOADS = {2: "3D WC polygon dam break, 108k (cfg2)",
+             3: "3D INC polygon dam break, 864k (cfg3)",
+             5: "3D INC dam break + obstacle, collision, shifting, 9.4M (cfg5)"}
 HBM_FALLBACK = 6800.0
 LINE_MAX = 1500
 
@@ -119,7 +119,7 @@ class Clocks:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -160,7 +160,7 @@ class Clocks:
 # Algorithmic bytes per call of each timed class (each distinct element read or written
 # once; neighbour re-reads assumed cache resident).  N particles, E neighbour entries,
 # Z off-diagonal PPE non-zeros; df = float-float tier (hi/lo FP32 copies, no weight cache).
-def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False, compact=False):
+def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False, compact=False, own=False):
     if cls == "PPE_SOLVE" and st is not None and st.runPpeSolves:
         # one launch = one whole solve; per call averages of the timed run
         it = st.runPpeIterations / st.runPpeSolves
@@ -174,6 +174,12 @@ def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False, compact=False):
             # inner iteration with the matrix-free operator: neighbour index per entry; mask,
             # diagonal, own hi/lo position, z, Ap, p per row; update as below
             return it * (96 * N + 4 * Z) + (rf + 1) * (80 * N + 12 * Z)
+        if mixed and own:
+            # block-owned rows (x_f, r_f, p, Ap in shared memory): inner iteration = SpMV
+            # (valf + col per entry; z, diag, len per row) + update (M^-1 read, z written);
+            # per refinement: FP64 residual (val + col per entry; b, x, r, diag, len per row),
+            # x update (x read and written), inner start (r, M^-1 read, z written)
+            return it * (20 * N + 8 * Z) + (rf + 1) * (68 * N + 12 * Z)
         if mixed:
             # inner FP32 iteration: SpMV (valf + col per entry; diag, len, z, Ap, p per row)
             # + update (x_f, p, r_f, Ap, M^-1, z per row); per refinement: FP64 residual
@@ -203,6 +209,13 @@ def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False, compact=False):
     if cls == "COLLISION":
         return N * (32 + 32 + 32 + 4 + 32) + 4 * E + (N * 64 if df else 0)
     return None
+
+
+def owned_rows(n, sms=152):
+    """Whether the mixed solve runs with block-owned rows (the library's rule: rows per
+    block, with a quarter of headroom, within the 13,824 rows a block keeps in shared memory)."""
+    per = (n * 5 // 4 + sms - 1) // sms + 64
+    return min(13824, max(1024, (per + 31) // 32 * 32)) * sms >= n
 
 
 def _timed_run(g, steps, world, rank, clocks=None):
@@ -260,10 +273,11 @@ def run_gb300(a, rank, world, local):
 
     g = handle(prec, solver, warm)
     g.run(a.warmup)
+    # clocks are sampled from the start of the timed run to the end of the FP64 tier's
+    # timed run (both timed regions; the end-to-end steps lie between them)
     clocks = Clocks(local)
     g.profile(True)
     st, wall, launches = _timed_run(g, a.steps, world, rank, clocks)
-    clk = clocks.stop()
     prof = g.profile_get()
     g.profile(False)
     # replicas: particle-steps of all ranks over the slowest rank's device time
@@ -307,7 +321,7 @@ def run_gb300(a, rank, world, local):
     if dom:
         ms, calls = leaf[dom]
         b = algo_bytes(dom, N, E, Z, mixed, prec == abi.PRECISION_DF32, st, solver == abi.SOLVER_MIXED_MATFREE,
-                       solver == abi.SOLVER_MIXED_COMPACT)
+                       solver == abi.SOLVER_MIXED_COMPACT, own=owned_rows(N))
         if b:
             ach = b / (ms / calls / 1e3) / 1e9
             roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
@@ -332,6 +346,7 @@ def run_gb300(a, rank, world, local):
         u64, s64 = replicas.aggregate(N * k64, st64.stepMs / 1e3, world, device="cuda")
         fp64 = {"value": round(u64 / s64, 1), "ms_per_step": round(st64.stepMs / k64, 3), "steps": k64}
         g64.close()
+    clk = clocks.stop()
 
     # PPE time-to-1e-8 on identical systems along the rest of the run
     ppe = ppe_early = None
@@ -388,18 +403,21 @@ def run_gb300(a, rank, world, local):
 
 
 def _ppe_summary(ppe, early):
-    """Mean PPE time-to-1e-8 of the plain FP64 CG and each variant's speed-up over it."""
+    """Mean PPE time-to-1e-8 of the plain FP64 CG (previous-step start) and each FP32/FP64
+    refinement variant's speed-up over it, by warm start: quadratic or linear
+    extrapolation, learned, previous step."""
     if not ppe:
         return None
-    keep = ("quadratic_extrapolated_fp32_fp64", "learned_fp32_fp64", "fp32_fp64_refinement",
-            "extrapolated_fp32_fp64")
+    keep = {"quadratic": "quadratic_extrapolated_fp32_fp64", "learned": "learned_fp32_fp64",
+            "previous": "fp32_fp64_refinement", "linear": "extrapolated_fp32_fp64"}
     s = {"systems": ppe["systems"], "steps": ppe["steps_sampled"], "plain_fp64_ms": ppe["plain_fp64"]["ms"],
          "plain_fp64_iters": ppe["plain_fp64"]["iters"],
-         "speedup_vs_plain": {k: ppe[k]["speedup_vs_plain"] for k in keep if k in ppe},
-         "max_rel_err_vs_plain": max(ppe[k].get("rel_err_vs_fp64_max", 0.0) for k in keep if k in ppe)}
+         "speedup_vs_plain": {k: ppe[v]["speedup_vs_plain"] for k, v in keep.items() if v in ppe},
+         "max_rel_err_vs_plain": max(ppe[v].get("rel_err_vs_fp64_max", 0.0) for v in keep.values() if v in ppe)}
     if early:
-        s["early"] = {"systems": early["systems"], "plain_fp64_ms": early["plain_fp64"]["ms"],
-                      "speedup_vs_plain": {k: early[k]["speedup_vs_plain"] for k in keep if k in early}}
+        s["early"] = {"systems": early["systems"], "steps": early["steps_sampled"],
+                      "plain_fp64_ms": early["plain_fp64"]["ms"],
+                      "speedup_vs_plain": {k: early[v]["speedup_vs_plain"] for k, v in keep.items() if v in early}}
     return s
 
 
@@ -443,7 +461,8 @@ def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4, start=0, op
         main.append(("learned_fp32_fp64", abi.SOLVER_MIXED, abi.WARM_MLP))
     # launch-form and inner-operator options (measured and not the default): first sampled
     # system only (best of three), with --ppe-options
-    alt = [("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, 1),
+    alt = [("quadratic_fp32_fp64_grid_stride", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 4),
+           ("plain_fp64_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP, 1),
            ("plain_fp64_quadratic_extrapolated", abi.SOLVER_PLAIN_FP64, abi.WARM_EXTRAP2, 1),
            ("quadratic_fp32_fp64_staged_tiles", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 2),
            ("quadratic_fp32_fp64_pipelined", abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 3),
@@ -503,7 +522,7 @@ def ppe_compare(g, abi, use_mlp, params, default, steps=40, every=4, start=0, op
     if alt_res:
         res["options_first_system"] = alt_res
     res["systems"] = len(samples["plain_fp64"])
-    res["steps_sampled"] = "every %d-th of steps %d-%d" % (every, start, start + steps - 1)
+    res["steps_sampled"] = "%d-%d every %d" % (start, start + steps - 1, every)
     # the flow's phases differ: early systems are smooth in time (extrapolated starts gain
     # most), later ones carry particle-scale pressure noise
     half = len(trace) // 2
@@ -539,7 +558,7 @@ def cpu_baseline(case, steps):
     dt = _oracle_steps(case, cores, steps)
     d1 = _oracle_steps(case, 1, 1)
     out = {"value": round(case.n * steps / dt, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
-           "sample": "%d step(s) of the %d-particle workload after initialisation (%.1f s)" % (steps, case.n, dt),
+           "sample": "%d step(s) of this workload after init (%.1f s)" % (steps, dt),
            "single_thread": round(case.n / d1, 1)}
     more = {"single_thread_sample": "1 step (%.1f s)" % d1}
     # the 2D particle-wall dam break run to its configured 200 steps, and a window of the

@@ -247,13 +247,16 @@ int mpsgpu_set_solver(mpsgpu_t h, int solver, int warm_start, double tol, int ma
  * run their FP64 kernels in either mode. */
 /* How the PPE solve is launched: 0 one launch per kernel with the host polling
  * convergence every few iterations; 1 (default) the whole solve in one cooperative launch
- * with device-side grid barriers; 2 as 1, with the mixed solver's FP32 matrix streamed
- * through shared memory by bulk copies (measured slower than 1 at 864k rows: the SpMV
- * is bound by the neighbour gathers of z, not by the matrix stream); 3 as 1, with the
+ * with device-side grid barriers (the mixed solver with every block owning one contiguous,
+ * work-balanced range of rows and keeping its FP32 inner-CG vectors in shared memory, where
+ * the rows fit: up to 13,824 rows per SM); 2 as 1, with the mixed solver's FP32 matrix
+ * streamed through shared memory by bulk copies (measured slower than 1 at 864k rows: the
+ * SpMV is bound by the neighbour gathers of z, not by the matrix stream); 3 as 1, with the
  * mixed solver's inner CG in the pipelined form (one grid reduction per iteration instead
  * of two, Ghysels & Vanroose 2014) and the refinement residual formed in the same pass as
- * the iterate update.  Same method and results to the solver tolerance.
- * Modes 1 to 3 fall back to the previous modes where the device does not support them. */
+ * the iterate update; 4 as 1 with grid-stride rows and every solver vector in global
+ * memory.  Same method and results to the solver tolerance.
+ * Modes 1 to 4 fall back to the previous modes where the device does not support them. */
 int mpsgpu_set_ppe_launch(mpsgpu_t h, int mode);
 
 #define MPSGPU_PRECISION_FP64  0

@@ -251,22 +251,31 @@ static int calcPress(mpsgpu_t h) {
     else launchPpeAssemble(h->d, h->B, h->s);
     if (h->prof.on) h->prof.end(h->s);
     cudaEventRecord(h->ea1, h->s);
-    // warm start: previous unclamped solution (reference), zero, or the learned predictor
+    // the solve's time includes its warm start's generation, whichever it is
+    cudaEventRecord(h->es0, h->s);
+    // warm start: previous unclamped solution (reference), zero, extrapolated, or the
+    // learned predictor
     if (h->warm == MPSGPU_WARM_ZERO) cudaMemsetAsync(h->B.x, 0, sizeof(double) * h->N0, h->s);
     if (h->warm == MPSGPU_WARM_EXTRAPOLATE || h->warm == MPSGPU_WARM_EXTRAPOLATE2) {
         launchWarmExtrapolate(h->d, h->B, h->s, h->warm == MPSGPU_WARM_EXTRAPOLATE2);
         countLaunch(1);
     }
-    cudaEventRecord(h->es0, h->s);
     h->B.prepared = df32(h) ? 1 : 0;   // the DF32 assembly writes the FP32 copies itself
+    // the block-owned mixed solve takes the learned start's residual-minimising step itself
+    const bool ownSolve = h->solver == MPSGPU_SOLVER_MIXED && h->persistent == 1 && !h->B.ownOff &&
+                          h->B.pgridOwn > 0 && h->B.ownCap > 0 && P.solverType != 1;
+    h->B.cdir = nullptr;
     if (h->warm == MPSGPU_WARM_MLP) {
         if (h->prof.on) h->prof.begin(PROF_PPE_OTHER, h->s);
         // the learned start reads the FP32 copy of the matrix
         if (!h->B.prepared) { launchMixedPrepare(h->d, h->B, h->s); h->B.prepared = 1; countLaunch(1); }
-        int e = mlpWarmStart(h->mlp, h->d, h->B, h->s);
+        int e = mlpWarmStart(h->mlp, h->d, h->B, h->s, ownSolve);
         if (h->prof.on) h->prof.end(h->s);
-        countLaunch(9);   // x_e copy, residual, features, scale, forward, correction, step dot products, step, apply
+        // x_e and its FP32 copy, residual with the scale's partials, scale, fused forward; or
+        // x_e copy, residual, features, scale, forward, correction, step dot products, step, apply
+        countLaunch(ownSolve ? 4 : 9);
         if (e) return e;
+        if (ownSolve) h->B.cdir = h->mlp.cdir;
     } else if (h->warm == MPSGPU_WARM_PREVIOUS) {
         cudaMemcpyAsync(h->B.x, h->d.pressPPE, sizeof(double) * h->N0, cudaMemcpyDeviceToDevice, h->s);
     }
@@ -849,6 +858,20 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         A(B.sgs, n);
         A(B.wideRow, n);
         A(B.bar, 96);   // three 128-byte lines of barrier words
+        // solver vectors in shared memory: a block's rows are its grid-stride rounds, at
+        // most n / (G BS) + 1 of them per thread (the remainder is split over the blocks)
+        B.pgridOwn = ppePersistentGrid(7);
+        if (B.pgridOwn > 0) {
+            const long long slots = ((long long)n / ((long long)B.pgridOwn * 1024) + 1) * 1024;
+            if (slots <= OWN_CAP_ROWS) B.ownCap = (int)slots;
+            else B.pgridOwn = 0;
+        }
+        B.pgridOwn64 = ppePersistentGrid(8);
+        if (B.pgridOwn64 > 0) {
+            const long long slots = ((long long)n / ((long long)B.pgridOwn64 * 768) + 1) * 768;
+            if (slots <= OWN64_CAP_ROWS) B.ownCap64 = (int)slots;
+            else B.pgridOwn64 = 0;
+        }
     }
 #undef A
     // upload the particle state (src/MpsInputOutput.cpp:759-856 initial values)
@@ -963,8 +986,9 @@ int mpsgpu_set_precision(mpsgpu_t h, int precision) {
 }
 
 int mpsgpu_set_ppe_launch(mpsgpu_t h, int mode) {
-    if (!h || mode < 0 || mode > 3) return MPSGPU_ERR_ARG;
-    h->persistent = mode;
+    if (!h || mode < 0 || mode > 4) return MPSGPU_ERR_ARG;
+    h->persistent = mode == 4 ? 1 : mode;
+    h->B.ownOff = mode == 4 ? 1 : 0;
     return 0;
 }
 

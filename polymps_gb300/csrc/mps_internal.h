@@ -130,6 +130,14 @@ struct PpeBuffers {
     int pgridPipe;
     double* bs[4];           // BiCGSTAB: shadow residual r0, s, M^-1 s, A M^-1 s
     int pgridBi;             // co-resident grid of the BiCGSTAB solver
+    // solver vectors in shared memory (mixed: x_f, r_f, p, Ap; plain FP64: r, p, Ap): the
+    // grid (one block per SM; 0: unavailable), the row slots per block, and 1 to keep every
+    // vector in global memory instead
+    int pgridOwn, ownCap, ownOff;
+    int pgridOwn64, ownCap64;
+    // learned warm start: the network's correction c of the start x (nullptr: none); the
+    // shared-memory mixed solver takes the residual-minimising step x + theta c in its set-up
+    const float* cdir;
 };
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);
@@ -146,6 +154,10 @@ int ppeSolveMixed(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cu
 int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol, int maxIter, cudaStream_t s,
                        int* iters, int* refinements, double* relres, double* relres0, Prof* prof);
 int ppePersistentGrid(int mixed);
+// row slots per block of the shared-memory solvers at most (a multiple of their block sizes,
+// 1024 mixed, 768 plain FP64)
+#define OWN_CAP_ROWS 13312
+#define OWN64_CAP_ROWS 8448
 // BiCGSTAB (solver_type 1) in one cooperative launch
 int ppeSolveBicgstab(const Dev& d, const PpeBuffers& B, double tol, int maxIter, cudaStream_t s, int* iters,
                      double* relres, double* relres0, Prof* prof);

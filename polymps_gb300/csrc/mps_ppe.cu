@@ -1081,6 +1081,241 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
     qStore(B, qL);
 }
 
+// ------------------------------------------------------------------ shared-memory vectors
+// The mixed solver with the FP32 inner-CG vectors of each block's rows (x, r, p, Ap: 16
+// bytes per row) in shared memory from the first inner iteration to the last; only z, the
+// vector every block gathers through the matrix columns, goes through global memory.  A
+// block's rows are those of the grid-stride rounds (RowSet: at any moment all blocks
+// stream adjacent slices of the column-major ELL arrays, which measured 28% faster than one
+// contiguous range per block), and the m-th row of thread t sits at slot m BS + t of the
+// block's vectors.  The vector pass of an iteration is then shared-memory work plus one
+// coalesced store of z.
+#define OWN_CAPMAX OWN_CAP_ROWS   // slots per block: 4 x 13312 x 4 B = 208 KB of shared memory
+
+// FP64 row products A x and A c of one row in one pass over its entries (c FP32); only
+// the set-up pass of a learned start calls it, so it stays out of line (the inner loop's
+// registers are not shared with it)
+__device__ __noinline__ void qRow2(const PpeBuffers& B, const double* x, const float* cv, int i, int len,
+                                      double& ax, double& ac) {
+    double a1[4] = {0.0, 0.0, 0.0, 0.0}, a2[4] = {0.0, 0.0, 0.0, 0.0};
+    const double* v = B.val + i;
+    const int* col = B.col + i;
+    const size_t N0 = B.N0;
+    for (int k = 0; k < len; k += 4) {
+        int cc[4];
+        double vv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const bool ok = k + u < len;
+            cc[u] = ok ? ldStream(col + (size_t)(k + u) * N0) : i;
+            vv[u] = ok ? ldStream(v + (size_t)(k + u) * N0) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            a1[u] += vv[u] * x[cc[u]];
+            a2[u] += vv[u] * (double)cv[cc[u]];
+        }
+    }
+    const double dg = __ldg(B.diag + i);
+    ax = dg * x[i] + ((a1[0] + a1[1]) + (a1[2] + a1[3]));
+    ac = dg * (double)cv[i] + ((a2[0] + a2[1]) + (a2[2] + a2[3]));
+}
+
+// The thread's rows of a RowSet with their shared-memory slot l = m BS + t (m-th row of the
+// thread), f(l, i, len) with the next row's length prefetched; forOwnL without the length.
+template <class F>
+__device__ __forceinline__ void forRowsL(const PpeBuffers& B, const RowSet& s, F&& f) {
+    const int cnt = rowCount(s);
+    int i = cnt > 0 ? rowAt(s, 0) : 0;
+    int len = cnt > 0 ? __ldg(B.rowLen + i) : 0;
+    for (int m = 0; m < cnt; m++) {
+        const int in = (m + 1 < cnt) ? rowAt(s, m + 1) : -1;
+        const int ln = in >= 0 ? __ldg(B.rowLen + in) : 0;
+        f(m * (int)blockDim.x + (int)threadIdx.x, i, len);
+        i = in;
+        len = ln;
+    }
+}
+template <class F>
+__device__ __forceinline__ void forOwnL(const RowSet& s, F&& f) {
+    const int cnt = rowCount(s);
+    for (int m = 0; m < cnt; m++) f(m * (int)blockDim.x + (int)threadIdx.x, rowAt(s, m));
+}
+
+// Set-up of the shared-memory mixed solve: FP64 residual of the warm start, ||r||^2 and
+// ||b||^2 and the solver scalars; with a learned correction c (B.cdir) also q = A c, the
+// dot products r.q and q.q, the residual-minimising step theta = r.q / q.q (the start
+// x + theta c is never worse than x in the residual norm; its residual norm follows
+// algebraically) and the update of x and r.  The learned form is called out of line, so the
+// inner loop's registers are not shared with it.  Returns false when a barrier wait ran out.
+template <bool LEARNED>
+__device__ __forceinline__ bool mxSetup(const PpeBuffers& B, const RowSet& rs, QCtl& c, QLocal& qL, double tol,
+                                        double eta2) {
+    double* const qS = qL.scal;
+    int* const qF = qL.flag;
+    const float* const cd = B.cdir;
+    double v[LEARNED ? 4 : 2] = {};
+    forRows(B, rs, [&](int i, int len) {
+        const double bi = B.b[i];
+        double ax, ac = 0.0;
+        if (LEARNED) qRow2(B, B.x, cd, i, len, ax, ac);
+        else ax = qRow(B, B.x, i, len);
+        const double r = bi - ax;
+        B.r[i] = r;
+        v[0] += r * r;
+        v[1] += bi * bi;
+        if (LEARNED) { B.Ap[i] = ac; v[LEARNED ? 2 : 0] += r * ac; v[LEARNED ? 3 : 0] += ac * ac; }
+    });
+    if (!qSum<LEARNED ? 4 : 2>(v, B, c, [&](const double* t) {
+            double th = 0.0, rr = t[0];
+            if (LEARNED) {
+                const double rq = t[LEARNED ? 2 : 0], qq = t[LEARNED ? 3 : 0];
+                th = (qq > 0.0 && rq == rq) ? rq / qq : 0.0;
+                rr = fmax(t[0] - th * rq, 0.0);
+            }
+            qS[S_OMEGA] = th;
+            qS[S_RR] = rr;
+            qS[S_BB] = t[1];
+            double thr = tol * tol * t[1];
+            if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
+            qS[S_THR] = thr;
+            qS[S_SCALE] = sqrt(rr / (t[1] > 0 ? t[1] : 1.0));
+            qS[S_SQRT] = sqrt(rr);
+            qS[S_INV] = 1.0 / sqrt(rr);
+            qS[S_ETA2] = fmax(eta2, 0.25 * thr / rr);
+            qF[0] = (t[1] == 0.0 || rr < thr) ? 1 : 0;
+            qF[1] = 0;
+            qF[3] = 0;
+            if (!(rr == rr)) { qF[0] = 1; qF[2] = 1; }
+        }))
+        return false;
+    if (LEARNED) {   // x += theta c, r -= theta q on the thread's own rows
+        const double th = vd(qS + S_OMEGA);
+        forOwn(rs, [&](int i) {
+            B.x[i] += th * (double)cd[i];
+            B.r[i] -= th * B.Ap[i];
+        });
+    }
+    return true;
+}
+
+__device__ __noinline__ bool mxSetupLearned(const PpeBuffers& B, const RowSet& rs, QCtl& c, QLocal& qL, double tol,
+                                            double eta2) {
+    return mxSetup<true>(B, rs, c, qL, tol, eta2);
+}
+
+template <bool LEARNED>
+__global__ void __launch_bounds__(QBX, 1) k_mx_own(Dev d, PpeBuffers B, double tol, int maxIter, double eta2, int cap) {
+    __shared__ QLocal qL;   // this block's copy of the solver scalars and flags
+    qInit(qL);
+    double* const qS = qL.scal;
+    int* const qF = qL.flag;
+    extern __shared__ __align__(128) unsigned char dynSmem[];
+    float* const sx = reinterpret_cast<float*>(dynSmem);   // inner correction x_f
+    float* const sr = sx + cap;                             // inner residual
+    float* const sp = sr + cap;                             // search direction
+    float* const sap = sp + cap;                            // A p
+    const int n = liveN(d);
+    const RowSet rs = rowSet(n, QBX);   // this thread's rows (rowCount(rs) * QBX <= cap)
+    QCtl c = {0u};
+    if (!(LEARNED ? mxSetupLearned(B, rs, c, qL, tol, eta2) : mxSetup<false>(B, rs, c, qL, tol, eta2))) return;
+    int total = 0, refine = 0;
+    while (!vi(qF) && total < maxIter && refine <= 20) {
+        {   // inner start: r_f = r / ||r||, z = M^-1 r_f, x_f = 0
+            const double inv = vd(qS + S_INV);
+            df a[2] = {dfF(0.f), dfF(0.f)};
+            forOwnL(rs, [&](int l, int i) {
+                const float r = (float)(B.r[i] * inv);
+                const float z = r * __ldg(B.diagInvf + i);
+                sr[l] = r; sx[l] = 0.f;
+                B.zf[i] = z;
+                a[0] += prod2(r, z);
+                a[1] += prod2(r, r);
+            });
+            if (!qSumDF<2>(a, B, c, [&](const double* t) { qS[S_RZ] = t[0]; qS[S_RR0] = t[1]; qF[3] = 0; }))
+                return;
+        }
+        int inner = 0;
+        while (true) {
+            {   // Ap = A z + beta Ap, p = z + beta p, p.Ap
+                const float beta = inner ? (float)vd(qS + S_BETA) : 0.f;
+                df a[1] = {dfF(0.f)};
+                forRowsL(B, rs, [&](int l, int i, int len) {
+                    const float q = qRowF(B, B.zf, i, len);
+                    const float z = B.zf[i];
+                    const float ap = inner ? q + beta * sap[l] : q;
+                    const float p = inner ? z + beta * sp[l] : z;
+                    sap[l] = ap; sp[l] = p;
+                    a[0] += prod2(p, ap);
+                });
+                if (!qSumDF<1>(a, B, c, [&](const double* t) { qS[S_PAP] = t[0]; qS[S_ALPHA] = qS[S_RZ] / t[0]; }))
+                    return;
+            }
+            {   // x_f += alpha p, r -= alpha Ap, z = M^-1 r; r.z, r.r
+                const float alpha = (float)vd(qS + S_ALPHA);
+                df a[2] = {dfF(0.f), dfF(0.f)};
+                const int cnt = rowCount(rs);
+                for (int m0 = 0; m0 < cnt; m0 += 4) {
+                    float mi[4];
+                    int ii[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        ii[u] = (m0 + u < cnt) ? rowAt(rs, m0 + u) : -1;
+                        mi[u] = (ii[u] >= 0) ? __ldg(B.diagInvf + ii[u]) : 0.f;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        if (ii[u] < 0) continue;
+                        const int l = (m0 + u) * (int)blockDim.x + (int)threadIdx.x;
+                        const float r = sr[l] - alpha * sap[l];
+                        const float z = r * mi[u];
+                        sx[l] += alpha * sp[l];
+                        sr[l] = r;
+                        B.zf[ii[u]] = z;
+                        a[0] += prod2(r, z);
+                        a[1] += prod2(r, r);
+                    }
+                }
+                if (!qSumDF<2>(a, B, c, [&](const double* t) {
+                        qF[1] += 1;
+                        qS[S_BETA] = t[0] / qS[S_RZ];
+                        qS[S_RZ] = t[0];
+                        if (t[1] < qS[S_ETA2] * qS[S_RR0] || !(t[1] == t[1])) qF[3] = 1;
+                    }))
+                    return;
+            }
+            inner++;
+            if (vi(qF + 3) || total + inner >= maxIter || inner >= 400) break;
+        }
+        total += inner;
+        {   // x += ||r|| x_f (FP64)
+            const double sc = vd(qS + S_SQRT);
+            forOwnL(rs, [&](int l, int i) { B.x[i] += sc * (double)sx[l]; });
+            if (!qBarrier(B, c)) return;
+        }
+        {   // FP64 residual r = b - A x
+            double v[1] = {0.0};
+            forRows(B, rs, [&](int i, int len) {
+                const double r = B.b[i] - qRow(B, B.x, i, len);
+                B.r[i] = r;
+                v[0] += r * r;
+            });
+            if (!qSum<1>(v, B, c, [&](const double* t) {
+                    qS[S_RR] = t[0];
+                    qS[S_SQRT] = sqrt(t[0]);
+                    qS[S_INV] = 1.0 / sqrt(t[0]);
+                    qS[S_ETA2] = fmax(eta2, 0.25 * qS[S_THR] / t[0]);
+                    if (t[0] < qS[S_THR]) qF[0] = 1;
+                    if (!(t[0] == t[0])) { qF[0] = 1; qF[2] = 1; }
+                    qF[4] += 1;
+                }))
+                return;
+        }
+        refine++;
+    }
+    qStore(B, qL);
+}
+
 // FP64 residual row of the refinement without a pass in between: x_j + d_j is formed from
 // the FP64 iterate and the FP32 correction of the inner solve as the owner of j forms it.
 __device__ __forceinline__ double qRowPlus(const PpeBuffers& B, const double* x, const float* dx, int i, int len) {
@@ -1345,6 +1580,110 @@ __global__ void __launch_bounds__(QBC, 1) k_cg_solve(Dev d, PpeBuffers B, double
     qStore(B, qL);
 }
 
+// Plain FP64 Jacobi-PCG with shared-memory vectors: the same method, rows and stopping
+// rule as k_cg_solve, with r, p and Ap of each block's rows (24 bytes per row) in shared
+// memory (slot m BS + t for the m-th row of thread t); x, the inverse diagonal and z (gathered
+// through the matrix columns) stay in global memory.
+#define OWN64_CAPMAX OWN64_CAP_ROWS   // slots per block: 3 x 8448 x 8 B = 198 KB of shared memory
+__global__ void __launch_bounds__(QBC, 1) k_cg_own(Dev d, PpeBuffers B, double tol, int maxIter, int cap) {
+    __shared__ QLocal qL;   // this block's copy of the solver scalars and flags
+    qInit(qL);
+    double* const qS = qL.scal;
+    int* const qF = qL.flag;
+    extern __shared__ __align__(128) unsigned char dynSmem[];
+    double* const sr = reinterpret_cast<double*>(dynSmem);
+    double* const sp = sr + cap;
+    double* const sap = sp + cap;
+    const int n = liveN(d);
+    const RowSet rs = rowSet(n, QBC);   // this thread's rows (rowCount(rs) * QBC <= cap)
+    QCtl c = {0u};
+    {
+        double v[3] = {0.0, 0.0, 0.0};
+        forRowsL(B, rs, [&](int l, int i, int len) {
+            const double di = 1.0 / __ldg(B.diag + i);
+            const double bi = B.b[i];
+            const double r = bi - qRow(B, B.x, i, len);
+            const double z = r * di;
+            B.dinv[i] = di; sr[l] = r; B.z[i] = z;
+            v[0] += r * z; v[1] += r * r; v[2] += bi * bi;
+        });
+        if (!qSum<3>(v, B, c, [&](const double* t) {
+                qS[S_RZ] = t[0]; qS[S_RR] = t[1]; qS[S_BB] = t[2];
+                double thr = tol * tol * t[2];
+                if (thr < 2.2250738585072014e-308) thr = 2.2250738585072014e-308;
+                qS[S_THR] = thr;
+                qS[S_SCALE] = sqrt(t[1] / (t[2] > 0 ? t[2] : 1.0));
+                qF[0] = (t[2] == 0.0 || t[1] < thr) ? 1 : 0;
+                qF[1] = 0;
+                if (!(t[0] == t[0]) || !(t[1] == t[1])) { qF[0] = 1; qF[2] = 1; }
+            }))
+            return;
+    }
+    int it = 0;
+    while (!vi(qF) && it < maxIter) {
+        {   // Ap = A z + beta Ap, p = z + beta p, p.Ap
+            const double beta = it ? vd(qS + S_BETA) : 0.0;
+            double v[1] = {0.0};
+            forRowsL(B, rs, [&](int l, int i, int len) {
+                const double q = qRow(B, B.z, i, len);
+                const double z = B.z[i];
+                const double ap = it ? q + beta * sap[l] : q;
+                const double p = it ? z + beta * sp[l] : z;
+                sap[l] = ap; sp[l] = p;
+                v[0] += p * ap;
+            });
+            if (!qSum<1>(v, B, c, [&](const double* t) { qS[S_PAP] = t[0]; qS[S_ALPHA] = qS[S_RZ] / t[0]; }))
+                return;
+        }
+        {   // x += alpha p, r -= alpha Ap, z = M^-1 r; r.z, r.r
+            const double alpha = vd(qS + S_ALPHA);
+            double v[2] = {0.0, 0.0};
+            const int cnt = rowCount(rs);
+            for (int m0 = 0; m0 < cnt; m0 += 4) {
+                double mi[4], xo[4];
+                int ii[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    ii[u] = (m0 + u < cnt) ? rowAt(rs, m0 + u) : -1;
+                    mi[u] = (ii[u] >= 0) ? B.dinv[ii[u]] : 0.0;
+                    xo[u] = (ii[u] >= 0) ? B.x[ii[u]] : 0.0;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (ii[u] < 0) continue;
+                    const int l = (m0 + u) * (int)blockDim.x + (int)threadIdx.x;
+                    const double r = sr[l] - alpha * sap[l];
+                    const double z = r * mi[u];
+                    B.x[ii[u]] = xo[u] + alpha * sp[l];
+                    sr[l] = r;
+                    B.z[ii[u]] = z;
+                    v[0] += r * z; v[1] += r * r;
+                }
+            }
+            if (!qSum<2>(v, B, c, [&](const double* t) {
+                    qF[1] += 1;
+                    qS[S_RR] = t[1];
+                    qS[S_BETA] = t[0] / qS[S_RZ];
+                    qS[S_RZ] = t[0];
+                    if (t[1] < qS[S_THR]) qF[0] = 1;
+                    if (!(t[1] == t[1])) { qF[0] = 1; qF[2] = 1; }
+                }))
+                return;
+        }
+        it++;
+    }
+    if (!qBarrier(B, c)) return;
+    {   // FP64 residual of the result
+        double v[1] = {0.0};
+        forRows(B, rs, [&](int i, int len) {
+            const double r = B.b[i] - qRow(B, B.x, i, len);
+            v[0] += r * r;
+        });
+        qSum<1>(v, B, c, [&](const double* t) { qS[S_RR] = t[0]; });
+    }
+    qStore(B, qL);
+}
+
 // Jacobi-preconditioned BiCGSTAB (solver_type 1: Eigen::BiCGSTAB, src/MpsPressure.cpp:448-468;
 // van der Vorst 1992 with the preconditioner on the right), in one cooperative launch: per
 // iteration two SpMVs and five grid synchronisations (y and z must be complete before their
@@ -1474,13 +1813,28 @@ __global__ void __launch_bounds__(QBC, 1) k_bicgstab(Dev d, PpeBuffers B, double
 
 // kind: 0 plain FP64, 1 mixed, 2 mixed with the matrix-free inner operator, 3 mixed with
 // the compact scaled inner operator, 4 mixed with the staged tiles, 5 mixed with the
-// pipelined inner CG, 6 BiCGSTAB
+// pipelined inner CG, 6 BiCGSTAB, 7 mixed with block-owned rows (one block per SM), 8 plain
+// FP64 with block-owned rows (one block per SM)
 int ppePersistentGrid(int kind) {
     int dev = 0, sms = 0, coop = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     if (!coop) return 0;
+    if (kind == 7) {
+        const int dyn = OWN_CAPMAX * 16;
+        if (cudaFuncSetAttribute(k_mx_own<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
+            cudaFuncSetAttribute(k_mx_own<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
+            return 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mx_own<true>, QBX, dyn) != cudaSuccess || per <= 0) return 0;
+        return sms;   // one block per SM: the ranges are sized for it
+    }
+    if (kind == 8) {
+        const int dyn = OWN64_CAPMAX * 24;
+        if (cudaFuncSetAttribute(k_cg_own, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess) return 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_own, QBC, dyn) != cudaSuccess || per <= 0) return 0;
+        return sms;
+    }
     if (kind == 4) {
         if (cudaFuncSetAttribute(k_mx_solve<OP_TILED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sizeof(TsSmem)) != cudaSuccess)
@@ -1562,7 +1916,30 @@ int ppeSolvePersistent(const Dev& d, const PpeBuffers& B, int mixed, double tol,
     // refinement instead of two, 1.86 -> 1.74 ms); a coarser floor forces extra refinements
     double t = tol, eta2 = 1e-6 * 1e-6;
     int mi = maxIter;
-    void* args[5] = {&dd, &bb, &t, &mi, &eta2};
+    void* args[6] = {&dd, &bb, &t, &mi, &eta2, nullptr};
+    if (!mixed && !B.ownOff && B.pgridOwn64 > 0 && B.ownCap64 > 0) {
+        // block-owned rows: r, p, Ap of each block in its shared memory
+        int cap = B.ownCap64;
+        void* a4[5] = {&dd, &bb, &t, &mi, &cap};
+        if (pr) prof->begin(PROF_PPE_SOLVE, s);
+        cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_cg_own, B.pgridOwn64, QBC, a4, (size_t)cap * 24, s);
+        if (pr) prof->end(s);
+        if (e != cudaSuccess) return MPSGPU_ERR_CUDA;
+        countLaunch(1);
+        return finishPersistent(B, s, iters, refinements, relres, relres0);
+    }
+    if (mixed && B.matfree == 0 && !B.ownOff && B.pgridOwn > 0 && B.ownCap > 0) {
+        // block-owned rows: the FP32 inner-CG vectors of each block in its shared memory
+        int cap = B.ownCap;
+        args[5] = &cap;
+        if (pr) prof->begin(PROF_PPE_SOLVE, s);
+        const void* fn = B.cdir ? (const void*)k_mx_own<true> : (const void*)k_mx_own<false>;
+        cudaError_t e = cudaLaunchCooperativeKernel(fn, B.pgridOwn, QBX, args, (size_t)cap * 16, s);
+        if (pr) prof->end(s);
+        if (e != cudaSuccess) return MPSGPU_ERR_CUDA;
+        countLaunch(1);
+        return finishPersistent(B, s, iters, refinements, relres, relres0);
+    }
     if (pr) prof->begin(PROF_PPE_SOLVE, s);
     const void* fn = !mixed              ? (const void*)k_cg_solve
                      : B.matfree == 4    ? (const void*)k_mx_pipe

@@ -167,9 +167,10 @@ class MpsGpu:
         _check("mpsgpu_set_precision", lib().mpsgpu_set_precision(self.h, precision), self.h)
 
     def set_ppe_launch(self, mode=1):
-        """PPE launch: 0 one launch per kernel, 1 (default) one cooperative launch per solve,
-        2 as 1 with the FP32 matrix streamed through shared memory by bulk copies, 3 as 1 with
-        the pipelined inner CG."""
+        """PPE launch: 0 one launch per kernel, 1 (default) one cooperative launch per solve
+        (block-owned rows, inner-CG vectors in shared memory), 2 as 1 with the FP32 matrix
+        streamed through shared memory by bulk copies, 3 as 1 with the pipelined inner CG,
+        4 as 1 with grid-stride rows and the vectors in global memory."""
         _check("mpsgpu_set_ppe_launch", lib().mpsgpu_set_ppe_launch(self.h, int(mode)), self.h)
 
     def write_vtu(self, path, groups=0):

@@ -7,6 +7,8 @@ and each operator's output is compared with the oracle's:
 
 * neighbour counts and integer fields bit-exact, free-surface flags equal except
   particles within 1e-6 relative of a threshold (counted, as the small-case tests do);
+  the diagnostic sign deviationDotPolygonNormal equal except where npcd . n is at the
+  rounding level (interior particles of the unjittered lattice, counted);
 * FP64 fields within 1e-10 normwise (FP64 tier) or 1e-8 (DF32 tier);
 * the PPE pressure of every solver path (plain FP64 CG from the previous solution, the
   FP32/FP64 refinement from the quadratic extrapolation, and the learned start with the
@@ -47,11 +49,29 @@ def _ambiguous(o, idx):
     return (np.abs(ps - p.betaPnd) <= 1e-6 * p.betaPnd) | (np.abs(d2 - p.delta2) <= 1e-6 * p.delta2)
 
 
+def _devdot_ambiguous(o, idx):
+    """deviationDotPolygonNormal is the sign of npcd . n (a diagnostic: the reference only
+    computes it).  On the unjittered lattice npcd vanishes by symmetry in the interior, and
+    its sign there is the rounding of the summation order: such particles are counted, not
+    compared."""
+    d = np.einsum("ij,ij->i", o.get(abi.F_NPCD)[idx], o.get(abi.F_POLYNORMAL)[idx])
+    scale = np.max(np.abs(o.get(abi.F_NPCD))) + 1e-300
+    return np.abs(d) <= 1e-9 * scale
+
+
 def compare(o, g, where, rtol, fields=None, counts=None):
     for f in fields or (VEC + SCA + INT):
         a, b = g.get(f), o.get(f)
         name = abi.FIELD_NAMES[f]
-        if f in abi.INT_FIELDS:
+        if f == abi.F_DEVDOT:
+            bad = np.nonzero(a != b)[0]
+            if len(bad):
+                amb = _devdot_ambiguous(o, bad)
+                if counts is not None:
+                    counts["devdot_at_rounding_level"] = counts.get("devdot_at_rounding_level", 0) + int(amb.sum())
+                bad = bad[~amb]
+            assert len(bad) == 0, "%s: %s differs at %d particles, e.g. %s" % (where, name, len(bad), bad[:5])
+        elif f in abi.INT_FIELDS:
             bad = np.nonzero(a != b)[0]
             if f == abi.F_BC and len(bad):
                 amb = _ambiguous(o, bad)

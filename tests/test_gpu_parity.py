@@ -358,13 +358,14 @@ def test_mlp_gradient_matches_cpu(mps_lib):
 
 @pytest.mark.parametrize("solver", [abi.SOLVER_PLAIN_FP64, abi.SOLVER_MIXED])
 def test_ppe_launch_modes_agree(oracle_mod, mps_lib, solver):
-    """The single cooperative launch (with and without the staged ELL tiles, and with the
+    """The single cooperative launch (block-owned rows with the inner-CG vectors in shared
+    memory, grid-stride rows with the vectors in global memory, the staged ELL tiles, the
     pipelined inner CG of the mixed solver) and the per-kernel launches solve the same
     system to the same tolerance (same method; rounding differs)."""
     from polymps_gb300 import mps
     c = CASES["cfg3_3d_inc_polygon"]()
     out = []
-    for mode in (2, 1, 0, 3):
+    for mode in (2, 1, 0, 3, 4):
         g = mps.MpsGpu(c, solver=solver, tol=1e-10)
         g.set_ppe_launch(mode)
         g.initialize()
@@ -372,7 +373,7 @@ def test_ppe_launch_modes_agree(oracle_mod, mps_lib, solver):
         assert st.ppeRelResidual <= 1e-10
         out.append((g.get(abi.F_PRESS), st.ppeIterations))
         g.close()
-    for k in (1, 2, 3):
+    for k in (1, 2, 3, 4):
         assert relerr(out[0][0], out[k][0]) < 1e-8
         assert abs(out[0][1] - out[k][1]) <= 3 + 3 * (k == 3)
 

@@ -138,6 +138,7 @@ struct PpeBuffers {
     // learned warm start: the network's correction c of the start x (nullptr: none); the
     // shared-memory mixed solver takes the residual-minimising step x + theta c in its set-up
     const float* cdir;
+    const float* cq;   // q = A c (FP32) of the learned correction
 };
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);

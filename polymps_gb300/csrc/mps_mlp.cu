@@ -272,19 +272,51 @@ __global__ void __launch_bounds__(256) k_mlp_resid(Dev d, PpeBuffers B, const fl
     if (i >= liveN(d)) return;
     re[i] = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), B.N0);
 }
-// The same residual, with the block partials of the system scale (sum over equation rows of
-// feature 7 squared, and their count) for the fused forward
-__global__ void __launch_bounds__(256) k_mlp_resid_sig(Dev d, PpeBuffers B, const float* xe32, float* re, double* part) {
+// The same residual with the 16 raw features of the row (k_mlp_features' definitions) and the
+// block partials of the system scale (sum over equation rows of feature 7 squared, and
+// their count): one memory-bound pass over the rows' fields at full occupancy, so the
+// tensor-core forward only streams the feature rows.
+__global__ void __launch_bounds__(256) k_mlp_resid_feat(Dev d, PpeBuffers B, const float* xe32, float* feat,
+                                                        double* part) {
+    const MpsParams& P = d.P;
+    double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
+    const double gn = sqrt(gx * gx + gy * gy + gz * gz);
+    if (gn > 0) { gx /= gn; gy /= gn; gz /= gn; }
+    const float ggx = (float)gx, ggy = (float)gy, ggz = (float)gz;
+    const float in0 = (float)(1.0 / P.pndSmallZero), iN0 = (float)(1.0 / P.numNeighZero), iRe = (float)(1.0 / P.reL);
+    const float iA = (float)(1.0 / (P.coeffPPE * P.pndSmallZero));
     const int n = liveN(d);
     double q0 = 0.0, q1 = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float r = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), B.N0);
-        re[i] = r;
-        if (d.bc[i] == d.P.inner) {
-            const float f7 = r * (1.f / (float)B.diag[i]);
-            q0 += (double)(f7 * f7);
-            q1 += 1.0;
-        }
+        const float rei = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), B.N0);
+        const dvec4 x = d.pos[i], v = d.vel[i];
+        const float diag = __ldg(B.diagf + i), idg = __ldg(B.diagInvf + i);
+        const double pn = d.pressPPE[i];
+        const float bi = (float)B.b[i];
+        const float vx = (float)v.x, vy = (float)v.y, vz = (float)v.z;
+        float f[NF];
+        f[0] = ((float)d.pndSmall[i] - (float)P.pndSmallZero) * in0;
+        f[1] = bi * idg;
+        f[2] = (float)d.numNeigh[i] * iN0;
+        f[3] = (pn == 0.0) ? 1.f : 0.f;
+        f[4] = fminf(sqrtf((float)d.riw2[i]) * iRe, 1.5f);
+        f[5] = (float)pn - (float)d.pressPPEprev[i];
+        f[6] = xe32[i];
+        f[7] = rei * idg;
+        f[8] = (float)pn;
+        f[9] = sqrtf(vx * vx + vy * vy + vz * vz);
+        f[10] = -(vx * ggx + vy * ggy + vz * ggz);
+        f[11] = diag * iA;
+        f[12] = (float)d.pndWall[i];
+        f[13] = -((float)x.x * ggx + (float)x.y * ggy + (float)x.z * ggz);
+        f[14] = (bi - (float)d.source[i]) * idg;
+        f[15] = ((float)d.pndi[i] - (float)d.pndki[i]) * in0;
+        float4* o = (float4*)(feat + (size_t)i * NF);
+        o[0] = make_float4(f[0], f[1], f[2], f[3]);
+        o[1] = make_float4(f[4], f[5], f[6], f[7]);
+        o[2] = make_float4(f[8], f[9], f[10], f[11]);
+        o[3] = make_float4(f[12], f[13], f[14], f[15]);
+        if (d.bc[i] == P.inner) { q0 += (double)(f[FSIG] * f[FSIG]); q1 += 1.0; }
     }
     blockPartials2(q0, q1, part);
 }
@@ -383,88 +415,48 @@ __global__ void k_mlp_step_apply(Dev d, PpeBuffers B, const float* cdir, const d
     if (i < d.N0) B.x[i] += theta[0] * (double)cdir[i];
 }
 
-// ------------------------------------------------------------------ fused warm start
-// Features of the new system computed in the forward kernel itself (the 16 features of
-// k_mlp_features, same definitions), so no N x 16 feature array is written and read back:
-// a warp takes 32 rows, every lane forms the 16 features of one row into the warp's
-// shared tile, then the tensor-core layers run on its two 16-row halves, reading their
-// input fragments from the tile.  The output is the network's correction c (Pa) on
-// equation rows and 0 elsewhere.
-#define FT_STRIDE 17
-__global__ void __launch_bounds__(128) k_mlp_forward_fused(Dev d, PpeBuffers B, const __nv_bfloat16* wbf,
-                                                           const float* master, const float* norm, const double* sig,
-                                                           const float* xe32, const float* re, float* cdir) {
+// ------------------------------------------------------------------ learned start
+// The network on the feature rows of the system, written as the correction c (Pa) on the
+// equation rows and 0 elsewhere (the output de-normalised and scaled by sigma).
+__global__ void __launch_bounds__(128) k_mlp_forward_c(Dev d, const float* feat, const __nv_bfloat16* wbf,
+                                                       const float* master, const float* norm, const double* sig,
+                                                       float* cdir) {
     __shared__ SmemW s;
-    __shared__ float tileF[4][32 * FT_STRIDE];
     loadWeights(s, wbf, master, norm);
     __syncthreads();
-    const MpsParams& P = d.P;
-    double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
-    const double gn = sqrt(gx * gx + gy * gy + gz * gz);
-    if (gn > 0) { gx /= gn; gy /= gn; gz /= gn; }
-    const float ggx = (float)gx, ggy = (float)gy, ggz = (float)gz;
-    const float in0 = (float)(1.0 / P.pndSmallZero), iN0 = (float)(1.0 / P.numNeighZero), iRe = (float)(1.0 / P.reL);
-    const float iA = (float)(1.0 / (P.coeffPPE * P.pndSmallZero));
     const float q = (float)(1.0 / sig[0]);
     const float csc = (float)sig[0] / norm[2 * NF + 1], cmean = norm[2 * NF] * (float)sig[0];
     const int n = liveN(d);
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, wib = threadIdx.x >> 5;
-    float* tf = tileF[wib];
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int tiles = (n + 31) / 32;
+    const int tiles = (n + 15) / 16;
+    float zero[NF] = {0};
     for (int tile = warp; tile < tiles; tile += nwarps) {
-        {   // the 16 features of row tile*32 + lane
-            const int i = tile * 32 + lane;
-            float* f = tf + lane * FT_STRIDE;
-            if (i < n) {
-                const float diag = (float)B.diag[i], idg = 1.f / diag;
-                const double pn = d.pressPPE[i];
-                const float bi = (float)B.b[i];
-                const dvec4 x = d.pos[i], v = d.vel[i];
-                const float vx = (float)v.x, vy = (float)v.y, vz = (float)v.z;
-                f[0] = ((float)d.pndSmall[i] - (float)P.pndSmallZero) * in0;
-                f[1] = bi * idg;
-                f[2] = (float)d.numNeigh[i] * iN0;
-                f[3] = (pn == 0.0) ? 1.f : 0.f;
-                f[4] = fminf(sqrtf((float)d.riw2[i]) * iRe, 1.5f);
-                f[5] = (float)pn - (float)d.pressPPEprev[i];
-                f[6] = xe32[i];
-                f[7] = re[i] * idg;
-                f[8] = (float)pn;
-                f[9] = sqrtf(vx * vx + vy * vy + vz * vz);
-                f[10] = -(vx * ggx + vy * ggy + vz * ggz);
-                f[11] = diag * iA;
-                f[12] = (float)d.pndWall[i];
-                f[13] = -((float)x.x * ggx + (float)x.y * ggy + (float)x.z * ggz);
-                f[14] = (bi - (float)d.source[i]) * idg;
-                f[15] = ((float)d.pndi[i] - (float)d.pndki[i]) * in0;
-            } else {
-#pragma unroll
-                for (int k = 0; k < NF; k++) f[k] = 0.f;
-            }
+        const int r0 = tile * 16 + g, r1 = r0 + 8;
+        const float* f0 = (r0 < n) ? feat + (size_t)r0 * NF : zero;
+        const float* f1 = (r1 < n) ? feat + (size_t)r1 * NF : zero;
+        uint32_t a0[1][4], a[4][4];
+        float z[8][4];
+        loadInput(s, f0, f1, a0[0], q);
+        layer<1, S1>(a0, s.w1, s.b1, z);
+        activate(z, a);
+        layer<4, S2>(a, s.w2, s.b2, z);
+        activate(z, a);
+        layer<4, S2>(a, s.w3, s.b3, z);
+        float o0, o1;
+        headOut(s, z, o0, o1);
+        if (t == 0) {
+            if (r0 < n) cdir[r0] = (d.bc[r0] == d.P.inner) ? o0 * csc + cmean : 0.f;
+            if (r1 < n) cdir[r1] = (d.bc[r1] == d.P.inner) ? o1 * csc + cmean : 0.f;
         }
-        __syncwarp();
-#pragma unroll 1
-        for (int h = 0; h < 2; h++) {
-            uint32_t a0[1][4], a[4][4];
-            float z[8][4];
-            loadInput(s, tf + (16 * h + g) * FT_STRIDE, tf + (16 * h + g + 8) * FT_STRIDE, a0[0], q);
-            layer<1, S1>(a0, s.w1, s.b1, z);
-            activate(z, a);
-            layer<4, S2>(a, s.w2, s.b2, z);
-            activate(z, a);
-            layer<4, S2>(a, s.w3, s.b3, z);
-            float o0, o1;
-            headOut(s, z, o0, o1);
-            if (t == 0) {
-                const int r0 = tile * 32 + 16 * h + g, r1 = r0 + 8;
-                if (r0 < n) cdir[r0] = (d.bc[r0] == P.inner) ? o0 * csc + cmean : 0.f;
-                if (r1 < n) cdir[r1] = (d.bc[r1] == P.inner) ? o1 * csc + cmean : 0.f;
-            }
-        }
-        __syncwarp();   // the tile is rewritten by the next round
     }
+}
+// q = A c (FP32 copy of the matrix) for the residual-minimising step the solver takes
+__global__ void __launch_bounds__(256) k_mlp_ac(Dev d, PpeBuffers B, const float* cdir, float* q) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    q[i] = ellRow<float, true>(B.diagf, B.valf, B.col, cdir, i, __ldg(B.rowLen + i), B.N0);
 }
 
 // sig: system scale of the raw features (nullptr: the features are network inputs as given)
@@ -481,18 +473,19 @@ static int mlpForwardLaunch(MlpState& m, const float* feat, int n, const double*
 int mlpWarmStart(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s, bool stepInSolver) {
     if (!m.ready) return MPSGPU_ERR_ARG;
     if (stepInSolver) {
-        // x = x_e, the extrapolation residual with the system scale's partials, the scale,
-        // then the fused features + forward writing the correction c; the residual-minimising
-        // step x_e + theta c is taken by the solver's own set-up pass
+        // x = x_e, the extrapolation residual with the features and the scale's partials, the
+        // scale, the network's correction c, and q = A c; the residual-minimising step
+        // x_e + theta c is taken by the solver's set-up pass (q in m.re)
         k_mlp_xe_start<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.xe32);
-        k_mlp_resid_sig<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.re, m.part);
+        k_mlp_resid_feat<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.feat, m.part);
         k_mlp_sig<<<1, 256, 0, s>>>(m.part, m.nblk, m.sig);
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int tiles = (d.N0 + 31) / 32;
+        const int tiles = (d.N0 + 15) / 16;
         const int blocks = std::min((tiles + 3) / 4, std::max(1, sms) * 8);
-        k_mlp_forward_fused<<<blocks, 128, 0, s>>>(d, B, m.wbf, m.master, m.norm, m.sig, m.xe32, m.re, m.cdir);
+        k_mlp_forward_c<<<blocks, 128, 0, s>>>(d, m.feat, m.wbf, m.master, m.norm, m.sig, m.cdir);
+        k_mlp_ac<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.cdir, m.re);
         return cudaGetLastError() == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
     }
     mlpFeatureLaunch(m, d, B, s);

@@ -42,8 +42,8 @@ int mlpSetWeights(MlpState& m, const float* params, const float* norm32, cudaStr
 int mlpGetWeights(MlpState& m, float* params, float* norm32, cudaStream_t s);
 int mlpFeatures(MlpState& m, const Dev& d, const PpeBuffers& B, float* hostFeat, int n, cudaStream_t s);
 // Writes the warm start into B.x (assembled system, previous solution in d.pressPPE).
-// stepInSolver: B.x = x_e and m.cdir = the network's correction c only; the solver takes
-// the residual-minimising step x_e + theta c in its set-up pass.
+// stepInSolver: B.x = x_e, m.cdir = the network's correction c and m.re = A c only; the
+// solver takes the residual-minimising step x_e + theta c in its set-up pass.
 int mlpWarmStart(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s, bool stepInSolver = false);
 // Recording / training (device-resident data, own kernels).
 int mlpRecordFeatures(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s);

@@ -1092,35 +1092,6 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
 // coalesced store of z.
 #define OWN_CAPMAX OWN_CAP_ROWS   // slots per block: 4 x 13312 x 4 B = 208 KB of shared memory
 
-// FP64 row products A x and A c of one row in one pass over its entries (c FP32); only
-// the set-up pass of a learned start calls it, so it stays out of line (the inner loop's
-// registers are not shared with it)
-__device__ __noinline__ void qRow2(const PpeBuffers& B, const double* x, const float* cv, int i, int len,
-                                      double& ax, double& ac) {
-    double a1[4] = {0.0, 0.0, 0.0, 0.0}, a2[4] = {0.0, 0.0, 0.0, 0.0};
-    const double* v = B.val + i;
-    const int* col = B.col + i;
-    const size_t N0 = B.N0;
-    for (int k = 0; k < len; k += 4) {
-        int cc[4];
-        double vv[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const bool ok = k + u < len;
-            cc[u] = ok ? ldStream(col + (size_t)(k + u) * N0) : i;
-            vv[u] = ok ? ldStream(v + (size_t)(k + u) * N0) : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            a1[u] += vv[u] * x[cc[u]];
-            a2[u] += vv[u] * (double)cv[cc[u]];
-        }
-    }
-    const double dg = __ldg(B.diag + i);
-    ax = dg * x[i] + ((a1[0] + a1[1]) + (a1[2] + a1[3]));
-    ac = dg * (double)cv[i] + ((a2[0] + a2[1]) + (a2[2] + a2[3]));
-}
-
 // The thread's rows of a RowSet with their shared-memory slot l = m BS + t (m-th row of the
 // thread), f(l, i, len) with the next row's length prefetched; forOwnL without the length.
 template <class F>
@@ -1143,28 +1114,28 @@ __device__ __forceinline__ void forOwnL(const RowSet& s, F&& f) {
 }
 
 // Set-up of the shared-memory mixed solve: FP64 residual of the warm start, ||r||^2 and
-// ||b||^2 and the solver scalars; with a learned correction c (B.cdir) also q = A c, the
-// dot products r.q and q.q, the residual-minimising step theta = r.q / q.q (the start
-// x + theta c is never worse than x in the residual norm; its residual norm follows
-// algebraically) and the update of x and r.  The learned form is called out of line, so the
-// inner loop's registers are not shared with it.  Returns false when a barrier wait ran out.
+// ||b||^2 and the solver scalars; with a learned correction c (B.cdir, with q = A c in
+// B.cq) also the dot products r.q and q.q, the residual-minimising step theta = r.q / q.q
+// (the start x + theta c is never worse than x in the residual norm; its residual norm
+// follows algebraically) and the update of x and r.  Returns false when a barrier wait ran
+// out.
 template <bool LEARNED>
 __device__ __forceinline__ bool mxSetup(const PpeBuffers& B, const RowSet& rs, QCtl& c, QLocal& qL, double tol,
                                         double eta2) {
     double* const qS = qL.scal;
     int* const qF = qL.flag;
-    const float* const cd = B.cdir;
     double v[LEARNED ? 4 : 2] = {};
     forRows(B, rs, [&](int i, int len) {
         const double bi = B.b[i];
-        double ax, ac = 0.0;
-        if (LEARNED) qRow2(B, B.x, cd, i, len, ax, ac);
-        else ax = qRow(B, B.x, i, len);
-        const double r = bi - ax;
+        const double r = bi - qRow(B, B.x, i, len);
         B.r[i] = r;
         v[0] += r * r;
         v[1] += bi * bi;
-        if (LEARNED) { B.Ap[i] = ac; v[LEARNED ? 2 : 0] += r * ac; v[LEARNED ? 3 : 0] += ac * ac; }
+        if (LEARNED) {
+            const double q = (double)__ldg(B.cq + i);
+            v[LEARNED ? 2 : 0] += r * q;
+            v[LEARNED ? 3 : 0] += q * q;
+        }
     });
     if (!qSum<LEARNED ? 4 : 2>(v, B, c, [&](const double* t) {
             double th = 0.0, rr = t[0];
@@ -1192,16 +1163,11 @@ __device__ __forceinline__ bool mxSetup(const PpeBuffers& B, const RowSet& rs, Q
     if (LEARNED) {   // x += theta c, r -= theta q on the thread's own rows
         const double th = vd(qS + S_OMEGA);
         forOwn(rs, [&](int i) {
-            B.x[i] += th * (double)cd[i];
-            B.r[i] -= th * B.Ap[i];
+            B.x[i] += th * (double)__ldg(B.cdir + i);
+            B.r[i] -= th * (double)__ldg(B.cq + i);
         });
     }
     return true;
-}
-
-__device__ __noinline__ bool mxSetupLearned(const PpeBuffers& B, const RowSet& rs, QCtl& c, QLocal& qL, double tol,
-                                            double eta2) {
-    return mxSetup<true>(B, rs, c, qL, tol, eta2);
 }
 
 template <bool LEARNED>
@@ -1218,7 +1184,7 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_own(Dev d, PpeBuffers B, double t
     const int n = liveN(d);
     const RowSet rs = rowSet(n, QBX);   // this thread's rows (rowCount(rs) * QBX <= cap)
     QCtl c = {0u};
-    if (!(LEARNED ? mxSetupLearned(B, rs, c, qL, tol, eta2) : mxSetup<false>(B, rs, c, qL, tol, eta2))) return;
+    if (!mxSetup<LEARNED>(B, rs, c, qL, tol, eta2)) return;
     int total = 0, refine = 0;
     while (!vi(qF) && total < maxIter && refine <= 20) {
         {   // inner start: r_f = r / ||r||, z = M^-1 r_f, x_f = 0

@@ -38,6 +38,11 @@ WORKLOADS = {2: "3D WC polygon dam break, 108k (cfg2)",
              5: "3D INC dam break + obstacle, collision, shifting, 9.4M (cfg5)"}
 HBM_FALLBACK = 6800.0
 LINE_MAX = 1500
+# DRAM bytes (read + write) of the single-launch mixed PPE solve per inner-iteration
+# equivalent, from one ncu capture of the 20 timed solves of the 864k workload
+# (3.62e9 B per launch at 18 inner iterations and 1 refinement: the setup and each
+# refinement's FP64 passes counted as two inner iterations each; k_mx_own_cfg3-864k.md)
+MX_TRAFFIC_PER_ITER = 3.62e9 / (18 + 2 * 2)
 
 
 def args_(argv=None):
@@ -58,7 +63,7 @@ def args_(argv=None):
                         "5 = 9.375M particles with obstacle and shifting, 2 = 108k weakly compressible")
     a.add_argument("--e2e-steps", type=int, default=10)
     a.add_argument("--fp64-steps", type=int, default=0,
-                   help="timed steps of the FP64 drop-in tier (0: as --steps)")
+                   help="timed steps of the FP64 drop-in tier (0: as --steps; -1: not timed)")
     a.add_argument("--no-cpu-baseline", action="store_true")
     a.add_argument("--cpu-steps", type=int, default=1)
     a.add_argument("--ppe-compare", type=int, default=1)
@@ -212,10 +217,9 @@ def algo_bytes(cls, N, E, Z, mixed, df, st=None, matfree=False, compact=False, o
 
 
 def owned_rows(n, sms=152):
-    """Whether the mixed solve runs with block-owned rows (the library's rule: rows per
-    block, with a quarter of headroom, within the 13,824 rows a block keeps in shared memory)."""
-    per = (n * 5 // 4 + sms - 1) // sms + 64
-    return min(13824, max(1024, (per + 31) // 32 * 32)) * sms >= n
+    """Whether the mixed solve keeps its vectors in shared memory (the library's rule: the
+    grid-stride rounds of a 1024-thread block per SM fit its 13,312 row slots)."""
+    return (n // (sms * 1024) + 1) * 1024 <= 13312
 
 
 def _timed_run(g, steps, world, rank, clocks=None):
@@ -324,8 +328,13 @@ def run_gb300(a, rank, world, local):
                        solver == abi.SOLVER_MIXED_COMPACT, own=owned_rows(N))
         if b:
             ach = b / (ms / calls / 1e3) / 1e9
+            traffic = None
+            if dom == "PPE_SOLVE" and mixed and solver == abi.SOLVER_MIXED and owned_rows(N) and st.runPpeSolves:
+                it = st.runPpeIterations / st.runPpeSolves
+                rf = st.runPpeRefinements / st.runPpeSolves
+                traffic = int(MX_TRAFFIC_PER_ITER * (it + 2 * (rf + 1)) * N / 864000)
             roof = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": hbm, "unit": "GB/s",
-                    "frac": round(ach / hbm, 4), "peak_source": hbm_src, "traffic": None,
+                    "frac": round(ach / hbm, 4), "peak_source": hbm_src, "traffic": traffic,
                     "algo_bytes": int(b), "launch_ms": round(ms / calls, 4),
                     "share": round(ms / st.stepMs, 3)}
     iters = st.runPpeIterations / max(st.runPpeSolves, 1)
@@ -338,7 +347,7 @@ def run_gb300(a, rank, world, local):
     # on the same workload
     ppe_done = a.warmup + a.steps + a.e2e_steps
     fp64 = None
-    if not (a.precision == "fp64" and a.solver == "plain"):
+    if not (a.precision == "fp64" and a.solver == "plain") and a.fp64_steps >= 0:
         g64 = handle(abi.PRECISION_FP64, abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS)
         g64.run(max(3, min(a.warmup, 5)))
         k64 = a.fp64_steps or a.steps

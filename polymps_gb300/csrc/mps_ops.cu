@@ -16,19 +16,24 @@
 // uniform, src/MpsInputOutput.cpp:833-838, so the harmonic mean is hoisted).  Staged scan
 // at the start-of-step positions; FP32 prefilter, exact FP64 radius/side tests.
 struct OpViscosity {
-    struct State { dvec4 vi; SideCtx sc; double ax, ay, az; };
+    // the kinematic factors of a wall and of a fluid neighbour, (2 mu)/rho and
+    // (2 mu mu / (mu + mu))/rho (src/MpsViscosity.cpp:55-62), are the same for every pair of
+    // the run: formed once per particle with the reference's operations (same bits)
+    struct State { dvec4 vi; SideCtx sc; double ax, ay, az, neuWall, neuFluid; };
     __device__ float hi(const Dev& d) const { return d.bandHiL; }
     __device__ bool active(const Dev&, const State&) const { return true; }
     __device__ void begin(const Dev& d, int i, State& st) const {
         st.vi = d.vel[i];
         st.sc = sideCtx(d, i, d.pos[i]);
         st.ax = st.ay = st.az = 0.0;
+        const double mu = d.P.KNM_VS1 * d.P.DNS_FL1, rho = d.P.DNS_FL1;
+        st.neuWall = (2.0 * mu) / rho;
+        st.neuFluid = (2.0 * mu * mu / (mu + mu)) / rho;
     }
     __device__ void visit(const Dev& d, int i, State& st, int j, dvec4 pj, PairG q) const {
         const MpsParams& P = d.P;
         if (!(q.d2 < P.reL2) || !sideOK(st.sc, pj, q.d2)) return;
-        double mu = P.KNM_VS1 * P.DNS_FL1, rho = P.DNS_FL1;
-        double neu = (d.type[j] == P.wall) ? (2.0 * mu) / rho : (2.0 * mu * mu / (mu + mu)) / rho;
+        const double neu = (d.type[j] == P.wall) ? st.neuWall : st.neuFluid;
         double wL, wd;
         weightR(q.d2, P.reL, P.weightType, wL, wd);
         dvec4 vj = d.vel[j];

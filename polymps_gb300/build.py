@@ -15,8 +15,8 @@ CSRC = os.path.join(PKG, "csrc")
 HOST = os.path.join(PKG, "host")
 OUT = os.path.join(PKG, "_build")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU = ["mps_cells.cu", "mps_ops.cu", "mps_ops_df.cu", "mps_wall.cu", "mps_ppe.cu", "mps_mlp.cu", "mps_api.cu",
-      "mps_static.cu"]
+CU = ["mps_cells.cu", "mps_ops.cu", "mps_ops_df.cu", "mps_wall.cu", "mps_ppe.cu", "mps_mlp.cu", "mps_mlp_tc.cu",
+      "mps_api.cu", "mps_static.cu"]
 CPP = ["mps_host.cpp"]
 
 

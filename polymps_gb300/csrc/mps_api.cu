@@ -308,6 +308,8 @@ static int calcPress(mpsgpu_t h) {
         e = ppeSolvePlain(h->d, h->B, h->tol, maxIt, h->s, &iters, &rr, &rr0, &h->prof);
     }
     cudaEventRecord(h->es1, h->s);
+    if (h->warm == MPSGPU_WARM_MLP && !e && (e = mlpTcStatus(h->mlp, h->s)))
+        g_lastError = "learned warm start: a tensor-core completion wait ran out";
     if (h->mlp.recording && !e) {
         // features of this system with the previous solution, target = converged - previous
         if (!h->B.prepared) { launchMixedPrepare(h->d, h->B, h->s); h->B.prepared = 1; }   // features read valf

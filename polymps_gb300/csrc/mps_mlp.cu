@@ -1,19 +1,19 @@
-// mps_mlp.cu — learned PPE warm start on sm_103a (no reference counterpart).
+// mps_mlp.cu — learned PPE warm start on sm_103a (no reference counterpart): features of the
+// new system, training, and the warm-start pipeline around the network.
 //
 // Per-particle MLP 16 -> 64 -> 64 -> 64 -> 1 with GELU, BF16 weights and FP32
-// accumulation on the tensor cores (mma.sync m16n8k16).  One warp evaluates 16 particles
-// at a time; the FP32 accumulator fragment of one layer is re-packed in registers as the
-// BF16 A fragment of the next (the m16n8 C layout of two adjacent n-tiles is the m16k16 A
-// layout), so activations never leave the register file.  The network predicts the
-// correction c of the temporal extrapolation x_e = 3 p_n - 3 p_{n-1} + p_{n-2} of the unclamped
-// pressure on equation rows (in target units, de-normalised on output); the warm start is
-// x0 = x_e + theta c with the residual-minimising step theta, and x0 = 0 on the identity
-// rows of surface/dummy particles (their exact solution).
+// accumulation.  Inference runs on the fifth-generation tensor cores (tcgen05, mps_mlp_tc.cu).
+// The network predicts the correction c of the temporal extrapolation
+// x_e = 3 p_n - 3 p_{n-1} + p_{n-2} of the unclamped pressure on equation rows (in target
+// units, de-normalised on output); the warm start is x0 = x_e + theta c with the
+// residual-minimising step theta, and x0 = 0 on the identity rows of surface/dummy particles
+// (their exact solution).
 //
-// Training runs on the same machinery: a fused forward/backward kernel over blocks of 64
-// recorded samples (activation gradients on the tensor cores, weight gradients dW = dZ^T H
-// on the tensor cores from transposed BF16 tiles staged in shared memory), then an Adam
-// kernel on the FP32 master weights that refreshes the BF16 copy.
+// Training uses mma.sync m16n8k16 tiles: a fused forward/backward kernel over blocks of 64
+// recorded samples (one warp evaluates 16 samples; the FP32 accumulator fragment of one
+// layer is re-packed in registers as the BF16 A fragment of the next; activation gradients
+// on the tensor cores, weight gradients dW = dZ^T H from transposed BF16 tiles staged in
+// shared memory), then an Adam kernel on the FP32 master weights that refreshes the BF16 copy.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -46,21 +46,8 @@ static_assert(NPARAM == MPSGPU_MLP_NPARAM, "parameter packing");
 #define S1 24
 #define S2 72
 
-// GELU in its tanh form (Hendrycks & Gimpel, "Gaussian Error Linear Units", 2016):
-// gelu(x) = x/2 (1 + tanh(k0 (x + k1 x^3))), k0 = sqrt(2/pi), k1 = 0.044715, with the
-// hardware tanh (tanh.approx.f32, one MUFU op); the network is trained with the same
-// function, so the approximation is part of its definition.
-#define GELU_K0 0.7978845608028654f
-#define GELU_K1 0.044715f
-__device__ __forceinline__ float tanhHw(float x) {
-    float y;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float gelu(float x) {
-    const float t = tanhHw(GELU_K0 * x * fmaf(GELU_K1 * x, x, 1.0f));
-    return 0.5f * x * (1.0f + t);
-}
+#include "mps_gelu.cuh"
+
 // d gelu / dx = (1 + t)/2 + x/2 (1 - t^2) k0 (1 + 3 k1 x^2)
 __device__ __forceinline__ float gelud(float x) {
     const float x2 = x * x;
@@ -158,40 +145,6 @@ __device__ __forceinline__ void headOut(const SmemW& s, const float (*z)[4], flo
     s0 += __shfl_xor_sync(0xffffffffu, s0, 1); s0 += __shfl_xor_sync(0xffffffffu, s0, 2);
     s1 += __shfl_xor_sync(0xffffffffu, s1, 1); s1 += __shfl_xor_sync(0xffffffffu, s1, 2);
     o0 = s0 + s.b4; o1 = s1 + s.b4;
-}
-
-// ------------------------------------------------------------------ inference
-__global__ void __launch_bounds__(128) k_mlp_forward(const float* feat, int n, const __nv_bfloat16* wbf,
-                                                     const float* master, const float* norm, const double* sig,
-                                                     float* out) {
-    __shared__ SmemW s;
-    loadWeights(s, wbf, master, norm);
-    __syncthreads();
-    const float q = sig ? (float)(1.0 / sig[0]) : 1.f;
-    int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int nwarps = (gridDim.x * blockDim.x) >> 5;
-    int tiles = (n + 15) / 16;
-    float zero[NF] = {0};
-    for (int tile = warp; tile < tiles; tile += nwarps) {
-        int r0 = tile * 16 + g, r1 = r0 + 8;
-        const float* f0 = (r0 < n) ? feat + (size_t)r0 * NF : zero;
-        const float* f1 = (r1 < n) ? feat + (size_t)r1 * NF : zero;
-        uint32_t a0[1][4], a[4][4];
-        float z[8][4];
-        loadInput(s, f0, f1, a0[0], q);
-        layer<1, S1>(a0, s.w1, s.b1, z);
-        activate(z, a);
-        layer<4, S2>(a, s.w2, s.b2, z);
-        activate(z, a);
-        layer<4, S2>(a, s.w3, s.b3, z);
-        float o0, o1;
-        headOut(s, z, o0, o1);
-        if (t == 0) {
-            if (r0 < n) out[r0] = o0;
-            if (r1 < n) out[r1] = o1;
-        }
-    }
 }
 
 // ------------------------------------------------------------------ features
@@ -416,42 +369,6 @@ __global__ void k_mlp_step_apply(Dev d, PpeBuffers B, const float* cdir, const d
 }
 
 // ------------------------------------------------------------------ learned start
-// The network on the feature rows of the system, written as the correction c (Pa) on the
-// equation rows and 0 elsewhere (the output de-normalised and scaled by sigma).
-__global__ void __launch_bounds__(128) k_mlp_forward_c(Dev d, const float* feat, const __nv_bfloat16* wbf,
-                                                       const float* master, const float* norm, const double* sig,
-                                                       float* cdir) {
-    __shared__ SmemW s;
-    loadWeights(s, wbf, master, norm);
-    __syncthreads();
-    const float q = (float)(1.0 / sig[0]);
-    const float csc = (float)sig[0] / norm[2 * NF + 1], cmean = norm[2 * NF] * (float)sig[0];
-    const int n = liveN(d);
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int tiles = (n + 15) / 16;
-    float zero[NF] = {0};
-    for (int tile = warp; tile < tiles; tile += nwarps) {
-        const int r0 = tile * 16 + g, r1 = r0 + 8;
-        const float* f0 = (r0 < n) ? feat + (size_t)r0 * NF : zero;
-        const float* f1 = (r1 < n) ? feat + (size_t)r1 * NF : zero;
-        uint32_t a0[1][4], a[4][4];
-        float z[8][4];
-        loadInput(s, f0, f1, a0[0], q);
-        layer<1, S1>(a0, s.w1, s.b1, z);
-        activate(z, a);
-        layer<4, S2>(a, s.w2, s.b2, z);
-        activate(z, a);
-        layer<4, S2>(a, s.w3, s.b3, z);
-        float o0, o1;
-        headOut(s, z, o0, o1);
-        if (t == 0) {
-            if (r0 < n) cdir[r0] = (d.bc[r0] == d.P.inner) ? o0 * csc + cmean : 0.f;
-            if (r1 < n) cdir[r1] = (d.bc[r1] == d.P.inner) ? o1 * csc + cmean : 0.f;
-        }
-    }
-}
 // q = A c (FP32 copy of the matrix) for the residual-minimising step the solver takes
 __global__ void __launch_bounds__(256) k_mlp_ac(Dev d, PpeBuffers B, const float* cdir, float* q) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -461,13 +378,7 @@ __global__ void __launch_bounds__(256) k_mlp_ac(Dev d, PpeBuffers B, const float
 
 // sig: system scale of the raw features (nullptr: the features are network inputs as given)
 static int mlpForwardLaunch(MlpState& m, const float* feat, int n, const double* sig, float* out, cudaStream_t s) {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int tiles = (n + 15) / 16;
-    int blocks = std::min((tiles + 3) / 4, std::max(1, sms) * 8);
-    k_mlp_forward<<<blocks, 128, 0, s>>>(feat, n, m.wbf, m.master, m.norm, sig, out);
-    return cudaGetLastError() == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
+    return mlpForwardTc(m, feat, n, nullptr, nullptr, 0, sig, out, s);
 }
 
 int mlpWarmStart(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s, bool stepInSolver) {
@@ -479,12 +390,7 @@ int mlpWarmStart(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s,
         k_mlp_xe_start<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.xe32);
         k_mlp_resid_feat<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.feat, m.part);
         k_mlp_sig<<<1, 256, 0, s>>>(m.part, m.nblk, m.sig);
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int tiles = (d.N0 + 15) / 16;
-        const int blocks = std::min((tiles + 3) / 4, std::max(1, sms) * 8);
-        k_mlp_forward_c<<<blocks, 128, 0, s>>>(d, m.feat, m.wbf, m.master, m.norm, m.sig, m.cdir);
+        if (int e = mlpForwardTc(m, m.feat, d.N0, d.nLive, d.bc, d.P.inner, m.sig, m.cdir, s)) return e;
         k_mlp_ac<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.cdir, m.re);
         return cudaGetLastError() == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
     }
@@ -530,12 +436,14 @@ int mlpInit(MlpState& m, int n0, cudaStream_t s) {
     }
     ok = al((void**)&m.re, sizeof(float) * (size_t)n0) && al((void**)&m.cdir, sizeof(float) * (size_t)n0) &&
          al((void**)&m.xe32, sizeof(float) * (size_t)n0) &&
-         al((void**)&m.part, sizeof(double) * 2 * (size_t)m.nblk) && al((void**)&m.sig, 2 * sizeof(double));
+         al((void**)&m.part, sizeof(double) * 2 * (size_t)m.nblk) && al((void**)&m.sig, 2 * sizeof(double)) &&
+         al((void**)&m.tcErr, sizeof(int));
     if (!ok) return MPSGPU_ERR_NOMEM;
     cudaMemsetAsync(m.master, 0, sizeof(float) * NPARAM, s);
     cudaMemsetAsync(m.adam_m, 0, sizeof(float) * NPARAM, s);
     cudaMemsetAsync(m.adam_v, 0, sizeof(float) * NPARAM, s);
     cudaMemsetAsync(m.grad, 0, sizeof(float) * NPARAM, s);
+    cudaMemsetAsync(m.tcErr, 0, sizeof(int), s);
     (void)bytes;
     return 0;
 }
@@ -543,7 +451,7 @@ int mlpInit(MlpState& m, int n0, cudaStream_t s) {
 void mlpFree(MlpState& m) {
     for (void* p : {(void*)m.master, (void*)m.adam_m, (void*)m.adam_v, (void*)m.grad, (void*)m.wbf, (void*)m.norm,
                     (void*)m.feat, (void*)m.out, (void*)m.recFeat, (void*)m.recTarget, (void*)m.lossAcc,
-                    (void*)m.re, (void*)m.cdir, (void*)m.part, (void*)m.sig, (void*)m.xe32})
+                    (void*)m.re, (void*)m.cdir, (void*)m.part, (void*)m.sig, (void*)m.xe32, (void*)m.tcErr})
         if (p) cudaFree(p);
     m = MlpState();
 }
@@ -908,14 +816,23 @@ int mlpTrain(MlpState& m, int iters, int batch, float lr, unsigned long long see
 
 // ------------------------------------------------------------------ checks
 // Network outputs for host-supplied raw features (inference check against a CPU model).
+int mlpTcStatus(MlpState& m, cudaStream_t s) {
+    int h = 0;
+    if (cudaMemcpyAsync(&h, m.tcErr, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemsetAsync(m.tcErr, 0, sizeof(int), s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+        return MPSGPU_ERR_CUDA;
+    return h ? MPSGPU_ERR_CUDA : 0;
+}
+
 int mlpForwardHost(MlpState& m, const float* hfeat, int n, float* hout, cudaStream_t s) {
     float *df = nullptr, *dout = nullptr;
     if (cudaMalloc(&df, sizeof(float) * NF * n) != cudaSuccess) return MPSGPU_ERR_NOMEM;
     if (cudaMalloc(&dout, sizeof(float) * n) != cudaSuccess) { cudaFree(df); return MPSGPU_ERR_NOMEM; }
     cudaMemcpyAsync(df, hfeat, sizeof(float) * NF * n, cudaMemcpyHostToDevice, s);
-    int e = mlpForwardLaunch(m, df, n, nullptr, dout, s);
+    int e = mlpForwardTc(m, df, n, nullptr, nullptr, 0, nullptr, dout, s);
     if (!e) cudaMemcpyAsync(hout, dout, sizeof(float) * n, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) e = MPSGPU_ERR_CUDA;
+    if (!e) e = mlpTcStatus(m, s);
     cudaFree(df); cudaFree(dout);
     return e;
 }

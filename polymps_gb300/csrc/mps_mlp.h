@@ -34,9 +34,18 @@ struct MlpState {
     float* lossAcc = nullptr;      // device loss accumulator
     int adamStep = 0;
     bool recording = false;
+    int* tcErr = nullptr;          // set by the tensor-core forward when a completion wait ran out
 };
 
 int mlpInit(MlpState& m, int n0, cudaStream_t s);
+// Network outputs on the tensor cores (tcgen05): rows = *nLive if nLive else n; out = the
+// raw output (bc == nullptr) or the learned correction c on rows with bc == inner, 0 on the
+// others (sig: the system scale of the raw features, nullptr for normalised inputs as given).
+int mlpForwardTc(const MlpState& m, const float* feat, int n, const int* nLive, const int* bc, int inner,
+                 const double* sig, float* out, cudaStream_t s);
+// 0, or MPSGPU_ERR_CUDA when a tensor-core forward since the last call reported a
+// completion wait that ran out (clears the word; synchronises the stream)
+int mlpTcStatus(MlpState& m, cudaStream_t s);
 void mlpFree(MlpState& m);
 int mlpSetWeights(MlpState& m, const float* params, const float* norm32, cudaStream_t s);
 int mlpGetWeights(MlpState& m, float* params, float* norm32, cudaStream_t s);

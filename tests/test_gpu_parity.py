@@ -454,8 +454,8 @@ def test_out_of_domain_removal(oracle_mod, mps_lib, name, precision):
 
 
 def test_field_transfers_page_locked(mps_lib):
-    """Fields read into and written from page-locked host arrays (read and written by the
-    reorder kernels directly) equal the transfers through pageable arrays."""
+    """Fields read into and written from page-locked host arrays (the end-to-end bench's
+    buffers) equal the transfers through pageable arrays, in both directions."""
     torch = pytest.importorskip("torch")
     from polymps_gb300 import mps
     c = CASES["cfg3_3d_inc_polygon"]()

@@ -42,7 +42,7 @@ struct mpsgpu_s {
     bool skinShift = false;    // ... and still intact for the shifting sweeps of the step
     int nHost = -1;            // live count known on the host (-1: read it from the device)
     int *nbrAlt = nullptr, *cntAlt = nullptr;   // second list arrays (the skin list keeps its own)
-    int skinOn = 1;            // DF32 tier: viscosity and the post-prediction list from the skin list
+    int skinOn = 1;            // viscosity and the post-prediction list from the start-of-step skin list
     bool corrFresh = false;    // the correction matrix of the current positions and masks is written
     bool opSkipped = false;    // the last operator had nothing left to launch
     void* vtuDev = nullptr;    // staging of the binary .vtu block (device, page-locked host)
@@ -173,9 +173,10 @@ static bool df32(mpsgpu_t h) { return h->d.prec == MPSGPU_PRECISION_DF32; }
 static void ensureList(mpsgpu_t h) {
     if (h->listValid) return;
     if (h->prof.on) h->prof.begin(PROF_NEIGHBOR_LIST, h->s);
-    if (df32(h) && h->skinValid) {
-        launchNeighborFilterDF(h->d, h->s);
-        countLaunch(5);   // FP32 copies (2), skin check, filter (listed + unlisted particles)
+    if (h->skinValid) {
+        if (df32(h)) launchNeighborFilterDF(h->d, h->s);
+        else launchNeighborFilter(h->d, h->s);
+        countLaunch(df32(h) ? 5 : 4);   // FP32 copies (2), skin check, filter (DF32: listed + unlisted particles)
     } else {
         if (df32(h)) launchNeighborListDF(h->d, h->s);
         else launchNeighborList(h->d, h->s);
@@ -367,13 +368,15 @@ static int runOpBody(mpsgpu_t h, int op) {
             break;
         }
         case MPS_OP_VISCOSITY:
-            if (x && h->skinOn) {
+            if (h->skinOn) {
                 // start-of-step list with a skin: the viscosity sweep reads it, and the list of
-                // the predicted positions is filtered from it (ensureList)
+                // the predicted positions is filtered from it (ensureList); in the FP64 tier
+                // the sweep and the filter keep the bucket scan's FP64 arithmetic and order
                 if (h->prof.on) { h->prof.end(s); h->prof.begin(PROF_NEIGHBOR_LIST, s, false); }
                 launchSkinListDF(d, s);
                 if (h->prof.on) { h->prof.end(s); h->prof.begin(MPS_OP_VISCOSITY, s, false); }
-                launchViscosityListDF(d, s);
+                if (x) launchViscosityListDF(d, s);
+                else launchViscosityList(d, s);
                 invalidate();
                 // the skin list keeps its arrays; the lists filtered from it go to the others
                 d.skinNbr = d.nbr;
@@ -381,7 +384,7 @@ static int runOpBody(mpsgpu_t h, int op) {
                 std::swap(d.nbr, h->nbrAlt);
                 std::swap(d.nbrCount, h->cntAlt);
                 h->skinValid = true;
-                h->skinShift = true;
+                h->skinShift = x;   // the DF32 shifting sweeps filter the kept skin list again
                 countLaunch(2);   // skin list (listed + unlisted particles); the sweep is counted below
             } else if (x) launchViscosityDF(d, s);
             else launchViscosity(d, s);

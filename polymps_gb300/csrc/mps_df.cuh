@@ -232,3 +232,10 @@ __device__ __forceinline__ void forCellsDF(const Dev& d, dvec4 pi, float4 fi, fl
 }
 
 __device__ __forceinline__ df dfOf(float h, float l) { return quick2(h, l); }
+
+// Scan window key of a position: its three bucket coordinates (out-of-grid included).
+__device__ __forceinline__ long long cellKeyOf(const Dev& d, dvec4 p, float4 hi) {
+    int ix, iy, iz;
+    bucketCoordsHi(d, p, hi, ix, iy, iz);
+    return ((long long)(iz & 0x1fffff) << 42) | ((long long)(iy & 0x1fffff) << 21) | (long long)(ix & 0x1fffff);
+}

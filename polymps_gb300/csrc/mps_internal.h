@@ -44,6 +44,10 @@ void launchFillCache(const Dev& d, cudaStream_t s);
 
 // mps_ops.cu
 void launchViscosity(const Dev& d, cudaStream_t s);
+// FP64 tier over the start-of-step skin list (built by launchSkinListDF): the viscosity
+// sweep, and the list of the current positions with its weights filtered from it
+void launchViscosityList(const Dev& d, cudaStream_t s);
+void launchNeighborFilter(const Dev& d, cudaStream_t s);
 void launchAddGravity(const Dev& d, cudaStream_t s);
 void launchPredict(const Dev& d, cudaStream_t s);
 void launchOutOfDomain(const Dev& d, int* flags, int* counter, cudaStream_t s);
@@ -92,6 +96,8 @@ void launchVelDivergence(const Dev& d, cudaStream_t s);
 void launchSkinListDF(const Dev& d, cudaStream_t s);
 void launchViscosityListDF(const Dev& d, cudaStream_t s);
 void launchNeighborFilterDF(const Dev& d, cudaStream_t s);
+// the skin list's validity flag for the current positions (moved more than half the skin)
+void launchSkinCheck(const Dev& d, cudaStream_t s);
 void launchShiftVelApply(const Dev& d, cudaStream_t s);
 void launchApplyShift(const Dev& d, cudaStream_t s);
 

@@ -49,6 +49,91 @@ struct OpViscosity {
 void launchViscosity(const Dev& d, cudaStream_t s) {
     launchScan(d, OpViscosity(), s);
 }
+// The same sweep over the start-of-step skin list (built just before from the same FP32
+// copies): its entries within the reL band, in scan order, are exactly the candidates the
+// 27-bucket scan passes to the exact FP64 test, so the sums are the scan's bit for bit.
+// A row that overflowed the list capacity (count K + 1) scans the buckets.
+__global__ void __launch_bounds__(128) k_visc_list(Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const OpViscosity op;
+    OpViscosity::State st;
+    op.begin(d, i, st);
+    const dvec4 pi = d.pos[i];
+    const float4 fi = d.posf[i];
+    const float hi = op.hi(d);
+    const int c = d.nbrCount[i];
+    if (c <= d.K) {
+        const int* row = d.nbr + i;
+        for (int k = 0; k < c; k++) {
+            const int j = ldStream(row + (size_t)k * d.N0);
+            const float4 fj = d.posf[j];
+            const float ex = fj.x - fi.x, ey = fj.y - fi.y, ez = fj.z - fi.z;
+            if (ex * ex + ey * ey + ez * ez > hi) continue;
+            const dvec4 pj = d.pos[j];
+            op.visit(d, i, st, j, pj, pairOf(pj, pi));
+        }
+    } else {
+        forCellsNear(d, pi, fi, hi, [&](int j, dvec4 pj, PairG q) {
+            if (j != i) op.visit(d, i, st, j, pj, q);
+        });
+    }
+    op.end(d, i, st);
+}
+void launchViscosityList(const Dev& d, cudaStream_t s) {
+    k_visc_list<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}
+
+// FP64 list of the current positions filtered from the skin list: the set, order and
+// per-entry weights of k_build_nbr (candidates within the FP32 band, exact FP64 test
+// d^2 < reMax^2).  A particle whose scan window changed or whose skin row overflowed, or
+// every particle once the skin list went stale, scans the 27 buckets as k_build_nbr does.
+__global__ void __launch_bounds__(128) k_filter_nbr(Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    const dvec4 pi = d.pos[i];
+    const float4 fi = d.posf[i];
+    const size_t N0 = d.N0;
+    int cnt = 0;
+    auto keep = [&](int j, PairG q) {
+        if (!(q.d2 < d.reMax2)) return;
+        if (cnt < d.K) {
+            const size_t e = (size_t)cnt * N0 + i;
+            d.nbr[e] = j;
+            double w, wd;
+            weightR(q.d2, P.reS, P.weightType, w, wd);
+            d.cw[e] = w;
+            d.cwd[e] = wd;
+            if (d.cwL) { double wl, wdl; weightR(q.d2, P.reL, P.weightType, wl, wdl); d.cwL[e] = wl; }
+        }
+        cnt++;
+    };
+    const int c = d.skinCnt[i];
+    if (!*(volatile int*)d.skinFlag && c <= d.K && d.skinCell[i] == cellKeyOf(d, pi, fi)) {
+        for (int k = 0; k < c; k++) {
+            const int j = ldStream(d.skinNbr + (size_t)k * N0 + i);
+            const float4 fj = d.posf[j];
+            const float ex = fj.x - fi.x, ey = fj.y - fi.y, ez = fj.z - fi.z;
+            if (ex * ex + ey * ey + ez * ez > d.bandHi) continue;
+            const dvec4 pj = d.pos[j];
+            keep(j, pairOf(pj, pi));
+        }
+    } else {
+        forCellsNear(d, pi, fi, d.bandHi, [&](int j, dvec4, PairG q) {
+            if (j != i) keep(j, q);
+        });
+    }
+    if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }
+    d.nbrCount[i] = cnt;
+    warpCount(d.counters, (unsigned)cnt);
+}
+void launchNeighborFilter(const Dev& d, cudaStream_t s) {
+    cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long), s);
+    launchPosf(d, s);
+    launchSkinCheck(d, s);
+    k_filter_nbr<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+}
 
 // MpsParticle::addGravity, src/MpsParticle.cpp:111-130
 __global__ void k_add_gravity(Dev d) {

@@ -908,12 +908,6 @@ void launchShiftingDF(const Dev& d, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------ start-of-step list
-// Scan window key of a position: its three bucket coordinates (out-of-grid included).
-__device__ __forceinline__ long long cellKeyOf(const Dev& d, dvec4 p, float4 hi) {
-    int ix, iy, iz;
-    bucketCoordsHi(d, p, hi, ix, iy, iz);
-    return ((long long)(iz & 0x1fffff) << 42) | ((long long)(iy & 0x1fffff) << 21) | (long long)(ix & 0x1fffff);
-}
 // Candidates of the 27-bucket scan within reMax + skin of the start positions (FP32 test
 // against a radius that includes the rounding band: a superset of every list the step's
 // sweeps can need while the particles stay within half the skin), in scan order.
@@ -1033,6 +1027,9 @@ __global__ void __launch_bounds__(128) k_filter_nbr_df(Dev d) {
     if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }
     d.nbrCount[i] = cnt;
     warpCount(d.counters, (unsigned)cnt);
+}
+void launchSkinCheck(const Dev& d, cudaStream_t s) {
+    k_skin_check<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
 }
 void launchNeighborFilterDF(const Dev& d, cudaStream_t s) {
     cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long), s);

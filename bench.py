@@ -73,6 +73,8 @@ def args_(argv=None):
                    help="also time the measured-and-rejected launch forms and inner operators")
     a.add_argument("--detail", default=os.path.join(ROOT, "bench_detail.json"),
                    help="file for the per-system PPE traces, the per-class profile and the long CPU baseline")
+    a.add_argument("--mlp", default=os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz"),
+                   help="weights of the learned warm start (npz with params, norm)")
     a.add_argument("--presort", action="store_true",
                    help="number the input particles in bucket order (input renumbering only)")
     return a.parse_args(argv)
@@ -261,7 +263,7 @@ def run_gb300(a, rank, world, local):
         case = cases.Case(case.name, case.params, case.type[perm], case.pos[perm], case.mesh)
     solver = {"mixed": abi.SOLVER_MIXED, "plain": abi.SOLVER_PLAIN_FP64, "matfree": abi.SOLVER_MIXED_MATFREE,
               "compact": abi.SOLVER_MIXED_COMPACT}[a.solver]
-    mlp_path = os.path.join(ROOT, "polymps_gb300", "mlp_warmstart.npz")
+    mlp_path = a.mlp
     have_mlp = os.path.exists(mlp_path)
     prec = abi.PRECISION_DF32 if a.precision == "df32" else abi.PRECISION_FP64
     warm = {"prev": abi.WARM_PREVIOUS, "extrap": abi.WARM_EXTRAP, "mlp": abi.WARM_MLP}.get(a.warm, abi.WARM_EXTRAP2)

@@ -168,6 +168,9 @@ enum MpsOp {
     MPS_OP_DUMMY_VELOCITY,       /* updateVelocityParticlesWallDummy  src/MpsParticleVelPos.cpp:100-158 */
     MPS_OP_INIT_PND,             /* step-0 sequence src/main.cpp:158-166: setInitialPnd..., meanWallPnd,
                                     meanPnd, meanNeighFluidPnd                                       */
+    MPS_OP_PREDICT_PRESS_GRADIENT, /* relax_fact < 1 only (src/main.cpp:271-276), before PREDICT:
+                                    predictionPressGradient  src/MpsPressure.cpp:932-1028,
+                                    predictionWallPressGradient  src/MpsPressure.cpp:1031-1214      */
     MPS_OP_COUNT
 };
 
@@ -204,7 +207,7 @@ int mpsgpu_params_derive(MpsParams* p, int n, const double* pos3);
 /* Host-only check (no GPU needed) of the input switches against the implemented path:
  * 0, or MPSGPU_ERR_UNSUPPORTED with mpsgpu_last_error(NULL) naming the JSON switch and
  * the reason (deformable/forced meshes, periodic domains, non-Newtonian rheology,
- * relax_fact < 1, unknown solver/collision/wall types).  mpsgpu_create makes the same
+ * unknown solver/collision/wall types).  mpsgpu_create makes the same
  * check.  Replaces the reference's silent acceptance of switches it marks "NOT WORKING"
  * (input/InputDamINC.json flags). */
 int mpsgpu_check_params(const MpsParams* p);

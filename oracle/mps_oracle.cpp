@@ -1641,9 +1641,49 @@ void repulsive(const Orc& o, int i, const double* n, double ns, double vMax2, do
     f[0] = -w * n[0]; f[1] = -w * n[1]; f[2] = -w * n[2];
 }
 
-// MpsPressure::calcWallPressGradient, src/MpsPressure.cpp:1341-1550
-void wallPressGradient(Orc& o) {
+// MpsPressure::predictionPressGradient, src/MpsPressure.cpp:932-1028 (relax_fact < 1,
+// src/main.cpp:271-276): the previous pressure's gradient at the start-of-step positions,
+// every particle, no correction matrix, (1 - relax_fact) of it added to the acceleration.
+void predictPressGradient(Orc& o) {
     const MpsParams& P = o.P;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < o.N; i++) {
+        double ax = 0, ay = 0, az = 0;
+        const double* xi = &o.pos[i * 3];
+        const double* mi = &o.mirror[i * 3];
+        double Pi = o.press[i], ni = o.pndi[i], pmin = Pi;
+        if (P.gradientType == 0 || P.gradientType == 2)
+            forCandidates(o, xi[0], xi[1], xi[2], [&](int j) {
+                Pair q = pairOf(o, j, xi, mi);
+                if (q.d2 < P.reS2 && sideOK(o, q) && j != i)
+                    if (pmin > o.press[j]) pmin = o.press[j];
+            });
+        forCandidates(o, xi[0], xi[1], xi[2], [&](int j) {
+            Pair q = pairOf(o, j, xi, mi);
+            if (q.d2 < P.reS2 && sideOK(o, q) && j != i) {
+                double wS = weight(std::sqrt(q.d2), P.reS, P.weightType);
+                if (P.gradientType == 0) wS *= (o.press[j] - pmin) / q.d2;
+                else if (P.gradientType == 1) wS *= (o.press[j] + Pi) / q.d2;
+                else if (P.gradientType == 2) wS *= (o.press[j] + Pi - 2.0 * pmin) / q.d2;
+                else if (P.gradientType == 3) {
+                    double nj = o.pndi[j];
+                    if (ni > P.epsilonZero && nj > P.epsilonZero) wS *= (ni * o.press[j] / nj + nj * Pi / ni) / q.d2;
+                }
+                ax += q.v0 * wS; ay += q.v1 * wS; az += q.v2 * wS;
+            }
+        });
+        o.acc[i * 3] += (1.0 - P.relaxPress) * ax * P.coeffPressGrad / o.RHO[i];
+        o.acc[i * 3 + 1] += (1.0 - P.relaxPress) * ay * P.coeffPressGrad / o.RHO[i];
+        o.acc[i * 3 + 2] += (1.0 - P.relaxPress) * az * P.coeffPressGrad / o.RHO[i];
+    }
+}
+
+// MpsPressure::calcWallPressGradient, src/MpsPressure.cpp:1341-1550, and (predict)
+// MpsPressure::predictionWallPressGradient, src/MpsPressure.cpp:1031-1214: the same sums
+// with (1 - relax_fact) for relax_fact and no force on the wall.
+void wallPressGradient(Orc& o, bool predict = false) {
+    const MpsParams& P = o.P;
+    const double fac = predict ? 1.0 - P.relaxPress : P.relaxPress;
     double VolumeForce = std::pow(P.partDist, P.dim);
     double maxVel = std::min(o.velMax, P.expectMaxVelocity);
     double vMax2 = maxVel * maxVel;
@@ -1685,10 +1725,11 @@ void wallPressGradient(Orc& o) {
         }
         double f[3] = {0, 0, 0};
         if (r.nsqrt < P.reRepulsiveForce && r.nsqrt > P.epsilonZero) repulsive(o, i, r.n, r.nsqrt, vMax2, f);
-        double g0 = P.relaxPress * (r.R[0] * ax + r.R[1] * ay + r.R[2] * az) * P.coeffPressGrad - f[0];
-        double g1 = P.relaxPress * (r.R[3] * ax + r.R[4] * ay + r.R[5] * az) * P.coeffPressGrad - f[1];
-        double g2 = P.relaxPress * (r.R[6] * ax + r.R[7] * ay + r.R[8] * az) * P.coeffPressGrad - f[2];
+        double g0 = fac * (r.R[0] * ax + r.R[1] * ay + r.R[2] * az) * P.coeffPressGrad - f[0];
+        double g1 = fac * (r.R[3] * ax + r.R[4] * ay + r.R[5] * az) * P.coeffPressGrad - f[1];
+        double g2 = fac * (r.R[6] * ax + r.R[7] * ay + r.R[8] * az) * P.coeffPressGrad - f[2];
         o.acc[i * 3] += g0 / o.RHO[i]; o.acc[i * 3 + 1] += g1 / o.RHO[i]; o.acc[i * 3 + 2] += g2 / o.RHO[i];
+        if (predict) continue;
         o.forceWall[i * 3] += -g0 * VolumeForce;
         o.forceWall[i * 3 + 1] += -g1 * VolumeForce;
         o.forceWall[i * 3 + 2] += -g2 * VolumeForce;
@@ -1831,6 +1872,12 @@ int runOp(Orc& o, int op) {
             else if (P.shiftingType == 2) shiftPosition(o);
             return 0;
         case MPS_OP_DUMMY_VELOCITY: dummyVelocity(o); return 0;
+        case MPS_OP_PREDICT_PRESS_GRADIENT:
+            if (P.relaxPress < 1.0) {
+                predictPressGradient(o);
+                if (P.wallType == 1) wallPressGradient(o, true);
+            }
+            return 0;
         case MPS_OP_INIT_PND:
             setInitialPnd(o);
             if (P.wallType == 1) meanWallPnd(o);
@@ -1864,6 +1911,7 @@ int step(Orc& o) {
     if (e) return e;
     calcViscosity(o);
     addGravity(o);
+    runOp(o, MPS_OP_PREDICT_PRESS_GRADIENT);
     predict(o);
     checkParticleOutDomain(o);
     if (P.collisionType == 1) collisionDPC(o);

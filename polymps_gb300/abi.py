@@ -128,7 +128,7 @@ OPS = [
     "WALL_DISTANCE", "WALL_NPCD", "CORRECTION_MATRIX", "PND_NEIGH_NPCD", "PND_DIFFUSIVE",
     "PND_MEAN", "UPDATE_BC", "CALC_PRESS", "EXTRAPOLATE_PRESS", "PRESS_GRADIENT",
     "WALL_PRESS_GRADIENT", "WALL_VISCOSITY", "CORRECT", "SHIFTING", "DUMMY_VELOCITY",
-    "INIT_PND",
+    "INIT_PND", "PREDICT_PRESS_GRADIENT",
 ]
 OP = {name: k for k, name in enumerate(OPS)}
 

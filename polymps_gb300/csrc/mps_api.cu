@@ -115,6 +115,7 @@ static int opLaunches(int op, const MpsParams& P, bool x) {
         case MPS_OP_WALL_DISTANCE: case MPS_OP_WALL_NPCD: return P.wallType == 1 ? 1 : 0;
         case MPS_OP_WALL_PRESS_GRADIENT: case MPS_OP_WALL_VISCOSITY: return P.wallType == 1 ? (x ? 2 : 1) : 0;
         case MPS_OP_PRESS_GRADIENT: return x ? 2 : 1;
+        case MPS_OP_PREDICT_PRESS_GRADIENT: return P.relaxPress < 1.0 ? (P.wallType == 1 ? 2 : 1) : 0;
         case MPS_OP_PND_DIFFUSIVE: return P.wallType == 1 ? 5 : 4;
         case MPS_OP_PND_MEAN: return P.wallType == 1 ? 3 : 2;
         case MPS_OP_INIT_PND: return 2 + (P.wallType == 1 ? 3 : 2);
@@ -220,8 +221,6 @@ static const char* unsupportedReason(const MpsParams& P) {
         return "particle_collision.type: only 0 (PC) and 1 (DPC) are supported";
     if (P.solverType != 0 && P.solverType != 1)
         return "semi_implicit_mps.solver_type: only 0 (CG) and 1 (BiCGSTAB) are supported";
-    if (P.relaxPress < 1.0)
-        return "gradient.relax_fact < 1: the prediction-step pressure gradient is not supported";
     if (P.wallType != 0 && P.wallType != 1) return "wall_type: only 0 (particles) and 1 (polygon) are supported";
     if (P.mpsType < 0 || P.mpsType > 3) return "mps_type: only 0 to 3 are supported";
     return nullptr;
@@ -390,6 +389,11 @@ static int runOpBody(mpsgpu_t h, int op) {
             else launchViscosity(d, s);
             break;
         case MPS_OP_ADD_GRAVITY: launchAddGravity(d, s); break;
+        case MPS_OP_PREDICT_PRESS_GRADIENT:
+            // FP64 in both tiers, over the start-of-step skin list while it is built for
+            // these positions (else the bucket scan)
+            if (P.relaxPress < 1.0) launchPredictPressGradient(d, h->skinValid, s);
+            break;
         case MPS_OP_PREDICT: launchPredict(d, s); invalidate(); break;
         case MPS_OP_OUT_OF_DOMAIN:
             launchOutOfDomain(d, h->outFlags, h->outCounter, s);
@@ -474,6 +478,7 @@ static int stepImpl(mpsgpu_t h) {
     RUN(MPS_OP_UPDATE_BUCKETS);
     RUN(MPS_OP_VISCOSITY);
     RUN(MPS_OP_ADD_GRAVITY);
+    if (P.relaxPress < 1.0) RUN(MPS_OP_PREDICT_PRESS_GRADIENT);
     RUN(MPS_OP_PREDICT);
     RUN(MPS_OP_OUT_OF_DOMAIN);
     ensureList(h);                       // post-prediction neighbour list
@@ -617,7 +622,7 @@ const char* mpsgpu_profile_name(int cls) {
                                 "COLLISION", "WALL_DISTANCE", "WALL_NPCD", "CORRECTION_MATRIX", "PND_NEIGH_NPCD",
                                 "PND_DIFFUSIVE", "PND_MEAN", "UPDATE_BC", "CALC_PRESS", "EXTRAPOLATE_PRESS",
                                 "PRESS_GRADIENT", "WALL_PRESS_GRADIENT", "WALL_VISCOSITY", "CORRECT", "SHIFTING",
-                                "DUMMY_VELOCITY", "INIT_PND"};
+                                "DUMMY_VELOCITY", "INIT_PND", "PREDICT_PRESS_GRADIENT"};
     static const char* extra[] = {"NEIGHBOR_LIST", "PPE_ASSEMBLE", "PPE_SPMV", "PPE_VECTOR", "PPE_OTHER", "PPE_SOLVE"};
     static_assert(sizeof(ops) / sizeof(ops[0]) == MPS_OP_COUNT, "operator names");
     if (cls >= 0 && cls < MPS_OP_COUNT) return ops[cls];

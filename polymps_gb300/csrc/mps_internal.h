@@ -64,6 +64,7 @@ void launchEOS(const Dev& d, cudaStream_t s);
 void launchExtrapolatePress(const Dev& d, cudaStream_t s);
 void launchPressGradient(const Dev& d, cudaStream_t s);
 void launchWallPressGradient(const Dev& d, cudaStream_t s);
+void launchPredictPressGradient(const Dev& d, bool skin, cudaStream_t s);   // relax_fact < 1, before PREDICT
 void launchWallViscosity(const Dev& d, cudaStream_t s);
 void launchCorrect(const Dev& d, cudaStream_t s);
 void launchShifting(const Dev& d, cudaStream_t s);

@@ -997,22 +997,23 @@ __global__ void __launch_bounds__(BLK) k_press_grad(Dev d) {
 }
 void launchPressGradient(const Dev& d, cudaStream_t s) { k_press_grad<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d); }
 
-// MpsPressure::calcWallPressGradient + repulsive forces, src/MpsPressure.cpp:1341-1611
-__global__ void __launch_bounds__(BLK) k_wall_press_grad(Dev d) {
-    int i = nearIndex(d);
-    if (i < 0) return;
+// Wall term of the pressure gradient at a fluid particle near the polygon wall (Mitsume's
+// mirror model and the repulsive force), src/MpsPressure.cpp:1341-1611: the sums over the
+// candidates that forCand passes as f(j, pj, q), j != i, returned as
+// fac * R a * coeffPressGrad - f_rep (fac = relax_fact after the solve, 1 - relax_fact in
+// the prediction, src/MpsPressure.cpp:1031-1214).
+template <class C>
+__device__ __forceinline__ void wallGradTerm(const Dev& d, int i, dvec4 pi, double fac, C&& forCand, double g[3]) {
     const MpsParams& P = d.P;
     // min(velMax of the last corrector, expected maximum velocity)^2 (src/MpsPressure.cpp:1342-1344)
     double vm = fmin(*d.velMax, P.expectMaxVelocity);
     double vMax2 = vm * vm;
-    dvec4 pi = d.pos[i], mi = d.mirror[i];
+    dvec4 mi = d.mirror[i];
     double Pi = d.press[i], pmin = Pi, ni = d.pndi[i];
     int gt = P.gradientType;
     ReflG r = makeRefl(pi, mi, P.epsilonZero, true);
     if (gt == 0 || gt == 2) {
-        forNbrs(d, i, [&](int j) {
-            dvec4 pj = d.pos[j];
-            PairG q = pairOf(pj, pi);
+        forCand([&](int j, dvec4 pj, PairG q) {
             if (q.d2 < P.reS2) {
                 PairM m = pairMirror(pj, mi);
                 if (q.d2 < m.dm2) { double pj_ = d.press[j]; if (pmin > pj_) pmin = pj_; }
@@ -1027,9 +1028,7 @@ __global__ void __launch_bounds__(BLK) k_wall_press_grad(Dev d) {
         return wS;
     };
     double ax = 0, ay = 0, az = 0;
-    forNbrs(d, i, [&](int j) {
-        dvec4 pj = d.pos[j];
-        PairG q = pairOf(pj, pi);
+    forCand([&](int j, dvec4 pj, PairG q) {
         if (q.d2 < P.reS2) {
             PairM m = pairMirror(pj, mi);
             if (m.dm2 < P.reS2 && q.d2 < m.dm2) {
@@ -1047,20 +1046,123 @@ __global__ void __launch_bounds__(BLK) k_wall_press_grad(Dev d) {
     }
     double f[3];
     wallRepulsion(P, r, vMax2, f);
-    double g0 = P.relaxPress * (r.R[0] * ax + r.R[1] * ay + r.R[2] * az) * P.coeffPressGrad - f[0];
-    double g1 = P.relaxPress * (r.R[3] * ax + r.R[4] * ay + r.R[5] * az) * P.coeffPressGrad - f[1];
-    double g2 = P.relaxPress * (r.R[6] * ax + r.R[7] * ay + r.R[8] * az) * P.coeffPressGrad - f[2];
+    g[0] = fac * (r.R[0] * ax + r.R[1] * ay + r.R[2] * az) * P.coeffPressGrad - f[0];
+    g[1] = fac * (r.R[3] * ax + r.R[4] * ay + r.R[5] * az) * P.coeffPressGrad - f[1];
+    g[2] = fac * (r.R[6] * ax + r.R[7] * ay + r.R[8] * az) * P.coeffPressGrad - f[2];
+}
+
+// MpsPressure::calcWallPressGradient + repulsive forces, src/MpsPressure.cpp:1341-1611,
+// over the post-prediction neighbour list.
+__global__ void __launch_bounds__(BLK) k_wall_press_grad(Dev d) {
+    int i = nearIndex(d);
+    if (i < 0) return;
+    const MpsParams& P = d.P;
+    dvec4 pi = d.pos[i];
+    double g[3];
+    wallGradTerm(d, i, pi, P.relaxPress, [&](auto&& f) {
+        forNbrs(d, i, [&](int j) { dvec4 pj = d.pos[j]; f(j, pj, pairOf(pj, pi)); });
+    }, g);
     dvec4 a = d.acc[i];
-    a.x += g0 / P.DNS_FL1; a.y += g1 / P.DNS_FL1; a.z += g2 / P.DNS_FL1;
+    a.x += g[0] / P.DNS_FL1; a.y += g[1] / P.DNS_FL1; a.z += g[2] / P.DNS_FL1;
     d.acc[i] = a;
     double vf = (P.dim == 3) ? P.partDist * P.partDist * P.partDist : P.partDist * P.partDist;
     dvec4 fw = d.forceWall[i];
-    fw.x += -g0 * vf; fw.y += -g1 * vf; fw.z += -g2 * vf;
+    fw.x += -g[0] * vf; fw.y += -g[1] * vf; fw.z += -g[2] * vf;
     d.forceWall[i] = fw;
 }
 void launchWallPressGradient(const Dev& d, cudaStream_t s) {
     if (d.P.wallType != 1) return;
     k_wall_press_grad<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d);
+}
+
+// ------------------------------------------------------------------ prediction-step pressure gradient
+// relax_fact < 1 (src/main.cpp:271-276): before the prediction, (1 - relax_fact) of the
+// previous pressure's gradient at the start-of-step positions is added to the
+// acceleration.  The candidates of i in scan order: the start-of-step skin list when it
+// is built for these positions (its entries within the FP32 band of the ball are the
+// candidates the 27-bucket scan passes to the exact FP64 test), else the scan itself.
+template <class F>
+__device__ __forceinline__ void forStartCandidates(const Dev& d, int i, dvec4 pi, float hi, bool skin, F&& f) {
+    const float4 fi = d.posf[i];
+    const int c = skin ? d.skinCnt[i] : d.K + 1;
+    if (c <= d.K) {
+        const int* row = d.skinNbr + i;
+        for (int k = 0; k < c; k++) {
+            const int j = ldStream(row + (size_t)k * d.N0);
+            const float4 fj = d.posf[j];
+            const float ex = fj.x - fi.x, ey = fj.y - fi.y, ez = fj.z - fi.z;
+            if (ex * ex + ey * ey + ez * ez > hi) continue;
+            const dvec4 pj = d.pos[j];
+            f(j, pj, pairOf(pj, pi));
+        }
+    } else {
+        forCellsNear(d, pi, fi, hi, [&](int j, dvec4 pj, PairG q) {
+            if (j != i) f(j, pj, q);
+        });
+    }
+}
+
+// MpsPressure::predictionPressGradient, src/MpsPressure.cpp:932-1028: every particle, the
+// gradient type's pair term without the correction matrix, in the reference's operation
+// order (w(r) from |r|, then times (...)/r^2).
+__global__ void __launch_bounds__(BLK) k_pred_press_grad(Dev d, bool skin) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    const dvec4 pi = d.pos[i];
+    const SideCtx sc = sideCtx(d, i, pi);
+    const double Pi = d.press[i], ni = d.pndi[i];
+    double pmin = Pi;
+    const int gt = P.gradientType;
+    if (gt == 0 || gt == 2) {
+        forStartCandidates(d, i, pi, d.bandHiS, skin, [&](int j, dvec4 pj, PairG q) {
+            if (q.d2 < P.reS2 && sideOK(sc, pj, q.d2)) { double pj_ = d.press[j]; if (pmin > pj_) pmin = pj_; }
+        });
+    }
+    double ax = 0, ay = 0, az = 0;
+    forStartCandidates(d, i, pi, d.bandHiS, skin, [&](int j, dvec4 pj, PairG q) {
+        if (!(q.d2 < P.reS2) || !sideOK(sc, pj, q.d2)) return;
+        double wS = wfun(sqrt(q.d2), P.reS, P.weightType);
+        const double Pj = d.press[j];
+        if (gt == 0) wS *= (Pj - pmin) / q.d2;
+        else if (gt == 1) wS *= (Pj + Pi) / q.d2;
+        else if (gt == 2) wS *= (Pj + Pi - 2.0 * pmin) / q.d2;
+        else if (gt == 3) {
+            const double nj = d.pndi[j];
+            if (ni > P.epsilonZero && nj > P.epsilonZero) wS *= (ni * Pj / nj + nj * Pi / ni) / q.d2;
+        }
+        ax += q.v0 * wS; ay += q.v1 * wS; az += q.v2 * wS;
+    });
+    const double fac = 1.0 - P.relaxPress;
+    dvec4 a = d.acc[i];
+    a.x += fac * ax * P.coeffPressGrad / P.DNS_FL1;
+    a.y += fac * ay * P.coeffPressGrad / P.DNS_FL1;
+    a.z += fac * az * P.coeffPressGrad / P.DNS_FL1;
+    d.acc[i] = a;
+}
+
+// MpsPressure::predictionWallPressGradient, src/MpsPressure.cpp:1031-1214: fluid particles
+// flagged near the wall by the last wall pass (its flags and mirror positions are still
+// held: the prediction resets them after this sweep), no force on the wall.
+__global__ void __launch_bounds__(BLK) k_pred_wall_press_grad(Dev d, bool skin) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    const MpsParams& P = d.P;
+    if (d.type[i] != P.fluid || !d.nearWall[i]) return;
+    const dvec4 pi = d.pos[i];
+    double g[3];
+    wallGradTerm(d, i, pi, 1.0 - P.relaxPress, [&](auto&& f) {
+        forStartCandidates(d, i, pi, d.bandHiS, skin, f);
+    }, g);
+    dvec4 a = d.acc[i];
+    a.x += g[0] / P.DNS_FL1; a.y += g[1] / P.DNS_FL1; a.z += g[2] / P.DNS_FL1;
+    d.acc[i] = a;
+}
+
+void launchPredictPressGradient(const Dev& d, bool skin, cudaStream_t s) {
+    k_pred_press_grad<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d, skin);
+    // the wall sweep reads the accelerations the particle sweep has completed
+    if (d.P.wallType == 1) k_pred_wall_press_grad<<<gridFor(d.N0, BLK), BLK, 0, s>>>(d, skin);
 }
 
 // ------------------------------------------------------------------ wall viscosity

@@ -1,6 +1,7 @@
 """Train the learned PPE warm start on the GPU with libmpsgpu's own kernels.
 
-1. Run the 3D incompressible polygon dam break at l0 = 0.01 m (108,000 particles) with the
+1. Run the 3D incompressible polygon dam break at l0 = 0.01 m (108,000 particles; or, with
+   --config 3, at the evaluation resolution l0 = 0.005 m) with the
    plain FP64 solver (previous-step warm start, tolerance 1e-10) and record, for every
    inner row of every recorded step, the 16 features of the assembled system and the
    difference between the converged pressure and the temporal extrapolation
@@ -38,8 +39,8 @@ def init_params(rng):
     return np.concatenate(p).astype(np.float32)
 
 
-def record(steps, every, tol, scale=1.0, warmup=20):
-    c = cases.config(4, scale=scale)
+def record(steps, every, tol, scale=1.0, warmup=20, config=4):
+    c = cases.config(config, scale=scale)
     g = mps.MpsGpu(c, solver=abi.SOLVER_PLAIN_FP64, tol=tol, max_iter=20000, precision=abi.PRECISION_DF32)
     g.initialize()
     g.run(warmup)
@@ -109,10 +110,14 @@ def main():
     ap.add_argument("--eval-steps", type=int, default=20)
     ap.add_argument("--eval-scale", type=float, default=1.0)
     ap.add_argument("--out", default=DEFAULT_OUT)
+    ap.add_argument("--config", type=int, default=4, choices=[3, 4],
+                    help="recorded workload: 4 = l0 0.01 m (108k particles), 3 = l0 0.005 m (864k, the "
+                         "evaluation resolution)")
+    ap.add_argument("--warmup", type=int, default=20, help="steps before the first recorded one")
     a = ap.parse_args()
     build.build()
     rng = np.random.default_rng(a.seed)
-    g, c, t_rec = record(a.steps, a.every, tol=1e-10)
+    g, c, t_rec = record(a.steps, a.every, tol=1e-10, warmup=a.warmup, config=a.config)
     nrec = g.mlp_num_records()
     g.mlp_set_weights(init_params(rng), np.concatenate([np.zeros(16), np.ones(16), [0.0, 1.0]]).astype(np.float32))
     g.mlp_fit_normalization()

@@ -121,6 +121,43 @@ def test_oracle_neighbors_bruteforce(oracle_mod, k):
         assert list(nbr[off[i]:off[i + 1]]) == sorted(nbr[off[i]:off[i + 1]], key=lambda j: 0) or True
 
 
+@pytest.mark.parametrize("gt", [0, 3])
+def test_oracle_prediction_gradient_bruteforce(oracle_mod, gt):
+    """The oracle's prediction-step pressure gradient (relax_fact < 1,
+    src/MpsPressure.cpp:932-1028) against a brute-force numpy sum over all pairs within
+    reS (particle walls: no mirror-side test) from the same state."""
+    c = cases.config(1, jitter=0.02)
+    c.params.update(relaxPress=0.8, gradientType=gt)
+    o = oracle_mod.Oracle(c)
+    o.set_solver(1e-12)
+    o.initialize()
+    for _ in range(3):
+        o.step()
+    for op in ("UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY"):
+        o.run_op(op)
+    acc0 = o.get(abi.F_ACC)
+    o.run_op("PREDICT_PRESS_GRADIENT")
+    term = o.get(abi.F_ACC) - acc0
+    p = o.params
+    pos, pr, nd = o.get(abi.F_POS), o.get(abi.F_PRESS), o.get(abi.F_PNDI)
+    want = np.zeros_like(pos)
+    for i in range(len(pos)):
+        v = pos - pos[i]
+        d2 = (v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1]) + v[:, 2] * v[:, 2]
+        m = d2 < p.reS2
+        m[i] = False
+        vj, d2j, pj, nj = v[m], d2[m], pr[m], nd[m]
+        w = p.reS / np.sqrt(d2j) - 1.0   # weight type 0
+        if gt == 0:
+            f = w * (pj - min(pr[i], pj.min(initial=np.inf))) / d2j
+        else:
+            ok = (nd[i] > p.epsilonZero) & (nj > p.epsilonZero)
+            f = np.where(ok, w * (nd[i] * pj / nj + nj * pr[i] / nd[i]) / d2j, w)
+        want[i] = (1.0 - p.relaxPress) * (vj * f[:, None]).sum(axis=0) * p.coeffPressGrad / p.DNS_FL1
+    assert np.linalg.norm(want) > 0
+    assert np.linalg.norm(term - want) <= 1e-12 * np.linalg.norm(want)
+
+
 def test_oracle_pcg_vs_scipy(oracle_mod):
     """The oracle's Jacobi-PCG (Eigen's documented CG) against a direct solve."""
     sp = pytest.importorskip("scipy.sparse")

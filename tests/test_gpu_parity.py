@@ -25,7 +25,17 @@ CASES = {
     "cfg2_3d_wc_polygon": lambda: cases.config(2, jitter=0.02, scale=3.0),
     "cfg3_3d_inc_polygon": lambda: cases.config(3, jitter=0.02, scale=5.0),
     "cfg5_3d_obstacle_shifting": lambda: cases.config(5, jitter=0.02, scale=6.0),
+    # relax_fact < 1: the prediction-step pressure gradient (src/main.cpp:271-276), with the
+    # polygon wall and gradient type 2 (p_min sweep), and with particle walls
+    "cfg3_relax_0.7_grad2": lambda: _relaxed(cases.config(3, jitter=0.02, scale=5.0), 0.7, gradientType=2),
+    "cfg1_relax_0.8": lambda: _relaxed(cases.config(1, jitter=0.02), 0.8),
 }
+
+
+def _relaxed(c, relax, **kw):
+    c.params.update(relaxPress=relax, **kw)
+    c.name += "_relax%g" % relax
+    return c
 
 
 def _pair(oracle_mod, mps, case, tol=1e-12):
@@ -66,7 +76,10 @@ def compare(o, g, where, fields=None, ambiguous_ok=0):
 
 
 def step_ops(p):
-    ops = ["UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY", "PREDICT", "OUT_OF_DOMAIN", "COLLISION"]
+    ops = ["UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY"]
+    if p.relaxPress < 1.0:
+        ops += ["PREDICT_PRESS_GRADIENT"]
+    ops += ["PREDICT", "OUT_OF_DOMAIN", "COLLISION"]
     if p.wallType == 1:
         ops += ["WALL_DISTANCE", "WALL_NPCD"]
     if p.gradientCorrection and (p.pndType == 2 or p.mpsType == 3):
@@ -173,6 +186,45 @@ def test_operator_parity_teacher_forced(oracle_mod, mps_lib, name):
             g.run_op(op)
             compare(o, g, "step %d op %s" % (s, op))
             sync(o, g)
+
+
+@pytest.mark.parametrize("name", ["cfg3_relax_0.7_grad2", "cfg1_relax_0.8"])
+@pytest.mark.parametrize("precision", [abi.PRECISION_FP64, abi.PRECISION_DF32])
+def test_prediction_pressure_gradient(oracle_mod, mps_lib, name, precision):
+    """The prediction-step gradient right after the start-of-step sweeps, with no state set
+    in between: the GPU reads the start-of-step skin list built by the viscosity sweep (the
+    teacher-forced test, which sets the state before every operator, covers the bucket
+    scan).  FP64 in both tiers: the acceleration within 1e-10 of the oracle's once the
+    viscosity term (the tier's own) is taken from the oracle."""
+    from polymps_gb300 import mps
+    c = CASES[name]()
+    o = oracle_mod.Oracle(c)
+    o.set_solver(1e-12)
+    g = mps.MpsGpu(c, tol=1e-12, precision=precision)
+    o.initialize()
+    for _ in range(4):
+        o.step()
+    ops = step_ops(o.params)
+    for s in range(2):
+        sync(o, g)
+        o.set_velmax(0.0)   # the GPU handle has run no corrector (wall repulsion reads velMax)
+        for op in ("UPDATE_BUCKETS", "VISCOSITY", "ADD_GRAVITY"):
+            o.run_op(op)
+            g.run_op(op)
+        acc0, gacc0 = o.get(abi.F_ACC), g.get(abi.F_ACC)
+        assert relerr(gacc0, acc0) <= (FP64_RTOL if precision == abi.PRECISION_FP64 else 1e-8)
+        o.run_op("PREDICT_PRESS_GRADIENT")
+        g.run_op("PREDICT_PRESS_GRADIENT")
+        term_o = o.get(abi.F_ACC) - acc0
+        term_g = g.get(abi.F_ACC) - gacc0
+        assert np.linalg.norm(term_o) > 0
+        e = relerr(term_g, term_o)
+        assert e <= FP64_RTOL, "step %d: prediction gradient rel err %.3e" % (s, e)
+        for op in ops[ops.index("PREDICT"):]:   # finish the step, then one more
+            o.run_op(op)
+        o.step()
+    g.close()
+    o.close()
 
 
 @pytest.mark.parametrize("name", ["cfg3_3d_inc_polygon", "cfg1_2d_particle_walls"])

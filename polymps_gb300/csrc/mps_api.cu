@@ -794,17 +794,24 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     if (d.K > 128) { g_lastError = "neighbour row capacity above the 128-entry masks"; mpsgpu_destroy(h); return MPSGPU_ERR_UNSUPPORTED; }
     // mesh and wall tables
     if (p->wallType == 1) {
-        std::vector<double> nrm(3 * mesh->ntri), tab(4 * MPS_TAB);
+        std::vector<double> nrm(3 * mesh->ntri), pln(16 * mesh->ntri), tab(4 * MPS_TAB);
         hostTriNormals(mesh->ntri, mesh->tri_xyz, nrm.data());
+        hostTrianglePlanes(mesh->ntri, mesh->tri_xyz, pln.data());
         hostWallTables(*p, tab.data());
-        double *dt = nullptr, *dn = nullptr, *dtab = nullptr;
+        double *dt = nullptr, *dn = nullptr, *dp = nullptr, *dtab = nullptr;
         A(dt, 9 * mesh->ntri);
         A(dn, 3 * mesh->ntri);
+        A(dp, 16 * mesh->ntri);
         A(dtab, 4 * MPS_TAB);
         cudaMemcpyAsync(dt, mesh->tri_xyz, sizeof(double) * 9 * mesh->ntri, cudaMemcpyHostToDevice, h->s);
         cudaMemcpyAsync(dn, nrm.data(), sizeof(double) * nrm.size(), cudaMemcpyHostToDevice, h->s);
+        cudaMemcpyAsync(dp, pln.data(), sizeof(double) * pln.size(), cudaMemcpyHostToDevice, h->s);
         cudaMemcpyAsync(dtab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, h->s);
-        d.tri = dt; d.triNormal = dn; d.tab = dtab; d.ntri = mesh->ntri;
+        d.tri = dt; d.triNormal = dn; d.triPlane = dp; d.tab = dtab; d.ntri = mesh->ntri;
+        // the reference interpolates at sqrt(reS2) and sqrt(reL2) (src/PolygonMesh.cpp:694-701);
+        // both square roots are correctly rounded, so these are the device's values
+        d.wallReS = std::sqrt(p->reS2);
+        d.wallReL = std::sqrt(p->reL2);
         if (mesh->ntri > MPS_MAX_TRI) {
             // large mesh: triangle BVH (host build, FP32 boxes) and FP32 triangle copies
             std::vector<float> lo4, hi4, tf(9 * (size_t)mesh->ntri);

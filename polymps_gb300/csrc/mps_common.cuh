@@ -141,6 +141,8 @@ struct Dev {
     int ntri;
     const double* tri;          // ntri * 9
     const double* triNormal;    // ntri * 3
+    const double* triPlane;     // ntri * 16: unit normal and offset, three inward edge normals and offsets
+    double wallReS, wallReL;    // sqrt(reS^2), sqrt(reL^2): the radii of the wall tables' interpolation
     const double* tab;          // xPND[50], Z[50], xNeigh[50], nNeigh[50] (as double)
     // meshes above MPS_MAX_TRI triangles: BVH nodes (FP32 boxes relative to domainMin, the
     // .w words hold child indices or leaf ranges), leaf order, FP32 triangle copies

@@ -185,6 +185,37 @@ void hostWallTables(const MpsParams& P, double* tab) {
     }
 }
 
+// Plane data of each triangle for the wall-distance kernel's projection path (16 doubles
+// per triangle): unit normal n and n.a, then for each edge (a,b), (b,c), (c,a) its unit
+// in-plane normal e pointing into the triangle and e.v0.  A degenerate triangle or edge
+// gets zero normals and offsets 1, so no point is ever inside it.
+void hostTrianglePlanes(int ntri, const double* tri, double* planes) {
+    for (int t = 0; t < ntri; t++) {
+        const double* v = tri + 9 * t;
+        double* pl = planes + 16 * t;
+        const double u[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]};
+        const double w[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
+        double n[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+        const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        for (int k = 0; k < 16; k++) pl[k] = (k % 4 == 3) ? 1.0 : 0.0;
+        if (!(nn > 0.0)) continue;
+        for (int k = 0; k < 3; k++) n[k] /= nn;
+        pl[0] = n[0]; pl[1] = n[1]; pl[2] = n[2];
+        pl[3] = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
+        for (int k = 0; k < 3; k++) {
+            const double* p0 = v + 3 * k;
+            const double* p1 = v + 3 * ((k + 1) % 3);
+            const double g[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+            double e[3] = {n[1] * g[2] - n[2] * g[1], n[2] * g[0] - n[0] * g[2], n[0] * g[1] - n[1] * g[0]};
+            const double ee = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+            if (!(ee > 0.0)) continue;
+            double* q = pl + 4 + 4 * k;
+            for (int c = 0; c < 3; c++) q[c] = e[c] / ee;
+            q[3] = q[0] * p0[0] + q[1] * p0[1] + q[2] * p0[2];
+        }
+    }
+}
+
 // Face normals of the triangle soup (igl::per_face_normals, src/PolygonMesh.cpp:98):
 // normalised (v1 - v0) x (v2 - v0).
 void hostTriNormals(int ntri, const double* tri, double* nrm) {

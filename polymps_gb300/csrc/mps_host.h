@@ -6,6 +6,7 @@
 int hostDeriveParams(MpsParams* P, int n, const double* pos);
 void hostWallTables(const MpsParams& P, double* tab);     // 4 x 50 doubles
 void hostTriNormals(int ntri, const double* tri, double* nrm);
+void hostTrianglePlanes(int ntri, const double* tri, double* planes);   // 16 doubles per triangle
 // Bounding-volume hierarchy over the triangles for the wall distance of large meshes:
 // nodes as (lo, hi) boxes in FP32 relative to `origin`, widened outward by one FP32 ulp of
 // every bound so they contain the FP32 copies of the vertices; lo[3]/hi[3] of an internal

@@ -7,7 +7,11 @@
 // it: exact point-triangle closest point (Ericson, Real-Time Collision Detection, 5.1.5),
 // evaluated with explicit round-to-nearest FP64 so the mirror positions, which decide
 // neighbour membership in every later sweep, match the FP64 CPU restatement bit for bit.
-// Ties between triangles go to the lowest index.
+// Ties between triangles go to the lowest index.  A mirror enters a decision only within
+// 1.1 reL of the wall (the side test of the sweeps, the wall sweeps, the near-wall flag);
+// a particle farther than 2 reL whose nearest triangle is the only one within the FP32
+// band and whose projection lies inside it takes that projection in FP64 (the same point
+// up to rounding, a quarter of the FP64 operations).
 #include "mps_common.cuh"
 #include "mps_internal.h"
 
@@ -83,30 +87,46 @@ __device__ float sqDistTriF(float px, float py, float pz, const float* t) {
     return dx * dx + dy * dy + dz * dz;
 }
 
+// The projection of p on the triangle's plane when it lies at least 1e-9 m inside every
+// edge (then Ericson's walk ends in its interior case, whose point is this projection).
+// pl: the triangle's plane data (unit normal n and n.a, then per edge (a,b), (b,c), (c,a)
+// the unit in-plane normal pointing into the triangle and its offset; hostTrianglePlanes).
+__device__ __forceinline__ bool projectInside(const double* pl, double px, double py, double pz, double& qx,
+                                              double& qy, double& qz) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const double* e = pl + 4 + 4 * k;
+        if (!(e[0] * px + e[1] * py + e[2] * pz - e[3] >= 1e-9)) return false;
+    }
+    const double sd = pl[0] * px + pl[1] * py + pl[2] * pz - pl[3];
+    qx = px - sd * pl[0]; qy = py - sd * pl[1]; qz = pz - sd * pl[2];
+    return true;
+}
+
 // PolygonMesh::interpolateWij / interpolateNumNeighWall (src/PolygonMesh.cpp:533-581),
 // linear interpolation with extrapolation over the 50-sample tables
+// (the reference's left-to-right search for the interval, as a binary search with the
+// same comparisons: i = the number of k >= 1 with xs[k] < r)
 __device__ double interpTab(const double* xs, const double* ys, double re, double x) {
     double r = x / re;
-    int i = 0;
+    int i;
     if (r >= xs[MPS_TAB - 2]) i = MPS_TAB - 2;
-    else while (r > xs[i + 1]) i++;
+    else {
+        int lo = 1, hi = MPS_TAB - 2;   // first k in [1, MPS_TAB - 2] with !(xs[k] < r): xs[MPS_TAB - 2] > r
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (xs[mid] < r) lo = mid + 1;
+            else hi = mid;
+        }
+        i = lo - 1;
+    }
     double xL = xs[i], yL = ys[i], xR = xs[i + 1], yR = ys[i + 1];
     double dydx = (yR - yL) / xsub(xR, xL);
     return xadd(yL, xmul(dydx, xsub(r, xL)));
 }
 
-__global__ void __launch_bounds__(128) k_wall_distance(Dev d) {
-    __shared__ double sTri[MPS_MAX_TRI * 9];
-    __shared__ float sTriF[MPS_MAX_TRI * 9];
-    __shared__ double sTab[4 * MPS_TAB];
-    for (int k = threadIdx.x; k < d.ntri * 9; k += blockDim.x) {
-        sTri[k] = d.tri[k];
-        sTriF[k] = (float)(d.tri[k] - d.P.domainMin[k % 3]);
-    }
-    for (int k = threadIdx.x; k < 4 * MPS_TAB; k += blockDim.x) sTab[k] = d.tab[k];
-    __syncthreads();
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= liveN(d)) return;
+__device__ __forceinline__ void wallDistanceAt(const Dev& d, int i, const double* sTri, const float* sTriF,
+                                               const double* sTab, const double* sPl) {
     const MpsParams& P = d.P;
     dvec4 p = d.pos[i];
     // FP32 pass over all triangles (coordinates relative to the domain corner)
@@ -123,13 +143,24 @@ __global__ void __launch_bounds__(128) k_wall_distance(Dev d) {
     double best = 1.0 / 0.0;
     int bt = -1;
     double bx = 0, by = 0, bz = 0;
-    for (int t = 0; t < d.ntri; t++) {
-        if (df[t] > lim) continue;
-        double qx, qy, qz;
-        closestPtTriX(p.x, p.y, p.z, sTri + t * 9, qx, qy, qz);
+    int inBand = 0, only = -1;
+    for (int t = 0; t < d.ntri; t++)
+        if (df[t] <= lim) { inBand++; only = t; }
+    // far from the wall (beyond 2 reL with the FP32 band to spare), one candidate: the
+    // FP64 projection when it lies inside the triangle
+    double qx, qy, qz;
+    if (inBand == 1 && bestf > (float)(4.0 * P.reL2) + 1e-4f && projectInside(sPl + only * 16, p.x, p.y, p.z, qx, qy, qz)) {
         double dx = xsub(p.x, qx), dy = xsub(p.y, qy), dz = xsub(p.z, qz);
-        double d2 = xnorm2(dx, dy, dz);
-        if (d2 < best) { best = d2; bt = t; bx = qx; by = qy; bz = qz; }
+        best = xnorm2(dx, dy, dz);
+        bt = only; bx = qx; by = qy; bz = qz;
+    } else {
+        for (int t = 0; t < d.ntri; t++) {
+            if (df[t] > lim) continue;
+            closestPtTriX(p.x, p.y, p.z, sTri + t * 9, qx, qy, qz);
+            double dx = xsub(p.x, qx), dy = xsub(p.y, qy), dz = xsub(p.z, qz);
+            double d2 = xnorm2(dx, dy, dz);
+            if (d2 < best) { best = d2; bt = t; bx = qx; by = qy; bz = qz; }
+        }
     }
     double riw2 = d.riw2[i];
     if (bt >= 0 && best < riw2) {
@@ -146,11 +177,30 @@ __global__ void __launch_bounds__(128) k_wall_distance(Dev d) {
     if (riw2 < P.reL2) {
         d.nearWall[i] = 1;
         double x = sqrt(riw2);
-        pw = interpTab(sTab, sTab + MPS_TAB, sqrt(P.reS2), x);
-        nw = (int)interpTab(sTab + 2 * MPS_TAB, sTab + 3 * MPS_TAB, sqrt(P.reL2), x);
+        pw = interpTab(sTab, sTab + MPS_TAB, d.wallReS, x);
+        nw = (int)interpTab(sTab + 2 * MPS_TAB, sTab + 3 * MPS_TAB, d.wallReL, x);
     }
     d.pndWall[i] = pw;
     d.nNeighWall[i] = nw;
+}
+
+// Each block stages the triangles, their FP32 copies, plane data and the wall tables in
+// shared memory; one particle per thread (a grid-stride loop over fewer resident blocks
+// measured slower: 0.263 vs 0.225 ms at 864k).
+__global__ void __launch_bounds__(128) k_wall_distance(Dev d) {
+    __shared__ double sTri[MPS_MAX_TRI * 9];
+    __shared__ float sTriF[MPS_MAX_TRI * 9];
+    __shared__ double sTab[4 * MPS_TAB];
+    __shared__ double sPl[MPS_MAX_TRI * 16];
+    for (int k = threadIdx.x; k < d.ntri * 9; k += blockDim.x) {
+        sTri[k] = d.tri[k];
+        sTriF[k] = (float)(d.tri[k] - d.P.domainMin[k % 3]);
+    }
+    for (int k = threadIdx.x; k < 4 * MPS_TAB; k += blockDim.x) sTab[k] = d.tab[k];
+    for (int k = threadIdx.x; k < d.ntri * 16; k += blockDim.x) sPl[k] = d.triPlane[k];
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < liveN(d)) wallDistanceAt(d, i, sTri, sTriF, sTab, sPl);
 }
 
 // Meshes above MPS_MAX_TRI triangles (libigl's AABB query for large meshes): depth-first
@@ -257,8 +307,8 @@ __global__ void __launch_bounds__(128) k_wall_distance_bvh(Dev d) {
     if (riw2 < P.reL2) {
         d.nearWall[i] = 1;
         double x = sqrt(riw2);
-        pw = interpTab(sTab, sTab + MPS_TAB, sqrt(P.reS2), x);
-        nw = (int)interpTab(sTab + 2 * MPS_TAB, sTab + 3 * MPS_TAB, sqrt(P.reL2), x);
+        pw = interpTab(sTab, sTab + MPS_TAB, d.wallReS, x);
+        nw = (int)interpTab(sTab + 2 * MPS_TAB, sTab + 3 * MPS_TAB, d.wallReL, x);
     }
     d.pndWall[i] = pw;
     d.nNeighWall[i] = nw;

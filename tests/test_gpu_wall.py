@@ -1,6 +1,7 @@
-"""Wall distance and mirror particles for meshes above the brute-force kernel's 64
-triangles (the triangle BVH walk): bit-exact against the oracle's brute force over all
-triangles (PolygonMesh::closestPointPNDBoundaryAABB, src/PolygonMesh.cpp:585-715)."""
+"""Wall distance and mirror particles against the oracle's brute force over all triangles
+(PolygonMesh::closestPointPNDBoundaryAABB, src/PolygonMesh.cpp:585-715): the triangle BVH
+walk of meshes above 64 triangles bit for bit, the brute-force kernel bit for bit within
+2 reL of the wall and to rounding beyond."""
 import numpy as np
 import pytest
 
@@ -47,6 +48,39 @@ def test_wall_distance_large_mesh(oracle_mod, mps_lib, levels, precision):
               abi.F_NEARWALL):
         assert np.array_equal(g.get(f), o.get(f)), abi.FIELD_NAMES[f]
     assert g.get(abi.F_NEARWALL).sum() > 0
+    g.close()
+
+
+@pytest.mark.parametrize("cfg,scale", [(3, 5.0), (5, 6.0)])
+def test_wall_distance_near_exact_far_projected(oracle_mod, mps_lib, cfg, scale):
+    """The brute-force kernel (meshes up to 64 triangles): within 2 reL of the wall (where
+    mirrors enter the sweeps' decisions) wall point, mirror and squared distance are the
+    oracle's bit for bit; farther out the FP64 projection on the nearest triangle agrees
+    with Ericson's walk to rounding; flags, normals and the wall tables' values exactly."""
+    from polymps_gb300 import mps
+    c = cases.config(cfg, jitter=0.02, scale=scale)
+    o = oracle_mod.Oracle(c)
+    g = mps.MpsGpu(c, tol=1e-12)
+    o.set_solver(1e-12)
+    o.initialize()
+    for _ in range(3):
+        o.step()
+    ops = step_ops(o.params)
+    sync(o, g)
+    for op in ops[: ops.index("WALL_DISTANCE")]:
+        o.run_op(op)
+    sync(o, g)
+    o.run_op("WALL_DISTANCE")
+    g.run_op("WALL_DISTANCE")
+    near = o.get(abi.F_RIW2) < 4.0 * o.params.reL2
+    assert 0 < near.sum() < len(near)
+    for f in (abi.F_POLYNORMAL, abi.F_PNDWALL, abi.F_NNEIGHWALL, abi.F_NEARWALL):
+        assert np.array_equal(g.get(f), o.get(f)), abi.FIELD_NAMES[f]
+    for f in (abi.F_RIW2, abi.F_WALLPOS, abi.F_MIRROR):
+        a, b = g.get(f), o.get(f)
+        assert np.array_equal(a[near], b[near]), abi.FIELD_NAMES[f]
+        tol = 1e-15 * 16 if f == abi.F_RIW2 else 1e-15 * 8
+        assert np.max(np.abs(a[~near] - b[~near])) <= tol * max(1.0, np.max(np.abs(b))), abi.FIELD_NAMES[f]
     g.close()
 
 

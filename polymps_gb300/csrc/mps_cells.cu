@@ -47,8 +47,8 @@ __global__ void k_cell_key(Dev d) {
         }
         atomicAdd(d.cellCount + key, 1);
         // FP32 copy of the start-of-step positions for the prefiltered scans
-        float4 hi = make_float4((float)(p.x - P.domainMin[0]), (float)(p.y - P.domainMin[1]),
-                                (float)(p.z - P.domainMin[2]), 0.f);
+        float4 hi = make_float4(d2fRN(p.x - P.domainMin[0]), d2fRN(p.y - P.domainMin[1]),
+                                d2fRN(p.z - P.domainMin[2]), 0.f);
         d.posf[i] = hi;
         d.posLo[i] = posLoOf(p, hi, P);
     }
@@ -226,8 +226,8 @@ __global__ void k_posf(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.N0) return;   // every slot: stale bucket entries may name removed particles
     dvec4 p = d.pos[i];
-    float4 hi = make_float4((float)(p.x - d.P.domainMin[0]), (float)(p.y - d.P.domainMin[1]),
-                            (float)(p.z - d.P.domainMin[2]), 0.f);
+    float4 hi = make_float4(d2fRN(p.x - d.P.domainMin[0]), d2fRN(p.y - d.P.domainMin[1]),
+                            d2fRN(p.z - d.P.domainMin[2]), 0.f);
     d.posf[i] = hi;
     d.posLo[i] = posLoOf(p, hi, d.P);
 }

@@ -179,6 +179,49 @@ __device__ __forceinline__ double xdot3(double ax, double ay, double az, double 
 }
 __device__ __forceinline__ double xnorm2(double x, double y, double z) { return xdot3(x, y, z, x, y, z); }
 
+// ------------------------------------------------------------------ FP32 <-> FP64 conversions
+// The conversion instructions run on the FP64 pipe, at 1/64 of the FP32 rate on GB300 like
+// FP64 arithmetic; these build the same bits with integer operations.
+// float -> double (exact: every float is a double; NaN payloads are kept).
+__device__ __forceinline__ double f2dExact(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+    const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    unsigned long long b;
+    if (e == 0xffu) b = s | 0x7ff0000000000000ull | ((unsigned long long)m << 29);   // inf, NaN
+    else if (e != 0u) b = s | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    else if (m == 0u) b = s;                                                           // +-0
+    else {   // subnormal float m 2^-149: the leading one at bit p, exponent p - 149
+        const int p = 31 - __clz((int)m);
+        b = s | ((unsigned long long)(p + 874) << 52) | (((unsigned long long)m << (52 - p)) & 0xfffffffffffffull);
+    }
+    return __longlong_as_double((long long)b);
+}
+// double -> float rounded to nearest, ties to even (as __double2float_rn): the 52-bit
+// significand rounded to 23 bits, a carry moving into the exponent (up to infinity);
+// float-subnormal results shifted and rounded the same way; NaN gives the canonical NaN.
+__device__ __forceinline__ float d2fRN(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned s = (unsigned)(b >> 32) & 0x80000000u;
+    const unsigned E = (unsigned)(b >> 52) & 0x7ffu;
+    const unsigned long long M = b & 0xfffffffffffffull;
+    if (E == 0x7ffu) return __uint_as_float(M ? 0x7fffffffu : (s | 0x7f800000u));
+    if (E >= 1151u) return __uint_as_float(s | 0x7f800000u);   // at least 2^128: infinity
+    if (E < 897u) {                                            // below 2^-126: subnormal or zero
+        if (E < 873u) return __uint_as_float(s);
+        const unsigned long long m53 = M | (1ull << 52);
+        const unsigned sh = 926u - E;                           // 30 .. 53
+        unsigned long long q = m53 >> sh;
+        const unsigned long long rem = m53 & ((1ull << sh) - 1ull), half = 1ull << (sh - 1u);
+        q += (rem > half || (rem == half && (q & 1ull))) ? 1ull : 0ull;
+        return __uint_as_float(s | (unsigned)q);
+    }
+    unsigned mh = (unsigned)(M >> 29);
+    const unsigned rem = (unsigned)(M & 0x1fffffffu);
+    mh += (rem > 0x10000000u || (rem == 0x10000000u && (mh & 1u))) ? 1u : 0u;
+    return __uint_as_float(s | (((E - 896u) << 23) + mh));
+}
+
 // MpsBucket::bucketCoordinates, src/MpsBucket.cpp:420-425: (int)((x - min) * inv + eps)
 __device__ __forceinline__ void bucketCoords(const MpsParams& P, double x, double y, double z,
                                              int& bx, int& by, int& bz) {
@@ -190,18 +233,28 @@ __device__ __forceinline__ void bucketCoords(const MpsParams& P, double x, doubl
 // The same coordinates from hi = fl32(x - min) (the particle's current FP32 copy): the FP32
 // quotient is within 4 * 2^-24 relative of the FP64 one, so its truncation is exact unless
 // it lies within a margin of an integer (or below it), where the FP64 expression decides.
-__device__ __forceinline__ int bucketCoord1(float h, double x, double mn, const MpsParams& P, float inv, float eps) {
+// The FP64 expressions sit out of line, for all three coordinates at once: inlined, the
+// compiler predicates them into every call and their twelve FP64-pipe instructions then run
+// for every particle.
+static __device__ __noinline__ int3 bucketCoordsExact(const MpsParams& P, double x, double y, double z) {
+    int3 b;
+    bucketCoords(P, x, y, z, b.x, b.y, b.z);
+    return b;
+}
+__device__ __forceinline__ bool bucketCoord1(float h, float inv, float eps, int& b) {
     const float q = fmaf(h, inv, eps);
     const float m = 5e-7f * fabsf(q) + 1e-6f;
     const float f = q - floorf(q);
-    if (q > m && f > m && f < 1.0f - m) return (int)q;
-    return (int)xadd(xmul(xsub(x, mn), P.invBucketSide), P.epsilonZero);
+    b = (int)q;
+    return q > m && f > m && f < 1.0f - m;
 }
 __device__ __forceinline__ void bucketCoordsHi(const Dev& d, dvec4 p, float4 hi, int& bx, int& by, int& bz) {
-    const MpsParams& P = d.P;
-    bx = bucketCoord1(hi.x, p.x, P.domainMin[0], P, d.invSidef, d.epsf);
-    by = bucketCoord1(hi.y, p.y, P.domainMin[1], P, d.invSidef, d.epsf);
-    bz = bucketCoord1(hi.z, p.z, P.domainMin[2], P, d.invSidef, d.epsf);
+    const bool ok = bucketCoord1(hi.x, d.invSidef, d.epsf, bx) & bucketCoord1(hi.y, d.invSidef, d.epsf, by) &
+                    bucketCoord1(hi.z, d.invSidef, d.epsf, bz);
+    if (!ok) {
+        const int3 b = bucketCoordsExact(d.P, p.x, p.y, p.z);
+        bx = b.x; by = b.y; bz = b.z;
+    }
 }
 
 // PPE source of an equation row: PND deviation (src/MpsPressure.cpp:256), or with the
@@ -344,23 +397,28 @@ __device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col,
     return __ldg(diag + i) * xi + (((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
 }
 
+// f(j, e, k) for the entries k of the mask (e = k N0 + i, the entry's ELL index).
 template <class F>
-__device__ __forceinline__ void forMask(const Dev& d, int i, Mask m, F&& f) {
+__device__ __forceinline__ void forMaskK(const Dev& d, int i, Mask m, F&& f) {
     const int* row = d.nbr + i;
     unsigned long long w = m.lo;   // entries 0..63, then 64..127 (rarely any)
     while (w) {
         const int k = __ffsll((long long)w) - 1;
         w &= w - 1ull;
         const size_t e = (size_t)k * d.N0 + i;
-        f(ldStream(row + e - i), e);
+        f(ldStream(row + e - i), e, k);
     }
     w = m.hi;
     while (w) {
         const int k = __ffsll((long long)w) + 63;
         w &= w - 1ull;
         const size_t e = (size_t)k * d.N0 + i;
-        f(ldStream(row + e - i), e);
+        f(ldStream(row + e - i), e, k);
     }
+}
+template <class F>
+__device__ __forceinline__ void forMask(const Dev& d, int i, Mask m, F&& f) {
+    forMaskK(d, i, m, [&](int j, size_t e, int) { f(j, e); });
 }
 
 // Weight for a squared distance through 1/r (rsqrt): w and w/r^2 (MpsParticle::weight,

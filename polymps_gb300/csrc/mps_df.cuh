@@ -66,12 +66,13 @@ __device__ __forceinline__ df& operator-=(df& a, df b) { a = a - b; return a; }
 __device__ __forceinline__ bool operator<(df a, df b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
 __device__ __forceinline__ bool operator>(df a, df b) { return b < a; }
 
-// conversions (FP64: per particle, not per pair)
+// conversions (per particle and per stored value; one FP64 addition each, the FP32 <-> FP64
+// conversions in integer operations)
 __device__ __forceinline__ df dfD(double x) {
-    float h = __double2float_rn(x);
-    return {h, __double2float_rn(x - (double)h)};
+    float h = d2fRN(x);
+    return {h, d2fRN(x - f2dExact(h))};
 }
-__device__ __forceinline__ double dD(df a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ double dD(df a) { return f2dExact(a.h) + f2dExact(a.l); }
 
 // 1/sqrt(a) for a > 0: FP32 estimate refined by one Newton step in float-float
 // (y1 = y + y (1 - a y^2) / 2; the estimate's relative error ~2^-22 becomes ~2^-44).
@@ -87,9 +88,8 @@ __device__ __forceinline__ df rsqrtDF(df a) {
 // Positions are held relative to domainMin as hi = fl32(x - min) (the posf copy the
 // prefilters already read) and lo = fl32((x - min) - hi): |x - min - hi - lo| <= 2^-48 |x - min|.
 __device__ __forceinline__ float4 posLoOf(dvec4 p, float4 hi, const MpsParams& P) {
-    return make_float4(__double2float_rn((p.x - P.domainMin[0]) - (double)hi.x),
-                       __double2float_rn((p.y - P.domainMin[1]) - (double)hi.y),
-                       __double2float_rn((p.z - P.domainMin[2]) - (double)hi.z), 0.f);
+    return make_float4(d2fRN((p.x - P.domainMin[0]) - f2dExact(hi.x)), d2fRN((p.y - P.domainMin[1]) - f2dExact(hi.y)),
+                       d2fRN((p.z - P.domainMin[2]) - f2dExact(hi.z)), 0.f);
 }
 
 struct V3 {
@@ -170,8 +170,7 @@ __device__ __forceinline__ SideDF sideDF(const Dev& d, int i, dvec4 pi) {
     s.check = (a * a + b * b + c * c) <= lim * lim;
     if (s.check) {
         const MpsParams& P = d.P;
-        s.mh = make_float4((float)(m.x - P.domainMin[0]), (float)(m.y - P.domainMin[1]),
-                           (float)(m.z - P.domainMin[2]), 0.f);
+        s.mh = make_float4(d2fRN(m.x - P.domainMin[0]), d2fRN(m.y - P.domainMin[1]), d2fRN(m.z - P.domainMin[2]), 0.f);
         s.ml = posLoOf(m, s.mh, P);
     }
     return s;

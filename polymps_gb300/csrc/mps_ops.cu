@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(BLK) k_pnd_diffusive(Dev d) {
     double invNi = 1.0 / ni;
     const Mask mL = d.maskL[i], mS = d.maskS[i] & mL;
     const double* wLc = d.cwL ? d.cwL : d.cw;
-    forMask(d, i, mL, [&](int j, size_t e) {
+    forMaskK(d, i, mL, [&](int j, size_t e, int k) {
         dvec4 pj = d.pos[j];
         double v0 = pj.x - pi.x, v1 = pj.y - pi.y, v2 = pj.z - pi.z;
         double wL = wLc[e];
@@ -595,7 +595,6 @@ __global__ void __launch_bounds__(BLK) k_pnd_diffusive(Dev d) {
             double pgh = -2.0 * (rho * rho / (rho + rho)) * (P.gravity[0] * v0 + P.gravity[1] * v1 + P.gravity[2] * v2);
             Di += P.timeStep / rho * P.coeffViscMultiphase * (d.press[j] - Pi - pgh) * wL;
         }
-        int k = (int)((e - i) / d.N0);
         if (maskHas(mS, k)) {
             dvec4 vj = d.vel[j];
             double vx = vj.x - vi.x, vy = vj.y - vi.y, vz = vj.z - vi.z;

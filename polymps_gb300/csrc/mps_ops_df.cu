@@ -17,10 +17,9 @@ __global__ void k_df_vel(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.N0) return;
     dvec4 v = d.vel[i];
-    float4 h = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+    float4 h = make_float4(d2fRN(v.x), d2fRN(v.y), d2fRN(v.z), 0.f);
     d.velHi[i] = h;
-    d.velLo[i] = make_float4(__double2float_rn(v.x - (double)h.x), __double2float_rn(v.y - (double)h.y),
-                             __double2float_rn(v.z - (double)h.z), 0.f);
+    d.velLo[i] = make_float4(d2fRN(v.x - f2dExact(h.x)), d2fRN(v.y - f2dExact(h.y)), d2fRN(v.z - f2dExact(h.z)), 0.f);
 }
 __global__ void k_df_press(Dev d) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -248,7 +247,7 @@ struct MirrorDF {
 __device__ __forceinline__ MirrorDF mirrorDF(const Dev& d, dvec4 m) {
     MirrorDF o;
     const MpsParams& P = d.P;
-    o.mh = make_float4((float)(m.x - P.domainMin[0]), (float)(m.y - P.domainMin[1]), (float)(m.z - P.domainMin[2]), 0.f);
+    o.mh = make_float4(d2fRN(m.x - P.domainMin[0]), d2fRN(m.y - P.domainMin[1]), d2fRN(m.z - P.domainMin[2]), 0.f);
     o.ml = posLoOf(m, o.mh, P);
     return o;
 }
@@ -465,7 +464,7 @@ __global__ void __launch_bounds__(128, 12) k_ppe_assemble_df(Dev d, PpeBuffers B
     df sum = dfF(0.f), src = dfF(0.f);
     int len = 0;
     Mask mm = maskNone();
-    forMask(d, i, d.maskL[i], [&](int j, size_t e) {
+    forMaskK(d, i, d.maskL[i], [&](int j, size_t, int ke) {
         PairF q = pairDF(d.posf[j], d.posLo[j], hi, li);
         df wL = weightDF(q.d2, RL, P.weightType).w;
         if (d.type[j] == P.dummyWall) {
@@ -479,7 +478,7 @@ __global__ void __launch_bounds__(128, 12) k_ppe_assemble_df(Dev d, PpeBuffers B
                 B.valf[k] = mij.h;   // the FP32 copy of the mixed solver (hi part = fl32)
                 B.col[k] = j;
                 len++;
-                maskSet(mm, (int)((e - i) / d.N0));
+                maskSet(mm, ke);
             }
         }
     });

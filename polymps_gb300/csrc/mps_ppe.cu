@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
     int len = 0;
     Mask mm = maskNone();
     const double* wLc = d.cwL ? d.cwL : d.cw;
-    forMask(d, i, d.maskL[i], [&](int j, size_t e) {
+    forMaskK(d, i, d.maskL[i], [&](int j, size_t e, int ke) {
         double wL = wLc[e];
         double mij = wL * P.coeffPPE;
         if (d.type[j] == P.dummyWall) {
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
                 B.val[k] = mij;
                 B.col[k] = j;
                 len++;
-                maskSet(mm, (int)((e - i) / d.N0));
+                maskSet(mm, ke);
             }
         }
     });

@@ -1391,8 +1391,8 @@ __global__ void k_apply_shift(Dev d) {
     dvec4 x = d.pos[i], s = d.shift[i];
     x.x += s.x; x.y += s.y; x.z += s.z;
     d.pos[i] = x;
-    float4 hi = make_float4((float)(x.x - d.P.domainMin[0]), (float)(x.y - d.P.domainMin[1]),
-                            (float)(x.z - d.P.domainMin[2]), 0.f);
+    float4 hi = make_float4(d2fRN(x.x - d.P.domainMin[0]), d2fRN(x.y - d.P.domainMin[1]),
+                            d2fRN(x.z - d.P.domainMin[2]), 0.f);
     d.posf[i] = hi;
     d.posLo[i] = posLoOf(x, hi, d.P);
 }

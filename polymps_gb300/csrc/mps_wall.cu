@@ -130,7 +130,7 @@ __device__ __forceinline__ void wallDistanceAt(const Dev& d, int i, const double
     const MpsParams& P = d.P;
     dvec4 p = d.pos[i];
     // FP32 pass over all triangles (coordinates relative to the domain corner)
-    float pxf = (float)(p.x - P.domainMin[0]), pyf = (float)(p.y - P.domainMin[1]), pzf = (float)(p.z - P.domainMin[2]);
+    float pxf = d2fRN(p.x - P.domainMin[0]), pyf = d2fRN(p.y - P.domainMin[1]), pzf = d2fRN(p.z - P.domainMin[2]);
     float df[MPS_MAX_TRI];
     float bestf = 3.0e38f;
     for (int t = 0; t < d.ntri; t++) {
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(128) k_wall_distance(Dev d) {
     __shared__ double sPl[MPS_MAX_TRI * 16];
     for (int k = threadIdx.x; k < d.ntri * 9; k += blockDim.x) {
         sTri[k] = d.tri[k];
-        sTriF[k] = (float)(d.tri[k] - d.P.domainMin[k % 3]);
+        sTriF[k] = d2fRN(d.tri[k] - d.P.domainMin[k % 3]);
     }
     for (int k = threadIdx.x; k < 4 * MPS_TAB; k += blockDim.x) sTab[k] = d.tab[k];
     for (int k = threadIdx.x; k < d.ntri * 16; k += blockDim.x) sPl[k] = d.triPlane[k];
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(128) k_wall_distance_bvh(Dev d) {
     if (i >= liveN(d)) return;
     const MpsParams& P = d.P;
     dvec4 p = d.pos[i];
-    const float px = (float)(p.x - P.domainMin[0]), py = (float)(p.y - P.domainMin[1]), pz = (float)(p.z - P.domainMin[2]);
+    const float px = d2fRN(p.x - P.domainMin[0]), py = d2fRN(p.y - P.domainMin[1]), pz = d2fRN(p.z - P.domainMin[2]);
     int stack[BVH_STACK];
     int cand[BVH_CAND];
     float candD[BVH_CAND];

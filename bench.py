@@ -421,14 +421,17 @@ def _ppe_summary(ppe, early):
         return None
     keep = {"quadratic": "quadratic_extrapolated_fp32_fp64", "learned": "learned_fp32_fp64",
             "previous": "fp32_fp64_refinement", "linear": "extrapolated_fp32_fp64"}
-    s = {"systems": ppe["systems"], "steps": ppe["steps_sampled"], "plain_fp64_ms": ppe["plain_fp64"]["ms"],
+    def sp(x):   # the printed line carries speed-ups to 2 decimals (3 in the detail file)
+        return None if x is None else round(x, 2)
+    s = {"systems": ppe["systems"], "steps": ppe["steps_sampled"], "plain_fp64_ms": round(ppe["plain_fp64"]["ms"], 2),
          "plain_fp64_iters": ppe["plain_fp64"]["iters"],
-         "speedup_vs_plain": {k: ppe[v]["speedup_vs_plain"] for k, v in keep.items() if v in ppe},
-         "max_rel_err_vs_plain": max(ppe[v].get("rel_err_vs_fp64_max", 0.0) for v in keep.values() if v in ppe)}
+         "speedup_vs_plain": {k: sp(ppe[v]["speedup_vs_plain"]) for k, v in keep.items() if v in ppe},
+         "max_rel_err_vs_plain": float("%.2g" % max(ppe[v].get("rel_err_vs_fp64_max", 0.0) for v in keep.values()
+                                                    if v in ppe))}
     if early:
         s["early"] = {"systems": early["systems"], "steps": early["steps_sampled"],
-                      "plain_fp64_ms": early["plain_fp64"]["ms"],
-                      "speedup_vs_plain": {k: early[v]["speedup_vs_plain"] for k, v in keep.items() if v in early}}
+                      "plain_fp64_ms": round(early["plain_fp64"]["ms"], 2),
+                      "speedup_vs_plain": {k: sp(early[v]["speedup_vs_plain"]) for k, v in keep.items() if v in early}}
     return s
 
 
@@ -569,7 +572,7 @@ def cpu_baseline(case, steps):
     dt = _oracle_steps(case, cores, steps)
     d1 = _oracle_steps(case, 1, 1)
     out = {"value": round(case.n * steps / dt, 1), "unit": "particle-steps/s", "cores": cores, "kind": "port",
-           "sample": "%d step(s) of this workload after init (%.1f s)" % (steps, dt),
+           "sample": "%d step(s) of this workload (%.1f s)" % (steps, dt),
            "single_thread": round(case.n / d1, 1)}
     more = {"single_thread_sample": "1 step (%.1f s)" % d1}
     # the 2D particle-wall dam break run to its configured 200 steps, and a window of the

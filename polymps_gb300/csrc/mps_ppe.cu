@@ -479,12 +479,17 @@ struct QCtl {
 struct QLocal {
     double scal[32];
     int flag[8];
+    float scalf[4];   // FP32 copies of the inner-CG step scalars (SF_*), formed once by thread 0
 };
+#define SF_ALPHA 0
+#define SF_BETA 1
 __device__ __forceinline__ void qInit(QLocal& L) {
     for (int t = threadIdx.x; t < 32; t += blockDim.x) L.scal[t] = 0.0;
     for (int t = threadIdx.x; t < 8; t += blockDim.x) L.flag[t] = 0;
+    for (int t = threadIdx.x; t < 4; t += blockDim.x) L.scalf[t] = 0.f;
     __syncthreads();
 }
+__device__ __forceinline__ float vf(const float* p) { return *(volatile const float*)p; }
 // block 0's scalars and flags to the global words the host reads
 __device__ __forceinline__ void qStore(const PpeBuffers& B, const QLocal& L) {
     __syncthreads();
@@ -548,21 +553,55 @@ __device__ __forceinline__ bool qSum(double (&v)[NV], const PpeBuffers& B, QCtl&
     __syncthreads();
     return true;
 }
-// The same with float-float per-thread partials (FP32 vectors): the warp reduces in
-// float-float, each warp's total is converted to FP64 once, the rest of the sum is FP64.
+// The same with float-float per-thread partials (FP32 vectors), reduced in float-float all
+// the way: the warps' shuffle trees, the block's sum of its warps, the block partials (two
+// floats in the same partial slots) and the final sum over the blocks, converted to FP64
+// once for fin.  In FP64 the shuffle trees of every warp and the final sum ran on the FP64
+// pipe (1/64 of the FP32 rate) between the last arrival and the release of every barrier.
+__device__ __forceinline__ df shflXorDF(df a, int o) {
+    return {__shfl_xor_sync(0xffffffffu, a.h, o), __shfl_xor_sync(0xffffffffu, a.l, o)};
+}
 template <int NV, class Fin>
 __device__ __forceinline__ bool qSumDF(df (&a)[NV], const PpeBuffers& B, QCtl& c, Fin fin) {
-    double v[NV];
+    __shared__ float2 sm[NV * 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int q = 0; q < NV; q++) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            df b = {__shfl_xor_sync(0xffffffffu, a[q].h, o), __shfl_xor_sync(0xffffffffu, a[q].l, o)};
-            a[q] = a[q] + b;
-        }
-        v[q] = ((threadIdx.x & 31) == 0) ? dD(a[q]) : 0.0;
+        for (int o = 16; o > 0; o >>= 1) a[q] += shflXorDF(a[q], o);
+        if (lane == 0) sm[q * 32 + w] = make_float2(a[q].h, a[q].l);
     }
-    return qSum<NV>(v, B, c, fin);
+    __syncthreads();
+    float2* part = reinterpret_cast<float2*>(B.partials + (size_t)(c.gen & 1u) * 4u * gridDim.x);
+    if (w == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            const float2 x = (lane < nw) ? sm[q * 32 + lane] : make_float2(0.f, 0.f);
+            df s = {x.x, x.y};
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += shflXorDF(s, o);
+            if (lane == 0) part[q * gridDim.x + blockIdx.x] = make_float2(s.h, s.l);
+        }
+    }
+    if (!qBarrier(B, c)) return false;
+    if (threadIdx.x < 32) {   // warp 0: lane-strided partial sums, then a fixed shuffle tree
+        double tot[NV];
+#pragma unroll
+        for (int q = 0; q < NV; q++) {
+            df s = dfF(0.f);
+            for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
+                // both floats in one volatile 8-byte load (x at the lower address)
+                const unsigned long long u = ((volatile unsigned long long*)part)[q * gridDim.x + b];
+                s += df{__uint_as_float((unsigned)u), __uint_as_float((unsigned)(u >> 32))};
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += shflXorDF(s, o);
+            tot[q] = dD(s);
+        }
+        if (threadIdx.x == 0) fin(tot);
+    }
+    __syncthreads();
+    return true;
 }
 
 // Rows inside the persistent kernels: matrix arrays are read-only for the launch, the
@@ -1204,7 +1243,7 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_own(Dev d, PpeBuffers B, double t
         int inner = 0;
         while (true) {
             {   // Ap = A z + beta Ap, p = z + beta p, p.Ap
-                const float beta = inner ? (float)vd(qS + S_BETA) : 0.f;
+                const float beta = inner ? vf(qL.scalf + SF_BETA) : 0.f;
                 df a[1] = {dfF(0.f)};
                 forRowsL(B, rs, [&](int l, int i, int len) {
                     const float q = qRowF(B, B.zf, i, len);
@@ -1214,11 +1253,15 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_own(Dev d, PpeBuffers B, double t
                     sap[l] = ap; sp[l] = p;
                     a[0] += prod2(p, ap);
                 });
-                if (!qSumDF<1>(a, B, c, [&](const double* t) { qS[S_PAP] = t[0]; qS[S_ALPHA] = qS[S_RZ] / t[0]; }))
+                if (!qSumDF<1>(a, B, c, [&](const double* t) {
+                        qS[S_PAP] = t[0];
+                        qS[S_ALPHA] = qS[S_RZ] / t[0];
+                        qL.scalf[SF_ALPHA] = d2fRN(qS[S_ALPHA]);
+                    }))
                     return;
             }
             {   // x_f += alpha p, r -= alpha Ap, z = M^-1 r; r.z, r.r
-                const float alpha = (float)vd(qS + S_ALPHA);
+                const float alpha = vf(qL.scalf + SF_ALPHA);
                 df a[2] = {dfF(0.f), dfF(0.f)};
                 const int cnt = rowCount(rs);
                 for (int m0 = 0; m0 < cnt; m0 += 4) {
@@ -1245,6 +1288,7 @@ __global__ void __launch_bounds__(QBX, 1) k_mx_own(Dev d, PpeBuffers B, double t
                 if (!qSumDF<2>(a, B, c, [&](const double* t) {
                         qF[1] += 1;
                         qS[S_BETA] = t[0] / qS[S_RZ];
+                        qL.scalf[SF_BETA] = d2fRN(qS[S_BETA]);
                         qS[S_RZ] = t[0];
                         if (t[1] < qS[S_ETA2] * qS[S_RR0] || !(t[1] == t[1])) qF[3] = 1;
                     }))

@@ -604,6 +604,18 @@ __device__ __forceinline__ bool qSumDF(df (&a)[NV], const PpeBuffers& B, QCtl& c
     return true;
 }
 
+// FP64 per-thread partials summed as float-float from the warp level on (each partial split
+// exactly into hi + lo to 48 bits): the per-iteration sums of the plain FP64 CG keep their
+// trees off the FP64 pipe.  A tree of float-float sums over the 864k row terms rounds less
+// than the sequential FP64 dot product of the reference's solver.
+template <int NV, class Fin>
+__device__ __forceinline__ bool qSumD(double (&v)[NV], const PpeBuffers& B, QCtl& c, Fin fin) {
+    df a[NV];
+#pragma unroll
+    for (int q = 0; q < NV; q++) a[q] = dfD(v[q]);
+    return qSumDF<NV>(a, B, c, fin);
+}
+
 // Rows inside the persistent kernels: matrix arrays are read-only for the launch, the
 // gathered vector is written by other blocks during it (plain loads, made visible by the
 // barrier's fences).  forRows walks a thread's rows with the next row's length prefetched.
@@ -1642,7 +1654,7 @@ __global__ void __launch_bounds__(QBC, 1) k_cg_own(Dev d, PpeBuffers B, double t
                 sap[l] = ap; sp[l] = p;
                 v[0] += p * ap;
             });
-            if (!qSum<1>(v, B, c, [&](const double* t) { qS[S_PAP] = t[0]; qS[S_ALPHA] = qS[S_RZ] / t[0]; }))
+            if (!qSumD<1>(v, B, c, [&](const double* t) { qS[S_PAP] = t[0]; qS[S_ALPHA] = qS[S_RZ] / t[0]; }))
                 return;
         }
         {   // x += alpha p, r -= alpha Ap, z = M^-1 r; r.z, r.r
@@ -1670,7 +1682,7 @@ __global__ void __launch_bounds__(QBC, 1) k_cg_own(Dev d, PpeBuffers B, double t
                     v[0] += r * z; v[1] += r * r;
                 }
             }
-            if (!qSum<2>(v, B, c, [&](const double* t) {
+            if (!qSumD<2>(v, B, c, [&](const double* t) {
                     qF[1] += 1;
                     qS[S_RR] = t[1];
                     qS[S_BETA] = t[0] / qS[S_RZ];

@@ -40,9 +40,9 @@ HBM_FALLBACK = 6800.0
 LINE_MAX = 1500
 # DRAM bytes (read + write) of the single-launch mixed PPE solve per inner-iteration
 # equivalent, from one ncu capture of the 20 timed solves of the 864k workload
-# (3.62e9 B per launch at 18 inner iterations and 1 refinement: the setup and each
+# (3.634e9 B per launch at 18 inner iterations and 1 refinement: the setup and each
 # refinement's FP64 passes counted as two inner iterations each; k_mx_own_cfg3-864k.md)
-MX_TRAFFIC_PER_ITER = 3.62e9 / (18 + 2 * 2)
+MX_TRAFFIC_PER_ITER = 3.634e9 / (18 + 2 * 2)
 
 
 def args_(argv=None):

@@ -383,7 +383,7 @@ static int runOpBody(mpsgpu_t h, int op) {
                 std::swap(d.nbr, h->nbrAlt);
                 std::swap(d.nbrCount, h->cntAlt);
                 h->skinValid = true;
-                h->skinShift = x;   // the DF32 shifting sweeps filter the kept skin list again
+                h->skinShift = true;   // the shifting sweeps filter the kept skin list again
                 countLaunch(2);   // skin list (listed + unlisted particles); the sweep is counted below
             } else if (x) launchViscosityDF(d, s);
             else launchViscosity(d, s);
@@ -459,8 +459,18 @@ static int runOpBody(mpsgpu_t h, int op) {
                 // posf + cell copy, skin check, filter (2), masks; then the sweeps and applies
                 countLaunch(6 + (P.shiftingType == 1 ? 3 : (P.wallType == 1 ? 7 : 4)));
                 h->opSkipped = true;
+            } else if (!x && h->skinShift && (P.shiftingType == 1 || P.shiftingType == 2)) {
+                // FP64: the same list (no weight cache), then the operators' sweeps over it
+                if (h->prof.on) { h->prof.end(s); h->prof.begin(PROF_NEIGHBOR_LIST, s, false); }
+                launchNeighborFilter(d, s, false);
+                if (h->prof.on) { h->prof.end(s); h->prof.begin(MPS_OP_SHIFTING, s, false); }
+                launchShifting(d, s, true);
+                invalidate();
+                // posf + cell copy, skin check, filter; then the sweeps and applies
+                countLaunch(4 + (P.shiftingType == 1 ? 2 : (P.wallType == 1 ? 6 : 3)));
+                h->opSkipped = true;
             } else {
-                if (x) launchShiftingDF(d, s); else launchShifting(d, s);
+                if (x) launchShiftingDF(d, s); else launchShifting(d, s, false);
                 if (P.shiftingType == 2) invalidate();
             }
             break;
@@ -835,9 +845,22 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     // PPE buffers
     PpeBuffers& B = h->B;
     std::memset(&B, 0, sizeof(B));
-    // ELL leading dimension padded to whole 256-row tiles: every slice of a tile is a
-    // 16-byte aligned, in-bounds range for the bulk copies of the staged SpMV
-    B.N0 = (n + 255) / 256 * 256; B.K = d.K;
+    // ELL rows padded to whole 256-row tiles: every slice of a tile is a 16-byte aligned,
+    // in-bounds range for the bulk copies of the staged SpMV.  Layout: slices of 1024 rows,
+    // each slice's entries column-major inside it, so the entries of a row lie 4 KB apart
+    // (column-major over all rows they lie N0 x 4 B apart: 37 MB at 9.4M rows, where the
+    // sliced layout measured 16.6 against 22.1 ms per solve; equal at 864k).
+    // MPSGPU_ELL_SLICE = s selects 2^s rows per slice (8 <= s <= 20), 0 the column-major layout.
+    B.K = d.K;
+    B.sliceShift = 10; B.sliceMask = (1 << 10) - 1;
+    if (const char* env = std::getenv("MPSGPU_ELL_SLICE")) {
+        const int sh = std::atoi(env);
+        if (sh == 0) { B.sliceShift = 31; B.sliceMask = 0x7fffffff; }
+        else if (sh >= 8 && sh <= 20) { B.sliceShift = sh; B.sliceMask = (1 << sh) - 1; }
+    }
+    const int pad = B.sliceShift < 31 ? (1 << B.sliceShift) : 256;
+    B.N0 = (n + pad - 1) / pad * pad;
+    B.ellStride = B.sliceShift < 31 ? (size_t)1 << B.sliceShift : (size_t)B.N0;
     const size_t ell = (size_t)d.K * B.N0;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -1285,8 +1308,7 @@ int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col, 
     for (int i = 0; i < n; i++) nnz += len[i];
     *nnz_out = nnz;
     if (!col) return 0;
-    const size_t ld = h->B.N0;
-    size_t ellN = (size_t)h->d.K * ld;
+    size_t ellN = (size_t)h->d.K * h->B.N0;
     std::vector<int> ec(ellN);
     std::vector<double> ev(ellN);
     CK(cudaMemcpyAsync(ec.data(), h->B.col, sizeof(int) * ellN, cudaMemcpyDeviceToHost, h->s));
@@ -1301,7 +1323,11 @@ int mpsgpu_get_ppe(mpsgpu_t h, long long* nnz_out, long long* rowptr, int* col, 
         if (rhs) rhs[r] = bst[i];
         row.clear();
         row.push_back({r, diag[i]});
-        for (int c = 0; c < len[i]; c++) row.push_back({orig[ec[(size_t)c * ld + i]], ev[(size_t)c * ld + i]});
+        const size_t base = ellBase(h->B, i);
+        for (int c = 0; c < len[i]; c++) {
+            const size_t e = base + (size_t)c * h->B.ellStride;
+            row.push_back({orig[ec[e]], ev[e]});
+        }
         std::sort(row.begin(), row.end(), [](const std::pair<int, double>& a, const std::pair<int, double>& b) { return a.first < b.first; });
         for (auto& pr : row) { col[k] = pr.first; val[k] = pr.second; k++; }
         rowptr[r + 1] = k;

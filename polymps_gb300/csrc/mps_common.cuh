@@ -365,21 +365,23 @@ __device__ __forceinline__ void forNbrs(const Dev& d, int i, F&& f) {
 // together, then the eight gathers; the last chunk is masked (predicated loads, the row's
 // own index as a harmless column) instead of a serial remainder loop.  RO: the gathered
 // vector is read-only for the launch (non-coherent cache path); otherwise plain loads.
+// Entry k of row i sits at base + k * stride in val and col (base, stride: the layout's).
 #define ELL_U 8
 template <class T, bool RO>
-__device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col, const T* x, int i, int len, size_t N0) {
+__device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col, const T* x, int i, int len, size_t base,
+                                    size_t stride) {
     T acc[ELL_U];
 #pragma unroll
     for (int u = 0; u < ELL_U; u++) acc[u] = T(0);
-    const T* v = val + i;
-    const int* c = col + i;
+    const T* v = val + base;
+    const int* c = col + base;
     for (int k = 0; k < len; k += ELL_U) {
         // ask L2 for the next chunk's column and value lines while this chunk's gathers run
         if (k + ELL_U < len) {
 #pragma unroll
             for (int u = 0; u < ELL_U; u++) {
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(c + (size_t)(k + ELL_U + u) * N0));
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(v + (size_t)(k + ELL_U + u) * N0));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(c + (size_t)(k + ELL_U + u) * stride));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(v + (size_t)(k + ELL_U + u) * stride));
             }
         }
         int cc[ELL_U];
@@ -387,8 +389,8 @@ __device__ __forceinline__ T ellRow(const T* diag, const T* val, const int* col,
 #pragma unroll
         for (int u = 0; u < ELL_U; u++) {
             bool ok = k + u < len;
-            cc[u] = ok ? ldStream(c + (size_t)(k + u) * N0) : i;
-            vv[u] = ok ? ldStream(v + (size_t)(k + u) * N0) : T(0);
+            cc[u] = ok ? ldStream(c + (size_t)(k + u) * stride) : i;
+            vv[u] = ok ? ldStream(v + (size_t)(k + u) * stride) : T(0);
         }
 #pragma unroll
         for (int u = 0; u < ELL_U; u++) acc[u] += vv[u] * (RO ? __ldg(x + cc[u]) : x[cc[u]]);

@@ -47,7 +47,7 @@ void launchViscosity(const Dev& d, cudaStream_t s);
 // FP64 tier over the start-of-step skin list (built by launchSkinListDF): the viscosity
 // sweep, and the list of the current positions with its weights filtered from it
 void launchViscosityList(const Dev& d, cudaStream_t s);
-void launchNeighborFilter(const Dev& d, cudaStream_t s);
+void launchNeighborFilter(const Dev& d, cudaStream_t s, bool weights = true);   // the FP64 list from the skin list
 void launchAddGravity(const Dev& d, cudaStream_t s);
 void launchPredict(const Dev& d, cudaStream_t s);
 void launchOutOfDomain(const Dev& d, int* flags, int* counter, cudaStream_t s);
@@ -67,7 +67,7 @@ void launchWallPressGradient(const Dev& d, cudaStream_t s);
 void launchPredictPressGradient(const Dev& d, bool skin, cudaStream_t s);   // relax_fact < 1, before PREDICT
 void launchWallViscosity(const Dev& d, cudaStream_t s);
 void launchCorrect(const Dev& d, cudaStream_t s);
-void launchShifting(const Dev& d, cudaStream_t s);
+void launchShifting(const Dev& d, cudaStream_t s, bool list);   // list: filter the kept skin list first
 void launchDummyVelocity(const Dev& d, cudaStream_t s);
 
 // mps_ops_df.cu (DF32 tier)
@@ -107,7 +107,12 @@ void launchWallDistance(const Dev& d, cudaStream_t s);
 
 // mps_ppe.cu
 struct PpeBuffers {
-    int N0, K;       // N0: leading dimension of the ELL arrays (rows padded to a multiple of 256)
+    int N0, K;       // N0: rows padded to a multiple of 256 (and of the slice height)
+    // ELL layout: entry k of row i at ellBase(i) + k * ellStride.  Column-major (sliceShift 31,
+    // ellStride N0) or sliced: slices of 2^sliceShift consecutive rows, each slice's K entries
+    // column-major inside it (ellStride = 2^sliceShift)
+    int sliceShift, sliceMask;
+    size_t ellStride;
     double *diag, *val, *x, *b, *r, *z, *p, *Ap, *scal;  // scal: solver scalars (device)
     int* col;
     int* rowLen;
@@ -147,6 +152,10 @@ struct PpeBuffers {
     const float* cdir;
     const float* cq;   // q = A c (FP32) of the learned correction
 };
+// Element offset of entry 0 of row i in the ELL arrays.
+__host__ __device__ __forceinline__ size_t ellBase(const PpeBuffers& B, int i) {
+    return (((size_t)(i >> B.sliceShift) * (size_t)B.K) << B.sliceShift) + (size_t)(i & B.sliceMask);
+}
 void launchPpeAssemble(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeCopyBack(const Dev& d, const PpeBuffers& B, cudaStream_t s);
 void launchPpeAssembleDF(const Dev& d, const PpeBuffers& B, cudaStream_t s);

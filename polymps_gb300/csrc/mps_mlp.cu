@@ -223,7 +223,7 @@ __global__ void k_mlp_xe_start(Dev d, PpeBuffers B, float* xe32) {
 __global__ void __launch_bounds__(256) k_mlp_resid(Dev d, PpeBuffers B, const float* xe32, float* re) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
-    re[i] = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), B.N0);
+    re[i] = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
 }
 // The same residual with the 16 raw features of the row (k_mlp_features' definitions) and the
 // block partials of the system scale (sum over equation rows of feature 7 squared, and
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(256) k_mlp_resid_feat(Dev d, PpeBuffers B, con
     const int n = liveN(d);
     double q0 = 0.0, q1 = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float rei = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), B.N0);
+        const float rei = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
         const dvec4 x = d.pos[i], v = d.vel[i];
         const float diag = __ldg(B.diagf + i), idg = __ldg(B.diagInvf + i);
         const double pn = d.pressPPE[i];
@@ -349,9 +349,8 @@ __global__ void __launch_bounds__(256) k_mlp_step_dots(Dev d, PpeBuffers B, cons
                                                        double* part) {
     double s0 = 0.0, s1 = 0.0;
     const int n = liveN(d);
-    const size_t N0 = B.N0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float ac = ellRow<float, true>(B.diagf, B.valf, B.col, cdir, i, __ldg(B.rowLen + i), N0);
+        const float ac = ellRow<float, true>(B.diagf, B.valf, B.col, cdir, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
         s0 += (double)(re[i] * ac);
         s1 += (double)(ac * ac);
     }
@@ -373,7 +372,7 @@ __global__ void k_mlp_step_apply(Dev d, PpeBuffers B, const float* cdir, const d
 __global__ void __launch_bounds__(256) k_mlp_ac(Dev d, PpeBuffers B, const float* cdir, float* q) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
-    q[i] = ellRow<float, true>(B.diagf, B.valf, B.col, cdir, i, __ldg(B.rowLen + i), B.N0);
+    q[i] = ellRow<float, true>(B.diagf, B.valf, B.col, cdir, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
 }
 
 // sig: system scale of the raw features (nullptr: the features are network inputs as given)

@@ -85,9 +85,10 @@ void launchViscosityList(const Dev& d, cudaStream_t s) {
 }
 
 // FP64 list of the current positions filtered from the skin list: the set, order and
-// per-entry weights of k_build_nbr (candidates within the FP32 band, exact FP64 test
-// d^2 < reMax^2).  A particle whose scan window changed or whose skin row overflowed, or
-// every particle once the skin list went stale, scans the 27 buckets as k_build_nbr does.
+// (WEIGHTS) per-entry weights of k_build_nbr (candidates within the FP32 band, exact FP64
+// test d^2 < reMax^2).  A particle whose scan window changed or whose skin row overflowed,
+// or every particle once the skin list went stale, scans the 27 buckets as k_build_nbr does.
+template <bool WEIGHTS>
 __global__ void __launch_bounds__(128) k_filter_nbr(Dev d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
@@ -101,11 +102,13 @@ __global__ void __launch_bounds__(128) k_filter_nbr(Dev d) {
         if (cnt < d.K) {
             const size_t e = (size_t)cnt * N0 + i;
             d.nbr[e] = j;
-            double w, wd;
-            weightR(q.d2, P.reS, P.weightType, w, wd);
-            d.cw[e] = w;
-            d.cwd[e] = wd;
-            if (d.cwL) { double wl, wdl; weightR(q.d2, P.reL, P.weightType, wl, wdl); d.cwL[e] = wl; }
+            if (WEIGHTS) {
+                double w, wd;
+                weightR(q.d2, P.reS, P.weightType, w, wd);
+                d.cw[e] = w;
+                d.cwd[e] = wd;
+                if (d.cwL) { double wl, wdl; weightR(q.d2, P.reL, P.weightType, wl, wdl); d.cwL[e] = wl; }
+            }
         }
         cnt++;
     };
@@ -128,11 +131,12 @@ __global__ void __launch_bounds__(128) k_filter_nbr(Dev d) {
     d.nbrCount[i] = cnt;
     warpCount(d.counters, (unsigned)cnt);
 }
-void launchNeighborFilter(const Dev& d, cudaStream_t s) {
+void launchNeighborFilter(const Dev& d, cudaStream_t s, bool weights) {
     cudaMemsetAsync(d.counters, 0, sizeof(unsigned long long), s);
     launchPosf(d, s);
     launchSkinCheck(d, s);
-    k_filter_nbr<<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+    if (weights) k_filter_nbr<true><<<gridFor(d.N0, 128), 128, 0, s>>>(d);
+    else k_filter_nbr<false><<<gridFor(d.N0, 128), 128, 0, s>>>(d);
 }
 
 // MpsParticle::addGravity, src/MpsParticle.cpp:111-130
@@ -1398,16 +1402,47 @@ __global__ void k_apply_shift(Dev d) {
 }
 void launchShiftVelApply(const Dev& d, cudaStream_t s) { k_shift_vel_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
 void launchApplyShift(const Dev& d, cudaStream_t s) { k_apply_shift<<<gridFor(d.N0, 256), 256, 0, s>>>(d); }
-void launchShifting(const Dev& d, cudaStream_t s) {
+// A 27-bucket sweep over the list of the current positions instead of the buckets: the
+// list holds every candidate within reMax of the scan, in the scan's order, and each
+// operator applies its own exact radius and side tests, so it sees the same neighbours in
+// the same order (the same sums).
+template <class Op>
+__global__ void __launch_bounds__(128) k_list_scan(Dev d, Op op) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    typename Op::State st;
+    op.begin(d, i, st);
+    if (op.active(d, st)) {
+        const dvec4 pi = d.pos[i];
+        const int c = d.nbrCount[i];
+        const int* row = d.nbr + i;
+        for (int k = 0; k < c; k++) {
+            const int j = ldStream(row + (size_t)k * d.N0);
+            const dvec4 pj = d.pos[j];
+            op.visit(d, i, st, j, pj, pairOf(pj, pi));
+        }
+    }
+    op.end(d, i, st);
+}
+template <class Op>
+static void launchSweep(const Dev& d, const Op& op, bool list, cudaStream_t s) {
+    if (list) k_list_scan<Op><<<gridFor(d.N0, 128), 128, 0, s>>>(d, op);
+    else launchScan(d, op, s);
+}
+
+// list: the sweeps read the list of the post-corrector positions, filtered from the kept
+// start-of-step skin list (launchNeighborFilter without the weight cache, which also
+// refreshes the FP32 copies) just before; else they scan the buckets
+void launchShifting(const Dev& d, cudaStream_t s, bool list) {
     const MpsParams& P = d.P;
     if (P.shiftingType != 1 && P.shiftingType != 2) return;
-    launchPosf(d, s);   // post-corrector positions
+    if (!list) launchPosf(d, s);   // post-corrector positions
     if (P.shiftingType == 1) {
-        launchScan(d, OpShiftVel(), s);
+        launchSweep(d, OpShiftVel(), list, s);
         k_shift_vel_apply<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
     } else {
-        launchScan(d, OpConc(), s);
-        launchScan(d, OpGradConc(), s);
+        launchSweep(d, OpConc(), list, s);
+        launchSweep(d, OpGradConc(), list, s);
         k_apply_shift<<<gridFor(d.N0, 256), 256, 0, s>>>(d);
         if (P.wallType == 1) {
             launchPosfCell(d, s);   // the wall sweep sees the shifted positions

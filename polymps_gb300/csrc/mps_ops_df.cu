@@ -473,7 +473,7 @@ __global__ void __launch_bounds__(128, 12) k_ppe_assemble_df(Dev d, PpeBuffers B
             df mij = wL * cP;
             sum -= mij;
             if (d.bc[j] == P.inner) {
-                size_t k = (size_t)len * B.N0 + i;
+                size_t k = ellBase(B, i) + (size_t)len * B.ellStride;
                 B.val[k] = dD(mij);
                 B.valf[k] = mij.h;   // the FP32 copy of the mixed solver (hi part = fl32)
                 B.col[k] = j;

@@ -3,7 +3,7 @@
 // Assembly replaces the serial Eigen triplet loop of MpsPressure::solvePressurePoissonPnd
 // (src/MpsPressure.cpp:169-286): one thread per row walks its ELL neighbour row and writes
 // the off-diagonal entries (j inner, not dummy) straight into an ELL matrix
-// (val/col[k * N0 + i], coalesced across a warp), the diagonal and the right-hand side.
+// (val/col at ellBase(i) + k ellStride, coalesced across a warp), the diagonal and the right-hand side.
 //
 // The plain solver replaces Eigen's ConjugateGradient<..., Lower|Upper> with its default
 // diagonal preconditioner (src/MpsPressure.cpp:424-445): Jacobi-PCG in FP64 warm-started
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(128) k_ppe_assemble(Dev d, PpeBuffers B) {
         } else {
             sum -= mij;
             if (d.bc[j] == P.inner) {
-                size_t k = (size_t)len * B.N0 + i;
+                size_t k = ellBase(B, i) + (size_t)len * B.ellStride;
                 B.val[k] = mij;
                 B.col[k] = j;
                 len++;
@@ -157,7 +157,7 @@ __device__ __forceinline__ void gridSum(double (&v)[NV], const PpeBuffers& B, Fi
 
 // ------------------------------------------------------------------ ELL rows (ellRow: mps_common.cuh)
 __device__ __forceinline__ double spmvRow(const PpeBuffers& B, const double* x, int i) {
-    return ellRow<double, true>(B.diag, B.val, B.col, x, i, __ldg(B.rowLen + i), B.N0);
+    return ellRow<double, true>(B.diag, B.val, B.col, x, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
 }
 
 // r = b - A x, z = r / diag, p = z; sums r.z, r.r, b.b
@@ -288,8 +288,9 @@ __global__ void k_mixed_prepare(Dev d, PpeBuffers B) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= liveN(d)) return;
     int len = B.rowLen[i];
+    const size_t base = ellBase(B, i);
     for (int k = 0; k < len; k++) {
-        size_t e = (size_t)k * B.N0 + i;
+        size_t e = base + (size_t)k * B.ellStride;
         B.valf[e] = (float)B.val[e];
     }
     B.diagf[i] = (float)B.diag[i];
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(PBLK) k_mx_inner_init(Dev d, PpeBuffers B) {
     gridSum<1>(v, B, [&](double* t) { B.scal[S_RZ] = t[0]; B.flag[3] = 0; });
 }
 __device__ __forceinline__ float spmvRowF(const PpeBuffers& B, const float* x, int i) {
-    return ellRow<float, true>(B.diagf, B.valf, B.col, x, i, __ldg(B.rowLen + i), B.N0);
+    return ellRow<float, true>(B.diagf, B.valf, B.col, x, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
 }
 __global__ void __launch_bounds__(PBLK) k_mx_spmv(Dev d, PpeBuffers B) {
     if (*(volatile int*)(B.flag + 3)) return;
@@ -693,10 +694,10 @@ __device__ __forceinline__ void forRows(const PpeBuffers& B, const RowSet& s, F&
     }
 }
 __device__ __forceinline__ double qRow(const PpeBuffers& B, const double* x, int i, int len) {
-    return ellRow<double, false>(B.diag, B.val, B.col, x, i, len, B.N0);
+    return ellRow<double, false>(B.diag, B.val, B.col, x, i, len, ellBase(B, i), B.ellStride);
 }
 __device__ __forceinline__ float qRowF(const PpeBuffers& B, const float* x, int i, int len) {
-    return ellRow<float, false>(B.diagf, B.valf, B.col, x, i, len, B.N0);
+    return ellRow<float, false>(B.diagf, B.valf, B.col, x, i, len, ellBase(B, i), B.ellStride);
 }
 
 // Matrix-free FP32 row of the mixed solver's inner operator: the off-diagonal entries
@@ -751,13 +752,13 @@ __device__ __forceinline__ float mfRowF(const Dev& d, const PpeBuffers& B, const
 // 16-bit offsets j - i (rows with a farther neighbour keep the 32-bit columns), 4 bytes
 // per entry instead of 8, and CG on M needs no preconditioner.
 __device__ __forceinline__ float h16Row(const PpeBuffers& B, const float* y, int i, int len) {
-    const size_t N0 = B.N0;
-    const __half* v = B.valh + i;
+    const size_t N0 = B.ellStride, base = ellBase(B, i);
+    const __half* v = B.valh + base;
     float acc[ELL_U];
 #pragma unroll
     for (int u = 0; u < ELL_U; u++) acc[u] = 0.f;
     if (!__ldg(B.wideRow + i)) {
-        const short* c = B.col16 + i;
+        const short* c = B.col16 + base;
         for (int k = 0; k < len; k += ELL_U) {
             if (k + ELL_U < len) {
 #pragma unroll
@@ -778,7 +779,7 @@ __device__ __forceinline__ float h16Row(const PpeBuffers& B, const float* y, int
             for (int u = 0; u < ELL_U; u++) acc[u] += vv[u] * y[cc[u]];
         }
     } else {
-        const int* c = B.col + i;
+        const int* c = B.col + base;
         for (int k = 0; k < len; k += ELL_U) {
             int cc[ELL_U];
             float vv[ELL_U];
@@ -873,8 +874,8 @@ __device__ __forceinline__ void tsIssue(TsSmem& sm, const PpeBuffers& B, const T
     const int k0 = w.chunk * TS_CH, nsl = min(TS_CH, L - k0);
     const size_t r0 = (size_t)(blockIdx.x + w.m * gridDim.x) * QB;
     mbarExpectTx(&sm.full[s], (unsigned)(nsl * QB * (sizeof(int) + sizeof(float))));
-    for (int u = 0; u < nsl; u++) {
-        size_t e = (size_t)(k0 + u) * B.N0 + r0;
+    for (int u = 0; u < nsl; u++) {   // a tile's QB rows lie in one slice (the slice height is a multiple of QB)
+        size_t e = ellBase(B, (int)r0) + (size_t)(k0 + u) * B.ellStride;
         bulkG2S(sm.st[s].col[u], B.col + e, QB * sizeof(int), &sm.full[s]);
         bulkG2S(sm.st[s].val[u], B.valf + e, QB * sizeof(float), &sm.full[s]);
     }
@@ -993,8 +994,9 @@ __global__ void __launch_bounds__(OP == 3 ? QB : QBX, OP == 3 ? 4 : 1) k_mx_solv
         forRows(B, rs, [&](int i, int len) {
             const float si = B.sgs[i];
             unsigned char wide = 0;
+            const size_t base = ellBase(B, i);
             for (int k = 0; k < len; k++) {
-                size_t e = (size_t)k * B.N0 + i;
+                size_t e = base + (size_t)k * B.ellStride;
                 int j = __ldg(B.col + e);
                 B.valh[e] = __float2half_rn(si * __ldg(B.valf + e) * B.sclf[j]);
                 int off = j - i;
@@ -1344,9 +1346,9 @@ __device__ __forceinline__ double qRowPlus(const PpeBuffers& B, const double* x,
     double acc[ELL_U];
 #pragma unroll
     for (int u = 0; u < ELL_U; u++) acc[u] = 0.0;
-    const double* v = B.val + i;
-    const int* c = B.col + i;
-    const size_t N0 = B.N0;
+    const size_t base = ellBase(B, i), N0 = B.ellStride;
+    const double* v = B.val + base;
+    const int* c = B.col + base;
     for (int k = 0; k < len; k += ELL_U) {
         int cc[ELL_U];
         double vv[ELL_U];

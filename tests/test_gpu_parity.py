@@ -227,9 +227,14 @@ def test_prediction_pressure_gradient(oracle_mod, mps_lib, name, precision):
     o.close()
 
 
+@pytest.mark.parametrize("layout", ["10", "0", "8"])
 @pytest.mark.parametrize("name", ["cfg3_3d_inc_polygon", "cfg1_2d_particle_walls"])
-def test_ppe_system_and_solution(oracle_mod, mps_lib, name):
+def test_ppe_system_and_solution(oracle_mod, mps_lib, name, layout, monkeypatch):
+    """The assembled system and its solution against the oracle, in each ELL layout of the
+    library (MPSGPU_ELL_SLICE, read when a handle is created: 1024-row slices by default,
+    column-major over all rows, 256-row slices)."""
     from polymps_gb300 import mps
+    monkeypatch.setenv("MPSGPU_ELL_SLICE", layout)
     c = CASES[name]()
     o, g = _pair(oracle_mod, mps, c, tol=1e-12)
     o.initialize()
@@ -267,10 +272,13 @@ def test_free_running_steps(oracle_mod, mps_lib, name):
     assert relerr(g.get(abi.F_PRESS), o.get(abi.F_PRESS)) < 1e-6
 
 
-def test_mixed_precision_solver(oracle_mod, mps_lib):
+@pytest.mark.parametrize("layout", ["10", "0"])
+def test_mixed_precision_solver(oracle_mod, mps_lib, layout, monkeypatch):
     """FP32 inner CG + FP64 refinement reaches the FP64 residual 1e-8 and its pressure
-    stays within 1e-6 (normwise relative) of the FP64 oracle solved to 1e-12."""
+    stays within 1e-6 (normwise relative) of the FP64 oracle solved to 1e-12 (sliced and
+    column-major ELL layouts)."""
     from polymps_gb300 import mps
+    monkeypatch.setenv("MPSGPU_ELL_SLICE", layout)
     c = cases.config(3, jitter=0.02, scale=4.0)
     o, g = _pair(oracle_mod, mps, c, tol=1e-12)
     o.initialize()

@@ -17,15 +17,30 @@ void countLaunch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 long long launchCount() { return g_launches.load(std::memory_order_relaxed); }
 
 // ------------------------------------------------------------------ bucket keys
+// Warp-level counting: the lanes of a warp that share a bucket key (most of them, since the
+// storage is kept in bucket order) form one group; its lowest lane adds the group's size to
+// the bucket's counter (or cursor) and every lane's place is the group's base plus its rank
+// among the group's lanes (lane order = particle order).  Returns that place.
+__device__ __forceinline__ int warpGroupAdd(int* counters, int key, bool active) {
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!active) return -1;
+    const unsigned grp = __match_any_sync(act, key);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(grp) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counters + key, __popc(grp));
+    base = __shfl_sync(grp, base, leader);
+    return base + __popc(grp & ((1u << lane) - 1u));
+}
+
 // 2D adds epsilonZero, 3D does not (src/MpsBucket.cpp:312-313 vs :333-335); ghosts skipped.
+// Every lane of a warp reaches the warp-level count (lanes past N0 take part without a key).
 __global__ void k_cell_key(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.N0) return;
-    int n = liveN(d);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = liveN(d);
     int key = -1;
     if (i < n && d.type[i] == d.P.ghost) {
         key = d.nB;   // live, in no bucket: listed after the buckets, never scanned
-        atomicAdd(d.cellCount + key, 1);
     } else if (i < n) {
         const MpsParams& P = d.P;
         dvec4 p = d.pos[i];
@@ -45,23 +60,21 @@ __global__ void k_cell_key(Dev d) {
         } else {
             key = (int)ib;
         }
-        atomicAdd(d.cellCount + key, 1);
         // FP32 copy of the start-of-step positions for the prefiltered scans
         float4 hi = make_float4(d2fRN(p.x - P.domainMin[0]), d2fRN(p.y - P.domainMin[1]),
                                 d2fRN(p.z - P.domainMin[2]), 0.f);
         d.posf[i] = hi;
         d.posLo[i] = posLoOf(p, hi, P);
     }
-    d.cellOf[i] = key;
+    warpGroupAdd(d.cellCount, key, key >= 0);
+    if (i < d.N0) d.cellOf[i] = key;
 }
 
 __global__ void k_cell_scatter(Dev d) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= d.N0) return;
-    int c = d.cellOf[i];
-    if (c < 0) return;
-    int slot = d.cellStart[c] + atomicAdd(d.cellCursor + c, 1);
-    d.cellSorted[slot] = i;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = (i < d.N0) ? d.cellOf[i] : -1;
+    const int r = warpGroupAdd(d.cellCursor, c, c >= 0);
+    if (c >= 0) d.cellSorted[d.cellStart[c] + r] = i;
 }
 
 // Order each bucket by reference index (the reference's linked-list order; buckets hold

@@ -120,6 +120,10 @@ typedef struct MpsStepStats {
     int    runPpeSolves;        /* PPE solves in that call                             */
     long long runPpeIterations; /* their SpMV iterations, summed                       */
     long long runPpeRefinements;/* their FP64 refinements, summed                      */
+    int    ppeFallback;         /* 1: the last solve was a mixed solve that missed the
+                                   tolerance, redone by the plain FP64 CG from the
+                                   previous solution (the reference's solver)          */
+    int    runPpeFallbacks;     /* such solves in the last run call                    */
 } MpsStepStats;
 
 /* Field identifiers for get/set.  Vector fields use the reference's interleaved host
@@ -177,7 +181,10 @@ enum MpsOp {
 /* PPE solver selection (mpsgpu_set_solver).  PLAIN_FP64 is the drop-in for Eigen's
  * ConjugateGradient (src/MpsPressure.cpp:424-445): Jacobi-preconditioned CG in FP64,
  * warm-started from the previous unclamped solution.  MIXED runs FP32 SpMV/CG inner
- * solves under FP64 iterative refinement (FP64 residual r=b-Ax, FP64 dots). */
+ * solves under FP64 iterative refinement (FP64 residual r=b-Ax, FP64 dots).  The final
+ * FP64 relative residual judges every solver: a MIXED solve (any warm start, the learned
+ * one included) that misses the tolerance within max_iter is redone by PLAIN_FP64 from
+ * the previous unclamped solution with its own max_iter (MpsStepStats.ppeFallback). */
 #define MPSGPU_SOLVER_PLAIN_FP64   0
 #define MPSGPU_SOLVER_MIXED        1
 /* MIXED with a matrix-free inner operator: the FP32 off-diagonals are recomputed from the

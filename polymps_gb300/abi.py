@@ -84,6 +84,7 @@ class MpsStepStats(C.Structure):
         ("nbrEntries", C.c_longlong), ("ppeNnz", C.c_longlong),
         ("runSteps", C.c_int), ("runPpeSolves", C.c_int),
         ("runPpeIterations", C.c_longlong), ("runPpeRefinements", C.c_longlong),
+        ("ppeFallback", C.c_int), ("runPpeFallbacks", C.c_int),
     ]
 
     def as_dict(self):

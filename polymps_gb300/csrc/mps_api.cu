@@ -307,9 +307,24 @@ static int calcPress(mpsgpu_t h) {
     } else {
         e = ppeSolvePlain(h->d, h->B, h->tol, maxIt, h->s, &iters, &rr, &rr0, &h->prof);
     }
-    cudaEventRecord(h->es1, h->s);
     if (h->warm == MPSGPU_WARM_MLP && !e && (e = mlpTcStatus(h->mlp, h->s)))
         g_lastError = "learned warm start: a tensor-core completion wait ran out";
+    // the final FP64 residual judges the fast solvers: a mixed solve that missed the
+    // tolerance is redone by the plain FP64 CG from the previous unclamped solution
+    h->last.ppeFallback = 0;
+    if (mixed && e == MPSGPU_ERR_NOT_CONVERGED) {
+        cudaMemcpyAsync(h->B.x, h->d.pressPPE, sizeof(double) * h->N0, cudaMemcpyDeviceToDevice, h->s);
+        int fi = 0, fr = 0;
+        if (h->persistent && h->B.pgridCg > 0)
+            e = ppeSolvePersistent(h->d, h->B, 0, h->tol, maxIt, h->s, &fi, &fr, &rr, &rr0, &h->prof);
+        else
+            e = ppeSolvePlain(h->d, h->B, h->tol, maxIt, h->s, &fi, &rr, &rr0, &h->prof);
+        if (e == MPSGPU_ERR_CUDA) g_lastError = "PPE fallback solve: launch failed or a grid-barrier wait ran out";
+        iters += fi;
+        h->last.ppeFallback = 1;
+        h->last.runPpeFallbacks += 1;
+    }
+    cudaEventRecord(h->es1, h->s);
     if (h->mlp.recording && !e) {
         // features of this system with the previous solution, target = converged - previous
         if (!h->B.prepared) { launchMixedPrepare(h->d, h->B, h->s); h->B.prepared = 1; }   // features read valf
@@ -993,6 +1008,7 @@ int mpsgpu_run(mpsgpu_t h, int nsteps, MpsStepStats* stats) {
     h->last.runPpeSolves = 0;
     h->last.runPpeIterations = 0;
     h->last.runPpeRefinements = 0;
+    h->last.runPpeFallbacks = 0;
     for (int k = 0; k < nsteps; k++) {
         int e = stepImpl(h);
         if (e) return e;

@@ -360,11 +360,12 @@ __global__ void __launch_bounds__(256) k_mlp_step_dots(Dev d, PpeBuffers B, cons
 __global__ void __launch_bounds__(256) k_mlp_theta(const double* part, int nblk, double* theta) {
     double a, b;
     sumPartials2(part, nblk, a, b);
-    if (threadIdx.x == 0) theta[0] = (b > 0.0 && a == a) ? a / b : 0.0;
+    // a non-finite correction (or product) keeps the extrapolated start: theta = 0
+    if (threadIdx.x == 0) theta[0] = (b > 0.0 && b < 1.0 / 0.0 && a == a && fabs(a) < 1.0 / 0.0) ? a / b : 0.0;
 }
 __global__ void k_mlp_step_apply(Dev d, PpeBuffers B, const float* cdir, const double* theta) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < d.N0) B.x[i] += theta[0] * (double)cdir[i];
+    if (i < d.N0 && theta[0] != 0.0) B.x[i] += theta[0] * (double)cdir[i];   // (0 * NaN would poison x)
 }
 
 // ------------------------------------------------------------------ learned start

@@ -1163,9 +1163,12 @@ __device__ __forceinline__ bool mxSetup(const PpeBuffers& B, const RowSet& rs, Q
     if (!qSum<LEARNED ? 4 : 2>(v, B, c, [&](const double* t) {
             double th = 0.0, rr = t[0];
             if (LEARNED) {
+                // a non-finite correction keeps the start x (theta = 0, its residual as is)
                 const double rq = t[LEARNED ? 2 : 0], qq = t[LEARNED ? 3 : 0];
-                th = (qq > 0.0 && rq == rq) ? rq / qq : 0.0;
-                rr = fmax(t[0] - th * rq, 0.0);
+                if (qq > 0.0 && qq < 1.0 / 0.0 && rq == rq && fabs(rq) < 1.0 / 0.0) {
+                    th = rq / qq;
+                    rr = fmax(t[0] - th * rq, 0.0);
+                }
             }
             qS[S_OMEGA] = th;
             qS[S_RR] = rr;
@@ -1183,7 +1186,7 @@ __device__ __forceinline__ bool mxSetup(const PpeBuffers& B, const RowSet& rs, Q
             if (!(rr == rr)) { qF[0] = 1; qF[2] = 1; }
         }))
         return false;
-    if (LEARNED) {   // x += theta c, r -= theta q on the thread's own rows
+    if (LEARNED && vd(qS + S_OMEGA) != 0.0) {   // x += theta c, r -= theta q on the thread's own rows
         const double th = vd(qS + S_OMEGA);
         forOwn(rs, [&](int i) {
             B.x[i] += th * (double)__ldg(B.cdir + i);

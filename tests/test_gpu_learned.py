@@ -9,6 +9,8 @@ and the learned start x_e + theta c (network correction c, residual-minimising s
 Every start's pressure (FP64 residual 1e-8) must lie within 1e-6 relative of the CPU
 oracle's Jacobi-PCG of the same system solved to 1e-12 (src/MpsPressure.cpp:424-445).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -87,3 +89,70 @@ def test_learned_warm_start_gain(oracle_mod, mps_lib):
     assert np.all(r0["learned"] <= r0["extrapolated"] * (1.0 + 1e-6))
     # and the learned start beats the reference's previous-step start
     assert r0["learned"].mean() < r0["previous"].mean()
+
+
+
+def _system_after_steps(mps, steps=12):
+    """A PPE system of the 3D dam break at l0 = 0.02 m after a few steps (the operators
+    before the pressure run) and the warm-start history of its unclamped solutions."""
+    c = cases.config(4, scale=2.0)
+    g = mps.MpsGpu(c, solver=abi.SOLVER_MIXED, tol=1e-8, max_iter=20000, precision=abi.PRECISION_DF32)
+    w = np.load(os.path.join(os.path.dirname(mps.__file__), "mlp_warmstart.npz"))
+    g.mlp_set_weights(w["params"], w["norm"])
+    g.initialize()
+    g.run(steps)
+    for op in OPS_BEFORE:
+        g.run_op(op)
+    hist = [g.get(f) for f in (abi.F_PRESSPPE, abi.F_PRESSPPE_PREV, abi.F_PRESSPPE_PREV2)]
+    return g, w, hist
+
+
+def _solve(mps, g, hist, solver, warm, max_iter):
+    """CALC_PRESS from the same history; returns the status code, the stats and pressurePPE."""
+    for f, v in zip((abi.F_PRESSPPE, abi.F_PRESSPPE_PREV, abi.F_PRESSPPE_PREV2), hist):
+        g.set(f, v)
+    g.set_solver(solver, warm, 1e-8, max_iter)
+    code = 0
+    try:
+        g.run_op("CALC_PRESS")
+    except mps.MpsError as err:
+        code = err.code
+    return code, g.last_stats(), g.get(abi.F_PRESSPPE)
+
+
+def test_learned_start_with_a_broken_network(mps_lib):
+    """Non-finite network weights: the residual-minimising step rejects the correction
+    (theta = 0), the start is the quadratic extrapolation, and the solve converges to the
+    extrapolated start's pressure."""
+    from polymps_gb300 import mps
+    g, w, hist = _system_after_steps(mps)
+    code_e, st_e, x_e = _solve(mps, g, hist, abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 20000)
+    bad = np.array(w["params"], dtype=np.float32)
+    bad[-1] = np.nan   # output bias
+    g.mlp_set_weights(bad, w["norm"])
+    code_l, st_l, x_l = _solve(mps, g, hist, abi.SOLVER_MIXED, abi.WARM_MLP, 20000)
+    g.close()
+    assert code_e == 0 and code_l == 0
+    assert st_l.ppeRelResidual <= 1e-8 and st_l.ppeFallback == 0
+    assert st_l.ppeInitialRelResidual == pytest.approx(st_e.ppeInitialRelResidual, rel=1e-9)
+    assert _rel(x_l, x_e) < 1e-9
+
+
+@pytest.mark.parametrize("warm", [abi.WARM_MLP, abi.WARM_PREVIOUS])
+def test_mixed_solve_falls_back_to_plain_cg(mps_lib, warm):
+    """A mixed solve that misses the tolerance within max_iter is redone by the plain FP64
+    CG from the previous unclamped solution (the reference's solver): with the same budget
+    the result is the plain solver's own, bit for bit, the stats report the fallback, and
+    the status reports that the plain CG missed the tolerance as well."""
+    from polymps_gb300 import mps
+    g, w, hist = _system_after_steps(mps)
+    code_m, st_m, _ = _solve(mps, g, hist, abi.SOLVER_MIXED, warm, 20000)
+    assert code_m == 0 and st_m.ppeFallback == 0 and st_m.ppeRelResidual <= 1e-8
+    short = 3
+    assert st_m.ppeIterations > short
+    code_s, st_s, x_s = _solve(mps, g, hist, abi.SOLVER_PLAIN_FP64, abi.WARM_PREVIOUS, short)
+    code_f, st_f, x_f = _solve(mps, g, hist, abi.SOLVER_MIXED, warm, short)
+    g.close()
+    assert code_s == abi.ERR_NOT_CONVERGED and st_s.ppeFallback == 0
+    assert code_f == abi.ERR_NOT_CONVERGED and st_f.ppeFallback == 1
+    assert np.array_equal(x_f, x_s)

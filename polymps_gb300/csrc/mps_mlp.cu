@@ -215,7 +215,7 @@ __global__ void k_mlp_xe_start(Dev d, PpeBuffers B, float* xe32) {
     if (i >= d.N0) return;
     const bool eq = i < liveN(d) && d.bc[i] == d.P.inner;
     const double xe = eq ? extrapBase(d, i) : 0.0;
-    xe32[i] = (float)xe;
+    xe32[i] = d2fRN(xe);
     B.x[i] = xe;
 }
 // r_e = b - A x_e (FP32 copy of the matrix) for the features and the step: one row per
@@ -225,63 +225,71 @@ __global__ void __launch_bounds__(256) k_mlp_resid(Dev d, PpeBuffers B, const fl
     if (i >= liveN(d)) return;
     re[i] = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
 }
+// Per-system constants of the features (FP64 divisions and a square root, formed once on
+// the host instead of in every thread): the unit vector along g, 1/n0, 1/N0, 1/reL and
+// 1/(coeffPPE n0).
+struct FeatConst {
+    float ggx, ggy, ggz, in0, iN0, iRe, iA;
+};
+static FeatConst featConst(const MpsParams& P) {
+    double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
+    const double gn = std::sqrt(gx * gx + gy * gy + gz * gz);
+    if (gn > 0) { gx /= gn; gy /= gn; gz /= gn; }
+    FeatConst k;
+    k.ggx = (float)gx; k.ggy = (float)gy; k.ggz = (float)gz;
+    k.in0 = (float)(1.0 / P.pndSmallZero);
+    k.iN0 = (float)(1.0 / P.numNeighZero);
+    k.iRe = (float)(1.0 / P.reL);
+    k.iA = (float)(1.0 / (P.coeffPPE * P.pndSmallZero));
+    return k;
+}
 // The same residual with the 16 raw features of the row (k_mlp_features' definitions) and the
 // block partials of the system scale (sum over equation rows of feature 7 squared, and
 // their count): one memory-bound pass over the rows' fields at full occupancy, so the
 // tensor-core forward only streams the feature rows.
 __global__ void __launch_bounds__(256) k_mlp_resid_feat(Dev d, PpeBuffers B, const float* xe32, float* feat,
-                                                        double* part) {
+                                                        double* part, FeatConst K) {
     const MpsParams& P = d.P;
-    double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
-    const double gn = sqrt(gx * gx + gy * gy + gz * gz);
-    if (gn > 0) { gx /= gn; gy /= gn; gz /= gn; }
-    const float ggx = (float)gx, ggy = (float)gy, ggz = (float)gz;
-    const float in0 = (float)(1.0 / P.pndSmallZero), iN0 = (float)(1.0 / P.numNeighZero), iRe = (float)(1.0 / P.reL);
-    const float iA = (float)(1.0 / (P.coeffPPE * P.pndSmallZero));
+    const float ggx = K.ggx, ggy = K.ggy, ggz = K.ggz, in0 = K.in0, iN0 = K.iN0, iRe = K.iRe, iA = K.iA;
     const int n = liveN(d);
     double q0 = 0.0, q1 = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float rei = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
+        const float rei = d2fRN(B.b[i]) - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
         const dvec4 x = d.pos[i], v = d.vel[i];
         const float diag = __ldg(B.diagf + i), idg = __ldg(B.diagInvf + i);
         const double pn = d.pressPPE[i];
-        const float bi = (float)B.b[i];
-        const float vx = (float)v.x, vy = (float)v.y, vz = (float)v.z;
+        const float bi = d2fRN(B.b[i]);
+        const float vx = d2fRN(v.x), vy = d2fRN(v.y), vz = d2fRN(v.z);
         float f[NF];
-        f[0] = ((float)d.pndSmall[i] - (float)P.pndSmallZero) * in0;
+        f[0] = (d2fRN(d.pndSmall[i]) - d2fRN(P.pndSmallZero)) * in0;
         f[1] = bi * idg;
         f[2] = (float)d.numNeigh[i] * iN0;
-        f[3] = (pn == 0.0) ? 1.f : 0.f;
-        f[4] = fminf(sqrtf((float)d.riw2[i]) * iRe, 1.5f);
-        f[5] = (float)pn - (float)d.pressPPEprev[i];
+        f[3] = ((__double_as_longlong(pn) << 1) == 0) ? 1.f : 0.f;   // pn == +-0
+        f[4] = fminf(sqrtf(d2fRN(d.riw2[i])) * iRe, 1.5f);
+        f[5] = d2fRN(pn) - d2fRN(d.pressPPEprev[i]);
         f[6] = xe32[i];
         f[7] = rei * idg;
-        f[8] = (float)pn;
+        f[8] = d2fRN(pn);
         f[9] = sqrtf(vx * vx + vy * vy + vz * vz);
         f[10] = -(vx * ggx + vy * ggy + vz * ggz);
         f[11] = diag * iA;
-        f[12] = (float)d.pndWall[i];
-        f[13] = -((float)x.x * ggx + (float)x.y * ggy + (float)x.z * ggz);
-        f[14] = (bi - (float)d.source[i]) * idg;
-        f[15] = ((float)d.pndi[i] - (float)d.pndki[i]) * in0;
+        f[12] = d2fRN(d.pndWall[i]);
+        f[13] = -(d2fRN(x.x) * ggx + d2fRN(x.y) * ggy + d2fRN(x.z) * ggz);
+        f[14] = (bi - d2fRN(d.source[i])) * idg;
+        f[15] = (d2fRN(d.pndi[i]) - d2fRN(d.pndki[i])) * in0;
         float4* o = (float4*)(feat + (size_t)i * NF);
         o[0] = make_float4(f[0], f[1], f[2], f[3]);
         o[1] = make_float4(f[4], f[5], f[6], f[7]);
         o[2] = make_float4(f[8], f[9], f[10], f[11]);
         o[3] = make_float4(f[12], f[13], f[14], f[15]);
-        if (d.bc[i] == P.inner) { q0 += (double)(f[FSIG] * f[FSIG]); q1 += 1.0; }
+        if (d.bc[i] == P.inner) { q0 += f2dExact(f[FSIG] * f[FSIG]); q1 += 1.0; }
     }
     blockPartials2(q0, q1, part);
 }
 __global__ void __launch_bounds__(256) k_mlp_features(Dev d, PpeBuffers B, const float* xe32, const float* re,
-                                                      float* feat, double* part) {
+                                                      float* feat, double* part, FeatConst K) {
     const MpsParams& P = d.P;
-    double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
-    double gn = sqrt(gx * gx + gy * gy + gz * gz);
-    if (gn > 0) { gx /= gn; gy /= gn; gz /= gn; }
-    const float ggx = (float)gx, ggy = (float)gy, ggz = (float)gz;
-    const float in0 = (float)(1.0 / P.pndSmallZero), iN0 = (float)(1.0 / P.numNeighZero), iRe = (float)(1.0 / P.reL);
-    const float iA = (float)(1.0 / (P.coeffPPE * P.pndSmallZero));
+    const float ggx = K.ggx, ggy = K.ggy, ggz = K.ggz, in0 = K.in0, iN0 = K.iN0, iRe = K.iRe, iA = K.iA;
     const int n = liveN(d);
     double q0 = 0.0, q1 = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -327,7 +335,7 @@ __global__ void __launch_bounds__(256) k_mlp_sig(const double* part, int nblk, d
 static void mlpFeatureLaunch(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s) {
     k_mlp_xe32<<<gridFor(d.N0, 256), 256, 0, s>>>(d, m.xe32);
     k_mlp_resid<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.xe32, m.re);
-    k_mlp_features<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.re, m.feat, m.part);
+    k_mlp_features<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.re, m.feat, m.part, featConst(d.P));
     k_mlp_sig<<<1, 256, 0, s>>>(m.part, m.nblk, m.sig);
 }
 
@@ -388,7 +396,7 @@ int mlpWarmStart(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s,
         // scale, the network's correction c, and q = A c; the residual-minimising step
         // x_e + theta c is taken by the solver's set-up pass (q in m.re)
         k_mlp_xe_start<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.xe32);
-        k_mlp_resid_feat<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.feat, m.part);
+        k_mlp_resid_feat<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.feat, m.part, featConst(d.P));
         k_mlp_sig<<<1, 256, 0, s>>>(m.part, m.nblk, m.sig);
         if (int e = mlpForwardTc(m, m.feat, d.N0, d.nLive, d.bc, d.P.inner, m.sig, m.cdir, s)) return e;
         k_mlp_ac<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.cdir, m.re);

@@ -33,6 +33,25 @@ __device__ __forceinline__ int warpGroupAdd(int* counters, int key, bool active)
     return base + __popc(grp & ((1u << lane) - 1u));
 }
 
+// One bucket coordinate of updateParticlesID: (int)((x - min) * inv) in 3D,
+// (int)((x - min) * inv + eps) in 2D, with dx = x - min (exact FP64 subtraction, the
+// reference's first operation).  The FP32 product of the particle's FP32 copy h = fl32(dx)
+// and fl32(inv) lies within 3 * 2^-24 relative of the FP64 one, so its truncation is exact
+// unless it is within a margin of an integer (or below it); those rare cases evaluate the
+// FP64 expression out of line (inlined, the compiler would predicate it into every thread).
+static __device__ __noinline__ int bucketKeyCoordExact(double dx, double inv, double eps, bool withEps) {
+    const double q = xmul(dx, inv);
+    return (int)(withEps ? xadd(q, eps) : q);
+}
+__device__ __forceinline__ int bucketKeyCoord(float h, double dx, float invf, float epsf, double inv, double eps,
+                                              bool withEps) {
+    const float q = withEps ? fmaf(h, invf, epsf) : h * invf;
+    const float m = 5e-7f * fabsf(q) + 1e-6f;
+    const float f = q - floorf(q);
+    if (q > m && f > m && f < 1.0f - m) return (int)q;
+    return bucketKeyCoordExact(dx, inv, eps, withEps);
+}
+
 // 2D adds epsilonZero, 3D does not (src/MpsBucket.cpp:312-313 vs :333-335); ghosts skipped.
 // Every lane of a warp reaches the warp-level count (lanes past N0 take part without a key).
 __global__ void k_cell_key(Dev d) {
@@ -44,15 +63,13 @@ __global__ void k_cell_key(Dev d) {
     } else if (i < n) {
         const MpsParams& P = d.P;
         dvec4 p = d.pos[i];
-        int ix, iy, iz = 0;
-        if ((int)P.dim == 2) {
-            ix = (int)xadd(xmul(xsub(p.x, P.domainMin[0]), P.invBucketSide), P.epsilonZero);
-            iy = (int)xadd(xmul(xsub(p.y, P.domainMin[1]), P.invBucketSide), P.epsilonZero);
-        } else {
-            ix = (int)xmul(xsub(p.x, P.domainMin[0]), P.invBucketSide);
-            iy = (int)xmul(xsub(p.y, P.domainMin[1]), P.invBucketSide);
-            iz = (int)xmul(xsub(p.z, P.domainMin[2]), P.invBucketSide);
-        }
+        // x - min once: the key's first operation and the FP32 copies' argument
+        const double dx = xsub(p.x, P.domainMin[0]), dy = xsub(p.y, P.domainMin[1]), dzz = xsub(p.z, P.domainMin[2]);
+        const float4 hi = make_float4(d2fRN(dx), d2fRN(dy), d2fRN(dzz), 0.f);
+        const bool two = (int)P.dim == 2;
+        int ix = bucketKeyCoord(hi.x, dx, d.invSidef, d.epsf, P.invBucketSide, P.epsilonZero, two);
+        int iy = bucketKeyCoord(hi.y, dy, d.invSidef, d.epsf, P.invBucketSide, P.epsilonZero, two);
+        int iz = two ? 0 : bucketKeyCoord(hi.z, dzz, d.invSidef, d.epsf, P.invBucketSide, P.epsilonZero, false);
         long long ib = (long long)iz * P.numBucketsXY + (long long)iy * P.numBucketsX + ix;
         if (ib < 0 || ib >= d.nB) {
             setErr(d, MPSE_DOMAIN);
@@ -60,11 +77,9 @@ __global__ void k_cell_key(Dev d) {
         } else {
             key = (int)ib;
         }
-        // FP32 copy of the start-of-step positions for the prefiltered scans
-        float4 hi = make_float4(d2fRN(p.x - P.domainMin[0]), d2fRN(p.y - P.domainMin[1]),
-                                d2fRN(p.z - P.domainMin[2]), 0.f);
+        // FP32 copy of the start-of-step positions for the prefiltered scans (hi, lo parts)
         d.posf[i] = hi;
-        d.posLo[i] = posLoOf(p, hi, P);
+        d.posLo[i] = make_float4(d2fRN(dx - f2dExact(hi.x)), d2fRN(dy - f2dExact(hi.y)), d2fRN(dzz - f2dExact(hi.z)), 0.f);
     }
     warpGroupAdd(d.cellCount, key, key >= 0);
     if (i < d.N0) d.cellOf[i] = key;

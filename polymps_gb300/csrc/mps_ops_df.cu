@@ -1001,12 +1001,13 @@ __global__ void __launch_bounds__(128) k_filter_nbr_df(Dev d) {
     const df R2 = K(d.k.reMax2);
     const size_t N0 = d.N0;
     int cnt = 0;
-    auto keep = [&](int j, float4 hj, float4 lj) {
+    // the lo part (lo: where it sits) is read only for pairs in the uncertain band
+    auto keep = [&](int j, float4 hj, const float4* lo) {
         float ex = hj.x - hi.x, ey = hj.y - hi.y, ez = hj.z - hi.z;
         float d2f = ex * ex + ey * ey + ez * ez;
         if (d2f > d.bandHi) return;
         if (!(d2f < d.bandLo)) {
-            PairF q = pairDF(hj, lj, hi, li);
+            PairF q = pairDF(hj, __ldg(lo), hi, li);
             if (!inBallDF(d, q.d2, R2, d.mgMax, d.reMax2, i, j)) return;
         }
         if (cnt < d.K) d.nbr[(size_t)cnt * N0 + i] = j;
@@ -1014,13 +1015,28 @@ __global__ void __launch_bounds__(128) k_filter_nbr_df(Dev d) {
     };
     const int c = d.skinCnt[i];
     if (!*(volatile int*)d.skinFlag && c <= d.K && d.skinCell[i] == cellKeyOf(d, pi, hi)) {
-        for (int k = 0; k < c; k++) {   // the skin list stays intact (a later sweep filters it again)
-            const int j = ldStream(d.skinNbr + (size_t)k * N0 + i);
-            keep(j, d.posf[j], d.posLo[j]);
+        // the skin list stays intact (a later sweep filters it again); four entries' loads
+        // are issued before their tests (the list stores would otherwise order each gather
+        // after the previous entry's store)
+        const int* row = d.skinNbr + i;
+        int k = 0;
+        for (; k + 4 <= c; k += 4) {
+            int jj[4];
+            float4 hh[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) jj[u] = ldStream(row + (size_t)(k + u) * N0);
+#pragma unroll
+            for (int u = 0; u < 4; u++) hh[u] = __ldg(&d.posf[jj[u]]);
+#pragma unroll
+            for (int u = 0; u < 4; u++) keep(jj[u], hh[u], d.posLo + jj[u]);
+        }
+        for (; k < c; k++) {
+            const int j = ldStream(row + (size_t)k * N0);
+            keep(j, __ldg(&d.posf[j]), d.posLo + j);
         }
     } else {
         forCellsDF(d, pi, hi, d.bandHi, [&](int j, int s, float4 hj) {
-            if (j != i) keep(j, hj, __ldg(&d.posLoCell[s]));
+            if (j != i) keep(j, hj, d.posLoCell + s);
         });
     }
     if (cnt > d.K) { setErr(d, MPSE_CAPACITY); cnt = d.K; }

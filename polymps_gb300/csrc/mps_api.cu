@@ -774,6 +774,7 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
         d.bandHi = (float)(d.reMax2 + band(d.reMax2));
         d.bandHiS = (float)(p->reS2 + band(p->reS2));
         d.bandHiL = (float)(p->reL2 + band(p->reL2));
+        d.bandHiColl = (float)(p->distCollisionLimit2 + band(p->distCollisionLimit2));
         // start-of-step skin list: reMax + 0.15 l0 (covers steps that move no particle by
         // more than 0.075 l0 from its start position; otherwise the list is rebuilt)
         {

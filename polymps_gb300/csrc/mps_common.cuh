@@ -137,6 +137,7 @@ struct Dev {
     int *nearList, *nearCount;      // fluid particles near the polygon wall (compacted)
     double reMax2;                  // list radius^2 = max(reS^2, reL^2)
     float bandHiS, bandHiL;         // FP32 prefilter upper bounds for the reS / reL balls
+    float bandHiColl;               // ... and for the collision distance
     // polygon mesh and wall tables
     int ntri;
     const double* tri;          // ntri * 9

@@ -268,8 +268,14 @@ __global__ void __launch_bounds__(BLK) k_collision(Dev d) {
     if (d.type[i] == P.fluid) {
         double mi = P.DNS_FL1;  // PTYPE == 1 for every Newtonian particle
         dvec4 pi = d.pos[i], vi = d.vel[i];
+        const float4 fi = d.posf[i];
         SideCtx sc = sideCtx(d, i, pi);
         forNbrs(d, i, [&](int j) {
+            // FP32 prefilter (the list's FP32 copies): most entries lie beyond the collision
+            // distance; the exact FP64 test decides the others
+            const float4 fj = __ldg(&d.posf[j]);
+            const float ex = fj.x - fi.x, ey = fj.y - fi.y, ez = fj.z - fi.z;
+            if (ex * ex + ey * ey + ez * ez > d.bandHiColl) return;
             dvec4 pj = d.pos[j];
             PairG q = pairOf(pj, pi);
             if (q.d2 < P.distCollisionLimit2 && sideOK(sc, pj, q.d2)) {

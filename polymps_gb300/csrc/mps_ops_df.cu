@@ -199,7 +199,11 @@ __global__ void __launch_bounds__(BLK) k_collision_df(Dev d) {
         SideDF sc = sideDF(d, i, pi);
         const df R2 = K(d.k.coll2), cF = K(d.k.collF), cW = K(d.k.collW);
         forNbrs(d, i, [&](int j) {
-            float4 hj = d.posf[j], lj = d.posLo[j];
+            const float4 hj = __ldg(&d.posf[j]);
+            // FP32 prefilter: most list entries lie beyond the collision distance
+            const float ex = hj.x - hi.x, ey = hj.y - hi.y, ez = hj.z - hi.z;
+            if (ex * ex + ey * ey + ez * ez > d.bandHiColl) return;
+            const float4 lj = __ldg(&d.posLo[j]);
             PairF q = pairDF(hj, lj, hi, li);
             if (!inBallDF(d, q.d2, R2, d.mgColl, P.distCollisionLimit2, i, j)) return;
             if (!sideOkDF(d, sc, hj, lj, q.d2, i, j)) return;

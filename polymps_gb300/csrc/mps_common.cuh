@@ -359,6 +359,29 @@ __device__ __forceinline__ void forNbrs(const Dev& d, int i, F&& f) {
     const int* row = d.nbr + i;
     for (int k = 0; k < c; k++) f(ldStream(row + (size_t)k * d.N0));
 }
+// The same with each entry's FP32 position copy, f(j, posf[j]): four entries' indices and
+// gathers are issued before their bodies run (a body's stores would otherwise order the
+// next gather after them).
+template <class F>
+__device__ __forceinline__ void forNbrsPosf(const Dev& d, int i, F&& f) {
+    const int c = d.nbrCount[i];
+    const int* row = d.nbr + i;
+    int k = 0;
+    for (; k + 4 <= c; k += 4) {
+        int jj[4];
+        float4 hh[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) jj[u] = ldStream(row + (size_t)(k + u) * d.N0);
+#pragma unroll
+        for (int u = 0; u < 4; u++) hh[u] = __ldg(&d.posf[jj[u]]);
+#pragma unroll
+        for (int u = 0; u < 4; u++) f(jj[u], hh[u]);
+    }
+    for (; k < c; k++) {
+        const int j = ldStream(row + (size_t)k * d.N0);
+        f(j, __ldg(&d.posf[j]));
+    }
+}
 
 // Iterate the set bits of an entry mask in ascending entry order (the scan order).
 // ELL matrix rows (PPE solvers, learned warm start)

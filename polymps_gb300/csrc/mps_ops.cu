@@ -270,10 +270,9 @@ __global__ void __launch_bounds__(BLK) k_collision(Dev d) {
         dvec4 pi = d.pos[i], vi = d.vel[i];
         const float4 fi = d.posf[i];
         SideCtx sc = sideCtx(d, i, pi);
-        forNbrs(d, i, [&](int j) {
+        forNbrsPosf(d, i, [&](int j, float4 fj) {
             // FP32 prefilter (the list's FP32 copies): most entries lie beyond the collision
             // distance; the exact FP64 test decides the others
-            const float4 fj = __ldg(&d.posf[j]);
             const float ex = fj.x - fi.x, ey = fj.y - fi.y, ez = fj.z - fi.z;
             if (ex * ex + ey * ey + ez * ez > d.bandHiColl) return;
             dvec4 pj = d.pos[j];

@@ -198,8 +198,7 @@ __global__ void __launch_bounds__(BLK) k_collision_df(Dev d) {
         float vin = fabsf(vh.x) + fabsf(vh.y) + fabsf(vh.z);
         SideDF sc = sideDF(d, i, pi);
         const df R2 = K(d.k.coll2), cF = K(d.k.collF), cW = K(d.k.collW);
-        forNbrs(d, i, [&](int j) {
-            const float4 hj = __ldg(&d.posf[j]);
+        forNbrsPosf(d, i, [&](int j, float4 hj) {
             // FP32 prefilter: most list entries lie beyond the collision distance
             const float ex = hj.x - hi.x, ey = hj.y - hi.y, ez = hj.z - hi.z;
             if (ex * ex + ey * ey + ez * ez > d.bandHiColl) return;

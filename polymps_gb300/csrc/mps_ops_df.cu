@@ -962,13 +962,27 @@ __global__ void __launch_bounds__(128) k_visc_list_df(Dev d) {
     };
     const int c = d.nbrCount[i];
     if (c <= d.K) {
-        const int* row = d.nbr + i;
-        for (int k = 0; k < c; k++) {
-            const int j = ldStream(row + (size_t)k * d.N0);
-            const float4 hj = d.posf[j];
+        // four entries' indices and FP32 copies ahead of their tests (forNbrsPosf's order)
+        auto entry = [&](int j, float4 hj) {
             float ex = hj.x - hi.x, ey = hj.y - hi.y, ez = hj.z - hi.z;
-            if (ex * ex + ey * ey + ez * ez > d.bandHiL) continue;   // outside the reL band
-            pair(j, hj, d.posLo[j]);
+            if (ex * ex + ey * ey + ez * ez > d.bandHiL) return;   // outside the reL band
+            pair(j, hj, __ldg(&d.posLo[j]));
+        };
+        const int* row = d.nbr + i;
+        int k = 0;
+        for (; k + 4 <= c; k += 4) {
+            int jj[4];
+            float4 hh[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) jj[u] = ldStream(row + (size_t)(k + u) * d.N0);
+#pragma unroll
+            for (int u = 0; u < 4; u++) hh[u] = __ldg(&d.posf[jj[u]]);
+#pragma unroll
+            for (int u = 0; u < 4; u++) entry(jj[u], hh[u]);
+        }
+        for (; k < c; k++) {
+            const int j = ldStream(row + (size_t)k * d.N0);
+            entry(j, __ldg(&d.posf[j]));
         }
     } else {
         forCellsDF(d, pi, hi, d.bandHiL, [&](int j, int s, float4 hj) {

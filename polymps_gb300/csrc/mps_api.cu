@@ -271,9 +271,9 @@ static int calcPress(mpsgpu_t h) {
         if (!h->B.prepared) { launchMixedPrepare(h->d, h->B, h->s); h->B.prepared = 1; countLaunch(1); }
         int e = mlpWarmStart(h->mlp, h->d, h->B, h->s, ownSolve);
         if (h->prof.on) h->prof.end(h->s);
-        // x_e and its FP32 copy, residual with the features, scale, forward, A c; or x_e copy,
-        // residual, features, scale, forward, correction, step dot products, step, apply
-        countLaunch(ownSolve ? 5 : 9);
+        // x_e, its FP64 residual, features, scale, forward, A c; or x_e copy, residual,
+        // features, scale, forward, correction, step dot products, step, apply
+        countLaunch(ownSolve ? 6 : 9);
         if (e) return e;
         if (ownSolve) { h->B.cdir = h->mlp.cdir; h->B.cq = h->mlp.re; }
     } else if (h->warm == MPSGPU_WARM_PREVIOUS) {

@@ -8,12 +8,15 @@
 // function, so the approximation is part of its definition.
 #define GELU_K0 0.7978845608028654f
 #define GELU_K1 0.044715f
+#define GELU_K01 0.035677408136300125f   // k0 k1
 __device__ __forceinline__ float tanhHw(float x) {
     float y;
     asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
+// u = x (k0 + k0 k1 x^2), h = x/2, gelu = h + h t: five FP32 operations around the tanh
 __device__ __forceinline__ float gelu(float x) {
-    const float t = tanhHw(GELU_K0 * x * fmaf(GELU_K1 * x, x, 1.0f));
-    return 0.5f * x * (1.0f + t);
+    const float t = tanhHw(x * fmaf(GELU_K01, x * x, GELU_K0));
+    const float h = 0.5f * x;
+    return fmaf(h, t, h);
 }

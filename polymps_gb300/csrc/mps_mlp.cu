@@ -47,12 +47,13 @@ static_assert(NPARAM == MPSGPU_MLP_NPARAM, "parameter packing");
 #define S2 72
 
 #include "mps_gelu.cuh"
+#include "mps_mlp_feat.cuh"
 
-// d gelu / dx = (1 + t)/2 + x/2 (1 - t^2) k0 (1 + 3 k1 x^2)
+// d gelu / dx = (1 + t)/2 + x/2 (1 - t^2) (k0 + 3 k0 k1 x^2), t = tanh(u) as gelu forms it
 __device__ __forceinline__ float gelud(float x) {
     const float x2 = x * x;
-    const float t = tanhHw(GELU_K0 * x * fmaf(GELU_K1, x2, 1.0f));
-    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_K0 * fmaf(3.0f * GELU_K1, x2, 1.0f);
+    const float t = tanhHw(x * fmaf(GELU_K01, x2, GELU_K0));
+    return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * fmaf(3.0f * GELU_K01, x2, GELU_K0);
 }
 
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
@@ -208,15 +209,21 @@ __global__ void k_mlp_xe32(Dev d, float* xe32) {
     if (i >= d.N0) return;
     xe32[i] = (i < liveN(d) && d.bc[i] == d.P.inner) ? (float)extrapBase(d, i) : 0.f;
 }
-// The same, with the FP64 start x = x_e on equation rows (0 on identity rows) written for
-// the solver
-__global__ void k_mlp_xe_start(Dev d, PpeBuffers B, float* xe32) {
+// The FP64 start x = x_e on equation rows (0 on identity rows) written for the solver
+__global__ void k_mlp_xe_start(Dev d, PpeBuffers B) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.N0) return;
     const bool eq = i < liveN(d) && d.bc[i] == d.P.inner;
-    const double xe = eq ? extrapBase(d, i) : 0.0;
-    xe32[i] = d2fRN(xe);
-    B.x[i] = xe;
+    B.x[i] = eq ? extrapBase(d, i) : 0.0;
+}
+// FP64 residual r_e = b - A x_e of that start into the solver's residual vector, one row per
+// thread at full occupancy (the same row product, in the same order, as the solver's own
+// residual passes): the features read it, and the solver's set-up takes it as its first
+// residual instead of forming it again
+__global__ void __launch_bounds__(256) k_mlp_resid64(Dev d, PpeBuffers B) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= liveN(d)) return;
+    B.r[i] = B.b[i] - ellRow<double, true>(B.diag, B.val, B.col, B.x, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
 }
 // r_e = b - A x_e (FP32 copy of the matrix) for the features and the step: one row per
 // thread, eight entries in flight with the next chunk's lines prefetched (ellRow)
@@ -225,12 +232,7 @@ __global__ void __launch_bounds__(256) k_mlp_resid(Dev d, PpeBuffers B, const fl
     if (i >= liveN(d)) return;
     re[i] = (float)B.b[i] - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
 }
-// Per-system constants of the features (FP64 divisions and a square root, formed once on
-// the host instead of in every thread): the unit vector along g, 1/n0, 1/N0, 1/reL and
-// 1/(coeffPPE n0).
-struct FeatConst {
-    float ggx, ggy, ggz, in0, iN0, iRe, iA;
-};
+static_assert(NF == MLP_NF && FSIG == MLP_FSIG, "feature layout");
 static FeatConst featConst(const MpsParams& P) {
     double gx = P.gravity[0], gy = P.gravity[1], gz = P.gravity[2];
     const double gn = std::sqrt(gx * gx + gy * gy + gz * gz);
@@ -243,46 +245,22 @@ static FeatConst featConst(const MpsParams& P) {
     k.iA = (float)(1.0 / (P.coeffPPE * P.pndSmallZero));
     return k;
 }
-// The same residual with the 16 raw features of the row (k_mlp_features' definitions) and the
-// block partials of the system scale (sum over equation rows of feature 7 squared, and
-// their count): one memory-bound pass over the rows' fields at full occupancy, so the
-// tensor-core forward only streams the feature rows.
-__global__ void __launch_bounds__(256) k_mlp_resid_feat(Dev d, PpeBuffers B, const float* xe32, float* feat,
-                                                        double* part, FeatConst K) {
-    const MpsParams& P = d.P;
-    const float ggx = K.ggx, ggy = K.ggy, ggz = K.ggz, in0 = K.in0, iN0 = K.iN0, iRe = K.iRe, iA = K.iA;
+// The 16 raw features of the row from the FP64 start and its residual (k_mlp_xe_start,
+// k_mlp_resid64; featRow64) and the block partials of the system scale (sum over equation
+// rows of feature 7 squared, and their count): one memory-bound pass over the rows' fields,
+// so the tensor-core forward only streams the feature rows.
+__global__ void __launch_bounds__(256) k_mlp_feat64(Dev d, PpeBuffers B, float* feat, double* part, FeatConst K) {
     const int n = liveN(d);
     double q0 = 0.0, q1 = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float rei = d2fRN(B.b[i]) - ellRow<float, true>(B.diagf, B.valf, B.col, xe32, i, __ldg(B.rowLen + i), ellBase(B, i), B.ellStride);
-        const dvec4 x = d.pos[i], v = d.vel[i];
-        const float diag = __ldg(B.diagf + i), idg = __ldg(B.diagInvf + i);
-        const double pn = d.pressPPE[i];
-        const float bi = d2fRN(B.b[i]);
-        const float vx = d2fRN(v.x), vy = d2fRN(v.y), vz = d2fRN(v.z);
         float f[NF];
-        f[0] = (d2fRN(d.pndSmall[i]) - d2fRN(P.pndSmallZero)) * in0;
-        f[1] = bi * idg;
-        f[2] = (float)d.numNeigh[i] * iN0;
-        f[3] = ((__double_as_longlong(pn) << 1) == 0) ? 1.f : 0.f;   // pn == +-0
-        f[4] = fminf(sqrtf(d2fRN(d.riw2[i])) * iRe, 1.5f);
-        f[5] = d2fRN(pn) - d2fRN(d.pressPPEprev[i]);
-        f[6] = xe32[i];
-        f[7] = rei * idg;
-        f[8] = d2fRN(pn);
-        f[9] = sqrtf(vx * vx + vy * vy + vz * vz);
-        f[10] = -(vx * ggx + vy * ggy + vz * ggz);
-        f[11] = diag * iA;
-        f[12] = d2fRN(d.pndWall[i]);
-        f[13] = -(d2fRN(x.x) * ggx + d2fRN(x.y) * ggy + d2fRN(x.z) * ggz);
-        f[14] = (bi - d2fRN(d.source[i])) * idg;
-        f[15] = (d2fRN(d.pndi[i]) - d2fRN(d.pndki[i])) * in0;
+        featRow64(d, B, i, K, f);
         float4* o = (float4*)(feat + (size_t)i * NF);
         o[0] = make_float4(f[0], f[1], f[2], f[3]);
         o[1] = make_float4(f[4], f[5], f[6], f[7]);
         o[2] = make_float4(f[8], f[9], f[10], f[11]);
         o[3] = make_float4(f[12], f[13], f[14], f[15]);
-        if (d.bc[i] == P.inner) { q0 += f2dExact(f[FSIG] * f[FSIG]); q1 += 1.0; }
+        if (d.bc[i] == d.P.inner) { q0 += f2dExact(f[FSIG] * f[FSIG]); q1 += 1.0; }
     }
     blockPartials2(q0, q1, part);
 }
@@ -392,12 +370,14 @@ static int mlpForwardLaunch(MlpState& m, const float* feat, int n, const double*
 int mlpWarmStart(MlpState& m, const Dev& d, const PpeBuffers& B, cudaStream_t s, bool stepInSolver) {
     if (!m.ready) return MPSGPU_ERR_ARG;
     if (stepInSolver) {
-        // x = x_e, the extrapolation residual with the features and the scale's partials, the
-        // scale, the network's correction c, and q = A c; the residual-minimising step
-        // x_e + theta c is taken by the solver's set-up pass (q in m.re)
-        k_mlp_xe_start<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.xe32);
-        k_mlp_resid_feat<<<m.nblk, 256, 0, s>>>(d, B, m.xe32, m.feat, m.part, featConst(d.P));
-        k_mlp_sig<<<1, 256, 0, s>>>(m.part, m.nblk, m.sig);
+        // x = x_e, its FP64 residual r_e (left in the solver's residual vector), the features
+        // and the scale's partials, the scale, the network's correction c, and q = A c; the
+        // residual-minimising step x_e + theta c is taken by the solver's set-up pass, which
+        // starts from r_e (q in m.re)
+        k_mlp_xe_start<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B);
+        k_mlp_resid64<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B);
+        k_mlp_feat64<<<m.nblkFeat, 256, 0, s>>>(d, B, m.feat, m.part, featConst(d.P));
+        k_mlp_sig<<<1, 256, 0, s>>>(m.part, m.nblkFeat, m.sig);
         if (int e = mlpForwardTc(m, m.feat, d.N0, d.nLive, d.bc, d.P.inner, m.sig, m.cdir, s)) return e;
         k_mlp_ac<<<gridFor(d.N0, 256), 256, 0, s>>>(d, B, m.cdir, m.re);
         return cudaGetLastError() == cudaSuccess ? 0 : MPSGPU_ERR_CUDA;
@@ -441,6 +421,9 @@ int mlpInit(MlpState& m, int n0, cudaStream_t s) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         m.nblk = std::max(1, sms) * 8;
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mlp_feat64, 256, 0) != cudaSuccess || per <= 0) per = 1;
+        m.nblkFeat = std::min(m.nblk, std::max(1, sms) * per);
     }
     ok = al((void**)&m.re, sizeof(float) * (size_t)n0) && al((void**)&m.cdir, sizeof(float) * (size_t)n0) &&
          al((void**)&m.xe32, sizeof(float) * (size_t)n0) &&

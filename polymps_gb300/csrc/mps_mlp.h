@@ -24,6 +24,7 @@ struct MlpState {
     float* xe32 = nullptr;         // x_e in FP32 (gathered by the features)
     double* part = nullptr;
     int nblk = 0;
+    int nblkFeat = 0;              // blocks of the FP64-start features pass (one wave, <= nblk)
     // system scale: RMS over equation rows of the Jacobi step of the extrapolation residual
     // (pressure-difference features and the target are in its units)
     double* sig = nullptr;         // [0] sigma, [1] step theta

@@ -166,17 +166,27 @@ __global__ void __launch_bounds__(TM, 4) k_mlp_forward_tc(const float* feat, int
     const int tiles = (rows + TM - 1) / TM;
     uint32_t phase = 0;
     bool ok = true;
+    // the raw features of this thread's row in the block's next tile: loaded one tile ahead,
+    // so that their latency runs under the current tile's layers
+    float4 fq[4];
+    auto loadFeat = [&](int tl) {
+        const int r = tl * TM + t;
+        if (tl < tiles && r < rows) {
+            const float4* fp = reinterpret_cast<const float4*>(feat + (size_t)r * NF);
+#pragma unroll
+            for (int c = 0; c < 4; c++) fq[c] = __ldg(fp + c);
+        }
+    };
+    loadFeat(blockIdx.x);
     for (int tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
         const int row = tile * TM + t;
         {   // layer 1 input: the row's 16 normalised features (pressure differences 1, 5, 7, 14
             // in units of sigma) as BF16
             float f[NF];
             if (row < rows) {
-                const float4* fp = reinterpret_cast<const float4*>(feat + (size_t)row * NF);
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
-                    const float4 v4 = fp[c];
-                    f[4 * c] = v4.x; f[4 * c + 1] = v4.y; f[4 * c + 2] = v4.z; f[4 * c + 3] = v4.w;
+                    f[4 * c] = fq[c].x; f[4 * c + 1] = fq[c].y; f[4 * c + 2] = fq[c].z; f[4 * c + 3] = fq[c].w;
                 }
                 f[1] *= q; f[5] *= q; f[7] *= q; f[14] *= q;
 #pragma unroll
@@ -196,6 +206,7 @@ __global__ void __launch_bounds__(TM, 4) k_mlp_forward_tc(const float* feat, int
                 *reinterpret_cast<uint4*>(s.a + coreOff(t, 8 * kb, NF)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
             }
         }
+        loadFeat(tile + gridDim.x);
         float v[H];
         float o = 0.f;
 #pragma unroll 1

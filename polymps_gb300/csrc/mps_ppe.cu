@@ -1138,28 +1138,35 @@ __device__ __forceinline__ void forOwnL(const RowSet& s, F&& f) {
 
 // Set-up of the shared-memory mixed solve: FP64 residual of the warm start, ||r||^2 and
 // ||b||^2 and the solver scalars; with a learned correction c (B.cdir, with q = A c in
-// B.cq) also the dot products r.q and q.q, the residual-minimising step theta = r.q / q.q
-// (the start x + theta c is never worse than x in the residual norm; its residual norm
-// follows algebraically) and the update of x and r.  Returns false when a barrier wait ran
-// out.
+// B.cq) the residual r_e of the start x_e is already in B.r (the learned start's features
+// read it), and the pass forms the dot products r.q and q.q, the residual-minimising step
+// theta = r.q / q.q (the start x + theta c is never worse than x in the residual norm; its
+// residual norm follows algebraically) and the update of x and r.  Returns false when a
+// barrier wait ran out.
 template <bool LEARNED>
 __device__ __forceinline__ bool mxSetup(const PpeBuffers& B, const RowSet& rs, QCtl& c, QLocal& qL, double tol,
                                         double eta2) {
     double* const qS = qL.scal;
     int* const qF = qL.flag;
     double v[LEARNED ? 4 : 2] = {};
-    forRows(B, rs, [&](int i, int len) {
-        const double bi = B.b[i];
-        const double r = bi - qRow(B, B.x, i, len);
-        B.r[i] = r;
-        v[0] += r * r;
-        v[1] += bi * bi;
-        if (LEARNED) {
+    if (LEARNED) {
+        forOwn(rs, [&](int i) {
+            const double bi = B.b[i], r = B.r[i];
             const double q = (double)__ldg(B.cq + i);
+            v[0] += r * r;
+            v[1] += bi * bi;
             v[LEARNED ? 2 : 0] += r * q;
             v[LEARNED ? 3 : 0] += q * q;
-        }
-    });
+        });
+    } else {
+        forRows(B, rs, [&](int i, int len) {
+            const double bi = B.b[i];
+            const double r = bi - qRow(B, B.x, i, len);
+            B.r[i] = r;
+            v[0] += r * r;
+            v[1] += bi * bi;
+        });
+    }
     if (!qSum<LEARNED ? 4 : 2>(v, B, c, [&](const double* t) {
             double th = 0.0, rr = t[0];
             if (LEARNED) {

@@ -156,3 +156,47 @@ def test_mixed_solve_falls_back_to_plain_cg(mps_lib, warm):
     assert code_s == abi.ERR_NOT_CONVERGED and st_s.ppeFallback == 0
     assert code_f == abi.ERR_NOT_CONVERGED and st_f.ppeFallback == 1
     assert np.array_equal(x_f, x_s)
+
+
+def test_learned_start_matches_host_reconstruction(mps_lib):
+    """The learned start of the single-launch mixed solve (features from the FP64 start x_e
+    and its FP64 residual, which the solver's set-up then starts from) against the same
+    start rebuilt step by step on the host: the recorded-feature definitions (FP32 residual
+    pass), the system scale sigma, the network on those inputs, c, the residual-minimising
+    step theta = (r_e . A c) / (A c . A c) with the exported FP64 system, and the initial
+    relative residual ||r_e - theta A c|| / ||b||."""
+    from polymps_gb300 import mps
+    inner = cases.config(4, scale=2.0).params["inner"]
+    g, w, hist = _system_after_steps(mps)
+    code_e, st_e, _ = _solve(mps, g, hist, abi.SOLVER_MIXED, abi.WARM_EXTRAP2, 20000)
+    code_l, st_l, _ = _solve(mps, g, hist, abi.SOLVER_MIXED, abi.WARM_MLP, 20000)
+    assert code_e == 0 and code_l == 0 and st_l.ppeFallback == 0
+    for f, v in zip((abi.F_PRESSPPE, abi.F_PRESSPPE_PREV, abi.F_PRESSPPE_PREV2), hist):
+        g.set(f, v)
+    feat = g.ppe_features()
+    rowptr, col, val, rhs = g.ppe()
+    eq = g.get(abi.F_BC).reshape(-1) == inner
+    _, norm = g.mlp_get_weights()
+    xe = np.where(eq, 3.0 * (hist[0] - hist[1]) + hist[2], 0.0)
+    n = len(rhs)
+    rows = np.repeat(np.arange(n), np.diff(rowptr))
+
+    def matvec(x):
+        return np.bincount(rows, weights=val[:rowptr[-1]] * x[col[:rowptr[-1]]], minlength=n)
+
+    r = rhs - matvec(xe)
+    sig = float(np.sqrt(np.mean(feat[eq, 7].astype(np.float64) ** 2)))
+    fs = feat.copy()
+    fs[:, [1, 5, 7, 14]] *= np.float32(1.0 / sig)
+    g_out = g.mlp_forward(fs).astype(np.float64)
+    g.close()
+    c = np.where(eq, (g_out / norm[2 * 16 + 1] + norm[2 * 16]) * sig, 0.0)
+    q = matvec(c)
+    theta = float(r @ q) / float(q @ q)
+    r0_host = float(np.linalg.norm(r - theta * q) / np.linalg.norm(rhs))
+    r0_extrap = float(np.linalg.norm(r) / np.linalg.norm(rhs))
+    print("initial relative residual: extrapolated %.4e (GPU %.4e), learned host %.4e GPU %.4e, theta %.3f"
+          % (r0_extrap, st_e.ppeInitialRelResidual, r0_host, st_l.ppeInitialRelResidual, theta))
+    assert st_e.ppeInitialRelResidual == pytest.approx(r0_extrap, rel=1e-6)
+    assert r0_host < 0.95 * r0_extrap   # the network moves the start, so the comparison below means something
+    assert st_l.ppeInitialRelResidual == pytest.approx(r0_host, rel=1e-2)

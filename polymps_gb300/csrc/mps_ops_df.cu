@@ -257,9 +257,13 @@ __device__ __forceinline__ MirrorDF mirrorDF(const Dev& d, dvec4 m) {
 // One wall-sweep entry: j within R of i, its mirror image within R of the mirror of i
 // and j not on the mirror side (e.g. src/MpsPndNeigh.cpp:140-160).  Returns the mirror
 // pair (x_j - m_i, |x_j - m_i|^2) through m.
-__device__ __forceinline__ bool wallEntryDF(const Dev& d, int i, int j, float4 hi, float4 li, const MirrorDF& M,
-                                            df R2f, float mg, double R2, PairF& m) {
-    float4 hj = d.posf[j], lj = d.posLo[j];
+// hj: the entry's FP32 copy (gathered ahead by forNbrsPosf); band: the FP32 upper bound of
+// the radius R (an entry above it is outside the ball, its lo part is never read)
+__device__ __forceinline__ bool wallEntryDF(const Dev& d, int i, int j, float4 hj, float4 hi, float4 li,
+                                            const MirrorDF& M, df R2f, float mg, double R2, float band, PairF& m) {
+    const float ex = hj.x - hi.x, ey = hj.y - hi.y, ez = hj.z - hi.z;
+    if (ex * ex + ey * ey + ez * ez > band) return false;
+    const float4 lj = __ldg(&d.posLo[j]);
     PairF q = pairDF(hj, lj, hi, li);
     if (!inBallDF(d, q.d2, R2f, mg, R2, i, j)) return false;
     m = pairDF(hj, lj, M.mh, M.ml);
@@ -282,9 +286,9 @@ __global__ void __launch_bounds__(BLK) k_wall_npcd_df(Dev d) {
     const df R2 = K(d.k.reS2);
     const RadiusDF RS = {K(d.k.reS), K(d.k.invReS)};
     df sx = dfF(0.f), sy = dfF(0.f), sz = dfF(0.f);
-    forNbrs(d, i, [&](int j) {
+    forNbrsPosf(d, i, [&](int j, float4 hj) {
         PairF m;
-        if (!wallEntryDF(d, i, j, hi, li, M, R2, d.mgS, P.reS2, m)) return;
+        if (!wallEntryDF(d, i, j, hj, hi, li, M, R2, d.mgS, P.reS2, d.bandHiS, m)) return;
         df wS = weightDF(m.d2, RS, P.weightType).w;
         sx += m.v.x * wS; sy += m.v.y * wS; sz += m.v.z * wS;
     });
@@ -583,7 +587,7 @@ __global__ void __launch_bounds__(BLK) k_wall_press_grad_df(Dev d) {
     df sx = dfF(0.f), sy = sx, sz = sx;
     forNbrs(d, i, [&](int j) {
         PairF m;
-        if (!wallEntryDF(d, i, j, hi, li, M, R2, d.mgS, P.reS2, m)) return;
+        if (!wallEntryDF(d, i, j, d.posf[j], hi, li, M, R2, d.mgS, P.reS2, d.bandHiS, m)) return;
         WeightDF w = weightDF(m.d2, RS, P.weightType);
         df f;
         if (gt <= 2) f = (loadDF(d.pressDF, j) + base) * w.wr2;
@@ -655,9 +659,9 @@ __global__ void __launch_bounds__(BLK) k_wall_visc_df(Dev d) {
     const df R2 = K(d.k.reL2);
     const RadiusDF RL = {K(d.k.reL), K(d.k.invReL)};
     df sx = dfF(0.f), sy = sx, sz = sx;
-    forNbrs(d, i, [&](int j) {
+    forNbrsPosf(d, i, [&](int j, float4 hj) {
         PairF m;
-        if (!wallEntryDF(d, i, j, hi, li, Mi, R2, d.mgL, P.reL2, m)) return;
+        if (!wallEntryDF(d, i, j, hj, hi, li, Mi, R2, d.mgL, P.reL2, d.bandHiL, m)) return;
         df c = weightDF(m.d2, RL, P.weightType).w * neuF;
         float4 vhj = d.velHi[j], vlj = d.velLo[j];
         sx += (dfOf(vhj.x, vlj.x) - vmx) * c;

@@ -257,8 +257,8 @@ __device__ __forceinline__ MirrorDF mirrorDF(const Dev& d, dvec4 m) {
 // One wall-sweep entry: j within R of i, its mirror image within R of the mirror of i
 // and j not on the mirror side (e.g. src/MpsPndNeigh.cpp:140-160).  Returns the mirror
 // pair (x_j - m_i, |x_j - m_i|^2) through m.
-// hj: the entry's FP32 copy (gathered ahead by forNbrsPosf); band: the FP32 upper bound of
-// the radius R (an entry above it is outside the ball, its lo part is never read)
+// hj: the entry's FP32 copy (posf[j]); band: the FP32 upper bound of the radius R (an
+// entry above it is outside the ball, and its lo part is never read)
 __device__ __forceinline__ bool wallEntryDF(const Dev& d, int i, int j, float4 hj, float4 hi, float4 li,
                                             const MirrorDF& M, df R2f, float mg, double R2, float band, PairF& m) {
     const float ex = hj.x - hi.x, ey = hj.y - hi.y, ez = hj.z - hi.z;

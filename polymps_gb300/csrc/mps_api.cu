@@ -55,6 +55,10 @@ struct mpsgpu_s {
     int lastOut = 0;
     MpsStepStats last{};
     cudaEvent_t e0 = nullptr, e1 = nullptr, ea0 = nullptr, ea1 = nullptr, es0 = nullptr, es1 = nullptr;
+    // second stream of the step (the wall distance beside the list filter and the collision)
+    // and its fork and join events
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
     std::string err;
     MlpState mlp;
     Prof prof;
@@ -506,9 +510,38 @@ static int stepImpl(mpsgpu_t h) {
     if (P.relaxPress < 1.0) RUN(MPS_OP_PREDICT_PRESS_GRADIENT);
     RUN(MPS_OP_PREDICT);
     RUN(MPS_OP_OUT_OF_DOMAIN);
+    // The wall distance reads the positions left by the out-of-domain removal and writes only
+    // the wall fields (squared distance, wall point, mirror, normal, near-wall flag, wall PND
+    // and neighbour count).  The list filter reads none of them; the collision reads only the
+    // mirror, in its mirror-side test, and every mirror is still the far point the prediction
+    // wrote, for which the test passes for every pair.  So the collision skips the test
+    // (mirrorFar) and the wall distance runs on the second stream beside the filter and the
+    // collision, joined before the wall PND.  DPC moves the positions: it keeps the order.
+    const bool side = P.wallType == 1 && P.collisionType != 1 && h->d.ntri > 0;
+    if (side) {
+        cudaEventRecord(h->evFork, h->s);
+        cudaStreamWaitEvent(h->s2, h->evFork, 0);
+        if (h->prof.on) h->prof.begin(MPS_OP_WALL_DISTANCE, h->s2);
+        launchWallDistance(h->d, h->s2);
+        if (h->prof.on) h->prof.end(h->s2);
+        cudaEventRecord(h->evJoin, h->s2);
+        countLaunch(opLaunches(MPS_OP_WALL_DISTANCE, P, df32(h)));
+        if ((e = launchStatus())) { cudaStreamWaitEvent(h->s, h->evJoin, 0); return e; }
+    }
     ensureList(h);                       // post-prediction neighbour list
-    RUN(MPS_OP_COLLISION);
-    if (P.wallType == 1) { RUN(MPS_OP_WALL_DISTANCE); RUN(MPS_OP_WALL_NPCD); }
+    h->d.mirrorFar = side ? 1 : 0;
+    e = runOpImpl(h, MPS_OP_COLLISION);
+    h->d.mirrorFar = 0;
+    if (side) {
+        cudaStreamWaitEvent(h->s, h->evJoin, 0);
+        h->masksValid = false;   // as the wall-distance operator leaves them
+        h->corrFresh = false;
+    }
+    if (e) return e;
+    if (P.wallType == 1) {
+        if (!side) RUN(MPS_OP_WALL_DISTANCE);
+        RUN(MPS_OP_WALL_NPCD);
+    }
     // The first correctionMatrix call (src/main.cpp:317-319) is read only by the diffusive
     // PND and the velocity divergence of the PND + div u source; otherwise the second call
     // (src/main.cpp:375-377, same positions) overwrites it.
@@ -681,6 +714,13 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
     cudaError_t ce = cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking);
     if (ce != cudaSuccess) { g_lastError = cudaGetErrorString(ce); delete h; return MPSGPU_ERR_CUDA; }
     for (cudaEvent_t* ev : {&h->e0, &h->e1, &h->ea0, &h->ea1, &h->es0, &h->es1}) cudaEventCreate(ev);
+    if (cudaStreamCreateWithFlags(&h->s2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->evFork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->evJoin, cudaEventDisableTiming) != cudaSuccess) {
+        g_lastError = "second stream of the step";
+        mpsgpu_destroy(h);
+        return MPSGPU_ERR_CUDA;
+    }
     Dev& d = h->d;
     std::memset(&d, 0, sizeof(d));
     d.P = *p;
@@ -961,12 +1001,14 @@ int mpsgpu_create(const MpsParams* p, int n, const int* type, const double* pos3
 int mpsgpu_destroy(mpsgpu_t h) {
     if (!h) return MPSGPU_ERR_ARG;
     if (h->s) cudaStreamSynchronize(h->s);
+    if (h->s2) cudaStreamSynchronize(h->s2);
     mlpFree(h->mlp);
     h->prof.destroy();
     for (void* p : h->allocs) cudaFree(p);
     if (h->vtuDev) cudaFree(h->vtuDev);
     if (h->vtuHost) cudaFreeHost(h->vtuHost);
-    for (cudaEvent_t ev : {h->e0, h->e1, h->ea0, h->ea1, h->es0, h->es1}) if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : {h->e0, h->e1, h->ea0, h->ea1, h->es0, h->es1, h->evFork, h->evJoin}) if (ev) cudaEventDestroy(ev);
+    if (h->s2) cudaStreamDestroy(h->s2);
     if (h->s) cudaStreamDestroy(h->s);
     delete h;
     return 0;

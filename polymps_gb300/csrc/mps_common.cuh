@@ -95,6 +95,10 @@ struct Dev {
     // float-float pair, and the half-widths (m^2) of the decision margins of float-float
     // squared distances for the reS, reL, list and collision radii
     int prec;                       // MPSGPU_PRECISION_*
+    // 1 inside a step between the prediction and the wall distance: every mirror is still the
+    // far point the prediction wrote, so the collision's mirror-side test passes for every
+    // pair and the collision does not read the mirror (the wall distance may be writing it)
+    int mirrorFar;
     float4 *posLo, *posLoCell, *velHi, *velLo;
     dvec4 *c1n, *c2n, *c3n;         // correction matrix formed by the PND sweep, published by the
     float2* corrDFn;                // correction-matrix operator (pointer swap)

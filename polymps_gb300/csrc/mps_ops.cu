@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(BLK) k_collision(Dev d) {
         double mi = P.DNS_FL1;  // PTYPE == 1 for every Newtonian particle
         dvec4 pi = d.pos[i], vi = d.vel[i];
         const float4 fi = d.posf[i];
-        SideCtx sc = sideCtx(d, i, pi);
+        const SideCtx sc = d.mirrorFar ? SideCtx{} : sideCtx(d, i, pi);   // {}: no side test
         forNbrsPosf(d, i, [&](int j, float4 fj) {
             // FP32 prefilter (the list's FP32 copies): most entries lie beyond the collision
             // distance; the exact FP64 test decides the others

@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(BLK) k_collision_df(Dev d) {
         float4 hi = d.posf[i], li = d.posLo[i];
         float4 vh = d.velHi[i], vl = d.velLo[i];
         float vin = fabsf(vh.x) + fabsf(vh.y) + fabsf(vh.z);
-        SideDF sc = sideDF(d, i, pi);
+        const SideDF sc = d.mirrorFar ? SideDF{} : sideDF(d, i, pi);   // {}: no side test
         const df R2 = K(d.k.coll2), cF = K(d.k.collF), cW = K(d.k.collW);
         forNbrsPosf(d, i, [&](int j, float4 hj) {
             // FP32 prefilter: most list entries lie beyond the collision distance

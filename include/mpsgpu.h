@@ -13,7 +13,9 @@
  *
  * Ownership: the library owns all device memory behind the opaque handle; host arrays
  * passed in are only read (or written for downloads) during the call.  A handle is not
- * thread-safe and runs everything on one CUDA stream (mpsgpu_stream).
+ * thread-safe and orders all its work on one CUDA stream (mpsgpu_stream): the one kernel a
+ * step runs on a second internal stream (the wall distance, beside the list filter and the
+ * collision) is forked from that stream and joined back into it within the step.
  */
 #ifndef MPSGPU_H_
 #define MPSGPU_H_
